@@ -1,0 +1,336 @@
+"""Benchmark: photon-transport throughput (histories/s) on the spiral-CT torso.
+
+Workload (one step): 256x256x200 seeded six-material torso at 1.5 mm, spiral CT
+120 kVp / 6 mm Al with the body bowtie, pitch 1.0, 40 mm collimation, 200 mm
+scan, 360 exposures x 2,777,778 = 1.00e9 histories, Woodcock tracking, FP64
+scoring.  Inputs are seeded synthetic data of the configured shape (no
+dataset exists for this path).
+
+  value   histories/s over K timed steps with the world resident in HBM
+  e2e     the same through the public C ABI with host buffers: H2D of the
+          density/material arrays from pinned memory, World build, transport,
+          D2H of the dose/variance/count arrays
+  roofline  algorithmic bytes of the transport kernel (4 B per voxel visit, 48 B
+          per deposit read-modify-write) / its CUDA-event time, vs measured HBM
+  cpu_baseline  the CPU oracle (FP64 port of the path) on this host's cores, on a
+          bounded sample of the same workload
+
+`--impl reference` times that CPU implementation alone (the reference's own
+engine, DXMClib, is not available to build: see the design doc).
+N > 1 (torchrun): every rank runs its own full job on its own GPU with its own
+Philox stream (independent histories; weak scaling, no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "BASELINE.json").exists() else \
+    "histories/s"
+WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 materials, +-2% density jitter), "
+            "120 kVp 6 mm Al + body bowtie, pitch 1.0, 40 mm collimation, 200 mm scan, 1e9 histories")
+# dram__bytes_read.sum + dram__bytes_write.sum of one transport launch, from the ncu
+# capture summarised in profiles/transport_kernel_torso.md, scaled to one full
+# 2^26-history launch; None until a capture exists.
+TRAFFIC_BYTES_PER_LAUNCH = None
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--histories", type=float, default=1e9, help="histories per step")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(histories: float):
+    from opendxmc_gb300 import phantoms as P
+
+    ph = P.torso_phantom(dims=(256, 256, 200), spacing=(0.15, 0.15, 0.15), seed=1)
+    n_exp = 360
+    ppe = int(-(-int(histories) // n_exp))
+    beam = P.ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=1.0, collimation_cm=4.0, scan_cm=20.0, particles=ppe)
+    return ph, beam, n_exp * ppe
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        for line in Path(self.file.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        loaded = sorted(sm)[len(sm) // 4:] if len(sm) > 4 else sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows),
+                "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
+
+
+def cpu_baseline(ph, beam, seconds: float) -> dict:
+    """The FP64 CPU oracle on this host's cores over a bounded sample of the job."""
+    from oracle import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    w = O.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    cal = 200_000
+    t = time.perf_counter()
+    w.run(beam, seed=1, stream=7, threads=threads, hist_begin=0, hist_end=cal)
+    rate0 = cal / (time.perf_counter() - t)
+    n = int(max(cal, min(rate0 * seconds, 5e8)))
+    w.clear()
+    t = time.perf_counter()
+    st = w.run(beam, seed=1, stream=7, threads=threads, hist_begin=0, hist_end=n)
+    dt = time.perf_counter() - t
+    return {"value": st["n_histories"] / dt, "unit": "histories/s", "cores": threads, "kind": "port",
+            "sample": f"first {st['n_histories']} histories of the same job ({dt:.1f} s, FP64 oracle, "
+                      f"{threads} threads)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    ph, beam, _ = workload(args.histories)
+    from oracle import oracle as O
+
+    O.build()
+    threads = os.cpu_count() or 1
+    w = O.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    cal = 100_000
+    t = time.perf_counter()
+    w.run(beam, seed=1, threads=threads, hist_end=cal)
+    rate = cal / (time.perf_counter() - t)
+    per_step = int(max(cal, min(rate * 4.0, 2e8)))  # ~4 s of CPU work per step
+    h = 0
+    for _ in range(args.warmup):
+        w.run(beam, seed=1, threads=threads, hist_begin=h, hist_end=h + per_step)
+        h += per_step
+    t = time.perf_counter()
+    done = 0
+    for _ in range(args.steps):
+        st = w.run(beam, seed=1, threads=threads, hist_begin=h, hist_end=h + per_step)
+        h += per_step
+        done += st["n_histories"]
+    dt = time.perf_counter() - t
+    value = done / dt
+    sample = f"{per_step} histories per step of the same job (FP64 oracle port, {threads} threads)"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample_histories_per_step": per_step},
+        "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+
+    from opendxmc_gb300 import build as B
+
+    if not B.LIB.exists():
+        B.build(verbose_ptxas=False)
+    from opendxmc_gb300 import engine as G
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    G.set_device(local)
+    import torch
+
+    torch.cuda.set_device(local)
+    ph, beam, hist = workload(args.histories)
+    gw = G.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    gw.set_data(ph.density, ph.material)
+    gw.build()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def step(seed):
+        flush.fill_(float(seed))
+        torch.cuda.synchronize()
+        return gw.run(beam, G.run_options(seed=seed, stream=rank))
+
+    for s in range(args.warmup):
+        step(1000 + s)
+    gw.clear()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    t0 = time.perf_counter()
+    stats = [step(1 + s) for s in range(args.steps)]
+    barrier()
+    dt = time.perf_counter() - t0
+    clk = clocks.stop()
+    if dist is not None:
+        tt = torch.tensor([dt], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dt = float(tt.item())
+    done = sum(s["n_histories"] for s in stats)
+    total_done = done * world
+    value = total_done / dt
+    kernel_ms = sum(s["kernel_ms"] for s in stats)
+    visits = sum(s["n_visits"] for s in stats)
+    deposits = sum(s["n_photo"] + s["n_compton"] + s["n_cutoff"] for s in stats)
+    chunk = 1 << 26
+    launches_per_step = -(-hist // chunk)
+    alg_bytes = 4.0 * visits + 48.0 * deposits
+    hbm, peak_kind = peaks()
+    achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "peak_source": peak_kind,
+            "traffic": TRAFFIC_BYTES_PER_LAUNCH,
+            "alg_bytes_per_launch": alg_bytes / (args.steps * launches_per_step),
+            "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step),
+            "visits_per_history": visits / done, "deposits_per_history": deposits / done}
+
+    # ---- end to end through the C ABI with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        N = ph.n_voxels
+        dens = torch.empty(N, dtype=torch.float64, pin_memory=True).numpy()
+        mat = torch.empty(N, dtype=torch.uint8, pin_memory=True).numpy()
+        dens[:] = ph.density.reshape(-1)
+        mat[:] = ph.material.reshape(-1)
+        outs = (torch.empty(N, dtype=torch.float64, pin_memory=True).numpy(),
+                torch.empty(N, dtype=torch.float64, pin_memory=True).numpy(),
+                torch.empty(N, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64))
+
+        def e2e_step(seed):
+            gw.set_data(dens, mat)
+            gw.build()
+            st = gw.run(beam, G.run_options(seed=seed, stream=rank))
+            gw.dose(out=outs)
+            return st
+
+        e2e_step(2000)
+        barrier()
+        t0 = time.perf_counter()
+        hs = sum(e2e_step(3000 + s)["n_histories"] for s in range(args.e2e_steps))
+        barrier()
+        de = time.perf_counter() - t0
+        if dist is not None:
+            tt = torch.tensor([de], dtype=torch.float64, device=f"cuda:{local}")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            de = float(tt.item())
+        e2e = {"value": hs * world / de, "unit": "histories/s", "h2d_bytes_per_step": N * 9,
+               "d2h_bytes_per_step": N * 24, "steps": args.e2e_steps,
+               "path": "dxmcg_world_set_data + dxmcg_world_build + dxmcg_transport_run + dxmcg_world_read_dose"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(ph, beam, args.cpu_seconds)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "grid": list(ph.dims), "voxel_mm": 1.5, "histories_per_step": hist,
+                       "exposures": 360, "tracking": "woodcock", "scoring": "fp64",
+                       "l2": "256 MB buffer written before every step; tally 420 MB > L2",
+                       "parallelism": f"replicas x{world} (independent Philox streams)"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches_per_step * args.steps, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+/*
+ * dxmcg.h -- C ABI of the GB300 photon-transport engine (libdxmcg.so).
+ *
+ * This is the drop-in boundary for the one call OpenDXMC makes into DXMClib's
+ * Monte Carlo engine:
+ *
+ *     transport(world, beam, progress, true);      src/libopendxmc/simulationpipeline.cpp:165
+ *
+ * together with the world ingest before it (simulationpipeline.cpp:127-153) and
+ * the per-voxel readback after it (simulationpipeline.cpp:174-231).  Plain C types
+ * only: pointers, sizes, status codes.  No exceptions cross this boundary.  The
+ * header-only C++ shim under include/dxmc/ re-creates the dxmc:: classes OpenDXMC
+ * compiles against on top of these functions.
+ *
+ * Conventions
+ *  - lengths in cm, energies in keV, angles in radians unless a name says _deg;
+ *  - voxel index i + nx*(j + ny*k), x fastest (otherphantomimportpipeline.cpp:44);
+ *  - the grid is centred on the world origin (datacontainer.cpp:174-178);
+ *  - every function returns DXMCG_OK (0) or a negative dxmcg_status; the text of
+ *    the last error on the calling thread is returned by dxmcg_last_error().
+ */
+#ifndef DXMCG_H
+#define DXMCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define DXMCG_API __attribute__((visibility("default")))
+#else
+#define DXMCG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DXMCG_VERSION 1
+#define DXMCG_MAX_ELEMENTS 16
+#define DXMCG_MAX_MATERIALS 255
+#define DXMCG_TRANSPARENT_MATERIAL 255
+#define DXMCG_NE 300 /* attenuation table energies: 1.0 + 0.5 i keV */
+
+typedef enum {
+    DXMCG_OK = 0,
+    DXMCG_ERR_ARGUMENT = -1,
+    DXMCG_ERR_CUDA = -2,
+    DXMCG_ERR_STATE = -3,
+    DXMCG_ERR_CANCELLED = -4,
+    DXMCG_ERR_DEVICE = -5, /* a device-side check failed (step limit, bad voxel) */
+    DXMCG_ERR_NO_DEVICE = -6,
+    DXMCG_ERR_CAPACITY = -7
+} dxmcg_status;
+
+typedef enum {
+    DXMCG_BEAM_DX = 0,
+    DXMCG_BEAM_CT_SPIRAL = 1,
+    DXMCG_BEAM_CT_SEQUENTIAL = 2,
+    DXMCG_BEAM_CBCT = 3,
+    DXMCG_BEAM_PENCIL = 4,
+    DXMCG_BEAM_CT_SPIRAL_DUAL_ENERGY = 5
+} dxmcg_beam_type;
+
+typedef enum { DXMCG_TRACK_WOODCOCK = 0, DXMCG_TRACK_SIDDON = 1 } dxmcg_tracking;
+
+/* Material by mass fractions of elements: Material<5>::byWeight(map<Z, w>)
+ * (simulationpipeline.cpp:136). Weights are normalised by the library. */
+typedef struct {
+    int32_t n;
+    int32_t Z[DXMCG_MAX_ELEMENTS];
+    double w[DXMCG_MAX_ELEMENTS];
+} dxmcg_material;
+
+/* Union of the beam parameters the OpenDXMC beam setters carry
+ * (beamsettingsmodel.cpp:459-1837; dxmc_specialization.hpp:37-77). */
+typedef struct {
+    int32_t type; /* dxmcg_beam_type */
+    double kvp;   /* setTubeVoltage (beamsettingsmodel.cpp:262) */
+    double anode_angle_deg;
+    int32_t n_filters; /* addTubeFiltrationMaterial(Z, mm) (beamsettingsmodel.cpp:286-323) */
+    int32_t filter_Z[8];
+    double filter_mm[8];
+    uint64_t particles_per_exposure;
+    uint64_t n_exposures; /* DX / pencil: number of identical exposures */
+    /* DX, pencil, CT sequential */
+    double position[3];
+    double cosines[2][3]; /* direction cosines; beam direction = c0 x c1 */
+    double half_angles[2]; /* collimation half angles */
+    double energy_kev;     /* pencil beam */
+    /* CT */
+    double start[3];
+    double stop[3];
+    double start_angle_deg;
+    double stop_angle_deg;
+    double step_angle_deg;
+    double pitch;
+    double collimation_cm;
+    double scan_fov_cm;
+    double sdd_cm;
+    double rotation_axis[3];
+    int32_t n_slices;
+    double slice_spacing_cm;
+    double kvp_b; /* dual energy, tube B */
+    int32_t n_filters_b;
+    int32_t filter_Z_b[8];
+    double filter_mm_b[8];
+    double tube_a_weight;
+    double fov_b_cm;
+    /* bowtie (BowtieFilter(vector<pair<angle_rad, weight>>), bowtiefilterreader.cpp:173-191) */
+    int32_t n_bowtie;
+    const double* bowtie_angle;
+    const double* bowtie_weight;
+    /* AEC (CTAECFilter(start, stop, weights), datacontainer.cpp:53-62) */
+    int32_t n_aec;
+    double aec_start[3];
+    double aec_stop[3];
+    const double* aec_weight;
+} dxmcg_beam;
+
+/* One source pose (exposure(i) in beamactorcontainer.cpp:114-121). */
+typedef struct {
+    double pos[3];
+    double c0[3];
+    double c1[3];
+    double half[2];
+    double weight;
+    int32_t tube;
+} dxmcg_exposure;
+
+typedef struct {
+    uint64_t seed;        /* Philox key */
+    uint32_t stream;      /* Philox counter word 1: independent stream per beam */
+    int32_t tracking;     /* dxmcg_tracking */
+    int32_t normalize;    /* trailing bool of transport(...): scale dose to the beam's DAP */
+    int32_t block_size;   /* 0 = library default / autotuned */
+    int32_t blocks_per_sm;
+    int32_t chunk_histories_log2; /* histories per launch (progress/cancel granularity), 0 = default */
+    uint64_t hist_begin;  /* history range [begin, end) of the beam; end 0 = all */
+    uint64_t hist_end;
+} dxmcg_run_options;
+
+typedef struct {
+    double e_source, e_deposited, e_escaped; /* keV, weighted */
+    uint64_t n_histories, n_missed, n_visits, n_photo, n_compton, n_rayleigh, n_cutoff, n_errors;
+    uint64_t n_interacted; /* histories with at least one real interaction */
+    double kernel_ms;   /* device time of the transport launches (CUDA events) */
+    double total_ms;    /* host wall time of the call */
+    double dose_scale;  /* mGy per (keV / g) applied by the dose readout */
+} dxmcg_stats;
+
+typedef struct dxmcg_world dxmcg_world;
+typedef struct dxmcg_progress dxmcg_progress;
+
+DXMCG_API int dxmcg_version(void);
+DXMCG_API const char* dxmcg_last_error(void);
+/* number of CUDA devices; 0 when none */
+DXMCG_API int dxmcg_device_count(void);
+/* device that later dxmcg_world_create calls on this thread use (one process per GPU) */
+DXMCG_API int dxmcg_set_device(int device);
+
+/* ---- host physics (FP64): Material<5>::attenuationValues, Tube --------------
+ * (ctsegmentationpipeline.cpp:66-104)                                        */
+DXMCG_API int dxmcg_material_attenuation(const dxmcg_material* m, int correction, int n, const double* energies,
+    double* photo, double* incoherent, double* coherent);
+DXMCG_API int dxmcg_tube_spectrum(double kvp, double anode_angle_deg, int n_filters, const int32_t* filter_Z,
+    const double* filter_mm, double* energies, double* weights, int cap, int* n_out);
+DXMCG_API int dxmcg_tube_mean_energy(double kvp, int n_filters, const int32_t* filter_Z, const double* filter_mm,
+    double* mean_kev);
+DXMCG_API int dxmcg_tube_al_hvl(double kvp, int n_filters, const int32_t* filter_Z, const double* filter_mm,
+    double* hvl_mm);
+/* numberOfExposures()/exposure(i) (beamactorcontainer.cpp:114-121); out may be NULL to count */
+DXMCG_API int dxmcg_beam_exposures(const dxmcg_beam* beam, dxmcg_exposure* out, int cap, int* n_out);
+
+/* ---- world: World<AAVoxelGrid<5, C, 255>> (simulationpipeline.cpp:127-153) ---- */
+DXMCG_API int dxmcg_world_create(const int32_t dims[3], const double spacing_cm[3], const dxmcg_material* materials,
+    int n_materials, int correction, dxmcg_world** out);
+/* AAVoxelGrid::setData(dims, density, material, materials): host arrays of N voxels */
+DXMCG_API int dxmcg_world_set_data(dxmcg_world* w, const double* density, const uint8_t* material);
+DXMCG_API int dxmcg_world_set_data_f32(dxmcg_world* w, const float* density, const uint8_t* material);
+/* World::build(): validate, pack the voxels on the device, tables, majorant */
+DXMCG_API int dxmcg_world_build(dxmcg_world* w);
+DXMCG_API void dxmcg_world_destroy(dxmcg_world* w);
+DXMCG_API int dxmcg_world_clear_tally(dxmcg_world* w);
+/* raw tallies: energy imparted (keV), sum of squared deposits, number of events */
+DXMCG_API int dxmcg_world_read_tally(dxmcg_world* w, double* energy, double* energy2, uint64_t* count);
+/* doseScored(i).dose()/.variance()/.numberOfEvents() for all voxels (simulationpipeline.cpp:174-231), mGy */
+DXMCG_API int dxmcg_world_read_dose(dxmcg_world* w, double* dose, double* variance, uint64_t* count);
+/* device copy of the FP32 tables (tests): per material photo/incoh/coh/total, majorant */
+DXMCG_API int dxmcg_world_tables(dxmcg_world* w, int material, float* xs4, float* majorant);
+DXMCG_API int dxmcg_world_packed_density(dxmcg_world* w, float* density, uint8_t* material);
+
+/* ---- transport: Transport::operator()(world, beam, progress, bool) ---------- */
+DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts,
+    dxmcg_progress* progress, dxmcg_stats* stats);
+
+/* ---- TransportProgress (simulationpipeline.cpp:114-120, :234, :261) ---------- */
+DXMCG_API dxmcg_progress* dxmcg_progress_create(void);
+DXMCG_API void dxmcg_progress_destroy(dxmcg_progress* p);
+DXMCG_API void dxmcg_progress_get(const dxmcg_progress* p, uint64_t* done, uint64_t* total);
+DXMCG_API void dxmcg_progress_stop(dxmcg_progress* p);
+DXMCG_API int dxmcg_progress_continue(const dxmcg_progress* p);
+DXMCG_API int dxmcg_progress_message(const dxmcg_progress* p, char* buf, int cap);
+
+/* ---- device test hooks: the hot-path pieces run alone on the GPU ------------ */
+/* Siddon traversal of n grid-local rays; per ray up to cap segments */
+DXMCG_API int dxmcg_siddon_trace(int n_rays, const float* origins, const float* directions, const int32_t dims[3],
+    const float spacing[3], int cap, int64_t* voxel, float* length, int32_t* n_segments);
+/* Philox4x32-10 blocks */
+DXMCG_API int dxmcg_philox(int n, const uint32_t* counters, const uint32_t key[2], uint32_t* out);
+/* samplers driven by injected uniforms (u_stride uniforms per sample) */
+DXMCG_API int dxmcg_sample_compton(int n, const double* energies, const dxmcg_material* m, int correction,
+    const double* uniforms, int u_stride, double* e_out, double* cos_out, int32_t* used);
+DXMCG_API int dxmcg_sample_rayleigh(int n, const double* energies, const dxmcg_material* m, const double* uniforms,
+    int u_stride, double* cos_out, int32_t* used);
+/* source photons of histories [hist_begin, hist_begin + n): E, weight, grid-local pos[3], dir[3] */
+DXMCG_API int dxmcg_sample_source(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts, int n,
+    double* out8);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

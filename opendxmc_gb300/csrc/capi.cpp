@@ -1,0 +1,991 @@
+// capi.cpp -- implementation of the C ABI declared in include/dxmcg.h.
+//
+// Host side of the engine: world ingest and build (AAVoxelGrid::setData,
+// World::build; simulationpipeline.cpp:127-153), the transport driver
+// (Transport::operator(); simulationpipeline.cpp:155-171), progress/cancel
+// (TransportProgress; :114-120, :234, :261) and the dose readback
+// (doseScored(i); :174-231).  There is no CPU transport here: every run goes to
+// the device kernels in transport.cu.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/dxmcg.h"
+#include "engine.hpp"
+#include "physics.hpp"
+
+using namespace dxmcg;
+
+namespace {
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg)
+{
+    g_error = msg;
+    return code;
+}
+
+int cudaFail(cudaError_t e, const char* what)
+{
+    return fail(DXMCG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define DXMCG_CUDA(call)                       \
+    do {                                       \
+        cudaError_t e_ = (call);               \
+        if (e_ != cudaSuccess)                 \
+            return cudaFail(e_, #call);        \
+    } while (0)
+
+template <class T>
+struct DeviceBuffer {
+    T* p = nullptr;
+    size_t n = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    ~DeviceBuffer() { reset(); }
+    cudaError_t alloc(size_t count)
+    {
+        if (count == n && p)
+            return cudaSuccess;
+        reset();
+        const cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess)
+            n = count;
+        else
+            p = nullptr;
+        return e;
+    }
+    void reset()
+    {
+        if (p)
+            cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+// Element cross-section tables on the energy grid are shared by all worlds.
+struct ElementTables {
+    std::vector<double> photo, incoh, coh;
+};
+std::mutex g_elementMutex;
+std::map<std::pair<int, int>, ElementTables> g_elements;
+
+const ElementTables& elementTables(int Z, int correction)
+{
+    std::lock_guard<std::mutex> lock(g_elementMutex);
+    auto key = std::make_pair(Z, correction);
+    auto it = g_elements.find(key);
+    if (it != g_elements.end())
+        return it->second;
+    ElementTables t;
+    t.photo.resize(kNE);
+    t.incoh.resize(kNE);
+    t.coh.resize(kNE);
+    for (int i = 0; i < kNE; ++i) {
+        const double E = kEmin + i * kDE;
+        t.photo[i] = phys::photoelectric(E, Z);
+        t.incoh[i] = phys::incoherent(E, Z, correction);
+        t.coh[i] = phys::coherent(E, Z);
+    }
+    return g_elements.emplace(key, std::move(t)).first->second;
+}
+
+constexpr double kAvogadro = 6.02214076e23;
+constexpr double kKeVToMilliGrayGram = 1.602176634e-10; // mGy * g per keV
+constexpr double kMajorantSafety = 1.0 + 1.0 / 1048576.0;
+constexpr int kDefaultChunkLog2 = 26;
+} // namespace
+
+struct dxmcg_progress {
+    std::atomic<uint64_t> done { 0 };
+    std::atomic<uint64_t> total { 1 };
+    std::atomic<int> stop { 0 };
+    std::mutex msgMutex;
+    std::string message;
+    void setMessage(const std::string& m)
+    {
+        std::lock_guard<std::mutex> l(msgMutex);
+        message = m;
+    }
+};
+
+struct dxmcg_world {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int32_t dims[3] {};
+    double spacing[3] {};
+    size_t N = 0;
+    int correction = 1;
+    std::vector<dxmcg_material> materials;
+    bool hasData = false;
+    bool built = false;
+    // device
+    DeviceBuffer<double> dens64;
+    DeviceBuffer<float> dens32;
+    DeviceBuffer<uint8_t> mat;
+    DeviceBuffer<uint32_t> vox;
+    DeviceBuffer<Tally> tally;
+    DeviceBuffer<float> tot;
+    DeviceBuffer<float4> xs;
+    DeviceBuffer<float> maj;
+    DeviceBuffer<DevMaterial> mats;
+    DeviceBuffer<DevCounters> counters;
+    DeviceBuffer<unsigned> scratch; // rho max bits [256] + error word
+    DeviceBuffer<DevExposure> exps;
+    DeviceBuffer<DevSpectrum> spec;
+    DeviceBuffer<DevBowtie> bowtie;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // host copies of the FP64 tables (tests)
+    std::vector<double> rhoMax;
+    double historiesScored = 0.0;
+    double voxelVolume = 0.0;
+};
+
+namespace {
+
+DevMaterial toDevMaterial(const dxmcg_material& m)
+{
+    const auto s = samplingElements(m);
+    DevMaterial d {};
+    d.n = s.n;
+    d.Zsum = static_cast<float>(s.Zsum);
+    for (int i = 0; i < s.n; ++i) {
+        d.nZ[i] = static_cast<float>(s.nZ[i]);
+        d.nZ2[i] = static_cast<float>(s.nZ2[i]);
+        d.a[i] = static_cast<float>(s.a[i]);
+    }
+    return d;
+}
+
+// Mass attenuation tables of one material on the grid, FP64, from cached element tables.
+void materialTables(const dxmcg_material& m, int correction, double* photo, double* incoh, double* coh)
+{
+    double wsum = 0;
+    for (int i = 0; i < m.n; ++i)
+        wsum += m.w[i];
+    for (int e = 0; e < kNE; ++e)
+        photo[e] = incoh[e] = coh[e] = 0.0;
+    for (int i = 0; i < m.n; ++i) {
+        const auto& t = elementTables(m.Z[i], correction);
+        const double f = (m.w[i] / wsum) * kAvogadro / phys::atomicMass(m.Z[i]) * 1e-24;
+        for (int e = 0; e < kNE; ++e) {
+            photo[e] += f * t.photo[e];
+            incoh[e] += f * t.incoh[e];
+            coh[e] += f * t.coh[e];
+        }
+    }
+}
+
+int ensureStream(dxmcg_world* w)
+{
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    if (!w->stream)
+        DXMCG_CUDA(cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking));
+    if (!w->ev0)
+        DXMCG_CUDA(cudaEventCreate(&w->ev0));
+    if (!w->ev1)
+        DXMCG_CUDA(cudaEventCreate(&w->ev1));
+    return DXMCG_OK;
+}
+
+struct BowtieHost {
+    std::vector<double> ang, w;
+    double eval(double a) const
+    {
+        const int n = static_cast<int>(ang.size());
+        if (a <= ang[0])
+            return w[0];
+        if (a >= ang[n - 1])
+            return w[n - 1];
+        int lo = 0, hi = n - 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) / 2;
+            (ang[mid] <= a ? lo : hi) = mid;
+        }
+        const double t = (a - ang[lo]) / (ang[hi] - ang[lo]);
+        return w[lo] + t * (w[hi] - w[lo]);
+    }
+    // exact mean over |angle| in [0, half] of the piecewise-linear profile
+    double mean(double half) const
+    {
+        if (half <= 0)
+            return 1.0;
+        std::vector<double> xs { 0.0 };
+        for (double a : ang)
+            if (a > 0 && a < half)
+                xs.push_back(a);
+        xs.push_back(half);
+        double s = 0;
+        for (size_t i = 0; i + 1 < xs.size(); ++i)
+            s += 0.5 * (eval(xs[i]) + eval(xs[i + 1])) * (xs[i + 1] - xs[i]);
+        return s / half;
+    }
+};
+
+// Everything a launch needs for one beam on one world.
+int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, DevJob& J, uint64_t& nHist)
+{
+    std::vector<dxmcg_exposure> ex;
+    if (expandExposures(b, ex) != DXMCG_OK || ex.empty())
+        return fail(DXMCG_ERR_ARGUMENT, "beam: invalid geometry");
+    if (b.particles_per_exposure == 0)
+        return fail(DXMCG_ERR_ARGUMENT, "beam: particles_per_exposure is 0");
+    if (b.particles_per_exposure > (1ull << 40) || ex.size() > (1u << 24))
+        return fail(DXMCG_ERR_ARGUMENT, "beam: too many histories");
+    nHist = static_cast<uint64_t>(ex.size()) * b.particles_per_exposure;
+
+    double origin[3];
+    for (int a = 0; a < 3; ++a)
+        origin[a] = -0.5 * w->dims[a] * w->spacing[a];
+    std::vector<DevExposure> dex(ex.size());
+    for (size_t i = 0; i < ex.size(); ++i) {
+        const auto& e = ex[i];
+        DevExposure& d = dex[i];
+        const double n[3] = { e.c0[1] * e.c1[2] - e.c0[2] * e.c1[1], e.c0[2] * e.c1[0] - e.c0[0] * e.c1[2],
+            e.c0[0] * e.c1[1] - e.c0[1] * e.c1[0] };
+        for (int a = 0; a < 3; ++a) {
+            d.pos[a] = static_cast<float>(e.pos[a] - origin[a]);
+            d.c0[a] = static_cast<float>(e.c0[a]);
+            d.c1[a] = static_cast<float>(e.c1[a]);
+            d.n[a] = static_cast<float>(n[a]);
+        }
+        d.half[0] = static_cast<float>(e.half[0]);
+        d.half[1] = static_cast<float>(e.half[1]);
+        d.weight = static_cast<float>(e.weight);
+        d.tube = e.tube;
+    }
+    DXMCG_CUDA(w->exps.alloc(dex.size()));
+    DXMCG_CUDA(cudaMemcpyAsync(w->exps.p, dex.data(), dex.size() * sizeof(DevExposure), cudaMemcpyHostToDevice,
+        w->stream));
+
+    std::vector<DevSpectrum> spec(2);
+    if (b.type != DXMCG_BEAM_PENCIL) {
+        for (int t = 0; t < 2; ++t) {
+            const bool dual = b.type == DXMCG_BEAM_CT_SPIRAL_DUAL_ENERGY && t == 1;
+            const auto s = tubeSpectrum(dual ? b.kvp_b : b.kvp, b.anode_angle_deg, dual ? b.n_filters_b : b.n_filters,
+                dual ? b.filter_Z_b : b.filter_Z, dual ? b.filter_mm_b : b.filter_mm);
+            if (s.energy.empty()) {
+                if (t == 0)
+                    return fail(DXMCG_ERR_ARGUMENT, "beam: tube voltage out of range");
+                spec[1] = spec[0];
+                continue;
+            }
+            if (s.energy.back() > kEmin + (kNE - 1) * kDE)
+                return fail(DXMCG_ERR_ARGUMENT, "beam: tube voltage above the table range (150 keV)");
+            const auto at = buildAlias(s);
+            DevSpectrum& d = spec[t];
+            d.n = static_cast<int>(at.energy.size());
+            for (int k = 0; k < d.n; ++k) {
+                d.E[k] = at.energy[k];
+                d.thr[k] = at.threshold[k];
+                d.alias[k] = at.alias[k];
+            }
+        }
+    } else if (!(b.energy_kev >= kEcut && b.energy_kev <= kEmin + (kNE - 1) * kDE)) {
+        return fail(DXMCG_ERR_ARGUMENT, "beam: pencil energy out of range");
+    }
+    DXMCG_CUDA(w->spec.alloc(2));
+    DXMCG_CUDA(cudaMemcpyAsync(w->spec.p, spec.data(), 2 * sizeof(DevSpectrum), cudaMemcpyHostToDevice, w->stream));
+
+    J = DevJob {};
+    J.bowtie = nullptr;
+    if (b.n_bowtie > 0 && b.bowtie_angle && b.bowtie_weight) {
+        if (b.n_bowtie > kMaxBowtie)
+            return fail(DXMCG_ERR_ARGUMENT, "beam: bowtie has too many points");
+        // sorted by angle: the bowtie JSON lists points unordered (bowtiefilters.json:4-32)
+        std::vector<std::pair<double, double>> pts;
+        for (int i = 0; i < b.n_bowtie; ++i)
+            pts.emplace_back(b.bowtie_angle[i], b.bowtie_weight[i]);
+        std::stable_sort(pts.begin(), pts.end(), [](auto& x, auto& y) { return x.first < y.first; });
+        BowtieHost bh;
+        for (auto& p : pts) {
+            bh.ang.push_back(p.first);
+            bh.w.push_back(p.second);
+        }
+        DevBowtie db {};
+        db.n = static_cast<int>(pts.size());
+        for (int i = 0; i < db.n; ++i) {
+            db.ang[i] = static_cast<float>(bh.ang[i]);
+            db.w[i] = static_cast<float>(bh.w[i]);
+        }
+        for (int t = 0; t < 2; ++t) {
+            double half = 0;
+            for (const auto& e : ex)
+                if (e.tube == t) {
+                    half = e.half[0];
+                    break;
+                }
+            const double m = bh.mean(half);
+            db.inv_norm[t] = static_cast<float>(m > 0 ? 1.0 / m : 1.0);
+        }
+        DXMCG_CUDA(w->bowtie.alloc(1));
+        DXMCG_CUDA(cudaMemcpyAsync(w->bowtie.p, &db, sizeof(DevBowtie), cudaMemcpyHostToDevice, w->stream));
+        J.bowtie = w->bowtie.p;
+    }
+    J.vox = w->vox.p;
+    J.nx = w->dims[0];
+    J.ny = w->dims[1];
+    J.nz = w->dims[2];
+    for (int a = 0; a < 3; ++a) {
+        J.sp[a] = static_cast<float>(w->spacing[a]);
+        J.isp[a] = static_cast<float>(1.0 / w->spacing[a]);
+        J.L[a] = static_cast<float>(w->dims[a] * w->spacing[a]);
+        J.Lin[a] = std::nextafter(J.L[a], 0.0f);
+    }
+    J.tot = w->tot.p;
+    J.xs = w->xs.p;
+    J.maj = w->maj.p;
+    J.mats = w->mats.p;
+    J.n_mats = static_cast<int>(w->materials.size());
+    J.correction = w->correction;
+    J.tally = w->tally.p;
+    J.exps = w->exps.p;
+    J.n_exp = static_cast<int>(ex.size());
+    J.ppe = b.particles_per_exposure;
+    J.spec = w->spec.p;
+    J.beam_type = b.type;
+    J.pencil_energy = static_cast<float>(b.energy_kev);
+    J.key0 = static_cast<uint32_t>(o.seed);
+    J.key1 = static_cast<uint32_t>(o.seed >> 32);
+    J.stream = o.stream;
+    J.tracking = o.tracking;
+    return DXMCG_OK;
+}
+
+LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, w->device);
+    LaunchShape s;
+    s.block = o.block_size > 0 ? o.block_size : 256;
+    s.block = std::max(32, std::min(256, s.block / 32 * 32));
+    const int per = o.blocks_per_sm > 0 ? o.blocks_per_sm : std::max(1, 2048 / s.block);
+    s.grid = std::max(1, sms) * per;
+    return s;
+}
+
+} // namespace
+
+// ============================================================================ C ABI
+extern "C" {
+
+DXMCG_API int dxmcg_version(void) { return DXMCG_VERSION; }
+
+DXMCG_API const char* dxmcg_last_error(void) { return g_error.c_str(); }
+
+DXMCG_API int dxmcg_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+DXMCG_API int dxmcg_set_device(int device)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1)
+        return fail(DXMCG_ERR_NO_DEVICE, "set_device: no CUDA device");
+    if (device < 0 || device >= n)
+        return fail(DXMCG_ERR_ARGUMENT, "set_device: no such device");
+    DXMCG_CUDA(cudaSetDevice(device));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_material_attenuation(const dxmcg_material* m, int correction, int n, const double* energies,
+    double* photo, double* incoherent, double* coherent)
+{
+    if (!m || !validComposition(*m) || n < 0 || (n > 0 && (!energies || !photo || !incoherent || !coherent)))
+        return fail(DXMCG_ERR_ARGUMENT, "material_attenuation: bad arguments");
+    for (int i = 0; i < n; ++i) {
+        const auto a = attenuation(*m, correction, energies[i]);
+        photo[i] = a.photo;
+        incoherent[i] = a.incoherent;
+        coherent[i] = a.coherent;
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_tube_spectrum(double kvp, double anode_angle_deg, int n_filters, const int32_t* filter_Z,
+    const double* filter_mm, double* energies, double* weights, int cap, int* n_out)
+{
+    if (n_filters < 0 || n_filters > 8 || (n_filters > 0 && (!filter_Z || !filter_mm)))
+        return fail(DXMCG_ERR_ARGUMENT, "tube_spectrum: bad filters");
+    const auto s = tubeSpectrum(kvp, anode_angle_deg, n_filters, filter_Z, filter_mm);
+    if (s.energy.empty())
+        return fail(DXMCG_ERR_ARGUMENT, "tube_spectrum: tube voltage out of range");
+    if (n_out)
+        *n_out = static_cast<int>(s.energy.size());
+    if (!energies || !weights)
+        return DXMCG_OK;
+    if (cap < static_cast<int>(s.energy.size()))
+        return fail(DXMCG_ERR_CAPACITY, "tube_spectrum: output too small");
+    std::copy(s.energy.begin(), s.energy.end(), energies);
+    std::copy(s.weight.begin(), s.weight.end(), weights);
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_tube_mean_energy(double kvp, int n_filters, const int32_t* filter_Z, const double* filter_mm,
+    double* mean_kev)
+{
+    const auto s = tubeSpectrum(kvp, 12.0, n_filters, filter_Z, filter_mm);
+    if (s.energy.empty() || !mean_kev)
+        return fail(DXMCG_ERR_ARGUMENT, "tube_mean_energy: bad arguments");
+    *mean_kev = tubeMeanEnergy(s);
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_tube_al_hvl(double kvp, int n_filters, const int32_t* filter_Z, const double* filter_mm,
+    double* hvl_mm)
+{
+    const auto s = tubeSpectrum(kvp, 12.0, n_filters, filter_Z, filter_mm);
+    if (s.energy.empty() || !hvl_mm)
+        return fail(DXMCG_ERR_ARGUMENT, "tube_al_hvl: bad arguments");
+    *hvl_mm = tubeAlHalfValueLayer(s);
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_beam_exposures(const dxmcg_beam* beam, dxmcg_exposure* out, int cap, int* n_out)
+{
+    if (!beam)
+        return fail(DXMCG_ERR_ARGUMENT, "beam_exposures: null beam");
+    std::vector<dxmcg_exposure> ex;
+    const int rc = expandExposures(*beam, ex);
+    if (rc != DXMCG_OK)
+        return fail(rc, "beam_exposures: invalid beam geometry");
+    if (n_out)
+        *n_out = static_cast<int>(ex.size());
+    if (!out)
+        return DXMCG_OK;
+    if (cap < static_cast<int>(ex.size()))
+        return fail(DXMCG_ERR_CAPACITY, "beam_exposures: output too small");
+    std::copy(ex.begin(), ex.end(), out);
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_world_create(const int32_t dims[3], const double spacing_cm[3], const dxmcg_material* materials,
+    int n_materials, int correction, dxmcg_world** out)
+{
+    if (!out)
+        return fail(DXMCG_ERR_ARGUMENT, "world_create: null output");
+    *out = nullptr;
+    if (!dims || !spacing_cm || !materials || n_materials < 1 || n_materials > DXMCG_MAX_MATERIALS)
+        return fail(DXMCG_ERR_ARGUMENT, "world_create: need 1..255 materials");
+    uint64_t N = 1;
+    for (int a = 0; a < 3; ++a) {
+        if (dims[a] < 1 || !(spacing_cm[a] > 0) || !std::isfinite(spacing_cm[a]))
+            return fail(DXMCG_ERR_ARGUMENT, "world_create: dimensions and spacing must be positive");
+        N *= static_cast<uint64_t>(dims[a]);
+    }
+    if (N >= (1ull << 32))
+        return fail(DXMCG_ERR_ARGUMENT, "world_create: more than 2^32-1 voxels");
+    for (int m = 0; m < n_materials; ++m)
+        if (!validComposition(materials[m]))
+            return fail(DXMCG_ERR_ARGUMENT, "world_create: invalid material composition " + std::to_string(m));
+    if (correction < 0 || correction > 2)
+        return fail(DXMCG_ERR_ARGUMENT, "world_create: correction must be 0, 1 or 2");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+        return fail(DXMCG_ERR_NO_DEVICE, "world_create: no CUDA device");
+    auto* w = new dxmcg_world();
+    cudaGetDevice(&w->device);
+    for (int a = 0; a < 3; ++a) {
+        w->dims[a] = dims[a];
+        w->spacing[a] = spacing_cm[a];
+    }
+    w->N = static_cast<size_t>(N);
+    w->voxelVolume = spacing_cm[0] * spacing_cm[1] * spacing_cm[2];
+    w->correction = correction;
+    w->materials.assign(materials, materials + n_materials);
+    const int rc = ensureStream(w);
+    if (rc != DXMCG_OK) {
+        dxmcg_world_destroy(w);
+        return rc;
+    }
+    *out = w;
+    return DXMCG_OK;
+}
+
+static int setData(dxmcg_world* w, const double* d64, const float* d32, const uint8_t* material)
+{
+    if (!w || (!d64 && !d32) || !material)
+        return fail(DXMCG_ERR_ARGUMENT, "world_set_data: null argument");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    DXMCG_CUDA(w->mat.alloc(w->N));
+    if (d64) {
+        w->dens32.reset();
+        DXMCG_CUDA(w->dens64.alloc(w->N));
+        DXMCG_CUDA(cudaMemcpyAsync(w->dens64.p, d64, w->N * sizeof(double), cudaMemcpyHostToDevice, w->stream));
+    } else {
+        w->dens64.reset();
+        DXMCG_CUDA(w->dens32.alloc(w->N));
+        DXMCG_CUDA(cudaMemcpyAsync(w->dens32.p, d32, w->N * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    }
+    DXMCG_CUDA(cudaMemcpyAsync(w->mat.p, material, w->N, cudaMemcpyHostToDevice, w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    w->hasData = true;
+    w->built = false;
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_world_set_data(dxmcg_world* w, const double* density, const uint8_t* material)
+{
+    return setData(w, density, nullptr, material);
+}
+
+DXMCG_API int dxmcg_world_set_data_f32(dxmcg_world* w, const float* density, const uint8_t* material)
+{
+    return setData(w, nullptr, density, material);
+}
+
+DXMCG_API int dxmcg_world_build(dxmcg_world* w)
+{
+    if (!w || !w->hasData)
+        return fail(DXMCG_ERR_STATE, "world_build: setData first");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    const int M = static_cast<int>(w->materials.size());
+    DXMCG_CUDA(w->vox.alloc(w->N));
+    DXMCG_CUDA(w->scratch.alloc(257));
+    DXMCG_CUDA(cudaMemsetAsync(w->scratch.p, 0, 257 * sizeof(unsigned), w->stream));
+    cudaError_t e = launchPack(w->dens64.p, w->dens32.p, w->mat.p, w->vox.p, w->N, M, w->scratch.p,
+        w->scratch.p + 256, w->stream);
+    if (e != cudaSuccess)
+        return cudaFail(e, "pack kernel");
+    unsigned host[257];
+    DXMCG_CUDA(cudaMemcpyAsync(host, w->scratch.p, sizeof(host), cudaMemcpyDeviceToHost, w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    if (host[256] & kErrBadMaterial)
+        return fail(DXMCG_ERR_ARGUMENT, "world_build: a voxel's material index is >= the number of materials");
+    if (host[256] & kErrBadDensity)
+        return fail(DXMCG_ERR_ARGUMENT, "world_build: negative or non-finite density");
+    w->dens64.reset();
+    w->dens32.reset();
+    w->mat.reset();
+
+    w->rhoMax.assign(M, 0.0);
+    for (int m = 0; m < M; ++m) {
+        float f;
+        std::memcpy(&f, &host[m], 4);
+        w->rhoMax[m] = f;
+    }
+    std::vector<float> tot(static_cast<size_t>(M) * kNE);
+    std::vector<float4> xs(static_cast<size_t>(M) * kNE);
+    std::vector<double> maj(kNE, 0.0);
+    std::vector<double> ph(kNE), ic(kNE), co(kNE);
+    std::vector<DevMaterial> dm(M);
+    for (int m = 0; m < M; ++m) {
+        materialTables(w->materials[m], w->correction, ph.data(), ic.data(), co.data());
+        for (int i = 0; i < kNE; ++i) {
+            const double t = ph[i] + ic[i] + co[i];
+            tot[m * kNE + i] = static_cast<float>(t);
+            xs[m * kNE + i] = make_float4(static_cast<float>(ph[i]), static_cast<float>(ic[i]),
+                static_cast<float>(co[i]), static_cast<float>(t));
+            maj[i] = std::max(maj[i], w->rhoMax[m] * t);
+        }
+        dm[m] = toDevMaterial(w->materials[m]);
+    }
+    std::vector<float> majf(kNE);
+    for (int i = 0; i < kNE; ++i)
+        majf[i] = static_cast<float>(std::max(maj[i] * kMajorantSafety, 1e-30));
+    DXMCG_CUDA(w->tot.alloc(tot.size()));
+    DXMCG_CUDA(w->xs.alloc(xs.size()));
+    DXMCG_CUDA(w->maj.alloc(kNE));
+    DXMCG_CUDA(w->mats.alloc(M));
+    DXMCG_CUDA(w->counters.alloc(1));
+    DXMCG_CUDA(w->tally.alloc(w->N));
+    DXMCG_CUDA(cudaMemcpyAsync(w->tot.p, tot.data(), tot.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    DXMCG_CUDA(cudaMemcpyAsync(w->xs.p, xs.data(), xs.size() * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
+    DXMCG_CUDA(cudaMemcpyAsync(w->maj.p, majf.data(), kNE * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    DXMCG_CUDA(cudaMemcpyAsync(w->mats.p, dm.data(), M * sizeof(DevMaterial), cudaMemcpyHostToDevice, w->stream));
+    DXMCG_CUDA(cudaMemsetAsync(w->tally.p, 0, w->N * sizeof(Tally), w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    w->historiesScored = 0.0;
+    w->built = true;
+    return DXMCG_OK;
+}
+
+DXMCG_API void dxmcg_world_destroy(dxmcg_world* w)
+{
+    if (!w)
+        return;
+    cudaSetDevice(w->device);
+    if (w->stream)
+        cudaStreamSynchronize(w->stream);
+    if (w->ev0)
+        cudaEventDestroy(w->ev0);
+    if (w->ev1)
+        cudaEventDestroy(w->ev1);
+    if (w->stream)
+        cudaStreamDestroy(w->stream);
+    delete w;
+}
+
+DXMCG_API int dxmcg_world_clear_tally(dxmcg_world* w)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_clear_tally: world not built");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    DXMCG_CUDA(cudaMemsetAsync(w->tally.p, 0, w->N * sizeof(Tally), w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    w->historiesScored = 0.0;
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_world_read_tally(dxmcg_world* w, double* energy, double* energy2, uint64_t* count)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_read_tally: world not built");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    std::vector<Tally> t(w->N);
+    DXMCG_CUDA(cudaMemcpyAsync(t.data(), w->tally.p, w->N * sizeof(Tally), cudaMemcpyDeviceToHost, w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    for (size_t i = 0; i < w->N; ++i) {
+        if (energy)
+            energy[i] = t[i].e;
+        if (energy2)
+            energy2[i] = t[i].e2;
+        if (count)
+            count[i] = t[i].n;
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_world_read_dose(dxmcg_world* w, double* dose, double* variance, uint64_t* count)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_read_dose: world not built");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    // finalize on the device into a scratch block, then one copy per array
+    DeviceBuffer<double> d, v;
+    DeviceBuffer<unsigned long long> c;
+    if (dose)
+        DXMCG_CUDA(d.alloc(w->N));
+    if (variance)
+        DXMCG_CUDA(v.alloc(w->N));
+    if (count)
+        DXMCG_CUDA(c.alloc(w->N));
+    cudaError_t e = launchFinalize(w->tally.p, w->vox.p, w->N, kKeVToMilliGrayGram / w->voxelVolume,
+        w->historiesScored, dose ? d.p : nullptr, variance ? v.p : nullptr, count ? c.p : nullptr, w->stream);
+    if (e != cudaSuccess)
+        return cudaFail(e, "finalize kernel");
+    if (dose)
+        DXMCG_CUDA(cudaMemcpyAsync(dose, d.p, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    if (variance)
+        DXMCG_CUDA(cudaMemcpyAsync(variance, v.p, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    if (count)
+        DXMCG_CUDA(cudaMemcpyAsync(count, c.p, w->N * sizeof(uint64_t), cudaMemcpyDeviceToHost, w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_world_tables(dxmcg_world* w, int material, float* xs4, float* majorant)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_tables: world not built");
+    if (material < 0 || material >= static_cast<int>(w->materials.size()))
+        return fail(DXMCG_ERR_ARGUMENT, "world_tables: bad material");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    if (xs4)
+        DXMCG_CUDA(cudaMemcpy(xs4, w->xs.p + static_cast<size_t>(material) * kNE, kNE * sizeof(float4),
+            cudaMemcpyDeviceToHost));
+    if (majorant)
+        DXMCG_CUDA(cudaMemcpy(majorant, w->maj.p, kNE * sizeof(float), cudaMemcpyDeviceToHost));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_world_packed_density(dxmcg_world* w, float* density, uint8_t* material)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_packed_density: world not built");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    std::vector<uint32_t> v(w->N);
+    DXMCG_CUDA(cudaMemcpy(v.data(), w->vox.p, w->N * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < w->N; ++i) {
+        if (density) {
+            const uint32_t b = v[i] & 0xffffff00u;
+            std::memcpy(&density[i], &b, 4);
+        }
+        if (material)
+            material[i] = static_cast<uint8_t>(v[i] & 0xffu);
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts,
+    dxmcg_progress* progress, dxmcg_stats* stats)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "transport_run: world not built");
+    if (!beam)
+        return fail(DXMCG_ERR_ARGUMENT, "transport_run: null beam");
+    dxmcg_run_options o {};
+    o.seed = 1;
+    if (opts)
+        o = *opts;
+    if (o.tracking != DXMCG_TRACK_WOODCOCK && o.tracking != DXMCG_TRACK_SIDDON)
+        return fail(DXMCG_ERR_ARGUMENT, "transport_run: unknown tracking mode");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    DevJob J;
+    uint64_t nHist = 0;
+    int rc = prepareJob(w, *beam, o, J, nHist);
+    if (rc != DXMCG_OK)
+        return rc;
+    const uint64_t h0 = std::min<uint64_t>(o.hist_begin, nHist);
+    const uint64_t h1 = o.hist_end == 0 ? nHist : std::min<uint64_t>(o.hist_end, nHist);
+    if (progress) {
+        progress->total.store(std::max<uint64_t>(h1 - h0, 1));
+        progress->done.store(0);
+        progress->setMessage("Simulating");
+    }
+    const LaunchShape shape = chooseShape(w, o);
+    const int chunkLog2 = o.chunk_histories_log2 > 0 ? std::min(o.chunk_histories_log2, 40) : kDefaultChunkLog2;
+    const uint64_t chunk = 1ull << chunkLog2;
+    DevCounters zero {};
+    DXMCG_CUDA(cudaMemcpyAsync(w->counters.p, &zero, sizeof(zero), cudaMemcpyHostToDevice, w->stream));
+    float kernelMs = 0.0f;
+    bool cancelled = false;
+    for (uint64_t a = h0; a < h1; a += chunk) {
+        if (progress && progress->stop.load()) {
+            cancelled = true;
+            break;
+        }
+        const uint64_t b = std::min(h1, a + chunk);
+        const unsigned long long head = a;
+        DXMCG_CUDA(cudaMemcpyAsync(&w->counters.p->next, &head, sizeof(head), cudaMemcpyHostToDevice, w->stream));
+        DXMCG_CUDA(cudaEventRecord(w->ev0, w->stream));
+        cudaError_t e = launchTransport(J, b, w->counters.p, shape, w->stream);
+        if (e != cudaSuccess)
+            return cudaFail(e, "transport kernel launch");
+        DXMCG_CUDA(cudaEventRecord(w->ev1, w->stream));
+        DXMCG_CUDA(cudaEventSynchronize(w->ev1));
+        float ms = 0;
+        DXMCG_CUDA(cudaEventElapsedTime(&ms, w->ev0, w->ev1));
+        kernelMs += ms;
+        if (progress)
+            progress->done.store(b - h0);
+    }
+    DevCounters c {};
+    DXMCG_CUDA(cudaMemcpyAsync(&c, w->counters.p, sizeof(c), cudaMemcpyDeviceToHost, w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    w->historiesScored += static_cast<double>(c.histories);
+    if (stats) {
+        stats->e_source = c.e_source;
+        stats->e_deposited = c.e_deposited;
+        stats->e_escaped = c.e_escaped;
+        stats->n_histories = c.histories;
+        stats->n_missed = c.missed;
+        stats->n_visits = c.visits;
+        stats->n_photo = c.photo;
+        stats->n_compton = c.compton;
+        stats->n_rayleigh = c.rayleigh;
+        stats->n_cutoff = c.cutoff;
+        stats->n_errors = c.errors;
+        stats->n_interacted = c.interacted;
+        stats->kernel_ms = kernelMs;
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->dose_scale = kKeVToMilliGrayGram / w->voxelVolume;
+    }
+    if (progress)
+        progress->setMessage(cancelled ? "Cancelled" : "Done");
+    if (c.error_flags & kErrStepLimit)
+        return fail(DXMCG_ERR_DEVICE, "transport: a history exceeded the step limit");
+    if (c.error_flags & kErrRejectLimit)
+        return fail(DXMCG_ERR_DEVICE, "transport: a sampler exceeded its rejection limit");
+    if (cancelled)
+        return fail(DXMCG_ERR_CANCELLED, "transport: cancelled");
+    return DXMCG_OK;
+}
+
+DXMCG_API dxmcg_progress* dxmcg_progress_create(void) { return new dxmcg_progress(); }
+DXMCG_API void dxmcg_progress_destroy(dxmcg_progress* p) { delete p; }
+DXMCG_API void dxmcg_progress_get(const dxmcg_progress* p, uint64_t* done, uint64_t* total)
+{
+    if (!p)
+        return;
+    if (done)
+        *done = p->done.load();
+    if (total)
+        *total = p->total.load();
+}
+DXMCG_API void dxmcg_progress_stop(dxmcg_progress* p)
+{
+    if (p)
+        p->stop.store(1);
+}
+DXMCG_API int dxmcg_progress_continue(const dxmcg_progress* p) { return p ? !p->stop.load() : 1; }
+DXMCG_API int dxmcg_progress_message(const dxmcg_progress* p, char* buf, int cap)
+{
+    if (!p || !buf || cap <= 0)
+        return 0;
+    auto* q = const_cast<dxmcg_progress*>(p);
+    std::lock_guard<std::mutex> l(q->msgMutex);
+    const int n = std::min<int>(cap - 1, static_cast<int>(q->message.size()));
+    std::memcpy(buf, q->message.data(), n);
+    buf[n] = 0;
+    return n;
+}
+
+// ---------------------------------------------------------------- test hooks
+DXMCG_API int dxmcg_siddon_trace(int n_rays, const float* origins, const float* directions, const int32_t dims[3],
+    const float spacing[3], int cap, int64_t* voxel, float* length, int32_t* n_segments)
+{
+    if (n_rays < 0 || !origins || !directions || !dims || !spacing || cap < 1 || !voxel || !length || !n_segments)
+        return fail(DXMCG_ERR_ARGUMENT, "siddon_trace: bad arguments");
+    if (n_rays == 0)
+        return DXMCG_OK;
+    DeviceBuffer<float> o, d, l;
+    DeviceBuffer<long long> v;
+    DeviceBuffer<int> c;
+    DXMCG_CUDA(o.alloc(3 * static_cast<size_t>(n_rays)));
+    DXMCG_CUDA(d.alloc(3 * static_cast<size_t>(n_rays)));
+    DXMCG_CUDA(v.alloc(static_cast<size_t>(n_rays) * cap));
+    DXMCG_CUDA(l.alloc(static_cast<size_t>(n_rays) * cap));
+    DXMCG_CUDA(c.alloc(n_rays));
+    DXMCG_CUDA(cudaMemcpy(o.p, origins, 3 * sizeof(float) * n_rays, cudaMemcpyHostToDevice));
+    DXMCG_CUDA(cudaMemcpy(d.p, directions, 3 * sizeof(float) * n_rays, cudaMemcpyHostToDevice));
+    cudaError_t e = launchSiddon(n_rays, o.p, d.p, dims[0], dims[1], dims[2], spacing[0], spacing[1], spacing[2], cap,
+        v.p, l.p, c.p, nullptr);
+    if (e != cudaSuccess)
+        return cudaFail(e, "siddon kernel");
+    DXMCG_CUDA(cudaMemcpy(voxel, v.p, sizeof(long long) * n_rays * static_cast<size_t>(cap), cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(length, l.p, sizeof(float) * n_rays * static_cast<size_t>(cap), cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(n_segments, c.p, sizeof(int) * n_rays, cudaMemcpyDeviceToHost));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_philox(int n, const uint32_t* counters, const uint32_t key[2], uint32_t* out)
+{
+    if (n < 0 || !counters || !key || !out)
+        return fail(DXMCG_ERR_ARGUMENT, "philox: bad arguments");
+    if (n == 0)
+        return DXMCG_OK;
+    DeviceBuffer<uint32_t> c, o;
+    DXMCG_CUDA(c.alloc(4 * static_cast<size_t>(n)));
+    DXMCG_CUDA(o.alloc(4 * static_cast<size_t>(n)));
+    DXMCG_CUDA(cudaMemcpy(c.p, counters, 16 * static_cast<size_t>(n), cudaMemcpyHostToDevice));
+    cudaError_t e = launchPhilox(n, c.p, key[0], key[1], o.p, nullptr);
+    if (e != cudaSuccess)
+        return cudaFail(e, "philox kernel");
+    DXMCG_CUDA(cudaMemcpy(out, o.p, 16 * static_cast<size_t>(n), cudaMemcpyDeviceToHost));
+    return DXMCG_OK;
+}
+
+static int samplerCommon(int n, const double* energies, const dxmcg_material* m, const double* uniforms, int stride,
+    DeviceBuffer<float>& E, DeviceBuffer<float>& U, DeviceBuffer<DevMaterial>& M)
+{
+    if (n < 0 || !energies || !m || !uniforms || stride < 1 || !validComposition(*m))
+        return fail(DXMCG_ERR_ARGUMENT, "sampler: bad arguments");
+    std::vector<float> e(n), u(static_cast<size_t>(n) * stride);
+    for (int i = 0; i < n; ++i)
+        e[i] = static_cast<float>(energies[i]);
+    for (size_t i = 0; i < u.size(); ++i)
+        u[i] = static_cast<float>(uniforms[i]);
+    const DevMaterial dm = toDevMaterial(*m);
+    DXMCG_CUDA(E.alloc(std::max(n, 1)));
+    DXMCG_CUDA(U.alloc(std::max<size_t>(u.size(), 1)));
+    DXMCG_CUDA(M.alloc(1));
+    DXMCG_CUDA(cudaMemcpy(E.p, e.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    DXMCG_CUDA(cudaMemcpy(U.p, u.data(), sizeof(float) * u.size(), cudaMemcpyHostToDevice));
+    DXMCG_CUDA(cudaMemcpy(M.p, &dm, sizeof(dm), cudaMemcpyHostToDevice));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_sample_compton(int n, const double* energies, const dxmcg_material* m, int correction,
+    const double* uniforms, int u_stride, double* e_out, double* cos_out, int32_t* used)
+{
+    if (!e_out || !cos_out || !used)
+        return fail(DXMCG_ERR_ARGUMENT, "sample_compton: null output");
+    DeviceBuffer<float> E, U, eo, co;
+    DeviceBuffer<DevMaterial> M;
+    DeviceBuffer<int> us;
+    int rc = samplerCommon(n, energies, m, uniforms, u_stride, E, U, M);
+    if (rc != DXMCG_OK || n == 0)
+        return rc;
+    DXMCG_CUDA(eo.alloc(n));
+    DXMCG_CUDA(co.alloc(n));
+    DXMCG_CUDA(us.alloc(n));
+    cudaError_t e = launchSampleCompton(n, E.p, M.p, correction, U.p, u_stride, eo.p, co.p, us.p, nullptr);
+    if (e != cudaSuccess)
+        return cudaFail(e, "compton kernel");
+    std::vector<float> a(n), b(n);
+    DXMCG_CUDA(cudaMemcpy(a.data(), eo.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(b.data(), co.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(used, us.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) {
+        e_out[i] = a[i];
+        cos_out[i] = b[i];
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_sample_rayleigh(int n, const double* energies, const dxmcg_material* m, const double* uniforms,
+    int u_stride, double* cos_out, int32_t* used)
+{
+    if (!cos_out || !used)
+        return fail(DXMCG_ERR_ARGUMENT, "sample_rayleigh: null output");
+    DeviceBuffer<float> E, U, co;
+    DeviceBuffer<DevMaterial> M;
+    DeviceBuffer<int> us;
+    int rc = samplerCommon(n, energies, m, uniforms, u_stride, E, U, M);
+    if (rc != DXMCG_OK || n == 0)
+        return rc;
+    DXMCG_CUDA(co.alloc(n));
+    DXMCG_CUDA(us.alloc(n));
+    cudaError_t e = launchSampleRayleigh(n, E.p, M.p, U.p, u_stride, co.p, us.p, nullptr);
+    if (e != cudaSuccess)
+        return cudaFail(e, "rayleigh kernel");
+    std::vector<float> b(n);
+    DXMCG_CUDA(cudaMemcpy(b.data(), co.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(used, us.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i)
+        cos_out[i] = b[i];
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_sample_source(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts, int n,
+    double* out8)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "sample_source: world not built");
+    if (!beam || n < 0 || !out8)
+        return fail(DXMCG_ERR_ARGUMENT, "sample_source: bad arguments");
+    dxmcg_run_options o {};
+    o.seed = 1;
+    if (opts)
+        o = *opts;
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    DevJob J;
+    uint64_t nHist = 0;
+    int rc = prepareJob(w, *beam, o, J, nHist);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (o.hist_begin + static_cast<uint64_t>(n) > nHist)
+        return fail(DXMCG_ERR_ARGUMENT, "sample_source: history range beyond the beam");
+    if (n == 0)
+        return DXMCG_OK;
+    DeviceBuffer<float> out;
+    DXMCG_CUDA(out.alloc(8 * static_cast<size_t>(n)));
+    cudaError_t e = launchSampleSource(J, o.hist_begin, n, out.p, w->stream);
+    if (e != cudaSuccess)
+        return cudaFail(e, "source kernel");
+    std::vector<float> h(8 * static_cast<size_t>(n));
+    DXMCG_CUDA(cudaMemcpyAsync(h.data(), out.p, h.size() * sizeof(float), cudaMemcpyDeviceToHost, w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    for (size_t i = 0; i < h.size(); ++i)
+        out8[i] = h[i];
+    return DXMCG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,136 @@
+// engine.hpp -- device data layout and kernel launchers shared by the host
+// library (capi.cpp) and the kernels (transport.cu).
+//
+// HBM layout of one world (N = nx*ny*nz voxels):
+//   vox    uint32[N]   density with the low 8 mantissa bits replaced by the
+//                      material index (one 4-byte gather per voxel visit;
+//                      density keeps 16 significant bits, |rel. rounding| <= 2^-16)
+//   tally  Tally[N]    {energy, energy^2, events} in one 32-byte sector
+//   tot    float[M][NE]        total mass attenuation per material (cm^2/g)
+//   xs     float4[M][NE]       (photo, incoherent, coherent, total)
+//   maj    float[NE]           majorant mu_max(E) over the grid (1/cm)
+//   mats   DevMaterial[M]      per-element sampling data
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/dxmcg.h"
+
+namespace dxmcg {
+
+constexpr int kMaxSpectrum = 512;
+constexpr int kMaxBowtie = 64;
+constexpr int kTableNE = DXMCG_NE;
+constexpr uint32_t kMaxStepsPerHistory = 1000000;
+constexpr int kMaxRejections = 100000;
+
+struct DevMaterial {
+    int n;
+    float Zsum;
+    float nZ[DXMCG_MAX_ELEMENTS];
+    float nZ2[DXMCG_MAX_ELEMENTS];
+    float a[DXMCG_MAX_ELEMENTS];
+};
+
+struct alignas(16) DevExposure {
+    float pos[3]; // grid-local cm
+    float c0[3];
+    float c1[3];
+    float n[3];   // c0 x c1
+    float half[2];
+    float weight;
+    int tube;
+};
+
+struct DevSpectrum {
+    int n;
+    float E[kMaxSpectrum];
+    uint32_t thr[kMaxSpectrum];
+    int32_t alias[kMaxSpectrum];
+};
+
+struct DevBowtie {
+    int n;
+    float ang[kMaxBowtie];
+    float w[kMaxBowtie];
+    float inv_norm[2];
+};
+
+struct alignas(32) Tally {
+    double e;
+    double e2;
+    unsigned long long n;
+    unsigned long long pad;
+};
+
+struct DevJob {
+    // world
+    const uint32_t* vox;
+    int nx, ny, nz;
+    float sp[3];
+    float isp[3];
+    float L[3];
+    float Lin[3]; // largest float strictly below L
+    const float* tot;
+    const float4* xs;
+    const float* maj;
+    const DevMaterial* mats;
+    int n_mats;
+    int correction;
+    Tally* tally;
+    // source
+    const DevExposure* exps;
+    int n_exp;
+    unsigned long long ppe;
+    const DevSpectrum* spec; // [2]
+    const DevBowtie* bowtie; // nullptr: none
+    int beam_type;
+    float pencil_energy;
+    uint32_t key0, key1, stream;
+    int tracking;
+};
+
+struct DevCounters {
+    unsigned long long next; // work-queue head (history index)
+    unsigned long long histories, missed, visits, photo, compton, rayleigh, cutoff, errors, interacted;
+    double e_source, e_escaped, e_deposited;
+    unsigned int error_flags;
+};
+
+enum ErrorFlag : unsigned {
+    kErrStepLimit = 1u,
+    kErrRejectLimit = 2u,
+    kErrBadDensity = 4u,
+    kErrBadMaterial = 8u,
+};
+
+struct LaunchShape {
+    int grid = 0;
+    int block = 256;
+};
+
+// kernels (transport.cu)
+cudaError_t launchPack(const double* dens64, const float* dens32, const uint8_t* mat, uint32_t* vox, size_t n,
+    int n_mats, unsigned* rho_max_bits, unsigned* err, cudaStream_t s);
+cudaError_t launchTransport(const DevJob& job, unsigned long long h_end, DevCounters* ctr, LaunchShape shape,
+    cudaStream_t s);
+cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, double energy_to_dose,
+    double n_histories, double* dose, double* var, unsigned long long* count, cudaStream_t s);
+cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int ny, int nz, float sx, float sy,
+    float sz, int cap, long long* idx, float* len, int* cnt, cudaStream_t s);
+cudaError_t launchPhilox(int n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t s);
+cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, int correction, const float* u,
+    int stride, float* e_out, float* cos_out, int* used, cudaStream_t s);
+cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* u, int stride,
+    float* cos_out, int* used, cudaStream_t s);
+cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s);
+int transportRegistersPerThread();
+
+// host helpers (geometry.cpp)
+int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out);
+
+} // namespace dxmcg

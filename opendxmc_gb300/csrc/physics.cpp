@@ -1,0 +1,337 @@
+// physics.cpp -- host FP64 physics model, see physics.hpp.
+#include "physics.hpp"
+
+#include <algorithm>
+#include <cmath>
+
+namespace dxmcg {
+namespace {
+    constexpr double kPi = 3.14159265358979323846;
+    constexpr double kRe2Barn = 0.0794077878;   // r_e^2 in barn
+    constexpr double kMeKeV = 510.99895;
+    constexpr double kAvogadro = 6.02214076e23;
+    constexpr double kHcKeVA = 12.398419843;    // keV * Angstrom
+    constexpr double kBohrA = 0.529177210903;
+    constexpr double kRydKeV = 13.605693122994e-3;
+    constexpr double kPhotoC = 30.0;            // barn keV^3
+    constexpr double kJumpK = 7.0;
+    constexpr double kJumpL = 3.0;
+    constexpr int kQuad = 1024;                 // Simpson panels over the scattering angle
+
+    // IUPAC abridged standard atomic weights, Z = 1..92.
+    constexpr std::array<double, 93> kAtomicMass = { 0.0, 1.008, 4.0026, 6.94, 9.0122, 10.81, 12.011, 14.007,
+        15.999, 18.998, 20.180, 22.990, 24.305, 26.982, 28.085, 30.974, 32.06, 35.45, 39.948, 39.098, 40.078,
+        44.956, 47.867, 50.942, 51.996, 54.938, 55.845, 58.933, 58.693, 63.546, 65.38, 69.723, 72.630, 74.922,
+        78.971, 79.904, 83.798, 85.468, 87.62, 88.906, 91.224, 92.906, 95.95, 98.0, 101.07, 102.91, 106.42,
+        107.87, 112.41, 114.82, 118.71, 121.76, 127.60, 126.90, 131.29, 132.91, 137.33, 138.91, 140.12, 140.91,
+        144.24, 145.0, 150.36, 151.96, 157.25, 158.93, 162.50, 164.93, 167.26, 168.93, 173.05, 174.97, 178.49,
+        180.95, 183.84, 186.21, 190.23, 192.22, 195.08, 196.97, 200.59, 204.38, 207.2, 208.98, 209.0, 210.0,
+        222.0, 223.0, 226.0, 227.0, 232.04, 231.04, 238.03 };
+
+    double simpsonWeight(int i)
+    {
+        if (i == 0 || i == kQuad)
+            return 1.0;
+        return (i & 1) ? 4.0 : 2.0;
+    }
+
+    // Klein-Nishina differential cross-section (barn/sr per electron).
+    double kleinNishinaDifferential(double k, double mu)
+    {
+        const double eps = 1.0 / (1.0 + k * (1.0 - mu));
+        return 0.5 * kRe2Barn * eps * eps * (eps + 1.0 / eps - (1.0 - mu * mu));
+    }
+
+    std::array<double, DXMCG_MAX_ELEMENTS> normalisedWeights(const dxmcg_material& m)
+    {
+        std::array<double, DXMCG_MAX_ELEMENTS> w {};
+        double s = 0;
+        for (int i = 0; i < m.n; ++i)
+            s += m.w[i];
+        for (int i = 0; i < m.n; ++i)
+            w[i] = s > 0 ? m.w[i] / s : 0.0;
+        return w;
+    }
+} // namespace
+
+namespace phys {
+    double atomicMass(int Z) { return (Z >= 1 && Z <= 92) ? kAtomicMass[Z] : 0.0; }
+
+    double elementDensity(int Z)
+    {
+        switch (Z) {
+        case 4: return 1.848;
+        case 13: return 2.699;
+        case 29: return 8.96;
+        case 42: return 10.22;
+        case 45: return 12.41;
+        case 47: return 10.49;
+        case 50: return 7.31;
+        case 64: return 7.90;
+        case 68: return 9.07;
+        case 73: return 16.65;
+        case 74: return 19.30;
+        case 79: return 19.32;
+        case 82: return 11.35;
+        default: return 0.0;
+        }
+    }
+
+    double formFactorScale(int Z)
+    {
+        const double x = std::cbrt(static_cast<double>(Z)) / (2.0 * kPi * kBohrA);
+        return x * x;
+    }
+
+    double kleinNishinaTotal(double E)
+    {
+        const double k = E / kMeKeV;
+        const double l = std::log1p(2.0 * k);
+        const double a = (1.0 + k) / (k * k) * (2.0 * (1.0 + k) / (1.0 + 2.0 * k) - l / k);
+        const double b = l / (2.0 * k);
+        const double c = (1.0 + 3.0 * k) / ((1.0 + 2.0 * k) * (1.0 + 2.0 * k));
+        return 2.0 * kPi * kRe2Barn * (a + b - c);
+    }
+
+    double photoelectric(double E, int Z)
+    {
+        const double z2 = static_cast<double>(Z) * Z;
+        double s = kPhotoC * z2 * z2 / (E * E * E);
+        const double edgeK = kRydKeV * (Z - 1.0) * (Z - 1.0);
+        const double edgeL = Z > 7 ? kRydKeV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0;
+        if (E < edgeK)
+            s /= kJumpK;
+        if (E < edgeL)
+            s /= kJumpL;
+        return s;
+    }
+
+    // Angular integrals use t = x^2 = T (1 - mu) / 2 mapped to s in [0, 1] by t = a (B^s - 1),
+    // B = 1 + T / a, which resolves the forward peak of F^2 and the rise of S.
+    double incoherent(double E, int Z, int correction)
+    {
+        if (correction <= 0)
+            return Z * kleinNishinaTotal(E);
+        const double k = E / kMeKeV;
+        const double T = (E / kHcKeVA) * (E / kHcKeVA);
+        const double a = formFactorScale(Z);
+        const double L = std::log1p(T / a);
+        double acc = 0;
+        for (int i = 0; i <= kQuad; ++i) {
+            const double s = static_cast<double>(i) / kQuad;
+            const double t = a * std::expm1(s * L);
+            const double mu = 1.0 - 2.0 * t / T;
+            const double S = Z * (-std::expm1(-4.0 * s * L));
+            acc += simpsonWeight(i) * kleinNishinaDifferential(k, mu) * S * a * L * std::exp(s * L);
+        }
+        acc *= 1.0 / (3.0 * kQuad);
+        return 2.0 * kPi * (2.0 / T) * acc;
+    }
+
+    double coherent(double E, int Z)
+    {
+        const double T = (E / kHcKeVA) * (E / kHcKeVA);
+        const double a = formFactorScale(Z);
+        const double L = std::log1p(T / a);
+        double acc = 0;
+        for (int i = 0; i <= kQuad; ++i) {
+            const double s = static_cast<double>(i) / kQuad;
+            const double t = a * std::expm1(s * L);
+            const double mu = 1.0 - 2.0 * t / T;
+            acc += simpsonWeight(i) * (1.0 + mu * mu) * a * L * std::exp(-3.0 * s * L);
+        }
+        acc *= 1.0 / (3.0 * kQuad);
+        return kPi * kRe2Barn * (2.0 / T) * static_cast<double>(Z) * Z * acc;
+    }
+
+    double knEnergyTransferFraction(double E)
+    {
+        const double k = E / kMeKeV;
+        double num = 0, den = 0;
+        for (int i = 0; i <= kQuad; ++i) {
+            const double mu = -1.0 + 2.0 * static_cast<double>(i) / kQuad;
+            const double eps = 1.0 / (1.0 + k * (1.0 - mu));
+            const double d = kleinNishinaDifferential(k, mu) * simpsonWeight(i);
+            num += d * (1.0 - eps);
+            den += d;
+        }
+        return num / den;
+    }
+} // namespace phys
+
+bool validComposition(const dxmcg_material& m)
+{
+    if (m.n < 1 || m.n > DXMCG_MAX_ELEMENTS)
+        return false;
+    double s = 0;
+    for (int i = 0; i < m.n; ++i) {
+        if (m.Z[i] < 1 || m.Z[i] > 92 || !(m.w[i] >= 0.0) || !std::isfinite(m.w[i]))
+            return false;
+        s += m.w[i];
+    }
+    return s > 0;
+}
+
+Attenuation attenuation(const dxmcg_material& m, int correction, double E)
+{
+    const auto w = normalisedWeights(m);
+    Attenuation a;
+    for (int i = 0; i < m.n; ++i) {
+        const int Z = m.Z[i];
+        const double f = w[i] * kAvogadro / phys::atomicMass(Z) * 1e-24;
+        a.photo += f * phys::photoelectric(E, Z);
+        a.incoherent += f * phys::incoherent(E, Z, correction);
+        a.coherent += f * phys::coherent(E, Z);
+    }
+    return a;
+}
+
+SamplingElements samplingElements(const dxmcg_material& m)
+{
+    const auto w = normalisedWeights(m);
+    SamplingElements s;
+    s.n = m.n;
+    for (int i = 0; i < m.n; ++i) {
+        const double ni = w[i] / phys::atomicMass(m.Z[i]);
+        s.nZ[i] = ni * m.Z[i];
+        s.nZ2[i] = ni * m.Z[i] * m.Z[i];
+        s.a[i] = phys::formFactorScale(m.Z[i]);
+        s.Zsum += s.nZ[i];
+    }
+    return s;
+}
+
+namespace {
+    constexpr double kTungstenKEdge = 69.525;
+    constexpr std::array<double, 4> kTungstenLines = { 57.981, 59.318, 67.244, 69.067 };
+    constexpr std::array<double, 4> kTungstenLineShare = { 0.27, 0.47, 0.18, 0.08 };
+    constexpr double kCharacteristicYield = 0.1;
+
+    double elementTotal(int Z, double E)
+    {
+        dxmcg_material m {};
+        m.n = 1;
+        m.Z[0] = Z;
+        m.w[0] = 1.0;
+        return attenuation(m, 1, E).sum();
+    }
+} // namespace
+
+Spectrum tubeSpectrum(double kvp, double /*anode_angle_deg*/, int n_filters, const int32_t* Z, const double* mm)
+{
+    Spectrum s;
+    const int n = static_cast<int>(std::floor(kvp));
+    if (n < 1 || n > 511)
+        return s;
+    s.energy.resize(n);
+    s.weight.resize(n);
+    double total = 0;
+    for (int k = 0; k < n; ++k) {
+        s.energy[k] = k + 1.0;
+        s.weight[k] = (kvp - s.energy[k]) / s.energy[k]; // Kramers
+        total += s.weight[k];
+    }
+    if (kvp > kTungstenKEdge) {
+        const double lines = kCharacteristicYield * std::pow(kvp / kTungstenKEdge - 1.0, 1.63) * total;
+        for (int l = 0; l < 4; ++l) {
+            const int bin = static_cast<int>(std::floor(kTungstenLines[l] + 0.5)) - 1;
+            if (bin >= 0 && bin < n)
+                s.weight[bin] += lines * kTungstenLineShare[l];
+        }
+    }
+    for (int f = 0; f < n_filters; ++f) {
+        const double rho = phys::elementDensity(Z[f]);
+        if (rho <= 0 || mm[f] <= 0)
+            continue;
+        for (int k = 0; k < n; ++k)
+            s.weight[k] *= std::exp(-elementTotal(Z[f], s.energy[k]) * rho * mm[f] * 0.1);
+    }
+    double sum = 0;
+    for (double w : s.weight)
+        sum += w;
+    for (double& w : s.weight)
+        w = sum > 0 ? w / sum : 0.0;
+    return s;
+}
+
+double tubeMeanEnergy(const Spectrum& s)
+{
+    double m = 0;
+    for (size_t k = 0; k < s.energy.size(); ++k)
+        m += s.energy[k] * s.weight[k];
+    return m;
+}
+
+double airEnergyAbsorption(double E)
+{
+    dxmcg_material air {};
+    air.n = 3;
+    air.Z[0] = 7;
+    air.Z[1] = 8;
+    air.Z[2] = 18;
+    air.w[0] = 0.755;
+    air.w[1] = 0.232;
+    air.w[2] = 0.013;
+    const auto a = attenuation(air, 1, E);
+    return a.photo + a.incoherent * phys::knEnergyTransferFraction(E);
+}
+
+double tubeAlHalfValueLayer(const Spectrum& s)
+{
+    const size_t n = s.energy.size();
+    if (n == 0)
+        return 0.0;
+    std::vector<double> kerma(n), mu(n);
+    double k0 = 0;
+    for (size_t k = 0; k < n; ++k) {
+        kerma[k] = s.weight[k] * s.energy[k] * airEnergyAbsorption(s.energy[k]);
+        mu[k] = elementTotal(13, s.energy[k]) * phys::elementDensity(13) * 0.1;
+        k0 += kerma[k];
+    }
+    double lo = 0, hi = 100;
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        double t = 0;
+        for (size_t k = 0; k < n; ++k)
+            t += kerma[k] * std::exp(-mu[k] * mid);
+        (t > 0.5 * k0 ? lo : hi) = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+// Vose's construction of Walker's alias table.
+AliasTable buildAlias(const Spectrum& s)
+{
+    const int n = static_cast<int>(s.weight.size());
+    AliasTable t;
+    t.energy.resize(n);
+    t.threshold.resize(n);
+    t.alias.resize(n);
+    std::vector<double> p(n), prob(n, 1.0);
+    std::vector<int> small, large;
+    double sum = 0;
+    for (double w : s.weight)
+        sum += w;
+    for (int i = 0; i < n; ++i) {
+        p[i] = s.weight[i] / sum * n;
+        t.alias[i] = i;
+        t.energy[i] = static_cast<float>(s.energy[i]);
+    }
+    for (int i = 0; i < n; ++i)
+        (p[i] < 1.0 ? small : large).push_back(i);
+    while (!small.empty() && !large.empty()) {
+        const int l = small.back();
+        small.pop_back();
+        const int g = large.back();
+        large.pop_back();
+        prob[l] = p[l];
+        t.alias[l] = g;
+        p[g] = (p[g] + p[l]) - 1.0;
+        (p[g] < 1.0 ? small : large).push_back(g);
+    }
+    for (int i = 0; i < n; ++i)
+        t.threshold[i] = static_cast<uint32_t>(std::floor(prob[i] * 8388608.0 + 0.5));
+    return t;
+}
+
+} // namespace dxmcg

@@ -1,0 +1,267 @@
+"""Thin Python handle over the C ABI: a built voxel world on the GPU plus runs.
+
+This is what the tests and the benchmark drive; the dxmc-style mirror classes in
+`opendxmc_gb300.api` are built on it.  Every call goes through libdxmcg.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import native as N
+
+
+def device_count() -> int:
+    return int(N.lib().dxmcg_device_count())
+
+
+def set_device(device: int) -> None:
+    N.check(N.lib().dxmcg_set_device(device))
+
+
+def attenuation(zw: dict, energies, correction: int = 1):
+    E = np.ascontiguousarray(energies, dtype=np.float64)
+    p, ic, co = (np.zeros_like(E) for _ in range(3))
+    m = N.Material.from_dict(zw)
+    N.check(N.lib().dxmcg_material_attenuation(C.byref(m), correction, E.size, N.ptr(E, C.c_double),
+                                               N.ptr(p, C.c_double), N.ptr(ic, C.c_double), N.ptr(co, C.c_double)))
+    return p, ic, co
+
+
+def _filters(filters: dict):
+    fz = (C.c_int32 * 8)()
+    fm = (C.c_double * 8)()
+    for k, (z, mm) in enumerate(filters.items()):
+        fz[k] = int(z)
+        fm[k] = float(mm)
+    return len(filters), fz, fm
+
+
+def tube_spectrum(kvp: float, filters: dict, anode_angle_deg: float = 12.0):
+    n_out = C.c_int(0)
+    n, fz, fm = _filters(filters)
+    N.check(N.lib().dxmcg_tube_spectrum(kvp, anode_angle_deg, n, fz, fm, None, None, 0, C.byref(n_out)))
+    E = np.zeros(n_out.value)
+    w = np.zeros(n_out.value)
+    N.check(N.lib().dxmcg_tube_spectrum(kvp, anode_angle_deg, n, fz, fm, N.ptr(E, C.c_double), N.ptr(w, C.c_double),
+                                        E.size, C.byref(n_out)))
+    return E, w
+
+
+def tube_mean_energy(kvp: float, filters: dict) -> float:
+    n, fz, fm = _filters(filters)
+    out = C.c_double(0)
+    N.check(N.lib().dxmcg_tube_mean_energy(kvp, n, fz, fm, C.byref(out)))
+    return out.value
+
+
+def tube_al_hvl(kvp: float, filters: dict) -> float:
+    n, fz, fm = _filters(filters)
+    out = C.c_double(0)
+    N.check(N.lib().dxmcg_tube_al_hvl(kvp, n, fz, fm, C.byref(out)))
+    return out.value
+
+
+def beam_exposures(params: dict) -> list[dict]:
+    b, keep = N.make_beam(params)
+    n = C.c_int(0)
+    N.check(N.lib().dxmcg_beam_exposures(C.byref(b), None, 0, C.byref(n)))
+    arr = (N.Exposure * max(n.value, 1))()
+    N.check(N.lib().dxmcg_beam_exposures(C.byref(b), arr, n.value, C.byref(n)))
+    return [{"pos": list(e.pos), "c0": list(e.c0), "c1": list(e.c1), "half": list(e.half), "weight": e.weight,
+             "tube": e.tube} for e in arr[:n.value]]
+
+
+def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_size=0, blocks_per_sm=0,
+                chunk_log2=0, hist_begin=0, hist_end=0) -> N.RunOptions:
+    o = N.RunOptions()
+    o.seed = seed
+    o.stream = stream
+    o.tracking = tracking
+    o.normalize = normalize
+    o.block_size = block_size
+    o.blocks_per_sm = blocks_per_sm
+    o.chunk_histories_log2 = chunk_log2
+    o.hist_begin = hist_begin
+    o.hist_end = hist_end
+    return o
+
+
+class Progress:
+    """TransportProgress mirror over dxmcg_progress (thread-safe in the library)."""
+
+    def __init__(self):
+        self._h = N.lib().dxmcg_progress_create()
+
+    def progress(self) -> tuple[int, int]:
+        d = C.c_uint64(0)
+        t = C.c_uint64(0)
+        N.lib().dxmcg_progress_get(self._h, C.byref(d), C.byref(t))
+        return d.value, t.value
+
+    def message(self) -> str:
+        buf = C.create_string_buffer(256)
+        N.lib().dxmcg_progress_message(self._h, buf, 256)
+        return buf.value.decode()
+
+    def continueSimulation(self) -> bool:
+        return bool(N.lib().dxmcg_progress_continue(self._h))
+
+    def setStopSimulation(self) -> None:
+        N.lib().dxmcg_progress_stop(self._h)
+
+    def __del__(self):
+        try:
+            if self._h:
+                N.lib().dxmcg_progress_destroy(self._h)
+        except Exception:
+            pass
+
+
+class GpuWorld:
+    """A voxel world resident on the GPU (World<AAVoxelGrid> after build())."""
+
+    def __init__(self, dims, spacing_cm, materials: list[dict], correction: int = 1):
+        self.dims = tuple(int(x) for x in dims)
+        self.N = int(np.prod(self.dims))
+        d = np.ascontiguousarray(self.dims, dtype=np.int32)
+        s = np.ascontiguousarray(spacing_cm, dtype=np.float64)
+        mats = (N.Material * len(materials))(*[N.Material.from_dict(m) for m in materials])
+        h = C.c_void_p()
+        N.check(N.lib().dxmcg_world_create(N.ptr(d, C.c_int32), N.ptr(s, C.c_double), mats, len(materials),
+                                           correction, C.byref(h)))
+        self._h = h
+
+    def set_data(self, density: np.ndarray, material: np.ndarray) -> None:
+        m = np.ascontiguousarray(material, dtype=np.uint8).reshape(-1)
+        if m.size != self.N or density.size != self.N:
+            raise ValueError("array size does not match dimensions")
+        if density.dtype == np.float32:
+            dd = np.ascontiguousarray(density).reshape(-1)
+            N.check(N.lib().dxmcg_world_set_data_f32(self._h, N.ptr(dd, C.c_float), N.ptr(m, C.c_uint8)))
+        else:
+            dd = np.ascontiguousarray(density, dtype=np.float64).reshape(-1)
+            N.check(N.lib().dxmcg_world_set_data(self._h, N.ptr(dd, C.c_double), N.ptr(m, C.c_uint8)))
+
+    def build(self) -> None:
+        N.check(N.lib().dxmcg_world_build(self._h))
+
+    def run(self, beam: dict, options: N.RunOptions | None = None, progress: Progress | None = None) -> dict:
+        b, keep = N.make_beam(beam)
+        st = N.Stats()
+        opts = options if options is not None else run_options()
+        rc = N.lib().dxmcg_transport_run(self._h, C.byref(b), C.byref(opts), progress._h if progress else None,
+                                         C.byref(st))
+        N.check(rc)
+        return st.as_dict()
+
+    def run_status(self, beam: dict, options=None, progress=None) -> tuple[int, dict]:
+        b, keep = N.make_beam(beam)
+        st = N.Stats()
+        opts = options if options is not None else run_options()
+        rc = N.lib().dxmcg_transport_run(self._h, C.byref(b), C.byref(opts), progress._h if progress else None,
+                                         C.byref(st))
+        return rc, st.as_dict()
+
+    def clear(self) -> None:
+        N.check(N.lib().dxmcg_world_clear_tally(self._h))
+
+    def tally(self):
+        e = np.zeros(self.N)
+        e2 = np.zeros(self.N)
+        c = np.zeros(self.N, dtype=np.uint64)
+        N.check(N.lib().dxmcg_world_read_tally(self._h, N.ptr(e, C.c_double), N.ptr(e2, C.c_double),
+                                               N.ptr(c, C.c_uint64)))
+        return e, e2, c
+
+    def dose(self, out=None):
+        """(dose mGy, variance, events) per voxel; `out` may supply the three arrays
+        (e.g. pinned host memory)."""
+        if out is not None:
+            d, v, c = out
+        else:
+            d = np.zeros(self.N)
+            v = np.zeros(self.N)
+            c = np.zeros(self.N, dtype=np.uint64)
+        N.check(N.lib().dxmcg_world_read_dose(self._h, N.ptr(d, C.c_double), N.ptr(v, C.c_double),
+                                              N.ptr(c, C.c_uint64)))
+        return d, v, c
+
+    def tables(self, material: int):
+        xs = np.zeros((N.NE, 4), dtype=np.float32)
+        mj = np.zeros(N.NE, dtype=np.float32)
+        N.check(N.lib().dxmcg_world_tables(self._h, material, N.ptr(xs, C.c_float), N.ptr(mj, C.c_float)))
+        return xs, mj
+
+    def packed_density(self):
+        d = np.zeros(self.N, dtype=np.float32)
+        m = np.zeros(self.N, dtype=np.uint8)
+        N.check(N.lib().dxmcg_world_packed_density(self._h, N.ptr(d, C.c_float), N.ptr(m, C.c_uint8)))
+        return d, m
+
+    def sample_source(self, beam: dict, n: int, options=None) -> np.ndarray:
+        b, keep = N.make_beam(beam)
+        out = np.zeros((n, 8))
+        opts = options if options is not None else run_options()
+        N.check(N.lib().dxmcg_sample_source(self._h, C.byref(b), C.byref(opts), n, N.ptr(out, C.c_double)))
+        return out
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().dxmcg_world_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def siddon_trace(origins, directions, dims, spacing, cap=4096):
+    o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(directions, dtype=np.float32).reshape(-1, 3)
+    n = o.shape[0]
+    dm = np.ascontiguousarray(dims, dtype=np.int32)
+    sp = np.ascontiguousarray(spacing, dtype=np.float32)
+    idx = np.zeros((n, cap), dtype=np.int64)
+    ln = np.zeros((n, cap), dtype=np.float32)
+    cnt = np.zeros(n, dtype=np.int32)
+    N.check(N.lib().dxmcg_siddon_trace(n, N.ptr(o, C.c_float), N.ptr(d, C.c_float), N.ptr(dm, C.c_int32),
+                                       N.ptr(sp, C.c_float), cap, N.ptr(idx, C.c_int64), N.ptr(ln, C.c_float),
+                                       N.ptr(cnt, C.c_int32)))
+    return [(idx[r, :cnt[r]].copy(), ln[r, :cnt[r]].copy()) for r in range(n)]
+
+
+def philox(counters, key):
+    c = np.ascontiguousarray(counters, dtype=np.uint32).reshape(-1, 4)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros_like(c)
+    N.check(N.lib().dxmcg_philox(c.shape[0], N.ptr(c, C.c_uint32), N.ptr(k, C.c_uint32), N.ptr(out, C.c_uint32)))
+    return out
+
+
+def sample_compton(energies, zw, correction, uniforms):
+    E = np.ascontiguousarray(energies, dtype=np.float64)
+    U = np.ascontiguousarray(uniforms, dtype=np.float64)
+    n, stride = U.shape
+    eo = np.zeros(n)
+    co = np.zeros(n)
+    used = np.zeros(n, dtype=np.int32)
+    m = N.Material.from_dict(zw)
+    N.check(N.lib().dxmcg_sample_compton(n, N.ptr(E, C.c_double), C.byref(m), correction, N.ptr(U, C.c_double), stride,
+                                         N.ptr(eo, C.c_double), N.ptr(co, C.c_double), N.ptr(used, C.c_int32)))
+    return eo, co, used
+
+
+def sample_rayleigh(energies, zw, uniforms):
+    E = np.ascontiguousarray(energies, dtype=np.float64)
+    U = np.ascontiguousarray(uniforms, dtype=np.float64)
+    n, stride = U.shape
+    co = np.zeros(n)
+    used = np.zeros(n, dtype=np.int32)
+    m = N.Material.from_dict(zw)
+    N.check(N.lib().dxmcg_sample_rayleigh(n, N.ptr(E, C.c_double), C.byref(m), N.ptr(U, C.c_double), stride,
+                                          N.ptr(co, C.c_double), N.ptr(used, C.c_int32)))
+    return co, used

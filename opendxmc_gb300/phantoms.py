@@ -1,0 +1,171 @@
+"""Seeded synthetic phantoms and the tissue compositions they use.
+
+Compositions are mass percentages per element (Z -> %), the rows of the ICRP
+adult-male media table OpenDXMC ships (data/phantoms/icrp/AM/AM_media.dat) and
+of data/phantoms/other/media.dat; the line of each row is cited.  Arrays are
+returned in the AAVoxelGrid layout: shape (nz, ny, nx), x fastest, grid centred
+on the origin, spacing in cm.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+AIR = {7: 80.0, 8: 20.0}  # AM_media.dat:56 "Air"
+LUNG = {1: 10.3, 6: 10.7, 7: 3.2, 8: 74.6, 11: 0.2, 15: 0.2, 16: 0.3, 17: 0.3, 19: 0.2}  # AM_media.dat:53
+ADIPOSE = {1: 11.4, 6: 58.8, 7: 0.8, 8: 28.7, 11: 0.1, 16: 0.1, 17: 0.1}  # AM_media.dat:52
+SOFT_TISSUE = {1: 10.4, 6: 23.1, 7: 2.8, 8: 62.7, 11: 0.1, 15: 0.2, 16: 0.3, 17: 0.2, 19: 0.2}  # AM_media.dat:48
+MUSCLE = {1: 10.2, 6: 14.2, 7: 3.4, 8: 71.1, 11: 0.1, 15: 0.2, 16: 0.3, 17: 0.1, 19: 0.4}  # AM_media.dat:32
+BONE = {1: 3.6, 6: 15.9, 7: 4.2, 8: 44.8, 11: 0.3, 12: 0.2, 15: 9.4, 16: 0.3, 20: 21.3}  # AM_media.dat:5
+WATER = {1: 11.2, 8: 88.8}  # other/media.dat:56
+
+# the six-material set: (name, composition, nominal density g/cm3)
+SIX_MATERIALS = [
+    ("air", AIR, 0.0012),
+    ("lung", LUNG, 0.26),
+    ("adipose", ADIPOSE, 0.95),
+    ("soft_tissue", SOFT_TISSUE, 1.03),
+    ("muscle", MUSCLE, 1.05),
+    ("bone", BONE, 1.92),
+]
+
+
+@dataclass
+class Phantom:
+    dims: tuple  # (nx, ny, nz)
+    spacing: tuple  # cm
+    density: np.ndarray  # float64 (nz, ny, nx)
+    material: np.ndarray  # uint8 (nz, ny, nx)
+    materials: list  # list of {Z: weight}
+    names: list = field(default_factory=list)
+
+    @property
+    def n_voxels(self) -> int:
+        return int(np.prod(self.dims))
+
+
+def _axes(dims, spacing):
+    nx, ny, nz = dims
+    sx, sy, sz = spacing
+    x = (np.arange(nx) + 0.5) * sx - 0.5 * nx * sx
+    y = (np.arange(ny) + 0.5) * sy - 0.5 * ny * sy
+    z = (np.arange(nz) + 0.5) * sz - 0.5 * nz * sz
+    return x, y, z
+
+
+def water_cylinder_phantom(dims=(128, 128, 64), spacing=(0.1, 0.1, 0.25)) -> Phantom:
+    """Air (0.0012) holding a water cylinder, 16 cm diameter and 15 cm long along z,
+    with a 3 cm diameter bone insert (1.92 g/cm3) centred 4 cm off axis."""
+    x, y, z = _axes(dims, spacing)
+    X, Y = np.meshgrid(x, y)  # (ny, nx)
+    in_z = np.abs(z) <= 7.5
+    cyl = X ** 2 + Y ** 2 <= 8.0 ** 2
+    ins = (X - 4.0) ** 2 + Y ** 2 <= 1.5 ** 2
+    mat2d = np.where(ins, 2, np.where(cyl, 1, 0)).astype(np.uint8)
+    material = np.where(in_z[:, None, None], mat2d[None], 0).astype(np.uint8)
+    dens_of = np.array([0.0012, 1.0, 1.92])
+    density = dens_of[material]
+    return Phantom(tuple(dims), tuple(spacing), density, material, [AIR, WATER, BONE], ["air", "water", "bone"])
+
+
+def torso_phantom(dims=(256, 256, 200), spacing=(0.15, 0.15, 0.15), seed=1, jitter=0.02) -> Phantom:
+    """Seeded nested-ellipsoid torso in the six materials (air, lung, adipose, soft
+    tissue, muscle, bone), density x U(1 - jitter, 1 + jitter) per voxel."""
+    rng = np.random.default_rng(seed)
+    x, y, z = _axes(dims, spacing)
+    nx, ny, nz = dims
+
+    def perturb(c, a, dc=0.4, da=0.05):
+        c = np.asarray(c, float) + rng.normal(0, dc, 3)
+        a = np.asarray(a, float) * rng.uniform(1 - da, 1 + da, 3)
+        return c, a
+
+    # (material index, centre, semi-axes); later entries overwrite earlier ones
+    shapes = [
+        (2, *perturb((0, 0, 0), (15.0, 10.5, 1e4), dc=0.2)),      # body: adipose
+        (4, *perturb((0, 0, 0), (13.6, 9.2, 1e4), dc=0.2)),       # muscle wall
+        (3, *perturb((0, 0.3, 0), (12.4, 8.1, 1e4), dc=0.2)),     # visceral soft tissue
+        (1, *perturb((-6.0, 0.8, 5.0), (4.6, 5.8, 11.0))),        # lungs
+        (1, *perturb((6.0, 0.8, 5.0), (4.6, 5.8, 11.0))),
+        (4, *perturb((1.5, -0.5, 3.0), (4.0, 3.6, 5.0))),         # heart (muscle)
+        (3, *perturb((-4.0, 1.0, -7.0), (6.0, 4.5, 6.0))),        # liver-like soft tissue
+        (2, *perturb((3.0, 2.0, -9.0), (3.0, 2.5, 4.0))),         # abdominal fat
+        (5, *perturb((0, -6.8, 0), (1.7, 1.5, 1e4), dc=0.1)),     # spine
+        (5, *perturb((-8.5, -1.5, -12.0), (3.0, 4.0, 3.5))),      # pelvis
+        (5, *perturb((8.5, -1.5, -12.0), (3.0, 4.0, 3.5))),
+        (5, *perturb((0, 7.6, 6.0), (1.2, 0.7, 6.0))),            # sternum
+    ]
+    X, Y = np.meshgrid(x, y)  # (ny, nx)
+    material = np.zeros((nz, ny, nx), dtype=np.uint8)
+    for k in range(nz):
+        sl = np.zeros((ny, nx), dtype=np.uint8)
+        for m, c, a in shapes:
+            dz = (z[k] - c[2]) / a[2]
+            if dz * dz >= 1.0:
+                continue
+            inside = ((X - c[0]) / a[0]) ** 2 + ((Y - c[1]) / a[1]) ** 2 < 1.0 - dz * dz
+            if m == 1:  # lungs stay inside the visceral cavity
+                inside &= sl == 3
+            sl[inside] = m
+        material[k] = sl
+    nominal = np.array([d for _, _, d in SIX_MATERIALS])
+    density = nominal[material] * rng.uniform(1.0 - jitter, 1.0 + jitter, size=material.shape)
+    return Phantom(tuple(dims), tuple(spacing), density, material, [c for _, c, _ in SIX_MATERIALS],
+                   [n for n, _, _ in SIX_MATERIALS])
+
+
+# Body bowtie profile (angle rad, relative weight): "Siemens Definition Flash Body W3
+# 120kV", data/bowtiefilters/bowtiefilters.json.template:4-33.
+BODY_BOWTIE = [
+    (0.0, 1.8816799700821794),
+    (0.041992107, 1.7771629567485092),
+    (0.083836642, 1.4858913256035922),
+    (0.166511074, 0.7320820089981582),
+    (0.246954945, 0.47181213705409936),
+    (0.324269441, 0.35287338971480264),
+    (0.390607044, 0.2984982117986585),
+]
+
+
+def dx_beam_params(kvp=70.0, al_mm=2.5, field_cm=10.0, sid_cm=100.0, particles=1_000_000, exposures=10) -> dict:
+    """Planar DX beam as OpenDXMC's DXBeam sets it up at 0/0 degrees: source at
+    +y, c0 = +z, c1 = -x, beam along -y (dxmc_specialization.cpp:98-103, :155-167);
+    square field of `field_cm` at the isocentre distance, half-angles from
+    DXBeam::setCollimation (dxmc_specialization.cpp:123-129)."""
+    half = float(np.tan(0.5 * field_cm / sid_cm))
+    return {
+        "type": 0,
+        "kvp": kvp,
+        "anode_angle_deg": 12.0,
+        "filters": {13: al_mm},
+        "particles_per_exposure": particles,
+        "n_exposures": exposures,
+        "position": [0.0, sid_cm, 0.0],
+        "cosines": [[0.0, 0.0, 1.0], [-1.0, 0.0, 0.0]],
+        "half_angles": [half, half],
+    }
+
+
+def ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=1.0, collimation_cm=4.0, scan_cm=20.0, sdd_cm=119.0,
+                     fov_cm=50.0, step_deg=5.0, particles=1_000_000, bowtie=BODY_BOWTIE) -> dict:
+    """CTSpiralBeam with OpenDXMC's defaults (SDD 119 cm, 5 degree step;
+    beamsettingsmodel.cpp:1165-1169) over a centred scan range."""
+    p = {
+        "type": 1,
+        "kvp": kvp,
+        "anode_angle_deg": 12.0,
+        "filters": {13: al_mm},
+        "particles_per_exposure": particles,
+        "start": [0.0, 0.0, -0.5 * scan_cm],
+        "stop": [0.0, 0.0, 0.5 * scan_cm],
+        "start_angle_deg": 0.0,
+        "step_angle_deg": step_deg,
+        "pitch": pitch,
+        "collimation_cm": collimation_cm,
+        "scan_fov_cm": fov_cm,
+        "sdd_cm": sdd_cm,
+    }
+    if bowtie:
+        p["bowtie"] = list(bowtie)
+    return p

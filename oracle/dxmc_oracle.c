@@ -1,0 +1,1509 @@
+/*
+ * dxmc_oracle.c -- FP64 CPU restatement of the photon-transport hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker, never the product).  PARITY UNPINNED
+ * against DXMClib, which the reference does not contain (CMakeLists.txt:68-75);
+ * see dxmc_oracle.h for what each part restates.
+ *
+ * Build: oracle/Makefile (gcc -O2 -ffp-contract=off, no fast-math: the FP32
+ * Siddon restatement below must round exactly like the device traversal).
+ */
+#include "dxmc_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------------- */
+/* Physical constants                                                         */
+/* ------------------------------------------------------------------------- */
+#define PI 3.14159265358979323846
+#define R_E2_BARN 0.0794077878 /* classical electron radius squared, barn */
+#define ME_KEV 510.99895
+#define N_A 6.02214076e23
+#define HC_KEV_A 12.398419843 /* h c in keV * Angstrom */
+#define BOHR_A 0.529177210903
+#define RYD_KEV 13.605693122994e-3
+/* project-authored photoelectric model constants (see or_sigma_photo) */
+#define C_PE 30.0
+#define J_K 7.0
+#define J_L 3.0
+#define QUAD_N 1024
+#define E_CUT 1.0
+#define MAX_STEPS 1000000
+
+/* Standard atomic weights (g/mol), Z = 1..92 (IUPAC abridged values). */
+static const double ATOMIC_MASS[93] = { 0.0, 1.008, 4.0026, 6.94, 9.0122, 10.81, 12.011, 14.007,
+    15.999, 18.998, 20.180, 22.990, 24.305, 26.982, 28.085, 30.974, 32.06, 35.45, 39.948, 39.098,
+    40.078, 44.956, 47.867, 50.942, 51.996, 54.938, 55.845, 58.933, 58.693, 63.546, 65.38, 69.723,
+    72.630, 74.922, 78.971, 79.904, 83.798, 85.468, 87.62, 88.906, 91.224, 92.906, 95.95, 98.0,
+    101.07, 102.91, 106.42, 107.87, 112.41, 114.82, 118.71, 121.76, 127.60, 126.90, 131.29, 132.91,
+    137.33, 138.91, 140.12, 140.91, 144.24, 145.0, 150.36, 151.96, 157.25, 158.93, 162.50, 164.93,
+    167.26, 168.93, 173.05, 174.97, 178.49, 180.95, 183.84, 186.21, 190.23, 192.22, 195.08, 196.97,
+    200.59, 204.38, 207.2, 208.98, 209.0, 210.0, 222.0, 223.0, 226.0, 227.0, 232.04, 231.04,
+    238.03 };
+
+double or_atomic_mass(int Z) { return (Z >= 1 && Z <= 92) ? ATOMIC_MASS[Z] : 0.0; }
+
+/* Mass densities (g/cm3) of elements used as tube filters. */
+double or_element_density(int Z)
+{
+    switch (Z) {
+    case 4: return 1.848;
+    case 13: return 2.699;
+    case 29: return 8.96;
+    case 42: return 10.22;
+    case 45: return 12.41;
+    case 47: return 10.49;
+    case 50: return 7.31;
+    case 64: return 7.90;
+    case 68: return 9.07;
+    case 73: return 16.65;
+    case 74: return 19.30;
+    case 79: return 19.32;
+    case 82: return 11.35;
+    default: return 0.0;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Physics model (project-authored, parametric; DXMClib's Livermore tables are
+ * not available).  Per atom, in barn, E in keV.
+ *  - Compton: Klein-Nishina; with correction >= 1 (simulationwidget.cpp:71-73,
+ *    "Livermore") the differential cross-section is multiplied by the
+ *    incoherent scattering function S(x, Z).
+ *  - Rayleigh: Thomson cross-section times the atomic form factor F(x, Z)^2.
+ *  - F and S use one hydrogen-like orbital scaled by the Thomas-Fermi radius:
+ *    F = Z / (1 + x^2/a_Z)^2, S = Z (1 - (F/Z)^2), a_Z = (Z^(1/3) / (2 pi a0))^2,
+ *    x = sin(theta/2) / lambda in 1/Angstrom.
+ *  - Photoelectric: C_PE Z^4 / E^3 with K and L edges at Moseley energies
+ *    (Ryd (Z-1)^2 and Ryd (Z-7.4)^2 / 4) and jump ratios J_K, J_L.           */
+/* ------------------------------------------------------------------------- */
+static double a_Z(int Z)
+{
+    const double x = cbrt((double)Z) / (2.0 * PI * BOHR_A);
+    return x * x;
+}
+
+double or_sigma_kn(double E)
+{
+    const double k = E / ME_KEV;
+    const double l = log1p(2.0 * k);
+    const double a = (1.0 + k) / (k * k) * (2.0 * (1.0 + k) / (1.0 + 2.0 * k) - l / k);
+    const double b = l / (2.0 * k);
+    const double c = (1.0 + 3.0 * k) / ((1.0 + 2.0 * k) * (1.0 + 2.0 * k));
+    return 2.0 * PI * R_E2_BARN * (a + b - c);
+}
+
+/* Klein-Nishina d sigma / d Omega per electron (barn/sr) at cos(theta) = mu. */
+static double kn_dcs(double k, double mu)
+{
+    const double eps = 1.0 / (1.0 + k * (1.0 - mu));
+    return 0.5 * R_E2_BARN * eps * eps * (eps + 1.0 / eps - (1.0 - mu * mu));
+}
+
+double or_sigma_photo(double E, int Z)
+{
+    const double z2 = (double)Z * (double)Z;
+    double s = C_PE * z2 * z2 / (E * E * E);
+    const double ek = RYD_KEV * (Z - 1.0) * (Z - 1.0);
+    const double el = Z > 7 ? RYD_KEV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0;
+    if (E < ek)
+        s /= J_K;
+    if (E < el)
+        s /= J_L;
+    return s;
+}
+
+/* Integrals over the scattering angle use t = x^2 = t_max (1 - mu) / 2 mapped as
+ * t = a (B^s - 1), B = 1 + t_max / a, s in [0, 1], composite Simpson, QUAD_N panels. */
+static double simpson_weight(int i)
+{
+    if (i == 0 || i == QUAD_N)
+        return 1.0;
+    return (i & 1) ? 4.0 : 2.0;
+}
+
+double or_sigma_incoh(double E, int Z, int correction)
+{
+    if (correction <= 0)
+        return Z * or_sigma_kn(E);
+    const double k = E / ME_KEV;
+    const double T = (E / HC_KEV_A) * (E / HC_KEV_A);
+    const double a = a_Z(Z);
+    const double L = log1p(T / a);
+    double acc = 0.0;
+    for (int i = 0; i <= QUAD_N; ++i) {
+        const double s = (double)i / QUAD_N;
+        const double t = a * expm1(s * L);
+        const double mu = 1.0 - 2.0 * t / T;
+        const double S = Z * (-expm1(-4.0 * s * L));
+        acc += simpson_weight(i) * kn_dcs(k, mu) * S * a * L * exp(s * L);
+    }
+    acc *= 1.0 / (3.0 * QUAD_N);
+    return 2.0 * PI * (2.0 / T) * acc;
+}
+
+double or_sigma_coh(double E, int Z)
+{
+    const double T = (E / HC_KEV_A) * (E / HC_KEV_A);
+    const double a = a_Z(Z);
+    const double L = log1p(T / a);
+    double acc = 0.0;
+    for (int i = 0; i <= QUAD_N; ++i) {
+        const double s = (double)i / QUAD_N;
+        const double t = a * expm1(s * L);
+        const double mu = 1.0 - 2.0 * t / T;
+        acc += simpson_weight(i) * (1.0 + mu * mu) * a * L * exp(-3.0 * s * L);
+    }
+    acc *= 1.0 / (3.0 * QUAD_N);
+    return PI * R_E2_BARN * (2.0 / T) * (double)Z * (double)Z * acc;
+}
+
+/* Mean fraction of the photon energy given to the free electron in a
+ * Klein-Nishina collision (for the air-kerma weighting of the HVL). */
+double or_kn_energy_transfer_fraction(double E)
+{
+    const double k = E / ME_KEV;
+    double num = 0.0, den = 0.0;
+    for (int i = 0; i <= QUAD_N; ++i) {
+        const double mu = -1.0 + 2.0 * (double)i / QUAD_N;
+        const double eps = 1.0 / (1.0 + k * (1.0 - mu));
+        const double d = kn_dcs(k, mu) * simpson_weight(i);
+        num += d * (1.0 - eps);
+        den += d;
+    }
+    return num / den;
+}
+
+static void normalised(const or_composition* c, double* w)
+{
+    double s = 0.0;
+    for (int i = 0; i < c->n; ++i)
+        s += c->w[i];
+    for (int i = 0; i < c->n; ++i)
+        w[i] = s > 0 ? c->w[i] / s : 0.0;
+}
+
+void or_attenuation(const or_composition* c, int correction, int n, const double* E, double* photo,
+    double* incoh, double* coh)
+{
+    double w[OR_MAX_ELEMENTS];
+    normalised(c, w);
+    for (int j = 0; j < n; ++j) {
+        double p = 0, ic = 0, co = 0;
+        for (int i = 0; i < c->n; ++i) {
+            const int Z = c->Z[i];
+            const double f = w[i] * N_A / or_atomic_mass(Z) * 1e-24;
+            p += f * or_sigma_photo(E[j], Z);
+            ic += f * or_sigma_incoh(E[j], Z, correction);
+            co += f * or_sigma_coh(E[j], Z);
+        }
+        photo[j] = p;
+        incoh[j] = ic;
+        coh[j] = co;
+    }
+}
+
+static double element_mu_rho(int Z, double E)
+{
+    or_composition c = { 1, { Z }, { 1.0 } };
+    double p, i, co;
+    or_attenuation(&c, 1, 1, &E, &p, &i, &co);
+    return p + i + co;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Tube (ctsegmentationpipeline.cpp:66-71; beamsettingsmodel.cpp:257-330):
+ * Kramers' thick-target law N(E) ~ (kVp - E) / E on 1 keV bins, tungsten K lines
+ * (K edge 69.525 keV) with Green-Cosslett (kVp/E_K - 1)^1.63 yield scaling, and
+ * exponential filtration by each added filter.  Anode angle is carried but the
+ * model has no heel/self-absorption term.                                    */
+/* ------------------------------------------------------------------------- */
+#define W_K_EDGE 69.525
+static const double W_LINES[4] = { 57.981, 59.318, 67.244, 69.067 };
+static const double W_LINE_FRAC[4] = { 0.27, 0.47, 0.18, 0.08 };
+#define C_CHAR 0.1
+
+int or_tube_spectrum(double kvp, double anode_angle_deg, int n_filters, const int32_t* fZ,
+    const double* fmm, double* energies, double* weights, int cap)
+{
+    (void)anode_angle_deg;
+    const int n = (int)floor(kvp);
+    if (n < 1 || n > cap)
+        return -1;
+    double total = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const double E = k + 1.0;
+        energies[k] = E;
+        weights[k] = (kvp - E) / E;
+        total += weights[k];
+    }
+    if (kvp > W_K_EDGE) {
+        const double nchar = C_CHAR * pow(kvp / W_K_EDGE - 1.0, 1.63) * total;
+        for (int l = 0; l < 4; ++l) {
+            const int bin = (int)floor(W_LINES[l] + 0.5) - 1;
+            if (bin >= 0 && bin < n)
+                weights[bin] += nchar * W_LINE_FRAC[l];
+        }
+    }
+    for (int f = 0; f < n_filters; ++f) {
+        const double rho = or_element_density(fZ[f]);
+        if (rho <= 0.0 || fmm[f] <= 0.0)
+            continue;
+        for (int k = 0; k < n; ++k)
+            weights[k] *= exp(-element_mu_rho(fZ[f], energies[k]) * rho * fmm[f] * 0.1);
+    }
+    double s = 0.0;
+    for (int k = 0; k < n; ++k)
+        s += weights[k];
+    for (int k = 0; k < n; ++k)
+        weights[k] = s > 0 ? weights[k] / s : 0.0;
+    return n;
+}
+
+double or_tube_mean_energy(double kvp, int n_filters, const int32_t* fZ, const double* fmm)
+{
+    double E[512], w[512];
+    const int n = or_tube_spectrum(kvp, 12.0, n_filters, fZ, fmm, E, w, 512);
+    double m = 0.0;
+    for (int k = 0; k < n; ++k)
+        m += E[k] * w[k];
+    return m;
+}
+
+/* Air (dry, by mass): N 75.5 %, O 23.2 %, Ar 1.3 %. */
+static const or_composition AIR = { 3, { 7, 8, 18 }, { 0.755, 0.232, 0.013 } };
+
+double or_tube_al_hvl_mm(double kvp, int n_filters, const int32_t* fZ, const double* fmm)
+{
+    double E[512], w[512], ph[512], ic[512], co[512], kw[512], mal[512];
+    const int n = or_tube_spectrum(kvp, 12.0, n_filters, fZ, fmm, E, w, 512);
+    if (n <= 0)
+        return 0.0;
+    or_attenuation(&AIR, 1, n, E, ph, ic, co);
+    double k0 = 0.0;
+    for (int k = 0; k < n; ++k) {
+        kw[k] = w[k] * E[k] * (ph[k] + ic[k] * or_kn_energy_transfer_fraction(E[k]));
+        mal[k] = element_mu_rho(13, E[k]) * or_element_density(13) * 0.1; /* per mm */
+        k0 += kw[k];
+    }
+    double lo = 0.0, hi = 100.0;
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        double s = 0.0;
+        for (int k = 0; k < n; ++k)
+            s += kw[k] * exp(-mal[k] * mid);
+        if (s > 0.5 * k0)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11).  */
+/* ------------------------------------------------------------------------- */
+void or_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        const uint32_t n1 = (uint32_t)p1;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        const uint32_t n3 = (uint32_t)p0;
+        c0 = n0;
+        c1 = n1;
+        c2 = n2;
+        c3 = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+/* (2 k + 1) / 2^24 with k the top 23 bits: exactly representable in FP32, in (0, 1). */
+double or_uniform_from_u32(uint32_t x) { return (double)((x >> 9) * 2u + 1u) * (1.0 / 16777216.0); }
+
+/* Draw source: either a Philox stream for one history, or injected uniforms. */
+typedef struct {
+    uint32_t key[2];
+    uint32_t ctr[4];
+    uint32_t buf[4];
+    int idx;
+    const double* inj;
+    int n_inj, used;
+} rng_t;
+
+static void rng_stream(rng_t* r, uint64_t seed, uint32_t stream, uint64_t hist)
+{
+    r->key[0] = (uint32_t)seed;
+    r->key[1] = (uint32_t)(seed >> 32);
+    r->ctr[0] = 0;
+    r->ctr[1] = stream;
+    r->ctr[2] = (uint32_t)hist;
+    r->ctr[3] = (uint32_t)(hist >> 32);
+    r->idx = 4;
+    r->inj = NULL;
+    r->used = 0;
+}
+
+static uint32_t rng_raw(rng_t* r)
+{
+    if (r->idx == 4) {
+        or_philox4x32(r->ctr, r->key, r->buf);
+        r->ctr[0]++;
+        r->idx = 0;
+    }
+    r->used++;
+    return r->buf[r->idx++];
+}
+
+static double rng_u(rng_t* r)
+{
+    if (r->inj) {
+        if (r->used >= r->n_inj)
+            return 0.5; /* exhausted: callers size the array generously */
+        return r->inj[r->used++];
+    }
+    return or_uniform_from_u32(rng_raw(r));
+}
+
+/* ------------------------------------------------------------------------- */
+/* Vector helpers                                                              */
+/* ------------------------------------------------------------------------- */
+static void cross3(const double a[3], const double b[3], double c[3])
+{
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static void normalise3(double v[3])
+{
+    const double n = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (n > 0) {
+        v[0] /= n;
+        v[1] /= n;
+        v[2] /= n;
+    }
+}
+
+/* Rodrigues rotation of v about unit axis k by angle a (right-handed). */
+static void rotate3(const double v[3], const double k[3], double a, double out[3])
+{
+    double kxv[3];
+    cross3(k, v, kxv);
+    const double kv = k[0] * v[0] + k[1] * v[1] + k[2] * v[2];
+    const double c = cos(a), s = sin(a);
+    for (int i = 0; i < 3; ++i)
+        out[i] = v[i] * c + kxv[i] * s + k[i] * kv * (1.0 - c);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Beam -> exposures.  DX: every exposure has the beam's pose
+ * (dxmc_specialization.cpp:155-167 sets position/cosines; collimation half-angles
+ * :123-129).  Rotating beams place the source at SDD/2 from the isocentre, the
+ * fan along c0, the rotation axis along c1, and direction = c0 x c1 pointing at
+ * the isocentre (beamactorcontainer.cpp:219-231 uses the same basis).         */
+/* ------------------------------------------------------------------------- */
+static double interp_profile(const double* w, int n, double f)
+{
+    /* w sampled uniformly on [0, 1] */
+    if (n <= 0)
+        return 1.0;
+    if (n == 1)
+        return w[0];
+    double x = f * (n - 1);
+    if (x <= 0)
+        return w[0];
+    if (x >= n - 1)
+        return w[n - 1];
+    const int i = (int)x;
+    const double t = x - i;
+    return w[i] + t * (w[i + 1] - w[i]);
+}
+
+static double aec_weight(const or_beam* b, double z)
+{
+    if (b->n_aec <= 0 || !b->aec_weight)
+        return 1.0;
+    const double z0 = b->aec_start[2], z1 = b->aec_stop[2];
+    const double f = (z1 != z0) ? (z - z0) / (z1 - z0) : 0.0;
+    return interp_profile(b->aec_weight, b->n_aec, f);
+}
+
+static void rotating_exposure(const double iso[3], const double axis_in[3], double angle, double sid,
+    double half_fan, double half_cone, or_exposure* e)
+{
+    double axis[3] = { axis_in[0], axis_in[1], axis_in[2] };
+    normalise3(axis);
+    const double xh[3] = { 1, 0, 0 }, yh[3] = { 0, 1, 0 };
+    double s0[3];
+    cross3(axis, xh, s0);
+    if (s0[0] * s0[0] + s0[1] * s0[1] + s0[2] * s0[2] < 1e-12)
+        cross3(axis, yh, s0);
+    normalise3(s0);
+    double s[3];
+    rotate3(s0, axis, angle, s);
+    double n[3] = { -s[0], -s[1], -s[2] };
+    for (int i = 0; i < 3; ++i) {
+        e->pos[i] = iso[i] + sid * s[i];
+        e->c1[i] = axis[i];
+    }
+    cross3(axis, n, e->c0);
+    e->half[0] = half_fan;
+    e->half[1] = half_cone;
+    e->weight = 1.0;
+    e->tube = 0;
+}
+
+int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
+{
+    int n = 0;
+    const double zaxis[3] = { 0, 0, 1 };
+    if (b->type == OR_BEAM_DX || b->type == OR_BEAM_PENCIL) {
+        n = (int)(b->n_exposures > 0 ? b->n_exposures : 1);
+        if (!out)
+            return n;
+        if (n > cap)
+            return -n;
+        for (int i = 0; i < n; ++i) {
+            or_exposure* e = &out[i];
+            memcpy(e->pos, b->position, sizeof(e->pos));
+            memcpy(e->c0, b->cosines[0], sizeof(e->c0));
+            memcpy(e->c1, b->cosines[1], sizeof(e->c1));
+            if (b->type == OR_BEAM_PENCIL) {
+                e->half[0] = e->half[1] = 0.0;
+            } else {
+                e->half[0] = b->half_angles[0];
+                e->half[1] = b->half_angles[1];
+            }
+            e->weight = 1.0;
+            e->tube = 0;
+        }
+        return n;
+    }
+    const double sid = 0.5 * b->sdd_cm;
+    const double step = b->step_angle_deg * PI / 180.0;
+    const double a0 = b->start_angle_deg * PI / 180.0;
+    if (b->type == OR_BEAM_CT_SPIRAL || b->type == OR_BEAM_CT_SPIRAL_DUAL) {
+        const double dz = b->stop[2] - b->start[2];
+        const double feed = b->collimation_cm * b->pitch; /* cm per rotation */
+        const double per_rot = 2.0 * PI / step;
+        long m = (long)ceil(fabs(dz) / feed * per_rot - 1e-9);
+        if (m < 1)
+            m = 1;
+        const int dual = b->type == OR_BEAM_CT_SPIRAL_DUAL;
+        n = (int)(dual ? 2 * m : m);
+        if (!out)
+            return n;
+        if (n > cap)
+            return -n;
+        const double half_cone = atan(0.5 * b->collimation_cm / sid);
+        for (long i = 0; i < m; ++i) {
+            const double ang = a0 + i * step;
+            const double z = b->start[2] + (dz >= 0 ? 1.0 : -1.0) * (double)i / per_rot * feed;
+            const double iso[3] = { b->start[0], b->start[1], z };
+            for (int t = 0; t < (dual ? 2 : 1); ++t) {
+                or_exposure* e = &out[dual ? 2 * i + t : i];
+                const double fov = (t == 1) ? b->fov_b_cm : b->scan_fov_cm;
+                rotating_exposure(iso, zaxis, ang + (t == 1 ? 0.5 * PI : 0.0), sid, atan(0.5 * fov / sid),
+                    half_cone, e);
+                e->tube = t;
+                const double tw = dual ? (t == 0 ? 2.0 * b->tube_a_weight : 2.0 * (1.0 - b->tube_a_weight)) : 1.0;
+                e->weight = aec_weight(b, z) * tw;
+            }
+        }
+    } else if (b->type == OR_BEAM_CT_SEQUENTIAL) {
+        const long per_rot = lround(2.0 * PI / step);
+        const int slices = b->n_slices > 0 ? b->n_slices : 1;
+        n = (int)(per_rot * slices);
+        if (!out)
+            return n;
+        if (n > cap)
+            return -n;
+        const double half_cone = atan(0.5 * b->collimation_cm / sid);
+        for (int s = 0; s < slices; ++s) {
+            const double iso[3] = { b->position[0], b->position[1], b->position[2] + s * b->slice_spacing_cm };
+            for (long i = 0; i < per_rot; ++i) {
+                or_exposure* e = &out[s * per_rot + i];
+                rotating_exposure(iso, zaxis, a0 + i * step, sid, atan(0.5 * b->scan_fov_cm / sid), half_cone, e);
+                e->weight = aec_weight(b, iso[2]);
+            }
+        }
+    } else if (b->type == OR_BEAM_CBCT) {
+        const double a1 = b->stop_angle_deg * PI / 180.0;
+        long m = (long)floor((a1 - a0) / step + 1e-9) + 1;
+        if (m < 1)
+            m = 1;
+        n = (int)m;
+        if (!out)
+            return n;
+        if (n > cap)
+            return -n;
+        for (long i = 0; i < m; ++i)
+            rotating_exposure(b->position, b->rotation_axis, a0 + i * step, sid, b->half_angles[0],
+                b->half_angles[1], &out[i]);
+    } else {
+        return 0;
+    }
+    /* AEC weights are relative: mean over exposures = 1 */
+    if (b->type != OR_BEAM_CBCT) {
+        double s = 0.0;
+        for (int i = 0; i < n; ++i)
+            s += out[i].weight;
+        const double mean = s / n;
+        if (mean > 0)
+            for (int i = 0; i < n; ++i)
+                out[i].weight /= mean;
+    }
+    return n;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Siddon / Amanatides-Woo traversal in grid-local coordinates (grid spans
+ * [0, n_a * sp_a) on each axis).  The FP32 variant fixes the operation order so
+ * that the device traversal reproduces it bit for bit.                        */
+/* ------------------------------------------------------------------------- */
+int or_siddon_f32(const float o[3], const float d[3], const int32_t n[3], const float sp[3], int cap,
+    int64_t* idx, float* len)
+{
+    float L[3], inv[3];
+    float tmin = 0.0f, tmax = FLT_MAX;
+    for (int a = 0; a < 3; ++a) {
+        L[a] = (float)n[a] * sp[a];
+        if (d[a] != 0.0f) {
+            inv[a] = 1.0f / d[a];
+            float t1 = (0.0f - o[a]) * inv[a];
+            float t2 = (L[a] - o[a]) * inv[a];
+            if (t1 > t2) {
+                const float tt = t1;
+                t1 = t2;
+                t2 = tt;
+            }
+            if (t1 > tmin)
+                tmin = t1;
+            if (t2 < tmax)
+                tmax = t2;
+        } else {
+            inv[a] = 0.0f;
+            if (o[a] < 0.0f || o[a] >= L[a])
+                return 0;
+        }
+    }
+    if (!(tmin < tmax))
+        return 0;
+    int i[3], st[3];
+    for (int a = 0; a < 3; ++a) {
+        const float p = o[a] + tmin * d[a];
+        int k = (int)floorf(p / sp[a]);
+        if (k < 0)
+            k = 0;
+        if (k > n[a] - 1)
+            k = n[a] - 1;
+        i[a] = k;
+        st[a] = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
+    }
+    float t = tmin;
+    int cnt = 0;
+    for (;;) {
+        float tn[3];
+        for (int a = 0; a < 3; ++a)
+            tn[a] = st[a] != 0 ? ((float)(i[a] + (st[a] > 0 ? 1 : 0)) * sp[a] - o[a]) * inv[a] : FLT_MAX;
+        int ax = 0;
+        if (tn[1] < tn[ax])
+            ax = 1;
+        if (tn[2] < tn[ax])
+            ax = 2;
+        float tnext = tn[ax] < tmax ? tn[ax] : tmax;
+        const float l = tnext - t;
+        if (l > 0.0f) {
+            if (cnt < cap) {
+                idx[cnt] = (int64_t)i[0] + (int64_t)n[0] * ((int64_t)i[1] + (int64_t)n[1] * i[2]);
+                len[cnt] = l;
+            }
+            cnt++;
+            t = tnext;
+        }
+        if (tnext >= tmax)
+            break;
+        i[ax] += st[ax];
+        if (i[ax] < 0 || i[ax] >= n[ax])
+            break;
+    }
+    return cnt <= cap ? cnt : -cnt;
+}
+
+int or_siddon_f64(const double o[3], const double d[3], const int32_t n[3], const double sp[3], int cap,
+    int64_t* idx, double* len)
+{
+    double L[3], inv[3];
+    double tmin = 0.0, tmax = DBL_MAX;
+    for (int a = 0; a < 3; ++a) {
+        L[a] = (double)n[a] * sp[a];
+        if (d[a] != 0.0) {
+            inv[a] = 1.0 / d[a];
+            double t1 = (0.0 - o[a]) * inv[a];
+            double t2 = (L[a] - o[a]) * inv[a];
+            if (t1 > t2) {
+                const double tt = t1;
+                t1 = t2;
+                t2 = tt;
+            }
+            if (t1 > tmin)
+                tmin = t1;
+            if (t2 < tmax)
+                tmax = t2;
+        } else {
+            inv[a] = 0.0;
+            if (o[a] < 0.0 || o[a] >= L[a])
+                return 0;
+        }
+    }
+    if (!(tmin < tmax))
+        return 0;
+    int i[3], st[3];
+    for (int a = 0; a < 3; ++a) {
+        const double p = o[a] + tmin * d[a];
+        int k = (int)floor(p / sp[a]);
+        if (k < 0)
+            k = 0;
+        if (k > n[a] - 1)
+            k = n[a] - 1;
+        i[a] = k;
+        st[a] = d[a] > 0.0 ? 1 : (d[a] < 0.0 ? -1 : 0);
+    }
+    double t = tmin;
+    int cnt = 0;
+    for (;;) {
+        double tn[3];
+        for (int a = 0; a < 3; ++a)
+            tn[a] = st[a] != 0 ? ((double)(i[a] + (st[a] > 0 ? 1 : 0)) * sp[a] - o[a]) * inv[a] : DBL_MAX;
+        int ax = 0;
+        if (tn[1] < tn[ax])
+            ax = 1;
+        if (tn[2] < tn[ax])
+            ax = 2;
+        double tnext = tn[ax] < tmax ? tn[ax] : tmax;
+        const double l = tnext - t;
+        if (l > 0.0) {
+            if (cnt < cap) {
+                idx[cnt] = (int64_t)i[0] + (int64_t)n[0] * ((int64_t)i[1] + (int64_t)n[1] * i[2]);
+                len[cnt] = l;
+            }
+            cnt++;
+            t = tnext;
+        }
+        if (tnext >= tmax)
+            break;
+        i[ax] += st[ax];
+        if (i[ax] < 0 || i[ax] >= n[ax])
+            break;
+    }
+    return cnt <= cap ? cnt : -cnt;
+}
+
+/* ------------------------------------------------------------------------- */
+/* Material data for sampling: per element n_i = w_i / A_i (mol/g), Z_i, a_Z.  */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    int n;
+    double nZ[OR_MAX_ELEMENTS];  /* n_i Z_i   (incoherent scattering function weight) */
+    double nZ2[OR_MAX_ELEMENTS]; /* n_i Z_i^2 (form-factor weight) */
+    double a[OR_MAX_ELEMENTS];
+    double Zsum;
+} mat_sampling;
+
+static void make_sampling(const or_composition* c, mat_sampling* m)
+{
+    double w[OR_MAX_ELEMENTS];
+    normalised(c, w);
+    m->n = c->n;
+    m->Zsum = 0.0;
+    for (int i = 0; i < c->n; ++i) {
+        const double ni = w[i] / or_atomic_mass(c->Z[i]);
+        m->nZ[i] = ni * c->Z[i];
+        m->nZ2[i] = ni * c->Z[i] * c->Z[i];
+        m->a[i] = a_Z(c->Z[i]);
+        m->Zsum += m->nZ[i];
+    }
+}
+
+/* Klein-Nishina by Kahn's rejection method (Kahn 1954; as given in Lux &
+ * Koblinger, Monte Carlo Particle Transport Methods, 1991), followed for
+ * correction >= 1 by rejection on S(x)/Z of the material.  Returns E'. */
+static double sample_compton(double E, const mat_sampling* m, int correction, rng_t* r, double* cos_theta)
+{
+    const double k = E / ME_KEV;
+    const double kk = 2.0 * k;
+    for (int guard = 0; guard < 100000; ++guard) {
+        const double r1 = rng_u(r), r2 = rng_u(r), r3 = rng_u(r);
+        double xm1; /* x - 1, x = E / E' */
+        int acc;
+        if (r1 * (9.0 + kk) <= 1.0 + kk) {
+            xm1 = kk * r2;
+            const double x = 1.0 + xm1;
+            acc = r3 * x * x <= 4.0 * (x - 1.0);
+        } else {
+            xm1 = kk * (1.0 - r2) / (1.0 + kk * r2);
+            const double x = 1.0 + xm1;
+            const double mu = 1.0 - xm1 / k;
+            acc = 2.0 * r3 <= mu * mu + 1.0 / x;
+        }
+        if (!acc)
+            continue;
+        const double omu = xm1 / k; /* 1 - cos theta */
+        if (correction >= 1) {
+            const double q = E / HC_KEV_A;
+            const double t = q * q * 0.5 * omu; /* x^2 */
+            double S = 0.0;
+            for (int i = 0; i < m->n; ++i) {
+                const double b = 1.0 + t / m->a[i];
+                const double b2 = b * b;
+                S += m->nZ[i] * (1.0 - 1.0 / (b2 * b2));
+            }
+            const double r4 = rng_u(r);
+            if (r4 * m->Zsum > S)
+                continue;
+        }
+        *cos_theta = 1.0 - omu;
+        return E / (1.0 + xm1);
+    }
+    *cos_theta = 1.0;
+    return E;
+}
+
+/* Rayleigh: pick an element by its share of the form-factor integral up to
+ * x_max = E / hc, invert that element's F^2 distribution in t = x^2 analytically,
+ * accept on (1 + cos^2) / 2 (the standard composition-rejection scheme). */
+static double sample_rayleigh(double E, const mat_sampling* m, rng_t* r)
+{
+    const double q = E / HC_KEV_A;
+    const double T = q * q;
+    double G[OR_MAX_ELEMENTS], c[OR_MAX_ELEMENTS];
+    double Gs = 0.0;
+    for (int i = 0; i < m->n; ++i) {
+        c[i] = -expm1(-3.0 * log1p(T / m->a[i]));
+        G[i] = m->nZ2[i] * m->a[i] * c[i];
+        Gs += G[i];
+    }
+    for (int guard = 0; guard < 100000; ++guard) {
+        const double r1 = rng_u(r), r2 = rng_u(r), r3 = rng_u(r);
+        int e = m->n - 1;
+        double acc = 0.0;
+        const double target = r1 * Gs;
+        for (int i = 0; i < m->n; ++i) {
+            acc += G[i];
+            if (target <= acc) {
+                e = i;
+                break;
+            }
+        }
+        const double y = r2 * c[e];
+        const double t = m->a[e] * expm1(-log1p(-y) / 3.0);
+        const double mu = 1.0 - 2.0 * t / T;
+        if (2.0 * r3 <= 1.0 + mu * mu)
+            return mu;
+    }
+    return 1.0;
+}
+
+double or_sample_compton(double E, const or_composition* c, int correction, const double* u, int nu, int* used,
+    double* cos_theta)
+{
+    mat_sampling m;
+    make_sampling(c, &m);
+    rng_t r;
+    memset(&r, 0, sizeof(r));
+    r.inj = u;
+    r.n_inj = nu;
+    const double Ep = sample_compton(E, &m, correction, &r, cos_theta);
+    *used = r.used;
+    return Ep;
+}
+
+double or_sample_rayleigh(double E, const or_composition* c, const double* u, int nu, int* used)
+{
+    mat_sampling m;
+    make_sampling(c, &m);
+    rng_t r;
+    memset(&r, 0, sizeof(r));
+    r.inj = u;
+    r.n_inj = nu;
+    const double mu = sample_rayleigh(E, &m, &r);
+    *used = r.used;
+    return mu;
+}
+
+/* ------------------------------------------------------------------------- */
+/* World: AAVoxelGrid ingest + build (simulationpipeline.cpp:127-153).  Grid
+ * centred on the origin (datacontainer.cpp:174-178), x fastest
+ * (otherphantomimportpipeline.cpp:44), spacing in cm (datacontainer.cpp:241-253). */
+/* ------------------------------------------------------------------------- */
+struct or_world {
+    int32_t n[3];
+    double sp[3];
+    size_t N;
+    double* density;
+    uint8_t* material;
+    int n_mats;
+    int correction;
+    or_composition* mats;
+    mat_sampling* samp;
+    double* photo; /* [m][OR_NE] cm^2/g */
+    double* incoh;
+    double* coh;
+    double* tot;
+    double maj[OR_NE]; /* 1/cm */
+    double* e;
+    double* e2;
+    uint64_t* cnt;
+};
+
+static const double MAJ_SAFETY = 1.0 + 1.0 / 1048576.0;
+
+or_world* or_world_create(const int32_t dims[3], const double spacing_cm[3], const double* density,
+    const uint8_t* material, const or_composition* mats, int n_mats, int correction)
+{
+    if (n_mats <= 0 || n_mats > 255)
+        return NULL;
+    or_world* w = (or_world*)calloc(1, sizeof(or_world));
+    for (int a = 0; a < 3; ++a) {
+        w->n[a] = dims[a];
+        w->sp[a] = spacing_cm[a];
+    }
+    w->N = (size_t)dims[0] * dims[1] * dims[2];
+    w->density = (double*)malloc(w->N * sizeof(double));
+    w->material = (uint8_t*)malloc(w->N);
+    memcpy(w->density, density, w->N * sizeof(double));
+    memcpy(w->material, material, w->N);
+    w->n_mats = n_mats;
+    w->correction = correction;
+    w->mats = (or_composition*)malloc(n_mats * sizeof(or_composition));
+    memcpy(w->mats, mats, n_mats * sizeof(or_composition));
+    w->samp = (mat_sampling*)malloc(n_mats * sizeof(mat_sampling));
+    w->photo = (double*)malloc(n_mats * OR_NE * sizeof(double));
+    w->incoh = (double*)malloc(n_mats * OR_NE * sizeof(double));
+    w->coh = (double*)malloc(n_mats * OR_NE * sizeof(double));
+    w->tot = (double*)malloc(n_mats * OR_NE * sizeof(double));
+    double E[OR_NE];
+    for (int i = 0; i < OR_NE; ++i)
+        E[i] = OR_EMIN + i * OR_DE;
+    for (int m = 0; m < n_mats; ++m) {
+        make_sampling(&mats[m], &w->samp[m]);
+        or_attenuation(&mats[m], correction, OR_NE, E, w->photo + m * OR_NE, w->incoh + m * OR_NE,
+            w->coh + m * OR_NE);
+        for (int i = 0; i < OR_NE; ++i)
+            w->tot[m * OR_NE + i] = w->photo[m * OR_NE + i] + w->incoh[m * OR_NE + i] + w->coh[m * OR_NE + i];
+    }
+    double rmax[256];
+    for (int m = 0; m < 256; ++m)
+        rmax[m] = 0.0;
+    for (size_t v = 0; v < w->N; ++v) {
+        const int m = w->material[v];
+        if (m < n_mats && w->density[v] > rmax[m])
+            rmax[m] = w->density[v];
+    }
+    for (int i = 0; i < OR_NE; ++i) {
+        double mx = 0.0;
+        for (int m = 0; m < n_mats; ++m) {
+            const double v = rmax[m] * w->tot[m * OR_NE + i];
+            if (v > mx)
+                mx = v;
+        }
+        w->maj[i] = mx * MAJ_SAFETY;
+    }
+    w->e = (double*)calloc(w->N, sizeof(double));
+    w->e2 = (double*)calloc(w->N, sizeof(double));
+    w->cnt = (uint64_t*)calloc(w->N, sizeof(uint64_t));
+    return w;
+}
+
+void or_world_destroy(or_world* w)
+{
+    if (!w)
+        return;
+    free(w->density);
+    free(w->material);
+    free(w->mats);
+    free(w->samp);
+    free(w->photo);
+    free(w->incoh);
+    free(w->coh);
+    free(w->tot);
+    free(w->e);
+    free(w->e2);
+    free(w->cnt);
+    free(w);
+}
+
+void or_world_clear(or_world* w)
+{
+    memset(w->e, 0, w->N * sizeof(double));
+    memset(w->e2, 0, w->N * sizeof(double));
+    memset(w->cnt, 0, w->N * sizeof(uint64_t));
+}
+
+int or_world_table(const or_world* w, int m, double* photo, double* incoh, double* coh)
+{
+    if (m < 0 || m >= w->n_mats)
+        return -1;
+    memcpy(photo, w->photo + m * OR_NE, OR_NE * sizeof(double));
+    memcpy(incoh, w->incoh + m * OR_NE, OR_NE * sizeof(double));
+    memcpy(coh, w->coh + m * OR_NE, OR_NE * sizeof(double));
+    return OR_NE;
+}
+
+int or_world_majorant(const or_world* w, double* maj)
+{
+    memcpy(maj, w->maj, sizeof(w->maj));
+    return OR_NE;
+}
+
+void or_world_tally(const or_world* w, double* energy, double* energy2, uint64_t* count)
+{
+    if (energy)
+        memcpy(energy, w->e, w->N * sizeof(double));
+    if (energy2)
+        memcpy(energy2, w->e2, w->N * sizeof(double));
+    if (count)
+        memcpy(count, w->cnt, w->N * sizeof(uint64_t));
+}
+
+/* ------------------------------------------------------------------------- */
+/* Transport                                                                   */
+/* ------------------------------------------------------------------------- */
+static inline void grid_pos(double E, int* i, double* f)
+{
+    const double x = (E - OR_EMIN) * (1.0 / OR_DE);
+    int k = (int)x;
+    if (k < 0)
+        k = 0;
+    if (k > OR_NE - 2)
+        k = OR_NE - 2;
+    *i = k;
+    *f = x - k;
+}
+
+static inline double lerp_tab(const double* t, int i, double f) { return t[i] + f * (t[i + 1] - t[i]); }
+
+static void atomic_add_f64(double* p, double v)
+{
+    uint64_t old = __atomic_load_n((uint64_t*)p, __ATOMIC_RELAXED);
+    for (;;) {
+        double cur;
+        memcpy(&cur, &old, 8);
+        const double nv = cur + v;
+        uint64_t nb;
+        memcpy(&nb, &nv, 8);
+        if (__atomic_compare_exchange_n((uint64_t*)p, &old, nb, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED))
+            return;
+    }
+}
+
+typedef struct {
+    int n;
+    double E[512];
+    uint32_t thr[512];
+    int32_t alias[512];
+} alias_table;
+
+/* Walker alias table (Vose's O(n) construction). Acceptance thresholds are
+ * stored as 23-bit integers so that the draw is exact on every device. */
+static void build_alias(const double* w, int n, alias_table* t)
+{
+    double p[512];
+    int small[512], large[512];
+    int ns = 0, nl = 0;
+    double s = 0.0;
+    for (int i = 0; i < n; ++i)
+        s += w[i];
+    for (int i = 0; i < n; ++i) {
+        p[i] = w[i] / s * n;
+        t->alias[i] = i;
+    }
+    for (int i = 0; i < n; ++i) {
+        if (p[i] < 1.0)
+            small[ns++] = i;
+        else
+            large[nl++] = i;
+    }
+    double prob[512];
+    while (ns > 0 && nl > 0) {
+        const int l = small[--ns];
+        const int g = large[--nl];
+        prob[l] = p[l];
+        t->alias[l] = g;
+        p[g] = (p[g] + p[l]) - 1.0;
+        if (p[g] < 1.0)
+            small[ns++] = g;
+        else
+            large[nl++] = g;
+    }
+    while (nl > 0)
+        prob[large[--nl]] = 1.0;
+    while (ns > 0)
+        prob[small[--ns]] = 1.0;
+    for (int i = 0; i < n; ++i)
+        t->thr[i] = (uint32_t)floor(prob[i] * 8388608.0 + 0.5);
+    t->n = n;
+}
+
+static int sample_alias(const alias_table* t, rng_t* r)
+{
+    const uint32_t x0 = rng_raw(r) >> 9;
+    const uint32_t x1 = rng_raw(r) >> 9;
+    const int k = (int)(((uint64_t)x0 * (uint64_t)t->n) >> 23);
+    return x1 < t->thr[k] ? k : t->alias[k];
+}
+
+typedef struct {
+    int n;
+    double ang[256];
+    double w[256];
+    double norm[2];
+} bowtie_t;
+
+static double bowtie_eval(const bowtie_t* b, double a)
+{
+    if (b->n <= 0)
+        return 1.0;
+    if (a <= b->ang[0])
+        return b->w[0];
+    if (a >= b->ang[b->n - 1])
+        return b->w[b->n - 1];
+    int lo = 0, hi = b->n - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (b->ang[mid] <= a)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    const double t = (a - b->ang[lo]) / (b->ang[hi] - b->ang[lo]);
+    return b->w[lo] + t * (b->w[hi] - b->w[lo]);
+}
+
+/* mean of the bowtie profile over |angle| in [0, half] (exact for piecewise linear) */
+static double bowtie_mean(const bowtie_t* b, double half)
+{
+    if (b->n <= 0 || half <= 0.0)
+        return 1.0;
+    double xs[260];
+    int m = 0;
+    xs[m++] = 0.0;
+    for (int i = 0; i < b->n; ++i)
+        if (b->ang[i] > 0.0 && b->ang[i] < half)
+            xs[m++] = b->ang[i];
+    xs[m++] = half;
+    double s = 0.0;
+    for (int i = 0; i + 1 < m; ++i)
+        s += 0.5 * (bowtie_eval(b, xs[i]) + bowtie_eval(b, xs[i + 1])) * (xs[i + 1] - xs[i]);
+    return s / half;
+}
+
+typedef struct {
+    or_world* w;
+    const or_beam* b;
+    or_exposure* exps;
+    int n_exp;
+    double gorigin[3];
+    alias_table spec[2];
+    bowtie_t bow;
+    uint64_t seed;
+    uint32_t stream;
+    int tracking;
+    uint64_t h0, h1;
+    uint64_t next;
+    pthread_mutex_t lock;
+    or_stats tot;
+} run_ctx;
+
+static void deposit(or_world* w, size_t v, double e, or_stats* st)
+{
+    atomic_add_f64(&w->e[v], e);
+    atomic_add_f64(&w->e2[v], e * e);
+    __atomic_fetch_add(&w->cnt[v], 1, __ATOMIC_RELAXED);
+    st->e_deposited += e;
+    st->n_deposits++;
+}
+
+static void scatter_dir(double d[3], double cost, double phi_u)
+{
+    const double sint = sqrt(fmax(0.0, 1.0 - cost * cost));
+    const double phi = 2.0 * PI * phi_u;
+    const double cp = cos(phi), sp = sin(phi);
+    double n[3];
+    if (fabs(d[2]) > 0.99999) {
+        n[0] = sint * cp;
+        n[1] = sint * sp;
+        n[2] = (d[2] > 0 ? 1.0 : -1.0) * cost;
+    } else {
+        const double tmp = sqrt(1.0 - d[2] * d[2]);
+        n[0] = sint * (d[0] * d[2] * cp - d[1] * sp) / tmp + d[0] * cost;
+        n[1] = sint * (d[1] * d[2] * cp + d[0] * sp) / tmp + d[1] * cost;
+        n[2] = -sint * cp * tmp + d[2] * cost;
+    }
+    normalise3(n);
+    d[0] = n[0];
+    d[1] = n[1];
+    d[2] = n[2];
+}
+
+static inline int inside(const or_world* w, const double p[3], size_t* v)
+{
+    int i[3];
+    for (int a = 0; a < 3; ++a) {
+        const double L = w->n[a] * w->sp[a];
+        if (!(p[a] >= 0.0 && p[a] < L))
+            return 0;
+        int k = (int)floor(p[a] / w->sp[a]);
+        if (k > w->n[a] - 1)
+            k = w->n[a] - 1;
+        i[a] = k;
+    }
+    *v = (size_t)i[0] + (size_t)w->n[0] * ((size_t)i[1] + (size_t)w->n[1] * i[2]);
+    return 1;
+}
+
+/* Real-interaction branch shared by both tracking modes; returns 0 if the photon died. */
+static int interact(or_world* w, size_t v, int m, double* E, double wgt, double d[3], rng_t* r, or_stats* st,
+    int* first)
+{
+    if (*first) {
+        st->n_interacted++;
+        *first = 0;
+    }
+    int ie;
+    double fe;
+    grid_pos(*E, &ie, &fe);
+    const double ph = lerp_tab(w->photo + m * OR_NE, ie, fe);
+    const double ic = lerp_tab(w->incoh + m * OR_NE, ie, fe);
+    const double co = lerp_tab(w->coh + m * OR_NE, ie, fe);
+    const double rt = rng_u(r) * (ph + ic + co);
+    st->n_real++;
+    if (rt < ph) {
+        st->n_photo++;
+        deposit(w, v, wgt * *E, st);
+        return 0;
+    }
+    if (rt < ph + ic) {
+        st->n_compton++;
+        double cost;
+        const double Ep = sample_compton(*E, &w->samp[m], w->correction, r, &cost);
+        scatter_dir(d, cost, rng_u(r));
+        deposit(w, v, wgt * (*E - Ep), st);
+        *E = Ep;
+        if (*E < E_CUT) {
+            st->n_cutoff++;
+            deposit(w, v, wgt * *E, st);
+            return 0;
+        }
+        return 1;
+    }
+    st->n_rayleigh++;
+    const double cost = sample_rayleigh(*E, &w->samp[m], r);
+    scatter_dir(d, cost, rng_u(r));
+    return 1;
+}
+
+/* Source photon of history h (draw order: 2 raw for the energy, fan, cone);
+ * position in grid-local cm. */
+static void sample_source(const run_ctx* c, uint64_t h, rng_t* r, double* E_out, double p[3], double d[3],
+    double* wgt_out)
+{
+    const uint64_t ppe = c->b->particles_per_exposure;
+    const or_exposure* ex = &c->exps[h / ppe];
+    double E;
+    if (c->b->type == OR_BEAM_PENCIL) {
+        (void)rng_raw(r);
+        (void)rng_raw(r);
+        E = c->b->energy_kev;
+    } else {
+        const alias_table* at = &c->spec[ex->tube];
+        E = at->E[sample_alias(at, r)];
+    }
+    const double ax = (2.0 * rng_u(r) - 1.0) * ex->half[0];
+    const double ay = (2.0 * rng_u(r) - 1.0) * ex->half[1];
+    const double sx = sin(ax), sy = sin(ay);
+    const double sz = sqrt(fmax(0.0, 1.0 - sx * sx - sy * sy));
+    double n[3];
+    cross3(ex->c0, ex->c1, n);
+    for (int a = 0; a < 3; ++a) {
+        d[a] = ex->c0[a] * sx + ex->c1[a] * sy + n[a] * sz;
+        p[a] = ex->pos[a] - c->gorigin[a];
+    }
+    double wgt = ex->weight;
+    if (c->bow.n > 0)
+        wgt *= bowtie_eval(&c->bow, fabs(ax)) / c->bow.norm[ex->tube];
+    *E_out = E;
+    *wgt_out = wgt;
+}
+
+static void run_history(run_ctx* c, uint64_t h, or_stats* st)
+{
+    or_world* w = c->w;
+    rng_t r;
+    rng_stream(&r, c->seed, c->stream, h);
+    double E, wgt, p[3], d[3];
+    sample_source(c, h, &r, &E, p, d, &wgt);
+    int first = 1;
+    st->n_histories++;
+    st->e_source += wgt * E;
+    /* enter the grid (slab test) */
+    double tmin = 0.0, tmax = DBL_MAX;
+    double L[3];
+    for (int a = 0; a < 3; ++a) {
+        L[a] = w->n[a] * w->sp[a];
+        if (d[a] != 0.0) {
+            double t1 = (0.0 - p[a]) / d[a], t2 = (L[a] - p[a]) / d[a];
+            if (t1 > t2) {
+                const double tt = t1;
+                t1 = t2;
+                t2 = tt;
+            }
+            if (t1 > tmin)
+                tmin = t1;
+            if (t2 < tmax)
+                tmax = t2;
+        } else if (p[a] < 0.0 || p[a] >= L[a]) {
+            tmax = -1.0;
+        }
+    }
+    if (!(tmin < tmax)) {
+        st->n_missed++;
+        st->e_escaped += wgt * E;
+        return;
+    }
+    for (int a = 0; a < 3; ++a) {
+        p[a] += tmin * d[a];
+        if (p[a] < 0.0)
+            p[a] = 0.0;
+        if (p[a] >= L[a])
+            p[a] = nextafter(L[a], 0.0);
+    }
+    for (long step = 0; step < MAX_STEPS; ++step) {
+        if (c->tracking == OR_TRACK_WOODCOCK) {
+            int ie;
+            double fe;
+            grid_pos(E, &ie, &fe);
+            const double mmax = lerp_tab(w->maj, ie, fe);
+            const double s = -log(rng_u(&r)) / mmax;
+            for (int a = 0; a < 3; ++a)
+                p[a] += s * d[a];
+            size_t v;
+            if (!inside(w, p, &v)) {
+                st->e_escaped += wgt * E;
+                return;
+            }
+            st->n_visits++;
+            const int m = w->material[v];
+            if (m == OR_TRANSPARENT)
+                continue;
+            const double mu = w->density[v] * lerp_tab(w->tot + m * OR_NE, ie, fe);
+            if (rng_u(&r) * mmax < mu) {
+                if (!interact(w, v, m, &E, wgt, d, &r, st, &first))
+                    return;
+            }
+        } else {
+            /* regular tracking: walk voxel segments until the sampled optical depth is used up */
+            const double tau = -log(rng_u(&r));
+            int ie;
+            double fe;
+            grid_pos(E, &ie, &fe);
+            int64_t idx[2048];
+            double len[2048];
+            const int32_t* nn = w->n;
+            const int ns = or_siddon_f64(p, d, nn, w->sp, 2048, idx, len);
+            double acc = 0.0, t = 0.0;
+            int hit = -1;
+            double thit = 0.0;
+            for (int k = 0; k < (ns < 0 ? -ns : ns) && k < 2048; ++k) {
+                st->n_visits++;
+                const int m = w->material[idx[k]];
+                const double mu = m == OR_TRANSPARENT ? 0.0 : w->density[idx[k]] * lerp_tab(w->tot + m * OR_NE, ie, fe);
+                if (mu > 0.0 && acc + mu * len[k] >= tau) {
+                    hit = k;
+                    thit = t + (tau - acc) / mu;
+                    break;
+                }
+                acc += mu * len[k];
+                t += len[k];
+            }
+            if (hit < 0) {
+                st->e_escaped += wgt * E;
+                return;
+            }
+            for (int a = 0; a < 3; ++a) {
+                p[a] += thit * d[a];
+                if (p[a] < 0.0)
+                    p[a] = 0.0;
+                if (p[a] >= L[a])
+                    p[a] = nextafter(L[a], 0.0);
+            }
+            const size_t v = (size_t)idx[hit];
+            if (!interact(w, v, w->material[v], &E, wgt, d, &r, st, &first))
+                return;
+        }
+    }
+    st->n_errors++;
+}
+
+static void* worker(void* arg)
+{
+    run_ctx* c = (run_ctx*)arg;
+    or_stats st;
+    memset(&st, 0, sizeof(st));
+    for (;;) {
+        const uint64_t b = __atomic_fetch_add(&c->next, 4096, __ATOMIC_RELAXED);
+        if (b >= c->h1)
+            break;
+        const uint64_t e = b + 4096 < c->h1 ? b + 4096 : c->h1;
+        for (uint64_t h = b; h < e; ++h)
+            run_history(c, h, &st);
+    }
+    pthread_mutex_lock(&c->lock);
+    c->tot.e_source += st.e_source;
+    c->tot.e_deposited += st.e_deposited;
+    c->tot.e_escaped += st.e_escaped;
+    c->tot.n_histories += st.n_histories;
+    c->tot.n_missed += st.n_missed;
+    c->tot.n_visits += st.n_visits;
+    c->tot.n_real += st.n_real;
+    c->tot.n_photo += st.n_photo;
+    c->tot.n_compton += st.n_compton;
+    c->tot.n_rayleigh += st.n_rayleigh;
+    c->tot.n_deposits += st.n_deposits;
+    c->tot.n_cutoff += st.n_cutoff;
+    c->tot.n_errors += st.n_errors;
+    c->tot.n_interacted += st.n_interacted;
+    pthread_mutex_unlock(&c->lock);
+    return NULL;
+}
+
+static int ctx_setup(run_ctx* c, or_world* w, const or_beam* b)
+{
+    memset(c, 0, sizeof(*c));
+    c->w = w;
+    c->b = b;
+    c->n_exp = or_beam_exposures(b, NULL, 0);
+    if (c->n_exp <= 0 || b->particles_per_exposure == 0)
+        return -1;
+    c->exps = (or_exposure*)malloc(c->n_exp * sizeof(or_exposure));
+    or_beam_exposures(b, c->exps, c->n_exp);
+    for (int a = 0; a < 3; ++a)
+        c->gorigin[a] = -0.5 * w->n[a] * w->sp[a];
+    if (b->type != OR_BEAM_PENCIL) {
+        for (int t = 0; t < 2; ++t) {
+            double E[512], wt[512];
+            const int dual = b->type == OR_BEAM_CT_SPIRAL_DUAL && t == 1;
+            const int n = or_tube_spectrum(dual ? b->kvp_b : b->kvp, b->anode_angle_deg,
+                dual ? b->n_filters_b : b->n_filters, dual ? b->filter_Z_b : b->filter_Z,
+                dual ? b->filter_mm_b : b->filter_mm, E, wt, 512);
+            if (n <= 0) {
+                if (t == 0) {
+                    free(c->exps);
+                    c->exps = NULL;
+                    return -2;
+                }
+                c->spec[1] = c->spec[0];
+                continue;
+            }
+            build_alias(wt, n, &c->spec[t]);
+            memcpy(c->spec[t].E, E, n * sizeof(double));
+        }
+    }
+    if (b->n_bowtie > 0 && b->bowtie_angle && b->bowtie_weight) {
+        /* sort by angle (the bowtie JSON is unordered, bowtiefilters.json:4-32) */
+        int n = b->n_bowtie > 256 ? 256 : b->n_bowtie;
+        for (int i = 0; i < n; ++i) {
+            c->bow.ang[i] = b->bowtie_angle[i];
+            c->bow.w[i] = b->bowtie_weight[i];
+        }
+        for (int i = 1; i < n; ++i)
+            for (int j = i; j > 0 && c->bow.ang[j - 1] > c->bow.ang[j]; --j) {
+                double t = c->bow.ang[j];
+                c->bow.ang[j] = c->bow.ang[j - 1];
+                c->bow.ang[j - 1] = t;
+                t = c->bow.w[j];
+                c->bow.w[j] = c->bow.w[j - 1];
+                c->bow.w[j - 1] = t;
+            }
+        c->bow.n = n;
+        for (int t = 0; t < 2; ++t) {
+            double half = 0.0;
+            for (int i = 0; i < c->n_exp; ++i)
+                if (c->exps[i].tube == t) {
+                    half = c->exps[i].half[0];
+                    break;
+                }
+            c->bow.norm[t] = bowtie_mean(&c->bow, half);
+        }
+    }
+    return 0;
+}
+
+int or_transport(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, int tracking, int n_threads,
+    uint64_t hist_begin, uint64_t hist_end, or_stats* stats)
+{
+    run_ctx c;
+    const int rc = ctx_setup(&c, w, b);
+    if (rc != 0)
+        return rc;
+    c.seed = seed;
+    c.stream = stream;
+    c.tracking = tracking;
+    const uint64_t total = (uint64_t)c.n_exp * b->particles_per_exposure;
+    c.h0 = hist_begin;
+    c.h1 = hist_end < total ? hist_end : total;
+    c.next = c.h0;
+    pthread_mutex_init(&c.lock, NULL);
+    if (n_threads < 1)
+        n_threads = 1;
+    pthread_t* th = (pthread_t*)malloc(n_threads * sizeof(pthread_t));
+    for (int i = 0; i < n_threads; ++i)
+        pthread_create(&th[i], NULL, worker, &c);
+    for (int i = 0; i < n_threads; ++i)
+        pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&c.lock);
+    free(c.exps);
+    if (stats)
+        *stats = c.tot;
+    return 0;
+}
+
+int or_sample_source(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, uint64_t h0, int n, double* out8)
+{
+    run_ctx c;
+    const int rc = ctx_setup(&c, w, b);
+    if (rc != 0)
+        return rc;
+    for (int i = 0; i < n; ++i) {
+        rng_t r;
+        rng_stream(&r, seed, stream, h0 + i);
+        double E, wgt, p[3], d[3];
+        sample_source(&c, h0 + i, &r, &E, p, d, &wgt);
+        double* o = out8 + 8 * (size_t)i;
+        o[0] = E;
+        o[1] = wgt;
+        o[2] = p[0];
+        o[3] = p[1];
+        o[4] = p[2];
+        o[5] = d[0];
+        o[6] = d[1];
+        o[7] = d[2];
+    }
+    free(c.exps);
+    return 0;
+}

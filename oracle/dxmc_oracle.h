@@ -1,0 +1,165 @@
+/*
+ * dxmc_oracle.h -- CPU oracle for the photon-transport hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker, never the product: only the
+ * test-suite, the smoke check and the benchmark's CPU-baseline leg load it.
+ *
+ * It restates, in plain C with FP64 arithmetic, the path OpenDXMC reaches at
+ * src/libopendxmc/simulationpipeline.cpp:165 (`transport(world, beam, progress, true)`):
+ * world ingest (simulationpipeline.cpp:127-153), tube spectrum
+ * (ctsegmentationpipeline.cpp:66-71), beam -> exposures (dxmc_specialization.cpp:155-167,
+ * beamactorcontainer.cpp:211-236), per-history source sampling, voxel traversal,
+ * interaction sampling and per-voxel energy scoring (readback at
+ * simulationpipeline.cpp:174-231).
+ *
+ * PARITY UNPINNED: the arithmetic of that call lives in DXMClib, which is not part
+ * of the reference tree (CMakeLists.txt:68-75 fetches branch `develop`, no pinned
+ * commit) and ships no known-answer tests.  The oracle therefore restates the
+ * algorithm from the call sites, with a project-authored parametric physics model
+ * (documented in physics comments below), and is pinned against analytic known
+ * answers (Klein-Nishina integrals, Beer-Lambert transmission, energy
+ * conservation) and the reference's own data files (media.dat, bowtie JSON).
+ */
+#ifndef DXMC_ORACLE_H
+#define DXMC_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Energy grid of the attenuation tables: E_i = OR_EMIN + i * OR_DE keV. */
+#define OR_NE 300
+#define OR_EMIN 1.0
+#define OR_DE 0.5
+#define OR_MAX_ELEMENTS 16
+#define OR_TRANSPARENT 255
+
+enum { OR_TRACK_WOODCOCK = 0, OR_TRACK_SIDDON = 1 };
+enum {
+    OR_BEAM_DX = 0,
+    OR_BEAM_CT_SPIRAL = 1,
+    OR_BEAM_CT_SEQUENTIAL = 2,
+    OR_BEAM_CBCT = 3,
+    OR_BEAM_PENCIL = 4,
+    OR_BEAM_CT_SPIRAL_DUAL = 5
+};
+
+typedef struct {
+    int32_t n;
+    int32_t Z[OR_MAX_ELEMENTS];
+    double w[OR_MAX_ELEMENTS]; /* mass fractions, normalised on use */
+} or_composition;
+
+/* Beam parameters, the union of what the OpenDXMC beam setters carry
+ * (beamsettingsmodel.cpp:459-1837).  Geometry is in world cm, angles in radians
+ * unless the field name says deg. */
+typedef struct {
+    int32_t type;
+    double kvp;
+    double anode_angle_deg;
+    int32_t n_filters;
+    int32_t filter_Z[8];
+    double filter_mm[8];
+    uint64_t particles_per_exposure;
+    uint64_t n_exposures; /* DX / pencil: number of identical exposures ("jobs") */
+    /* DX, pencil, CT sequential */
+    double position[3];
+    double cosines[2][3];
+    double half_angles[2];
+    double energy_kev; /* pencil beam mono-energy */
+    /* CT */
+    double start[3];
+    double stop[3];
+    double start_angle_deg;
+    double stop_angle_deg;
+    double step_angle_deg;
+    double pitch;
+    double collimation_cm;
+    double scan_fov_cm;
+    double sdd_cm;
+    double rotation_axis[3];
+    int32_t n_slices; /* CT sequential: number of axial positions */
+    double slice_spacing_cm;
+    double kvp_b; /* dual energy: second tube */
+    int32_t n_filters_b;
+    int32_t filter_Z_b[8];
+    double filter_mm_b[8];
+    double tube_a_weight; /* dual energy: relative mAs of tube A */
+    double fov_b_cm;
+    /* bowtie (angle rad, weight), unsorted allowed */
+    int32_t n_bowtie;
+    const double* bowtie_angle;
+    const double* bowtie_weight;
+    /* AEC (CTAECFilter(start, stop, weights)) */
+    int32_t n_aec;
+    double aec_start[3];
+    double aec_stop[3];
+    const double* aec_weight;
+} or_beam;
+
+typedef struct {
+    double pos[3]; /* world cm */
+    double c0[3];
+    double c1[3];
+    double half[2];
+    double weight;
+    int32_t tube; /* 0 = A, 1 = B (dual energy) */
+} or_exposure;
+
+typedef struct {
+    double e_source, e_deposited, e_escaped;
+    uint64_t n_histories, n_missed, n_visits, n_real, n_photo, n_compton, n_rayleigh,
+        n_deposits, n_cutoff, n_errors, n_interacted;
+} or_stats;
+
+typedef struct or_world or_world;
+
+/* physics (per atom, barn; energies keV) */
+double or_atomic_mass(int Z);
+double or_element_density(int Z);
+double or_sigma_kn(double E);
+double or_sigma_photo(double E, int Z);
+double or_sigma_incoh(double E, int Z, int correction);
+double or_sigma_coh(double E, int Z);
+double or_kn_energy_transfer_fraction(double E);
+/* mass coefficients (cm^2/g) of a composition at arbitrary energies */
+void or_attenuation(const or_composition* c, int correction, int n, const double* E,
+    double* photo, double* incoh, double* coh);
+/* tube */
+int or_tube_spectrum(double kvp, double anode_angle_deg, int n_filters, const int32_t* fZ,
+    const double* fmm, double* energies, double* weights, int cap);
+double or_tube_mean_energy(double kvp, int n_filters, const int32_t* fZ, const double* fmm);
+double or_tube_al_hvl_mm(double kvp, int n_filters, const int32_t* fZ, const double* fmm);
+/* rng */
+void or_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+double or_uniform_from_u32(uint32_t x);
+/* beam geometry */
+int or_beam_exposures(const or_beam* b, or_exposure* out, int cap);
+/* traversal on a grid-local ray; returns number of segments (or -needed if cap too small) */
+int or_siddon_f32(const float o[3], const float d[3], const int32_t n[3], const float sp[3], int cap,
+    int64_t* idx, float* len);
+int or_siddon_f64(const double o[3], const double d[3], const int32_t n[3], const double sp[3], int cap,
+    int64_t* idx, double* len);
+/* samplers driven by injected uniforms (u consumed sequentially, *used returns count) */
+double or_sample_compton(double E, const or_composition* c, int correction, const double* u,
+    int nu, int* used, double* cos_theta);
+double or_sample_rayleigh(double E, const or_composition* c, const double* u, int nu, int* used);
+/* world */
+or_world* or_world_create(const int32_t dims[3], const double spacing_cm[3], const double* density,
+    const uint8_t* material, const or_composition* mats, int n_mats, int correction);
+void or_world_destroy(or_world* w);
+void or_world_clear(or_world* w);
+int or_world_table(const or_world* w, int m, double* photo, double* incoh, double* coh);
+int or_world_majorant(const or_world* w, double* maj);
+int or_transport(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, int tracking,
+    int n_threads, uint64_t hist_begin, uint64_t hist_end, or_stats* stats);
+int or_sample_source(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, uint64_t h0, int n,
+    double* out8);
+void or_world_tally(const or_world* w, double* energy, double* energy2, uint64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,118 @@
+"""CPU tests of the engine library: it builds, loads and exports every symbol
+include/dxmcg.h declares; its host-side FP64 physics, spectra and beam geometry
+agree with the oracle; it refuses bad input before touching a device."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from opendxmc_gb300 import phantoms as P
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    text = (ROOT / "include" / "dxmcg.h").read_text()
+    return sorted(set(re.findall(r"DXMCG_API[^;]*?\b(dxmcg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(engine):
+    from opendxmc_gb300 import native
+
+    lib = native.lib()
+    names = declared_functions()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+    assert sorted(native.EXPORTED) == names
+    assert lib.dxmcg_version() == 1
+
+
+def test_library_exports_nothing_else(engine):
+    import subprocess
+
+    from opendxmc_gb300 import native
+
+    out = subprocess.run(["nm", "-D", "--defined-only", str(native.LIB_PATH)], capture_output=True, text=True).stdout
+    ours = sorted({l.split()[-1] for l in out.splitlines() if " T dxmcg_" in l})
+    assert ours == declared_functions()
+
+
+@pytest.mark.parametrize("zw", [P.WATER, P.BONE, P.LUNG, P.AIR, P.ADIPOSE, {53: 1.0}, {74: 1.0}])
+@pytest.mark.parametrize("correction", [0, 1, 2])
+def test_host_attenuation_matches_oracle(engine, oracle, zw, correction):
+    E = np.concatenate([oracle.energy_grid(), [1.3, 33.17, 69.6, 149.9]])
+    a = oracle.attenuation(zw, E, correction)
+    b = engine.attenuation(zw, E, correction)
+    for x, y in zip(a, b):
+        np.testing.assert_allclose(y, x, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("kvp,filters", [(70.0, {13: 2.5}), (120.0, {13: 6.0}), (140.0, {13: 3.0, 29: 0.1}),
+                                         (80.0, {13: 9.0, 50: 0.4}), (150.0, {})])
+def test_tube_matches_oracle(engine, oracle, kvp, filters):
+    e1, w1 = oracle.tube_spectrum(kvp, filters)
+    e2, w2 = engine.tube_spectrum(kvp, filters)
+    np.testing.assert_array_equal(e1, e2)
+    np.testing.assert_allclose(w2, w1, rtol=1e-13, atol=1e-300)
+    assert engine.tube_mean_energy(kvp, filters) == pytest.approx(oracle.tube_mean_energy(kvp, filters), rel=1e-13)
+    assert engine.tube_al_hvl(kvp, filters) == pytest.approx(oracle.tube_al_hvl_mm(kvp, filters), rel=1e-12)
+
+
+BEAMS = {
+    "dx": P.dx_beam_params(particles=10, exposures=4),
+    "ct_spiral": P.ct_spiral_params(particles=10),
+    "ct_spiral_aec": dict(P.ct_spiral_params(particles=10, pitch=0.8, collimation_cm=8.0),
+                          aec=([0, 0, -10], [0, 0, 10], [1.0, 2.0, 0.5, 1.5])),
+    "ct_sequential": {"type": 2, "kvp": 120.0, "filters": {13: 6.0}, "particles_per_exposure": 10,
+                      "position": [0, 0, -3.0], "step_angle_deg": 10.0, "collimation_cm": 3.84, "scan_fov_cm": 50.0,
+                      "sdd_cm": 119.0, "n_slices": 3, "slice_spacing_cm": 3.84},
+    "cbct": {"type": 3, "kvp": 90.0, "filters": {13: 4.0}, "particles_per_exposure": 10, "position": [1.0, 0, 0],
+             "rotation_axis": [0, 0, 1], "start_angle_deg": -90.0, "stop_angle_deg": 90.0, "step_angle_deg": 2.0,
+             "sdd_cm": 120.0, "half_angles": [0.17, 0.17]},
+    "pencil": {"type": 4, "energy_kev": 60.0, "particles_per_exposure": 10, "n_exposures": 2,
+               "position": [0, 40, 0], "cosines": [[0, 0, 1], [-1, 0, 0]]},
+    "dual_energy": dict(P.ct_spiral_params(particles=10), type=5, kvp_b=140.0, filters_b={13: 6.0, 50: 0.4},
+                        tube_a_weight=0.4, fov_b_cm=33.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(BEAMS))
+def test_exposures_match_oracle(engine, oracle, name):
+    a = oracle.beam_exposures(BEAMS[name])
+    b = engine.beam_exposures(BEAMS[name])
+    assert len(a) == len(b) > 0
+    for x, y in zip(a, b):
+        for k in ("pos", "c0", "c1", "half"):
+            np.testing.assert_allclose(y[k], x[k], rtol=0, atol=1e-12)
+        assert y["weight"] == pytest.approx(x["weight"], rel=1e-13)
+        assert y["tube"] == x["tube"]
+
+
+def test_world_create_rejects_bad_input_on_host(engine):
+    from opendxmc_gb300 import native as N
+
+    lib = N.lib()
+    dims = (C.c_int32 * 3)(4, 4, 4)
+    sp = (C.c_double * 3)(0.1, 0.1, 0.1)
+    good = (N.Material * 1)(N.Material.from_dict(P.WATER))
+    h = C.c_void_p()
+    bad_dims = (C.c_int32 * 3)(4, 0, 4)
+    assert lib.dxmcg_world_create(bad_dims, sp, good, 1, 1, C.byref(h)) == -1
+    bad = N.Material()
+    bad.n = 1
+    bad.Z[0] = 200
+    bad.w[0] = 1.0
+    assert lib.dxmcg_world_create(dims, sp, (N.Material * 1)(bad), 1, 1, C.byref(h)) == -1
+    assert b"composition" in lib.dxmcg_last_error()
+    assert lib.dxmcg_world_create(dims, sp, good, 0, 1, C.byref(h)) == -1
+    assert lib.dxmcg_world_create(dims, sp, good, 1, 3, C.byref(h)) == -1
+
+
+def test_no_device_is_an_error_not_a_fallback(engine):
+    if engine.device_count() > 0:
+        pytest.skip("a device is visible")
+    with pytest.raises(Exception, match="NO_DEVICE"):
+        engine.GpuWorld((4, 4, 4), (0.1, 0.1, 0.1), [P.WATER])

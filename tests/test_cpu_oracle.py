@@ -1,0 +1,207 @@
+"""CPU tests of the oracle: pinned to the reference's own data files (golden
+fixtures) and to analytic known answers.  No GPU needed."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from opendxmc_gb300 import phantoms as P
+import parity
+
+GOLDEN = json.loads((Path(__file__).parent / "golden" / "reference_data.json").read_text())
+SIGMA_THOMSON = 8.0 * np.pi / 3.0 * 0.0794077878  # barn
+
+
+def as_zw(comp: dict) -> dict:
+    return {int(z): float(w) for z, w in comp.items()}
+
+
+@pytest.mark.parametrize("row,const", [("2", P.BONE), ("29", P.MUSCLE), ("45", P.SOFT_TISSUE),
+                                       ("49", P.ADIPOSE), ("50", P.LUNG), ("53", P.AIR)])
+def test_compositions_match_reference_media_table(row, const):
+    assert as_zw(GOLDEN["AM_media"][row]["composition"]) == {int(z): float(w) for z, w in const.items()}
+
+
+def test_water_and_bowtie_match_reference_files():
+    assert as_zw(GOLDEN["other_media"]["53"]["composition"]) == P.WATER
+    assert GOLDEN["other_media"]["53"]["name"] == "Water"
+    tpl = GOLDEN["bowtie_template"]["Siemens Definition Flash Body W3 120kV"]
+    assert [tuple(x) for x in tpl] == P.BODY_BOWTIE
+    assert "Siemens Definition Flash W1 120kV" in GOLDEN["bowtiefilters"]  # default key, beamsettingsmodel.cpp:1303
+    assert len(GOLDEN["bowtiefilters"]) == 41
+
+
+def test_klein_nishina_limits(oracle):
+    L = oracle.lib()
+    assert L.or_sigma_kn(0.01) == pytest.approx(SIGMA_THOMSON, rel=1e-4)
+    assert L.or_sigma_kn(100.0) < L.or_sigma_kn(10.0) < SIGMA_THOMSON
+    # level 0 is free-electron KN; binding (S < Z) only lowers it
+    for Z in (1, 8, 20):
+        for E in (5.0, 30.0, 100.0):
+            assert L.or_sigma_incoh(E, Z, 0) == pytest.approx(Z * L.or_sigma_kn(E), rel=1e-12)
+            assert L.or_sigma_incoh(E, Z, 1) < L.or_sigma_incoh(E, Z, 0)
+    # S saturates for hydrogen at high energy
+    assert L.or_sigma_incoh(150.0, 1, 1) / L.or_sigma_kn(150.0) > 0.99
+
+
+def test_rayleigh_low_energy_limit(oracle):
+    # F -> Z as x -> 0: sigma_coh -> Z^2 sigma_Thomson
+    L = oracle.lib()
+    for Z in (1, 8, 20):
+        assert L.or_sigma_coh(1e-3, Z) == pytest.approx(Z * Z * SIGMA_THOMSON, rel=1e-3)
+
+
+def test_water_attenuation_plausible(oracle):
+    p, ic, co = oracle.attenuation(P.WATER, [30.0, 60.0, 100.0])
+    tot = p + ic + co
+    # project model within 10 % of the textbook values 0.376 / 0.206 / 0.171 cm2/g
+    assert tot == pytest.approx([0.376, 0.206, 0.171], rel=0.10)
+    assert p[0] == pytest.approx(ic[0], rel=0.3)  # photo/Compton crossover near 30 keV
+
+
+def _chi2_p(hist, expected):
+    from scipy import stats
+
+    m = expected > 5
+    chi2 = float((((hist - expected) ** 2) / expected)[m].sum())
+    return stats.chi2.sf(chi2, m.sum() - 1)
+
+
+@pytest.mark.parametrize("E", [20.0, 80.0, 150.0])
+def test_compton_sampler_matches_klein_nishina(oracle, E):
+    rng = np.random.default_rng(7)
+    n = 20000
+    mus = np.array([oracle.sample_compton(E, {8: 1.0}, 0, rng.random(64))[1] for _ in range(n)])
+    k = E / 510.99895
+    edges = np.linspace(-1, 1, 41)
+    x = np.linspace(-1, 1, 4001)
+    eps = 1 / (1 + k * (1 - x))
+    pdf = eps ** 2 * (eps + 1 / eps - (1 - x * x))
+    cdf = np.concatenate([[0], np.cumsum(0.5 * (pdf[1:] + pdf[:-1]) * np.diff(x))])
+    cdf /= cdf[-1]
+    expected = np.diff(np.interp(edges, x, cdf)) * n
+    hist, _ = np.histogram(mus, edges)
+    assert _chi2_p(hist, expected) > 1e-4
+
+
+def test_compton_with_incoherent_function_suppresses_forward(oracle):
+    rng = np.random.default_rng(9)
+    E = 20.0
+    mu0 = np.array([oracle.sample_compton(E, P.WATER, 0, rng.random(256))[1] for _ in range(5000)])
+    mu1 = np.array([oracle.sample_compton(E, P.WATER, 1, rng.random(256))[1] for _ in range(5000)])
+    assert (mu1 > 0.95).mean() < 0.5 * (mu0 > 0.95).mean()
+
+
+def test_rayleigh_sampler_matches_form_factor(oracle):
+    rng = np.random.default_rng(11)
+    E, Z = 40.0, 8
+    n = 20000
+    mus = np.array([oracle.sample_rayleigh(E, {Z: 1.0}, rng.random(128))[0] for _ in range(n)])
+    a = (Z ** (1 / 3) / (2 * np.pi * 0.529177210903)) ** 2
+    q = E / 12.398419843
+    x = np.linspace(-1, 1, 20001)
+    t = q * q * (1 - x) / 2
+    pdf = (1 + x * x) / (1 + t / a) ** 4
+    cdf = np.concatenate([[0], np.cumsum(0.5 * (pdf[1:] + pdf[:-1]) * np.diff(x))])
+    cdf /= cdf[-1]
+    edges = np.concatenate([np.linspace(-1, 0.9, 20), np.linspace(0.91, 1, 10)])
+    expected = np.diff(np.interp(edges, x, cdf)) * n
+    hist, _ = np.histogram(mus, edges)
+    assert _chi2_p(hist, expected) > 1e-4
+
+
+def test_philox_uniforms(oracle):
+    from scipy import stats
+
+    u = np.array([oracle.lib().or_uniform_from_u32(x) for x in
+                  np.array([oracle.philox([i, 0, 5, 0], [1, 0]) for i in range(5000)], dtype=np.uint32).ravel()])
+    assert u.min() > 0 and u.max() < 1
+    assert stats.kstest(u, "uniform").pvalue > 1e-3
+    assert oracle.lib().or_uniform_from_u32(0) == 2.0 ** -24
+    assert oracle.lib().or_uniform_from_u32(0xFFFFFFFF) == 1.0 - 2.0 ** -24
+
+
+def test_tube_spectrum_properties(oracle):
+    E, w = oracle.tube_spectrum(120.0, {13: 6.0})
+    assert E[0] == 1.0 and E[-1] == 120.0 and len(E) == 120
+    assert w.sum() == pytest.approx(1.0, abs=1e-12)
+    assert w[57] > w[55] and w[58] > w[60]  # tungsten K lines at 58 and 59 keV
+    assert oracle.tube_mean_energy(120, {13: 9.0}) > oracle.tube_mean_energy(120, {13: 6.0})
+    assert oracle.tube_al_hvl_mm(120, {13: 9.0}) > oracle.tube_al_hvl_mm(120, {13: 6.0})
+    assert 4.0 < oracle.tube_al_hvl_mm(120, {13: 6.0}) < 9.0
+
+
+def test_ct_spiral_exposure_geometry(oracle):
+    cp = P.ct_spiral_params(particles=1)
+    ex = oracle.beam_exposures(cp)
+    assert len(ex) == 360  # 20 cm / (4 cm x pitch 1) x 72 views
+    sid = 119.0 / 2
+    for i, e in enumerate(ex[:80]):
+        pos, c0, c1 = map(np.array, (e["pos"], e["c0"], e["c1"]))
+        iso = np.array([0.0, 0.0, -10.0 + i * 4.0 / 72])
+        assert np.linalg.norm((pos - iso)[:2]) == pytest.approx(sid)
+        assert pos[2] == pytest.approx(iso[2])
+        n = np.cross(c0, c1)
+        assert np.dot(n, (iso - pos) / sid) == pytest.approx(1.0)
+        assert np.dot(c0, c1) == pytest.approx(0.0, abs=1e-12)
+    assert ex[0]["half"][0] == pytest.approx(np.arctan(25.0 / sid))
+    assert ex[0]["half"][1] == pytest.approx(np.arctan(2.0 / sid))
+
+
+def test_dx_pose_matches_reference_dxbeam(oracle):
+    # DXBeam at 0/0 deg: source at rotation centre + SPD * (0, 1, 0), beam along -y
+    ex = oracle.beam_exposures(P.dx_beam_params(particles=1, exposures=3))
+    assert len(ex) == 3
+    n = np.cross(ex[0]["c0"], ex[0]["c1"])
+    assert np.allclose(n, [0, -1, 0]) and np.allclose(ex[0]["pos"], [0, 100, 0])
+
+
+def test_aec_weights_are_relative(oracle):
+    cp = P.ct_spiral_params(particles=1)
+    cp["aec"] = ([0, 0, -10], [0, 0, 10], [1.0, 3.0])
+    w = np.array([e["weight"] for e in oracle.beam_exposures(cp)])
+    assert w.mean() == pytest.approx(1.0)
+    assert w[-1] / w[0] == pytest.approx(3.0, rel=0.02)
+
+
+def test_oracle_energy_conservation(oracle):
+    ph = parity.small_cylinder()
+    w = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    st = w.run(P.dx_beam_params(particles=2000, exposures=5), threads=4)
+    e, _, _ = w.tally()
+    assert st["n_histories"] == 10000 and st["n_errors"] == 0
+    assert e.sum() + st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-12)
+    assert e.sum() == pytest.approx(st["e_deposited"], rel=1e-12)
+
+
+def test_oracle_beer_lambert_transmission(oracle):
+    # 60 keV pencil beam through 10 cm of water: P(no interaction) = exp(-mu L)
+    dims = (4, 40, 4)
+    dens = np.ones(dims[::-1])
+    mat = np.zeros(dims[::-1], dtype=np.uint8)
+    w = oracle.World(dims, (0.25, 0.25, 0.25), dens, mat, [P.WATER])
+    n = 40000
+    beam = {"type": oracle.BEAM_PENCIL, "energy_kev": 60.0, "particles_per_exposure": n, "n_exposures": 1,
+            "position": [0.0, 50.0, 0.0], "cosines": [[0, 0, 1], [-1, 0, 0]]}
+    st = w.run(beam, threads=4)
+    p, ic, co = oracle.attenuation(P.WATER, [60.0])
+    trans = np.exp(-(p + ic + co)[0] * 1.0 * 10.0)
+    measured = 1.0 - st["n_interacted"] / n
+    assert measured == pytest.approx(trans, abs=4 * np.sqrt(trans * (1 - trans) / n))
+
+
+def test_oracle_woodcock_and_siddon_tracking_agree(oracle):
+    ph = parity.small_cylinder()
+    w = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    beam = P.dx_beam_params(particles=20000, exposures=5)
+    s1 = w.run(beam, tracking=oracle.TRACK_WOODCOCK, threads=8)
+    e1, q1, _ = w.tally()
+    w.clear()
+    s2 = w.run(beam, tracking=oracle.TRACK_SIDDON, threads=8, stream=1)
+    e2, q2, _ = w.tally()
+    n = s1["n_histories"]
+    frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
+                                                 parity.tally_variance(e2, q2, n))
+    assert nvox > 100 and frac >= 0.99
+    assert e1.sum() == pytest.approx(e2.sum(), rel=0.01)

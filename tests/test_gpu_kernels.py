@@ -1,0 +1,128 @@
+"""GPU tests of the hot-path pieces run alone through the C ABI, against the
+oracle on identical inputs: Philox streams, Siddon traversal (bit-exact),
+interaction samplers fed identical uniforms, source sampling."""
+import numpy as np
+import pytest
+
+from opendxmc_gb300 import phantoms as P
+import parity
+
+pytestmark = pytest.mark.gpu
+
+
+def test_philox_bit_exact(gpu, oracle):
+    rng = np.random.default_rng(1)
+    ctr = rng.integers(0, 2 ** 32, size=(4096, 4), dtype=np.uint64).astype(np.uint32)
+    for key in ([0, 0], [1, 0], [0xDEADBEEF, 0x12345678], [0xFFFFFFFF, 0xFFFFFFFF]):
+        out = gpu.philox(ctr, key)
+        ref = np.array([oracle.philox(c, key) for c in ctr[:512]], dtype=np.uint32)
+        np.testing.assert_array_equal(out[:512], ref)
+
+
+def _rays(rng, n, L):
+    """Rays starting within a few cm of the grid box, aimed at random inner points,
+    plus axis-aligned, diagonal and corner-tie cases and rays starting inside."""
+    L = np.asarray(L)
+    tgt = rng.uniform(0.05, 0.95, (n, 3)) * L
+    org = L / 2 + rng.normal(0, 1, (n, 3)) * L
+    org[: n // 4] = rng.uniform(0, 1, (n // 4, 3)) * L  # start inside
+    d = tgt - org
+    d[n // 4: n // 4 + 16] = np.eye(3)[rng.integers(0, 3, 16)] * rng.choice([-1, 1], (16, 1))
+    d[n // 4 + 16: n // 4 + 32] = rng.choice([-1, 1], (16, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return org.astype(np.float32), d.astype(np.float32)
+
+
+@pytest.mark.parametrize("dims,spacing", [((37, 23, 19), (0.3, 0.25, 0.5)), ((64, 64, 64), (0.125, 0.125, 0.125)),
+                                          ((256, 256, 200), (0.15, 0.15, 0.15))])
+def test_siddon_bit_exact_and_path_lengths(gpu, oracle, dims, spacing):
+    rng = np.random.default_rng(sum(dims))
+    L = np.array(dims) * np.array(spacing)
+    org, d = _rays(rng, 400, L)
+    # corner ties: rays through exact voxel corners
+    org[-8:] = np.float32(0.0)
+    d[-8:] = np.array([1, 1, 1], np.float32) / np.float32(np.sqrt(3))
+    got = gpu.siddon_trace(org, d, dims, spacing)
+    same64 = 0
+    hits = 0
+    for r in range(len(org)):
+        i32, l32 = oracle.siddon_f32(org[r], d[r], dims, np.float32(spacing))
+        gi, gl = got[r]
+        np.testing.assert_array_equal(gi, i32)
+        np.testing.assert_array_equal(gl, l32)  # bit for bit
+        i64, l64 = oracle.siddon_f64(org[r].astype(np.float64), d[r].astype(np.float64), dims,
+                                     np.float64(np.float32(spacing)))
+        if len(i64):
+            hits += 1
+            chord = l64.sum()
+            assert abs(gl.astype(np.float64).sum() - chord) <= 1e-6 * chord + 1e-6
+            if len(i64) == len(gi) and np.array_equal(i64, gi):
+                same64 += 1
+                assert np.max(np.abs(gl - l64)) <= 1e-6 * max(chord, 1.0)
+    assert hits > 300
+    assert same64 >= 0.99 * hits
+
+
+COMPOSITIONS = [P.WATER, P.BONE, P.LUNG, {53: 1.0}]
+
+
+@pytest.mark.parametrize("correction", [0, 1])
+@pytest.mark.parametrize("zw", COMPOSITIONS)
+def test_compton_sampler_matches_oracle(gpu, oracle, zw, correction):
+    rng = np.random.default_rng(5 + correction)
+    n, stride = 4000, 96
+    E = rng.uniform(1.0, 150.0, n)
+    U = parity.uniforms_f32_exact(rng, (n, stride))
+    eg, cg, ug = gpu.sample_compton(E, zw, correction, U)
+    same = 0
+    for i in range(n):
+        eo, co, uo = oracle.sample_compton(E[i], zw, correction, U[i])
+        if uo != ug[i]:
+            continue  # a comparison rounded the other way: different branch
+        same += 1
+        assert abs(eg[i] - eo) <= 1e-6 * eo
+        assert abs(cg[i] - co) <= 1e-6
+    assert same >= 0.998 * n
+
+
+@pytest.mark.parametrize("zw", COMPOSITIONS)
+def test_rayleigh_sampler_matches_oracle(gpu, oracle, zw):
+    rng = np.random.default_rng(17)
+    n, stride = 4000, 96
+    E = rng.uniform(1.0, 150.0, n)
+    U = parity.uniforms_f32_exact(rng, (n, stride))
+    cg, ug = gpu.sample_rayleigh(E, zw, U)
+    same = 0
+    for i in range(n):
+        co, uo = oracle.sample_rayleigh(E[i], zw, U[i])
+        if uo != ug[i]:
+            continue
+        same += 1
+        assert abs(cg[i] - co) <= 1e-6
+    assert same >= 0.998 * n
+
+
+@pytest.mark.parametrize("which", ["dx", "ct_bowtie", "pencil"])
+def test_source_sampling_matches_oracle(gpu, oracle, which):
+    ph = parity.small_torso()
+    if which == "dx":
+        beam = P.dx_beam_params(particles=500, exposures=8)
+    elif which == "ct_bowtie":
+        beam = P.ct_spiral_params(particles=50)
+    else:
+        beam = {"type": 4, "energy_kev": 55.5, "particles_per_exposure": 1000, "n_exposures": 4,
+                "position": [1.0, 40.0, -2.0], "cosines": [[0, 0, 1], [-1, 0, 0]]}
+    gw = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    gw.set_data(ph.density, ph.material)
+    gw.build()
+    ow = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    n = 4000
+    g = gw.sample_source(beam, n, gpu.run_options(seed=99, stream=3))
+    o = oracle.sample_source(ow, beam, n, seed=99, stream=3)
+    np.testing.assert_array_equal(g[:, 0], o[:, 0])  # energies: integer alias draw, exact
+    np.testing.assert_allclose(g[:, 1], o[:, 1], rtol=2e-6)
+    np.testing.assert_allclose(g[:, 2:5], o[:, 2:5], atol=2e-5)
+    np.testing.assert_allclose(g[:, 5:8], o[:, 5:8], atol=2e-6)
+    if which == "ct_bowtie":
+        assert g[:, 1].std() > 0.1  # bowtie weights vary across the fan
+        assert g[:, 1].mean() == pytest.approx(1.0, rel=0.05)

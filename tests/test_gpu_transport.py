@@ -1,0 +1,275 @@
+"""GPU transport parity against the CPU oracle, through the C ABI.
+
+Two kinds of comparison:
+  * independent streams (different Philox stream words): per-voxel energy
+    imparted within 3 combined standard errors in >= 99 % of voxels above 5 % of
+    the maximum, total energy within 0.3 %;
+  * shared streams (same seed and stream): the GPU (FP32 tracking) and the
+    oracle (FP64) draw the same uniforms per history, so totals agree far more
+    tightly; what is left is FP32 vs FP64 rounding flipping a few decisions.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from opendxmc_gb300 import phantoms as P
+import parity
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_world(gpu, ph, correction=1):
+    w = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials, correction)
+    w.set_data(ph.density, ph.material)
+    w.build()
+    return w
+
+
+def oracle_world_on_packed(oracle, gw, ph, correction=1):
+    """Oracle world fed the densities exactly as the device stores them."""
+    d, m = gw.packed_density()
+    np.testing.assert_array_equal(m, ph.material.ravel())
+    assert np.max(np.abs(d.astype(np.float64) / ph.density.ravel() - 1)) <= 2.0 ** -16
+    return oracle.World(ph.dims, ph.spacing, d.astype(np.float64), ph.material, ph.materials, correction)
+
+
+def compare(gw, ow, n_hist):
+    e1, q1, c1 = gw.tally()
+    e2, q2, c2 = ow.tally()
+    frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n_hist), e2,
+                                                 parity.tally_variance(e2, q2, n_hist))
+    return frac, nvox, e1, e2
+
+
+@pytest.fixture(scope="module")
+def c1(gpu, oracle):
+    """Water cylinder with bone insert, 128x128x64 at 1 x 1 x 2.5 mm, DX 70 kVp."""
+    ph = P.water_cylinder_phantom()
+    gw = gpu_world(gpu, ph)
+    ow = oracle_world_on_packed(oracle, gw, ph)
+    return ph, gw, ow
+
+
+def test_c1_dx_independent_streams(c1, gpu):
+    ph, gw, ow = c1
+    gw.clear()
+    ow.clear()
+    beam = P.dx_beam_params(particles=1_000_000, exposures=10)  # 1e7 histories from seed 1
+    sg = gw.run(beam, gpu.run_options(seed=1, stream=0))
+    so = ow.run(beam, seed=1, stream=1)
+    assert sg["n_histories"] == so["n_histories"] == 10_000_000
+    assert sg["n_errors"] == 0
+    frac, nvox, e1, e2 = compare(gw, ow, 10_000_000)
+    assert nvox > 10000
+    assert frac >= 0.99, frac
+    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+
+
+def test_c1_dx_shared_streams(c1, gpu):
+    ph, gw, ow = c1
+    gw.clear()
+    ow.clear()
+    beam = P.dx_beam_params(particles=200_000, exposures=10)
+    sg = gw.run(beam, gpu.run_options(seed=7, stream=2))
+    so = ow.run(beam, seed=7, stream=2)
+    for k in ("n_histories", "n_missed"):
+        assert sg[k] == so[k]
+    # decisions agree except where FP32 and FP64 round a comparison differently
+    for k in ("n_photo", "n_compton", "n_rayleigh", "n_interacted"):
+        assert sg[k] == pytest.approx(so[k], rel=2e-3), k
+    e1, _, c1_ = gw.tally()
+    e2, _, c2 = ow.tally()
+    assert e1.sum() == pytest.approx(e2.sum(), rel=2e-3)
+    assert np.mean(c1_ == c2) > 0.99
+
+
+def test_energy_conservation(c1, gpu):
+    ph, gw, ow = c1
+    gw.clear()
+    st = gw.run(P.dx_beam_params(particles=100_000, exposures=10), gpu.run_options(seed=3))
+    e, _, _ = gw.tally()
+    assert st["e_deposited"] == pytest.approx(e.sum(), rel=1e-9)
+    assert e.sum() + st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-5)
+
+
+def test_counts_deterministic_and_shardable(c1, gpu):
+    """Event counts are integers: identical across runs, launch shapes, chunking
+    and history-range splits (the basis of multi-GPU replicas)."""
+    ph, gw, ow = c1
+    beam = P.dx_beam_params(particles=50_000, exposures=4)
+    gw.clear()
+    gw.run(beam, gpu.run_options(seed=5))
+    e_a, _, c_a = gw.tally()
+    gw.clear()
+    gw.run(beam, gpu.run_options(seed=5, block_size=128, blocks_per_sm=3, chunk_log2=14))
+    e_b, _, c_b = gw.tally()
+    gw.clear()
+    gw.run(beam, gpu.run_options(seed=5, hist_begin=0, hist_end=77_777))
+    gw.run(beam, gpu.run_options(seed=5, hist_begin=77_777, hist_end=0))
+    e_c, _, c_c = gw.tally()
+    np.testing.assert_array_equal(c_a, c_b)
+    np.testing.assert_array_equal(c_a, c_c)
+    np.testing.assert_allclose(e_b, e_a, rtol=1e-9)
+    np.testing.assert_allclose(e_c, e_a, rtol=1e-9)
+
+
+def test_c2_spiral_ct_torso_independent_streams(gpu, oracle):
+    ph = P.torso_phantom(seed=1)
+    gw = gpu_world(gpu, ph)
+    ow = oracle_world_on_packed(oracle, gw, ph)
+    beam = P.ct_spiral_params(particles=8000)  # 360 exposures -> 2.88e6 histories
+    sg = gw.run(beam, gpu.run_options(seed=11, stream=0))
+    so = ow.run(beam, seed=11, stream=1)
+    n = sg["n_histories"]
+    assert n == so["n_histories"] == 360 * 8000
+    frac, nvox, e1, e2 = compare(gw, ow, n)
+    assert nvox > 2000
+    assert frac >= 0.99, frac
+    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+
+
+def test_siddon_tracking_matches_woodcock(gpu):
+    ph = parity.small_torso(scale=2)
+    gw = gpu_world(gpu, ph)
+    beam = P.ct_spiral_params(particles=2000, scan_cm=10.0)
+    s1 = gw.run(beam, gpu.run_options(seed=1, tracking=0))
+    e1, q1, _ = gw.tally()
+    gw.clear()
+    s2 = gw.run(beam, gpu.run_options(seed=1, stream=9, tracking=1))
+    e2, q2, _ = gw.tally()
+    n = s1["n_histories"]
+    frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
+                                                 parity.tally_variance(e2, q2, n))
+    assert nvox > 500 and frac >= 0.99
+    assert e1.sum() == pytest.approx(e2.sum(), rel=5e-3)
+    assert s2["n_visits"] > s1["n_visits"]  # exact stepping visits every voxel on the path
+
+
+def test_siddon_tracking_matches_oracle(gpu, oracle):
+    ph = parity.small_cylinder()
+    gw = gpu_world(gpu, ph)
+    ow = oracle_world_on_packed(oracle, gw, ph)
+    beam = P.dx_beam_params(particles=100_000, exposures=4)
+    sg = gw.run(beam, gpu.run_options(seed=2, stream=0, tracking=1))
+    ow.run(beam, seed=2, stream=1, tracking=oracle.TRACK_SIDDON)
+    frac, nvox, e1, e2 = compare(gw, ow, sg["n_histories"])
+    assert nvox > 500 and frac >= 0.99
+    assert e1.sum() == pytest.approx(e2.sum(), rel=5e-3)
+
+
+def test_beer_lambert_transmission(gpu, oracle):
+    dims = (4, 40, 4)
+    ph = P.Phantom(dims, (0.25, 0.25, 0.25), np.ones(dims[::-1]), np.zeros(dims[::-1], np.uint8), [P.WATER])
+    gw = gpu_world(gpu, ph)
+    n = 1_000_000
+    beam = {"type": 4, "energy_kev": 60.0, "particles_per_exposure": n, "n_exposures": 1,
+            "position": [0.0, 50.0, 0.0], "cosines": [[0, 0, 1], [-1, 0, 0]]}
+    st = gw.run(beam)
+    xs, _ = gw.tables(0)
+    mu = float(xs[(60 - 1) * 2, 3])  # 60 keV is a grid node
+    trans = np.exp(-mu * 10.0)
+    measured = 1.0 - st["n_interacted"] / n
+    assert measured == pytest.approx(trans, abs=5 * np.sqrt(trans * (1 - trans) / n))
+
+
+def test_device_tables_match_oracle(gpu, oracle):
+    ph = parity.small_torso()
+    gw = gpu_world(gpu, ph)
+    ow = oracle_world_on_packed(oracle, gw, ph)
+    for m in range(len(ph.materials)):
+        xs, maj = gw.tables(m)
+        p, ic, co = ow.table(m)
+        np.testing.assert_allclose(xs[:, 0], p, rtol=1e-6)
+        np.testing.assert_allclose(xs[:, 1], ic, rtol=1e-6)
+        np.testing.assert_allclose(xs[:, 2], co, rtol=1e-6)
+    np.testing.assert_allclose(maj, ow.majorant(), rtol=1e-6)
+
+
+def test_dose_readout(c1, gpu):
+    ph, gw, ow = c1
+    gw.clear()
+    st = gw.run(P.dx_beam_params(particles=20_000, exposures=5))
+    e, e2, c = gw.tally()
+    d, v, c2 = gw.dose()
+    np.testing.assert_array_equal(c, c2)
+    rho, _ = gw.packed_density()
+    vol = np.prod(ph.spacing)
+    scale = st["dose_scale"]
+    assert scale == pytest.approx(1.602176634e-10 / vol)
+    np.testing.assert_allclose(d, e * scale / rho.astype(np.float64), rtol=1e-12)
+    var = np.maximum(e2 - e * e / st["n_histories"], 0) * (scale / rho.astype(np.float64)) ** 2
+    np.testing.assert_allclose(v, var, rtol=1e-9, atol=1e-300)
+
+
+def test_invalid_material_index_rejected(gpu):
+    ph = parity.small_cylinder()
+    mat = ph.material.copy()
+    mat[3, 3, 3] = 7  # only 3 materials
+    w = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    w.set_data(ph.density, mat)
+    with pytest.raises(Exception, match="material index"):
+        w.build()
+
+
+def test_invalid_density_rejected(gpu):
+    ph = parity.small_cylinder()
+    dens = ph.density.copy()
+    dens[1, 2, 3] = np.nan
+    w = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    w.set_data(dens, ph.material)
+    with pytest.raises(Exception, match="density"):
+        w.build()
+
+
+def test_transparent_material_is_skipped(gpu):
+    ph = parity.small_cylinder()
+    mat = np.full_like(ph.material, 255)
+    gw = gpu_world(gpu, P.Phantom(ph.dims, ph.spacing, ph.density, mat, ph.materials))
+    st = gw.run(P.dx_beam_params(particles=10_000, exposures=2))
+    e, _, _ = gw.tally()
+    assert e.sum() == 0 and st["n_interacted"] == 0
+    assert st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-6)
+
+
+def test_cancel_stops_between_launches(gpu):
+    ph = parity.small_cylinder()
+    gw = gpu_world(gpu, ph)
+    prog = gpu.Progress()
+    prog.setStopSimulation()
+    rc, st = gw.run_status(P.dx_beam_params(particles=100_000, exposures=10), gpu.run_options(chunk_log2=14),
+                           prog)
+    assert rc == -4 and st["n_histories"] == 0
+    assert not prog.continueSimulation()
+    # stop from another thread while the run is in flight
+    prog2 = gpu.Progress()
+    res = {}
+
+    def work():
+        res["rc"], res["st"] = gw.run_status(P.dx_beam_params(particles=10_000_000, exposures=10),
+                                             gpu.run_options(chunk_log2=16), prog2)
+
+    t = threading.Thread(target=work)
+    t.start()
+    for _ in range(2000):
+        done, total = prog2.progress()
+        if done > 0:
+            break
+        time.sleep(0.005)
+    prog2.setStopSimulation()
+    t.join(timeout=120)
+    assert not t.is_alive()
+    assert res["rc"] in (-4, 0)
+    if res["rc"] == -4:
+        assert res["st"]["n_histories"] < 100_000_000
+        assert prog2.message() == "Cancelled"
+
+
+def test_progress_reports_histories(gpu):
+    ph = parity.small_cylinder()
+    gw = gpu_world(gpu, ph)
+    prog = gpu.Progress()
+    gw.run(P.dx_beam_params(particles=100_000, exposures=3), gpu.run_options(chunk_log2=15), prog)
+    assert prog.progress() == (300_000, 300_000)
+    assert prog.message() == "Done"

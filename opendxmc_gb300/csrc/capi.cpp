@@ -370,7 +370,9 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o)
     LaunchShape s;
     s.block = o.block_size > 0 ? o.block_size : 256;
     s.block = std::max(32, std::min(256, s.block / 32 * 32));
-    const int per = o.blocks_per_sm > 0 ? o.blocks_per_sm : std::max(1, 2048 / s.block);
+    // one wave of resident blocks: the kernel is persistent and pulls work from its queue
+    const int resident = transportMaxBlocksPerSM(s.block);
+    const int per = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, resident) : resident;
     s.grid = std::max(1, sms) * per;
     return s;
 }

@@ -129,6 +129,7 @@ cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, co
     float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s);
 int transportRegistersPerThread();
+int transportMaxBlocksPerSM(int block);
 
 // host helpers (geometry.cpp)
 int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out);

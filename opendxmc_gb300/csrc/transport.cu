@@ -188,8 +188,16 @@ namespace {
                 if (target <= acc)
                     break;
             }
+            // t = a ((1 - y)^(-1/3) - 1), y = r2 c.  For y >= 1/2, 1 - y is formed as
+            // (1 - r2) + r2 (1 + T/a)^-3 (1 - r2 is exact) so FP32 keeps its precision.
             const float y = r2 * c;
-            const float t = a * expm1f(-log1pf(-y) / 3.0f);
+            float t;
+            if (y < 0.5f) {
+                t = a * expm1f(-log1pf(-y) / 3.0f);
+            } else {
+                const float omy = (1.0f - r2) + r2 * expf(-3.0f * log1pf(T / a));
+                t = a * expm1f(-logf(omy) / 3.0f);
+            }
             const float mu = 1.0f - 2.0f * t / T;
             if (2.0f * r3 <= 1.0f + mu * mu)
                 return mu;
@@ -225,9 +233,19 @@ namespace {
     // Exact voxel stepping in grid-local coordinates; the FP32 operation order is
     // fixed with _rn intrinsics (no FMA contraction) so that a host restatement
     // compiled without contraction produces the same voxel sequence bit for bit.
+    // Ray parameter of the crossing with the plane k * sp; the plane position is a
+    // double-float (hi + fma remainder) so grazing rays do not amplify its rounding.
+    __device__ __forceinline__ float crossF32(int k, float sp, float o, float d)
+    {
+        const float kf = __int2float_rn(k);
+        const float hi = __fmul_rn(kf, sp);
+        const float lo = __fmaf_rn(kf, sp, -hi);
+        return __fdiv_rn(__fadd_rn(__fsub_rn(hi, o), lo), d);
+    }
+
     struct Siddon {
         int i[3], st[3];
-        float o[3], inv[3], sp[3];
+        float o[3], d[3], sp[3];
         float t, tmax;
         int n[3];
 
@@ -241,11 +259,10 @@ namespace {
                 n[a] = dims[a];
                 sp[a] = spacing[a];
                 o[a] = org[a];
-                const float L = __fmul_rn(__int2float_rn(dims[a]), spacing[a]);
+                d[a] = dir[a];
                 if (dir[a] != 0.0f) {
-                    inv[a] = __frcp_rn(dir[a]);
-                    float t1 = __fmul_rn(__fsub_rn(0.0f, org[a]), inv[a]);
-                    float t2 = __fmul_rn(__fsub_rn(L, org[a]), inv[a]);
+                    float t1 = crossF32(0, spacing[a], org[a], dir[a]);
+                    float t2 = crossF32(dims[a], spacing[a], org[a], dir[a]);
                     if (t1 > t2) {
                         const float tt = t1;
                         t1 = t2;
@@ -255,10 +272,8 @@ namespace {
                         tmin = t1;
                     if (t2 < tmax)
                         tmax = t2;
-                } else {
-                    inv[a] = 0.0f;
-                    if (org[a] < 0.0f || org[a] >= L)
-                        return false;
+                } else if (org[a] < 0.0f || org[a] >= __fmul_rn(__int2float_rn(dims[a]), spacing[a])) {
+                    return false;
                 }
             }
             if (!(tmin < tmax))
@@ -282,9 +297,7 @@ namespace {
             float tn[3];
 #pragma unroll
             for (int a = 0; a < 3; ++a)
-                tn[a] = st[a] != 0
-                    ? __fmul_rn(__fsub_rn(__fmul_rn(__int2float_rn(i[a] + (st[a] > 0 ? 1 : 0)), sp[a]), o[a]), inv[a])
-                    : FLT_MAX;
+                tn[a] = st[a] != 0 ? crossF32(i[a] + (st[a] > 0 ? 1 : 0), sp[a], o[a], d[a]) : FLT_MAX;
             int ax = 0;
             if (tn[1] < tn[ax])
                 ax = 1;
@@ -870,6 +883,14 @@ cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, 
 {
     sourceKernel<<<(n + 127) / 128, 128, 0, s>>>(job, h0, n, out8);
     return cudaGetLastError();
+}
+
+int transportMaxBlocksPerSM(int block)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transportKernel, block, 0) != cudaSuccess)
+        return 1;
+    return n > 0 ? n : 1;
 }
 
 int transportRegistersPerThread()

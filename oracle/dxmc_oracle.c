@@ -575,17 +575,26 @@ int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
  * [0, n_a * sp_a) on each axis).  The FP32 variant fixes the operation order so
  * that the device traversal reproduces it bit for bit.                        */
 /* ------------------------------------------------------------------------- */
+/* Ray parameter where the ray o + t d crosses the plane at k * sp.  The plane
+ * position is carried as a double-float (hi + fma remainder) so that its FP32
+ * rounding is not amplified by 1/|d| on grazing rays: the result is within about
+ * one ulp of t.  Division, not a rounded reciprocal. */
+static float cross_f32(int k, float sp, float o, float d)
+{
+    const float kf = (float)k;
+    const float hi = kf * sp;
+    const float lo = fmaf(kf, sp, -hi);
+    return ((hi - o) + lo) / d;
+}
+
 int or_siddon_f32(const float o[3], const float d[3], const int32_t n[3], const float sp[3], int cap,
     int64_t* idx, float* len)
 {
-    float L[3], inv[3];
     float tmin = 0.0f, tmax = FLT_MAX;
     for (int a = 0; a < 3; ++a) {
-        L[a] = (float)n[a] * sp[a];
         if (d[a] != 0.0f) {
-            inv[a] = 1.0f / d[a];
-            float t1 = (0.0f - o[a]) * inv[a];
-            float t2 = (L[a] - o[a]) * inv[a];
+            float t1 = cross_f32(0, sp[a], o[a], d[a]);
+            float t2 = cross_f32(n[a], sp[a], o[a], d[a]);
             if (t1 > t2) {
                 const float tt = t1;
                 t1 = t2;
@@ -595,10 +604,8 @@ int or_siddon_f32(const float o[3], const float d[3], const int32_t n[3], const 
                 tmin = t1;
             if (t2 < tmax)
                 tmax = t2;
-        } else {
-            inv[a] = 0.0f;
-            if (o[a] < 0.0f || o[a] >= L[a])
-                return 0;
+        } else if (o[a] < 0.0f || o[a] >= (float)n[a] * sp[a]) {
+            return 0;
         }
     }
     if (!(tmin < tmax))
@@ -619,7 +626,7 @@ int or_siddon_f32(const float o[3], const float d[3], const int32_t n[3], const 
     for (;;) {
         float tn[3];
         for (int a = 0; a < 3; ++a)
-            tn[a] = st[a] != 0 ? ((float)(i[a] + (st[a] > 0 ? 1 : 0)) * sp[a] - o[a]) * inv[a] : FLT_MAX;
+            tn[a] = st[a] != 0 ? cross_f32(i[a] + (st[a] > 0 ? 1 : 0), sp[a], o[a], d[a]) : FLT_MAX;
         int ax = 0;
         if (tn[1] < tn[ax])
             ax = 1;

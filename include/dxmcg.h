@@ -137,6 +137,8 @@ typedef struct {
     int32_t chunk_histories_log2; /* histories per launch (progress/cancel granularity), 0 = default */
     uint64_t hist_begin;  /* history range [begin, end) of the beam; end 0 = all */
     uint64_t hist_end;
+    int32_t interact_batch; /* parked scatterings a warp gathers before sampling them, 0 = default */
+    int32_t refill_batch;   /* dead lanes a warp gathers before starting new histories, 0 = default */
 } dxmcg_run_options;
 
 typedef struct {
@@ -207,6 +209,9 @@ DXMCG_API int dxmcg_siddon_trace(int n_rays, const float* origins, const float* 
     const float spacing[3], int cap, int64_t* voxel, float* length, int32_t* n_segments);
 /* Philox4x32-10 blocks */
 DXMCG_API int dxmcg_philox(int n, const uint32_t* counters, const uint32_t key[2], uint32_t* out);
+/* first n_draws raw 32-bit draws of the streams of histories h0 .. h0 + n_hist - 1 */
+DXMCG_API int dxmcg_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, int n_draws,
+    uint32_t* out);
 /* samplers driven by injected uniforms (u_stride uniforms per sample) */
 DXMCG_API int dxmcg_sample_compton(int n, const double* energies, const dxmcg_material* m, int correction,
     const double* uniforms, int u_stride, double* e_out, double* cos_out, int32_t* used);

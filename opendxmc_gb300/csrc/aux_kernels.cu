@@ -1,0 +1,232 @@
+// aux_kernels.cu -- kernels around the transport: voxel packing at World::build,
+// dose finalisation at readout, and the device test hooks that run single
+// pieces of the hot path (traversal, Philox, samplers, source) on given inputs.
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "device.cuh"
+
+namespace dxmcg {
+namespace {
+    using namespace dev;
+
+    // ---------------------------------------------------------------- world build
+    __global__ void packKernel(const double* __restrict__ d64, const float* __restrict__ d32,
+        const uint8_t* __restrict__ mat, uint32_t* __restrict__ vox, size_t n, int nMats,
+        unsigned* __restrict__ rhoMax, unsigned* __restrict__ err)
+    {
+        __shared__ unsigned smax[256];
+        for (int i = threadIdx.x; i < 256; i += blockDim.x)
+            smax[i] = 0u;
+        __syncthreads();
+        unsigned e = 0;
+        for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+             i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+            const float rho = d64 ? static_cast<float>(d64[i]) : d32[i];
+            const unsigned m = mat[i];
+            if (!(rho >= 0.0f) || !isfinite(rho))
+                e |= kErrBadDensity;
+            if (m >= static_cast<unsigned>(nMats) && m != DXMCG_TRANSPARENT_MATERIAL)
+                e |= kErrBadMaterial;
+            const unsigned bits = (rho > 0.0f && isfinite(rho)) ? ((__float_as_uint(rho) + 0x80u) & 0xffffff00u) : 0u;
+            vox[i] = bits | m;
+            if (bits > smax[m])
+                atomicMax(&smax[m], bits);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 256; i += blockDim.x)
+            if (smax[i])
+                atomicMax(&rhoMax[i], smax[i]);
+        if (e)
+            atomicOr(err, e);
+    }
+
+    __global__ void finalizeKernel(const Tally* __restrict__ t, const uint32_t* __restrict__ vox, size_t n,
+        double toDose, double nh, double* __restrict__ dose, double* __restrict__ var,
+        unsigned long long* __restrict__ cnt)
+    {
+        for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+             i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+            const Tally r = t[i];
+            const float rho = __uint_as_float(vox[i] & 0xffffff00u);
+            const double s = rho > 0.0f ? toDose / rho : 0.0;
+            if (dose)
+                dose[i] = r.e * s;
+            if (var) {
+                const double v = nh > 0 ? (r.e2 - r.e * r.e / nh) : 0.0;
+                var[i] = (v > 0.0 ? v : 0.0) * s * s;
+            }
+            if (cnt)
+                cnt[i] = r.n;
+        }
+    }
+
+    // ---------------------------------------------------------------- test kernels
+    __global__ void siddonKernel(int nRays, const float* __restrict__ o, const float* __restrict__ d, int nx, int ny,
+        int nz, float sx, float sy, float sz, int cap, long long* __restrict__ idx, float* __restrict__ len,
+        int* __restrict__ cnt)
+    {
+        const int r = blockIdx.x * blockDim.x + threadIdx.x;
+        if (r >= nRays)
+            return;
+        const int dims[3] = { nx, ny, nz };
+        const float sp[3] = { sx, sy, sz };
+        Siddon s;
+        int c = 0;
+        if (s.begin(o + 3 * r, d + 3 * r, dims, sp)) {
+            while (!s.done) {
+                long long v;
+                float l, t0;
+                s.next(v, l, t0);
+                if (l > 0.0f) {
+                    if (c < cap) {
+                        idx[static_cast<size_t>(r) * cap + c] = v;
+                        len[static_cast<size_t>(r) * cap + c] = l;
+                    }
+                    ++c;
+                }
+            }
+        }
+        cnt[r] = c;
+    }
+
+    __global__ void philoxKernel(int n, const uint32_t* __restrict__ c, uint32_t k0, uint32_t k1,
+        uint32_t* __restrict__ out)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        uint32_t a = c[4 * i], b = c[4 * i + 1], e = c[4 * i + 2], f = c[4 * i + 3];
+        philox10(a, b, e, f, k0, k1);
+        out[4 * i] = a;
+        out[4 * i + 1] = b;
+        out[4 * i + 2] = e;
+        out[4 * i + 3] = f;
+    }
+
+    __global__ void streamKernel(uint32_t k0, uint32_t k1, uint32_t stream, unsigned long long h0, int nHist,
+        int nDraws, uint32_t* __restrict__ out)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= nHist)
+            return;
+        Rng r;
+        r.init(k0, k1, stream, h0 + i);
+        for (int k = 0; k < nDraws; ++k)
+            out[static_cast<size_t>(i) * nDraws + k] = r.raw();
+    }
+
+    __global__ void comptonKernel(int n, const float* __restrict__ E, const DevMaterial* __restrict__ M,
+        int correction, const float* __restrict__ u, int stride, float* __restrict__ eo, float* __restrict__ co,
+        int* __restrict__ used)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        InjectedUniforms r { u + static_cast<size_t>(i) * stride, stride, 0 };
+        unsigned err = 0;
+        float cost;
+        eo[i] = sampleCompton(E[i], M, correction, r, cost, err);
+        co[i] = cost;
+        used[i] = r.used;
+    }
+
+    __global__ void rayleighKernel(int n, const float* __restrict__ E, const DevMaterial* __restrict__ M,
+        const float* __restrict__ u, int stride, float* __restrict__ co, int* __restrict__ used)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        InjectedUniforms r { u + static_cast<size_t>(i) * stride, stride, 0 };
+        unsigned err = 0;
+        co[i] = sampleRayleigh(E[i], M, r, err);
+        used[i] = r.used;
+    }
+
+    __global__ void sourceKernel(const DevJob J, unsigned long long h0, int n, float* __restrict__ out)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        Rng r;
+        r.init(J.key0, J.key1, J.stream, h0 + i);
+        Photon ph;
+        sampleSource(J, h0 + i, ph, r);
+        float* o = out + 8 * static_cast<size_t>(i);
+        o[0] = ph.E;
+        o[1] = ph.w;
+        o[2] = ph.px;
+        o[3] = ph.py;
+        o[4] = ph.pz;
+        o[5] = ph.dx;
+        o[6] = ph.dy;
+        o[7] = ph.dz;
+    }
+
+    int gridFor(size_t n, int block)
+    {
+        const size_t g = (n + block - 1) / block;
+        return static_cast<int>(g < 1 ? 1 : (g > 65535 * 8 ? 65535 * 8 : g));
+    }
+} // namespace
+
+cudaError_t launchPack(const double* dens64, const float* dens32, const uint8_t* mat, uint32_t* vox, size_t n,
+    int n_mats, unsigned* rho_max_bits, unsigned* err, cudaStream_t s)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int grid = static_cast<int>(std::min<size_t>(gridFor(n, 256), static_cast<size_t>(sms) * 8));
+    packKernel<<<grid, 256, 0, s>>>(dens64, dens32, mat, vox, n, n_mats, rho_max_bits, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, double energy_to_dose,
+    double n_histories, double* dose, double* var, unsigned long long* count, cudaStream_t s)
+{
+    finalizeKernel<<<gridFor(n, 256), 256, 0, s>>>(tally, vox, n, energy_to_dose, n_histories, dose, var, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int ny, int nz, float sx, float sy,
+    float sz, int cap, long long* idx, float* len, int* cnt, cudaStream_t s)
+{
+    siddonKernel<<<(n_rays + 127) / 128, 128, 0, s>>>(n_rays, o, d, nx, ny, nz, sx, sy, sz, cap, idx, len, cnt);
+    return cudaGetLastError();
+}
+
+cudaError_t launchPhilox(int n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t s)
+{
+    philoxKernel<<<(n + 255) / 256, 256, 0, s>>>(n, ctr, k0, k1, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchHistoryStream(uint32_t k0, uint32_t k1, uint32_t stream, unsigned long long h0, int n_hist,
+    int n_draws, uint32_t* out, cudaStream_t s)
+{
+    streamKernel<<<(n_hist + 127) / 128, 128, 0, s>>>(k0, k1, stream, h0, n_hist, n_draws, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, int correction, const float* u,
+    int stride, float* e_out, float* cos_out, int* used, cudaStream_t s)
+{
+    comptonKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, correction, u, stride, e_out, cos_out, used);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* u, int stride,
+    float* cos_out, int* used, cudaStream_t s)
+{
+    rayleighKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, u, stride, cos_out, used);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s)
+{
+    sourceKernel<<<(n + 127) / 128, 128, 0, s>>>(job, h0, n, out8);
+    return cudaGetLastError();
+}
+
+} // namespace dxmcg

@@ -371,9 +371,11 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o)
     s.block = o.block_size > 0 ? o.block_size : 256;
     s.block = std::max(32, std::min(256, s.block / 32 * 32));
     // one wave of resident blocks: the kernel is persistent and pulls work from its queue
-    const int resident = transportMaxBlocksPerSM(s.block);
+    const int resident = transportMaxBlocksPerSM(s.block, o.tracking);
     const int per = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, resident) : resident;
     s.grid = std::max(1, sms) * per;
+    s.interact_batch = std::min(32, std::max(0, o.interact_batch));
+    s.refill_batch = std::min(32, std::max(0, o.refill_batch));
     return s;
 }
 
@@ -881,6 +883,24 @@ DXMCG_API int dxmcg_philox(int n, const uint32_t* counters, const uint32_t key[2
     if (e != cudaSuccess)
         return cudaFail(e, "philox kernel");
     DXMCG_CUDA(cudaMemcpy(out, o.p, 16 * static_cast<size_t>(n), cudaMemcpyDeviceToHost));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, int n_draws,
+    uint32_t* out)
+{
+    if (n_hist < 0 || n_draws < 0 || !out)
+        return fail(DXMCG_ERR_ARGUMENT, "history_stream: bad arguments");
+    const size_t n = static_cast<size_t>(n_hist) * n_draws;
+    if (n == 0)
+        return DXMCG_OK;
+    DeviceBuffer<uint32_t> o;
+    DXMCG_CUDA(o.alloc(n));
+    cudaError_t e = launchHistoryStream(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32), stream, h0,
+        n_hist, n_draws, o.p, nullptr);
+    if (e != cudaSuccess)
+        return cudaFail(e, "stream kernel");
+    DXMCG_CUDA(cudaMemcpy(out, o.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return DXMCG_OK;
 }
 

@@ -1,0 +1,425 @@
+// device.cuh -- device functions of the photon-transport hot path shared by the
+// transport kernel and the test kernels: per-history random streams, table
+// interpolation, interaction samplers, direction update, exact voxel traversal,
+// source sampling.
+#pragma once
+
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "engine.hpp"
+
+namespace dxmcg {
+namespace dev {
+
+    constexpr unsigned kFull = 0xffffffffu;
+    constexpr float kMeKeV = 510.99895f;
+    constexpr float kInvHc = 1.0f / 12.398419843f;
+
+    // ---------------------------------------------------------------- Philox
+    __device__ __forceinline__ void philox10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3, uint32_t k0,
+        uint32_t k1)
+    {
+#pragma unroll
+        for (int r = 0; r < 10; ++r) {
+            const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+            const uint32_t lo0 = 0xD2511F53u * c0;
+            const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+            const uint32_t lo1 = 0xCD9E8D57u * c2;
+            const uint32_t n0 = hi1 ^ c1 ^ k0;
+            const uint32_t n2 = hi0 ^ c3 ^ k1;
+            c0 = n0;
+            c1 = lo1;
+            c2 = n2;
+            c3 = lo0;
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+    }
+
+    // (2k + 1) / 2^24 from the top 23 bits: exact in FP32 and FP64, never 0 or 1.
+    __device__ __forceinline__ float toUniform(uint32_t x)
+    {
+        return __uint2float_rn(((x >> 9) << 1) | 1u) * 5.9604644775390625e-8f;
+    }
+
+    // Stream of one history: a xoshiro128** generator (Blackman & Vigna 2018) whose
+    // 128-bit state is the Philox4x32-10 block at counter (0, stream, h) under the
+    // seed.  One Philox evaluation per history, then ten 32-bit ALU operations per
+    // draw with no data-dependent branch, so lanes stay converged while drawing.
+    struct Rng {
+        uint32_t s0, s1, s2, s3;
+
+        __device__ __forceinline__ void init(uint32_t key0, uint32_t key1, uint32_t stream, unsigned long long h)
+        {
+            s0 = 0u;
+            s1 = stream;
+            s2 = static_cast<uint32_t>(h);
+            s3 = static_cast<uint32_t>(h >> 32);
+            philox10(s0, s1, s2, s3, key0, key1);
+            if ((s0 | s1 | s2 | s3) == 0u)
+                s0 = 0x9E3779B9u;
+        }
+        __device__ __forceinline__ uint32_t raw()
+        {
+            const uint32_t out = __funnelshift_l(s1 * 5u, s1 * 5u, 7) * 9u;
+            const uint32_t t = s1 << 9;
+            s2 ^= s0;
+            s3 ^= s1;
+            s1 ^= s2;
+            s0 ^= s3;
+            s2 ^= t;
+            s3 = __funnelshift_l(s3, s3, 11);
+            return out;
+        }
+        __device__ __forceinline__ float u() { return toUniform(raw()); }
+    };
+
+    // Injected uniforms (sampler tests).
+    struct InjectedUniforms {
+        const float* p;
+        int n, used;
+        __device__ float u()
+        {
+            if (used >= n)
+                return 0.5f;
+            return p[used++];
+        }
+    };
+
+    // ---------------------------------------------------------------- tables
+    __device__ __forceinline__ void gridPos(float E, int& i, float& f)
+    {
+        const float x = (E - 1.0f) * 2.0f;
+        int k = static_cast<int>(x);
+        k = k < 0 ? 0 : (k > kTableNE - 2 ? kTableNE - 2 : k);
+        i = k;
+        f = x - static_cast<float>(k);
+    }
+
+    __device__ __forceinline__ float lerp1(const float* t, int i, float f)
+    {
+        const float a = __ldg(t + i);
+        const float b = __ldg(t + i + 1);
+        return fmaf(f, b - a, a);
+    }
+
+    // ---------------------------------------------------------------- samplers
+    template <class U>
+    __device__ float sampleCompton(float E, const DevMaterial* __restrict__ M, int correction, U& r, float& cost,
+        unsigned& err)
+    {
+        const float k = E / kMeKeV;
+        const float kk = 2.0f * k;
+        for (int guard = 0; guard < kMaxRejections; ++guard) {
+            const float r1 = r.u(), r2 = r.u(), r3 = r.u();
+            float xm1;
+            bool acc;
+            if (r1 * (9.0f + kk) <= 1.0f + kk) {
+                xm1 = kk * r2;
+                const float x = 1.0f + xm1;
+                acc = r3 * x * x <= 4.0f * xm1;
+            } else {
+                xm1 = kk * (1.0f - r2) / (1.0f + kk * r2);
+                const float x = 1.0f + xm1;
+                const float mu = 1.0f - xm1 / k;
+                acc = 2.0f * r3 <= mu * mu + 1.0f / x;
+            }
+            if (!acc)
+                continue;
+            const float omu = xm1 / k;
+            if (correction >= 1) {
+                const float q = E * kInvHc;
+                const float t = q * q * 0.5f * omu;
+                const int n = M->n;
+                float S = 0.0f;
+                for (int i = 0; i < n; ++i) {
+                    const float b = 1.0f + t / __ldg(&M->a[i]);
+                    const float b2 = b * b;
+                    S += __ldg(&M->nZ[i]) * (1.0f - 1.0f / (b2 * b2));
+                }
+                const float r4 = r.u();
+                if (r4 * __ldg(&M->Zsum) > S)
+                    continue;
+            }
+            cost = 1.0f - omu;
+            return E / (1.0f + xm1);
+        }
+        err |= kErrRejectLimit;
+        cost = 1.0f;
+        return E;
+    }
+
+    template <class U>
+    __device__ float sampleRayleigh(float E, const DevMaterial* __restrict__ M, U& r, unsigned& err)
+    {
+        const float q = E * kInvHc;
+        const float T = q * q;
+        const int n = M->n;
+        float Gs = 0.0f;
+        for (int i = 0; i < n; ++i) {
+            const float a = __ldg(&M->a[i]);
+            Gs += __ldg(&M->nZ2[i]) * a * (-expm1f(-3.0f * log1pf(T / a)));
+        }
+        for (int guard = 0; guard < kMaxRejections; ++guard) {
+            const float r1 = r.u(), r2 = r.u(), r3 = r.u();
+            const float target = r1 * Gs;
+            float acc = 0.0f, a = 0.0f, c = 0.0f;
+            for (int i = 0; i < n; ++i) {
+                a = __ldg(&M->a[i]);
+                c = -expm1f(-3.0f * log1pf(T / a));
+                acc += __ldg(&M->nZ2[i]) * a * c;
+                if (target <= acc)
+                    break;
+            }
+            // t = a ((1 - y)^(-1/3) - 1), y = r2 c.  For y >= 1/2, 1 - y is formed as
+            // (1 - r2) + r2 (1 + T/a)^-3 (1 - r2 is exact) so FP32 keeps its precision.
+            const float y = r2 * c;
+            float t;
+            if (y < 0.5f) {
+                t = a * expm1f(-log1pf(-y) / 3.0f);
+            } else {
+                const float omy = (1.0f - r2) + r2 * expf(-3.0f * log1pf(T / a));
+                t = a * expm1f(-logf(omy) / 3.0f);
+            }
+            const float mu = 1.0f - 2.0f * t / T;
+            if (2.0f * r3 <= 1.0f + mu * mu)
+                return mu;
+        }
+        err |= kErrRejectLimit;
+        return 1.0f;
+    }
+
+    __device__ __forceinline__ void scatterDirection(float& dx, float& dy, float& dz, float cost, float phiU)
+    {
+        const float sint = sqrtf(fmaxf(0.0f, 1.0f - cost * cost));
+        float sp, cp;
+        sincospif(2.0f * phiU, &sp, &cp);
+        float nx, ny, nz;
+        if (fabsf(dz) > 0.99999f) {
+            nx = sint * cp;
+            ny = sint * sp;
+            nz = (dz > 0.0f ? 1.0f : -1.0f) * cost;
+        } else {
+            const float tmp = sqrtf(1.0f - dz * dz);
+            const float it = 1.0f / tmp;
+            nx = sint * (dx * dz * cp - dy * sp) * it + dx * cost;
+            ny = sint * (dy * dz * cp + dx * sp) * it + dy * cost;
+            nz = -sint * cp * tmp + dz * cost;
+        }
+        const float inv = rsqrtf(nx * nx + ny * ny + nz * nz);
+        dx = nx * inv;
+        dy = ny * inv;
+        dz = nz * inv;
+    }
+
+    // ---------------------------------------------------------------- Siddon
+    // Exact voxel stepping in grid-local coordinates; the FP32 operation order is
+    // fixed with _rn intrinsics (no FMA contraction) so that a host restatement
+    // compiled without contraction produces the same voxel sequence bit for bit.
+    // Ray parameter of the crossing with the plane k * sp; the plane position is a
+    // double-float (hi + fma remainder) so grazing rays do not amplify its rounding.
+    __device__ __forceinline__ float crossF32(int k, float sp, float o, float d)
+    {
+        const float kf = __int2float_rn(k);
+        const float hi = __fmul_rn(kf, sp);
+        const float lo = __fmaf_rn(kf, sp, -hi);
+        return __fdiv_rn(__fadd_rn(__fsub_rn(hi, o), lo), d);
+    }
+
+    struct Siddon {
+        int i[3], st[3];
+        float o[3], d[3], sp[3];
+        float t, tmax;
+        int n[3];
+
+        // returns false if the ray misses the grid
+        __device__ bool begin(const float* org, const float* dir, const int* dims, const float* spacing)
+        {
+            float tmin = 0.0f;
+            tmax = FLT_MAX;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                n[a] = dims[a];
+                sp[a] = spacing[a];
+                o[a] = org[a];
+                d[a] = dir[a];
+                if (dir[a] != 0.0f) {
+                    float t1 = crossF32(0, spacing[a], org[a], dir[a]);
+                    float t2 = crossF32(dims[a], spacing[a], org[a], dir[a]);
+                    if (t1 > t2) {
+                        const float tt = t1;
+                        t1 = t2;
+                        t2 = tt;
+                    }
+                    if (t1 > tmin)
+                        tmin = t1;
+                    if (t2 < tmax)
+                        tmax = t2;
+                } else if (org[a] < 0.0f || org[a] >= __fmul_rn(__int2float_rn(dims[a]), spacing[a])) {
+                    return false;
+                }
+            }
+            if (!(tmin < tmax))
+                return false;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float p = __fadd_rn(org[a], __fmul_rn(tmin, dir[a]));
+                int k = static_cast<int>(floorf(__fdiv_rn(p, sp[a])));
+                k = k < 0 ? 0 : (k > n[a] - 1 ? n[a] - 1 : k);
+                i[a] = k;
+                st[a] = dir[a] > 0.0f ? 1 : (dir[a] < 0.0f ? -1 : 0);
+            }
+            t = tmin;
+            return true;
+        }
+
+        // next segment: returns false when the ray has left the grid.
+        // *len may be 0 for degenerate steps (callers skip them).
+        __device__ bool next(long long& voxel, float& len, float& t0)
+        {
+            float tn[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                tn[a] = st[a] != 0 ? crossF32(i[a] + (st[a] > 0 ? 1 : 0), sp[a], o[a], d[a]) : FLT_MAX;
+            int ax = 0;
+            if (tn[1] < tn[ax])
+                ax = 1;
+            if (tn[2] < tn[ax])
+                ax = 2;
+            const float tnext = tn[ax] < tmax ? tn[ax] : tmax;
+            const float l = __fsub_rn(tnext, t);
+            voxel = static_cast<long long>(i[0]) + static_cast<long long>(n[0])
+                    * (static_cast<long long>(i[1]) + static_cast<long long>(n[1]) * i[2]);
+            t0 = t;
+            if (l > 0.0f) {
+                len = l;
+                t = tnext;
+            } else {
+                len = 0.0f;
+            }
+            if (tnext >= tmax) {
+                done = true;
+                return true;
+            }
+            i[ax] += st[ax];
+            if (i[ax] < 0 || i[ax] >= n[ax])
+                done = true;
+            return true;
+        }
+        bool done = false;
+    };
+
+    // ---------------------------------------------------------------- photon
+    struct Photon {
+        float px, py, pz;
+        float dx, dy, dz;
+        float E, w;
+    };
+
+    // FP64 reductions into the voxel's 32-byte record (one L2 sector).
+    __device__ __forceinline__ void deposit(Tally* __restrict__ tally, uint32_t v, double e)
+    {
+        atomicAdd(&tally[v].e, e);
+        atomicAdd(&tally[v].e2, e * e);
+        atomicAdd(&tally[v].n, 1ull);
+    }
+
+    __device__ __forceinline__ float bowtieAt(const DevBowtie* __restrict__ b, float a)
+    {
+        const int n = b->n;
+        if (a <= b->ang[0])
+            return b->w[0];
+        if (a >= b->ang[n - 1])
+            return b->w[n - 1];
+        int lo = 0, hi = n - 1;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (b->ang[mid] <= a)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const float t = (a - b->ang[lo]) / (b->ang[hi] - b->ang[lo]);
+        return b->w[lo] + t * (b->w[hi] - b->w[lo]);
+    }
+
+    // exposure of history h (histories are numbered exposure-major)
+    __device__ __forceinline__ unsigned exposureOf(const DevJob& J, unsigned long long h)
+    {
+        if ((h >> 32) == 0ull && (J.ppe >> 32) == 0ull)
+            return static_cast<uint32_t>(h) / static_cast<uint32_t>(J.ppe);
+        return static_cast<unsigned>(h / J.ppe);
+    }
+
+    // Source sampling (draw order: 2 raw for the energy, fan, cone).  Leaves the
+    // photon at its source position (grid-local).
+    __device__ __forceinline__ void sampleSource(const DevJob& J, unsigned long long h, Photon& ph, Rng& r)
+    {
+        const DevExposure* __restrict__ ex = J.exps + exposureOf(J, h);
+        const int tube = ex->tube;
+        if (J.beam_type == DXMCG_BEAM_PENCIL) {
+            (void)r.raw();
+            (void)r.raw();
+            ph.E = J.pencil_energy;
+        } else {
+            const DevSpectrum* __restrict__ S = J.spec + tube;
+            const uint32_t x0 = r.raw() >> 9;
+            const uint32_t x1 = r.raw() >> 9;
+            const int n = S->n;
+            int k = static_cast<int>((static_cast<unsigned long long>(x0) * static_cast<unsigned long long>(n)) >> 23);
+            k = x1 < __ldg(&S->thr[k]) ? k : __ldg(&S->alias[k]);
+            ph.E = __ldg(&S->E[k]);
+        }
+        const float ax = (2.0f * r.u() - 1.0f) * ex->half[0];
+        const float ay = (2.0f * r.u() - 1.0f) * ex->half[1];
+        const float sx = sinf(ax), sy = sinf(ay);
+        const float sz = sqrtf(fmaxf(0.0f, 1.0f - sx * sx - sy * sy));
+        ph.dx = ex->c0[0] * sx + ex->c1[0] * sy + ex->n[0] * sz;
+        ph.dy = ex->c0[1] * sx + ex->c1[1] * sy + ex->n[1] * sz;
+        ph.dz = ex->c0[2] * sx + ex->c1[2] * sy + ex->n[2] * sz;
+        ph.px = ex->pos[0];
+        ph.py = ex->pos[1];
+        ph.pz = ex->pos[2];
+        float w = ex->weight;
+        if (J.bowtie)
+            w *= bowtieAt(J.bowtie, fabsf(ax)) * J.bowtie->inv_norm[tube];
+        ph.w = w;
+    }
+
+    // Move a source photon to its entry point on the grid box; false if it misses.
+    __device__ __forceinline__ bool enterGrid(const DevJob& J, Photon& ph)
+    {
+        float p[3] = { ph.px, ph.py, ph.pz };
+        const float d[3] = { ph.dx, ph.dy, ph.dz };
+        float tmin = 0.0f, tmax = FLT_MAX;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (d[a] != 0.0f) {
+                const float inv = 1.0f / d[a];
+                float t1 = (0.0f - p[a]) * inv, t2 = (J.L[a] - p[a]) * inv;
+                if (t1 > t2) {
+                    const float tt = t1;
+                    t1 = t2;
+                    t2 = tt;
+                }
+                tmin = fmaxf(tmin, t1);
+                tmax = fminf(tmax, t2);
+            } else if (p[a] < 0.0f || p[a] >= J.L[a]) {
+                tmax = -1.0f;
+            }
+        }
+        if (!(tmin < tmax))
+            return false;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            p[a] = fminf(fmaxf(p[a] + tmin * d[a], 0.0f), J.Lin[a]);
+        ph.px = p[0];
+        ph.py = p[1];
+        ph.pz = p[2];
+        return true;
+    }
+
+} // namespace dev
+} // namespace dxmcg

@@ -111,6 +111,8 @@ enum ErrorFlag : unsigned {
 struct LaunchShape {
     int grid = 0;
     int block = 256;
+    int refill_batch = 0;   // dead lanes a warp gathers before starting new histories (0: default)
+    int interact_batch = 0; // parked lanes a warp gathers before running scatterings (0: default)
 };
 
 // kernels (transport.cu)
@@ -128,8 +130,10 @@ cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, int
 cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* u, int stride,
     float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s);
-int transportRegistersPerThread();
-int transportMaxBlocksPerSM(int block);
+cudaError_t launchHistoryStream(uint32_t k0, uint32_t k1, uint32_t stream, unsigned long long h0, int n_hist,
+    int n_draws, uint32_t* out, cudaStream_t s);
+int transportRegistersPerThread(int tracking);
+int transportMaxBlocksPerSM(int block, int tracking);
 
 // host helpers (geometry.cpp)
 int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out);

@@ -74,7 +74,7 @@ def beam_exposures(params: dict) -> list[dict]:
 
 
 def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_size=0, blocks_per_sm=0,
-                chunk_log2=0, hist_begin=0, hist_end=0) -> N.RunOptions:
+                chunk_log2=0, hist_begin=0, hist_end=0, interact_batch=0, refill_batch=0) -> N.RunOptions:
     o = N.RunOptions()
     o.seed = seed
     o.stream = stream
@@ -85,6 +85,8 @@ def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_
     o.chunk_histories_log2 = chunk_log2
     o.hist_begin = hist_begin
     o.hist_end = hist_end
+    o.interact_batch = interact_batch
+    o.refill_batch = refill_batch
     return o
 
 
@@ -239,6 +241,12 @@ def philox(counters, key):
     k = np.ascontiguousarray(key, dtype=np.uint32)
     out = np.zeros_like(c)
     N.check(N.lib().dxmcg_philox(c.shape[0], N.ptr(c, C.c_uint32), N.ptr(k, C.c_uint32), N.ptr(out, C.c_uint32)))
+    return out
+
+
+def history_stream(seed: int, stream: int, h0: int, n_hist: int, n_draws: int) -> np.ndarray:
+    out = np.zeros((n_hist, n_draws), dtype=np.uint32)
+    N.check(N.lib().dxmcg_history_stream(seed, stream, h0, n_hist, n_draws, N.ptr(out, C.c_uint32)))
     return out
 
 

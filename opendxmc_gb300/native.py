@@ -31,7 +31,8 @@ EXPORTED = [
     "dxmcg_world_clear_tally", "dxmcg_world_read_tally", "dxmcg_world_read_dose", "dxmcg_world_tables",
     "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_progress_create", "dxmcg_progress_destroy",
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_continue", "dxmcg_progress_message",
-    "dxmcg_siddon_trace", "dxmcg_philox", "dxmcg_sample_compton", "dxmcg_sample_rayleigh", "dxmcg_sample_source",
+    "dxmcg_siddon_trace", "dxmcg_philox", "dxmcg_history_stream", "dxmcg_sample_compton", "dxmcg_sample_rayleigh",
+    "dxmcg_sample_source",
 ]
 
 
@@ -107,7 +108,8 @@ class Exposure(C.Structure):
 class RunOptions(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("stream", C.c_uint32), ("tracking", C.c_int32), ("normalize", C.c_int32),
                 ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk_histories_log2", C.c_int32),
-                ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64)]
+                ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64), ("interact_batch", C.c_int32),
+                ("refill_batch", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -164,6 +166,7 @@ def lib() -> C.CDLL:
         "dxmcg_progress_message": (i, [vp, cp, i]),
         "dxmcg_siddon_trace": (i, [i, pf, pf, pi32, pf, i, pi64, pf, pi32]),
         "dxmcg_philox": (i, [i, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+        "dxmcg_history_stream": (i, [u64, C.c_uint32, u64, i, i, C.POINTER(C.c_uint32)]),
         "dxmcg_sample_compton": (i, [i, pd, C.POINTER(Material), i, pd, i, pd, pd, pi32]),
         "dxmcg_sample_rayleigh": (i, [i, pd, C.POINTER(Material), pd, i, pd, pi32]),
         "dxmcg_sample_source": (i, [vp, C.POINTER(Beam), C.POINTER(RunOptions), i, pd]),

@@ -334,38 +334,43 @@ void or_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]
 /* (2 k + 1) / 2^24 with k the top 23 bits: exactly representable in FP32, in (0, 1). */
 double or_uniform_from_u32(uint32_t x) { return (double)((x >> 9) * 2u + 1u) * (1.0 / 16777216.0); }
 
-/* Draw source: either a Philox stream for one history, or injected uniforms. */
+/* Draw source: either the stream of one history, or injected uniforms.
+ * History h's stream: the 128-bit state of a xoshiro128** generator (Blackman &
+ * Vigna, "Scrambled linear pseudorandom number generators", 2018) is the Philox4x32-10
+ * block at counter (0, stream, h_lo, h_hi) under key = seed, so every history's
+ * draws depend only on (seed, stream, h). */
 typedef struct {
-    uint32_t key[2];
-    uint32_t ctr[4];
-    uint32_t buf[4];
-    int idx;
+    uint32_t s[4];
     const double* inj;
     int n_inj, used;
 } rng_t;
 
 static void rng_stream(rng_t* r, uint64_t seed, uint32_t stream, uint64_t hist)
 {
-    r->key[0] = (uint32_t)seed;
-    r->key[1] = (uint32_t)(seed >> 32);
-    r->ctr[0] = 0;
-    r->ctr[1] = stream;
-    r->ctr[2] = (uint32_t)hist;
-    r->ctr[3] = (uint32_t)(hist >> 32);
-    r->idx = 4;
+    const uint32_t key[2] = { (uint32_t)seed, (uint32_t)(seed >> 32) };
+    const uint32_t ctr[4] = { 0u, stream, (uint32_t)hist, (uint32_t)(hist >> 32) };
+    or_philox4x32(ctr, key, r->s);
+    if ((r->s[0] | r->s[1] | r->s[2] | r->s[3]) == 0u)
+        r->s[0] = 0x9E3779B9u; /* the all-zero state is the generator's fixed point */
     r->inj = NULL;
     r->used = 0;
 }
 
+static inline uint32_t rotl32(uint32_t x, int k) { return (x << k) | (x >> (32 - k)); }
+
 static uint32_t rng_raw(rng_t* r)
 {
-    if (r->idx == 4) {
-        or_philox4x32(r->ctr, r->key, r->buf);
-        r->ctr[0]++;
-        r->idx = 0;
-    }
+    uint32_t* s = r->s;
+    const uint32_t out = rotl32(s[1] * 5u, 7) * 9u;
+    const uint32_t t = s[1] << 9;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl32(s[3], 11);
     r->used++;
-    return r->buf[r->idx++];
+    return out;
 }
 
 static double rng_u(rng_t* r)
@@ -1513,4 +1518,14 @@ int or_sample_source(or_world* w, const or_beam* b, uint64_t seed, uint32_t stre
     }
     free(c.exps);
     return 0;
+}
+
+void or_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, int n_draws, uint32_t* out)
+{
+    for (int i = 0; i < n_hist; ++i) {
+        rng_t r;
+        rng_stream(&r, seed, stream, h0 + (uint64_t)i);
+        for (int k = 0; k < n_draws; ++k)
+            out[(size_t)i * n_draws + k] = rng_raw(&r);
+    }
 }

@@ -238,6 +238,15 @@ def philox(ctr, key):
     return list(o)
 
 
+def history_stream(seed: int, stream: int, h0: int, n_hist: int, n_draws: int) -> np.ndarray:
+    out = np.zeros((n_hist, n_draws), dtype=np.uint32)
+    L = lib()
+    L.or_history_stream.restype = None
+    L.or_history_stream.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_uint32)]
+    L.or_history_stream(seed, stream, h0, n_hist, n_draws, _p(out, C.c_uint32))
+    return out
+
+
 def make_beam(params: dict) -> tuple[Beam, list]:
     """Fill an oracle Beam from a plain dict; returns (beam, keepalive)."""
     b = Beam()

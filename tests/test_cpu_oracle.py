@@ -122,6 +122,37 @@ def test_philox_uniforms(oracle):
     assert oracle.lib().or_uniform_from_u32(0xFFFFFFFF) == 1.0 - 2.0 ** -24
 
 
+def _xoshiro128ss(state, n):
+    """Plain-Python xoshiro128** (Blackman & Vigna 2018) for checking the oracle."""
+    s = [int(x) for x in state]
+    M = 0xFFFFFFFF
+    rotl = lambda x, k: ((x << k) | (x >> (32 - k))) & M
+    out = []
+    for _ in range(n):
+        out.append((rotl((s[1] * 5) & M, 7) * 9) & M)
+        t = (s[1] << 9) & M
+        s[2] ^= s[0]
+        s[3] ^= s[1]
+        s[1] ^= s[2]
+        s[0] ^= s[3]
+        s[2] ^= t
+        s[3] = rotl(s[3], 11)
+    return out
+
+
+def test_history_streams_are_philox_seeded_xoshiro(oracle):
+    seed, stream = 0x1234567890ABCDEF, 3
+    got = oracle.history_stream(seed, stream, 2 ** 33 - 2, 4, 12)
+    for i in range(4):
+        h = 2 ** 33 - 2 + i
+        state = oracle.philox([0, stream, h & 0xFFFFFFFF, h >> 32], [seed & 0xFFFFFFFF, seed >> 32])
+        assert list(got[i]) == _xoshiro128ss(state, 12)
+    # streams of neighbouring histories and stream words differ
+    a = oracle.history_stream(1, 0, 0, 2, 8)
+    b = oracle.history_stream(1, 1, 0, 1, 8)
+    assert not np.array_equal(a[0], a[1]) and not np.array_equal(a[0], b[0])
+
+
 def test_tube_spectrum_properties(oracle):
     E, w = oracle.tube_spectrum(120.0, {13: 6.0})
     assert E[0] == 1.0 and E[-1] == 120.0 and len(E) == 120

@@ -19,6 +19,13 @@ def test_philox_bit_exact(gpu, oracle):
         np.testing.assert_array_equal(out[:512], ref)
 
 
+def test_history_streams_bit_exact(gpu, oracle):
+    for seed, stream, h0 in ((1, 0, 0), (0xFEEDFACECAFEBEEF, 7, 2 ** 32 - 100), (42, 0xFFFFFFFF, 10 ** 12)):
+        g = gpu.history_stream(seed, stream, h0, 1000, 37)
+        o = oracle.history_stream(seed, stream, h0, 1000, 37)
+        np.testing.assert_array_equal(g, o)
+
+
 def _rays(rng, n, L):
     """Rays starting within a few cm of the grid box, aimed at random inner points,
     plus axis-aligned, diagonal and corner-tie cases and rays starting inside."""

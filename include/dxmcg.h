@@ -195,6 +195,31 @@ DXMCG_API int dxmcg_world_packed_density(dxmcg_world* w, float* density, uint8_t
 DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts,
     dxmcg_progress* progress, dxmcg_stats* stats);
 
+/* ---- transport that allocates no device memory ------------------------------
+ * No counterpart in the reference.  For callers that may not call cudaMalloc or
+ * any other device allocator while they run (their GPU memory comes only from
+ * their own pool, or they were given a fixed device budget up front): every input
+ * and output is a caller-owned device array, and all scratch (queue head,
+ * statistics, tables, exposures, spectra, bowtie) lives in one 512 KiB
+ * file-scope __device__ array that each GPU loading the library keeps until exit.
+ * Limits: at most 16 materials and 4096 exposures (DXMCG_ERR_CAPACITY beyond).
+ * The first call on a device looks the array up (cudaGetSymbolAddress) and so
+ * should come before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race, so issue them one after another.  The call runs on
+ * `cuda_stream` (NULL: the default stream) and returns after it completes.
+ * Deposits are added to device_tally (N records, zero it to start afresh);
+ * stats->kernel_ms is 0 here and total_ms is the host wall time of the run. */
+typedef struct {
+    double energy;  /* energy imparted, keV */
+    double energy2; /* sum of squared deposits */
+    uint64_t count; /* number of deposits */
+    uint64_t reserved;
+} dxmcg_tally_record;
+DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], const double spacing_cm[3],
+    const float* device_density, const uint8_t* device_material, const dxmcg_material* materials, int n_materials,
+    int correction, const dxmcg_beam* beam, const dxmcg_run_options* opts, dxmcg_tally_record* device_tally,
+    void* cuda_stream, dxmcg_stats* stats);
+
 /* ---- TransportProgress (simulationpipeline.cpp:114-120, :234, :261) ---------- */
 DXMCG_API dxmcg_progress* dxmcg_progress_create(void);
 DXMCG_API void dxmcg_progress_destroy(dxmcg_progress* p);

@@ -20,6 +20,7 @@
 
 #include "../../include/dxmcg.h"
 #include "engine.hpp"
+#include "jobs.hpp"
 #include "physics.hpp"
 
 using namespace dxmcg;
@@ -74,38 +75,11 @@ struct DeviceBuffer {
     }
 };
 
-// Element cross-section tables on the energy grid are shared by all worlds.
-struct ElementTables {
-    std::vector<double> photo, incoh, coh;
-};
-std::mutex g_elementMutex;
-std::map<std::pair<int, int>, ElementTables> g_elements;
-
-const ElementTables& elementTables(int Z, int correction)
-{
-    std::lock_guard<std::mutex> lock(g_elementMutex);
-    auto key = std::make_pair(Z, correction);
-    auto it = g_elements.find(key);
-    if (it != g_elements.end())
-        return it->second;
-    ElementTables t;
-    t.photo.resize(kNE);
-    t.incoh.resize(kNE);
-    t.coh.resize(kNE);
-    for (int i = 0; i < kNE; ++i) {
-        const double E = kEmin + i * kDE;
-        t.photo[i] = phys::photoelectric(E, Z);
-        t.incoh[i] = phys::incoherent(E, Z, correction);
-        t.coh[i] = phys::coherent(E, Z);
-    }
-    return g_elements.emplace(key, std::move(t)).first->second;
-}
-
-constexpr double kAvogadro = 6.02214076e23;
 constexpr double kKeVToMilliGrayGram = 1.602176634e-10; // mGy * g per keV
-constexpr double kMajorantSafety = 1.0 + 1.0 / 1048576.0;
 constexpr int kDefaultChunkLog2 = 26;
 } // namespace
+
+int dxmcg::reportError(int code, const std::string& msg) { return fail(code, msg); }
 
 struct dxmcg_progress {
     std::atomic<uint64_t> done { 0 };
@@ -154,39 +128,6 @@ struct dxmcg_world {
 
 namespace {
 
-DevMaterial toDevMaterial(const dxmcg_material& m)
-{
-    const auto s = samplingElements(m);
-    DevMaterial d {};
-    d.n = s.n;
-    d.Zsum = static_cast<float>(s.Zsum);
-    for (int i = 0; i < s.n; ++i) {
-        d.nZ[i] = static_cast<float>(s.nZ[i]);
-        d.nZ2[i] = static_cast<float>(s.nZ2[i]);
-        d.a[i] = static_cast<float>(s.a[i]);
-    }
-    return d;
-}
-
-// Mass attenuation tables of one material on the grid, FP64, from cached element tables.
-void materialTables(const dxmcg_material& m, int correction, double* photo, double* incoh, double* coh)
-{
-    double wsum = 0;
-    for (int i = 0; i < m.n; ++i)
-        wsum += m.w[i];
-    for (int e = 0; e < kNE; ++e)
-        photo[e] = incoh[e] = coh[e] = 0.0;
-    for (int i = 0; i < m.n; ++i) {
-        const auto& t = elementTables(m.Z[i], correction);
-        const double f = (m.w[i] / wsum) * kAvogadro / phys::atomicMass(m.Z[i]) * 1e-24;
-        for (int e = 0; e < kNE; ++e) {
-            photo[e] += f * t.photo[e];
-            incoh[e] += f * t.incoh[e];
-            coh[e] += f * t.coh[e];
-        }
-    }
-}
-
 int ensureStream(dxmcg_world* w)
 {
     DXMCG_CUDA(cudaSetDevice(w->device));
@@ -199,167 +140,38 @@ int ensureStream(dxmcg_world* w)
     return DXMCG_OK;
 }
 
-struct BowtieHost {
-    std::vector<double> ang, w;
-    double eval(double a) const
-    {
-        const int n = static_cast<int>(ang.size());
-        if (a <= ang[0])
-            return w[0];
-        if (a >= ang[n - 1])
-            return w[n - 1];
-        int lo = 0, hi = n - 1;
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) / 2;
-            (ang[mid] <= a ? lo : hi) = mid;
-        }
-        const double t = (a - ang[lo]) / (ang[hi] - ang[lo]);
-        return w[lo] + t * (w[hi] - w[lo]);
-    }
-    // exact mean over |angle| in [0, half] of the piecewise-linear profile
-    double mean(double half) const
-    {
-        if (half <= 0)
-            return 1.0;
-        std::vector<double> xs { 0.0 };
-        for (double a : ang)
-            if (a > 0 && a < half)
-                xs.push_back(a);
-        xs.push_back(half);
-        double s = 0;
-        for (size_t i = 0; i + 1 < xs.size(); ++i)
-            s += 0.5 * (eval(xs[i]) + eval(xs[i + 1])) * (xs[i + 1] - xs[i]);
-        return s / half;
-    }
-};
-
-// Everything a launch needs for one beam on one world.
+// Everything a launch needs for one beam on one world, uploaded into the world's buffers.
 int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, DevJob& J, uint64_t& nHist)
 {
-    std::vector<dxmcg_exposure> ex;
-    if (expandExposures(b, ex) != DXMCG_OK || ex.empty())
-        return fail(DXMCG_ERR_ARGUMENT, "beam: invalid geometry");
-    if (b.particles_per_exposure == 0)
-        return fail(DXMCG_ERR_ARGUMENT, "beam: particles_per_exposure is 0");
-    if (b.particles_per_exposure > (1ull << 40) || ex.size() > (1u << 24))
-        return fail(DXMCG_ERR_ARGUMENT, "beam: too many histories");
-    nHist = static_cast<uint64_t>(ex.size()) * b.particles_per_exposure;
-
-    double origin[3];
-    for (int a = 0; a < 3; ++a)
-        origin[a] = -0.5 * w->dims[a] * w->spacing[a];
-    std::vector<DevExposure> dex(ex.size());
-    for (size_t i = 0; i < ex.size(); ++i) {
-        const auto& e = ex[i];
-        DevExposure& d = dex[i];
-        const double n[3] = { e.c0[1] * e.c1[2] - e.c0[2] * e.c1[1], e.c0[2] * e.c1[0] - e.c0[0] * e.c1[2],
-            e.c0[0] * e.c1[1] - e.c0[1] * e.c1[0] };
-        for (int a = 0; a < 3; ++a) {
-            d.pos[a] = static_cast<float>(e.pos[a] - origin[a]);
-            d.c0[a] = static_cast<float>(e.c0[a]);
-            d.c1[a] = static_cast<float>(e.c1[a]);
-            d.n[a] = static_cast<float>(n[a]);
-        }
-        d.half[0] = static_cast<float>(e.half[0]);
-        d.half[1] = static_cast<float>(e.half[1]);
-        d.weight = static_cast<float>(e.weight);
-        d.tube = e.tube;
-    }
-    DXMCG_CUDA(w->exps.alloc(dex.size()));
-    DXMCG_CUDA(cudaMemcpyAsync(w->exps.p, dex.data(), dex.size() * sizeof(DevExposure), cudaMemcpyHostToDevice,
-        w->stream));
-
-    std::vector<DevSpectrum> spec(2);
-    if (b.type != DXMCG_BEAM_PENCIL) {
-        for (int t = 0; t < 2; ++t) {
-            const bool dual = b.type == DXMCG_BEAM_CT_SPIRAL_DUAL_ENERGY && t == 1;
-            const auto s = tubeSpectrum(dual ? b.kvp_b : b.kvp, b.anode_angle_deg, dual ? b.n_filters_b : b.n_filters,
-                dual ? b.filter_Z_b : b.filter_Z, dual ? b.filter_mm_b : b.filter_mm);
-            if (s.energy.empty()) {
-                if (t == 0)
-                    return fail(DXMCG_ERR_ARGUMENT, "beam: tube voltage out of range");
-                spec[1] = spec[0];
-                continue;
-            }
-            if (s.energy.back() > kEmin + (kNE - 1) * kDE)
-                return fail(DXMCG_ERR_ARGUMENT, "beam: tube voltage above the table range (150 keV)");
-            const auto at = buildAlias(s);
-            DevSpectrum& d = spec[t];
-            d.n = static_cast<int>(at.energy.size());
-            for (int k = 0; k < d.n; ++k) {
-                d.E[k] = at.energy[k];
-                d.thr[k] = at.threshold[k];
-                d.alias[k] = at.alias[k];
-            }
-        }
-    } else if (!(b.energy_kev >= kEcut && b.energy_kev <= kEmin + (kNE - 1) * kDE)) {
-        return fail(DXMCG_ERR_ARGUMENT, "beam: pencil energy out of range");
-    }
+    HostJob hj;
+    std::string err;
+    const int rc = buildHostJob(b, w->dims, w->spacing, hj, err);
+    if (rc != DXMCG_OK)
+        return fail(rc, err);
+    nHist = hj.nHist;
+    DXMCG_CUDA(w->exps.alloc(hj.exposures.size()));
+    DXMCG_CUDA(cudaMemcpyAsync(w->exps.p, hj.exposures.data(), hj.exposures.size() * sizeof(DevExposure),
+        cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(w->spec.alloc(2));
-    DXMCG_CUDA(cudaMemcpyAsync(w->spec.p, spec.data(), 2 * sizeof(DevSpectrum), cudaMemcpyHostToDevice, w->stream));
-
+    DXMCG_CUDA(cudaMemcpyAsync(w->spec.p, hj.spec, 2 * sizeof(DevSpectrum), cudaMemcpyHostToDevice, w->stream));
     J = DevJob {};
-    J.bowtie = nullptr;
-    if (b.n_bowtie > 0 && b.bowtie_angle && b.bowtie_weight) {
-        if (b.n_bowtie > kMaxBowtie)
-            return fail(DXMCG_ERR_ARGUMENT, "beam: bowtie has too many points");
-        // sorted by angle: the bowtie JSON lists points unordered (bowtiefilters.json:4-32)
-        std::vector<std::pair<double, double>> pts;
-        for (int i = 0; i < b.n_bowtie; ++i)
-            pts.emplace_back(b.bowtie_angle[i], b.bowtie_weight[i]);
-        std::stable_sort(pts.begin(), pts.end(), [](auto& x, auto& y) { return x.first < y.first; });
-        BowtieHost bh;
-        for (auto& p : pts) {
-            bh.ang.push_back(p.first);
-            bh.w.push_back(p.second);
-        }
-        DevBowtie db {};
-        db.n = static_cast<int>(pts.size());
-        for (int i = 0; i < db.n; ++i) {
-            db.ang[i] = static_cast<float>(bh.ang[i]);
-            db.w[i] = static_cast<float>(bh.w[i]);
-        }
-        for (int t = 0; t < 2; ++t) {
-            double half = 0;
-            for (const auto& e : ex)
-                if (e.tube == t) {
-                    half = e.half[0];
-                    break;
-                }
-            const double m = bh.mean(half);
-            db.inv_norm[t] = static_cast<float>(m > 0 ? 1.0 / m : 1.0);
-        }
+    if (hj.hasBowtie) {
         DXMCG_CUDA(w->bowtie.alloc(1));
-        DXMCG_CUDA(cudaMemcpyAsync(w->bowtie.p, &db, sizeof(DevBowtie), cudaMemcpyHostToDevice, w->stream));
+        DXMCG_CUDA(cudaMemcpyAsync(w->bowtie.p, &hj.bowtie, sizeof(DevBowtie), cudaMemcpyHostToDevice, w->stream));
         J.bowtie = w->bowtie.p;
     }
+    // the host staging must outlive the asynchronous copies
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    fillJobFields(J, b, o, w->dims, w->spacing, w->correction, static_cast<int>(w->materials.size()),
+        static_cast<int>(hj.exposures.size()));
     J.vox = w->vox.p;
-    J.nx = w->dims[0];
-    J.ny = w->dims[1];
-    J.nz = w->dims[2];
-    for (int a = 0; a < 3; ++a) {
-        J.sp[a] = static_cast<float>(w->spacing[a]);
-        J.isp[a] = static_cast<float>(1.0 / w->spacing[a]);
-        J.L[a] = static_cast<float>(w->dims[a] * w->spacing[a]);
-        J.Lin[a] = std::nextafter(J.L[a], 0.0f);
-    }
     J.tot = w->tot.p;
     J.xs = w->xs.p;
     J.maj = w->maj.p;
     J.mats = w->mats.p;
-    J.n_mats = static_cast<int>(w->materials.size());
-    J.correction = w->correction;
     J.tally = w->tally.p;
     J.exps = w->exps.p;
-    J.n_exp = static_cast<int>(ex.size());
-    J.ppe = b.particles_per_exposure;
     J.spec = w->spec.p;
-    J.beam_type = b.type;
-    J.pencil_energy = static_cast<float>(b.energy_kev);
-    J.key0 = static_cast<uint32_t>(o.seed);
-    J.key1 = static_cast<uint32_t>(o.seed >> 32);
-    J.stream = o.stream;
-    J.tracking = o.tracking;
     return DXMCG_OK;
 }
 
@@ -585,23 +397,10 @@ DXMCG_API int dxmcg_world_build(dxmcg_world* w)
     }
     std::vector<float> tot(static_cast<size_t>(M) * kNE);
     std::vector<float4> xs(static_cast<size_t>(M) * kNE);
-    std::vector<double> maj(kNE, 0.0);
-    std::vector<double> ph(kNE), ic(kNE), co(kNE);
-    std::vector<DevMaterial> dm(M);
-    for (int m = 0; m < M; ++m) {
-        materialTables(w->materials[m], w->correction, ph.data(), ic.data(), co.data());
-        for (int i = 0; i < kNE; ++i) {
-            const double t = ph[i] + ic[i] + co[i];
-            tot[m * kNE + i] = static_cast<float>(t);
-            xs[m * kNE + i] = make_float4(static_cast<float>(ph[i]), static_cast<float>(ic[i]),
-                static_cast<float>(co[i]), static_cast<float>(t));
-            maj[i] = std::max(maj[i], w->rhoMax[m] * t);
-        }
-        dm[m] = toDevMaterial(w->materials[m]);
-    }
     std::vector<float> majf(kNE);
-    for (int i = 0; i < kNE; ++i)
-        majf[i] = static_cast<float>(std::max(maj[i] * kMajorantSafety, 1e-30));
+    std::vector<DevMaterial> dm(M);
+    buildDeviceTables(w->materials.data(), M, w->correction, w->rhoMax.data(), tot.data(), xs.data(), majf.data(),
+        dm.data());
     DXMCG_CUDA(w->tot.alloc(tot.size()));
     DXMCG_CUDA(w->xs.alloc(xs.size()));
     DXMCG_CUDA(w->maj.alloc(kNE));

@@ -14,6 +14,7 @@
 
 #include <array>
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -70,6 +71,8 @@ struct alignas(32) Tally {
 struct DevJob {
     // world
     const uint32_t* vox;
+    const float* dens;   // unpacked voxel arrays (the allocation-free entry point)
+    const uint8_t* mat;
     int nx, ny, nz;
     float sp[3];
     float isp[3];
@@ -134,8 +137,14 @@ cudaError_t launchHistoryStream(uint32_t k0, uint32_t k1, uint32_t stream, unsig
     int n_draws, uint32_t* out, cudaStream_t s);
 int transportRegistersPerThread(int tracking);
 int transportMaxBlocksPerSM(int block, int tracking);
+// the same kernel reading caller-owned float density / uint8 material arrays
+cudaError_t launchTransportUnpacked(const DevJob& job, unsigned long long h_end, DevCounters* ctr,
+    LaunchShape shape, cudaStream_t s);
+int transportMaxBlocksPerSMUnpacked(int block, int tracking);
 
 // host helpers (geometry.cpp)
 int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out);
+// sets the calling thread's dxmcg_last_error() text and returns code (capi.cpp)
+int reportError(int code, const std::string& msg);
 
 } // namespace dxmcg

@@ -1,0 +1,261 @@
+// jobs.cpp -- see jobs.hpp.
+#include "jobs.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <utility>
+
+namespace dxmcg {
+namespace {
+    constexpr double kAvogadro = 6.02214076e23;
+    constexpr double kMajorantSafety = 1.0 + 1.0 / 1048576.0;
+
+    // Element cross-section tables on the energy grid, shared by all worlds.
+    struct ElementTables {
+        std::vector<double> photo, incoh, coh;
+    };
+    std::mutex g_elementMutex;
+    std::map<std::pair<int, int>, ElementTables> g_elements;
+
+    const ElementTables& elementTables(int Z, int correction)
+    {
+        std::lock_guard<std::mutex> lock(g_elementMutex);
+        const auto key = std::make_pair(Z, correction);
+        auto it = g_elements.find(key);
+        if (it != g_elements.end())
+            return it->second;
+        ElementTables t;
+        t.photo.resize(kNE);
+        t.incoh.resize(kNE);
+        t.coh.resize(kNE);
+        for (int i = 0; i < kNE; ++i) {
+            const double E = kEmin + i * kDE;
+            t.photo[i] = phys::photoelectric(E, Z);
+            t.incoh[i] = phys::incoherent(E, Z, correction);
+            t.coh[i] = phys::coherent(E, Z);
+        }
+        return g_elements.emplace(key, std::move(t)).first->second;
+    }
+
+    struct BowtieProfile {
+        std::vector<double> ang, w;
+        double at(double a) const
+        {
+            const int n = static_cast<int>(ang.size());
+            if (a <= ang[0])
+                return w[0];
+            if (a >= ang[n - 1])
+                return w[n - 1];
+            int lo = 0, hi = n - 1;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) / 2;
+                (ang[mid] <= a ? lo : hi) = mid;
+            }
+            const double t = (a - ang[lo]) / (ang[hi] - ang[lo]);
+            return w[lo] + t * (w[hi] - w[lo]);
+        }
+        // exact mean over |angle| in [0, half] of the piecewise-linear profile
+        double mean(double half) const
+        {
+            if (half <= 0)
+                return 1.0;
+            std::vector<double> xs { 0.0 };
+            for (double a : ang)
+                if (a > 0 && a < half)
+                    xs.push_back(a);
+            xs.push_back(half);
+            double s = 0;
+            for (size_t i = 0; i + 1 < xs.size(); ++i)
+                s += 0.5 * (at(xs[i]) + at(xs[i + 1])) * (xs[i + 1] - xs[i]);
+            return s / half;
+        }
+    };
+} // namespace
+
+void materialTables(const dxmcg_material& m, int correction, double* photo, double* incoh, double* coh)
+{
+    double wsum = 0;
+    for (int i = 0; i < m.n; ++i)
+        wsum += m.w[i];
+    for (int e = 0; e < kNE; ++e)
+        photo[e] = incoh[e] = coh[e] = 0.0;
+    for (int i = 0; i < m.n; ++i) {
+        const auto& t = elementTables(m.Z[i], correction);
+        const double f = (m.w[i] / wsum) * kAvogadro / phys::atomicMass(m.Z[i]) * 1e-24;
+        for (int e = 0; e < kNE; ++e) {
+            photo[e] += f * t.photo[e];
+            incoh[e] += f * t.incoh[e];
+            coh[e] += f * t.coh[e];
+        }
+    }
+}
+
+DevMaterial toDevMaterial(const dxmcg_material& m)
+{
+    const auto s = samplingElements(m);
+    DevMaterial d {};
+    d.n = s.n;
+    d.Zsum = static_cast<float>(s.Zsum);
+    for (int i = 0; i < s.n; ++i) {
+        d.nZ[i] = static_cast<float>(s.nZ[i]);
+        d.nZ2[i] = static_cast<float>(s.nZ2[i]);
+        d.a[i] = static_cast<float>(s.a[i]);
+    }
+    return d;
+}
+
+void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const double* rhoMax, float* tot,
+    float4* xs, float* maj, DevMaterial* dm)
+{
+    std::vector<double> mx(kNE, 0.0), ph(kNE), ic(kNE), co(kNE);
+    for (int m = 0; m < M; ++m) {
+        materialTables(mats[m], correction, ph.data(), ic.data(), co.data());
+        for (int i = 0; i < kNE; ++i) {
+            const double t = ph[i] + ic[i] + co[i];
+            tot[m * kNE + i] = static_cast<float>(t);
+            xs[m * kNE + i] = make_float4(static_cast<float>(ph[i]), static_cast<float>(ic[i]),
+                static_cast<float>(co[i]), static_cast<float>(t));
+            mx[i] = std::max(mx[i], rhoMax[m] * t);
+        }
+        dm[m] = toDevMaterial(mats[m]);
+    }
+    for (int i = 0; i < kNE; ++i)
+        maj[i] = static_cast<float>(std::max(mx[i] * kMajorantSafety, 1e-30));
+}
+
+int buildHostJob(const dxmcg_beam& b, const int32_t dims[3], const double spacing[3], HostJob& out, std::string& err)
+{
+    std::vector<dxmcg_exposure> ex;
+    if (expandExposures(b, ex) != DXMCG_OK || ex.empty()) {
+        err = "beam: invalid geometry";
+        return DXMCG_ERR_ARGUMENT;
+    }
+    if (b.particles_per_exposure == 0) {
+        err = "beam: particles_per_exposure is 0";
+        return DXMCG_ERR_ARGUMENT;
+    }
+    if (b.particles_per_exposure > (1ull << 40) || ex.size() > (1u << 24)) {
+        err = "beam: too many histories";
+        return DXMCG_ERR_ARGUMENT;
+    }
+    out.nHist = static_cast<uint64_t>(ex.size()) * b.particles_per_exposure;
+
+    double origin[3];
+    for (int a = 0; a < 3; ++a)
+        origin[a] = -0.5 * dims[a] * spacing[a];
+    out.exposures.resize(ex.size());
+    for (size_t i = 0; i < ex.size(); ++i) {
+        const auto& e = ex[i];
+        DevExposure& d = out.exposures[i];
+        const double n[3] = { e.c0[1] * e.c1[2] - e.c0[2] * e.c1[1], e.c0[2] * e.c1[0] - e.c0[0] * e.c1[2],
+            e.c0[0] * e.c1[1] - e.c0[1] * e.c1[0] };
+        for (int a = 0; a < 3; ++a) {
+            d.pos[a] = static_cast<float>(e.pos[a] - origin[a]);
+            d.c0[a] = static_cast<float>(e.c0[a]);
+            d.c1[a] = static_cast<float>(e.c1[a]);
+            d.n[a] = static_cast<float>(n[a]);
+        }
+        d.half[0] = static_cast<float>(e.half[0]);
+        d.half[1] = static_cast<float>(e.half[1]);
+        d.weight = static_cast<float>(e.weight);
+        d.tube = e.tube;
+    }
+
+    out.spec[0] = DevSpectrum {};
+    out.spec[1] = DevSpectrum {};
+    if (b.type != DXMCG_BEAM_PENCIL) {
+        for (int t = 0; t < 2; ++t) {
+            const bool dual = b.type == DXMCG_BEAM_CT_SPIRAL_DUAL_ENERGY && t == 1;
+            const auto s = tubeSpectrum(dual ? b.kvp_b : b.kvp, b.anode_angle_deg, dual ? b.n_filters_b : b.n_filters,
+                dual ? b.filter_Z_b : b.filter_Z, dual ? b.filter_mm_b : b.filter_mm);
+            if (s.energy.empty()) {
+                if (t == 0) {
+                    err = "beam: tube voltage out of range";
+                    return DXMCG_ERR_ARGUMENT;
+                }
+                out.spec[1] = out.spec[0];
+                continue;
+            }
+            if (s.energy.back() > kEmin + (kNE - 1) * kDE) {
+                err = "beam: tube voltage above the table range (150 keV)";
+                return DXMCG_ERR_ARGUMENT;
+            }
+            const auto at = buildAlias(s);
+            DevSpectrum& d = out.spec[t];
+            d.n = static_cast<int>(at.energy.size());
+            for (int k = 0; k < d.n; ++k) {
+                d.E[k] = at.energy[k];
+                d.thr[k] = at.threshold[k];
+                d.alias[k] = at.alias[k];
+            }
+        }
+    } else if (!(b.energy_kev >= kEcut && b.energy_kev <= kEmin + (kNE - 1) * kDE)) {
+        err = "beam: pencil energy out of range";
+        return DXMCG_ERR_ARGUMENT;
+    }
+
+    out.hasBowtie = false;
+    if (b.n_bowtie > 0 && b.bowtie_angle && b.bowtie_weight) {
+        if (b.n_bowtie > kMaxBowtie) {
+            err = "beam: bowtie has too many points";
+            return DXMCG_ERR_ARGUMENT;
+        }
+        // sorted by angle: the bowtie JSON lists points unordered (bowtiefilters.json:4-32)
+        std::vector<std::pair<double, double>> pts;
+        for (int i = 0; i < b.n_bowtie; ++i)
+            pts.emplace_back(b.bowtie_angle[i], b.bowtie_weight[i]);
+        std::stable_sort(pts.begin(), pts.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
+        BowtieProfile prof;
+        for (const auto& p : pts) {
+            prof.ang.push_back(p.first);
+            prof.w.push_back(p.second);
+        }
+        DevBowtie& db = out.bowtie;
+        db = DevBowtie {};
+        db.n = static_cast<int>(pts.size());
+        for (int i = 0; i < db.n; ++i) {
+            db.ang[i] = static_cast<float>(prof.ang[i]);
+            db.w[i] = static_cast<float>(prof.w[i]);
+        }
+        for (int t = 0; t < 2; ++t) {
+            double half = 0;
+            for (const auto& e : ex)
+                if (e.tube == t) {
+                    half = e.half[0];
+                    break;
+                }
+            const double m = prof.mean(half);
+            db.inv_norm[t] = static_cast<float>(m > 0 ? 1.0 / m : 1.0);
+        }
+        out.hasBowtie = true;
+    }
+    return DXMCG_OK;
+}
+
+void fillJobFields(DevJob& J, const dxmcg_beam& b, const dxmcg_run_options& o, const int32_t dims[3],
+    const double spacing[3], int correction, int n_mats, int n_exp)
+{
+    J.nx = dims[0];
+    J.ny = dims[1];
+    J.nz = dims[2];
+    for (int a = 0; a < 3; ++a) {
+        J.sp[a] = static_cast<float>(spacing[a]);
+        J.isp[a] = static_cast<float>(1.0 / spacing[a]);
+        J.L[a] = static_cast<float>(dims[a] * spacing[a]);
+        J.Lin[a] = std::nextafter(J.L[a], 0.0f);
+    }
+    J.n_mats = n_mats;
+    J.correction = correction;
+    J.n_exp = n_exp;
+    J.ppe = b.particles_per_exposure;
+    J.beam_type = b.type;
+    J.pencil_energy = static_cast<float>(b.energy_kev);
+    J.key0 = static_cast<uint32_t>(o.seed);
+    J.key1 = static_cast<uint32_t>(o.seed >> 32);
+    J.stream = o.stream;
+    J.tracking = o.tracking;
+}
+
+} // namespace dxmcg

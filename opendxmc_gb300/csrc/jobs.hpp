@@ -1,0 +1,42 @@
+// jobs.hpp -- host-side preparation of what one transport launch needs, shared by
+// the world-based entry points (capi.cpp) and the allocation-free entry point
+// (noalloc.cu): per-material FP32 tables and majorant, exposures in grid-local
+// coordinates, spectrum alias tables, the bowtie profile.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+#include "physics.hpp"
+
+namespace dxmcg {
+
+struct HostJob {
+    std::vector<DevExposure> exposures;
+    DevSpectrum spec[2];
+    bool hasBowtie = false;
+    DevBowtie bowtie {};
+    uint64_t nHist = 0;
+};
+
+// Beam -> exposures, spectra, bowtie for a grid of dims x spacing centred on the
+// origin.  Returns DXMCG_OK or an error code with `err` set.
+int buildHostJob(const dxmcg_beam& b, const int32_t dims[3], const double spacing[3], HostJob& out, std::string& err);
+
+// Grid, stream and beam fields of a DevJob (device pointers are set by the caller).
+void fillJobFields(DevJob& J, const dxmcg_beam& b, const dxmcg_run_options& o, const int32_t dims[3],
+    const double spacing[3], int correction, int n_mats, int n_exp);
+
+// Mass attenuation of one material on the table grid (FP64), from per-element
+// tables cached for the life of the process.
+void materialTables(const dxmcg_material& m, int correction, double* photo, double* incoh, double* coh);
+
+// FP32 device tables for M materials and the majorant (rho_max[m] * total, times a
+// small safety factor, maximised over m) on the table grid.
+void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const double* rhoMax, float* tot,
+    float4* xs, float* maj, DevMaterial* dm);
+
+DevMaterial toDevMaterial(const dxmcg_material& m);
+
+} // namespace dxmcg

@@ -63,7 +63,22 @@ namespace {
         }
     };
 
+    // Density and material of voxel v: one 4-byte word in the packed layout, or two
+    // loads from caller-owned arrays in the unpacked layout.
+    template <bool PACKED>
+    __device__ __forceinline__ float voxelAt(const DevJob& J, uint32_t v, int& m)
+    {
+        if (PACKED) {
+            const uint32_t word = __ldg(J.vox + v);
+            m = static_cast<int>(word & 0xffu);
+            return __uint_as_float(word & 0xffffff00u);
+        }
+        m = static_cast<int>(__ldg(J.mat + v));
+        return __ldg(J.dens + v);
+    }
+
     // Woodcock step; returns true on a real collision in voxel v / material m.
+    template <bool PACKED>
     __device__ __forceinline__ bool woodcockStep(const DevJob& J, Photon& ph, Rng& rng, const EnergyCache& ec,
         bool& escaped, uint32_t& v, int& m, unsigned& visits)
     {
@@ -81,15 +96,15 @@ namespace {
         const int iy = min(static_cast<int>(ph.py * J.isp[1]), J.ny - 1);
         const int iz = min(static_cast<int>(ph.pz * J.isp[2]), J.nz - 1);
         v = static_cast<uint32_t>(ix + J.nx * (iy + J.ny * iz));
-        const uint32_t word = __ldg(J.vox + v);
-        m = static_cast<int>(word & 0xffu);
+        const float rho = voxelAt<PACKED>(J, v, m);
         if (m == DXMCG_TRANSPARENT_MATERIAL)
             return false;
-        const float mu = __uint_as_float(word & 0xffffff00u) * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
+        const float mu = rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
         return rng.u() * ec.mmax < mu;
     }
 
     // One free flight with exact voxel path lengths; true on a collision.
+    template <bool PACKED>
     __device__ __forceinline__ bool siddonFlight(const DevJob& J, Photon& ph, Rng& rng, const EnergyCache& ec,
         bool& escaped, uint32_t& v, int& m, unsigned& visits)
     {
@@ -109,11 +124,11 @@ namespace {
                 if (len <= 0.0f)
                     continue;
                 ++visits;
-                const uint32_t word = __ldg(J.vox + vox);
-                const int mm = static_cast<int>(word & 0xffu);
+                int mm;
+                const float rho = voxelAt<PACKED>(J, static_cast<uint32_t>(vox), mm);
                 if (mm == DXMCG_TRANSPARENT_MATERIAL)
                     continue;
-                const float mu = __uint_as_float(word & 0xffffff00u) * lerp1(J.tot + mm * kTableNE, ec.ie, ec.fe);
+                const float mu = rho * lerp1(J.tot + mm * kTableNE, ec.ie, ec.fe);
                 if (mu > 0.0f && acc + mu * len >= tau) {
                     hit = true;
                     v = static_cast<uint32_t>(vox);
@@ -134,7 +149,7 @@ namespace {
         return true;
     }
 
-    template <int TRACKING>
+    template <int TRACKING, bool PACKED = true>
     __global__ void __launch_bounds__(256) transportKernel(const DevJob J, unsigned long long h_end,
         DevCounters* __restrict__ ctr, int refillBatch, int interactBatch)
     {
@@ -263,8 +278,8 @@ namespace {
                 uint32_t v = 0;
                 int m = 0;
                 const bool real = TRACKING == DXMCG_TRACK_WOODCOCK
-                    ? woodcockStep(J, ph, rng, ec, escaped, v, m, visits)
-                    : siddonFlight(J, ph, rng, ec, escaped, v, m, visits);
+                    ? woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits)
+                    : siddonFlight<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
                 if (escaped) {
                     eesc += static_cast<double>(ph.w) * ph.E;
                     st = kDead;
@@ -350,6 +365,30 @@ cudaError_t launchTransport(const DevJob& job, unsigned long long h_end, DevCoun
     else
         transportKernel<DXMCG_TRACK_WOODCOCK><<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill, interact);
     return cudaGetLastError();
+}
+
+cudaError_t launchTransportUnpacked(const DevJob& job, unsigned long long h_end, DevCounters* ctr,
+    LaunchShape shape, cudaStream_t s)
+{
+    const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
+    const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
+    if (job.tracking == DXMCG_TRACK_SIDDON)
+        transportKernel<DXMCG_TRACK_SIDDON, false><<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill, interact);
+    else
+        transportKernel<DXMCG_TRACK_WOODCOCK, false><<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill,
+            interact);
+    return cudaGetLastError();
+}
+
+int transportMaxBlocksPerSMUnpacked(int block, int tracking)
+{
+    int n = 0;
+    const cudaError_t e = tracking == DXMCG_TRACK_SIDDON
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transportKernel<DXMCG_TRACK_SIDDON, false>, block, 0)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transportKernel<DXMCG_TRACK_WOODCOCK, false>, block, 0);
+    if (e != cudaSuccess)
+        return 1;
+    return n > 0 ? n : 1;
 }
 
 int transportMaxBlocksPerSM(int block, int tracking)

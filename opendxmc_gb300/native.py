@@ -29,7 +29,8 @@ EXPORTED = [
     "dxmcg_tube_mean_energy", "dxmcg_tube_al_hvl", "dxmcg_beam_exposures", "dxmcg_world_create",
     "dxmcg_world_set_data", "dxmcg_world_set_data_f32", "dxmcg_world_build", "dxmcg_world_destroy",
     "dxmcg_world_clear_tally", "dxmcg_world_read_tally", "dxmcg_world_read_dose", "dxmcg_world_tables",
-    "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_progress_create", "dxmcg_progress_destroy",
+    "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_transport_run_noalloc", "dxmcg_progress_create",
+    "dxmcg_progress_destroy",
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_continue", "dxmcg_progress_message",
     "dxmcg_siddon_trace", "dxmcg_philox", "dxmcg_history_stream", "dxmcg_sample_compton", "dxmcg_sample_rayleigh",
     "dxmcg_sample_source",
@@ -158,6 +159,8 @@ def lib() -> C.CDLL:
         "dxmcg_world_tables": (i, [vp, i, pf, pf]),
         "dxmcg_world_packed_density": (i, [vp, pf, pu8]),
         "dxmcg_transport_run": (i, [vp, C.POINTER(Beam), C.POINTER(RunOptions), vp, C.POINTER(Stats)]),
+        "dxmcg_transport_run_noalloc": (i, [pi32, pd, vp, vp, C.POINTER(Material), i, i, C.POINTER(Beam),
+                                            C.POINTER(RunOptions), vp, vp, C.POINTER(Stats)]),
         "dxmcg_progress_create": (vp, []),
         "dxmcg_progress_destroy": (None, [vp]),
         "dxmcg_progress_get": (None, [vp, pu64, pu64]),

@@ -135,9 +135,9 @@ namespace dev {
                 const int n = M->n;
                 float S = 0.0f;
                 for (int i = 0; i < n; ++i) {
-                    const float b = 1.0f + t / __ldg(&M->a[i]);
+                    const float b = fmaf(t, __ldg(&M->ia[i]), 1.0f);
                     const float b2 = b * b;
-                    S += __ldg(&M->nZ[i]) * (1.0f - 1.0f / (b2 * b2));
+                    S += __ldg(&M->nZ[i]) * (1.0f - __frcp_rn(b2 * b2));
                 }
                 const float r4 = r.u();
                 if (r4 * __ldg(&M->Zsum) > S)
@@ -374,7 +374,8 @@ namespace dev {
         }
         const float ax = (2.0f * r.u() - 1.0f) * ex->half[0];
         const float ay = (2.0f * r.u() - 1.0f) * ex->half[1];
-        const float sx = sinf(ax), sy = sinf(ay);
+        // |angle| < pi/2: the hardware sine is within 2^-21.4
+        const float sx = __sinf(ax), sy = __sinf(ay);
         const float sz = sqrtf(fmaxf(0.0f, 1.0f - sx * sx - sy * sy));
         ph.dx = ex->c0[0] * sx + ex->c1[0] * sy + ex->n[0] * sz;
         ph.dy = ex->c0[1] * sx + ex->c1[1] * sy + ex->n[1] * sz;

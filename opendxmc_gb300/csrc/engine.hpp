@@ -35,6 +35,7 @@ struct DevMaterial {
     float nZ[DXMCG_MAX_ELEMENTS];
     float nZ2[DXMCG_MAX_ELEMENTS];
     float a[DXMCG_MAX_ELEMENTS];
+    float ia[DXMCG_MAX_ELEMENTS]; // 1 / a
 };
 
 struct alignas(16) DevExposure {

@@ -102,6 +102,7 @@ DevMaterial toDevMaterial(const dxmcg_material& m)
         d.nZ[i] = static_cast<float>(s.nZ[i]);
         d.nZ2[i] = static_cast<float>(s.nZ2[i]);
         d.a[i] = static_cast<float>(s.a[i]);
+        d.ia[i] = static_cast<float>(1.0 / s.a[i]);
     }
     return d;
 }

@@ -82,7 +82,8 @@ namespace {
     __device__ __forceinline__ bool woodcockStep(const DevJob& J, Photon& ph, Rng& rng, const EnergyCache& ec,
         bool& escaped, uint32_t& v, int& m, unsigned& visits)
     {
-        const float s = -logf(rng.u()) * ec.invMmax;
+        // hardware log2: |error| <= 2^-21.4 near u = 1, where the step is < 1e-6 mean free paths
+        const float s = fmaxf(-__logf(rng.u()), 0.0f) * ec.invMmax;
         ph.px = fmaf(s, ph.dx, ph.px);
         ph.py = fmaf(s, ph.dy, ph.py);
         ph.pz = fmaf(s, ph.dz, ph.pz);
@@ -153,12 +154,14 @@ namespace {
     __global__ void __launch_bounds__(256) transportKernel(const DevJob J, unsigned long long h_end,
         DevCounters* __restrict__ ctr, int refillBatch, int interactBatch)
     {
-        __shared__ unsigned long long sCount[cNum];
-        if (threadIdx.x < cNum)
-            sCount[threadIdx.x] = 0ull;
-        __syncthreads();
-
+        // event counters per warp (no block-wide barrier: warps finish independently)
+        __shared__ unsigned long long sCountAll[256 / 32][cNum];
         const unsigned lane = threadIdx.x & 31u;
+        unsigned long long* sCount = sCountAll[threadIdx.x >> 5];
+        if (lane < cNum)
+            sCount[lane] = 0ull;
+        __syncwarp();
+
         const unsigned ltMask = (1u << lane) - 1u;
         unsigned long long poolNext = 0, poolEnd = 0;
         bool exhausted = false;
@@ -332,6 +335,7 @@ namespace {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             errAll |= __shfl_xor_sync(kFull, errAll, o);
+        __syncwarp();
         if (lane == 0) {
             atomicAdd(&ctr->visits, vi);
             atomicAdd(&ctr->e_source, es);
@@ -339,9 +343,6 @@ namespace {
             atomicAdd(&ctr->e_deposited, ed);
             if (errAll)
                 atomicOr(&ctr->error_flags, errAll);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
             atomicAdd(&ctr->histories, sCount[cHist]);
             atomicAdd(&ctr->missed, sCount[cMissed]);
             atomicAdd(&ctr->photo, sCount[cPhoto]);

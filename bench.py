@@ -39,10 +39,11 @@ METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "
     "histories/s"
 WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 materials, +-2% density jitter), "
             "120 kVp 6 mm Al + body bowtie, pitch 1.0, 40 mm collimation, 200 mm scan, 1e9 histories")
-# dram__bytes_read.sum + dram__bytes_write.sum of one transport launch, from the ncu
-# capture summarised in profiles/transport_kernel_torso.md, scaled to one full
-# 2^26-history launch; None until a capture exists.
-TRAFFIC_BYTES_PER_LAUNCH = None
+# dram__bytes_read.sum + dram__bytes_write.sum of one full transport launch
+# (67,000,320 histories of this workload: 2.60 GB read + 1.01 GB written), from the
+# 1-pass ncu capture summarised in profiles/transport_kernel_torso.md.  bench.py's
+# launches hold up to 2^26 histories, 0.2 % more than the captured one.
+TRAFFIC_BYTES_PER_LAUNCH = 3.61e9
 
 
 def parse():

@@ -319,10 +319,11 @@ namespace dev {
     };
 
     // FP64 reductions into the voxel's 32-byte record (one L2 sector).
-    __device__ __forceinline__ void deposit(Tally* __restrict__ tally, uint32_t v, double e)
+    // The deposit is formed in FP32 and widened only for the reductions.
+    __device__ __forceinline__ void deposit(Tally* __restrict__ tally, uint32_t v, float e)
     {
-        atomicAdd(&tally[v].e, e);
-        atomicAdd(&tally[v].e2, e * e);
+        atomicAdd(&tally[v].e, static_cast<double>(e));
+        atomicAdd(&tally[v].e2, static_cast<double>(e * e));
         atomicAdd(&tally[v].n, 1ull);
     }
 

@@ -52,6 +52,19 @@ namespace {
         return v;
     }
 
+    // Kahan-compensated FP32 sum; value() returns it in FP64 once, at the end.
+    struct KahanSum {
+        float s = 0.0f, c = 0.0f;
+        __device__ __forceinline__ void add(float x)
+        {
+            const float y = x - c;
+            const float t = s + y;
+            c = (t - s) - y;
+            s = t;
+        }
+        __device__ __forceinline__ double value() const { return static_cast<double>(s) - static_cast<double>(c); }
+    };
+
     struct EnergyCache {
         int ie;
         float fe, mmax, invMmax;
@@ -173,7 +186,7 @@ namespace {
         int pm = 0;      // its material
         unsigned steps = 0, visits = 0, err = 0;
         bool fresh = false;
-        double esrc = 0.0, eesc = 0.0, edep = 0.0;
+        KahanSum esrc, eesc, edep; // FP32 compensated sums: no FP64 on the per-event path
 
         for (;;) {
             const unsigned stepping = __ballot_sync(kFull, st == kStepping);
@@ -204,7 +217,7 @@ namespace {
                     const unsigned long long h = poolNext + rank;
                     rng.init(J.key0, J.key1, J.stream, h);
                     sampleSource(J, h, ph, rng);
-                    esrc += static_cast<double>(ph.w) * ph.E;
+                    esrc.add(ph.w * ph.E);
                     entered = enterGrid(J, ph);
                     if (entered) {
                         st = kStepping;
@@ -215,7 +228,7 @@ namespace {
                         else
                             gridPos(ph.E, ec.ie, ec.fe);
                     } else {
-                        eesc += static_cast<double>(ph.w) * ph.E;
+                        eesc.add(ph.w * ph.E);
                     }
                 }
                 poolNext += min(static_cast<unsigned long long>(__popc(dead)), avail);
@@ -236,14 +249,14 @@ namespace {
                     float cost;
                     const float Ep = sampleCompton(ph.E, J.mats + pm, J.correction, rng, cost, err);
                     scatterDirection(ph.dx, ph.dy, ph.dz, cost, rng.u());
-                    const double e = static_cast<double>(ph.w) * (ph.E - Ep);
+                    const float e = ph.w * (ph.E - Ep);
                     deposit(J.tally, pv, e);
-                    edep += e;
+                    edep.add(e);
                     ph.E = Ep;
                     if (Ep < 1.0f) {
-                        const double r = static_cast<double>(ph.w) * Ep;
+                        const float r = ph.w * Ep;
                         deposit(J.tally, pv, r);
-                        edep += r;
+                        edep.add(r);
                         st = kDead;
                         cut = true;
                     } else {
@@ -284,7 +297,7 @@ namespace {
                     ? woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits)
                     : siddonFlight<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
                 if (escaped) {
-                    eesc += static_cast<double>(ph.w) * ph.E;
+                    eesc.add(ph.w * ph.E);
                     st = kDead;
                 } else if (real) {
                     first = fresh;
@@ -296,9 +309,9 @@ namespace {
                     const float co = fmaf(ec.fe, b.z - a.z, a.z);
                     const float rt = rng.u() * (pe + ic + co);
                     if (rt < pe) {
-                        const double e = static_cast<double>(ph.w) * ph.E;
+                        const float e = ph.w * ph.E;
                         deposit(J.tally, v, e);
-                        edep += e;
+                        edep.add(e);
                         st = kDead;
                         photo = true;
                     } else {
@@ -328,9 +341,9 @@ namespace {
 
         // ---- flush: per-lane sums by warp, block counters by one thread
         const unsigned long long vi = warpSum(static_cast<unsigned long long>(visits));
-        const double es = warpSum(esrc);
-        const double ee = warpSum(eesc);
-        const double ed = warpSum(edep);
+        const double es = warpSum(esrc.value());
+        const double ee = warpSum(eesc.value());
+        const double ed = warpSum(edep.value());
         unsigned errAll = err;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)

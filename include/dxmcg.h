@@ -115,6 +115,21 @@ typedef struct {
     double aec_start[3];
     double aec_stop[3];
     const double* aec_weight;
+    /* organ AEC: tube output lowered over an angular sector (beamsettingsmodel.cpp:349-438) */
+    int32_t organ_aec;
+    double organ_aec_start_deg;
+    double organ_aec_stop_deg;
+    double organ_aec_ramp_deg;
+    double organ_aec_low_weight;
+    int32_t organ_aec_compensate;
+    /* dose calibration targets used when dxmcg_run_options.normalize is set:
+     * DX / CBCT: dose-area product (setDAPvalue, beamsettingsmodel.cpp:576);
+     * CT: CTDIvol, or CTDIw when ctdi_vol_mgy is 0, measured in a PMMA phantom of
+     * ctdi_diameter_cm (setCTDIvol / setCTDIw / setCTDIdiameter, :1054, :1278-1293) */
+    double dap_mgycm2;
+    double ctdi_vol_mgy;
+    double ctdi_w_mgy;
+    double ctdi_diameter_cm;
 } dxmcg_beam;
 
 /* One source pose (exposure(i) in beamactorcontainer.cpp:114-121). */
@@ -148,6 +163,7 @@ typedef struct {
     double kernel_ms;   /* device time of the transport launches (CUDA events) */
     double total_ms;    /* host wall time of the call */
     double dose_scale;  /* mGy per (keV / g) applied by the dose readout */
+    double calibration; /* factor applied to every history weight (1 unless normalize) */
 } dxmcg_stats;
 
 typedef struct dxmcg_world dxmcg_world;
@@ -225,6 +241,8 @@ DXMCG_API dxmcg_progress* dxmcg_progress_create(void);
 DXMCG_API void dxmcg_progress_destroy(dxmcg_progress* p);
 DXMCG_API void dxmcg_progress_get(const dxmcg_progress* p, uint64_t* done, uint64_t* total);
 DXMCG_API void dxmcg_progress_stop(dxmcg_progress* p);
+/* clears a stop request and the counters (a new simulation starts) */
+DXMCG_API void dxmcg_progress_reset(dxmcg_progress* p);
 DXMCG_API int dxmcg_progress_continue(const dxmcg_progress* p);
 DXMCG_API int dxmcg_progress_message(const dxmcg_progress* p, char* buf, int cap);
 

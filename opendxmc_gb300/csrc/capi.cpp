@@ -141,14 +141,21 @@ int ensureStream(dxmcg_world* w)
 }
 
 // Everything a launch needs for one beam on one world, uploaded into the world's buffers.
-int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, DevJob& J, uint64_t& nHist)
+int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, DevJob& J, uint64_t& nHist,
+    double& calibration)
 {
     HostJob hj;
     std::string err;
-    const int rc = buildHostJob(b, w->dims, w->spacing, hj, err);
+    int rc = buildHostJob(b, w->dims, w->spacing, hj, err);
     if (rc != DXMCG_OK)
         return fail(rc, err);
     nHist = hj.nHist;
+    rc = calibrationFactor(b, w->correction, o, hj.nHist, true, calibration, err);
+    if (rc != DXMCG_OK)
+        return fail(rc, err);
+    if (calibration != 1.0)
+        for (auto& e : hj.exposures)
+            e.weight = static_cast<float>(e.weight * calibration);
     DXMCG_CUDA(w->exps.alloc(hj.exposures.size()));
     DXMCG_CUDA(cudaMemcpyAsync(w->exps.p, hj.exposures.data(), hj.exposures.size() * sizeof(DevExposure),
         cudaMemcpyHostToDevice, w->stream));
@@ -542,9 +549,11 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
     DXMCG_CUDA(cudaSetDevice(w->device));
     DevJob J;
     uint64_t nHist = 0;
-    int rc = prepareJob(w, *beam, o, J, nHist);
+    double calibration = 1.0;
+    int rc = prepareJob(w, *beam, o, J, nHist, calibration);
     if (rc != DXMCG_OK)
         return rc;
+    DXMCG_CUDA(cudaSetDevice(w->device)); // the CTDI calibration may have run another world
     const uint64_t h0 = std::min<uint64_t>(o.hist_begin, nHist);
     const uint64_t h1 = o.hist_end == 0 ? nHist : std::min<uint64_t>(o.hist_end, nHist);
     if (progress) {
@@ -599,6 +608,7 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
         stats->kernel_ms = kernelMs;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->dose_scale = kKeVToMilliGrayGram / w->voxelVolume;
+        stats->calibration = calibration;
     }
     if (progress)
         progress->setMessage(cancelled ? "Cancelled" : "Done");
@@ -626,6 +636,15 @@ DXMCG_API void dxmcg_progress_stop(dxmcg_progress* p)
 {
     if (p)
         p->stop.store(1);
+}
+DXMCG_API void dxmcg_progress_reset(dxmcg_progress* p)
+{
+    if (!p)
+        return;
+    p->stop.store(0);
+    p->done.store(0);
+    p->total.store(1);
+    p->setMessage("");
 }
 DXMCG_API int dxmcg_progress_continue(const dxmcg_progress* p) { return p ? !p->stop.load() : 1; }
 DXMCG_API int dxmcg_progress_message(const dxmcg_progress* p, char* buf, int cap)
@@ -789,9 +808,11 @@ DXMCG_API int dxmcg_sample_source(dxmcg_world* w, const dxmcg_beam* beam, const 
     DXMCG_CUDA(cudaSetDevice(w->device));
     DevJob J;
     uint64_t nHist = 0;
-    int rc = prepareJob(w, *beam, o, J, nHist);
+    double calibration = 1.0;
+    int rc = prepareJob(w, *beam, o, J, nHist, calibration);
     if (rc != DXMCG_OK)
         return rc;
+    DXMCG_CUDA(cudaSetDevice(w->device));
     if (o.hist_begin + static_cast<uint64_t>(n) > nHist)
         return fail(DXMCG_ERR_ARGUMENT, "sample_source: history range beyond the beam");
     if (n == 0)

@@ -147,5 +147,10 @@ int transportMaxBlocksPerSMUnpacked(int block, int tracking);
 int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out);
 // sets the calling thread's dxmcg_last_error() text and returns code (capi.cpp)
 int reportError(int code, const std::string& msg);
+// dose calibration (calibration.cpp): DAP per history of the beam's spectrum, and the
+// factor F applied to every history weight when opts.normalize is set
+double dapPerHistory(const dxmcg_beam& b);
+int calibrationFactor(const dxmcg_beam& b, int correction, const dxmcg_run_options& o, uint64_t nHist,
+    bool allowPhantom, double& F, std::string& err);
 
 } // namespace dxmcg

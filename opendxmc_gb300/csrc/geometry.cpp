@@ -90,6 +90,47 @@ namespace {
         e.tube = 0;
         return e;
     }
+    // Organ AEC: the tube output is lowered to `low` over the gantry sector
+    // [start, stop] (degrees, counter-clockwise, wrapping at 360) and ramps back to 1
+    // linearly over `ramp` degrees on both sides.  With compensation the exposures
+    // outside the sector and its ramps are raised so that the mean weight is kept.
+    void applyOrganAec(const dxmcg_beam& b, const std::vector<double>& angleDeg, std::vector<dxmcg_exposure>& out)
+    {
+        if (!b.organ_aec || out.empty() || angleDeg.size() != out.size())
+            return;
+        const auto wrap = [](double a) {
+            a = std::fmod(a, 360.0);
+            return a < 0 ? a + 360.0 : a;
+        };
+        const double low = std::min(1.0, std::max(0.0, b.organ_aec_low_weight));
+        const double ramp = std::max(0.0, b.organ_aec_ramp_deg);
+        const double s0 = wrap(b.organ_aec_start_deg);
+        const double span = wrap(b.organ_aec_stop_deg - b.organ_aec_start_deg);
+        std::vector<double> f(out.size());
+        double lowered = 0.0;
+        size_t nOut = 0;
+        for (size_t i = 0; i < out.size(); ++i) {
+            const double d = wrap(angleDeg[i] - s0);
+            if (d <= span) {
+                f[i] = low;
+            } else {
+                const double dist = std::min(d - span, 360.0 - d);
+                f[i] = dist < ramp ? low + (1.0 - low) * dist / ramp : 1.0;
+            }
+            if (f[i] < 1.0)
+                lowered += f[i];
+            else
+                ++nOut;
+        }
+        if (b.organ_aec_compensate && nOut > 0) {
+            const double raise = (static_cast<double>(out.size()) - lowered) / static_cast<double>(nOut);
+            for (auto& x : f)
+                if (x >= 1.0)
+                    x = raise;
+        }
+        for (size_t i = 0; i < out.size(); ++i)
+            out[i].weight *= f[i];
+    }
 } // namespace
 
 int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out)
@@ -119,6 +160,7 @@ int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out)
     const double step = b.step_angle_deg * kPi / 180.0;
     const double a0 = b.start_angle_deg * kPi / 180.0;
     const V3 zaxis = { 0, 0, 1 };
+    std::vector<double> angles; // gantry angle of every exposure, degrees
     switch (b.type) {
     case DXMCG_BEAM_CT_SPIRAL:
     case DXMCG_BEAM_CT_SPIRAL_DUAL_ENERGY: {
@@ -142,6 +184,7 @@ int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out)
                 const double tubeShare = dual ? (t == 0 ? 2.0 * b.tube_a_weight : 2.0 * (1.0 - b.tube_a_weight)) : 1.0;
                 e.weight = aecAt(b, z) * tubeShare;
                 out.push_back(e);
+                angles.push_back((angle + (t == 1 ? 0.5 * kPi : 0.0)) * 180.0 / kPi);
             }
         }
         break;
@@ -156,6 +199,7 @@ int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out)
                 auto e = rotatingPose(iso, zaxis, a0 + i * step, sid, std::atan(0.5 * b.scan_fov_cm / sid), halfCone);
                 e.weight = aecAt(b, iso[2]);
                 out.push_back(e);
+                angles.push_back((a0 + i * step) * 180.0 / kPi);
             }
         }
         break;
@@ -167,9 +211,12 @@ int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out)
         const V3 axis = { b.rotation_axis[0], b.rotation_axis[1], b.rotation_axis[2] };
         if (dot(axis, axis) <= 0)
             return DXMCG_ERR_ARGUMENT;
-        for (long i = 0; i < m; ++i)
+        for (long i = 0; i < m; ++i) {
             out.push_back(rotatingPose(iso, axis, a0 + i * step, sid, b.half_angles[0], b.half_angles[1]));
-        return DXMCG_OK; // CBCT exposures are not AEC weighted
+            angles.push_back((a0 + i * step) * 180.0 / kPi);
+        }
+        applyOrganAec(b, angles, out); // CBCT exposures carry no z-AEC weight
+        return DXMCG_OK;
     }
     default:
         return DXMCG_ERR_ARGUMENT;
@@ -181,6 +228,7 @@ int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out)
     if (mean > 0)
         for (auto& e : out)
             e.weight /= mean;
+    applyOrganAec(b, angles, out);
     return DXMCG_OK;
 }
 

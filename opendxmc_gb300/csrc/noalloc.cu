@@ -166,6 +166,13 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     if (hj.exposures.size() > static_cast<size_t>(kMaxExposures))
         return fail(DXMCG_ERR_CAPACITY, "transport_run_noalloc: more than 4096 exposures (" +
                 std::to_string(hj.exposures.size()) + ") do not fit the scratch array");
+    double calibration = 1.0;
+    rc = calibrationFactor(*beam, correction, o, hj.nHist, false, calibration, err);
+    if (rc != DXMCG_OK)
+        return fail(rc, "transport_run_noalloc: " + err);
+    if (calibration != 1.0)
+        for (auto& e : hj.exposures)
+            e.weight = static_cast<float>(e.weight * calibration);
 
     unsigned char* base = nullptr;
     rc = scratchAddress(&base);
@@ -271,6 +278,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
         stats->kernel_ms = 0.0; // no CUDA events on this path: host wall time of launch + readback below
         stats->total_ms = ms;
         stats->dose_scale = 1.602176634e-10 / (spacing_cm[0] * spacing_cm[1] * spacing_cm[2]);
+        stats->calibration = calibration;
     }
     if (c.error_flags & kErrStepLimit)
         return fail(DXMCG_ERR_DEVICE, "transport_run_noalloc: a history exceeded the step limit");

@@ -31,7 +31,8 @@ EXPORTED = [
     "dxmcg_world_clear_tally", "dxmcg_world_read_tally", "dxmcg_world_read_dose", "dxmcg_world_tables",
     "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_transport_run_noalloc", "dxmcg_progress_create",
     "dxmcg_progress_destroy",
-    "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_continue", "dxmcg_progress_message",
+    "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_reset", "dxmcg_progress_continue",
+    "dxmcg_progress_message",
     "dxmcg_siddon_trace", "dxmcg_philox", "dxmcg_history_stream", "dxmcg_sample_compton", "dxmcg_sample_rayleigh",
     "dxmcg_sample_source",
 ]
@@ -98,6 +99,16 @@ class Beam(C.Structure):
         ("aec_start", C.c_double * 3),
         ("aec_stop", C.c_double * 3),
         ("aec_weight", C.POINTER(C.c_double)),
+        ("organ_aec", C.c_int32),
+        ("organ_aec_start_deg", C.c_double),
+        ("organ_aec_stop_deg", C.c_double),
+        ("organ_aec_ramp_deg", C.c_double),
+        ("organ_aec_low_weight", C.c_double),
+        ("organ_aec_compensate", C.c_int32),
+        ("dap_mgycm2", C.c_double),
+        ("ctdi_vol_mgy", C.c_double),
+        ("ctdi_w_mgy", C.c_double),
+        ("ctdi_diameter_cm", C.c_double),
     ]
 
 
@@ -117,7 +128,8 @@ class Stats(C.Structure):
     _fields_ = [("e_source", C.c_double), ("e_deposited", C.c_double), ("e_escaped", C.c_double)] + [
         (n, C.c_uint64) for n in ("n_histories", "n_missed", "n_visits", "n_photo", "n_compton", "n_rayleigh",
                                   "n_cutoff", "n_errors", "n_interacted")] + [
-        ("kernel_ms", C.c_double), ("total_ms", C.c_double), ("dose_scale", C.c_double)]
+        ("kernel_ms", C.c_double), ("total_ms", C.c_double), ("dose_scale", C.c_double),
+        ("calibration", C.c_double)]
 
     def as_dict(self) -> dict:
         return {f[0]: getattr(self, f[0]) for f in self._fields_}
@@ -165,6 +177,7 @@ def lib() -> C.CDLL:
         "dxmcg_progress_destroy": (None, [vp]),
         "dxmcg_progress_get": (None, [vp, pu64, pu64]),
         "dxmcg_progress_stop": (None, [vp]),
+        "dxmcg_progress_reset": (None, [vp]),
         "dxmcg_progress_continue": (i, [vp]),
         "dxmcg_progress_message": (i, [vp, cp, i]),
         "dxmcg_siddon_trace": (i, [i, pf, pf, pi32, pf, i, pi64, pf, pi32]),

@@ -472,8 +472,55 @@ static void rotating_exposure(const double iso[3], const double axis_in[3], doub
     e->tube = 0;
 }
 
+/* Organ AEC: tube output lowered to `low` over the gantry sector [start, stop]
+ * (degrees, counter-clockwise, wrapping), ramped back to 1 over `ramp` degrees on
+ * both sides; with compensation the exposures outside are raised to keep the mean. */
+static double wrap360(double a)
+{
+    a = fmod(a, 360.0);
+    return a < 0 ? a + 360.0 : a;
+}
+
+static void organ_aec(const or_beam* b, const double* gantry, or_exposure* out, int n)
+{
+    if (!b->organ_aec || n <= 0)
+        return;
+    double low = b->organ_aec_low_weight;
+    low = low < 0.0 ? 0.0 : (low > 1.0 ? 1.0 : low);
+    const double ramp = b->organ_aec_ramp_deg > 0.0 ? b->organ_aec_ramp_deg : 0.0;
+    const double s0 = wrap360(b->organ_aec_start_deg);
+    const double span = wrap360(b->organ_aec_stop_deg - b->organ_aec_start_deg);
+    double* f = (double*)malloc(n * sizeof(double));
+    double lowered = 0.0;
+    int n_out = 0;
+    for (int i = 0; i < n; ++i) {
+        const double d = wrap360(gantry[i] - s0);
+        if (d <= span) {
+            f[i] = low;
+        } else {
+            const double a = d - span, c = 360.0 - d;
+            const double dist = a < c ? a : c;
+            f[i] = dist < ramp ? low + (1.0 - low) * dist / ramp : 1.0;
+        }
+        if (f[i] < 1.0)
+            lowered += f[i];
+        else
+            n_out++;
+    }
+    if (b->organ_aec_compensate && n_out > 0) {
+        const double raise = ((double)n - lowered) / (double)n_out;
+        for (int i = 0; i < n; ++i)
+            if (f[i] >= 1.0)
+                f[i] = raise;
+    }
+    for (int i = 0; i < n; ++i)
+        out[i].weight *= f[i];
+    free(f);
+}
+
 int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
 {
+    double gantry[1 << 14];
     int n = 0;
     const double zaxis[3] = { 0, 0, 1 };
     if (b->type == OR_BEAM_DX || b->type == OR_BEAM_PENCIL) {
@@ -510,6 +557,8 @@ int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
             m = 1;
         const int dual = b->type == OR_BEAM_CT_SPIRAL_DUAL;
         n = (int)(dual ? 2 * m : m);
+        if (n > (1 << 14))
+            return 0; /* the oracle records at most 16384 gantry angles */
         if (!out)
             return n;
         if (n > cap)
@@ -527,12 +576,15 @@ int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
                 e->tube = t;
                 const double tw = dual ? (t == 0 ? 2.0 * b->tube_a_weight : 2.0 * (1.0 - b->tube_a_weight)) : 1.0;
                 e->weight = aec_weight(b, z) * tw;
+                gantry[dual ? 2 * i + t : i] = (ang + (t == 1 ? 0.5 * PI : 0.0)) * 180.0 / PI;
             }
         }
     } else if (b->type == OR_BEAM_CT_SEQUENTIAL) {
         const long per_rot = lround(2.0 * PI / step);
         const int slices = b->n_slices > 0 ? b->n_slices : 1;
         n = (int)(per_rot * slices);
+        if (n > (1 << 14))
+            return 0; /* the oracle records at most 16384 gantry angles */
         if (!out)
             return n;
         if (n > cap)
@@ -544,6 +596,7 @@ int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
                 or_exposure* e = &out[s * per_rot + i];
                 rotating_exposure(iso, zaxis, a0 + i * step, sid, atan(0.5 * b->scan_fov_cm / sid), half_cone, e);
                 e->weight = aec_weight(b, iso[2]);
+                gantry[s * per_rot + i] = (a0 + i * step) * 180.0 / PI;
             }
         }
     } else if (b->type == OR_BEAM_CBCT) {
@@ -552,13 +605,17 @@ int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
         if (m < 1)
             m = 1;
         n = (int)m;
+        if (n > (1 << 14))
+            return 0; /* the oracle records at most 16384 gantry angles */
         if (!out)
             return n;
         if (n > cap)
             return -n;
-        for (long i = 0; i < m; ++i)
+        for (long i = 0; i < m; ++i) {
             rotating_exposure(b->position, b->rotation_axis, a0 + i * step, sid, b->half_angles[0],
                 b->half_angles[1], &out[i]);
+            gantry[i] = (a0 + i * step) * 180.0 / PI;
+        }
     } else {
         return 0;
     }
@@ -572,6 +629,7 @@ int or_beam_exposures(const or_beam* b, or_exposure* out, int cap)
             for (int i = 0; i < n; ++i)
                 out[i].weight /= mean;
     }
+    organ_aec(b, gantry, out, n);
     return n;
 }
 

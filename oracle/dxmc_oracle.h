@@ -97,6 +97,18 @@ typedef struct {
     double aec_start[3];
     double aec_stop[3];
     const double* aec_weight;
+    /* organ AEC: lowered tube output over an angular sector (beamsettingsmodel.cpp:349-438) */
+    int32_t organ_aec;
+    double organ_aec_start_deg;
+    double organ_aec_stop_deg;
+    double organ_aec_ramp_deg;
+    double organ_aec_low_weight;
+    int32_t organ_aec_compensate;
+    /* calibration targets (not used by the oracle's transport) */
+    double dap_mgycm2;
+    double ctdi_vol_mgy;
+    double ctdi_w_mgy;
+    double ctdi_diameter_cm;
 } or_beam;
 
 typedef struct {

@@ -82,6 +82,16 @@ class Beam(C.Structure):
         ("aec_start", C.c_double * 3),
         ("aec_stop", C.c_double * 3),
         ("aec_weight", C.POINTER(C.c_double)),
+        ("organ_aec", C.c_int32),
+        ("organ_aec_start_deg", C.c_double),
+        ("organ_aec_stop_deg", C.c_double),
+        ("organ_aec_ramp_deg", C.c_double),
+        ("organ_aec_low_weight", C.c_double),
+        ("organ_aec_compensate", C.c_int32),
+        ("dap_mgycm2", C.c_double),
+        ("ctdi_vol_mgy", C.c_double),
+        ("ctdi_w_mgy", C.c_double),
+        ("ctdi_diameter_cm", C.c_double),
     ]
 
 

@@ -76,6 +76,14 @@ BEAMS = {
                "position": [0, 40, 0], "cosines": [[0, 0, 1], [-1, 0, 0]]},
     "dual_energy": dict(P.ct_spiral_params(particles=10), type=5, kvp_b=140.0, filters_b={13: 6.0, 50: 0.4},
                         tube_a_weight=0.4, fov_b_cm=33.0),
+    "ct_spiral_organ_aec": dict(P.ct_spiral_params(particles=10), organ_aec=1, organ_aec_start_deg=300.0,
+                                organ_aec_stop_deg=60.0, organ_aec_ramp_deg=20.0, organ_aec_low_weight=0.4,
+                                organ_aec_compensate=1),
+    "cbct_organ_aec": {"type": 3, "kvp": 90.0, "filters": {13: 4.0}, "particles_per_exposure": 10,
+                       "position": [0, 0, 0], "rotation_axis": [0, 0, 1], "start_angle_deg": 0.0,
+                       "stop_angle_deg": 358.0, "step_angle_deg": 2.0, "sdd_cm": 120.0, "half_angles": [0.17, 0.17],
+                       "organ_aec": 1, "organ_aec_start_deg": 45.0, "organ_aec_stop_deg": 135.0,
+                       "organ_aec_ramp_deg": 10.0, "organ_aec_low_weight": 0.2, "organ_aec_compensate": 0},
 }
 
 

@@ -196,6 +196,26 @@ def test_aec_weights_are_relative(oracle):
     assert w[-1] / w[0] == pytest.approx(3.0, rel=0.02)
 
 
+@pytest.mark.parametrize("compensate", [0, 1])
+def test_organ_aec_weights(oracle, compensate):
+    cp = dict(P.ct_spiral_params(particles=1, scan_cm=8.0), organ_aec=1, organ_aec_start_deg=332.5,
+              organ_aec_stop_deg=27.5, organ_aec_ramp_deg=12.0, organ_aec_low_weight=0.3,
+              organ_aec_compensate=compensate)
+    ex = oracle.beam_exposures(cp)
+    w = np.array([e["weight"] for e in ex])
+    ang = (np.arange(len(ex)) * 5.0) % 360.0
+    inside = (ang >= 332.5) | (ang <= 27.5)
+    ramp = ((ang > 27.5) & (ang < 39.5)) | ((ang > 320.5) & (ang < 332.5))
+    assert np.allclose(w[inside], 0.3)
+    assert np.all((w[ramp] > 0.3) & (w[ramp] < 1.0))
+    out = ~(inside | ramp)
+    if compensate:
+        assert w.mean() == pytest.approx(1.0)
+        assert np.allclose(w[out], w[out][0]) and w[out][0] > 1.0
+    else:
+        assert np.allclose(w[out], 1.0) and w.mean() < 1.0
+
+
 def test_oracle_energy_conservation(oracle):
     ph = parity.small_cylinder()
     w = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)

@@ -2,7 +2,8 @@
 
 Workload (one step): 256x256x200 seeded six-material torso at 1.5 mm, spiral CT
 120 kVp / 6 mm Al with the body bowtie, pitch 1.0, 40 mm collimation, 200 mm
-scan, 360 exposures x 2,777,778 = 1.00e9 histories, Woodcock tracking, FP64
+scan, 360 exposures x 2,777,778 = 1.00e9 histories, Woodcock tracking against
+the grid-wide majorant (--tracking macro|siddon for the other modes), FP64
 scoring.  Inputs are seeded synthetic data of the configured shape (no
 dataset exists for this path).
 
@@ -56,7 +57,12 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--tracking", choices=list(TRACKING), default="woodcock")
+    p.add_argument("--macro-cell", type=int, default=16, help="macro-cell edge in voxels (macro tracking)")
     return p.parse_args()
+
+
+TRACKING = {"woodcock": 0, "siddon": 1, "macro": 2}
 
 
 def dist_env():
@@ -233,10 +239,13 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    def run_opts(seed):
+        return G.run_options(seed=seed, stream=rank, tracking=TRACKING[args.tracking], macro_cell=args.macro_cell)
+
     def step(seed):
         flush.fill_(float(seed))
         torch.cuda.synchronize()
-        return gw.run(beam, G.run_options(seed=seed, stream=rank))
+        return gw.run(beam, run_opts(seed))
 
     for s in range(args.warmup):
         step(1000 + s)
@@ -258,10 +267,13 @@ def run_ours(args):
     value = total_done / dt
     kernel_ms = sum(s["kernel_ms"] for s in stats)
     visits = sum(s["n_visits"] for s in stats)
+    crossings = sum(s["n_crossings"] for s in stats)
     deposits = sum(s["n_photo"] + s["n_compton"] + s["n_cutoff"] for s in stats)
     chunk = 1 << 26
     launches_per_step = -(-hist // chunk)
-    alg_bytes = 4.0 * visits + 48.0 * deposits
+    # 4 B per voxel visit (packed word), 4 B per macro-cell crossing (cell scale),
+    # 48 B per deposit (read-modify-write of the 24-byte tally record)
+    alg_bytes = 4.0 * visits + 4.0 * crossings + 48.0 * deposits
     hbm, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -269,7 +281,8 @@ def run_ours(args):
             "traffic": TRAFFIC_BYTES_PER_LAUNCH,
             "alg_bytes_per_launch": alg_bytes / (args.steps * launches_per_step),
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step),
-            "visits_per_history": visits / done, "deposits_per_history": deposits / done}
+            "visits_per_history": visits / done, "crossings_per_history": crossings / done,
+            "deposits_per_history": deposits / done}
 
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None
@@ -286,7 +299,7 @@ def run_ours(args):
         def e2e_step(seed):
             gw.set_data(dens, mat)
             gw.build()
-            st = gw.run(beam, G.run_options(seed=seed, stream=rank))
+            st = gw.run(beam, run_opts(seed))
             gw.dose(out=outs)
             return st
 
@@ -314,7 +327,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": list(ph.dims), "voxel_mm": 1.5, "histories_per_step": hist,
-                       "exposures": 360, "tracking": "woodcock", "scoring": "fp64",
+                       "exposures": 360, "tracking": args.tracking,
+                       "macro_cell_voxels": args.macro_cell if args.tracking == "macro" else None, "scoring": "fp64",
                        "l2": "256 MB buffer written before every step; tally 420 MB > L2",
                        "parallelism": f"replicas x{world} (independent Philox streams)"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,

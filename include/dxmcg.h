@@ -61,7 +61,11 @@ typedef enum {
     DXMCG_BEAM_CT_SPIRAL_DUAL_ENERGY = 5
 } dxmcg_beam_type;
 
-typedef enum { DXMCG_TRACK_WOODCOCK = 0, DXMCG_TRACK_SIDDON = 1 } dxmcg_tracking;
+/* WOODCOCK: delta tracking against the grid-wide majorant mu_max(E).
+ * SIDDON: regular tracking with exact voxel path lengths.
+ * MACRO: delta tracking against a per-macro-cell majorant s_c mu_max(E), cells of
+ *        macro_cell^3 voxels; the sampled optical depth is spent cell by cell. */
+typedef enum { DXMCG_TRACK_WOODCOCK = 0, DXMCG_TRACK_SIDDON = 1, DXMCG_TRACK_MACRO = 2 } dxmcg_tracking;
 
 /* Material by mass fractions of elements: Material<5>::byWeight(map<Z, w>)
  * (simulationpipeline.cpp:136). Weights are normalised by the library. */
@@ -154,6 +158,7 @@ typedef struct {
     uint64_t hist_end;
     int32_t interact_batch; /* parked scatterings a warp gathers before sampling them, 0 = default */
     int32_t refill_batch;   /* dead lanes a warp gathers before starting new histories, 0 = default */
+    int32_t macro_cell;     /* MACRO tracking: cell edge in voxels, 0 = default (16) */
 } dxmcg_run_options;
 
 typedef struct {
@@ -164,6 +169,7 @@ typedef struct {
     double total_ms;    /* host wall time of the call */
     double dose_scale;  /* mGy per (keV / g) applied by the dose readout */
     double calibration; /* factor applied to every history weight (1 unless normalize) */
+    uint64_t n_crossings; /* MACRO tracking: macro-cell boundary crossings */
 } dxmcg_stats;
 
 typedef struct dxmcg_world dxmcg_world;

@@ -42,6 +42,38 @@ namespace {
             atomicOr(err, e);
     }
 
+    // One block per macro cell: the largest rho * ratio[m] over the cell's voxels,
+    // times (1 + 2^-20).  Transparent voxels contribute 0.
+    __global__ void macroScaleKernel(const uint32_t* __restrict__ vox, int nx, int ny, int nz, int mb, int mcx,
+        int mcy, const float* __restrict__ ratio, unsigned* __restrict__ scaleBits)
+    {
+        const int c = blockIdx.x;
+        const int cx = c % mcx, cy = (c / mcx) % mcy, cz = c / (mcx * mcy);
+        const int x0 = cx * mb, y0 = cy * mb, z0 = cz * mb;
+        const int ex = min(mb, nx - x0), ey = min(mb, ny - y0), ez = min(mb, nz - z0);
+        const int n = ex * ey * ez;
+        float best = 0.0f;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int ix = x0 + i % ex, iy = y0 + (i / ex) % ey, iz = z0 + i / (ex * ey);
+            const uint32_t w = vox[ix + static_cast<size_t>(nx) * (iy + static_cast<size_t>(ny) * iz)];
+            const int m = static_cast<int>(w & 0xffu);
+            if (m != DXMCG_TRANSPARENT_MATERIAL)
+                best = fmaxf(best, __uint_as_float(w & 0xffffff00u) * ratio[m]);
+        }
+        for (int o = 16; o > 0; o >>= 1)
+            best = fmaxf(best, __shfl_xor_sync(kFull, best, o));
+        __shared__ float warpBest[32];
+        if ((threadIdx.x & 31) == 0)
+            warpBest[threadIdx.x >> 5] = best;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float b = 0.0f;
+            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w)
+                b = fmaxf(b, warpBest[w]);
+            scaleBits[c] = __float_as_uint(b * (1.0f + 9.5367431640625e-7f));
+        }
+    }
+
     __global__ void finalizeKernel(const Tally* __restrict__ t, const uint32_t* __restrict__ vox, size_t n,
         double toDose, double nh, double* __restrict__ dose, double* __restrict__ var,
         unsigned long long* __restrict__ cnt)
@@ -179,6 +211,14 @@ cudaError_t launchPack(const double* dens64, const float* dens32, const uint8_t*
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int grid = static_cast<int>(std::min<size_t>(gridFor(n, 256), static_cast<size_t>(sms) * 8));
     packKernel<<<grid, 256, 0, s>>>(dens64, dens32, mat, vox, n, n_mats, rho_max_bits, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMacroScale(const uint32_t* vox, int nx, int ny, int nz, int mb, int mcx, int mcy,
+    const float* ratio, unsigned* scaleBits, cudaStream_t s)
+{
+    const int mcz = (nz + mb - 1) / mb;
+    macroScaleKernel<<<mcx * mcy * mcz, 256, 0, s>>>(vox, nx, ny, nz, mb, mcx, mcy, ratio, scaleBits);
     return cudaGetLastError();
 }
 

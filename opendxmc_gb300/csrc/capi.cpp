@@ -120,7 +120,12 @@ struct dxmcg_world {
     DeviceBuffer<DevSpectrum> spec;
     DeviceBuffer<DevBowtie> bowtie;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // host copies of the FP64 tables (tests)
+    // macro cells for MACRO tracking, built for one cell size at a time
+    DeviceBuffer<float> mscale;
+    DeviceBuffer<float> mratio;
+    int macroB = 0;
+    int mc[3] {};
+    std::vector<float> hostTot, hostMaj; // FP32 tables as uploaded
     std::vector<double> rhoMax;
     double historiesScored = 0.0;
     double voxelVolume = 0.0;
@@ -137,6 +142,37 @@ int ensureStream(dxmcg_world* w)
         DXMCG_CUDA(cudaEventCreate(&w->ev0));
     if (!w->ev1)
         DXMCG_CUDA(cudaEventCreate(&w->ev1));
+    return DXMCG_OK;
+}
+
+// Macro cells of B^3 voxels: ratio[m] = max over the table energies of
+// total_m(E) / majorant(E) (host), then s_c = max over the cell of rho * ratio[m]
+// (device, one block per cell).
+int ensureMacroCells(dxmcg_world* w, int B)
+{
+    if (w->macroB == B && w->mscale.p)
+        return DXMCG_OK;
+    const int M = static_cast<int>(w->materials.size());
+    std::vector<float> ratio(256, 0.0f);
+    for (int m = 0; m < M; ++m) {
+        double r = 0;
+        for (int i = 0; i < kNE; ++i)
+            if (w->hostMaj[i] > 0)
+                r = std::max(r, static_cast<double>(w->hostTot[m * kNE + i]) / w->hostMaj[i]);
+        ratio[m] = static_cast<float>(r);
+    }
+    for (int a = 0; a < 3; ++a)
+        w->mc[a] = (w->dims[a] + B - 1) / B;
+    const size_t nc = static_cast<size_t>(w->mc[0]) * w->mc[1] * w->mc[2];
+    DXMCG_CUDA(w->mratio.alloc(256));
+    DXMCG_CUDA(w->mscale.alloc(nc));
+    DXMCG_CUDA(cudaMemcpyAsync(w->mratio.p, ratio.data(), 256 * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    const cudaError_t e = launchMacroScale(w->vox.p, w->dims[0], w->dims[1], w->dims[2], B, w->mc[0], w->mc[1],
+        w->mratio.p, reinterpret_cast<unsigned*>(w->mscale.p), w->stream);
+    if (e != cudaSuccess)
+        return cudaFail(e, "macro-cell kernel");
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    w->macroB = B;
     return DXMCG_OK;
 }
 
@@ -179,6 +215,18 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
     J.tally = w->tally.p;
     J.exps = w->exps.p;
     J.spec = w->spec.p;
+    if (o.tracking == DXMCG_TRACK_MACRO) {
+        const int B = o.macro_cell > 0 ? std::min(o.macro_cell, 1024) : 16;
+        rc = ensureMacroCells(w, B);
+        if (rc != DXMCG_OK)
+            return rc;
+        J.mscale = w->mscale.p;
+        J.mb = B;
+        for (int a = 0; a < 3; ++a) {
+            J.mc[a] = w->mc[a];
+            J.cellL[a] = static_cast<float>(B * w->spacing[a]);
+        }
+    }
     return DXMCG_OK;
 }
 
@@ -408,6 +456,9 @@ DXMCG_API int dxmcg_world_build(dxmcg_world* w)
     std::vector<DevMaterial> dm(M);
     buildDeviceTables(w->materials.data(), M, w->correction, w->rhoMax.data(), tot.data(), xs.data(), majf.data(),
         dm.data());
+    w->hostTot = tot;
+    w->hostMaj = majf;
+    w->macroB = 0;
     DXMCG_CUDA(w->tot.alloc(tot.size()));
     DXMCG_CUDA(w->xs.alloc(xs.size()));
     DXMCG_CUDA(w->maj.alloc(kNE));
@@ -544,7 +595,7 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
     o.seed = 1;
     if (opts)
         o = *opts;
-    if (o.tracking != DXMCG_TRACK_WOODCOCK && o.tracking != DXMCG_TRACK_SIDDON)
+    if (o.tracking != DXMCG_TRACK_WOODCOCK && o.tracking != DXMCG_TRACK_SIDDON && o.tracking != DXMCG_TRACK_MACRO)
         return fail(DXMCG_ERR_ARGUMENT, "transport_run: unknown tracking mode");
     DXMCG_CUDA(cudaSetDevice(w->device));
     DevJob J;
@@ -605,6 +656,7 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
         stats->n_cutoff = c.cutoff;
         stats->n_errors = c.errors;
         stats->n_interacted = c.interacted;
+        stats->n_crossings = c.crossings;
         stats->kernel_ms = kernelMs;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->dose_scale = kKeVToMilliGrayGram / w->voxelVolume;

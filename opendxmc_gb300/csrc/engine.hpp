@@ -86,6 +86,11 @@ struct DevJob {
     int n_mats;
     int correction;
     Tally* tally;
+    // macro cells (MACRO tracking): scale s_c per cell of mb^3 voxels
+    const float* mscale;
+    int mc[3];
+    int mb;
+    float cellL[3]; // cell edge in cm
     // source
     const DevExposure* exps;
     int n_exp;
@@ -100,7 +105,7 @@ struct DevJob {
 
 struct DevCounters {
     unsigned long long next; // work-queue head (history index)
-    unsigned long long histories, missed, visits, photo, compton, rayleigh, cutoff, errors, interacted;
+    unsigned long long histories, missed, visits, photo, compton, rayleigh, cutoff, errors, interacted, crossings;
     double e_source, e_escaped, e_deposited;
     unsigned int error_flags;
 };
@@ -124,6 +129,9 @@ cudaError_t launchPack(const double* dens64, const float* dens32, const uint8_t*
     int n_mats, unsigned* rho_max_bits, unsigned* err, cudaStream_t s);
 cudaError_t launchTransport(const DevJob& job, unsigned long long h_end, DevCounters* ctr, LaunchShape shape,
     cudaStream_t s);
+// per-macro-cell majorant scale: max over the cell's voxels of rho * ratio[m]
+cudaError_t launchMacroScale(const uint32_t* vox, int nx, int ny, int nz, int mb, int mcx, int mcy,
+    const float* ratio, unsigned* scaleBits, cudaStream_t s);
 cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, double energy_to_dose,
     double n_histories, double* dose, double* var, unsigned long long* count, cudaStream_t s);
 cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int ny, int nz, float sx, float sy,

@@ -155,7 +155,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     if (opts)
         o = *opts;
     if (o.tracking != DXMCG_TRACK_WOODCOCK && o.tracking != DXMCG_TRACK_SIDDON)
-        return fail(DXMCG_ERR_ARGUMENT, "transport_run_noalloc: unknown tracking mode");
+        return fail(DXMCG_ERR_ARGUMENT, "transport_run_noalloc: Woodcock or Siddon tracking only");
 
     // host-side preparation; sizes are checked against the scratch capacity first
     HostJob hj;

@@ -163,6 +163,91 @@ namespace {
         return true;
     }
 
+    // Delta tracking against the macro cell's majorant s_c mu_max(E): the sampled
+    // optical depth is spent cell by cell (cell indices advance as integers, so every
+    // crossing makes progress); a tentative collision in the cell is real with
+    // probability mu(voxel) / (s_c mu_max).  True on a real collision.
+    template <bool PACKED>
+    __device__ __forceinline__ bool macroFlight(const DevJob& J, Photon& ph, Rng& rng, const EnergyCache& ec, int& cx,
+        int& cy, int& cz, bool& escaped, uint32_t& v, int& m, unsigned& visits, unsigned& crossings, unsigned& err)
+    {
+        float tau = fmaxf(-__logf(rng.u()), 0.0f);
+        const float ix = __frcp_rn(ph.dx), iy = __frcp_rn(ph.dy), iz = __frcp_rn(ph.dz);
+        float muc = 0.0f;
+        for (int guard = 0;; ++guard) {
+            if (guard > (1 << 16)) { // cannot happen: each pass moves one cell along a fixed direction
+                err |= kErrStepLimit;
+                escaped = true;
+                return false;
+            }
+            muc = __ldg(J.mscale + cx + J.mc[0] * (cy + J.mc[1] * cz)) * ec.mmax;
+            float tx = FLT_MAX;
+            int ax = 0;
+            if (ph.dx != 0.0f) {
+                const float b = fminf(static_cast<float>(cx + (ph.dx > 0.0f ? 1 : 0)) * J.cellL[0], J.L[0]);
+                tx = (b - ph.px) * ix;
+            }
+            if (ph.dy != 0.0f) {
+                const float b = fminf(static_cast<float>(cy + (ph.dy > 0.0f ? 1 : 0)) * J.cellL[1], J.L[1]);
+                const float t = (b - ph.py) * iy;
+                if (t < tx) {
+                    tx = t;
+                    ax = 1;
+                }
+            }
+            if (ph.dz != 0.0f) {
+                const float b = fminf(static_cast<float>(cz + (ph.dz > 0.0f ? 1 : 0)) * J.cellL[2], J.L[2]);
+                const float t = (b - ph.pz) * iz;
+                if (t < tx) {
+                    tx = t;
+                    ax = 2;
+                }
+            }
+            tx = fmaxf(tx, 0.0f);
+            if (tau < muc * tx) {
+                const float t = tau / muc;
+                ph.px = fmaf(t, ph.dx, ph.px);
+                ph.py = fmaf(t, ph.dy, ph.py);
+                ph.pz = fmaf(t, ph.dz, ph.pz);
+                break;
+            }
+            tau -= muc * tx;
+            ph.px = fmaf(tx, ph.dx, ph.px);
+            ph.py = fmaf(tx, ph.dy, ph.py);
+            ph.pz = fmaf(tx, ph.dz, ph.pz);
+            ++crossings;
+            bool out;
+            if (ax == 0) {
+                cx += ph.dx > 0.0f ? 1 : -1;
+                out = cx < 0 || cx >= J.mc[0];
+            } else if (ax == 1) {
+                cy += ph.dy > 0.0f ? 1 : -1;
+                out = cy < 0 || cy >= J.mc[1];
+            } else {
+                cz += ph.dz > 0.0f ? 1 : -1;
+                out = cz < 0 || cz >= J.mc[2];
+            }
+            if (out) {
+                escaped = true;
+                return false;
+            }
+        }
+        // the voxel of the tentative collision, kept inside the current cell
+        const int vx = min(max(static_cast<int>(ph.px * J.isp[0]), cx * J.mb), min(cx * J.mb + J.mb, J.nx) - 1);
+        const int vy = min(max(static_cast<int>(ph.py * J.isp[1]), cy * J.mb), min(cy * J.mb + J.mb, J.ny) - 1);
+        const int vz = min(max(static_cast<int>(ph.pz * J.isp[2]), cz * J.mb), min(cz * J.mb + J.mb, J.nz) - 1);
+        ph.px = fminf(fmaxf(ph.px, 0.0f), J.Lin[0]);
+        ph.py = fminf(fmaxf(ph.py, 0.0f), J.Lin[1]);
+        ph.pz = fminf(fmaxf(ph.pz, 0.0f), J.Lin[2]);
+        ++visits;
+        v = static_cast<uint32_t>(vx + J.nx * (vy + J.ny * vz));
+        const float rho = voxelAt<PACKED>(J, v, m);
+        if (m == DXMCG_TRANSPARENT_MATERIAL)
+            return false;
+        const float mu = rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
+        return rng.u() * muc < mu;
+    }
+
     template <int TRACKING, bool PACKED = true>
     __global__ void __launch_bounds__(256) transportKernel(const DevJob J, unsigned long long h_end,
         DevCounters* __restrict__ ctr, int refillBatch, int interactBatch)
@@ -184,7 +269,8 @@ namespace {
         EnergyCache ec { 0, 0.0f, 1.0f, 1.0f };
         uint32_t pv = 0; // voxel of the parked interaction
         int pm = 0;      // its material
-        unsigned steps = 0, visits = 0, err = 0;
+        unsigned steps = 0, visits = 0, crossings = 0, err = 0;
+        int cx = 0, cy = 0, cz = 0; // macro cell of the photon (MACRO tracking)
         bool fresh = false;
         KahanSum esrc, eesc, edep; // FP32 compensated sums: no FP64 on the per-event path
 
@@ -223,10 +309,15 @@ namespace {
                         st = kStepping;
                         steps = 0;
                         fresh = true;
-                        if (TRACKING == DXMCG_TRACK_WOODCOCK)
-                            ec.set(J, ph.E);
-                        else
+                        if (TRACKING == DXMCG_TRACK_SIDDON)
                             gridPos(ph.E, ec.ie, ec.fe);
+                        else
+                            ec.set(J, ph.E);
+                        if (TRACKING == DXMCG_TRACK_MACRO) {
+                            cx = min(static_cast<int>(ph.px / J.cellL[0]), J.mc[0] - 1);
+                            cy = min(static_cast<int>(ph.py / J.cellL[1]), J.mc[1] - 1);
+                            cz = min(static_cast<int>(ph.pz / J.cellL[2]), J.mc[2] - 1);
+                        }
                     } else {
                         eesc.add(ph.w * ph.E);
                     }
@@ -261,10 +352,10 @@ namespace {
                         cut = true;
                     } else {
                         st = kStepping;
-                        if (TRACKING == DXMCG_TRACK_WOODCOCK)
-                            ec.set(J, ph.E);
-                        else
+                        if (TRACKING == DXMCG_TRACK_SIDDON)
                             gridPos(ph.E, ec.ie, ec.fe);
+                        else
+                            ec.set(J, ph.E);
                     }
                 } else if (st == kRayleigh) {
                     const float cost = sampleRayleigh(ph.E, J.mats + pm, rng, err);
@@ -293,9 +384,13 @@ namespace {
                 bool escaped = false;
                 uint32_t v = 0;
                 int m = 0;
-                const bool real = TRACKING == DXMCG_TRACK_WOODCOCK
-                    ? woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits)
-                    : siddonFlight<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
+                bool real;
+                if (TRACKING == DXMCG_TRACK_WOODCOCK)
+                    real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
+                else if (TRACKING == DXMCG_TRACK_SIDDON)
+                    real = siddonFlight<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
+                else
+                    real = macroFlight<PACKED>(J, ph, rng, ec, cx, cy, cz, escaped, v, m, visits, crossings, err);
                 if (escaped) {
                     eesc.add(ph.w * ph.E);
                     st = kDead;
@@ -341,6 +436,7 @@ namespace {
 
         // ---- flush: per-lane sums by warp, block counters by one thread
         const unsigned long long vi = warpSum(static_cast<unsigned long long>(visits));
+        const unsigned long long cr = warpSum(static_cast<unsigned long long>(crossings));
         const double es = warpSum(esrc.value());
         const double ee = warpSum(eesc.value());
         const double ed = warpSum(edep.value());
@@ -351,6 +447,8 @@ namespace {
         __syncwarp();
         if (lane == 0) {
             atomicAdd(&ctr->visits, vi);
+            if (cr)
+                atomicAdd(&ctr->crossings, cr);
             atomicAdd(&ctr->e_source, es);
             atomicAdd(&ctr->e_escaped, ee);
             atomicAdd(&ctr->e_deposited, ed);
@@ -369,60 +467,69 @@ namespace {
 
 } // namespace
 
+namespace {
+    using TransportFn = void (*)(const DevJob, unsigned long long, DevCounters*, int, int);
+
+    // kernel instance for a tracking mode on the packed (world) or unpacked
+    // (caller-owned arrays) voxel layout; nullptr where no instance exists
+    TransportFn kernelFor(int tracking, bool packed)
+    {
+        if (packed) {
+            switch (tracking) {
+            case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, true>;
+            case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, true>;
+            case DXMCG_TRACK_MACRO: return transportKernel<DXMCG_TRACK_MACRO, true>;
+            default: return nullptr;
+            }
+        }
+        switch (tracking) {
+        case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, false>;
+        case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, false>;
+        default: return nullptr;
+        }
+    }
+
+    cudaError_t launchWith(TransportFn fn, const DevJob& job, unsigned long long h_end, DevCounters* ctr,
+        LaunchShape shape, cudaStream_t s)
+    {
+        if (!fn)
+            return cudaErrorInvalidValue;
+        const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
+        const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
+        fn<<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill, interact);
+        return cudaGetLastError();
+    }
+
+    int residentBlocks(TransportFn fn, int block)
+    {
+        int n = 0;
+        if (!fn || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, 0) != cudaSuccess)
+            return 1;
+        return n > 0 ? n : 1;
+    }
+} // namespace
+
 cudaError_t launchTransport(const DevJob& job, unsigned long long h_end, DevCounters* ctr, LaunchShape shape,
     cudaStream_t s)
 {
-    const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
-    const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
-    if (job.tracking == DXMCG_TRACK_SIDDON)
-        transportKernel<DXMCG_TRACK_SIDDON><<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill, interact);
-    else
-        transportKernel<DXMCG_TRACK_WOODCOCK><<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill, interact);
-    return cudaGetLastError();
+    return launchWith(kernelFor(job.tracking, true), job, h_end, ctr, shape, s);
 }
 
 cudaError_t launchTransportUnpacked(const DevJob& job, unsigned long long h_end, DevCounters* ctr,
     LaunchShape shape, cudaStream_t s)
 {
-    const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
-    const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
-    if (job.tracking == DXMCG_TRACK_SIDDON)
-        transportKernel<DXMCG_TRACK_SIDDON, false><<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill, interact);
-    else
-        transportKernel<DXMCG_TRACK_WOODCOCK, false><<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill,
-            interact);
-    return cudaGetLastError();
+    return launchWith(kernelFor(job.tracking, false), job, h_end, ctr, shape, s);
 }
 
-int transportMaxBlocksPerSMUnpacked(int block, int tracking)
-{
-    int n = 0;
-    const cudaError_t e = tracking == DXMCG_TRACK_SIDDON
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transportKernel<DXMCG_TRACK_SIDDON, false>, block, 0)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transportKernel<DXMCG_TRACK_WOODCOCK, false>, block, 0);
-    if (e != cudaSuccess)
-        return 1;
-    return n > 0 ? n : 1;
-}
+int transportMaxBlocksPerSMUnpacked(int block, int tracking) { return residentBlocks(kernelFor(tracking, false), block); }
 
-int transportMaxBlocksPerSM(int block, int tracking)
-{
-    int n = 0;
-    const cudaError_t e = tracking == DXMCG_TRACK_SIDDON
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transportKernel<DXMCG_TRACK_SIDDON>, block, 0)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transportKernel<DXMCG_TRACK_WOODCOCK>, block, 0);
-    if (e != cudaSuccess)
-        return 1;
-    return n > 0 ? n : 1;
-}
+int transportMaxBlocksPerSM(int block, int tracking) { return residentBlocks(kernelFor(tracking, true), block); }
 
 int transportRegistersPerThread(int tracking)
 {
     cudaFuncAttributes a {};
-    const cudaError_t e = tracking == DXMCG_TRACK_SIDDON
-        ? cudaFuncGetAttributes(&a, transportKernel<DXMCG_TRACK_SIDDON>)
-        : cudaFuncGetAttributes(&a, transportKernel<DXMCG_TRACK_WOODCOCK>);
-    return e == cudaSuccess ? a.numRegs : -1;
+    const TransportFn fn = kernelFor(tracking, true);
+    return fn && cudaFuncGetAttributes(&a, fn) == cudaSuccess ? a.numRegs : -1;
 }
 
 } // namespace dxmcg

@@ -16,7 +16,7 @@ LIB_PATH = PKG / "_lib" / "libdxmcg.so"
 
 MAX_ELEMENTS = 16
 NE = 300
-TRACK_WOODCOCK, TRACK_SIDDON = 0, 1
+TRACK_WOODCOCK, TRACK_SIDDON, TRACK_MACRO = 0, 1, 2
 BEAM_DX, BEAM_CT_SPIRAL, BEAM_CT_SEQUENTIAL, BEAM_CBCT, BEAM_PENCIL, BEAM_CT_SPIRAL_DUAL_ENERGY = range(6)
 
 STATUS = {0: "OK", -1: "ARGUMENT", -2: "CUDA", -3: "STATE", -4: "CANCELLED", -5: "DEVICE", -6: "NO_DEVICE",
@@ -121,7 +121,7 @@ class RunOptions(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("stream", C.c_uint32), ("tracking", C.c_int32), ("normalize", C.c_int32),
                 ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk_histories_log2", C.c_int32),
                 ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64), ("interact_batch", C.c_int32),
-                ("refill_batch", C.c_int32)]
+                ("refill_batch", C.c_int32), ("macro_cell", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -129,7 +129,7 @@ class Stats(C.Structure):
         (n, C.c_uint64) for n in ("n_histories", "n_missed", "n_visits", "n_photo", "n_compton", "n_rayleigh",
                                   "n_cutoff", "n_errors", "n_interacted")] + [
         ("kernel_ms", C.c_double), ("total_ms", C.c_double), ("dose_scale", C.c_double),
-        ("calibration", C.c_double)]
+        ("calibration", C.c_double), ("n_crossings", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {f[0]: getattr(self, f[0]) for f in self._fields_}

@@ -935,6 +935,9 @@ struct or_world {
     double* coh;
     double* tot;
     double maj[OR_NE]; /* 1/cm */
+    int mb;            /* macro-cell edge in voxels (0: none) */
+    int mc[3];
+    double* mscale;    /* per macro cell: majorant scale s_c */
     double* e;
     double* e2;
     uint64_t* cnt;
@@ -1014,6 +1017,7 @@ void or_world_destroy(or_world* w)
     free(w->e);
     free(w->e2);
     free(w->cnt);
+    free(w->mscale);
     free(w);
 }
 
@@ -1362,8 +1366,86 @@ static void run_history(run_ctx* c, uint64_t h, or_stats* st)
         if (p[a] >= L[a])
             p[a] = nextafter(L[a], 0.0);
     }
+    int cell[3] = { 0, 0, 0 };
+    if (c->tracking == OR_TRACK_MACRO) {
+        if (!w->mscale) {
+            st->n_errors++;
+            return;
+        }
+        for (int a = 0; a < 3; ++a) {
+            int k = (int)floor(p[a] / (w->mb * w->sp[a]));
+            cell[a] = k < 0 ? 0 : (k > w->mc[a] - 1 ? w->mc[a] - 1 : k);
+        }
+    }
     for (long step = 0; step < MAX_STEPS; ++step) {
-        if (c->tracking == OR_TRACK_WOODCOCK) {
+        if (c->tracking == OR_TRACK_MACRO) {
+            /* delta tracking against the macro cell's majorant s_c * mu_max(E):
+             * the sampled optical depth is spent cell by cell; a tentative collision
+             * inside the cell is real with probability mu(voxel) / (s_c mu_max) */
+            int ie;
+            double fe;
+            grid_pos(E, &ie, &fe);
+            const double mmax = lerp_tab(w->maj, ie, fe);
+            double tau = -log(rng_u(&r));
+            for (;;) {
+                const size_t ci = (size_t)cell[0] + (size_t)w->mc[0] * ((size_t)cell[1] + (size_t)w->mc[1] * cell[2]);
+                const double muc = w->mscale[ci] * mmax;
+                double tx = DBL_MAX;
+                int ax = -1;
+                for (int a = 0; a < 3; ++a) {
+                    if (d[a] == 0.0)
+                        continue;
+                    double b = (cell[a] + (d[a] > 0.0 ? 1 : 0)) * w->mb * w->sp[a];
+                    if (b > L[a])
+                        b = L[a];
+                    const double t = (b - p[a]) / d[a];
+                    if (t < tx) {
+                        tx = t;
+                        ax = a;
+                    }
+                }
+                if (tx < 0.0)
+                    tx = 0.0;
+                if (muc > 0.0 && tau < muc * tx) {
+                    const double t = tau / muc;
+                    for (int a = 0; a < 3; ++a)
+                        p[a] += t * d[a];
+                    break;
+                }
+                tau -= muc * tx;
+                for (int a = 0; a < 3; ++a)
+                    p[a] += tx * d[a];
+                st->n_crossings++;
+                cell[ax] += d[ax] > 0.0 ? 1 : -1;
+                if (cell[ax] < 0 || cell[ax] >= w->mc[ax]) {
+                    st->e_escaped += wgt * E;
+                    return;
+                }
+            }
+            /* voxel of the tentative collision, kept inside the current cell */
+            int vi[3];
+            for (int a = 0; a < 3; ++a) {
+                int k = (int)floor(p[a] / w->sp[a]);
+                const int lo = cell[a] * w->mb, hi = lo + w->mb - 1 < w->n[a] - 1 ? lo + w->mb - 1 : w->n[a] - 1;
+                vi[a] = k < lo ? lo : (k > hi ? hi : k);
+                if (p[a] < 0.0)
+                    p[a] = 0.0;
+                if (p[a] >= L[a])
+                    p[a] = nextafter(L[a], 0.0);
+            }
+            const size_t v = (size_t)vi[0] + (size_t)w->n[0] * ((size_t)vi[1] + (size_t)w->n[1] * vi[2]);
+            st->n_visits++;
+            const int m = w->material[v];
+            const size_t ci = (size_t)cell[0] + (size_t)w->mc[0] * ((size_t)cell[1] + (size_t)w->mc[1] * cell[2]);
+            const double muc = w->mscale[ci] * mmax;
+            if (m == OR_TRANSPARENT)
+                continue;
+            const double mu = w->density[v] * lerp_tab(w->tot + m * OR_NE, ie, fe);
+            if (rng_u(&r) * muc < mu) {
+                if (!interact(w, v, m, &E, wgt, d, &r, st, &first))
+                    return;
+            }
+        } else if (c->tracking == OR_TRACK_WOODCOCK) {
             int ie;
             double fe;
             grid_pos(E, &ie, &fe);
@@ -1457,6 +1539,7 @@ static void* worker(void* arg)
     c->tot.n_cutoff += st.n_cutoff;
     c->tot.n_errors += st.n_errors;
     c->tot.n_interacted += st.n_interacted;
+    c->tot.n_crossings += st.n_crossings;
     pthread_mutex_unlock(&c->lock);
     return NULL;
 }
@@ -1586,4 +1669,45 @@ void or_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, 
         for (int k = 0; k < n_draws; ++k)
             out[(size_t)i * n_draws + k] = rng_raw(&r);
     }
+}
+
+/* Macro cells of B x B x B voxels.  s_c bounds mu(voxel, E) / mu_max(E) over the cell
+ * for every table energy: s_c = max over its voxels of rho * r_m (times a small
+ * safety factor), r_m = max_E mu_m(E) / mu_max(E). */
+int or_world_set_macro(or_world* w, int B, double* scale_out)
+{
+    if (B < 1)
+        return -1;
+    double r[256];
+    for (int m = 0; m < w->n_mats; ++m) {
+        double mx = 0.0;
+        for (int i = 0; i < OR_NE; ++i)
+            if (w->maj[i] > 0.0) {
+                const double q = w->tot[m * OR_NE + i] / w->maj[i];
+                if (q > mx)
+                    mx = q;
+            }
+        r[m] = mx;
+    }
+    free(w->mscale);
+    w->mb = B;
+    for (int a = 0; a < 3; ++a)
+        w->mc[a] = (w->n[a] + B - 1) / B;
+    const size_t nc = (size_t)w->mc[0] * w->mc[1] * w->mc[2];
+    w->mscale = (double*)calloc(nc, sizeof(double));
+    for (int k = 0; k < w->n[2]; ++k)
+        for (int j = 0; j < w->n[1]; ++j)
+            for (int i = 0; i < w->n[0]; ++i) {
+                const size_t v = (size_t)i + (size_t)w->n[0] * ((size_t)j + (size_t)w->n[1] * k);
+                const int m = w->material[v];
+                if (m >= w->n_mats)
+                    continue;
+                const double s = w->density[v] * r[m] * MAJ_SAFETY;
+                const size_t c = (size_t)(i / B) + (size_t)w->mc[0] * ((size_t)(j / B) + (size_t)w->mc[1] * (k / B));
+                if (s > w->mscale[c])
+                    w->mscale[c] = s;
+            }
+    if (scale_out)
+        memcpy(scale_out, w->mscale, nc * sizeof(double));
+    return (int)nc;
 }

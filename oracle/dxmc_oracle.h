@@ -36,7 +36,7 @@ extern "C" {
 #define OR_MAX_ELEMENTS 16
 #define OR_TRANSPARENT 255
 
-enum { OR_TRACK_WOODCOCK = 0, OR_TRACK_SIDDON = 1 };
+enum { OR_TRACK_WOODCOCK = 0, OR_TRACK_SIDDON = 1, OR_TRACK_MACRO = 2 };
 enum {
     OR_BEAM_DX = 0,
     OR_BEAM_CT_SPIRAL = 1,
@@ -123,7 +123,7 @@ typedef struct {
 typedef struct {
     double e_source, e_deposited, e_escaped;
     uint64_t n_histories, n_missed, n_visits, n_real, n_photo, n_compton, n_rayleigh,
-        n_deposits, n_cutoff, n_errors, n_interacted;
+        n_deposits, n_cutoff, n_errors, n_interacted, n_crossings;
 } or_stats;
 
 typedef struct or_world or_world;
@@ -167,6 +167,8 @@ void or_world_destroy(or_world* w);
 void or_world_clear(or_world* w);
 int or_world_table(const or_world* w, int m, double* photo, double* incoh, double* coh);
 int or_world_majorant(const or_world* w, double* maj);
+/* macro cells of B^3 voxels with majorant scales (for OR_TRACK_MACRO); fills scale if not NULL */
+int or_world_set_macro(or_world* w, int B, double* scale_out);
 int or_transport(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, int tracking,
     int n_threads, uint64_t hist_begin, uint64_t hist_end, or_stats* stats);
 int or_sample_source(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, uint64_t h0, int n,

@@ -24,6 +24,7 @@ MAX_ELEMENTS = 16
 
 TRACK_WOODCOCK = 0
 TRACK_SIDDON = 1
+TRACK_MACRO = 2
 BEAM_DX, BEAM_CT_SPIRAL, BEAM_CT_SEQUENTIAL, BEAM_CBCT, BEAM_PENCIL, BEAM_CT_SPIRAL_DUAL = range(6)
 
 
@@ -121,6 +122,7 @@ class Stats(C.Structure):
             "n_cutoff",
             "n_errors",
             "n_interacted",
+            "n_crossings",
         )
     ]
 
@@ -388,6 +390,15 @@ class World:
         p, ic, co = (np.zeros(NE) for _ in range(3))
         lib().or_world_table(self._h, m, _p(p, C.c_double), _p(ic, C.c_double), _p(co, C.c_double))
         return p, ic, co
+
+    def set_macro(self, B: int) -> np.ndarray:
+        L = lib()
+        L.or_world_set_macro.restype = C.c_int
+        L.or_world_set_macro.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        n = L.or_world_set_macro(self._h, B, None)
+        out = np.zeros(max(n, 0))
+        L.or_world_set_macro(self._h, B, _p(out, C.c_double))
+        return out
 
     def majorant(self):
         m = np.zeros(NE)

@@ -130,6 +130,53 @@ def test_c2_spiral_ct_torso_independent_streams(gpu, oracle):
     assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
 
 
+@pytest.mark.parametrize("cell", [8, 16])
+def test_macro_tracking_matches_oracle(c1, gpu, cell):
+    """Macro-cell majorants: shared streams follow the oracle's histories; the
+    independent-stream estimate agrees within 3 combined standard errors."""
+    ph, gw, ow = c1
+    ow.set_macro(cell)
+    beam = P.dx_beam_params(particles=200_000, exposures=5)
+    gw.clear()
+    ow.clear()
+    sg = gw.run(beam, gpu.run_options(seed=13, stream=6, tracking=2, macro_cell=cell))
+    so = ow.run(beam, seed=13, stream=6, tracking=oracle_macro())
+    assert sg["n_errors"] == 0 and sg["n_crossings"] > 0
+    assert sg["n_visits"] == pytest.approx(so["n_visits"], rel=2e-3)
+    assert sg["n_crossings"] == pytest.approx(so["n_crossings"], rel=2e-3)
+    for k in ("n_photo", "n_compton", "n_rayleigh", "n_interacted"):
+        assert sg[k] == pytest.approx(so[k], rel=2e-3), k
+    e1, _, _ = gw.tally()
+    e2, _, _ = ow.tally()
+    assert e1.sum() == pytest.approx(e2.sum(), rel=2e-3)
+    gw.clear()
+    ow.clear()
+    sg = gw.run(beam, gpu.run_options(seed=14, stream=0, tracking=2, macro_cell=cell))
+    ow.run(beam, seed=14, stream=1, tracking=0)
+    frac, nvox, e1, e2 = compare(gw, ow, sg["n_histories"])
+    assert nvox > 5000 and frac >= 0.99
+    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+
+
+def oracle_macro():
+    from oracle import oracle as O
+
+    return O.TRACK_MACRO
+
+
+def test_macro_tracking_c2_torso(gpu, oracle):
+    ph = P.torso_phantom(seed=2)
+    gw = gpu_world(gpu, ph)
+    ow = oracle_world_on_packed(oracle, gw, ph)
+    beam = P.ct_spiral_params(particles=5000)
+    sg = gw.run(beam, gpu.run_options(seed=3, stream=0, tracking=2))
+    ow.run(beam, seed=3, stream=1)
+    assert sg["n_visits"] < 0.4 * 20.5 * sg["n_histories"]  # far fewer voxel lookups than global Woodcock
+    frac, nvox, e1, e2 = compare(gw, ow, sg["n_histories"])
+    assert nvox > 2000 and frac >= 0.99
+    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+
+
 def test_siddon_tracking_matches_woodcock(gpu):
     ph = parity.small_torso(scale=2)
     gw = gpu_world(gpu, ph)

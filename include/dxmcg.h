@@ -217,6 +217,39 @@ DXMCG_API int dxmcg_world_packed_density(dxmcg_world* w, float* density, uint8_t
 DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts,
     dxmcg_progress* progress, dxmcg_stats* stats);
 
+/* ---- batches: many (world, beam) jobs in one persistent launch --------------
+ * No counterpart in the reference, which runs one beam per Transport call
+ * (simulationpipeline.cpp:165).  All jobs draw from one shared history queue, so
+ * a batch of small or uneven jobs keeps every SM busy until the last history.
+ * Job j runs histories 0..N_j-1 of beams[j] with opts[j].seed and opts[j].stream
+ * and deposits into worlds[j]'s tally: the same histories, hence the same tallies
+ * up to the summation order, as dxmcg_transport_run(worlds[j], beams + j,
+ * opts + j, ...).  A world may appear in several jobs (their doses add).
+ * Requirements: every world built and on one device, one tracking mode for all
+ * jobs (launch shape from opts[0]), hist_begin = hist_end = 0, one macro_cell
+ * per world.  Exposures, spectra and calibrations are fixed at create time; the
+ * worlds must outlive the batch and must not run other transports meanwhile.
+ * The first dxmcg_batch_run captures a CUDA graph (counter reset + the launch)
+ * that every later run replays; each run adds N_j histories to world j's dose
+ * normalisation.  stats are summed over all jobs (calibration: job 0's). */
+typedef struct dxmcg_batch dxmcg_batch;
+DXMCG_API int dxmcg_batch_create(int n_jobs, dxmcg_world* const* worlds, const dxmcg_beam* beams,
+    const dxmcg_run_options* opts, dxmcg_batch** out);
+/* histories and calibration factor per job (arrays of n_jobs, each may be NULL) */
+DXMCG_API int dxmcg_batch_info(const dxmcg_batch* b, int* n_jobs, uint64_t* job_histories, double* job_calibration);
+DXMCG_API int dxmcg_batch_run(dxmcg_batch* b, dxmcg_stats* stats);
+DXMCG_API void dxmcg_batch_destroy(dxmcg_batch* b);
+
+/* ---- launch-shape autotuner ----------------------------------------------------
+ * No counterpart in the reference.  Times the transport kernel on
+ * sample_histories (0: 2^24) histories from the middle of the beam for each
+ * block size {128, 256} x interact batch {8, 12, 16, 24} x refill batch
+ * {4, 8, 16}, depositing into a scratch tally (the world's dose is untouched),
+ * and writes the fastest block_size / interact_batch / refill_batch into *opts
+ * (blocks_per_sm = 0: all resident blocks).  histories_per_second may be NULL. */
+DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_options* opts,
+    uint64_t sample_histories, double* histories_per_second);
+
 /* ---- transport that allocates no device memory ------------------------------
  * No counterpart in the reference.  For callers that may not call cudaMalloc or
  * any other device allocator while they run (their GPU memory comes only from

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -77,6 +78,13 @@ struct DeviceBuffer {
 
 constexpr double kKeVToMilliGrayGram = 1.602176634e-10; // mGy * g per keV
 constexpr int kDefaultChunkLog2 = 26;
+
+// per-beam device inputs of one job
+struct JobBuffers {
+    DeviceBuffer<DevExposure> exps;
+    DeviceBuffer<DevSpectrum> spec;
+    DeviceBuffer<DevBowtie> bowtie;
+};
 } // namespace
 
 int dxmcg::reportError(int code, const std::string& msg) { return fail(code, msg); }
@@ -116,9 +124,7 @@ struct dxmcg_world {
     DeviceBuffer<DevMaterial> mats;
     DeviceBuffer<DevCounters> counters;
     DeviceBuffer<unsigned> scratch; // rho max bits [256] + error word
-    DeviceBuffer<DevExposure> exps;
-    DeviceBuffer<DevSpectrum> spec;
-    DeviceBuffer<DevBowtie> bowtie;
+    JobBuffers job; // exposures, spectra, bowtie of the last transport_run
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // macro cells for MACRO tracking, built for one cell size at a time
     DeviceBuffer<float> mscale;
@@ -177,9 +183,13 @@ int ensureMacroCells(dxmcg_world* w, int B)
 }
 
 // Everything a launch needs for one beam on one world, uploaded into the world's buffers.
+// The beam's exposures, spectra and bowtie go to `jb` (the world's own set unless a
+// batch passes one of its own).
 int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, DevJob& J, uint64_t& nHist,
-    double& calibration)
+    double& calibration, JobBuffers* jb = nullptr)
 {
+    if (!jb)
+        jb = &w->job;
     HostJob hj;
     std::string err;
     int rc = buildHostJob(b, w->dims, w->spacing, hj, err);
@@ -192,16 +202,16 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
     if (calibration != 1.0)
         for (auto& e : hj.exposures)
             e.weight = static_cast<float>(e.weight * calibration);
-    DXMCG_CUDA(w->exps.alloc(hj.exposures.size()));
-    DXMCG_CUDA(cudaMemcpyAsync(w->exps.p, hj.exposures.data(), hj.exposures.size() * sizeof(DevExposure),
+    DXMCG_CUDA(jb->exps.alloc(hj.exposures.size()));
+    DXMCG_CUDA(cudaMemcpyAsync(jb->exps.p, hj.exposures.data(), hj.exposures.size() * sizeof(DevExposure),
         cudaMemcpyHostToDevice, w->stream));
-    DXMCG_CUDA(w->spec.alloc(2));
-    DXMCG_CUDA(cudaMemcpyAsync(w->spec.p, hj.spec, 2 * sizeof(DevSpectrum), cudaMemcpyHostToDevice, w->stream));
+    DXMCG_CUDA(jb->spec.alloc(2));
+    DXMCG_CUDA(cudaMemcpyAsync(jb->spec.p, hj.spec, 2 * sizeof(DevSpectrum), cudaMemcpyHostToDevice, w->stream));
     J = DevJob {};
     if (hj.hasBowtie) {
-        DXMCG_CUDA(w->bowtie.alloc(1));
-        DXMCG_CUDA(cudaMemcpyAsync(w->bowtie.p, &hj.bowtie, sizeof(DevBowtie), cudaMemcpyHostToDevice, w->stream));
-        J.bowtie = w->bowtie.p;
+        DXMCG_CUDA(jb->bowtie.alloc(1));
+        DXMCG_CUDA(cudaMemcpyAsync(jb->bowtie.p, &hj.bowtie, sizeof(DevBowtie), cudaMemcpyHostToDevice, w->stream));
+        J.bowtie = jb->bowtie.p;
     }
     // the host staging must outlive the asynchronous copies
     DXMCG_CUDA(cudaStreamSynchronize(w->stream));
@@ -213,8 +223,8 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
     J.maj = w->maj.p;
     J.mats = w->mats.p;
     J.tally = w->tally.p;
-    J.exps = w->exps.p;
-    J.spec = w->spec.p;
+    J.exps = jb->exps.p;
+    J.spec = jb->spec.p;
     if (o.tracking == DXMCG_TRACK_MACRO) {
         const int B = o.macro_cell > 0 ? std::min(o.macro_cell, 1024) : 16;
         rc = ensureMacroCells(w, B);
@@ -230,7 +240,7 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
     return DXMCG_OK;
 }
 
-LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o)
+LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o, bool batch = false)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, w->device);
@@ -238,7 +248,8 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o)
     s.block = o.block_size > 0 ? o.block_size : 256;
     s.block = std::max(32, std::min(256, s.block / 32 * 32));
     // one wave of resident blocks: the kernel is persistent and pulls work from its queue
-    const int resident = transportMaxBlocksPerSM(s.block, o.tracking);
+    const int resident = batch ? transportMaxBlocksPerSMBatch(s.block, o.tracking)
+                               : transportMaxBlocksPerSM(s.block, o.tracking);
     const int per = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, resident) : resident;
     s.grid = std::max(1, sms) * per;
     s.interact_batch = std::min(32, std::max(0, o.interact_batch));
@@ -246,7 +257,74 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o)
     return s;
 }
 
+void fillStats(const DevCounters& c, dxmcg_stats* stats)
+{
+    stats->e_source = c.e_source;
+    stats->e_deposited = c.e_deposited;
+    stats->e_escaped = c.e_escaped;
+    stats->n_histories = c.histories;
+    stats->n_missed = c.missed;
+    stats->n_visits = c.visits;
+    stats->n_photo = c.photo;
+    stats->n_compton = c.compton;
+    stats->n_rayleigh = c.rayleigh;
+    stats->n_cutoff = c.cutoff;
+    stats->n_errors = c.errors;
+    stats->n_interacted = c.interacted;
+    stats->n_crossings = c.crossings;
+}
+
+// the device's error flags as a status (DXMCG_OK when none)
+int deviceErrors(const DevCounters& c, const char* what)
+{
+    if (c.error_flags & kErrStepLimit)
+        return fail(DXMCG_ERR_DEVICE, std::string(what) + ": a history exceeded the step limit");
+    if (c.error_flags & kErrRejectLimit)
+        return fail(DXMCG_ERR_DEVICE, std::string(what) + ": a sampler exceeded its rejection limit");
+    return DXMCG_OK;
+}
+
 } // namespace
+
+// Several (world, beam) jobs run by one persistent launch over a shared history
+// queue; the launch (counter reset + kernel) is a CUDA graph replayed by each run.
+struct dxmcg_batch {
+    int device = 0;
+    int tracking = DXMCG_TRACK_WOODCOCK;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<dxmcg_world*> worlds;
+    std::vector<uint64_t> nHist;
+    std::vector<double> calibration;
+    std::vector<std::unique_ptr<JobBuffers>> inputs;
+    DeviceBuffer<DevJob> jobs;
+    DeviceBuffer<unsigned long long> offsets;
+    DeviceBuffer<DevCounters> counters;
+    LaunchShape shape;
+    uint64_t total = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+
+    dxmcg_batch() = default;
+    dxmcg_batch(const dxmcg_batch&) = delete;
+    dxmcg_batch& operator=(const dxmcg_batch&) = delete;
+    ~dxmcg_batch()
+    {
+        cudaSetDevice(device);
+        if (stream)
+            cudaStreamSynchronize(stream);
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (ev0)
+            cudaEventDestroy(ev0);
+        if (ev1)
+            cudaEventDestroy(ev1);
+        if (stream)
+            cudaStreamDestroy(stream);
+    }
+};
 
 // ============================================================================ C ABI
 extern "C" {
@@ -670,6 +748,211 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
         return fail(DXMCG_ERR_DEVICE, "transport: a sampler exceeded its rejection limit");
     if (cancelled)
         return fail(DXMCG_ERR_CANCELLED, "transport: cancelled");
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_batch_create(int n_jobs, dxmcg_world* const* worlds, const dxmcg_beam* beams,
+    const dxmcg_run_options* opts, dxmcg_batch** out)
+{
+    if (!out)
+        return fail(DXMCG_ERR_ARGUMENT, "batch_create: null out");
+    *out = nullptr;
+    if (n_jobs < 1 || !worlds || !beams || !opts)
+        return fail(DXMCG_ERR_ARGUMENT, "batch_create: need n_jobs >= 1 worlds, beams and options");
+    const int tracking = opts[0].tracking;
+    if (tracking != DXMCG_TRACK_WOODCOCK && tracking != DXMCG_TRACK_SIDDON && tracking != DXMCG_TRACK_MACRO)
+        return fail(DXMCG_ERR_ARGUMENT, "batch_create: unknown tracking mode");
+    for (int j = 0; j < n_jobs; ++j) {
+        if (!worlds[j] || !worlds[j]->built)
+            return fail(DXMCG_ERR_STATE, "batch_create: job " + std::to_string(j) + ": world not built");
+        if (worlds[j]->device != worlds[0]->device)
+            return fail(DXMCG_ERR_ARGUMENT, "batch_create: all worlds must be on one device");
+        if (opts[j].tracking != tracking)
+            return fail(DXMCG_ERR_ARGUMENT, "batch_create: all jobs must use one tracking mode");
+        if (opts[j].hist_begin != 0 || opts[j].hist_end != 0)
+            return fail(DXMCG_ERR_ARGUMENT, "batch_create: jobs run whole beams (hist_begin/hist_end must be 0)");
+    }
+    auto b = std::make_unique<dxmcg_batch>();
+    b->device = worlds[0]->device;
+    b->tracking = tracking;
+    DXMCG_CUDA(cudaSetDevice(b->device));
+    DXMCG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    DXMCG_CUDA(cudaEventCreate(&b->ev0));
+    DXMCG_CUDA(cudaEventCreate(&b->ev1));
+    std::vector<DevJob> J(n_jobs);
+    std::vector<unsigned long long> off(n_jobs + 1, 0ull);
+    for (int j = 0; j < n_jobs; ++j) {
+        b->inputs.push_back(std::make_unique<JobBuffers>());
+        uint64_t n = 0;
+        double cal = 1.0;
+        const int rc = prepareJob(worlds[j], beams[j], opts[j], J[j], n, cal, b->inputs.back().get());
+        if (rc != DXMCG_OK)
+            return rc;
+        b->worlds.push_back(worlds[j]);
+        b->nHist.push_back(n);
+        b->calibration.push_back(cal);
+        off[j + 1] = off[j] + n;
+    }
+    // a world's macro cells are rebuilt when a later job asks for another size
+    if (tracking == DXMCG_TRACK_MACRO)
+        for (int j = 0; j < n_jobs; ++j)
+            if (J[j].mb != worlds[j]->macroB || J[j].mscale != worlds[j]->mscale.p)
+                return fail(DXMCG_ERR_ARGUMENT, "batch_create: jobs on one world must use one macro_cell");
+    b->total = off[n_jobs];
+    DXMCG_CUDA(cudaSetDevice(b->device));
+    DXMCG_CUDA(b->jobs.alloc(n_jobs));
+    DXMCG_CUDA(b->offsets.alloc(n_jobs + 1));
+    DXMCG_CUDA(b->counters.alloc(1));
+    DXMCG_CUDA(cudaMemcpyAsync(b->jobs.p, J.data(), n_jobs * sizeof(DevJob), cudaMemcpyHostToDevice, b->stream));
+    DXMCG_CUDA(cudaMemcpyAsync(b->offsets.p, off.data(), off.size() * sizeof(unsigned long long),
+        cudaMemcpyHostToDevice, b->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(b->stream));
+    // the occupancy query also loads the kernel, so the later graph capture loads nothing
+    b->shape = chooseShape(worlds[0], opts[0], true);
+    *out = b.release();
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_batch_info(const dxmcg_batch* b, int* n_jobs, uint64_t* job_histories, double* job_calibration)
+{
+    if (!b)
+        return fail(DXMCG_ERR_ARGUMENT, "batch_info: null batch");
+    const int n = static_cast<int>(b->worlds.size());
+    if (n_jobs)
+        *n_jobs = n;
+    for (int j = 0; j < n; ++j) {
+        if (job_histories)
+            job_histories[j] = b->nHist[j];
+        if (job_calibration)
+            job_calibration[j] = b->calibration[j];
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_batch_run(dxmcg_batch* b, dxmcg_stats* stats)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!b)
+        return fail(DXMCG_ERR_ARGUMENT, "batch_run: null batch");
+    DXMCG_CUDA(cudaSetDevice(b->device));
+    if (!b->exec) {
+        DXMCG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaMemsetAsync(b->counters.p, 0, sizeof(DevCounters), b->stream);
+        if (e == cudaSuccess)
+            e = launchTransportBatch(b->tracking, b->jobs.p, b->offsets.p, static_cast<int>(b->worlds.size()),
+                b->total, b->counters.p, b->shape, b->stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess || ee != cudaSuccess) {
+            if (g)
+                cudaGraphDestroy(g);
+            return cudaFail(e != cudaSuccess ? e : ee, "batch_run: graph capture");
+        }
+        b->graph = g;
+        DXMCG_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    }
+    DXMCG_CUDA(cudaEventRecord(b->ev0, b->stream));
+    DXMCG_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    DXMCG_CUDA(cudaEventRecord(b->ev1, b->stream));
+    DevCounters c {};
+    DXMCG_CUDA(cudaMemcpyAsync(&c, b->counters.p, sizeof(c), cudaMemcpyDeviceToHost, b->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(b->stream));
+    float ms = 0.0f;
+    DXMCG_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    for (size_t j = 0; j < b->worlds.size(); ++j)
+        b->worlds[j]->historiesScored += static_cast<double>(b->nHist[j]);
+    if (stats) {
+        fillStats(c, stats);
+        stats->kernel_ms = ms;
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        stats->dose_scale = kKeVToMilliGrayGram / b->worlds[0]->voxelVolume;
+        stats->calibration = b->calibration[0];
+    }
+    return deviceErrors(c, "batch_run");
+}
+
+DXMCG_API void dxmcg_batch_destroy(dxmcg_batch* b) { delete b; }
+
+DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_options* opts,
+    uint64_t sample_histories, double* histories_per_second)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "autotune: world not built");
+    if (!beam || !opts)
+        return fail(DXMCG_ERR_ARGUMENT, "autotune: null beam or options");
+    dxmcg_run_options o = *opts;
+    if (o.tracking != DXMCG_TRACK_WOODCOCK && o.tracking != DXMCG_TRACK_SIDDON && o.tracking != DXMCG_TRACK_MACRO)
+        return fail(DXMCG_ERR_ARGUMENT, "autotune: unknown tracking mode");
+    o.normalize = 0; // trial runs need no calibration run
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    DevJob J;
+    uint64_t nHist = 0;
+    double calibration = 1.0;
+    int rc = prepareJob(w, *beam, o, J, nHist, calibration);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (nHist == 0)
+        return fail(DXMCG_ERR_ARGUMENT, "autotune: the beam has no histories");
+    // trials deposit into a scratch tally, never into the world's dose
+    DeviceBuffer<Tally> scratch;
+    DXMCG_CUDA(scratch.alloc(w->N));
+    J.tally = scratch.p;
+    const uint64_t n = std::min<uint64_t>(sample_histories > 0 ? sample_histories : (1ull << 24), nHist);
+    const unsigned long long h0 = (nHist - n) / 2; // the middle of the beam's histories
+    const unsigned long long h1 = h0 + n;
+
+    auto trial = [&](const LaunchShape& shape, float& ms) -> int {
+        DevCounters zero {};
+        zero.next = h0;
+        DXMCG_CUDA(cudaMemcpyAsync(w->counters.p, &zero, sizeof(zero), cudaMemcpyHostToDevice, w->stream));
+        DXMCG_CUDA(cudaEventRecord(w->ev0, w->stream));
+        const cudaError_t e = launchTransport(J, h1, w->counters.p, shape, w->stream);
+        if (e != cudaSuccess)
+            return cudaFail(e, "autotune: transport kernel launch");
+        DXMCG_CUDA(cudaEventRecord(w->ev1, w->stream));
+        DXMCG_CUDA(cudaEventSynchronize(w->ev1));
+        DXMCG_CUDA(cudaEventElapsedTime(&ms, w->ev0, w->ev1));
+        DevCounters c {};
+        DXMCG_CUDA(cudaMemcpy(&c, w->counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+        return deviceErrors(c, "autotune");
+    };
+
+    static const int kBlocks[] = { 128, 256 };
+    static const int kInteract[] = { 8, 12, 16, 24 };
+    static const int kRefill[] = { 4, 8, 16 };
+    float warm = 0.0f;
+    rc = trial(chooseShape(w, o), warm);
+    if (rc != DXMCG_OK)
+        return rc;
+    float best = 0.0f;
+    dxmcg_run_options bestOpt = o;
+    for (int blk : kBlocks)
+        for (int ib : kInteract)
+            for (int rb : kRefill) {
+                dxmcg_run_options t = o;
+                t.block_size = blk;
+                t.blocks_per_sm = 0;
+                t.interact_batch = ib;
+                t.refill_batch = rb;
+                const LaunchShape shape = chooseShape(w, t);
+                float m = 0.0f, m2 = 0.0f;
+                rc = trial(shape, m);
+                if (rc == DXMCG_OK)
+                    rc = trial(shape, m2);
+                if (rc != DXMCG_OK)
+                    return rc;
+                const float tmin = std::min(m, m2);
+                if (best == 0.0f || tmin < best) {
+                    best = tmin;
+                    bestOpt = t;
+                }
+            }
+    opts->block_size = bestOpt.block_size;
+    opts->blocks_per_sm = 0;
+    opts->interact_batch = bestOpt.interact_batch;
+    opts->refill_batch = bestOpt.refill_batch;
+    if (histories_per_second)
+        *histories_per_second = best > 0.0f ? static_cast<double>(n) / (best * 1e-3) : 0.0;
     return DXMCG_OK;
 }
 

@@ -150,6 +150,11 @@ int transportMaxBlocksPerSM(int block, int tracking);
 cudaError_t launchTransportUnpacked(const DevJob& job, unsigned long long h_end, DevCounters* ctr,
     LaunchShape shape, cudaStream_t s);
 int transportMaxBlocksPerSMUnpacked(int block, int tracking);
+// one persistent launch over several jobs (device descriptors `jobs`, packed worlds):
+// offsets[j] is job j's first history in the shared queue, offsets[nJobs] == h_end
+cudaError_t launchTransportBatch(int tracking, const DevJob* jobs, const unsigned long long* offsets, int nJobs,
+    unsigned long long h_end, DevCounters* ctr, LaunchShape shape, cudaStream_t s);
+int transportMaxBlocksPerSMBatch(int block, int tracking);
 
 // host helpers (geometry.cpp)
 int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out);

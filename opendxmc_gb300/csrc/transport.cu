@@ -248,10 +248,15 @@ namespace {
         return rng.u() * muc < mu;
     }
 
-    template <int TRACKING, bool PACKED = true>
-    __global__ void __launch_bounds__(256) transportKernel(const DevJob J, unsigned long long h_end,
+    // MULTI: one queue over the concatenated history ranges of nJobs jobs (offsets[j]
+    // is the first global history of job j, offsets[nJobs] the total); each lane
+    // reads its job's descriptor from `jobs`.  Otherwise J0 is the only job.
+    template <int TRACKING, bool PACKED, bool MULTI>
+    __global__ void __launch_bounds__(256) transportKernel(const DevJob J0, const DevJob* __restrict__ jobs,
+        const unsigned long long* __restrict__ offsets, int nJobs, unsigned long long h_end,
         DevCounters* __restrict__ ctr, int refillBatch, int interactBatch)
     {
+        int jid = 0;
         // event counters per warp (no block-wide barrier: warps finish independently)
         __shared__ unsigned long long sCountAll[256 / 32][cNum];
         const unsigned lane = threadIdx.x & 31u;
@@ -300,11 +305,24 @@ namespace {
                 const bool start = st == kDead && rank < avail;
                 bool entered = false;
                 if (start) {
-                    const unsigned long long h = poolNext + rank;
-                    rng.init(J.key0, J.key1, J.stream, h);
-                    sampleSource(J, h, ph, rng);
+                    unsigned long long h = poolNext + rank;
+                    if (MULTI) { // the queue spans all jobs: find this history's job
+                        int lo = 0, hi = nJobs;
+                        while (hi - lo > 1) {
+                            const int mid = (lo + hi) >> 1;
+                            if (__ldg(offsets + mid) <= h)
+                                lo = mid;
+                            else
+                                hi = mid;
+                        }
+                        jid = lo;
+                        h -= __ldg(offsets + lo);
+                    }
+                    const DevJob& Jr = MULTI ? jobs[jid] : J0;
+                    rng.init(Jr.key0, Jr.key1, Jr.stream, h);
+                    sampleSource(Jr, h, ph, rng);
                     esrc.add(ph.w * ph.E);
-                    entered = enterGrid(J, ph);
+                    entered = enterGrid(Jr, ph);
                     if (entered) {
                         st = kStepping;
                         steps = 0;
@@ -312,11 +330,11 @@ namespace {
                         if (TRACKING == DXMCG_TRACK_SIDDON)
                             gridPos(ph.E, ec.ie, ec.fe);
                         else
-                            ec.set(J, ph.E);
+                            ec.set(Jr, ph.E);
                         if (TRACKING == DXMCG_TRACK_MACRO) {
-                            cx = min(static_cast<int>(ph.px / J.cellL[0]), J.mc[0] - 1);
-                            cy = min(static_cast<int>(ph.py / J.cellL[1]), J.mc[1] - 1);
-                            cz = min(static_cast<int>(ph.pz / J.cellL[2]), J.mc[2] - 1);
+                            cx = min(static_cast<int>(ph.px / Jr.cellL[0]), Jr.mc[0] - 1);
+                            cy = min(static_cast<int>(ph.py / Jr.cellL[1]), Jr.mc[1] - 1);
+                            cz = min(static_cast<int>(ph.pz / Jr.cellL[2]), Jr.mc[2] - 1);
                         }
                     } else {
                         eesc.add(ph.w * ph.E);
@@ -330,6 +348,9 @@ namespace {
                     atomicAdd(&sCount[cMissed], static_cast<unsigned long long>(__popc(mStart & ~mIn)));
                 }
             }
+
+            // the lane's job, after the refill may have changed it
+            const DevJob& J = MULTI ? jobs[jid] : J0;
 
             // ---- interact
             const int nPark = __popc(parked);
@@ -468,35 +489,45 @@ namespace {
 } // namespace
 
 namespace {
-    using TransportFn = void (*)(const DevJob, unsigned long long, DevCounters*, int, int);
+    using TransportFn = void (*)(const DevJob, const DevJob*, const unsigned long long*, int, unsigned long long,
+        DevCounters*, int, int);
 
     // kernel instance for a tracking mode on the packed (world) or unpacked
-    // (caller-owned arrays) voxel layout; nullptr where no instance exists
-    TransportFn kernelFor(int tracking, bool packed)
+    // (caller-owned arrays) voxel layout, single job or a batch of jobs;
+    // nullptr where no instance exists
+    TransportFn kernelFor(int tracking, bool packed, bool multi = false)
     {
+        if (multi) {
+            switch (tracking) {
+            case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, true, true>;
+            case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, true, true>;
+            case DXMCG_TRACK_MACRO: return transportKernel<DXMCG_TRACK_MACRO, true, true>;
+            default: return nullptr;
+            }
+        }
         if (packed) {
             switch (tracking) {
-            case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, true>;
-            case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, true>;
-            case DXMCG_TRACK_MACRO: return transportKernel<DXMCG_TRACK_MACRO, true>;
+            case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, true, false>;
+            case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, true, false>;
+            case DXMCG_TRACK_MACRO: return transportKernel<DXMCG_TRACK_MACRO, true, false>;
             default: return nullptr;
             }
         }
         switch (tracking) {
-        case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, false>;
-        case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, false>;
+        case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, false, false>;
+        case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, false, false>;
         default: return nullptr;
         }
     }
 
-    cudaError_t launchWith(TransportFn fn, const DevJob& job, unsigned long long h_end, DevCounters* ctr,
-        LaunchShape shape, cudaStream_t s)
+    cudaError_t launchWith(TransportFn fn, const DevJob& job, const DevJob* jobs, const unsigned long long* offsets,
+        int nJobs, unsigned long long h_end, DevCounters* ctr, LaunchShape shape, cudaStream_t s)
     {
         if (!fn)
             return cudaErrorInvalidValue;
         const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
         const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
-        fn<<<shape.grid, shape.block, 0, s>>>(job, h_end, ctr, refill, interact);
+        fn<<<shape.grid, shape.block, 0, s>>>(job, jobs, offsets, nJobs, h_end, ctr, refill, interact);
         return cudaGetLastError();
     }
 
@@ -512,14 +543,25 @@ namespace {
 cudaError_t launchTransport(const DevJob& job, unsigned long long h_end, DevCounters* ctr, LaunchShape shape,
     cudaStream_t s)
 {
-    return launchWith(kernelFor(job.tracking, true), job, h_end, ctr, shape, s);
+    return launchWith(kernelFor(job.tracking, true), job, nullptr, nullptr, 1, h_end, ctr, shape, s);
 }
 
 cudaError_t launchTransportUnpacked(const DevJob& job, unsigned long long h_end, DevCounters* ctr,
     LaunchShape shape, cudaStream_t s)
 {
-    return launchWith(kernelFor(job.tracking, false), job, h_end, ctr, shape, s);
+    return launchWith(kernelFor(job.tracking, false), job, nullptr, nullptr, 1, h_end, ctr, shape, s);
 }
+
+cudaError_t launchTransportBatch(int tracking, const DevJob* jobs, const unsigned long long* offsets, int nJobs,
+    unsigned long long h_end, DevCounters* ctr, LaunchShape shape, cudaStream_t s)
+{
+    if (!jobs || !offsets || nJobs < 1)
+        return cudaErrorInvalidValue;
+    const DevJob unused {};
+    return launchWith(kernelFor(tracking, true, true), unused, jobs, offsets, nJobs, h_end, ctr, shape, s);
+}
+
+int transportMaxBlocksPerSMBatch(int block, int tracking) { return residentBlocks(kernelFor(tracking, true, true), block); }
 
 int transportMaxBlocksPerSMUnpacked(int block, int tracking) { return residentBlocks(kernelFor(tracking, false), block); }
 

@@ -211,9 +211,65 @@ class GpuWorld:
         N.check(N.lib().dxmcg_sample_source(self._h, C.byref(b), C.byref(opts), n, N.ptr(out, C.c_double)))
         return out
 
+    def autotune(self, beam: dict, options: N.RunOptions | None = None, sample_histories: int = 0):
+        """Fastest launch shape for this beam: (options with block_size, interact_batch
+        and refill_batch set, histories per second of the best trial)."""
+        b, keep = N.make_beam(beam)
+        opts = N.RunOptions.from_buffer_copy(options if options is not None else run_options())
+        rate = C.c_double(0)
+        N.check(N.lib().dxmcg_autotune(self._h, C.byref(b), C.byref(opts), sample_histories, C.byref(rate)))
+        return opts, rate.value
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             N.lib().dxmcg_world_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several (world, beam, options) jobs in one persistent launch over a shared
+    history queue, replayed as a CUDA graph by run().  The worlds must outlive it."""
+
+    def __init__(self, jobs: list[tuple[GpuWorld, dict, N.RunOptions | None]]):
+        n = len(jobs)
+        if n < 1:
+            raise ValueError("a batch needs at least one job")
+        self.worlds = [w for w, _, _ in jobs]  # keeps the worlds alive
+        beams = (N.Beam * n)()
+        opts = (N.RunOptions * n)()
+        self._keep = []
+        for k, (w, beam, o) in enumerate(jobs):
+            b, keep = N.make_beam(beam)
+            beams[k] = b
+            self._keep.append(keep)
+            opts[k] = o if o is not None else run_options()
+        handles = (C.c_void_p * n)(*[w._h for w in self.worlds])
+        h = C.c_void_p()
+        N.check(N.lib().dxmcg_batch_create(n, handles, beams, opts, C.byref(h)))
+        self._h = h
+        self.n_jobs = n
+
+    def info(self):
+        """(histories per job, calibration factor per job)"""
+        hist = np.zeros(self.n_jobs, dtype=np.uint64)
+        cal = np.zeros(self.n_jobs)
+        N.check(N.lib().dxmcg_batch_info(self._h, None, N.ptr(hist, C.c_uint64), N.ptr(cal, C.c_double)))
+        return hist, cal
+
+    def run(self) -> dict:
+        st = N.Stats()
+        N.check(N.lib().dxmcg_batch_run(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().dxmcg_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

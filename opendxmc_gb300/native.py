@@ -29,7 +29,8 @@ EXPORTED = [
     "dxmcg_tube_mean_energy", "dxmcg_tube_al_hvl", "dxmcg_beam_exposures", "dxmcg_world_create",
     "dxmcg_world_set_data", "dxmcg_world_set_data_f32", "dxmcg_world_build", "dxmcg_world_destroy",
     "dxmcg_world_clear_tally", "dxmcg_world_read_tally", "dxmcg_world_read_dose", "dxmcg_world_tables",
-    "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_transport_run_noalloc", "dxmcg_progress_create",
+    "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_batch_create", "dxmcg_batch_info",
+    "dxmcg_batch_run", "dxmcg_batch_destroy", "dxmcg_autotune", "dxmcg_transport_run_noalloc", "dxmcg_progress_create",
     "dxmcg_progress_destroy",
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_reset", "dxmcg_progress_continue",
     "dxmcg_progress_message",
@@ -171,6 +172,11 @@ def lib() -> C.CDLL:
         "dxmcg_world_tables": (i, [vp, i, pf, pf]),
         "dxmcg_world_packed_density": (i, [vp, pf, pu8]),
         "dxmcg_transport_run": (i, [vp, C.POINTER(Beam), C.POINTER(RunOptions), vp, C.POINTER(Stats)]),
+        "dxmcg_batch_create": (i, [i, C.POINTER(vp), C.POINTER(Beam), C.POINTER(RunOptions), C.POINTER(vp)]),
+        "dxmcg_batch_info": (i, [vp, C.POINTER(C.c_int), pu64, pd]),
+        "dxmcg_batch_run": (i, [vp, C.POINTER(Stats)]),
+        "dxmcg_batch_destroy": (None, [vp]),
+        "dxmcg_autotune": (i, [vp, C.POINTER(Beam), C.POINTER(RunOptions), u64, pd]),
         "dxmcg_transport_run_noalloc": (i, [pi32, pd, vp, vp, C.POINTER(Material), i, i, C.POINTER(Beam),
                                             C.POINTER(RunOptions), vp, vp, C.POINTER(Stats)]),
         "dxmcg_progress_create": (vp, []),

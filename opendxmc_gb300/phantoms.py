@@ -169,3 +169,70 @@ def ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=1.0, collimation_cm=4.0, scan_c
     if bowtie:
         p["bowtie"] = list(bowtie)
     return p
+
+
+def ellipsoid_phantom(dims, spacing, seed=1, jitter=0.02, n_inserts=8) -> Phantom:
+    """Seeded six-material ellipsoid phantom of any grid size: an adipose body
+    ellipsoid filling 80-90 % of the grid, a muscle wall and a soft-tissue
+    interior, and `n_inserts` random ellipsoids of lung, adipose, muscle or bone
+    inside it; density x U(1 - jitter, 1 + jitter) per voxel (float32)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = (int(d) for d in dims)
+    x, y, z = _axes((nx, ny, nz), spacing)
+    ext = np.array([nx * spacing[0], ny * spacing[1], nz * spacing[2]]) * 0.5
+    body = ext * rng.uniform(0.8, 0.9, 3)
+    shapes = [(2, np.zeros(3), body), (4, np.zeros(3), body * 0.92), (3, np.zeros(3), body * 0.84)]
+    for _ in range(n_inserts):
+        m = int(rng.choice([1, 2, 4, 5]))
+        a = body * 0.84 * rng.uniform(0.08, 0.3, 3)
+        c = body * 0.84 * rng.uniform(-0.6, 0.6, 3)
+        shapes.append((m, c, a))
+    material = np.zeros((nz, ny, nx), dtype=np.uint8)
+    for m, c, a in shapes:
+        # evaluate each ellipsoid only over its bounding box
+        i0, i1 = np.searchsorted(x, c[0] - a[0]), np.searchsorted(x, c[0] + a[0])
+        j0, j1 = np.searchsorted(y, c[1] - a[1]), np.searchsorted(y, c[1] + a[1])
+        k0, k1 = np.searchsorted(z, c[2] - a[2]), np.searchsorted(z, c[2] + a[2])
+        if i0 >= i1 or j0 >= j1 or k0 >= k1:
+            continue
+        dx = ((x[i0:i1] - c[0]) / a[0]) ** 2
+        dy = ((y[j0:j1] - c[1]) / a[1]) ** 2
+        dz = ((z[k0:k1] - c[2]) / a[2]) ** 2
+        inside = (dz[:, None, None] + dy[None, :, None] + dx[None, None, :]) < 1.0
+        box = material[k0:k1, j0:j1, i0:i1]
+        box[inside] = m
+    nominal = np.array([d for _, _, d in SIX_MATERIALS], dtype=np.float32)
+    density = nominal[material] * rng.uniform(1.0 - jitter, 1.0 + jitter, size=material.shape).astype(np.float32)
+    return Phantom((nx, ny, nz), tuple(float(s) for s in spacing), density, material,
+                   [c for _, c, _ in SIX_MATERIALS], [n for n, _, _ in SIX_MATERIALS])
+
+
+def batched_jobs(n_jobs=64, seed=1, dim_range=(64, 320), spacing_cm=(0.1, 0.3), kvp_range=(60.0, 140.0),
+                 hist_range=(1e6, 1e8)) -> list[dict]:
+    """Seeded specs of independent DX / CBCT jobs: grid dimensions uniform in
+    `dim_range` per axis, voxel size uniform in `spacing_cm`, kVp uniform in
+    `kvp_range`, histories log-uniform in `hist_range`.  Each spec holds the
+    phantom arguments and the beam dict (make the phantom with
+    ellipsoid_phantom(spec["dims"], spec["spacing"], spec["seed"]))."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for j in range(n_jobs):
+        dims = tuple(int(v) for v in rng.integers(dim_range[0], dim_range[1] + 1, 3))
+        spacing = tuple(float(v) for v in np.round(rng.uniform(spacing_cm[0], spacing_cm[1], 3), 4))
+        kvp = float(np.round(rng.uniform(*kvp_range), 1))
+        hist = float(np.exp(rng.uniform(np.log(hist_range[0]), np.log(hist_range[1]))))
+        ext = np.array(dims) * np.array(spacing)
+        if j % 2 == 0:  # DX, 10 exposures, square field over 70 % of the smaller face
+            field = float(np.clip(0.7 * min(ext[0], ext[2]), 2.0, 40.0))
+            beam = dx_beam_params(kvp=kvp, al_mm=2.5, field_cm=field, particles=max(1, int(hist / 10)),
+                                  exposures=10)
+        else:  # CBCT, half rotation in 2 degree steps (91 projections)
+            sdd = 120.0
+            half_xy = float(np.arctan(0.4 * max(ext[0], ext[1]) / (0.5 * sdd)))
+            half_z = float(np.arctan(0.4 * ext[2] / (0.5 * sdd)))
+            beam = {"type": 3, "kvp": kvp, "anode_angle_deg": 12.0, "filters": {13: 4.0},
+                    "particles_per_exposure": max(1, int(hist / 91)), "position": [0.0, 0.0, 0.0],
+                    "rotation_axis": [0.0, 0.0, 1.0], "start_angle_deg": 0.0, "stop_angle_deg": 180.0,
+                    "step_angle_deg": 2.0, "sdd_cm": sdd, "half_angles": [half_xy, half_z]}
+        jobs.append({"dims": dims, "spacing": spacing, "seed": seed * 1000 + j, "kvp": kvp, "beam": beam})
+    return jobs

@@ -124,3 +124,47 @@ def test_no_device_is_an_error_not_a_fallback(engine):
         pytest.skip("a device is visible")
     with pytest.raises(Exception, match="NO_DEVICE"):
         engine.GpuWorld((4, 4, 4), (0.1, 0.1, 0.1), [P.WATER])
+
+
+def test_batch_and_autotune_reject_bad_arguments_on_host(engine):
+    from opendxmc_gb300 import native as N
+
+    lib = N.lib()
+    h = C.c_void_p()
+    beams = (N.Beam * 1)()
+    opts = (N.RunOptions * 1)()
+    worlds = (C.c_void_p * 1)()
+    assert lib.dxmcg_batch_create(0, worlds, beams, opts, C.byref(h)) == -1
+    assert lib.dxmcg_batch_create(1, None, beams, opts, C.byref(h)) == -1
+    assert lib.dxmcg_batch_create(1, worlds, beams, opts, None) == -1
+    opts[0].tracking = 7
+    assert lib.dxmcg_batch_create(1, worlds, beams, opts, C.byref(h)) == -1
+    assert b"tracking" in lib.dxmcg_last_error()
+    opts[0].tracking = 0
+    assert lib.dxmcg_batch_create(1, worlds, beams, opts, C.byref(h)) == -3  # null world: not built
+    assert lib.dxmcg_batch_run(None, None) == -1
+    lib.dxmcg_batch_destroy(None)
+    assert lib.dxmcg_batch_info(None, None, None, None) == -1
+    assert lib.dxmcg_autotune(None, beams, opts, 0, None) == -3
+
+
+def test_batched_job_generator_ranges():
+    jobs = P.batched_jobs()
+    assert len(jobs) == 64
+    for j in jobs:
+        assert all(64 <= d <= 320 for d in j["dims"])
+        assert all(0.1 <= s <= 0.3 for s in j["spacing"])
+        assert 60.0 <= j["kvp"] <= 140.0
+        b = j["beam"]
+        n_exp = b.get("n_exposures", 91)
+        assert 0.9e6 <= b["particles_per_exposure"] * n_exp <= 1e8
+    assert {j["beam"]["type"] for j in jobs} == {0, 3}
+    from opendxmc_gb300 import engine as G
+
+    assert len(G.beam_exposures(jobs[1]["beam"])) == 91
+    ph = P.ellipsoid_phantom((40, 30, 20), (0.2, 0.3, 0.25), seed=4)
+    assert ph.density.shape == (20, 30, 40) and ph.density.dtype == np.float32
+    assert ph.material.max() <= 5 and (ph.material > 0).mean() > 0.2
+    again = P.ellipsoid_phantom((40, 30, 20), (0.2, 0.3, 0.25), seed=4)
+    np.testing.assert_array_equal(ph.material, again.material)
+    np.testing.assert_array_equal(ph.density, again.density)

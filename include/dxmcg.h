@@ -275,6 +275,56 @@ DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], const double sp
     int correction, const dxmcg_beam* beam, const dxmcg_run_options* opts, dxmcg_tally_record* device_tally,
     void* cuda_stream, dxmcg_stats* stats);
 
+/* ---- around the transport: segmentation, dose readout, organ dose table ----- */
+#define DXMCG_MAX_SEG_MATERIALS 64
+/* CTSegmentationPipeline's tables (ctsegmentationpipeline.cpp:59-111): for a tube
+ * of kvp with al_mm Al and sn_mm Sn filtration, the spectrum-weighted mean CT
+ * number and mass attenuation of each material (ascending CT numbers expected),
+ * and of water (1.0 g/cm3) and dry air (0.001205 g/cm3). */
+typedef struct {
+    int32_t n_materials;
+    double hu[DXMCG_MAX_SEG_MATERIALS];
+    double separator[DXMCG_MAX_SEG_MATERIALS - 1]; /* (hu[i] + hu[i+1]) / 2 */
+    double attenuation[DXMCG_MAX_SEG_MATERIALS];   /* cm2/g */
+    double water_attenuation, water_density, air_attenuation, air_density;
+} dxmcg_segmentation;
+DXMCG_API int dxmcg_ct_segmentation_table(double kvp, double al_mm, double sn_mm, int n_materials,
+    const dxmcg_material* materials, const double* densities, dxmcg_segmentation* out);
+/* CTSegmentationPipeline::updateImageData's per-voxel pass (:117-160) on the GPU:
+ * material = first i with hu < separator[i] (else n_materials - 1), density from the
+ * water/air line over the material's attenuation, clamped at 0.  Host arrays of n;
+ * the _device form takes device arrays and runs on cuda_stream (NULL: default). */
+DXMCG_API int dxmcg_ct_segment(const dxmcg_segmentation* table, const double* hu, uint64_t n, uint8_t* material,
+    double* density);
+DXMCG_API int dxmcg_ct_segment_device(const dxmcg_segmentation* table, const double* hu, uint64_t n,
+    uint8_t* material, double* density, void* cuda_stream);
+
+/* DoseTablePipeline::updateImageData (dosetablepipeline.cpp:55-85): per organ label
+ * i < n_organs, voxels, volume (cm3), mass (g) and mean dose = sum(dose x voxel mass)
+ * / organ mass, in the dose array's unit.  Labels >= n_organs are ignored; organs
+ * without voxels get zeros. */
+typedef struct {
+    uint64_t n_voxels;
+    double volume_cm3;
+    double mass_g;
+    double dose;
+} dxmcg_organ_dose;
+DXMCG_API int dxmcg_organ_dose_table(const uint8_t* organ, const double* dose, const double* density, uint64_t n,
+    const double spacing_cm[3], int n_organs, dxmcg_organ_dose* out);
+DXMCG_API int dxmcg_organ_dose_table_device(const uint8_t* organ, const double* dose, const double* density,
+    uint64_t n, const double spacing_cm[3], int n_organs, dxmcg_organ_dose* out, void* cuda_stream);
+/* The same table straight from a world's tally (dose in mGy as dxmcg_world_read_dose
+ * gives it, mass from the world's stored densities), without a dose array;
+ * delete_air_dose: material-0 voxels count with zero dose (simulationpipeline.cpp:180-185). */
+DXMCG_API int dxmcg_world_organ_dose(dxmcg_world* w, const uint8_t* organ, int n_organs, int delete_air_dose,
+    dxmcg_organ_dose* out);
+/* The worker's readout (simulationpipeline.cpp:173-231) on the GPU: dose, variance
+ * and event count (as double) with material-0 voxels zeroed when delete_air_dose,
+ * and, when the largest dose is below 1 mGy, dose x 1e3 and variance x 1e6 with
+ * *micro_gray = 1 (uGy).  Any output may be NULL. */
+DXMCG_API int dxmcg_world_read_dose_postprocessed(dxmcg_world* w, int delete_air_dose, double* dose,
+    double* variance, double* count, int* micro_gray);
+
 /* ---- TransportProgress (simulationpipeline.cpp:114-120, :234, :261) ---------- */
 DXMCG_API dxmcg_progress* dxmcg_progress_create(void);
 DXMCG_API void dxmcg_progress_destroy(dxmcg_progress* p);

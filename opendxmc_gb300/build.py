@@ -21,7 +21,9 @@ OBJ_DIR = PKG / "_build"
 LIB = OUT_DIR / "libdxmcg.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-O2",
+# host code: no contraction into fused multiply-adds, so that x86-64 and aarch64 hosts
+# round the FP64 table and geometry arithmetic alike
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden,-O2,-ffp-contract=off",
           f"-I{ROOT / 'include'}"]
 
 

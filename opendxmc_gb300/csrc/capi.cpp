@@ -326,6 +326,109 @@ struct dxmcg_batch {
     }
 };
 
+// helpers of the segmentation, organ dose table and readout entry points
+namespace {
+constexpr uint64_t kStreamChunk = 1ull << 25; // voxels per host<->device round trip
+
+// compositions of the two calibration media of the CT number scale
+dxmcg_material waterMaterial()
+{
+    dxmcg_material m {};
+    m.n = 2;
+    m.Z[0] = 1;
+    m.w[0] = 11.19;
+    m.Z[1] = 8;
+    m.w[1] = 88.81;
+    return m;
+}
+dxmcg_material dryAirMaterial()
+{
+    dxmcg_material m {};
+    m.n = 3;
+    m.Z[0] = 7;
+    m.w[0] = 75.5;
+    m.Z[1] = 8;
+    m.w[1] = 23.2;
+    m.Z[2] = 18;
+    m.w[2] = 1.3;
+    return m;
+}
+
+int toSegTable(const dxmcg_segmentation* t, SegTable& s)
+{
+    if (!t || t->n_materials < 1 || t->n_materials > DXMCG_MAX_SEG_MATERIALS)
+        return fail(DXMCG_ERR_ARGUMENT, "ct_segment: bad segmentation table");
+    s = SegTable {};
+    s.nSep = t->n_materials - 1;
+    s.slope = t->water_attenuation * t->water_density - t->air_attenuation * t->air_density;
+    s.offset = t->water_attenuation * t->water_density;
+    for (int i = 0; i < s.nSep; ++i)
+        s.sep[i] = t->separator[i];
+    for (int i = 0; i < t->n_materials; ++i)
+        s.att[i] = t->attenuation[i];
+    return DXMCG_OK;
+}
+
+void organRows(const std::vector<unsigned long long>& cnt, const std::vector<double>& rho,
+    const std::vector<double>& e, double voxelVolume, int nOrgans, dxmcg_organ_dose* out)
+{
+    for (int i = 0; i < nOrgans; ++i) {
+        out[i] = dxmcg_organ_dose {};
+        if (cnt[i] == 0)
+            continue;
+        out[i].n_voxels = cnt[i];
+        out[i].volume_cm3 = static_cast<double>(cnt[i]) * voxelVolume;
+        out[i].mass_g = voxelVolume * rho[i];
+        out[i].dose = out[i].mass_g > 0.0 ? e[i] / out[i].mass_g : 0.0;
+    }
+}
+
+// per-organ sums on the device: count, sum of density, sum of dose x mass
+struct OrganSums {
+    DeviceBuffer<unsigned long long> cnt;
+    DeviceBuffer<double> rho, e;
+    int alloc(cudaStream_t s)
+    {
+        DXMCG_CUDA(cnt.alloc(256));
+        DXMCG_CUDA(rho.alloc(256));
+        DXMCG_CUDA(e.alloc(256));
+        DXMCG_CUDA(cudaMemsetAsync(cnt.p, 0, 256 * sizeof(unsigned long long), s));
+        DXMCG_CUDA(cudaMemsetAsync(rho.p, 0, 256 * sizeof(double), s));
+        DXMCG_CUDA(cudaMemsetAsync(e.p, 0, 256 * sizeof(double), s));
+        return DXMCG_OK;
+    }
+    int read(double voxelVolume, int nOrgans, dxmcg_organ_dose* out, cudaStream_t s)
+    {
+        std::vector<unsigned long long> c(256);
+        std::vector<double> r(256), en(256);
+        DXMCG_CUDA(cudaMemcpyAsync(c.data(), cnt.p, 256 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        DXMCG_CUDA(cudaMemcpyAsync(r.data(), rho.p, 256 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        DXMCG_CUDA(cudaMemcpyAsync(en.data(), e.p, 256 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        DXMCG_CUDA(cudaStreamSynchronize(s));
+        organRows(c, r, en, voxelVolume, nOrgans, out);
+        return DXMCG_OK;
+    }
+};
+
+int checkOrganArgs(const double* spacing, int nOrgans, const dxmcg_organ_dose* out, double& V)
+{
+    if (!spacing || !out || nOrgans < 1 || nOrgans > 256)
+        return fail(DXMCG_ERR_ARGUMENT, "organ_dose_table: need spacing, 1..256 organs and an output array");
+    V = spacing[0] * spacing[1] * spacing[2];
+    if (!(V > 0.0))
+        return fail(DXMCG_ERR_ARGUMENT, "organ_dose_table: spacing must be positive");
+    return DXMCG_OK;
+}
+
+int currentDevice()
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1)
+        return fail(DXMCG_ERR_NO_DEVICE, "no CUDA device");
+    return DXMCG_OK;
+}
+} // namespace
+
 // ============================================================================ C ABI
 extern "C" {
 
@@ -953,6 +1056,216 @@ DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_o
     opts->refill_batch = bestOpt.refill_batch;
     if (histories_per_second)
         *histories_per_second = best > 0.0f ? static_cast<double>(n) / (best * 1e-3) : 0.0;
+    return DXMCG_OK;
+}
+
+// ---------------------------------------------------------------- segmentation, dose table, readout
+
+DXMCG_API int dxmcg_ct_segmentation_table(double kvp, double al_mm, double sn_mm, int n_materials,
+    const dxmcg_material* materials, const double* densities, dxmcg_segmentation* out)
+{
+    if (!out || !materials || !densities || n_materials < 1 || n_materials > DXMCG_MAX_SEG_MATERIALS)
+        return fail(DXMCG_ERR_ARGUMENT, "ct_segmentation_table: need 1..64 materials, densities and an output");
+    if (!(kvp > 1.0))
+        return fail(DXMCG_ERR_ARGUMENT, "ct_segmentation_table: bad tube voltage");
+    for (int i = 0; i < n_materials; ++i)
+        if (!validComposition(materials[i]) || !(densities[i] >= 0.0))
+            return fail(DXMCG_ERR_ARGUMENT, "ct_segmentation_table: material " + std::to_string(i) + " is invalid");
+    // Tube tube(kvp); setAlFiltration; setSnFiltration; getSpecter(energies, true)
+    const int32_t fz[2] = { 13, 50 };
+    const double fmm[2] = { std::max(0.0, al_mm), std::max(0.0, sn_mm) };
+    const auto spec = tubeSpectrum(kvp, 12.0, 2, fz, fmm);
+    const dxmcg_material water = waterMaterial(), air = dryAirMaterial();
+    const double wd = 1.0, ad = 0.001205;
+    *out = dxmcg_segmentation {};
+    out->n_materials = n_materials;
+    out->water_density = wd;
+    out->air_density = ad;
+    const size_t ne = spec.energy.size();
+    std::vector<double> uw(ne), ua(ne);
+    for (size_t k = 0; k < ne; ++k) {
+        uw[k] = attenuation(water, 1, spec.energy[k]).sum();
+        ua[k] = attenuation(air, 1, spec.energy[k]).sum();
+        out->water_attenuation += spec.weight[k] * uw[k];
+        out->air_attenuation += spec.weight[k] * ua[k];
+    }
+    for (int i = 0; i < n_materials; ++i) {
+        double hu = 0.0, att = 0.0;
+        for (size_t k = 0; k < ne; ++k) {
+            const double um = attenuation(materials[i], 1, spec.energy[k]).sum();
+            const double w = spec.weight[k];
+            hu += w * (um * densities[i] - uw[k] * wd) / (uw[k] * wd - ua[k] * ad);
+            att += w * um;
+        }
+        out->hu[i] = 1000.0 * hu;
+        out->attenuation[i] = att;
+    }
+    for (int i = 0; i + 1 < n_materials; ++i)
+        out->separator[i] = (out->hu[i] + out->hu[i + 1]) / 2;
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_ct_segment_device(const dxmcg_segmentation* table, const double* hu, uint64_t n,
+    uint8_t* material, double* density, void* cuda_stream)
+{
+    SegTable t;
+    int rc = toSegTable(table, t);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (n == 0)
+        return DXMCG_OK;
+    if (!hu || !material || !density)
+        return fail(DXMCG_ERR_ARGUMENT, "ct_segment_device: null array");
+    const cudaError_t e = launchSegment(hu, n, t, material, density, static_cast<cudaStream_t>(cuda_stream));
+    if (e != cudaSuccess)
+        return cudaFail(e, "segmentation kernel launch");
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_ct_segment(const dxmcg_segmentation* table, const double* hu, uint64_t n, uint8_t* material,
+    double* density)
+{
+    SegTable t;
+    int rc = toSegTable(table, t);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (n == 0)
+        return DXMCG_OK;
+    if (!hu || !material || !density)
+        return fail(DXMCG_ERR_ARGUMENT, "ct_segment: null array");
+    if ((rc = currentDevice()) != DXMCG_OK)
+        return rc;
+    const size_t chunk = std::min<uint64_t>(n, kStreamChunk);
+    DeviceBuffer<double> dh, dd;
+    DeviceBuffer<uint8_t> dm;
+    DXMCG_CUDA(dh.alloc(chunk));
+    DXMCG_CUDA(dd.alloc(chunk));
+    DXMCG_CUDA(dm.alloc(chunk));
+    for (uint64_t a = 0; a < n; a += chunk) {
+        const size_t m = std::min<uint64_t>(chunk, n - a);
+        DXMCG_CUDA(cudaMemcpy(dh.p, hu + a, m * sizeof(double), cudaMemcpyHostToDevice));
+        const cudaError_t e = launchSegment(dh.p, m, t, dm.p, dd.p, nullptr);
+        if (e != cudaSuccess)
+            return cudaFail(e, "segmentation kernel launch");
+        DXMCG_CUDA(cudaMemcpy(material + a, dm.p, m, cudaMemcpyDeviceToHost));
+        DXMCG_CUDA(cudaMemcpy(density + a, dd.p, m * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_organ_dose_table_device(const uint8_t* organ, const double* dose, const double* density,
+    uint64_t n, const double spacing_cm[3], int n_organs, dxmcg_organ_dose* out, void* cuda_stream)
+{
+    double V = 0;
+    int rc = checkOrganArgs(spacing_cm, n_organs, out, V);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (n > 0 && (!organ || !dose || !density))
+        return fail(DXMCG_ERR_ARGUMENT, "organ_dose_table_device: null array");
+    const auto s = static_cast<cudaStream_t>(cuda_stream);
+    OrganSums sums;
+    if ((rc = sums.alloc(s)) != DXMCG_OK)
+        return rc;
+    if (n > 0) {
+        const cudaError_t e = launchOrganTable(organ, dose, density, n, V, n_organs, sums.cnt.p, sums.rho.p,
+            sums.e.p, s);
+        if (e != cudaSuccess)
+            return cudaFail(e, "organ table kernel launch");
+    }
+    return sums.read(V, n_organs, out, s);
+}
+
+DXMCG_API int dxmcg_organ_dose_table(const uint8_t* organ, const double* dose, const double* density, uint64_t n,
+    const double spacing_cm[3], int n_organs, dxmcg_organ_dose* out)
+{
+    double V = 0;
+    int rc = checkOrganArgs(spacing_cm, n_organs, out, V);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (n > 0 && (!organ || !dose || !density))
+        return fail(DXMCG_ERR_ARGUMENT, "organ_dose_table: null array");
+    if ((rc = currentDevice()) != DXMCG_OK)
+        return rc;
+    OrganSums sums;
+    if ((rc = sums.alloc(nullptr)) != DXMCG_OK)
+        return rc;
+    const size_t chunk = std::max<uint64_t>(1, std::min<uint64_t>(n, kStreamChunk));
+    DeviceBuffer<uint8_t> dor;
+    DeviceBuffer<double> dd, dr;
+    DXMCG_CUDA(dor.alloc(chunk));
+    DXMCG_CUDA(dd.alloc(chunk));
+    DXMCG_CUDA(dr.alloc(chunk));
+    for (uint64_t a = 0; a < n; a += chunk) {
+        const size_t m = std::min<uint64_t>(chunk, n - a);
+        DXMCG_CUDA(cudaMemcpy(dor.p, organ + a, m, cudaMemcpyHostToDevice));
+        DXMCG_CUDA(cudaMemcpy(dd.p, dose + a, m * sizeof(double), cudaMemcpyHostToDevice));
+        DXMCG_CUDA(cudaMemcpy(dr.p, density + a, m * sizeof(double), cudaMemcpyHostToDevice));
+        const cudaError_t e = launchOrganTable(dor.p, dd.p, dr.p, m, V, n_organs, sums.cnt.p, sums.rho.p, sums.e.p,
+            nullptr);
+        if (e != cudaSuccess)
+            return cudaFail(e, "organ table kernel launch");
+    }
+    return sums.read(V, n_organs, out, nullptr);
+}
+
+DXMCG_API int dxmcg_world_organ_dose(dxmcg_world* w, const uint8_t* organ, int n_organs, int delete_air_dose,
+    dxmcg_organ_dose* out)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_organ_dose: world not built");
+    double V = 0;
+    int rc = checkOrganArgs(w->spacing, n_organs, out, V);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (!organ)
+        return fail(DXMCG_ERR_ARGUMENT, "world_organ_dose: null organ array");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    OrganSums sums;
+    if ((rc = sums.alloc(w->stream)) != DXMCG_OK)
+        return rc;
+    DeviceBuffer<uint8_t> dor;
+    DXMCG_CUDA(dor.alloc(w->N));
+    DXMCG_CUDA(cudaMemcpyAsync(dor.p, organ, w->N, cudaMemcpyHostToDevice, w->stream));
+    const cudaError_t e = launchWorldOrganTable(dor.p, w->tally.p, w->vox.p, w->N, kKeVToMilliGrayGram / V,
+        delete_air_dose ? 1 : 0, V, n_organs, sums.cnt.p, sums.rho.p, sums.e.p, w->stream);
+    if (e != cudaSuccess)
+        return cudaFail(e, "world organ table kernel launch");
+    return sums.read(V, n_organs, out, w->stream);
+}
+
+DXMCG_API int dxmcg_world_read_dose_postprocessed(dxmcg_world* w, int delete_air_dose, double* dose,
+    double* variance, double* count, int* micro_gray)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_read_dose_postprocessed: world not built");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    DeviceBuffer<double> d, v, c;
+    DeviceBuffer<unsigned long long> mx;
+    DeviceBuffer<int> micro;
+    if (dose)
+        DXMCG_CUDA(d.alloc(w->N));
+    if (variance)
+        DXMCG_CUDA(v.alloc(w->N));
+    if (count)
+        DXMCG_CUDA(c.alloc(w->N));
+    DXMCG_CUDA(mx.alloc(1));
+    DXMCG_CUDA(micro.alloc(1));
+    const cudaError_t e = launchDosePostprocess(w->tally.p, w->vox.p, w->N, kKeVToMilliGrayGram / w->voxelVolume,
+        w->historiesScored, delete_air_dose ? 1 : 0, mx.p, dose ? d.p : nullptr, variance ? v.p : nullptr,
+        count ? c.p : nullptr, micro.p, w->stream);
+    if (e != cudaSuccess)
+        return cudaFail(e, "dose post-processing launch");
+    if (dose)
+        DXMCG_CUDA(cudaMemcpyAsync(dose, d.p, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    if (variance)
+        DXMCG_CUDA(cudaMemcpyAsync(variance, v.p, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    if (count)
+        DXMCG_CUDA(cudaMemcpyAsync(count, c.p, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    int mu = 0;
+    DXMCG_CUDA(cudaMemcpyAsync(&mu, micro.p, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    if (micro_gray)
+        *micro_gray = mu;
     return DXMCG_OK;
 }
 

@@ -156,6 +156,26 @@ cudaError_t launchTransportBatch(int tracking, const DevJob* jobs, const unsigne
     unsigned long long h_end, DevCounters* ctr, LaunchShape shape, cudaStream_t s);
 int transportMaxBlocksPerSMBatch(int block, int tracking);
 
+// per-voxel passes around the transport (pipelines.cu)
+constexpr int kMaxSegMaterials = 64;
+struct SegTable {
+    int nSep = 0;       // number of separators (materials - 1)
+    double slope = 0;   // w_att * w_dens - a_att * a_dens
+    double offset = 0;  // w_att * w_dens
+    double sep[kMaxSegMaterials - 1] {}; // HU midpoints between consecutive materials
+    double att[kMaxSegMaterials] {};     // spectrum-weighted mass attenuation per material
+};
+cudaError_t launchSegment(const double* hu, size_t n, const SegTable& t, uint8_t* mat, double* dens,
+    cudaStream_t s);
+cudaError_t launchOrganTable(const uint8_t* organ, const double* dose, const double* density, size_t n,
+    double voxel_volume, int n_organs, unsigned long long* cnt, double* sum_rho, double* sum_e, cudaStream_t s);
+cudaError_t launchWorldOrganTable(const uint8_t* organ, const Tally* tally, const uint32_t* vox, size_t n,
+    double energy_to_dose, int air_mask, double voxel_volume, int n_organs, unsigned long long* cnt,
+    double* sum_rho, double* sum_e, cudaStream_t s);
+cudaError_t launchDosePostprocess(const Tally* tally, const uint32_t* vox, size_t n, double energy_to_dose,
+    double n_histories, int air_mask, unsigned long long* max_bits, double* dose, double* var, double* count,
+    int* micro, cudaStream_t s);
+
 // host helpers (geometry.cpp)
 int expandExposures(const dxmcg_beam& b, std::vector<dxmcg_exposure>& out);
 // sets the calling thread's dxmcg_last_error() text and returns code (capi.cpp)

@@ -92,6 +92,53 @@ def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_
     return o
 
 
+def ct_segmentation_table(kvp=120.0, al_mm=0.0, sn_mm=0.0, materials=None) -> N.Segmentation:
+    """CTSegmentationPipeline's CT-number table for a tube setting; `materials` is a
+    list of (composition, density) in ascending CT number (default: the pipeline's
+    five, phantoms.SEGMENTATION_MATERIALS)."""
+    if materials is None:
+        from . import phantoms as P
+
+        materials = [(c, d) for _, c, d in P.SEGMENTATION_MATERIALS]
+    mats = (N.Material * len(materials))(*[N.Material.from_dict(c) for c, _ in materials])
+    dens = np.ascontiguousarray([d for _, d in materials], dtype=np.float64)
+    t = N.Segmentation()
+    N.check(N.lib().dxmcg_ct_segmentation_table(kvp, al_mm, sn_mm, len(materials), mats, N.ptr(dens, C.c_double),
+                                                C.byref(t)))
+    return t
+
+
+def ct_segment(table: N.Segmentation, hu: np.ndarray):
+    """HU array -> (uint8 material, float64 density), computed on the GPU."""
+    h = np.ascontiguousarray(hu, dtype=np.float64).reshape(-1)
+    m = np.zeros(h.size, dtype=np.uint8)
+    d = np.zeros(h.size, dtype=np.float64)
+    N.check(N.lib().dxmcg_ct_segment(C.byref(table), N.ptr(h, C.c_double), h.size, N.ptr(m, C.c_uint8),
+                                     N.ptr(d, C.c_double)))
+    return m.reshape(np.shape(hu)), d.reshape(np.shape(hu))
+
+
+def _organ_rows(out, n_organs):
+    return {"n_voxels": np.array([out[i].n_voxels for i in range(n_organs)], dtype=np.uint64),
+            "volume_cm3": np.array([out[i].volume_cm3 for i in range(n_organs)]),
+            "mass_g": np.array([out[i].mass_g for i in range(n_organs)]),
+            "dose": np.array([out[i].dose for i in range(n_organs)])}
+
+
+def organ_dose_table(organ: np.ndarray, dose: np.ndarray, density: np.ndarray, spacing_cm, n_organs: int) -> dict:
+    """DoseTablePipeline's table (per organ: voxels, volume, mass, mean dose), on the GPU."""
+    o = np.ascontiguousarray(organ, dtype=np.uint8).reshape(-1)
+    d = np.ascontiguousarray(dose, dtype=np.float64).reshape(-1)
+    r = np.ascontiguousarray(density, dtype=np.float64).reshape(-1)
+    if not (o.size == d.size == r.size):
+        raise ValueError("organ, dose and density must have the same size")
+    sp = np.ascontiguousarray(spacing_cm, dtype=np.float64)
+    out = (N.OrganDose * n_organs)()
+    N.check(N.lib().dxmcg_organ_dose_table(N.ptr(o, C.c_uint8), N.ptr(d, C.c_double), N.ptr(r, C.c_double), o.size,
+                                           N.ptr(sp, C.c_double), n_organs, out))
+    return _organ_rows(out, n_organs)
+
+
 class Progress:
     """TransportProgress mirror over dxmcg_progress (thread-safe in the library)."""
 
@@ -210,6 +257,27 @@ class GpuWorld:
         opts = options if options is not None else run_options()
         N.check(N.lib().dxmcg_sample_source(self._h, C.byref(b), C.byref(opts), n, N.ptr(out, C.c_double)))
         return out
+
+    def organ_dose(self, organ: np.ndarray, n_organs: int, delete_air_dose: bool = True) -> dict:
+        """Organ dose table straight from the tally (mGy)."""
+        o = np.ascontiguousarray(organ, dtype=np.uint8).reshape(-1)
+        if o.size != self.N:
+            raise ValueError("organ array size does not match the world")
+        out = (N.OrganDose * n_organs)()
+        N.check(N.lib().dxmcg_world_organ_dose(self._h, N.ptr(o, C.c_uint8), n_organs, int(delete_air_dose), out))
+        return _organ_rows(out, n_organs)
+
+    def dose_postprocessed(self, delete_air_dose: bool = True):
+        """(dose, variance, count as float64, micro_gray) as the worker stores them:
+        air voxels zeroed, uGy (x1e3, variance x1e6) when the maximum is below 1 mGy."""
+        d = np.zeros(self.N)
+        v = np.zeros(self.N)
+        c = np.zeros(self.N)
+        mu = C.c_int(0)
+        N.check(N.lib().dxmcg_world_read_dose_postprocessed(self._h, int(delete_air_dose), N.ptr(d, C.c_double),
+                                                            N.ptr(v, C.c_double), N.ptr(c, C.c_double),
+                                                            C.byref(mu)))
+        return d, v, c, bool(mu.value)
 
     def autotune(self, beam: dict, options: N.RunOptions | None = None, sample_histories: int = 0):
         """Fastest launch shape for this beam: (options with block_size, interact_batch

@@ -30,7 +30,10 @@ EXPORTED = [
     "dxmcg_world_set_data", "dxmcg_world_set_data_f32", "dxmcg_world_build", "dxmcg_world_destroy",
     "dxmcg_world_clear_tally", "dxmcg_world_read_tally", "dxmcg_world_read_dose", "dxmcg_world_tables",
     "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_batch_create", "dxmcg_batch_info",
-    "dxmcg_batch_run", "dxmcg_batch_destroy", "dxmcg_autotune", "dxmcg_transport_run_noalloc", "dxmcg_progress_create",
+    "dxmcg_batch_run", "dxmcg_batch_destroy", "dxmcg_autotune", "dxmcg_transport_run_noalloc",
+    "dxmcg_ct_segmentation_table", "dxmcg_ct_segment", "dxmcg_ct_segment_device", "dxmcg_organ_dose_table",
+    "dxmcg_organ_dose_table_device", "dxmcg_world_organ_dose", "dxmcg_world_read_dose_postprocessed",
+    "dxmcg_progress_create",
     "dxmcg_progress_destroy",
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_reset", "dxmcg_progress_continue",
     "dxmcg_progress_message",
@@ -43,6 +46,21 @@ class DxmcgError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"dxmcg {STATUS.get(code, code)}: {msg}")
         self.code = code
+
+
+MAX_SEG_MATERIALS = 64
+
+
+class Segmentation(C.Structure):
+    _fields_ = [("n_materials", C.c_int32), ("hu", C.c_double * MAX_SEG_MATERIALS),
+                ("separator", C.c_double * (MAX_SEG_MATERIALS - 1)),
+                ("attenuation", C.c_double * MAX_SEG_MATERIALS), ("water_attenuation", C.c_double),
+                ("water_density", C.c_double), ("air_attenuation", C.c_double), ("air_density", C.c_double)]
+
+
+class OrganDose(C.Structure):
+    _fields_ = [("n_voxels", C.c_uint64), ("volume_cm3", C.c_double), ("mass_g", C.c_double),
+                ("dose", C.c_double)]
 
 
 class Material(C.Structure):
@@ -179,6 +197,13 @@ def lib() -> C.CDLL:
         "dxmcg_autotune": (i, [vp, C.POINTER(Beam), C.POINTER(RunOptions), u64, pd]),
         "dxmcg_transport_run_noalloc": (i, [pi32, pd, vp, vp, C.POINTER(Material), i, i, C.POINTER(Beam),
                                             C.POINTER(RunOptions), vp, vp, C.POINTER(Stats)]),
+        "dxmcg_ct_segmentation_table": (i, [d, d, d, i, C.POINTER(Material), pd, C.POINTER(Segmentation)]),
+        "dxmcg_ct_segment": (i, [C.POINTER(Segmentation), pd, u64, pu8, pd]),
+        "dxmcg_ct_segment_device": (i, [C.POINTER(Segmentation), vp, u64, vp, vp, vp]),
+        "dxmcg_organ_dose_table": (i, [pu8, pd, pd, u64, pd, i, C.POINTER(OrganDose)]),
+        "dxmcg_organ_dose_table_device": (i, [vp, vp, vp, u64, pd, i, C.POINTER(OrganDose), vp]),
+        "dxmcg_world_organ_dose": (i, [vp, pu8, i, i, C.POINTER(OrganDose)]),
+        "dxmcg_world_read_dose_postprocessed": (i, [vp, i, pd, pd, pd, C.POINTER(C.c_int)]),
         "dxmcg_progress_create": (vp, []),
         "dxmcg_progress_destroy": (None, [vp]),
         "dxmcg_progress_get": (None, [vp, pu64, pu64]),

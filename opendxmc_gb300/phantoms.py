@@ -31,6 +31,19 @@ SIX_MATERIALS = [
 ]
 
 
+# The five materials CTSegmentationPipeline segments CT numbers into
+# (ctsegmentationpipeline.cpp:120-127): air, adipose, soft tissue, muscle and cortical
+# bone, with bone's density lowered to 1.09 g/cm3 as there.  DXMClib's NIST
+# compositions are not available here; the ICRP media rows above stand in for them.
+SEGMENTATION_MATERIALS = [
+    ("Air, Dry (near sea level)", AIR, 0.001205),
+    ("Adipose Tissue (ICRP)", ADIPOSE, 0.95),
+    ("Tissue, Soft (ICRP)", SOFT_TISSUE, 1.03),
+    ("Muscle, Skeletal", MUSCLE, 1.04),
+    ("Bone, Cortical (ICRP)", BONE, 1.09),
+]
+
+
 @dataclass
 class Phantom:
     dims: tuple  # (nx, ny, nz)

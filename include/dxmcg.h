@@ -325,6 +325,59 @@ DXMCG_API int dxmcg_world_organ_dose(dxmcg_world* w, const uint8_t* organ, int n
 DXMCG_API int dxmcg_world_read_dose_postprocessed(dxmcg_world* w, int delete_air_dose, double* dose,
     double* variance, double* count, int* micro_gray);
 
+/* ---- dose denoiser ---------------------------------------------------------------
+ * No counterpart in the reference.  A 3D convolutional encoder-decoder maps a
+ * short run's dose (with the density and material maps) to the converged dose.
+ * Levels l = 0..levels-1 at resolution R / 2^l with channels[l] (multiples of 16):
+ * two 3x3x3 conv + ReLU per level, 2x2x2 average pooling down, nearest upsampling
+ * and concatenation with the level's encoder output up, then a 1x1x1 head.
+ * Weights and activations bf16, FP32 accumulation, FP32 master weights and Adam.
+ * Tensors are device arrays [B][D][H][W][C] ("channels last"); the input has 16
+ * channels: log(1 + dose / scale), density, one-hot of material 0..5, 8 zeros.
+ * D, H and W must be multiples of 2^(levels - 1).  Calls take a CUDA stream
+ * (NULL: the default stream) and are ordered on it; they return after queuing,
+ * except where a host result (loss, parameters) is returned. */
+typedef struct dxmcg_denoiser dxmcg_denoiser;
+typedef struct {
+    int32_t levels;      /* 1..5 */
+    int32_t channels[5]; /* per level, multiples of 16; channels[0] 16 or 32 */
+    uint64_t seed;       /* He-normal initialisation */
+} dxmcg_denoiser_config;
+DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* config, dxmcg_denoiser** out);
+DXMCG_API void dxmcg_denoiser_destroy(dxmcg_denoiser* d);
+/* parameters as one FP32 vector: per conv layer (enc0a, enc0b, ..., enc(L-1)b,
+ * dec(L-2)a, dec(L-2)b, ..., dec0a, dec0b) weights [Cout][27][Cin] then bias
+ * [Cout]; then the head's weights [channels[0]] and bias */
+DXMCG_API int dxmcg_denoiser_param_count(const dxmcg_denoiser* d, uint64_t* n);
+DXMCG_API int dxmcg_denoiser_get_params(dxmcg_denoiser* d, float* host);
+/* sets the parameters and restarts the optimiser (Adam moments and step 0) */
+DXMCG_API int dxmcg_denoiser_set_params(dxmcg_denoiser* d, const float* host);
+/* gradients of the last dxmcg_denoiser_backward, same layout */
+DXMCG_API int dxmcg_denoiser_get_grads(dxmcg_denoiser* d, float* host);
+/* pred[B][D][H][W] (FP32, normalised dose) */
+DXMCG_API int dxmcg_denoiser_forward(dxmcg_denoiser* d, const void* input, int B, int D, int H, int W, float* pred,
+    void* cuda_stream);
+/* forward, L1 loss against target[B][D][H][W] and backward; *loss = mean |pred - target| */
+DXMCG_API int dxmcg_denoiser_backward(dxmcg_denoiser* d, const void* input, const float* target, int B, int D,
+    int H, int W, double* loss, void* cuda_stream);
+/* one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) with the last gradients */
+DXMCG_API int dxmcg_denoiser_adam(dxmcg_denoiser* d, float lr, void* cuda_stream);
+/* the 16 input channels of n voxels from device arrays (dose, density, material) */
+DXMCG_API int dxmcg_denoiser_prepare_input(const float* dose, const float* density, const uint8_t* material,
+    uint64_t n, double scale, void* input, void* cuda_stream);
+/* copy n_patch cubes of edge P into batch tensors: volume v < n_volumes has device
+ * input inputs[v] (16 channels) and target targets[v] of dims[3v..3v+2] = (D, H, W);
+ * origins[4p..4p+3] = (v, z, y, x); all four arrays in device memory.  Voxels of a
+ * patch outside its volume are written as zeros. */
+DXMCG_API int dxmcg_denoiser_gather_patches(const void* const* inputs, const float* const* targets,
+    const int32_t* dims, int n_volumes, const int32_t* origins, int n_patch, int P, void* input_batch,
+    float* target_batch, void* cuda_stream);
+/* A world's dose, denoised: input from its tally and voxels, scale = the mean dose
+ * of voxels denser than 0.2 g/cm3 (or `scale` when > 0), dose_out (host, N, mGy as
+ * dxmcg_world_read_dose; may be NULL) and *scale_used (may be NULL). */
+DXMCG_API int dxmcg_world_denoise(dxmcg_world* w, dxmcg_denoiser* d, double scale, double* dose_out,
+    double* scale_used);
+
 /* ---- TransportProgress (simulationpipeline.cpp:114-120, :234, :261) ---------- */
 DXMCG_API dxmcg_progress* dxmcg_progress_create(void);
 DXMCG_API void dxmcg_progress_destroy(dxmcg_progress* p);

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/dxmcg.h"
+#include "denoiser.hpp"
 #include "engine.hpp"
 #include "jobs.hpp"
 #include "physics.hpp"
@@ -409,6 +410,19 @@ struct OrganSums {
         return DXMCG_OK;
     }
 };
+
+// the calling thread's sums on its current device, kept between calls (a table is a
+// few hundred bytes; allocating it per call would put a cudaFree in every call)
+OrganSums& organSums()
+{
+    thread_local std::map<int, std::unique_ptr<OrganSums>> perDevice;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    auto& p = perDevice[dev];
+    if (!p)
+        p = std::make_unique<OrganSums>();
+    return *p;
+}
 
 int checkOrganArgs(const double* spacing, int nOrgans, const dxmcg_organ_dose* out, double& V)
 {
@@ -1163,7 +1177,7 @@ DXMCG_API int dxmcg_organ_dose_table_device(const uint8_t* organ, const double* 
     if (n > 0 && (!organ || !dose || !density))
         return fail(DXMCG_ERR_ARGUMENT, "organ_dose_table_device: null array");
     const auto s = static_cast<cudaStream_t>(cuda_stream);
-    OrganSums sums;
+    OrganSums& sums = organSums();
     if ((rc = sums.alloc(s)) != DXMCG_OK)
         return rc;
     if (n > 0) {
@@ -1186,7 +1200,7 @@ DXMCG_API int dxmcg_organ_dose_table(const uint8_t* organ, const double* dose, c
         return fail(DXMCG_ERR_ARGUMENT, "organ_dose_table: null array");
     if ((rc = currentDevice()) != DXMCG_OK)
         return rc;
-    OrganSums sums;
+    OrganSums& sums = organSums();
     if ((rc = sums.alloc(nullptr)) != DXMCG_OK)
         return rc;
     const size_t chunk = std::max<uint64_t>(1, std::min<uint64_t>(n, kStreamChunk));
@@ -1220,7 +1234,7 @@ DXMCG_API int dxmcg_world_organ_dose(dxmcg_world* w, const uint8_t* organ, int n
     if (!organ)
         return fail(DXMCG_ERR_ARGUMENT, "world_organ_dose: null organ array");
     DXMCG_CUDA(cudaSetDevice(w->device));
-    OrganSums sums;
+    OrganSums& sums = organSums();
     if ((rc = sums.alloc(w->stream)) != DXMCG_OK)
         return rc;
     DeviceBuffer<uint8_t> dor;
@@ -1267,6 +1281,19 @@ DXMCG_API int dxmcg_world_read_dose_postprocessed(dxmcg_world* w, int delete_air
     if (micro_gray)
         *micro_gray = mu;
     return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_world_denoise(dxmcg_world* w, dxmcg_denoiser* d, double scale, double* dose_out,
+    double* scale_used)
+{
+    if (!w || !w->built)
+        return fail(DXMCG_ERR_STATE, "world_denoise: world not built");
+    if (!d)
+        return fail(DXMCG_ERR_ARGUMENT, "world_denoise: null denoiser");
+    DXMCG_CUDA(cudaSetDevice(w->device));
+    DXMCG_CUDA(cudaStreamSynchronize(w->stream));
+    return nn::denoiseWorld(d, w->device, w->tally.p, w->vox.p, w->dims[0], w->dims[1], w->dims[2],
+        kKeVToMilliGrayGram / w->voxelVolume, scale, dose_out, scale_used, w->stream);
 }
 
 DXMCG_API dxmcg_progress* dxmcg_progress_create(void) { return new dxmcg_progress(); }

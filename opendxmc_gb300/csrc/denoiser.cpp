@@ -1,0 +1,489 @@
+// denoiser.cpp -- the dose denoiser network on the GPU: parameters, activation
+// buffers, forward, backward and Adam, and the C ABI (include/dxmcg.h).  Every
+// tensor operation is a kernel of denoiser_kernels.cu.  No counterpart in the
+// reference.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/dxmcg.h"
+#include "denoiser.hpp"
+#include "devbuf.hpp"
+
+using namespace dxmcg;
+using bf16 = __nv_bfloat16;
+
+#define NN_CUDA(call)                                                                                               \
+    do {                                                                                                            \
+        const cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess)                                                                                      \
+            return reportError(DXMCG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+struct dxmcg_denoiser {
+    struct Layer {
+        int cin, cout;
+        size_t w, b, wt; // offsets: weights and bias in the parameter vector, weights in the transposed copy
+    };
+    int device = 0;
+    int L = 0;
+    int ch[5] {};
+    std::vector<Layer> layers;
+    size_t head = 0, nParams = 0, nWt = 0;
+    DevBuf<float> p, g, m, v;
+    DevBuf<bf16> pb, wt;
+    long step = 0;
+    bool configured = false;
+
+    // activations and gradients of the current shape, per level
+    int B = 0, D = 0, H = 0, W = 0;
+    std::vector<DevBuf<bf16>> x, ea, eb, da, db, gx, gea, geb, gda, gdb, dcat;
+    DevBuf<bf16> dz;
+    DevBuf<float> pred;
+    DevBuf<double> loss;
+
+    int encA(int l) const { return 2 * l; }
+    int encB(int l) const { return 2 * l + 1; }
+    int decA(int l) const { return 2 * L + 2 * (L - 2 - l); }
+    int decB(int l) const { return decA(l) + 1; }
+    size_t nvox(int l) const { return static_cast<size_t>(B) * (D >> l) * (H >> l) * (W >> l); }
+};
+
+namespace {
+
+int fail(int code, const std::string& msg) { return reportError(code, msg); }
+
+int ensureShape(dxmcg_denoiser* d, int B, int D, int H, int W)
+{
+    const int f = 1 << (d->L - 1);
+    if (B < 1 || D < f || H < f || W < f || D % f || H % f || W % f)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser: dims must be positive multiples of 2^(levels-1)");
+    if (d->B == B && d->D == D && d->H == H && d->W == W)
+        return DXMCG_OK;
+    d->B = B;
+    d->D = D;
+    d->H = H;
+    d->W = W;
+    const int L = d->L;
+    for (auto* vec : { &d->x, &d->ea, &d->eb, &d->da, &d->db, &d->gx, &d->gea, &d->geb, &d->gda, &d->gdb,
+             &d->dcat }) {
+        vec->clear();
+        vec->resize(L);
+    }
+    size_t dzMax = 0;
+    for (int l = 0; l < L; ++l) {
+        const size_t n = d->nvox(l);
+        const size_t c = d->ch[l];
+        if (l > 0) {
+            NN_CUDA(d->x[l].reserve(n * d->ch[l - 1]));
+            NN_CUDA(d->gx[l].reserve(n * d->ch[l - 1]));
+        }
+        NN_CUDA(d->ea[l].reserve(n * c));
+        NN_CUDA(d->eb[l].reserve(n * c));
+        NN_CUDA(d->gea[l].reserve(n * c));
+        NN_CUDA(d->geb[l].reserve(n * c));
+        if (l < L - 1) {
+            NN_CUDA(d->da[l].reserve(n * c));
+            NN_CUDA(d->db[l].reserve(n * c));
+            NN_CUDA(d->gda[l].reserve(n * c));
+            NN_CUDA(d->gdb[l].reserve(n * c));
+            NN_CUDA(d->dcat[l].reserve(n * (c + d->ch[l + 1])));
+        }
+        dzMax = std::max(dzMax, n * c);
+    }
+    NN_CUDA(d->dz.reserve(dzMax));
+    NN_CUDA(d->pred.reserve(d->nvox(0)));
+    NN_CUDA(d->loss.reserve(1));
+    return DXMCG_OK;
+}
+
+int refreshWeights(dxmcg_denoiser* d, cudaStream_t s)
+{
+    for (const auto& ly : d->layers)
+        NN_CUDA(nn::launchTransposeWeights(d->pb.p + ly.w, d->wt.p + ly.wt, ly.cout, ly.cin, s));
+    return DXMCG_OK;
+}
+
+int conv(dxmcg_denoiser* d, int k, const nn::ConvIn& in, int l, bf16* out, cudaStream_t s)
+{
+    const auto& ly = d->layers[k];
+    NN_CUDA(nn::launchConv3(in, d->B, d->D >> l, d->H >> l, d->W >> l, ly.cin, d->pb.p + ly.w, d->p.p + ly.b,
+        ly.cout, true, out, s));
+    return DXMCG_OK;
+}
+
+nn::ConvIn plain(const bf16* t, int c)
+{
+    nn::ConvIn in;
+    in.a = t;
+    in.ca = c;
+    return in;
+}
+
+// input of decoder level l: upsample(d_{l+1}) ++ e_lb
+nn::ConvIn decIn(dxmcg_denoiser* d, int l)
+{
+    nn::ConvIn in;
+    in.a = l + 1 < d->L - 1 ? d->db[l + 1].p : d->eb[d->L - 1].p;
+    in.ca = d->ch[l + 1];
+    in.halfA = 1;
+    in.b = d->eb[l].p;
+    in.cb = d->ch[l];
+    return in;
+}
+
+nn::ConvIn encIn(dxmcg_denoiser* d, int l, const bf16* input)
+{
+    return l == 0 ? plain(input, 16) : plain(d->x[l].p, d->ch[l - 1]);
+}
+
+int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s)
+{
+    int rc;
+    for (int l = 0; l < d->L; ++l) {
+        if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s)) != DXMCG_OK)
+            return rc;
+        if ((rc = conv(d, d->encB(l), plain(d->ea[l].p, d->ch[l]), l, d->eb[l].p, s)) != DXMCG_OK)
+            return rc;
+        if (l < d->L - 1)
+            NN_CUDA(nn::launchAvgPool(d->eb[l].p, d->x[l + 1].p, d->B, d->D >> l, d->H >> l, d->W >> l, d->ch[l], s));
+    }
+    for (int l = d->L - 2; l >= 0; --l) {
+        if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s)) != DXMCG_OK)
+            return rc;
+        if ((rc = conv(d, d->decB(l), plain(d->da[l].p, d->ch[l]), l, d->db[l].p, s)) != DXMCG_OK)
+            return rc;
+    }
+    return DXMCG_OK;
+}
+
+const bf16* finalActivation(dxmcg_denoiser* d) { return d->L > 1 ? d->db[0].p : d->eb[0].p; }
+
+// relu backward + weight/bias gradients, and the input gradient when dxOut
+int layerBack(dxmcg_denoiser* d, int k, const nn::ConvIn& xin, const bf16* y, const bf16* dy, bf16* dxOut, int l,
+    cudaStream_t s)
+{
+    const auto& ly = d->layers[k];
+    const int Dl = d->D >> l, Hl = d->H >> l, Wl = d->W >> l;
+    NN_CUDA(nn::launchReluBackward(dy, y, d->dz.p, d->nvox(l), ly.cout, d->g.p + ly.b, s));
+    NN_CUDA(nn::launchWgrad(xin, d->dz.p, d->B, Dl, Hl, Wl, ly.cin, ly.cout, d->g.p + ly.w, s));
+    if (dxOut)
+        NN_CUDA(nn::launchConv3(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr,
+            ly.cin, false, dxOut, s));
+    return DXMCG_OK;
+}
+
+int backward(dxmcg_denoiser* d, const bf16* input, const float* target, cudaStream_t s)
+{
+    NN_CUDA(cudaMemsetAsync(d->g.p, 0, d->nParams * sizeof(float), s));
+    NN_CUDA(cudaMemsetAsync(d->loss.p, 0, sizeof(double), s));
+    const int L = d->L;
+    bf16* gFinal = L > 1 ? d->gdb[0].p : d->geb[0].p;
+    NN_CUDA(nn::launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, d->nvox(0), target, d->pred.p, 1.0,
+        nullptr, gFinal, d->g.p + d->head, d->loss.p, s));
+    int rc;
+    // decoder, from the head towards the bottleneck
+    for (int l = 0; l < L - 1; ++l) {
+        if ((rc = layerBack(d, d->decB(l), plain(d->da[l].p, d->ch[l]), d->db[l].p, d->gdb[l].p, d->gda[l].p, l, s))
+            != DXMCG_OK)
+            return rc;
+        if ((rc = layerBack(d, d->decA(l), decIn(d, l), d->da[l].p, d->gda[l].p, d->dcat[l].p, l, s)) != DXMCG_OK)
+            return rc;
+        bf16* du = l + 1 < L - 1 ? d->gdb[l + 1].p : d->geb[L - 1].p;
+        NN_CUDA(nn::launchSplitConcatGrad(d->dcat[l].p, d->ch[l + 1], d->ch[l], nullptr, du, nullptr, d->B,
+            d->D >> l, d->H >> l, d->W >> l, s));
+    }
+    // encoder, from the bottleneck down
+    for (int l = L - 1; l >= 0; --l) {
+        if (l < L - 1)
+            NN_CUDA(nn::launchSplitConcatGrad(d->dcat[l].p, d->ch[l + 1], d->ch[l], d->gx[l + 1].p, nullptr,
+                d->geb[l].p, d->B, d->D >> l, d->H >> l, d->W >> l, s));
+        if ((rc = layerBack(d, d->encB(l), plain(d->ea[l].p, d->ch[l]), d->eb[l].p, d->geb[l].p, d->gea[l].p, l, s))
+            != DXMCG_OK)
+            return rc;
+        if ((rc = layerBack(d, d->encA(l), encIn(d, l, input), d->ea[l].p, d->gea[l].p, l > 0 ? d->gx[l].p : nullptr,
+                 l, s))
+            != DXMCG_OK)
+            return rc;
+    }
+    return DXMCG_OK;
+}
+
+int checkNet(const dxmcg_denoiser* d)
+{
+    if (!d)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser: null handle");
+    return cudaSetDevice(d->device) == cudaSuccess ? DXMCG_OK : fail(DXMCG_ERR_CUDA, "denoiser: cudaSetDevice");
+}
+
+} // namespace
+
+namespace dxmcg {
+namespace nn {
+    // the world path (capi.cpp): input from a tally, forward, dose = pred * scale
+    int denoiseWorld(dxmcg_denoiser* d, int device, const Tally* tally, const uint32_t* vox, int nx, int ny, int nz,
+        double toDose, double scale, double* hostOut, double* scaleUsed, cudaStream_t s)
+    {
+        int rc = checkNet(d);
+        if (rc != DXMCG_OK)
+            return rc;
+        if (d->device != device)
+            return fail(DXMCG_ERR_ARGUMENT, "world_denoise: the denoiser and the world are on different devices");
+        if ((rc = ensureShape(d, 1, nz, ny, nx)) != DXMCG_OK)
+            return rc;
+        const size_t n = static_cast<size_t>(nx) * ny * nz;
+        if (!(scale > 0.0)) {
+            DevBuf<double> sum;
+            DevBuf<unsigned long long> cnt;
+            NN_CUDA(sum.reserve(1));
+            NN_CUDA(cnt.reserve(1));
+            NN_CUDA(cudaMemsetAsync(sum.p, 0, sizeof(double), s));
+            NN_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), s));
+            NN_CUDA(launchDoseMean(tally, vox, toDose, n, 0.2f, sum.p, cnt.p, s));
+            double hs = 0;
+            unsigned long long hc = 0;
+            NN_CUDA(cudaMemcpyAsync(&hs, sum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+            NN_CUDA(cudaMemcpyAsync(&hc, cnt.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
+            NN_CUDA(cudaStreamSynchronize(s));
+            scale = hc ? hs / static_cast<double>(hc) : 0.0;
+            if (!(scale > 0.0))
+                return fail(DXMCG_ERR_STATE, "world_denoise: no dose above 0.2 g/cm3 to normalise by");
+        }
+        if (scaleUsed)
+            *scaleUsed = scale;
+        DevBuf<bf16> input;
+        DevBuf<double> out;
+        NN_CUDA(input.reserve(n * 16));
+        NN_CUDA(out.reserve(n));
+        NN_CUDA(launchPrepareInput(nullptr, nullptr, nullptr, tally, vox, toDose, n, static_cast<float>(1.0 / scale),
+            input.p, s));
+        if ((rc = forward(d, input.p, s)) != DXMCG_OK)
+            return rc;
+        NN_CUDA(launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, n, nullptr, nullptr, scale, out.p, nullptr,
+            nullptr, nullptr, s));
+        if (hostOut)
+            NN_CUDA(cudaMemcpyAsync(hostOut, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        NN_CUDA(cudaStreamSynchronize(s));
+        return DXMCG_OK;
+    }
+} // namespace nn
+} // namespace dxmcg
+
+extern "C" {
+
+DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* c, dxmcg_denoiser** out)
+{
+    if (!out || !c)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_create: null argument");
+    *out = nullptr;
+    if (c->levels < 1 || c->levels > 5)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_create: levels must be 1..5");
+    for (int l = 0; l < c->levels; ++l)
+        if (c->channels[l] < 16 || c->channels[l] % 16 || c->channels[l] > 256)
+            return fail(DXMCG_ERR_ARGUMENT, "denoiser_create: channels must be multiples of 16 up to 256");
+    if (c->channels[0] != 16 && c->channels[0] != 32)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_create: channels[0] must be 16 or 32");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1)
+        return fail(DXMCG_ERR_NO_DEVICE, "denoiser_create: no CUDA device");
+    auto d = std::make_unique<dxmcg_denoiser>();
+    cudaGetDevice(&d->device);
+    d->L = c->levels;
+    for (int l = 0; l < d->L; ++l)
+        d->ch[l] = c->channels[l];
+    std::vector<std::pair<int, int>> shapes; // (cin, cout) in layer order
+    int prev = 16;
+    for (int l = 0; l < d->L; ++l) {
+        shapes.push_back({ prev, d->ch[l] });
+        shapes.push_back({ d->ch[l], d->ch[l] });
+        prev = d->ch[l];
+    }
+    for (int l = d->L - 2; l >= 0; --l) {
+        shapes.push_back({ d->ch[l + 1] + d->ch[l], d->ch[l] });
+        shapes.push_back({ d->ch[l], d->ch[l] });
+    }
+    size_t o = 0, ot = 0;
+    for (auto [ci, co] : shapes) {
+        dxmcg_denoiser::Layer ly { ci, co, o, o + static_cast<size_t>(co) * 27 * ci, ot };
+        d->layers.push_back(ly);
+        o += static_cast<size_t>(co) * 27 * ci + co;
+        ot += static_cast<size_t>(co) * 27 * ci;
+    }
+    d->head = o;
+    d->nParams = o + d->ch[0] + 1;
+    d->nWt = ot;
+    // He-normal initialisation on the host (std::normal_distribution, seeded)
+    std::vector<float> h(d->nParams, 0.0f);
+    std::mt19937_64 rng(c->seed);
+    for (const auto& ly : d->layers) {
+        std::normal_distribution<double> nd(0.0, std::sqrt(2.0 / (27.0 * ly.cin)));
+        for (size_t i = ly.w; i < ly.b; ++i)
+            h[i] = static_cast<float>(nd(rng));
+    }
+    std::normal_distribution<double> nh(0.0, std::sqrt(1.0 / d->ch[0]));
+    for (int i = 0; i < d->ch[0]; ++i)
+        h[d->head + i] = static_cast<float>(nh(rng));
+    NN_CUDA(nn::conv3Configure());
+    NN_CUDA(d->p.reserve(d->nParams));
+    NN_CUDA(d->g.reserve(d->nParams));
+    NN_CUDA(d->m.reserve(d->nParams));
+    NN_CUDA(d->v.reserve(d->nParams));
+    NN_CUDA(d->pb.reserve(d->nParams));
+    NN_CUDA(d->wt.reserve(d->nWt));
+    *out = d.release();
+    const int rc = dxmcg_denoiser_set_params(*out, h.data());
+    if (rc != DXMCG_OK) {
+        delete *out;
+        *out = nullptr;
+    }
+    return rc;
+}
+
+DXMCG_API void dxmcg_denoiser_destroy(dxmcg_denoiser* d)
+{
+    if (!d)
+        return;
+    cudaSetDevice(d->device);
+    cudaDeviceSynchronize();
+    delete d;
+}
+
+DXMCG_API int dxmcg_denoiser_param_count(const dxmcg_denoiser* d, uint64_t* n)
+{
+    if (!d || !n)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_param_count: null argument");
+    *n = d->nParams;
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_denoiser_get_params(dxmcg_denoiser* d, float* host)
+{
+    int rc = checkNet(d);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (!host)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_get_params: null output");
+    NN_CUDA(cudaDeviceSynchronize());
+    NN_CUDA(cudaMemcpy(host, d->p.p, d->nParams * sizeof(float), cudaMemcpyDeviceToHost));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_denoiser_set_params(dxmcg_denoiser* d, const float* host)
+{
+    int rc = checkNet(d);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (!host)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_set_params: null input");
+    NN_CUDA(cudaDeviceSynchronize());
+    NN_CUDA(cudaMemcpy(d->p.p, host, d->nParams * sizeof(float), cudaMemcpyHostToDevice));
+    NN_CUDA(cudaMemset(d->m.p, 0, d->nParams * sizeof(float)));
+    NN_CUDA(cudaMemset(d->v.p, 0, d->nParams * sizeof(float)));
+    NN_CUDA(cudaMemset(d->g.p, 0, d->nParams * sizeof(float)));
+    d->step = 0;
+    NN_CUDA(nn::launchToBf16(d->p.p, d->pb.p, d->nParams, nullptr));
+    if ((rc = refreshWeights(d, nullptr)) != DXMCG_OK)
+        return rc;
+    NN_CUDA(cudaDeviceSynchronize());
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_denoiser_get_grads(dxmcg_denoiser* d, float* host)
+{
+    int rc = checkNet(d);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (!host)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_get_grads: null output");
+    NN_CUDA(cudaDeviceSynchronize());
+    NN_CUDA(cudaMemcpy(host, d->g.p, d->nParams * sizeof(float), cudaMemcpyDeviceToHost));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_denoiser_forward(dxmcg_denoiser* d, const void* input, int B, int D, int H, int W, float* pred,
+    void* cuda_stream)
+{
+    int rc = checkNet(d);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (!input || !pred)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_forward: null array");
+    if ((rc = ensureShape(d, B, D, H, W)) != DXMCG_OK)
+        return rc;
+    const auto s = static_cast<cudaStream_t>(cuda_stream);
+    if ((rc = forward(d, static_cast<const bf16*>(input), s)) != DXMCG_OK)
+        return rc;
+    NN_CUDA(nn::launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, d->nvox(0), nullptr, pred, 1.0, nullptr,
+        nullptr, nullptr, nullptr, s));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_denoiser_backward(dxmcg_denoiser* d, const void* input, const float* target, int B, int D,
+    int H, int W, double* loss, void* cuda_stream)
+{
+    int rc = checkNet(d);
+    if (rc != DXMCG_OK)
+        return rc;
+    if (!input || !target)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_backward: null array");
+    if ((rc = ensureShape(d, B, D, H, W)) != DXMCG_OK)
+        return rc;
+    const auto s = static_cast<cudaStream_t>(cuda_stream);
+    const auto* in = static_cast<const bf16*>(input);
+    if ((rc = forward(d, in, s)) != DXMCG_OK)
+        return rc;
+    if ((rc = backward(d, in, target, s)) != DXMCG_OK)
+        return rc;
+    if (loss) {
+        double h = 0;
+        NN_CUDA(cudaMemcpyAsync(&h, d->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+        NN_CUDA(cudaStreamSynchronize(s));
+        *loss = h / static_cast<double>(d->nvox(0));
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_denoiser_adam(dxmcg_denoiser* d, float lr, void* cuda_stream)
+{
+    int rc = checkNet(d);
+    if (rc != DXMCG_OK)
+        return rc;
+    const auto s = static_cast<cudaStream_t>(cuda_stream);
+    const double b1 = 0.9, b2 = 0.999;
+    ++d->step;
+    const float c1 = static_cast<float>(1.0 / (1.0 - std::pow(b1, static_cast<double>(d->step))));
+    const float c2 = static_cast<float>(1.0 / (1.0 - std::pow(b2, static_cast<double>(d->step))));
+    NN_CUDA(nn::launchAdam(d->p.p, d->g.p, d->m.p, d->v.p, d->pb.p, d->nParams, lr, static_cast<float>(b1),
+        static_cast<float>(b2), 1e-8f, c1, c2, s));
+    return refreshWeights(d, s);
+}
+
+DXMCG_API int dxmcg_denoiser_prepare_input(const float* dose, const float* density, const uint8_t* material,
+    uint64_t n, double scale, void* input, void* cuda_stream)
+{
+    if (n == 0)
+        return DXMCG_OK;
+    if (!dose || !density || !material || !input || !(scale > 0.0))
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_prepare_input: null array or scale <= 0");
+    NN_CUDA(nn::launchPrepareInput(dose, density, material, nullptr, nullptr, 0.0, n, static_cast<float>(1.0 / scale),
+        static_cast<bf16*>(input), static_cast<cudaStream_t>(cuda_stream)));
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_denoiser_gather_patches(const void* const* inputs, const float* const* targets,
+    const int32_t* dims, int n_volumes, const int32_t* origins, int n_patch, int P, void* input_batch,
+    float* target_batch, void* cuda_stream)
+{
+    if (n_volumes < 1 || n_patch < 1 || P < 1 || !inputs || !targets || !dims || !origins || !input_batch
+        || !target_batch)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_gather_patches: bad arguments");
+    NN_CUDA(nn::launchGatherPatches(reinterpret_cast<const bf16* const*>(inputs), targets, dims, n_volumes, origins,
+        n_patch, P, static_cast<bf16*>(input_batch), target_batch, static_cast<cudaStream_t>(cuda_stream)));
+    return DXMCG_OK;
+}
+
+} // extern "C"

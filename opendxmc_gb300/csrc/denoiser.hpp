@@ -1,0 +1,67 @@
+// denoiser.hpp -- launchers of the denoiser kernels (denoiser_kernels.cu) and the
+// network that drives them (denoiser.cpp).  Tensors are [B][D][H][W][C] bf16,
+// C a multiple of 16; weights [Cout][27][Cin] bf16 with tap (dz+1)*9+(dy+1)*3+(dx+1).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "engine.hpp"
+
+namespace dxmcg {
+namespace nn {
+
+// Input of a convolution: channels [0, ca) from tensor a (at half resolution,
+// nearest-upsampled on the fly, when halfA), channels [ca, ca + cb) from b.
+struct ConvIn {
+    const __nv_bfloat16* a = nullptr;
+    int ca = 0;
+    int halfA = 0;
+    const __nv_bfloat16* b = nullptr;
+    int cb = 0;
+};
+
+size_t conv3SmemBytes(int nt);
+size_t wgradSmemBytes(int nt);
+cudaError_t conv3Configure(); // opt the kernels into their shared-memory size (once per device)
+
+// out = act(conv3(in) + bias), act = relu or identity; bias may be null
+cudaError_t launchConv3(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
+    const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);
+// dW[co][t][ci] += sum_v dz[v][co] x[v + off(t)][ci]  (FP32 atomics)
+cudaError_t launchWgrad(const ConvIn& in, const __nv_bfloat16* dz, int B, int D, int H, int W, int Cin, int Cout,
+    float* dW, cudaStream_t s);
+// dz = dy * (y > 0), db += sum over voxels of dz
+cudaError_t launchReluBackward(const __nv_bfloat16* dy, const __nv_bfloat16* y, __nv_bfloat16* dz, size_t nvox,
+    int C, float* db, cudaStream_t s);
+cudaError_t launchAvgPool(const __nv_bfloat16* x, __nv_bfloat16* out, int B, int D, int H, int W, int C,
+    cudaStream_t s);
+// du (half res) = sum of children of dcat[:, :cu]; de = dcat[:, cu:] + dxNext(parent) / 8 (either may be null)
+cudaError_t launchSplitConcatGrad(const __nv_bfloat16* dcat, int cu, int cs, const __nv_bfloat16* dxNext,
+    __nv_bfloat16* du, __nv_bfloat16* de, int B, int D, int H, int W, cudaStream_t s);
+// head: pred = d . w + b; with a target also the L1 loss sum and the gradients
+cudaError_t launchHead(const __nv_bfloat16* d, int C0, const float* hw, size_t nvox, const float* target,
+    float* pred, double predScale, double* predOut, __nv_bfloat16* dd, float* dhw, double* lossSum, cudaStream_t s);
+cudaError_t launchAdam(float* p, const float* g, float* m, float* v, __nv_bfloat16* pb, size_t n, float lr, float b1,
+    float b2, float eps, float c1, float c2, cudaStream_t s);
+cudaError_t launchToBf16(const float* p, __nv_bfloat16* pb, size_t n, cudaStream_t s);
+cudaError_t launchTransposeWeights(const __nv_bfloat16* w, __nv_bfloat16* wt, int Cout, int Cin, cudaStream_t s);
+// input channels [log1p(d / s), density, one-hot(material 0..5), 0 x 8] from arrays
+// (dose, dens, mat) or from a world (tally, vox, toDose)
+cudaError_t launchPrepareInput(const float* dose, const float* dens, const uint8_t* mat, const Tally* tally,
+    const uint32_t* vox, double toDose, size_t n, float invScale, __nv_bfloat16* out, cudaStream_t s);
+// patches outside their volume (or of a volume index out of range) are written as zeros
+cudaError_t launchGatherPatches(const __nv_bfloat16* const* inputs, const float* const* targets, const int* dims,
+    int nVolumes, const int* origins, int nPatch, int P, __nv_bfloat16* xin, float* tgt, cudaStream_t s);
+cudaError_t launchDoseMean(const Tally* tally, const uint32_t* vox, double toDose, size_t n, float rhoMin,
+    double* sum, unsigned long long* count, cudaStream_t s);
+
+// a world's dose through the network (denoiser.cpp); dims nx, ny, nz (x fastest)
+int denoiseWorld(dxmcg_denoiser* d, int device, const Tally* tally, const uint32_t* vox, int nx, int ny, int nz,
+    double toDose, double scale, double* hostOut, double* scaleUsed, cudaStream_t s);
+
+} // namespace nn
+} // namespace dxmcg

@@ -347,6 +347,104 @@ class Batch:
             pass
 
 
+class Denoiser:
+    """The dose denoiser (a 3D convolutional encoder-decoder run by the library's
+    kernels).  Tensors passed in and out are CUDA tensors (torch is used as the
+    device-memory container only): inputs bf16 [B, D, H, W, 16], targets and
+    predictions float32 [B, D, H, W]."""
+
+    def __init__(self, channels=(16, 32, 64, 128), seed=0):
+        cfg = N.DenoiserConfig()
+        cfg.levels = len(channels)
+        for k, c in enumerate(channels):
+            cfg.channels[k] = int(c)
+        cfg.seed = seed
+        h = C.c_void_p()
+        N.check(N.lib().dxmcg_denoiser_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.channels = tuple(int(c) for c in channels)
+        n = C.c_uint64(0)
+        N.check(N.lib().dxmcg_denoiser_param_count(self._h, C.byref(n)))
+        self.n_params = n.value
+
+    @staticmethod
+    def _stream(stream):
+        return C.c_void_p(stream.cuda_stream) if stream is not None else None
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        N.check(N.lib().dxmcg_denoiser_get_params(self._h, N.ptr(out, C.c_float)))
+        return out
+
+    def set_params(self, params) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters")
+        N.check(N.lib().dxmcg_denoiser_set_params(self._h, N.ptr(p, C.c_float)))
+
+    def grads(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        N.check(N.lib().dxmcg_denoiser_get_grads(self._h, N.ptr(out, C.c_float)))
+        return out
+
+    def forward(self, x, out=None, stream=None):
+        import torch
+
+        B, D, H, W, _ = x.shape
+        if out is None:
+            out = torch.empty((B, D, H, W), dtype=torch.float32, device=x.device)
+        N.check(N.lib().dxmcg_denoiser_forward(self._h, C.c_void_p(x.data_ptr()), B, D, H, W,
+                                               C.c_void_p(out.data_ptr()), self._stream(stream)))
+        return out
+
+    def backward(self, x, target, stream=None) -> float:
+        B, D, H, W, _ = x.shape
+        loss = C.c_double(0)
+        N.check(N.lib().dxmcg_denoiser_backward(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(target.data_ptr()),
+                                                B, D, H, W, C.byref(loss), self._stream(stream)))
+        return loss.value
+
+    def adam(self, lr: float, stream=None) -> None:
+        N.check(N.lib().dxmcg_denoiser_adam(self._h, C.c_float(lr), self._stream(stream)))
+
+    def train_step(self, x, target, lr: float, stream=None) -> float:
+        loss = self.backward(x, target, stream)
+        self.adam(lr, stream)
+        return loss
+
+    def denoise_world(self, world: "GpuWorld", scale: float = 0.0):
+        """(denoised dose in mGy per voxel, scale used)"""
+        out = np.zeros(world.N)
+        s = C.c_double(0)
+        N.check(N.lib().dxmcg_world_denoise(world._h, self._h, scale, N.ptr(out, C.c_double), C.byref(s)))
+        return out, s.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().dxmcg_denoiser_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def prepare_input(dose, density, material, scale: float, out=None, stream=None):
+    """The denoiser's 16 input channels from CUDA tensors (float32 dose and density,
+    uint8 material) of one volume [D, H, W]."""
+    import torch
+
+    n = dose.numel()
+    if out is None:
+        out = torch.empty((*dose.shape, 16), dtype=torch.bfloat16, device=dose.device)
+    N.check(N.lib().dxmcg_denoiser_prepare_input(C.c_void_p(dose.data_ptr()), C.c_void_p(density.data_ptr()),
+                                                 C.c_void_p(material.data_ptr()), n, scale,
+                                                 C.c_void_p(out.data_ptr()), Denoiser._stream(stream)))
+    return out
+
+
 def siddon_trace(origins, directions, dims, spacing, cap=4096):
     o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
     d = np.ascontiguousarray(directions, dtype=np.float32).reshape(-1, 3)

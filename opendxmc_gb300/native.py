@@ -33,6 +33,9 @@ EXPORTED = [
     "dxmcg_batch_run", "dxmcg_batch_destroy", "dxmcg_autotune", "dxmcg_transport_run_noalloc",
     "dxmcg_ct_segmentation_table", "dxmcg_ct_segment", "dxmcg_ct_segment_device", "dxmcg_organ_dose_table",
     "dxmcg_organ_dose_table_device", "dxmcg_world_organ_dose", "dxmcg_world_read_dose_postprocessed",
+    "dxmcg_denoiser_create", "dxmcg_denoiser_destroy", "dxmcg_denoiser_param_count", "dxmcg_denoiser_get_params",
+    "dxmcg_denoiser_set_params", "dxmcg_denoiser_get_grads", "dxmcg_denoiser_forward", "dxmcg_denoiser_backward",
+    "dxmcg_denoiser_adam", "dxmcg_denoiser_prepare_input", "dxmcg_denoiser_gather_patches", "dxmcg_world_denoise",
     "dxmcg_progress_create",
     "dxmcg_progress_destroy",
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_reset", "dxmcg_progress_continue",
@@ -61,6 +64,10 @@ class Segmentation(C.Structure):
 class OrganDose(C.Structure):
     _fields_ = [("n_voxels", C.c_uint64), ("volume_cm3", C.c_double), ("mass_g", C.c_double),
                 ("dose", C.c_double)]
+
+
+class DenoiserConfig(C.Structure):
+    _fields_ = [("levels", C.c_int32), ("channels", C.c_int32 * 5), ("seed", C.c_uint64)]
 
 
 class Material(C.Structure):
@@ -204,6 +211,18 @@ def lib() -> C.CDLL:
         "dxmcg_organ_dose_table_device": (i, [vp, vp, vp, u64, pd, i, C.POINTER(OrganDose), vp]),
         "dxmcg_world_organ_dose": (i, [vp, pu8, i, i, C.POINTER(OrganDose)]),
         "dxmcg_world_read_dose_postprocessed": (i, [vp, i, pd, pd, pd, C.POINTER(C.c_int)]),
+        "dxmcg_denoiser_create": (i, [C.POINTER(DenoiserConfig), C.POINTER(vp)]),
+        "dxmcg_denoiser_destroy": (None, [vp]),
+        "dxmcg_denoiser_param_count": (i, [vp, pu64]),
+        "dxmcg_denoiser_get_params": (i, [vp, pf]),
+        "dxmcg_denoiser_set_params": (i, [vp, pf]),
+        "dxmcg_denoiser_get_grads": (i, [vp, pf]),
+        "dxmcg_denoiser_forward": (i, [vp, vp, i, i, i, i, vp, vp]),
+        "dxmcg_denoiser_backward": (i, [vp, vp, vp, i, i, i, i, pd, vp]),
+        "dxmcg_denoiser_adam": (i, [vp, C.c_float, vp]),
+        "dxmcg_denoiser_prepare_input": (i, [vp, vp, vp, u64, d, vp, vp]),
+        "dxmcg_denoiser_gather_patches": (i, [vp, vp, vp, i, vp, i, i, vp, vp, vp]),
+        "dxmcg_world_denoise": (i, [vp, vp, d, pd, pd]),
         "dxmcg_progress_create": (vp, []),
         "dxmcg_progress_destroy": (None, [vp]),
         "dxmcg_progress_get": (None, [vp, pu64, pu64]),

@@ -1,0 +1,183 @@
+"""The denoiser's GPU kernels against the FP64 restatement (oracle/denoiser.py),
+which rounds to bfloat16 wherever the GPU stores bf16, so that what is left is the
+FP32-vs-FP64 accumulation order: forward predictions, every parameter gradient and
+the Adam update; plus the input preparation, patch gathering, training progress
+and the world-to-denoised-dose path, all through the C ABI."""
+import numpy as np
+import pytest
+
+from oracle import denoiser as OD
+from opendxmc_gb300 import phantoms as P
+
+pytestmark = pytest.mark.gpu
+
+CH = [16, 16, 32]  # three levels: D, H, W multiples of 4
+TOL = 1e-2         # relative L2 error allowed against the bf16-emulating FP64 oracle
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a, float) - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+def make_case(seed, B=2, D=16, H=8, W=12):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((B, D, H, W, 16))
+    x[..., 0] = np.log1p(rng.gamma(1.0, 1.0, (B, D, H, W)))
+    x[..., 1] = rng.uniform(0.0, 2.0, (B, D, H, W))
+    m = rng.integers(0, 6, (B, D, H, W))
+    for k in range(6):
+        x[..., 2 + k] = m == k
+    x = OD.round_bf16(x)
+    t = rng.gamma(2.0, 0.5, (B, D, H, W)).astype(np.float32).astype(np.float64)
+    return x, t
+
+
+@pytest.fixture(scope="module")
+def case(gpu, torch):
+    net = OD.UNet(CH, in_channels=16, seed=5)
+    net.params = net.params.astype(np.float32).astype(np.float64)  # the GPU's FP32 master copy
+    dn = gpu.Denoiser(CH, seed=1)
+    dn.set_params(net.params)
+    x, t = make_case(7)
+    xt = torch.tensor(x, dtype=torch.bfloat16, device="cuda")
+    tt = torch.tensor(t, dtype=torch.float32, device="cuda")
+    return net, dn, x, t, xt, tt
+
+
+def test_forward_matches_oracle(case):
+    net, dn, x, t, xt, tt = case
+    got = dn.forward(xt).cpu().numpy()
+    ref, _ = net.forward(x, bf16=True)
+    assert got.shape == ref.shape
+    assert rel(got, ref) < TOL
+
+
+def test_gradients_match_oracle(case):
+    net, dn, x, t, xt, tt = case
+    loss = dn.backward(xt, tt)
+    g = dn.grads()
+    ref_loss, gref, _ = net.gradient(x, t, bf16=True)
+    assert abs(loss / ref_loss - 1) < 1e-4
+    for name, (w0, w1, b1, ci, co) in net.offsets.items():
+        assert rel(g[w0:w1], gref[w0:w1]) < TOL, name
+        assert rel(g[w1:b1], gref[w1:b1]) < TOL, name + " bias"
+    h0, h1, h2 = net.head
+    assert rel(g[h0:h2], gref[h0:h2]) < TOL
+
+
+def test_adam_step_matches_oracle(gpu, torch):
+    x, t = make_case(11, B=1, D=8, H=8, W=8)
+    dn = gpu.Denoiser(CH, seed=2)
+    p0 = dn.get_params().astype(np.float64)
+    dn.backward(torch.tensor(x, dtype=torch.bfloat16, device="cuda"),
+                torch.tensor(t, dtype=torch.float32, device="cuda"))
+    g = dn.grads().astype(np.float64)
+    dn.adam(1e-3)
+    got = dn.get_params()
+    ref = OD.adam_step(p0.copy(), g, np.zeros_like(g), np.zeros_like(g), 1, 1e-3)
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-8)
+
+
+def test_training_lowers_the_loss(gpu, torch):
+    """Overfit one batch of a smoothing task: the loss must fall to well under half."""
+    rng = np.random.default_rng(3)
+    B, D = 4, 16
+    z, y, xx = np.meshgrid(*[np.linspace(-1, 1, D)] * 3, indexing="ij")
+    f = np.stack([np.exp(-((z - rng.uniform(-.5, .5)) ** 2 + (y - rng.uniform(-.5, .5)) ** 2 + xx ** 2) * 3)
+                  for _ in range(B)])
+    x = np.zeros((B, D, D, D, 16))
+    x[..., 0] = np.log1p(np.maximum(f + rng.normal(0, 0.2, f.shape), 0))
+    x[..., 1] = 1.0
+    x[..., 5] = 1.0
+    xt = torch.tensor(x, dtype=torch.bfloat16, device="cuda")
+    tt = torch.tensor(f, dtype=torch.float32, device="cuda")
+    dn = gpu.Denoiser(CH, seed=4)
+    losses = [dn.train_step(xt, tt, 2e-3) for _ in range(80)]
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.5 * losses[0]
+
+
+def test_prepare_input(gpu, torch):
+    rng = np.random.default_rng(5)
+    n = (10, 12, 14)
+    dose = rng.gamma(1.0, 2.0, n).astype(np.float32)
+    dose.flat[:5] = [0.0, -1.0, 1e-30, 3.0e4, 7.5]
+    dens = rng.uniform(0, 2, n).astype(np.float32)
+    mat = rng.integers(0, 8, n).astype(np.uint8)  # 6 and 7 have no channel
+    out = gpu.prepare_input(torch.tensor(dose, device="cuda"), torch.tensor(dens, device="cuda"),
+                            torch.tensor(mat, device="cuda"), 2.5).float().cpu().numpy()
+    assert out.shape == (*n, 16)
+    ref0 = OD.round_bf16(np.log1p(np.maximum(dose, 0).astype(np.float64) / 2.5))
+    np.testing.assert_allclose(out[..., 0], ref0, rtol=8e-3, atol=0)  # log1pf: within one bf16 step
+    np.testing.assert_array_equal(out[..., 1], OD.round_bf16(dens))
+    for k in range(6):
+        np.testing.assert_array_equal(out[..., 2 + k], (mat == k).astype(np.float64))
+    assert not out[..., 8:].any()
+
+
+def test_gather_patches(gpu, torch):
+    import ctypes as C
+
+    from opendxmc_gb300 import native as N
+
+    rng = np.random.default_rng(8)
+    dims = [(10, 9, 8), (6, 7, 12)]
+    vols = [torch.tensor(rng.normal(size=(*d, 16)), dtype=torch.bfloat16, device="cuda") for d in dims]
+    tgts = [torch.tensor(rng.normal(size=d), dtype=torch.float32, device="cuda") for d in dims]
+    ptr_in = torch.tensor([v.data_ptr() for v in vols], dtype=torch.int64, device="cuda")
+    ptr_t = torch.tensor([v.data_ptr() for v in tgts], dtype=torch.int64, device="cuda")
+    dd = torch.tensor(np.array(dims).ravel(), dtype=torch.int32, device="cuda")
+    P_ = 4
+    origins = [(0, 0, 0, 0), (1, 2, 3, 8), (0, 6, 5, 4), (1, 4, 4, 10), (5, 0, 0, 0)]  # the last two: partly / fully out
+    org = torch.tensor(np.array(origins).ravel(), dtype=torch.int32, device="cuda")
+    xb = torch.empty((len(origins), P_, P_, P_, 16), dtype=torch.bfloat16, device="cuda")
+    tb = torch.empty((len(origins), P_, P_, P_), dtype=torch.float32, device="cuda")
+    N.check(N.lib().dxmcg_denoiser_gather_patches(C.c_void_p(ptr_in.data_ptr()), C.c_void_p(ptr_t.data_ptr()),
+                                                  C.c_void_p(dd.data_ptr()), len(dims), C.c_void_p(org.data_ptr()),
+                                                  len(origins), P_, C.c_void_p(xb.data_ptr()),
+                                                  C.c_void_p(tb.data_ptr()), None))
+    torch.cuda.synchronize()
+    xs = xb.float().cpu().numpy()
+    ts = tb.cpu().numpy()
+    for k, (v, z, y, x) in enumerate(origins):
+        ref_x = np.zeros((P_, P_, P_, 16))
+        ref_t = np.zeros((P_, P_, P_))
+        if v < len(dims):
+            src = vols[v].float().cpu().numpy()
+            st = tgts[v].cpu().numpy()
+            D, H, W = dims[v]
+            for a in range(P_):
+                for b in range(P_):
+                    for c in range(P_):
+                        if z + a < D and y + b < H and x + c < W:
+                            ref_x[a, b, c] = src[z + a, y + b, x + c]
+                            ref_t[a, b, c] = st[z + a, y + b, x + c]
+        np.testing.assert_array_equal(xs[k], ref_x)
+        np.testing.assert_array_equal(ts[k], ref_t)
+
+
+def test_world_denoise_path(gpu, torch):
+    ph = P.ellipsoid_phantom((32, 28, 24), (0.4, 0.4, 0.4), seed=6)
+    w = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials, 1)
+    w.set_data(ph.density, ph.material)
+    w.build()
+    w.run(P.dx_beam_params(kvp=90.0, field_cm=12.0, particles=20_000, exposures=10), gpu.run_options(seed=9))
+    dn = gpu.Denoiser(CH, seed=3)
+    out, scale = dn.denoise_world(w)
+    d, _, _ = w.dose()
+    rho, mat = w.packed_density()
+    sel = rho > 0.2
+    assert abs(scale / d[sel].mean() - 1) < 1e-9
+    # the same through the array path: prepare_input + forward, times the scale
+    shape = (ph.dims[2], ph.dims[1], ph.dims[0])
+    xin = gpu.prepare_input(torch.tensor(d.reshape(shape), dtype=torch.float32, device="cuda"),
+                            torch.tensor(rho.reshape(shape), device="cuda"),
+                            torch.tensor(mat.reshape(shape), device="cuda"), scale)
+    pred = dn.forward(xin[None]).cpu().numpy().ravel()
+    assert np.isfinite(out).all()
+    np.testing.assert_allclose(out, pred.astype(np.float64) * scale, rtol=2e-2, atol=1e-3 * np.abs(out).max())

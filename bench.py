@@ -59,9 +59,13 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--tracking", choices=list(TRACKING), default="woodcock")
     p.add_argument("--macro-cell", type=int, default=16, help="macro-cell edge in voxels (macro tracking)")
-    p.add_argument("--workload", choices=["torso", "batch", "pipelines"], default="torso",
+    p.add_argument("--small", action="store_true", help="denoise-experiment: a small quick configuration")
+    p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
+    p.add_argument("--workload", choices=["torso", "batch", "pipelines", "denoiser", "denoise-experiment"],
+                   default="torso",
                    help="torso: the spiral-CT torso job; batch: 64 uneven DX/CBCT jobs in one persistent launch; "
-                        "pipelines: segmentation and organ dose table passes")
+                        "pipelines: segmentation and organ dose table passes; denoiser: training step and "
+                        "inference throughput")
     return p.parse_args()
 
 
@@ -472,7 +476,7 @@ def run_pipelines(args):
     dims = (512, 512, 400)
     n = int(np.prod(dims))
     rng = np.random.default_rng(1)
-    hu = rng.uniform(-1100.0, 2000.0, n)
+    hu = np.rint(rng.uniform(-1024.0, 2000.0, n))  # CT numbers are integers
     table = G.ct_segmentation_table(120.0, 2.5, 0.0)
     d_hu = torch.from_numpy(hu).cuda()
     d_mat = torch.empty(n, dtype=torch.uint8, device="cuda")
@@ -527,13 +531,93 @@ def run_pipelines(args):
     line = {
         "metric": "voxels/s", "value": n / (seg_ms * 1e-3), "unit": "voxels/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "per-voxel passes on a 512x512x400 volume (104,857,600 voxels)",
+        "config": {"workload": "per-voxel passes on a 512x512x400 volume (104,857,600 voxels, integer CT "
+                               "numbers uniform in [-1024, 2000])",
                    "l2": "256 MB buffer written before every launch; inputs 0.8-1.8 GB > L2"},
         "peak_gbs": hbm, "peak_source": peak_kind,
         "segmentation": row(17, seg_ms, seg_e2e),
         "organ_dose_table": row(17, org_ms, org_e2e),
     }
     print(json.dumps(line), flush=True)
+
+
+def run_denoiser(args):
+    """Throughput of the denoiser kernels: one training step (batch 8 of 64^3
+    patches, channels 16/32/64/128: forward, L1 loss, input and weight gradients,
+    Adam) and one forward pass over a 512x512x400 volume; conv FLOPs / CUDA-event
+    time against the measured bf16 tensor peak."""
+    import torch
+
+    from opendxmc_gb300 import build as B
+    from opendxmc_gb300 import denoise as DN
+
+    if not B.LIB.exists():
+        B.build(verbose_ptxas=False)
+    from opendxmc_gb300 import engine as G
+
+    G.set_device(0)
+    torch.cuda.set_device(0)
+    ch = (16, 32, 64, 128)
+    net = G.Denoiser(ch, seed=0)
+    fwd_per_vox, train_per_vox = DN.conv_flops(ch)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.rand((8, 64, 64, 64, 16), device="cuda", generator=gen).to(torch.bfloat16)
+    t = torch.rand((8, 64, 64, 64), device="cuda", generator=gen)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        ms = []
+        for r in range(args.warmup + reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            if r >= args.warmup:
+                ms.append(a.elapsed_time(b))
+        return statistics.median(ms)
+
+    step_ms = timed(lambda: (net.backward(x, t, stream), net.adam(1e-4, stream)), max(args.steps, 5))
+    vol = torch.rand((1, 400, 512, 512, 16), device="cuda", generator=gen).to(torch.bfloat16)
+    out = torch.empty((1, 400, 512, 512), dtype=torch.float32, device="cuda")
+    inf_ms = timed(lambda: net.forward(vol, out, stream), max(2, args.steps // 2))
+    peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
+    step_tf = train_per_vox * 8 * 64 ** 3 / (step_ms * 1e-3) / 1e12
+    inf_tf = fwd_per_vox * 512 * 512 * 400 / (inf_ms * 1e-3) / 1e12
+    print(json.dumps({
+        "metric": "denoiser training step", "value": step_ms, "unit": "ms", "higher_is_better": False, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": "3D conv encoder-decoder 16/32/64/128, batch 8 x 64^3 patches; inference 512x512x400"},
+        "train_step_ms": step_ms, "train_tflops": step_tf, "train_frac": step_tf / peak,
+        "inference_ms_512x512x400": inf_ms, "inference_tflops": inf_tf, "inference_frac": inf_tf / peak,
+        "peak_bf16_tflops": peak, "params": net.n_params,
+    }), flush=True)
+
+
+def run_denoise_experiment(args):
+    """Seconds to 2 % dose error, plain Monte Carlo vs a short run plus the denoiser,
+    on the 512x512x400 spiral-CT torso (trains the network first: a few minutes)."""
+    import numpy as np
+    import torch
+
+    from opendxmc_gb300 import build as B
+    from opendxmc_gb300 import denoise as DN
+
+    if not B.LIB.exists():
+        B.build(verbose_ptxas=False)
+    from opendxmc_gb300 import engine as G
+
+    G.set_device(0)
+    torch.cuda.set_device(0)
+    kw = {}
+    if args.small:
+        kw = dict(dims=(128, 128, 96), spacing=(0.32, 0.32, 0.4), train_seeds=(11, 12), lows=(1e6, 1e7), high=1e8,
+                  steps=60)
+    out, net = DN.experiment(torch, log=lambda m: print(m, file=sys.stderr, flush=True), **kw)
+    if args.save_weights:
+        np.save(args.save_weights, net.get_params())
+    print(json.dumps({"metric": "s to <=2% RMS dose error (plain MC / MC + denoiser)", **out}), flush=True)
 
 
 def main():
@@ -544,6 +628,10 @@ def main():
         run_batch(args)
     elif args.workload == "pipelines":
         run_pipelines(args)
+    elif args.workload == "denoiser":
+        run_denoiser(args)
+    elif args.workload == "denoise-experiment":
+        run_denoise_experiment(args)
     else:
         run_ours(args)
 

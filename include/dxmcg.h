@@ -372,8 +372,9 @@ DXMCG_API int dxmcg_denoiser_prepare_input(const float* dose, const float* densi
 DXMCG_API int dxmcg_denoiser_gather_patches(const void* const* inputs, const float* const* targets,
     const int32_t* dims, int n_volumes, const int32_t* origins, int n_patch, int P, void* input_batch,
     float* target_batch, void* cuda_stream);
-/* A world's dose, denoised: input from its tally and voxels, scale = the mean dose
- * of voxels denser than 0.2 g/cm3 (or `scale` when > 0), dose_out (host, N, mGy as
+/* A world's dose, denoised: input from its tally and voxels (air, material 0, enters
+ * with zero dose as the worker's readout deletes it), scale = the mean dose of voxels
+ * denser than 0.2 g/cm3 (or `scale` when > 0), dose_out (host, N, mGy as
  * dxmcg_world_read_dose; may be NULL) and *scale_used (may be NULL). */
 DXMCG_API int dxmcg_world_denoise(dxmcg_world* w, dxmcg_denoiser* d, double scale, double* dose_out,
     double* scale_used);

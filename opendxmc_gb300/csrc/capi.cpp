@@ -327,6 +327,18 @@ struct dxmcg_batch {
     }
 };
 
+// the segmentation kernel's per-voxel arithmetic, on the host (no contraction into
+// fused multiply-adds: the library's host code is compiled with -ffp-contract=off)
+void dxmcg::segmentHost(double h, const SegTable& t, uint8_t& m, double& d)
+{
+    int i = 0;
+    while (i < t.nSep && !(h < t.sep[i]))
+        ++i;
+    m = static_cast<uint8_t>(i);
+    const double v = ((t.slope * h) / 1000.0 + t.offset) / t.att[i];
+    d = v < 0.0 ? 0.0 : v;
+}
+
 // helpers of the segmentation, organ dose table and readout entry points
 namespace {
 constexpr uint64_t kStreamChunk = 1ull << 25; // voxels per host<->device round trip
@@ -353,6 +365,47 @@ dxmcg_material dryAirMaterial()
     m.Z[2] = 18;
     m.w[2] = 1.3;
     return m;
+}
+
+bool sameTable(const SegTable& a, const SegTable& b)
+{
+    return a.nSep == b.nSep && a.slope == b.slope && a.offset == b.offset
+        && std::memcmp(a.sep, b.sep, sizeof(double) * a.nSep) == 0
+        && std::memcmp(a.att, b.att, sizeof(double) * (a.nSep + 1)) == 0;
+}
+
+// The integer-CT-number lookup table of a segmentation table on the current device,
+// kept per thread until the table changes.
+struct SegLut {
+    int device = -1;
+    SegTable key {};
+    DeviceBuffer<double> d;
+    DeviceBuffer<uint8_t> m;
+};
+int segLut(const SegTable& t, const double*& lutD, const uint8_t*& lutM)
+{
+    thread_local SegLut cache;
+    int dev = 0;
+    DXMCG_CUDA(cudaGetDevice(&dev));
+    if (cache.device != dev || !sameTable(cache.key, t)) {
+        std::vector<double> hd(kSegLutSize);
+        std::vector<uint8_t> hm(kSegLutSize);
+        for (int k = 0; k < kSegLutSize; ++k)
+            segmentHost(static_cast<double>(kSegLutMin + k), t, hm[k], hd[k]);
+        if (cache.device != dev) {
+            cache.d.reset();
+            cache.m.reset();
+        }
+        DXMCG_CUDA(cache.d.alloc(kSegLutSize));
+        DXMCG_CUDA(cache.m.alloc(kSegLutSize));
+        DXMCG_CUDA(cudaMemcpy(cache.d.p, hd.data(), kSegLutSize * sizeof(double), cudaMemcpyHostToDevice));
+        DXMCG_CUDA(cudaMemcpy(cache.m.p, hm.data(), kSegLutSize, cudaMemcpyHostToDevice));
+        cache.device = dev;
+        cache.key = t;
+    }
+    lutD = cache.d.p;
+    lutM = cache.m.p;
+    return DXMCG_OK;
 }
 
 int toSegTable(const dxmcg_segmentation* t, SegTable& s)
@@ -1130,7 +1183,12 @@ DXMCG_API int dxmcg_ct_segment_device(const dxmcg_segmentation* table, const dou
         return DXMCG_OK;
     if (!hu || !material || !density)
         return fail(DXMCG_ERR_ARGUMENT, "ct_segment_device: null array");
-    const cudaError_t e = launchSegment(hu, n, t, material, density, static_cast<cudaStream_t>(cuda_stream));
+    const double* lutD = nullptr;
+    const uint8_t* lutM = nullptr;
+    if ((rc = segLut(t, lutD, lutM)) != DXMCG_OK)
+        return rc;
+    const cudaError_t e
+        = launchSegment(hu, n, t, lutD, lutM, material, density, static_cast<cudaStream_t>(cuda_stream));
     if (e != cudaSuccess)
         return cudaFail(e, "segmentation kernel launch");
     return DXMCG_OK;
@@ -1149,6 +1207,10 @@ DXMCG_API int dxmcg_ct_segment(const dxmcg_segmentation* table, const double* hu
         return fail(DXMCG_ERR_ARGUMENT, "ct_segment: null array");
     if ((rc = currentDevice()) != DXMCG_OK)
         return rc;
+    const double* lutD = nullptr;
+    const uint8_t* lutM = nullptr;
+    if ((rc = segLut(t, lutD, lutM)) != DXMCG_OK)
+        return rc;
     const size_t chunk = std::min<uint64_t>(n, kStreamChunk);
     DeviceBuffer<double> dh, dd;
     DeviceBuffer<uint8_t> dm;
@@ -1158,7 +1220,7 @@ DXMCG_API int dxmcg_ct_segment(const dxmcg_segmentation* table, const double* hu
     for (uint64_t a = 0; a < n; a += chunk) {
         const size_t m = std::min<uint64_t>(chunk, n - a);
         DXMCG_CUDA(cudaMemcpy(dh.p, hu + a, m * sizeof(double), cudaMemcpyHostToDevice));
-        const cudaError_t e = launchSegment(dh.p, m, t, dm.p, dd.p, nullptr);
+        const cudaError_t e = launchSegment(dh.p, m, t, lutD, lutM, dm.p, dd.p, nullptr);
         if (e != cudaSuccess)
             return cudaFail(e, "segmentation kernel launch");
         DXMCG_CUDA(cudaMemcpy(material + a, dm.p, m, cudaMemcpyDeviceToHost));

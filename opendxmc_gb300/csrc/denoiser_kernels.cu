@@ -599,7 +599,8 @@ namespace {
                 const uint32_t w = vox[i];
                 rho = __uint_as_float(w & 0xffffff00u);
                 m = static_cast<int>(w & 0xffu);
-                d = rho > 0.0f ? static_cast<float>(tally[i].e * (toDose / rho)) : 0.0f;
+                // air (material 0) enters with zero dose, as the worker's readout deletes it
+                d = rho > 0.0f && m != 0 ? static_cast<float>(tally[i].e * (toDose / rho)) : 0.0f;
             } else {
                 d = dose[i];
                 rho = dens[i];

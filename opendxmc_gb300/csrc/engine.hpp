@@ -165,8 +165,13 @@ struct SegTable {
     double sep[kMaxSegMaterials - 1] {}; // HU midpoints between consecutive materials
     double att[kMaxSegMaterials] {};     // spectrum-weighted mass attenuation per material
 };
-cudaError_t launchSegment(const double* hu, size_t n, const SegTable& t, uint8_t* mat, double* dens,
-    cudaStream_t s);
+// lookup table for integer CT numbers [kSegLutMin, kSegLutMin + kSegLutSize): density
+// and material of each, computed on the host with the kernel's FP64 operations
+constexpr int kSegLutMin = -1024;
+constexpr int kSegLutSize = 4096;
+void segmentHost(double h, const SegTable& t, uint8_t& m, double& d);
+cudaError_t launchSegment(const double* hu, size_t n, const SegTable& t, const double* lutD, const uint8_t* lutM,
+    uint8_t* mat, double* dens, cudaStream_t s);
 cudaError_t launchOrganTable(const uint8_t* organ, const double* dose, const double* density, size_t n,
     double voxel_volume, int n_organs, unsigned long long* cnt, double* sum_rho, double* sum_e, cudaStream_t s);
 cudaError_t launchWorldOrganTable(const uint8_t* organ, const Tally* tally, const uint32_t* vox, size_t n,

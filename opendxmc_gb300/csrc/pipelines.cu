@@ -21,8 +21,20 @@ namespace {
     using namespace dev;
 
     // ---------------------------------------------------------------- segmentation
-    __device__ __forceinline__ void segmentOne(double h, const SegTable& t, uint8_t& m, double& d)
+    // Integer CT numbers in [kSegLutMin, kSegLutMin + kSegLutSize) read their result
+    // from a table filled once per segmentation table with the same FP64 operations
+    // (on GB300 the two FP64 divisions per voxel would otherwise bound the pass);
+    // any other value is computed here.
+    __device__ __forceinline__ void segmentOne(double h, const SegTable& t, const double* __restrict__ lutD,
+        const uint8_t* __restrict__ lutM, uint8_t& m, double& d)
     {
+        if (lutD && h == rint(h) && h >= static_cast<double>(kSegLutMin)
+            && h < static_cast<double>(kSegLutMin + kSegLutSize)) {
+            const int k = static_cast<int>(h) - kSegLutMin;
+            m = __ldg(lutM + k);
+            d = __ldg(lutD + k);
+            return;
+        }
         int i = 0;
         while (i < t.nSep && !(h < t.sep[i]))
             ++i;
@@ -35,7 +47,8 @@ namespace {
     // Four voxels per thread and iteration: 32 B of HU in, 4 B of material and 32 B of
     // density out with 16-byte / 4-byte vector accesses (the host checks alignment).
     __global__ void segmentKernel(const double* __restrict__ hu, size_t n, const SegTable t,
-        uint8_t* __restrict__ mat, double* __restrict__ dens, int vec)
+        const double* __restrict__ lutD, const uint8_t* __restrict__ lutM, uint8_t* __restrict__ mat,
+        double* __restrict__ dens, int vec)
     {
         const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
         const size_t nq = n / 4;
@@ -46,10 +59,10 @@ namespace {
                 const double2 b = reinterpret_cast<const double2*>(hu)[2 * q + 1];
                 uchar4 m;
                 double2 da, db;
-                segmentOne(a.x, t, m.x, da.x);
-                segmentOne(a.y, t, m.y, da.y);
-                segmentOne(b.x, t, m.z, db.x);
-                segmentOne(b.y, t, m.w, db.y);
+                segmentOne(a.x, t, lutD, lutM, m.x, da.x);
+                segmentOne(a.y, t, lutD, lutM, m.y, da.y);
+                segmentOne(b.x, t, lutD, lutM, m.z, db.x);
+                segmentOne(b.y, t, lutD, lutM, m.w, db.y);
                 reinterpret_cast<uchar4*>(mat)[q] = m;
                 reinterpret_cast<double2*>(dens)[2 * q] = da;
                 reinterpret_cast<double2*>(dens)[2 * q + 1] = db;
@@ -57,7 +70,7 @@ namespace {
             q = 4 * nq + blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; // the tail
         }
         for (; q < n; q += stride)
-            segmentOne(hu[q], t, mat[q], dens[q]);
+            segmentOne(hu[q], t, lutD, lutM, mat[q], dens[q]);
     }
 
     // ---------------------------------------------------------------- organ dose table
@@ -205,12 +218,12 @@ namespace {
     }
 } // namespace
 
-cudaError_t launchSegment(const double* hu, size_t n, const SegTable& t, uint8_t* mat, double* dens,
-    cudaStream_t s)
+cudaError_t launchSegment(const double* hu, size_t n, const SegTable& t, const double* lutD, const uint8_t* lutM,
+    uint8_t* mat, double* dens, cudaStream_t s)
 {
     const bool vec = (reinterpret_cast<uintptr_t>(hu) % 16 == 0) && (reinterpret_cast<uintptr_t>(dens) % 16 == 0)
         && (reinterpret_cast<uintptr_t>(mat) % 4 == 0);
-    segmentKernel<<<streamingGrid(vec ? n / 4 : n), 256, 0, s>>>(hu, n, t, mat, dens, vec ? 1 : 0);
+    segmentKernel<<<streamingGrid(vec ? n / 4 : n), 256, 0, s>>>(hu, n, t, lutD, lutM, mat, dens, vec ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,274 @@
+"""Training data, training loop and evaluation of the dose denoiser.
+
+The data come from the GPU transport itself: for each seeded phantom a short run
+(the network's input) and a long run (its target) of the same beam with
+independent random streams.  Inputs are normalised by the short run's mean dose
+over voxels denser than 0.2 g/cm3; targets are the long run's dose over the same
+scale.  Everything stays in device memory (CUDA tensors; torch is the container),
+and every operation on it is a library kernel: transport, input preparation, patch
+gathering, forward, backward, Adam.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import engine as G
+from . import native as N
+
+
+def conv_flops(channels, in_channels=16):
+    """Multiply-add FLOPs per output voxel of level 0 for one forward pass, and the
+    same for one training step (forward + input gradients + weight gradients)."""
+    L = len(channels)
+    fwd = 0.0
+    dgrad = 0.0
+    prev = in_channels
+    for l, c in enumerate(channels):
+        scale = 1.0 / 8 ** l
+        for k, (ci, co) in enumerate([(prev, c), (c, c)]):
+            f = 2 * 27 * ci * co * scale
+            fwd += f
+            if not (l == 0 and k == 0):
+                dgrad += f
+        prev = c
+    for l in range(L - 2, -1, -1):
+        scale = 1.0 / 8 ** l
+        for ci, co in [(channels[l + 1] + channels[l], channels[l]), (channels[l], channels[l])]:
+            f = 2 * 27 * ci * co * scale
+            fwd += f
+            dgrad += f
+    return fwd, 2 * fwd + dgrad  # training: forward + weight gradients (= forward) + input gradients
+
+
+@dataclass
+class Pair:
+    """One training volume on the device."""
+    input: object   # bf16 [D, H, W, 16]
+    target: object  # float32 [D, H, W]
+    scale: float
+    dims: tuple     # (D, H, W)
+
+
+def dose_pair(world: "G.GpuWorld", beam: dict, low: int, high: int, seed: int, stream_base: int = 0):
+    """(low-history dose, high-history dose) of one beam on one world, mGy per voxel
+    (host arrays); the two runs use independent Philox streams."""
+    def run(n, stream):
+        b = dict(beam)
+        world.clear()
+        ppe = max(1, int(round(n / _exposures(b))))
+        b["particles_per_exposure"] = ppe
+        world.run(b, G.run_options(seed=seed, stream=stream))
+        return world.dose()[0]
+
+    d_low = run(low, stream_base)
+    d_high = run(high, stream_base + 1)
+    return d_low, d_high
+
+
+def _exposures(beam: dict) -> int:
+    return len(G.beam_exposures(dict(beam, particles_per_exposure=1)))
+
+
+def make_pair(torch, world: "G.GpuWorld", dims_zyx, d_low, d_high, rho, mat) -> Pair:
+    sel = rho > 0.2
+    scale = float(d_low[sel].mean()) if sel.any() and d_low[sel].mean() > 0 else float(d_low.mean() or 1.0)
+    dev = "cuda"
+    x = G.prepare_input(torch.tensor(d_low.reshape(dims_zyx), dtype=torch.float32, device=dev),
+                        torch.tensor(rho.reshape(dims_zyx), dtype=torch.float32, device=dev),
+                        torch.tensor(mat.reshape(dims_zyx), dtype=torch.uint8, device=dev), scale)
+    t = torch.tensor((d_high / scale).reshape(dims_zyx), dtype=torch.float32, device=dev)
+    return Pair(x, t, scale, tuple(dims_zyx))
+
+
+class PatchSampler:
+    """Random patch origins over a list of Pairs; gathers batches on the device.
+    With `centers` (per pair, an array of (z, y, x) voxels) a fraction `focus` of the
+    patches is centred on one of them (e.g. the body), the rest anywhere."""
+
+    def __init__(self, torch, pairs: list[Pair], patch: int, batch: int, seed: int = 0, centers=None,
+                 focus: float = 0.9):
+        self.torch = torch
+        self.pairs = pairs
+        self.P = patch
+        self.B = batch
+        self.rng = np.random.default_rng(seed)
+        self.centers = centers
+        self.focus = focus
+        dev = "cuda"
+        self.ptr_in = torch.tensor([p.input.data_ptr() for p in pairs], dtype=torch.int64, device=dev)
+        self.ptr_t = torch.tensor([p.target.data_ptr() for p in pairs], dtype=torch.int64, device=dev)
+        self.dims = torch.tensor(np.array([p.dims for p in pairs]).ravel(), dtype=torch.int32, device=dev)
+        self.xb = torch.empty((batch, patch, patch, patch, 16), dtype=torch.bfloat16, device=dev)
+        self.tb = torch.empty((batch, patch, patch, patch), dtype=torch.float32, device=dev)
+
+    def sample(self):
+        org = np.zeros((self.B, 4), dtype=np.int32)
+        for k in range(self.B):
+            v = int(self.rng.integers(len(self.pairs)))
+            D, H, W = self.pairs[v].dims
+            if self.centers is not None and len(self.centers[v]) and self.rng.random() < self.focus:
+                c = self.centers[v][self.rng.integers(len(self.centers[v]))]
+                h = self.P // 2
+                org[k] = (v, min(max(c[0] - h, 0), D - self.P), min(max(c[1] - h, 0), H - self.P),
+                          min(max(c[2] - h, 0), W - self.P))
+            else:
+                org[k] = (v, self.rng.integers(0, D - self.P + 1), self.rng.integers(0, H - self.P + 1),
+                          self.rng.integers(0, W - self.P + 1))
+        o = self.torch.tensor(org.ravel(), dtype=self.torch.int32, device="cuda")
+        N.check(N.lib().dxmcg_denoiser_gather_patches(C.c_void_p(self.ptr_in.data_ptr()),
+                                                      C.c_void_p(self.ptr_t.data_ptr()),
+                                                      C.c_void_p(self.dims.data_ptr()), len(self.pairs),
+                                                      C.c_void_p(o.data_ptr()), self.B, self.P,
+                                                      C.c_void_p(self.xb.data_ptr()), C.c_void_p(self.tb.data_ptr()),
+                                                      None))
+        return self.xb, self.tb
+
+
+def train(net: "G.Denoiser", sampler: PatchSampler, steps: int, lr: float = 1e-3, log_every: int = 0,
+          lr_final: float | None = None, log=print):
+    """Adam on random patches; returns the loss history.  With lr_final the rate
+    decays geometrically from lr to lr_final."""
+    losses = []
+    for s in range(steps):
+        rate = lr if lr_final is None else lr * (lr_final / lr) ** (s / max(1, steps - 1))
+        x, t = sampler.sample()
+        losses.append(net.train_step(x, t, rate))
+        if log_every and (s + 1) % log_every == 0:
+            log(f"step {s + 1}: loss {np.mean(losses[-log_every:]):.4f}")
+    return losses
+
+
+def relative_errors(estimate, reference, reference2=None, threshold=0.1, mask=None):
+    """Errors over voxels whose reference dose exceeds `threshold` x its maximum:
+    mean |e - r| / r against the reference, and, with a second independent
+    reference, the RMS relative error with the references' own noise removed:
+    E[(e - r1)(e - r2)] = E[(e - truth)^2] when r1 and r2 are independent of e and
+    of each other."""
+    ref = reference if reference2 is None else 0.5 * (reference + reference2)
+    cand = ref if mask is None else np.where(mask, ref, 0.0)
+    sel = cand > threshold * cand.max()
+    e = estimate[sel]
+    out = {"voxels": int(sel.sum()), "mean_rel": float(np.mean(np.abs(e - ref[sel]) / ref[sel]))}
+    if reference2 is not None:
+        r1 = reference[sel]
+        r2 = reference2[sel]
+        cross = (e - r1) * (e - r2) / (ref[sel] ** 2)
+        out["rms_rel_unbiased"] = float(np.sqrt(max(np.mean(cross), 0.0)))
+        # the references' own RMS relative noise: E[(r1 - r2)^2] / 2
+        out["reference_rms_rel"] = float(np.sqrt(np.mean((r1 - r2) ** 2 / (ref[sel] ** 2)) / 2))
+    return out
+
+
+# ---------------------------------------------------------------- the spiral-CT experiment
+def spiral_beam(histories: float, pitch=0.8, collimation_cm=8.0, scan_cm=20.0, kvp=120.0, al_mm=6.0) -> dict:
+    from . import phantoms as P
+
+    b = P.ct_spiral_params(kvp=kvp, al_mm=al_mm, pitch=pitch, collimation_cm=collimation_cm, scan_cm=scan_cm,
+                           particles=1)
+    n_exp = _exposures(b)
+    b["particles_per_exposure"] = max(1, int(np.ceil(histories / n_exp)))
+    return b
+
+
+def run_dose(world, beam, seed, stream, air):
+    """One transport run from a cleared tally: (dose with air zeroed, stats)."""
+    world.clear()
+    st = world.run(beam, G.run_options(seed=seed, stream=stream))
+    d = world.dose()[0]
+    d[air] = 0.0
+    return d, st
+
+
+def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_seeds=(11, 12, 13, 14, 15, 16),
+               eval_seed=99, lows=(1e8, 3e8, 1e9), high=1e10, steps=6000, batch=8, patch=64, lr=1e-3,
+               lr_final=1e-4, channels=(16, 32, 64, 128), target_error=0.02, log=print):
+    """Train the denoiser on torso phantoms (inputs: runs of each history count in
+    `lows`; target: a `high`-history run), then, on a held-out torso, compare the
+    time to `target_error` of plain Monte Carlo with that of a short run plus
+    denoising, for each input history count.  Error: RMS relative error over
+    non-air voxels above 10 % of the maximum dose, made unbiased by two independent
+    `high`-history references; plain Monte Carlo's error at N histories is one
+    reference's own noise scaled by sqrt(high / N)."""
+    from . import phantoms as P
+
+    nx, ny, nz = dims
+    beam_high = spiral_beam(high)
+    world = G.GpuWorld(dims, spacing, [c for _, c, _ in P.SIX_MATERIALS])
+    pairs, centers = [], []
+    t0 = time.perf_counter()
+    mc_s = 0.0
+    for s in train_seeds:
+        ph = P.torso_phantom(dims=dims, spacing=spacing, seed=s)
+        world.set_data(ph.density, ph.material)
+        world.build()
+        rho, mat = world.packed_density()
+        air = mat == 0
+        d_high, st = run_dose(world, beam_high, s, 1, air)
+        mc_s += st["total_ms"] * 1e-3
+        body = np.flatnonzero(rho > 0.2)
+        pick = np.random.default_rng(s).choice(body, size=min(200_000, body.size), replace=False)
+        c = np.stack(np.unravel_index(pick, (nz, ny, nx)), axis=1)
+        for k, low in enumerate(lows):
+            d_low, st = run_dose(world, spiral_beam(low), s, 10 + k, air)
+            mc_s += st["total_ms"] * 1e-3
+            pairs.append(make_pair(torch, world, (nz, ny, nx), d_low, d_high, rho, mat))
+            centers.append(c)
+        log(f"phantom {s}: {len(lows)} inputs, target {high:.3g} histories, scale {pairs[-1].scale:.4g}")
+    t_data = time.perf_counter() - t0
+
+    net = G.Denoiser(channels, seed=0)
+    sampler = PatchSampler(torch, pairs, patch, batch, seed=1, centers=centers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = train(net, sampler, steps, lr=lr, lr_final=lr_final, log_every=max(1, steps // 10), log=log)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del sampler, pairs
+
+    # held-out torso
+    ph = P.torso_phantom(dims=dims, spacing=spacing, seed=eval_seed)
+    world.set_data(ph.density, ph.material)
+    world.build()
+    rho, mat = world.packed_density()
+    air = mat == 0
+    nonair = ~air
+    r1, s_r1 = run_dose(world, beam_high, eval_seed, 2, air)
+    r2, _ = run_dose(world, beam_high, eval_seed, 3, air)
+    rate = s_r1["n_histories"] / (s_r1["total_ms"] * 1e-3)
+    levels = []
+    sigma_ref = None
+    for k, low in enumerate(lows):
+        d_low, s_low = run_dose(world, spiral_beam(low), eval_seed, 20 + k, air)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        d_dn, scale = net.denoise_world(world)
+        t_inf = time.perf_counter() - t1
+        d_dn[air] = 0.0
+        e_dn = relative_errors(d_dn, r1, r2, mask=nonair)
+        e_low = relative_errors(d_low, r1, r2, mask=nonair)
+        sigma_ref = e_dn["reference_rms_rel"]
+        t_low = s_low["total_ms"] * 1e-3
+        levels.append({"histories": low, "mc_s": t_low, "inference_s": t_inf, "total_s": t_low + t_inf,
+                       "low_rms_rel": e_low["rms_rel_unbiased"], "denoised_rms_rel": e_dn["rms_rel_unbiased"],
+                       "denoised_mean_rel": e_dn["mean_rel"], "voxels_scored": e_dn["voxels"],
+                       "meets_target": bool(e_dn["rms_rel_unbiased"] <= target_error)})
+        log(f"eval {low:.3g}: denoised RMS {e_dn['rms_rel_unbiased']:.4f}, input RMS {e_low['rms_rel_unbiased']:.4f}")
+    n_plain = high * (sigma_ref / target_error) ** 2
+    t_plain = n_plain / rate
+    ok = [lv for lv in levels if lv["meets_target"]]
+    best = min(ok, key=lambda lv: lv["total_s"]) if ok else None
+    out = {
+        "dims": list(dims), "spacing_cm": list(spacing), "train_phantoms": len(train_seeds), "inputs": list(lows),
+        "high": high, "train_steps": steps, "batch": batch, "patch": patch,
+        "final_loss": float(np.mean(losses[-100:])), "data_s": t_data, "data_mc_s": mc_s, "train_s": t_train,
+        "histories_per_s": rate, "reference_rms_rel": sigma_ref, "target_error": target_error,
+        "plain_histories_to_target": n_plain, "plain_s_to_target": t_plain, "levels": levels,
+        "denoised_s_to_target": best["total_s"] if best else None,
+        "denoised_histories": best["histories"] if best else None,
+        "speedup": t_plain / best["total_s"] if best else None,
+    }
+    return out, net

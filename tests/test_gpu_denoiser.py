@@ -175,7 +175,8 @@ def test_world_denoise_path(gpu, torch):
     assert abs(scale / d[sel].mean() - 1) < 1e-9
     # the same through the array path: prepare_input + forward, times the scale
     shape = (ph.dims[2], ph.dims[1], ph.dims[0])
-    xin = gpu.prepare_input(torch.tensor(d.reshape(shape), dtype=torch.float32, device="cuda"),
+    d_in = np.where(mat == 0, 0.0, d)  # air enters with zero dose
+    xin = gpu.prepare_input(torch.tensor(d_in.reshape(shape), dtype=torch.float32, device="cuda"),
                             torch.tensor(rho.reshape(shape), device="cuda"),
                             torch.tensor(mat.reshape(shape), device="cuda"), scale)
     pred = dn.forward(xin[None]).cpu().numpy().ravel()

@@ -23,9 +23,15 @@ def table_dict(t):
 
 
 def hu_volume(n, seed):
+    """Fractional and integer CT numbers (the integer ones in [-1024, 3071] take the
+    kernel's lookup-table path), including the table's edges and just beyond."""
     rng = np.random.default_rng(seed)
     hu = rng.uniform(-1100.0, 2500.0, n)
     hu[: n // 4] = rng.normal(40.0, 60.0, n // 4)  # soft-tissue-like bulk
+    hu[n // 2:] = np.rint(rng.uniform(-1200.0, 3300.0, n - n // 2))
+    tail = np.array([-1025.0, -1024.0, 3071.0, 3072.0, -0.0, 0.5])
+    k = min(tail.size, n - n // 2)
+    hu[n - k:] = tail[:k]
     return hu
 
 

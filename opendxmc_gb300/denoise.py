@@ -73,14 +73,17 @@ def _exposures(beam: dict) -> int:
     return len(G.beam_exposures(dict(beam, particles_per_exposure=1)))
 
 
-def make_pair(torch, world: "G.GpuWorld", dims_zyx, d_low, d_high, rho, mat) -> Pair:
+def make_pair(torch, world: "G.GpuWorld", dims_zyx, d_low, d_high, rho, mat, ratio: float = 1.0) -> Pair:
+    """Input from the short run, target = the long run's dose x `ratio` (= short /
+    long history count: dose is not normalised per history, so this puts the
+    target in the short run's units), both over the short run's scale."""
     sel = rho > 0.2
     scale = float(d_low[sel].mean()) if sel.any() and d_low[sel].mean() > 0 else float(d_low.mean() or 1.0)
     dev = "cuda"
     x = G.prepare_input(torch.tensor(d_low.reshape(dims_zyx), dtype=torch.float32, device=dev),
                         torch.tensor(rho.reshape(dims_zyx), dtype=torch.float32, device=dev),
                         torch.tensor(mat.reshape(dims_zyx), dtype=torch.uint8, device=dev), scale)
-    t = torch.tensor((d_high / scale).reshape(dims_zyx), dtype=torch.float32, device=dev)
+    t = torch.tensor((d_high * (ratio / scale)).reshape(dims_zyx), dtype=torch.float32, device=dev)
     return Pair(x, t, scale, tuple(dims_zyx))
 
 
@@ -184,7 +187,7 @@ def run_dose(world, beam, seed, stream, air):
 
 
 def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_seeds=(11, 12, 13, 14, 15, 16),
-               eval_seed=99, lows=(1e8, 3e8, 1e9), high=1e10, steps=6000, batch=8, patch=64, lr=1e-3,
+               eval_seed=99, lows=(1e8, 3e8, 1e9), high=1e10, steps=8000, batch=8, patch=64, lr=1e-3,
                lr_final=1e-4, channels=(16, 32, 64, 128), target_error=0.02, log=print):
     """Train the denoiser on torso phantoms (inputs: runs of each history count in
     `lows`; target: a `high`-history run), then, on a held-out torso, compare the
@@ -215,7 +218,7 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
         for k, low in enumerate(lows):
             d_low, st = run_dose(world, spiral_beam(low), s, 10 + k, air)
             mc_s += st["total_ms"] * 1e-3
-            pairs.append(make_pair(torch, world, (nz, ny, nx), d_low, d_high, rho, mat))
+            pairs.append(make_pair(torch, world, (nz, ny, nx), d_low, d_high, rho, mat, low / high))
             centers.append(c)
         log(f"phantom {s}: {len(lows)} inputs, target {high:.3g} histories, scale {pairs[-1].scale:.4g}")
     t_data = time.perf_counter() - t0
@@ -248,8 +251,9 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
         d_dn, scale = net.denoise_world(world)
         t_inf = time.perf_counter() - t1
         d_dn[air] = 0.0
+        d_dn *= high / low  # in the references' units
         e_dn = relative_errors(d_dn, r1, r2, mask=nonair)
-        e_low = relative_errors(d_low, r1, r2, mask=nonair)
+        e_low = relative_errors(d_low * (high / low), r1, r2, mask=nonair)
         sigma_ref = e_dn["reference_rms_rel"]
         t_low = s_low["total_ms"] * 1e-3
         levels.append({"histories": low, "mc_s": t_low, "inference_s": t_inf, "total_s": t_low + t_inf,

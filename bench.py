@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--tracking", choices=list(TRACKING), default="woodcock")
     p.add_argument("--macro-cell", type=int, default=16, help="macro-cell edge in voxels (macro tracking)")
+    p.add_argument("--correction", type=int, choices=[0, 1, 2], default=1,
+                   help="bound-electron correction: 0 free electrons, 1 form factors (the reference's default), "
+                        "2 impulse approximation + fluorescence")
     p.add_argument("--small", action="store_true", help="denoise-experiment: a small quick configuration")
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
     p.add_argument("--workload", choices=["torso", "batch", "pipelines", "denoiser", "denoise-experiment"],
@@ -155,13 +158,13 @@ class ClockSampler:
                 "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
 
 
-def cpu_baseline(ph, beam, seconds: float) -> dict:
+def cpu_baseline(ph, beam, seconds: float, correction: int = 1) -> dict:
     """The FP64 CPU oracle on this host's cores over a bounded sample of the job."""
     from oracle import oracle as O
 
     O.build()
     threads = os.cpu_count() or 1
-    w = O.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    w = O.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials, correction)
     cal = 200_000
     t = time.perf_counter()
     w.run(beam, seed=1, stream=7, threads=threads, hist_begin=0, hist_end=cal)
@@ -185,7 +188,7 @@ def run_reference(args):
 
     O.build()
     threads = os.cpu_count() or 1
-    w = O.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    w = O.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials, args.correction)
     cal = 100_000
     t = time.perf_counter()
     w.run(beam, seed=1, threads=threads, hist_end=cal)
@@ -236,7 +239,7 @@ def run_ours(args):
 
     torch.cuda.set_device(local)
     ph, beam, hist = workload(args.histories)
-    gw = G.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    gw = G.GpuWorld(ph.dims, ph.spacing, ph.materials, args.correction)
     gw.set_data(ph.density, ph.material)
     gw.build()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
@@ -326,7 +329,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(ph, beam, args.cpu_seconds)
+        cpu = cpu_baseline(ph, beam, args.cpu_seconds, args.correction)
 
     if rank == 0:
         line = {
@@ -334,7 +337,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": list(ph.dims), "voxel_mm": 1.5, "histories_per_step": hist,
-                       "exposures": 360, "tracking": args.tracking,
+                       "exposures": 360, "tracking": args.tracking, "correction": args.correction,
                        "macro_cell_voxels": args.macro_cell if args.tracking == "macro" else None, "scoring": "fp64",
                        "l2": "256 MB buffer written before every step; tally 420 MB > L2",
                        "parallelism": f"replicas x{world} (independent Philox streams)"},

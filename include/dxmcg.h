@@ -170,6 +170,7 @@ typedef struct {
     double dose_scale;  /* mGy per (keV / g) applied by the dose readout */
     double calibration; /* factor applied to every history weight (1 unless normalize) */
     uint64_t n_crossings; /* MACRO tracking: macro-cell boundary crossings */
+    uint64_t n_fluorescence; /* correction level 2: K fluorescence photons emitted */
 } dxmcg_stats;
 
 typedef struct dxmcg_world dxmcg_world;
@@ -403,6 +404,10 @@ DXMCG_API int dxmcg_sample_compton(int n, const double* energies, const dxmcg_ma
     const double* uniforms, int u_stride, double* e_out, double* cos_out, int32_t* used);
 DXMCG_API int dxmcg_sample_rayleigh(int n, const double* energies, const dxmcg_material* m, const double* uniforms,
     int u_stride, double* cos_out, int32_t* used);
+/* correction level 2 photoelectric absorption: energy of the K fluorescence photon
+ * that leaves the atom (0: none) and the z cosine of its isotropic direction */
+DXMCG_API int dxmcg_sample_photoelectric(int n, const double* energies, const dxmcg_material* m,
+    const double* uniforms, int u_stride, double* e_out, double* dz_out, int32_t* used);
 /* source photons of histories [hist_begin, hist_begin + n): E, weight, grid-local pos[3], dir[3] */
 DXMCG_API int dxmcg_sample_source(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts, int n,
     double* out8);

@@ -176,6 +176,25 @@ namespace {
         used[i] = r.used;
     }
 
+    __global__ void photoKernel(int n, const float* __restrict__ E, const DevMaterial* __restrict__ M,
+        const float* __restrict__ u, int stride, float* __restrict__ eo, float* __restrict__ dzo,
+        int* __restrict__ used)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        InjectedUniforms r { u + static_cast<size_t>(i) * stride, stride, 0 };
+        const float Ef = samplePhotoFluorescence(E[i], M, r);
+        float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+        if (Ef > 0.0f) {
+            const float u1 = r.u();
+            isotropicDirection(dx, dy, dz, u1, r.u());
+        }
+        eo[i] = Ef;
+        dzo[i] = dz;
+        used[i] = r.used;
+    }
+
     __global__ void sourceKernel(const DevJob J, unsigned long long h0, int n, float* __restrict__ out)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -253,6 +272,13 @@ cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, int
     int stride, float* e_out, float* cos_out, int* used, cudaStream_t s)
 {
     comptonKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, correction, u, stride, e_out, cos_out, used);
+    return cudaGetLastError();
+}
+
+cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const float* u, int stride, float* e_out,
+    float* dz_out, int* used, cudaStream_t s)
+{
+    photoKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, u, stride, e_out, dz_out, used);
     return cudaGetLastError();
 }
 

@@ -273,6 +273,7 @@ void fillStats(const DevCounters& c, dxmcg_stats* stats)
     stats->n_errors = c.errors;
     stats->n_interacted = c.interacted;
     stats->n_crossings = c.crossings;
+    stats->n_fluorescence = c.fluorescence;
 }
 
 // the device's error flags as a status (DXMCG_OK when none)
@@ -905,6 +906,7 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
         stats->n_errors = c.errors;
         stats->n_interacted = c.interacted;
         stats->n_crossings = c.crossings;
+        stats->n_fluorescence = c.fluorescence;
         stats->kernel_ms = kernelMs;
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->dose_scale = kKeVToMilliGrayGram / w->voxelVolume;
@@ -1503,6 +1505,34 @@ DXMCG_API int dxmcg_sample_compton(int n, const double* energies, const dxmcg_ma
     for (int i = 0; i < n; ++i) {
         e_out[i] = a[i];
         cos_out[i] = b[i];
+    }
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_sample_photoelectric(int n, const double* energies, const dxmcg_material* m,
+    const double* uniforms, int u_stride, double* e_out, double* dz_out, int32_t* used)
+{
+    if (!e_out || !dz_out || !used)
+        return fail(DXMCG_ERR_ARGUMENT, "sample_photoelectric: null output");
+    DeviceBuffer<float> E, U, eo, dz;
+    DeviceBuffer<DevMaterial> M;
+    DeviceBuffer<int> us;
+    int rc = samplerCommon(n, energies, m, uniforms, u_stride, E, U, M);
+    if (rc != DXMCG_OK || n == 0)
+        return rc;
+    DXMCG_CUDA(eo.alloc(n));
+    DXMCG_CUDA(dz.alloc(n));
+    DXMCG_CUDA(us.alloc(n));
+    cudaError_t e = launchSamplePhoto(n, E.p, M.p, U.p, u_stride, eo.p, dz.p, us.p, nullptr);
+    if (e != cudaSuccess)
+        return cudaFail(e, "photoelectric kernel");
+    std::vector<float> a(n), b(n);
+    DXMCG_CUDA(cudaMemcpy(a.data(), eo.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(b.data(), dz.p, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(used, us.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) {
+        e_out[i] = a[i];
+        dz_out[i] = b[i];
     }
     return DXMCG_OK;
 }

@@ -106,6 +106,68 @@ namespace dev {
     }
 
     // ---------------------------------------------------------------- samplers
+    constexpr float kCutoffKeV = 1.0f; // photons below this energy are absorbed on the spot
+    constexpr int kPzTries = 32;       // electron-momentum draws per accepted scattering angle
+
+    // Correction level 2 (impulse approximation): the scattered energy for a bound
+    // electron.  A = E / E_C (E_C: the Compton line) and omu = 1 - cos(theta) come
+    // from the angle already sampled.  A shell is picked by its electrons among the
+    // shells bound by less than E; its projected momentum p_z = p_s t / sqrt(5) with t
+    // Student-t of 5 degrees of freedom, which is the profile (1 + (p_z/p_s)^2)^-3,
+    // drawn by Bailey's polar method (Math. Comp. 62, 779, 1994).  rho = p_z / m_e c
+    // gives E' from the impulse-approximation energy relation (Ribberfors 1975)
+    //   rho = (E E' (1 - cos) / m_e c^2 - (E - E')) / |E - E'| (photon momenta in keV),
+    // solved as E'/E = (A - rho^2 cos + rho sqrt((A - cos)^2 + omu (2 - omu) (1 - rho^2)))
+    //                  / (A^2 - rho^2).
+    // Accepted when E' > 0 and E - E' exceeds the shell's binding; false after
+    // kPzTries draws (the caller then samples a new angle).
+    template <class U>
+    __device__ bool dopplerEnergy(float E, float A, float omu, const DevMaterial* __restrict__ M, U& r, float& Ep)
+    {
+        const int ns = M->nShell;
+        float tot = 0.0f;
+        for (int k = 0; k < ns; ++k)
+            if (__ldg(&M->shellBinding[k]) < E)
+                tot += __ldg(&M->shellElectrons[k]);
+        const float target = r.u() * tot;
+        int sh = -1;
+        float acc = 0.0f;
+        for (int k = 0; k < ns; ++k) {
+            if (__ldg(&M->shellBinding[k]) < E) {
+                sh = k;
+                acc += __ldg(&M->shellElectrons[k]);
+                if (target <= acc)
+                    break;
+            }
+        }
+        if (sh < 0)
+            return false;
+        const float bind = __ldg(&M->shellBinding[sh]);
+        const float ps = __ldg(&M->shellMomentum[sh]);
+        const float c = 1.0f - omu;
+        const float am = A - c;
+        const float sin2 = omu * (2.0f - omu);
+        for (int t = 0; t < kPzTries; ++t) {
+            const float a = 2.0f * r.u() - 1.0f;
+            const float b = 2.0f * r.u() - 1.0f;
+            const float w = a * a + b * b;
+            if (w >= 1.0f)
+                continue;
+            const float rho = ps * a * sqrtf((powf(w, -0.4f) - 1.0f) / w);
+            const float rho2 = rho * rho;
+            const float den = A * A - rho2;
+            const float disc = am * am + sin2 * (1.0f - rho2);
+            if (!(den > 0.0f) || !(disc >= 0.0f))
+                continue;
+            const float e1 = E * ((A - rho2 * c + rho * sqrtf(disc)) / den);
+            if (e1 > 0.0f && E - e1 > bind) {
+                Ep = e1;
+                return true;
+            }
+        }
+        return false;
+    }
+
     template <class U>
     __device__ float sampleCompton(float E, const DevMaterial* __restrict__ M, int correction, U& r, float& cost,
         unsigned& err)
@@ -144,6 +206,12 @@ namespace dev {
                     continue;
             }
             cost = 1.0f - omu;
+            if (correction >= 2) {
+                float Ep;
+                if (!dopplerEnergy(E, 1.0f + xm1, omu, M, r, Ep))
+                    continue;
+                return Ep;
+            }
             return E / (1.0f + xm1);
         }
         err |= kErrRejectLimit;
@@ -189,6 +257,62 @@ namespace dev {
         }
         err |= kErrRejectLimit;
         return 1.0f;
+    }
+
+    // Correction level 2, photoelectric absorption: the absorbing element by its share
+    // n_i Z_i^4 (/ J_K below its K edge, / J_L below its L edge) of the cross-section,
+    // a K vacancy with probability 1 - 1/J_K above the element's K edge, then a K-alpha
+    // photon with the element's K fluorescence yield.  Returns the fluorescence
+    // energy, or 0 when no photon above the cutoff leaves the atom (all of E is then
+    // deposited).  Draws: element; above the K edge the shell; for a K vacancy the
+    // yield.
+    __device__ __forceinline__ float photoShare(float E, const DevMaterial* __restrict__ M, int i)
+    {
+        float w = __ldg(&M->nZ4[i]);
+        if (E < __ldg(&M->eK[i]))
+            w *= __ldg(&M->invJumpK);
+        if (E < __ldg(&M->eL[i]))
+            w *= __ldg(&M->invJumpL);
+        return w;
+    }
+
+    template <class U>
+    __device__ float samplePhotoFluorescence(float E, const DevMaterial* __restrict__ M, U& r)
+    {
+        const int n = M->n;
+        float tot = 0.0f;
+        for (int i = 0; i < n; ++i)
+            tot += photoShare(E, M, i);
+        const float target = r.u() * tot;
+        int e = n - 1;
+        float acc = 0.0f;
+        for (int i = 0; i < n; ++i) {
+            acc += photoShare(E, M, i);
+            if (target <= acc) {
+                e = i;
+                break;
+            }
+        }
+        if (E < __ldg(&M->eK[e]))
+            return 0.0f;
+        if (r.u() >= 1.0f - __ldg(&M->invJumpK))
+            return 0.0f; // L or outer shell: its fluorescence stays below the cutoff here
+        if (r.u() >= __ldg(&M->omegaK[e]))
+            return 0.0f; // Auger electrons: local
+        const float ka = __ldg(&M->kAlpha[e]);
+        return ka >= kCutoffKeV ? ka : 0.0f;
+    }
+
+    // isotropic direction from two uniforms: cos(theta) = 2 u1 - 1, phi = 2 pi u2
+    __device__ __forceinline__ void isotropicDirection(float& dx, float& dy, float& dz, float u1, float u2)
+    {
+        const float ct = 2.0f * u1 - 1.0f;
+        const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+        float sp, cp;
+        sincospif(2.0f * u2, &sp, &cp);
+        dx = st * cp;
+        dy = st * sp;
+        dz = ct;
     }
 
     __device__ __forceinline__ void scatterDirection(float& dx, float& dy, float& dz, float cost, float phiU)

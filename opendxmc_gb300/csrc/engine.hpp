@@ -36,6 +36,18 @@ struct DevMaterial {
     float nZ2[DXMCG_MAX_ELEMENTS];
     float a[DXMCG_MAX_ELEMENTS];
     float ia[DXMCG_MAX_ELEMENTS]; // 1 / a
+    // correction level 2: photoelectric element choice and K fluorescence
+    float nZ4[DXMCG_MAX_ELEMENTS];
+    float eK[DXMCG_MAX_ELEMENTS];
+    float eL[DXMCG_MAX_ELEMENTS];
+    float kAlpha[DXMCG_MAX_ELEMENTS];
+    float omegaK[DXMCG_MAX_ELEMENTS];
+    float invJumpK, invJumpL;
+    // correction level 2: Compton shells of the material (all elements)
+    int nShell;
+    float shellElectrons[3 * DXMCG_MAX_ELEMENTS];
+    float shellBinding[3 * DXMCG_MAX_ELEMENTS];
+    float shellMomentum[3 * DXMCG_MAX_ELEMENTS];
 };
 
 struct alignas(16) DevExposure {
@@ -105,7 +117,8 @@ struct DevJob {
 
 struct DevCounters {
     unsigned long long next; // work-queue head (history index)
-    unsigned long long histories, missed, visits, photo, compton, rayleigh, cutoff, errors, interacted, crossings;
+    unsigned long long histories, missed, visits, photo, compton, rayleigh, cutoff, errors, interacted, crossings,
+        fluorescence;
     double e_source, e_escaped, e_deposited;
     unsigned int error_flags;
 };
@@ -139,6 +152,8 @@ cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int
 cudaError_t launchPhilox(int n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t s);
 cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, int correction, const float* u,
     int stride, float* e_out, float* cos_out, int* used, cudaStream_t s);
+cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const float* u, int stride, float* e_out,
+    float* dz_out, int* used, cudaStream_t s);
 cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* u, int stride,
     float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s);

@@ -103,6 +103,19 @@ DevMaterial toDevMaterial(const dxmcg_material& m)
         d.nZ2[i] = static_cast<float>(s.nZ2[i]);
         d.a[i] = static_cast<float>(s.a[i]);
         d.ia[i] = static_cast<float>(1.0 / s.a[i]);
+        d.nZ4[i] = static_cast<float>(s.nZ4[i]);
+        d.eK[i] = static_cast<float>(s.eK[i]);
+        d.eL[i] = static_cast<float>(s.eL[i]);
+        d.kAlpha[i] = static_cast<float>(s.kAlpha[i]);
+        d.omegaK[i] = static_cast<float>(s.omegaK[i]);
+    }
+    d.invJumpK = static_cast<float>(1.0 / phys::kJumpRatioK);
+    d.invJumpL = static_cast<float>(1.0 / phys::kJumpRatioL);
+    d.nShell = s.nShell;
+    for (int k = 0; k < s.nShell; ++k) {
+        d.shellElectrons[k] = static_cast<float>(s.shellElectrons[k]);
+        d.shellBinding[k] = static_cast<float>(s.shellBinding[k]);
+        d.shellMomentum[k] = static_cast<float>(s.shellMomentum[k]);
     }
     return d;
 }

@@ -275,6 +275,8 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
         stats->n_cutoff = c.cutoff;
         stats->n_errors = c.errors;
         stats->n_interacted = c.interacted;
+        stats->n_crossings = c.crossings;
+        stats->n_fluorescence = c.fluorescence;
         stats->kernel_ms = 0.0; // no CUDA events on this path: host wall time of launch + readback below
         stats->total_ms = ms;
         stats->dose_scale = 1.602176634e-10 / (spacing_cm[0] * spacing_cm[1] * spacing_cm[2]);

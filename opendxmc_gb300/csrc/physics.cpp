@@ -14,8 +14,9 @@ namespace {
     constexpr double kBohrA = 0.529177210903;
     constexpr double kRydKeV = 13.605693122994e-3;
     constexpr double kPhotoC = 30.0;            // barn keV^3
-    constexpr double kJumpK = 7.0;
-    constexpr double kJumpL = 3.0;
+    constexpr double kJumpK = phys::kJumpRatioK;
+    constexpr double kJumpL = phys::kJumpRatioL;
+    constexpr double kFineStructure = 7.2973525693e-3; // 1 atomic unit of momentum in m_e c
     constexpr int kQuad = 1024;                 // Simpson panels over the scattering angle
 
     // IUPAC abridged standard atomic weights, Z = 1..92.
@@ -93,15 +94,44 @@ namespace phys {
         return 2.0 * kPi * kRe2Barn * (a + b - c);
     }
 
+    double kEdge(int Z) { return kRydKeV * (Z - 1.0) * (Z - 1.0); }
+    double lEdge(int Z) { return Z > 7 ? kRydKeV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0; }
+    double kAlphaEnergy(int Z) { return 0.75 * kEdge(Z); }
+
+    double fluorescenceYieldK(int Z)
+    {
+        const double z = static_cast<double>(Z);
+        const double x = 0.015 + 0.0327 * z - 0.64e-6 * z * z * z;
+        const double x4 = x * x * x * x;
+        return x4 / (1.0 + x4);
+    }
+
+    Shells comptonShells(int Z)
+    {
+        Shells s;
+        const double z = static_cast<double>(Z);
+        const double occ[3] = { std::min(z, 2.0), std::min(std::max(z - 2.0, 0.0), 8.0), std::max(z - 10.0, 0.0) };
+        const double zk = std::max(z - 1.0, 1.0);
+        const double zl = std::max(z - 7.4, 0.5 * z);
+        const double bind[3] = { kRydKeV * zk * zk, kRydKeV * zl * zl / 4.0, kRydKeV * (z / 3.0) * (z / 3.0) / 9.0 };
+        for (int k = 0; k < 3; ++k) {
+            if (occ[k] <= 0.0)
+                continue;
+            s.electrons[s.n] = occ[k];
+            s.binding[s.n] = bind[k];
+            s.momentum[s.n] = std::sqrt(bind[k] / kRydKeV) * kFineStructure;
+            ++s.n;
+        }
+        return s;
+    }
+
     double photoelectric(double E, int Z)
     {
         const double z2 = static_cast<double>(Z) * Z;
         double s = kPhotoC * z2 * z2 / (E * E * E);
-        const double edgeK = kRydKeV * (Z - 1.0) * (Z - 1.0);
-        const double edgeL = Z > 7 ? kRydKeV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0;
-        if (E < edgeK)
+        if (E < kEdge(Z))
             s /= kJumpK;
-        if (E < edgeL)
+        if (E < lEdge(Z))
             s /= kJumpL;
         return s;
     }
@@ -197,6 +227,19 @@ SamplingElements samplingElements(const dxmcg_material& m)
         s.nZ2[i] = ni * m.Z[i] * m.Z[i];
         s.a[i] = phys::formFactorScale(m.Z[i]);
         s.Zsum += s.nZ[i];
+        const double z2 = static_cast<double>(m.Z[i]) * m.Z[i];
+        s.nZ4[i] = ni * z2 * z2;
+        s.eK[i] = phys::kEdge(m.Z[i]);
+        s.eL[i] = phys::lEdge(m.Z[i]);
+        s.kAlpha[i] = phys::kAlphaEnergy(m.Z[i]);
+        s.omegaK[i] = phys::fluorescenceYieldK(m.Z[i]);
+        const auto sh = phys::comptonShells(m.Z[i]);
+        for (int k = 0; k < sh.n; ++k) {
+            s.shellElectrons[s.nShell] = ni * sh.electrons[k];
+            s.shellBinding[s.nShell] = sh.binding[k];
+            s.shellMomentum[s.nShell] = sh.momentum[k];
+            ++s.nShell;
+        }
     }
     return s;
 }

@@ -11,7 +11,16 @@
 //    Thomas-Fermi radius scaling, a_Z = (Z^(1/3) / (2 pi a0))^2, x = sin(theta/2)/lambda [1/A];
 //  * photoelectric: C Z^4 / E^3 with K/L edges at Moseley energies and jump ratios;
 //  * tube: Kramers' thick-target law on 1 keV bins plus tungsten K lines with
-//    Green-Cosslett yield scaling, exponential filtration.
+//    Green-Cosslett yield scaling, exponential filtration;
+//  * correction level 2 (impulse approximation, simulationwidget.cpp:68-73): each
+//    element has three Compton shells (K: min(Z, 2) electrons bound by the Moseley K
+//    edge; L: up to 8 electrons bound by Ryd max(Z - 7.4, Z/2)^2 / 4; the rest bound by
+//    Ryd (Z/3)^2 / 9), each with the hydrogen-like 1s Compton profile
+//    J(p) ~ (1 + (p/p_s)^2)^-3 whose momentum scale p_s = sqrt(U_s / Ryd) atomic units
+//    follows from its binding energy U_s; a photoelectric absorption above the K edge
+//    leaves a K vacancy with probability 1 - 1/J_K, which emits a K-alpha photon of
+//    0.75 Ryd (Z - 1)^2 with the yield omega_K(Z) of Bambynek et al. (Rev. Mod. Phys.
+//    44, 716, 1972): omega = X^4 / (1 + X^4), X = 0.015 + 0.0327 Z - 0.64e-6 Z^3.
 #pragma once
 
 #include <array>
@@ -28,6 +37,8 @@ constexpr double kDE = 0.5;
 constexpr double kEcut = 1.0;
 
 namespace phys {
+    constexpr double kJumpRatioK = 7.0; // photoelectric jump ratios at the K and L edges
+    constexpr double kJumpRatioL = 3.0;
     double atomicMass(int Z);
     double elementDensity(int Z);
     double kleinNishinaTotal(double E);       // barn per electron
@@ -36,6 +47,17 @@ namespace phys {
     double coherent(double E, int Z);
     double knEnergyTransferFraction(double E);
     double formFactorScale(int Z);            // a_Z in 1/A^2
+    double kEdge(int Z);                      // keV
+    double lEdge(int Z);                      // keV, 0 for Z <= 7
+    double kAlphaEnergy(int Z);               // keV
+    double fluorescenceYieldK(int Z);
+    // correction level 2 Compton shells: electrons, binding energy (keV) and the
+    // momentum scale of the profile in units of m_e c
+    struct Shells {
+        int n = 0;
+        double electrons[3] {}, binding[3] {}, momentum[3] {};
+    };
+    Shells comptonShells(int Z);
 }
 
 // Composition -> mass attenuation (cm^2/g) at arbitrary energies.
@@ -46,11 +68,18 @@ struct Attenuation {
 bool validComposition(const dxmcg_material& m);
 Attenuation attenuation(const dxmcg_material& m, int correction, double E);
 
-// Per-element data the device samplers use (n_i = w_i / A_i).
+// Per-element data the device samplers use (n_i = w_i / A_i).  Correction level 2
+// adds per element n_i Z^4 (the photoelectric share up to the common C / E^3), the K
+// and L edges, the K-alpha energy and the K fluorescence yield, and the material's
+// Compton shells (electrons n_i x occupancy, binding, momentum scale).
+constexpr int kMaxShells = 3 * DXMCG_MAX_ELEMENTS;
 struct SamplingElements {
     int n = 0;
     std::array<double, DXMCG_MAX_ELEMENTS> nZ {}, nZ2 {}, a {};
+    std::array<double, DXMCG_MAX_ELEMENTS> nZ4 {}, eK {}, eL {}, kAlpha {}, omegaK {};
     double Zsum = 0;
+    int nShell = 0;
+    std::array<double, kMaxShells> shellElectrons {}, shellBinding {}, shellMomentum {};
 };
 SamplingElements samplingElements(const dxmcg_material& m);
 

@@ -34,8 +34,20 @@ namespace {
 
     constexpr int kChunk = 256; // histories a warp takes from the queue at once
 
-    enum LaneState : int { kDead = 0, kStepping = 1, kCompton = 2, kRayleigh = 3 };
-    enum BlockCount : int { cHist, cMissed, cPhoto, cCompton, cRayleigh, cCutoff, cErrors, cInteracted, cNum };
+    // kPhoto: a photoelectric absorption waiting for its fluorescence (correction level 2)
+    enum LaneState : int { kDead = 0, kStepping = 1, kCompton = 2, kRayleigh = 3, kPhoto = 4 };
+    enum BlockCount : int {
+        cHist,
+        cMissed,
+        cPhoto,
+        cCompton,
+        cRayleigh,
+        cCutoff,
+        cErrors,
+        cInteracted,
+        cFluorescence,
+        cNum
+    };
 
     __device__ __forceinline__ unsigned long long warpSum(unsigned long long v)
     {
@@ -356,7 +368,8 @@ namespace {
             const int nPark = __popc(parked);
             if (parked && (nPark >= interactBatch || nPark >= nStep)) {
                 const bool compton = st == kCompton;
-                bool cut = false;
+                const bool rayleigh = st == kRayleigh;
+                bool cut = false, fluor = false;
                 if (compton) {
                     float cost;
                     const float Ep = sampleCompton(ph.E, J.mats + pm, J.correction, rng, cost, err);
@@ -378,18 +391,44 @@ namespace {
                         else
                             ec.set(J, ph.E);
                     }
-                } else if (st == kRayleigh) {
+                } else if (rayleigh) {
                     const float cost = sampleRayleigh(ph.E, J.mats + pm, rng, err);
                     scatterDirection(ph.dx, ph.dy, ph.dz, cost, rng.u());
                     st = kStepping;
+                } else if (st == kPhoto) {
+                    // correction level 2: the atom may emit a K-alpha photon, which the lane
+                    // follows from the absorption point in an isotropic direction
+                    const float Ef = samplePhotoFluorescence(ph.E, J.mats + pm, rng);
+                    const float e = ph.w * (ph.E - Ef);
+                    deposit(J.tally, pv, e);
+                    edep.add(e);
+                    if (Ef > 0.0f) {
+                        const float u1 = rng.u();
+                        isotropicDirection(ph.dx, ph.dy, ph.dz, u1, rng.u());
+                        ph.E = Ef;
+                        st = kStepping;
+                        fluor = true;
+                        if (TRACKING == DXMCG_TRACK_SIDDON)
+                            gridPos(ph.E, ec.ie, ec.fe);
+                        else
+                            ec.set(J, ph.E);
+                    } else {
+                        st = kDead;
+                    }
                 }
                 const unsigned mC = __ballot_sync(kFull, compton);
+                const unsigned mR = __ballot_sync(kFull, rayleigh);
                 const unsigned mCut = __ballot_sync(kFull, cut);
+                const unsigned mF = __ballot_sync(kFull, fluor);
                 if (lane == 0) {
-                    atomicAdd(&sCount[cCompton], static_cast<unsigned long long>(__popc(mC)));
-                    atomicAdd(&sCount[cRayleigh], static_cast<unsigned long long>(__popc(parked & ~mC)));
+                    if (mC)
+                        atomicAdd(&sCount[cCompton], static_cast<unsigned long long>(__popc(mC)));
+                    if (mR)
+                        atomicAdd(&sCount[cRayleigh], static_cast<unsigned long long>(__popc(mR)));
                     if (mCut)
                         atomicAdd(&sCount[cCutoff], static_cast<unsigned long long>(__popc(mCut)));
+                    if (mF)
+                        atomicAdd(&sCount[cFluorescence], static_cast<unsigned long long>(__popc(mF)));
                 }
             }
 
@@ -425,11 +464,17 @@ namespace {
                     const float co = fmaf(ec.fe, b.z - a.z, a.z);
                     const float rt = rng.u() * (pe + ic + co);
                     if (rt < pe) {
-                        const float e = ph.w * ph.E;
-                        deposit(J.tally, v, e);
-                        edep.add(e);
-                        st = kDead;
                         photo = true;
+                        if (J.correction >= 2) {
+                            pv = v;
+                            pm = m;
+                            st = kPhoto;
+                        } else {
+                            const float e = ph.w * ph.E;
+                            deposit(J.tally, v, e);
+                            edep.add(e);
+                            st = kDead;
+                        }
                     } else {
                         pv = v;
                         pm = m;
@@ -483,6 +528,8 @@ namespace {
             atomicAdd(&ctr->cutoff, sCount[cCutoff]);
             atomicAdd(&ctr->errors, sCount[cErrors]);
             atomicAdd(&ctr->interacted, sCount[cInteracted]);
+            if (sCount[cFluorescence])
+                atomicAdd(&ctr->fluorescence, sCount[cFluorescence]);
         }
     }
 

@@ -487,6 +487,22 @@ def sample_compton(energies, zw, correction, uniforms):
     return eo, co, used
 
 
+def sample_photoelectric(energies, zw, uniforms):
+    """Correction level 2 photoelectric absorption: (fluorescence energy, its z
+    cosine, uniforms used) per energy."""
+    E = np.ascontiguousarray(energies, dtype=np.float64)
+    U = np.ascontiguousarray(uniforms, dtype=np.float64)
+    n, stride = U.shape
+    eo = np.zeros(n)
+    dz = np.zeros(n)
+    used = np.zeros(n, dtype=np.int32)
+    m = N.Material.from_dict(zw)
+    N.check(N.lib().dxmcg_sample_photoelectric(n, N.ptr(E, C.c_double), C.byref(m), N.ptr(U, C.c_double), stride,
+                                               N.ptr(eo, C.c_double), N.ptr(dz, C.c_double),
+                                               N.ptr(used, C.c_int32)))
+    return eo, dz, used
+
+
 def sample_rayleigh(energies, zw, uniforms):
     E = np.ascontiguousarray(energies, dtype=np.float64)
     U = np.ascontiguousarray(uniforms, dtype=np.float64)

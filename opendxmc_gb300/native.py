@@ -41,6 +41,7 @@ EXPORTED = [
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_reset", "dxmcg_progress_continue",
     "dxmcg_progress_message",
     "dxmcg_siddon_trace", "dxmcg_philox", "dxmcg_history_stream", "dxmcg_sample_compton", "dxmcg_sample_rayleigh",
+    "dxmcg_sample_photoelectric",
     "dxmcg_sample_source",
 ]
 
@@ -155,7 +156,8 @@ class Stats(C.Structure):
         (n, C.c_uint64) for n in ("n_histories", "n_missed", "n_visits", "n_photo", "n_compton", "n_rayleigh",
                                   "n_cutoff", "n_errors", "n_interacted")] + [
         ("kernel_ms", C.c_double), ("total_ms", C.c_double), ("dose_scale", C.c_double),
-        ("calibration", C.c_double), ("n_crossings", C.c_uint64)]
+        ("calibration", C.c_double), ("n_crossings", C.c_uint64),
+        ("n_fluorescence", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {f[0]: getattr(self, f[0]) for f in self._fields_}
@@ -235,6 +237,7 @@ def lib() -> C.CDLL:
         "dxmcg_history_stream": (i, [u64, C.c_uint32, u64, i, i, C.POINTER(C.c_uint32)]),
         "dxmcg_sample_compton": (i, [i, pd, C.POINTER(Material), i, pd, i, pd, pd, pi32]),
         "dxmcg_sample_rayleigh": (i, [i, pd, C.POINTER(Material), pd, i, pd, pi32]),
+        "dxmcg_sample_photoelectric": (i, [i, pd, C.POINTER(Material), pd, i, pd, pd, pi32]),
         "dxmcg_sample_source": (i, [vp, C.POINTER(Beam), C.POINTER(RunOptions), i, pd]),
     }
     for name, (res, args) in sig.items():

@@ -104,6 +104,48 @@ static double kn_dcs(double k, double mu)
     return 0.5 * R_E2_BARN * eps * eps * (eps + 1.0 / eps - (1.0 - mu * mu));
 }
 
+/* Correction level 2 element data (project model, independent restatement):
+ * K edge Ryd (Z-1)^2, L edge Ryd (Z-7.4)^2/4 (Z > 7), K-alpha 0.75 Ryd (Z-1)^2, K
+ * fluorescence yield omega = X^4/(1+X^4), X = 0.015 + 0.0327 Z - 0.64e-6 Z^3
+ * (Bambynek et al., Rev. Mod. Phys. 44, 716, 1972).  Compton shells: K with
+ * min(Z,2) electrons bound by Ryd max(Z-1,1)^2; L with up to 8 electrons bound by
+ * Ryd max(Z-7.4, Z/2)^2/4; the rest bound by Ryd (Z/3)^2/9; each with the
+ * hydrogen-like 1s Compton profile of momentum scale sqrt(U/Ryd) atomic units
+ * (alpha m_e c per atomic unit). */
+#define FINE_STRUCTURE 7.2973525693e-3
+double or_k_edge(int Z) { return RYD_KEV * (Z - 1.0) * (Z - 1.0); }
+double or_l_edge(int Z) { return Z > 7 ? RYD_KEV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0; }
+double or_k_alpha(int Z) { return 0.75 * or_k_edge(Z); }
+double or_fluorescence_yield_k(int Z)
+{
+    const double x = 0.015 + 0.0327 * Z - 0.64e-6 * (double)Z * Z * Z;
+    const double x4 = x * x * x * x;
+    return x4 / (1.0 + x4);
+}
+int or_compton_shells(int Z, double electrons[3], double binding[3], double momentum[3])
+{
+    const double z = (double)Z;
+    double occ[3], bind[3];
+    occ[0] = z < 2.0 ? z : 2.0;
+    occ[1] = z - 2.0 < 0.0 ? 0.0 : (z - 2.0 > 8.0 ? 8.0 : z - 2.0);
+    occ[2] = z - 10.0 < 0.0 ? 0.0 : z - 10.0;
+    const double zk = z - 1.0 > 1.0 ? z - 1.0 : 1.0;
+    const double zl = z - 7.4 > 0.5 * z ? z - 7.4 : 0.5 * z;
+    bind[0] = RYD_KEV * zk * zk;
+    bind[1] = RYD_KEV * zl * zl / 4.0;
+    bind[2] = RYD_KEV * (z / 3.0) * (z / 3.0) / 9.0;
+    int n = 0;
+    for (int k = 0; k < 3; ++k) {
+        if (occ[k] <= 0.0)
+            continue;
+        electrons[n] = occ[k];
+        binding[n] = bind[k];
+        momentum[n] = sqrt(bind[k] / RYD_KEV) * FINE_STRUCTURE;
+        ++n;
+    }
+    return n;
+}
+
 double or_sigma_photo(double E, int Z)
 {
     const double z2 = (double)Z * (double)Z;
@@ -786,12 +828,18 @@ int or_siddon_f64(const double o[3], const double d[3], const int32_t n[3], cons
 /* ------------------------------------------------------------------------- */
 /* Material data for sampling: per element n_i = w_i / A_i (mol/g), Z_i, a_Z.  */
 /* ------------------------------------------------------------------------- */
+#define OR_MAX_SHELLS (3 * OR_MAX_ELEMENTS)
 typedef struct {
     int n;
     double nZ[OR_MAX_ELEMENTS];  /* n_i Z_i   (incoherent scattering function weight) */
     double nZ2[OR_MAX_ELEMENTS]; /* n_i Z_i^2 (form-factor weight) */
     double a[OR_MAX_ELEMENTS];
     double Zsum;
+    /* correction level 2 */
+    double nZ4[OR_MAX_ELEMENTS]; /* n_i Z_i^4 (photoelectric share up to C / E^3) */
+    double eK[OR_MAX_ELEMENTS], eL[OR_MAX_ELEMENTS], kAlpha[OR_MAX_ELEMENTS], omegaK[OR_MAX_ELEMENTS];
+    int nShell;
+    double shElectrons[OR_MAX_SHELLS], shBinding[OR_MAX_SHELLS], shMomentum[OR_MAX_SHELLS];
 } mat_sampling;
 
 static void make_sampling(const or_composition* c, mat_sampling* m)
@@ -800,13 +848,130 @@ static void make_sampling(const or_composition* c, mat_sampling* m)
     normalised(c, w);
     m->n = c->n;
     m->Zsum = 0.0;
+    m->nShell = 0;
     for (int i = 0; i < c->n; ++i) {
         const double ni = w[i] / or_atomic_mass(c->Z[i]);
         m->nZ[i] = ni * c->Z[i];
         m->nZ2[i] = ni * c->Z[i] * c->Z[i];
         m->a[i] = a_Z(c->Z[i]);
         m->Zsum += m->nZ[i];
+        const double z2 = (double)c->Z[i] * c->Z[i];
+        m->nZ4[i] = ni * z2 * z2;
+        m->eK[i] = or_k_edge(c->Z[i]);
+        m->eL[i] = or_l_edge(c->Z[i]);
+        m->kAlpha[i] = or_k_alpha(c->Z[i]);
+        m->omegaK[i] = or_fluorescence_yield_k(c->Z[i]);
+        double el[3], bd[3], mo[3];
+        const int ns = or_compton_shells(c->Z[i], el, bd, mo);
+        for (int k = 0; k < ns; ++k) {
+            m->shElectrons[m->nShell] = ni * el[k];
+            m->shBinding[m->nShell] = bd[k];
+            m->shMomentum[m->nShell] = mo[k];
+            m->nShell++;
+        }
     }
+}
+
+/* Impulse-approximation energy for a projected electron momentum rho = p_z / m_e c
+ * (Ribberfors 1975: rho = (E E' (1 - cos)/m_e c^2 - (E - E')) / |E - E'|, photon
+ * momenta in keV), solved for E': with A = E / E_C and omu = 1 - cos,
+ *   E'/E = (A - rho^2 cos + rho sqrt((A - cos)^2 + omu (2 - omu)(1 - rho^2))) / (A^2 - rho^2).
+ * Returns 0 when no root exists. */
+double or_doppler_energy(double E, double A, double omu, double rho)
+{
+    const double c = 1.0 - omu;
+    const double den = A * A - rho * rho;
+    const double disc = (A - c) * (A - c) + omu * (2.0 - omu) * (1.0 - rho * rho);
+    if (!(den > 0.0) || !(disc >= 0.0))
+        return 0.0;
+    return E * ((A - rho * rho * c + rho * sqrt(disc)) / den);
+}
+
+/* Correction level 2 Compton energy: shell by its electrons among the shells bound
+ * by less than E, projected momentum from the shell's profile
+ * (1 + (p/p_s)^2)^-3 = Student-t with 5 degrees of freedom scaled by p_s / sqrt(5),
+ * drawn by Bailey's polar method (Math. Comp. 62, 779, 1994); accepted when E' > 0
+ * and E - E' exceeds the binding; 0 after DOPPLER_TRIES draws. */
+#define DOPPLER_TRIES 32
+static double doppler_sample(double E, double A, double omu, const mat_sampling* m, rng_t* r)
+{
+    double tot = 0.0;
+    for (int k = 0; k < m->nShell; ++k)
+        if (m->shBinding[k] < E)
+            tot += m->shElectrons[k];
+    const double target = rng_u(r) * tot;
+    int sh = -1;
+    double acc = 0.0;
+    for (int k = 0; k < m->nShell; ++k) {
+        if (m->shBinding[k] < E) {
+            sh = k;
+            acc += m->shElectrons[k];
+            if (target <= acc)
+                break;
+        }
+    }
+    if (sh < 0)
+        return 0.0;
+    for (int t = 0; t < DOPPLER_TRIES; ++t) {
+        const double a = 2.0 * rng_u(r) - 1.0;
+        const double b = 2.0 * rng_u(r) - 1.0;
+        const double w = a * a + b * b;
+        if (w >= 1.0)
+            continue;
+        const double rho = m->shMomentum[sh] * a * sqrt((pow(w, -0.4) - 1.0) / w);
+        const double e1 = or_doppler_energy(E, A, omu, rho);
+        if (e1 > 0.0 && E - e1 > m->shBinding[sh])
+            return e1;
+    }
+    return 0.0;
+}
+
+/* Correction level 2 photoelectric absorption: element by n_i Z_i^4 (/ J_K below its
+ * K edge, / J_L below its L edge), K vacancy with probability 1 - 1/J_K above the
+ * K edge, K-alpha emission with the yield omega_K.  Returns the fluorescence energy
+ * or 0 (none above the cutoff). */
+static double photo_share(double E, const mat_sampling* m, int i)
+{
+    double w = m->nZ4[i];
+    if (E < m->eK[i])
+        w /= J_K;
+    if (E < m->eL[i])
+        w /= J_L;
+    return w;
+}
+
+static double sample_photo_fluorescence(double E, const mat_sampling* m, rng_t* r)
+{
+    double tot = 0.0;
+    for (int i = 0; i < m->n; ++i)
+        tot += photo_share(E, m, i);
+    const double target = rng_u(r) * tot;
+    int e = m->n - 1;
+    double acc = 0.0;
+    for (int i = 0; i < m->n; ++i) {
+        acc += photo_share(E, m, i);
+        if (target <= acc) {
+            e = i;
+            break;
+        }
+    }
+    if (E < m->eK[e])
+        return 0.0;
+    if (rng_u(r) >= 1.0 - 1.0 / J_K)
+        return 0.0;
+    if (rng_u(r) >= m->omegaK[e])
+        return 0.0;
+    return m->kAlpha[e] >= E_CUT ? m->kAlpha[e] : 0.0;
+}
+
+static void isotropic_dir(double d[3], double u1, double u2)
+{
+    const double ct = 2.0 * u1 - 1.0;
+    const double st = sqrt(fmax(0.0, 1.0 - ct * ct));
+    const double phi = 2.0 * PI * u2;
+    d[0] = st * cos(phi);
+    d[1] = st * sin(phi);
+    d[2] = ct;
 }
 
 /* Klein-Nishina by Kahn's rejection method (Kahn 1954; as given in Lux &
@@ -847,6 +1012,12 @@ static double sample_compton(double E, const mat_sampling* m, int correction, rn
                 continue;
         }
         *cos_theta = 1.0 - omu;
+        if (correction >= 2) {
+            const double Ep = doppler_sample(E, 1.0 + xm1, omu, m, r);
+            if (Ep <= 0.0)
+                continue;
+            return Ep;
+        }
         return E / (1.0 + xm1);
     }
     *cos_theta = 1.0;
@@ -900,6 +1071,26 @@ double or_sample_compton(double E, const or_composition* c, int correction, cons
     const double Ep = sample_compton(E, &m, correction, &r, cos_theta);
     *used = r.used;
     return Ep;
+}
+
+double or_sample_photoelectric(double E, const or_composition* c, const double* u, int nu, int* used, double* dz)
+{
+    mat_sampling m;
+    make_sampling(c, &m);
+    rng_t r;
+    memset(&r, 0, sizeof(r));
+    r.inj = u;
+    r.n_inj = nu;
+    const double Ef = sample_photo_fluorescence(E, &m, &r);
+    *dz = 0.0;
+    if (Ef > 0.0) {
+        double d[3];
+        const double u1 = rng_u(&r);
+        isotropic_dir(d, u1, rng_u(&r));
+        *dz = d[2];
+    }
+    *used = r.used;
+    return Ef;
 }
 
 double or_sample_rayleigh(double E, const or_composition* c, const double* u, int nu, int* used)
@@ -1268,6 +1459,19 @@ static int interact(or_world* w, size_t v, int m, double* E, double wgt, double 
     st->n_real++;
     if (rt < ph) {
         st->n_photo++;
+        if (w->correction >= 2) {
+            /* the atom may emit a K-alpha photon, followed from here in an isotropic direction */
+            const double Ef = sample_photo_fluorescence(*E, &w->samp[m], r);
+            deposit(w, v, wgt * (*E - Ef), st);
+            if (Ef > 0.0) {
+                st->n_fluorescence++;
+                const double u1 = rng_u(r);
+                isotropic_dir(d, u1, rng_u(r));
+                *E = Ef;
+                return 1;
+            }
+            return 0;
+        }
         deposit(w, v, wgt * *E, st);
         return 0;
     }
@@ -1540,6 +1744,7 @@ static void* worker(void* arg)
     c->tot.n_errors += st.n_errors;
     c->tot.n_interacted += st.n_interacted;
     c->tot.n_crossings += st.n_crossings;
+    c->tot.n_fluorescence += st.n_fluorescence;
     pthread_mutex_unlock(&c->lock);
     return NULL;
 }

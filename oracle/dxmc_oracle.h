@@ -123,7 +123,7 @@ typedef struct {
 typedef struct {
     double e_source, e_deposited, e_escaped;
     uint64_t n_histories, n_missed, n_visits, n_real, n_photo, n_compton, n_rayleigh,
-        n_deposits, n_cutoff, n_errors, n_interacted, n_crossings;
+        n_deposits, n_cutoff, n_errors, n_interacted, n_crossings, n_fluorescence;
 } or_stats;
 
 typedef struct or_world or_world;
@@ -160,6 +160,15 @@ int or_siddon_f64(const double o[3], const double d[3], const int32_t n[3], cons
 double or_sample_compton(double E, const or_composition* c, int correction, const double* u,
     int nu, int* used, double* cos_theta);
 double or_sample_rayleigh(double E, const or_composition* c, const double* u, int nu, int* used);
+/* correction level 2 photoelectric absorption: fluorescence energy (0: none), dz of its direction */
+double or_sample_photoelectric(double E, const or_composition* c, const double* u, int nu, int* used, double* dz);
+/* correction level 2 element data and the impulse-approximation energy relation */
+double or_k_edge(int Z);
+double or_l_edge(int Z);
+double or_k_alpha(int Z);
+double or_fluorescence_yield_k(int Z);
+int or_compton_shells(int Z, double electrons[3], double binding[3], double momentum[3]);
+double or_doppler_energy(double E, double A, double omu, double rho);
 /* world */
 or_world* or_world_create(const int32_t dims[3], const double spacing_cm[3], const double* density,
     const uint8_t* material, const or_composition* mats, int n_mats, int correction);

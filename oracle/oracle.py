@@ -123,6 +123,7 @@ class Stats(C.Structure):
             "n_errors",
             "n_interacted",
             "n_crossings",
+            "n_fluorescence",
         )
     ]
 
@@ -179,6 +180,15 @@ def lib() -> C.CDLL:
     L.or_siddon_f64.argtypes = [pd, pd, C.POINTER(C.c_int32), pd, i, C.POINTER(C.c_int64), pd]
     L.or_sample_compton.restype = d
     L.or_sample_compton.argtypes = [d, C.POINTER(Composition), i, pd, i, C.POINTER(C.c_int), pd]
+    L.or_sample_photoelectric.restype = d
+    L.or_sample_photoelectric.argtypes = [d, C.POINTER(Composition), pd, i, C.POINTER(C.c_int), pd]
+    L.or_compton_shells.restype = i
+    L.or_compton_shells.argtypes = [i, pd, pd, pd]
+    L.or_doppler_energy.restype = d
+    L.or_doppler_energy.argtypes = [d, d, d, d]
+    for f in ("or_k_edge", "or_l_edge", "or_k_alpha", "or_fluorescence_yield_k"):
+        getattr(L, f).restype = d
+        getattr(L, f).argtypes = [i]
     L.or_sample_rayleigh.restype = d
     L.or_sample_rayleigh.argtypes = [d, C.POINTER(Composition), pd, i, C.POINTER(C.c_int)]
     L.or_world_create.restype = vp
@@ -345,6 +355,29 @@ def sample_compton(E, zw, correction, uniforms):
     c = Composition.from_dict(zw)
     Ep = lib().or_sample_compton(E, C.byref(c), correction, _p(u, C.c_double), u.size, C.byref(used), C.byref(cost))
     return Ep, cost.value, used.value
+
+
+def sample_photoelectric(E, zw, uniforms):
+    """(fluorescence energy or 0, z cosine of its direction, uniforms used)"""
+    u = np.ascontiguousarray(uniforms, dtype=np.float64)
+    used = C.c_int(0)
+    dz = C.c_double(0)
+    c = Composition.from_dict(zw)
+    Ef = lib().or_sample_photoelectric(E, C.byref(c), _p(u, C.c_double), u.size, C.byref(used), C.byref(dz))
+    return Ef, dz.value, used.value
+
+
+def compton_shells(Z):
+    """(electrons, binding keV, momentum scale in m_e c) of the level-2 Compton shells"""
+    e = (C.c_double * 3)()
+    b = (C.c_double * 3)()
+    m = (C.c_double * 3)()
+    n = lib().or_compton_shells(Z, e, b, m)
+    return np.array(e[:n]), np.array(b[:n]), np.array(m[:n])
+
+
+def doppler_energy(E, A, omu, rho):
+    return lib().or_doppler_energy(E, A, omu, rho)
 
 
 def sample_rayleigh(E, zw, uniforms):

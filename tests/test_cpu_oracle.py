@@ -256,3 +256,85 @@ def test_oracle_woodcock_and_siddon_tracking_agree(oracle):
                                                  parity.tally_variance(e2, q2, n))
     assert nvox > 100 and frac >= 0.99
     assert e1.sum() == pytest.approx(e2.sum(), rel=0.01)
+
+
+# ---- correction level 2 (impulse approximation, fluorescence)
+ME = 510.99895
+
+
+def test_doppler_energy_solves_the_impulse_relation(oracle):
+    rng = np.random.default_rng(3)
+    for _ in range(2000):
+        E = rng.uniform(5.0, 150.0)
+        c = rng.uniform(-1.0, 1.0)
+        rho = rng.uniform(-0.3, 0.3)
+        omu = 1.0 - c
+        A = 1.0 + E / ME * omu
+        x = oracle.doppler_energy(E, A, omu, rho)
+        assert x > 0.0
+        q = np.sqrt(E * E + x * x - 2.0 * E * x * c)
+        back = (E * x * omu / ME - (E - x)) / q
+        assert back == pytest.approx(rho, rel=1e-9, abs=1e-12)
+    # no electron momentum: the Compton line
+    assert oracle.doppler_energy(60.0, 1.0 + 60.0 / ME, 1.0, 0.0) == pytest.approx(60.0 / (1.0 + 60.0 / ME))
+
+
+def test_level2_shells_and_yields(oracle):
+    for Z in (1, 6, 8, 15, 20, 53, 74):
+        e, b, m = oracle.compton_shells(Z)
+        assert e.sum() == pytest.approx(Z)
+        assert np.all(np.diff(b) < 0)  # inner shells bound more tightly
+        assert b[0] == pytest.approx(oracle.lib().or_k_edge(Z) if Z > 1 else 13.605693122994e-3)
+        assert np.allclose(m, np.sqrt(b / 13.605693122994e-3) / 137.035999084, rtol=1e-9)
+    # K fluorescence yields of the Bambynek fit: calcium ~0.16, tungsten ~0.96
+    assert oracle.lib().or_fluorescence_yield_k(20) == pytest.approx(0.163, abs=0.005)
+    assert oracle.lib().or_fluorescence_yield_k(74) == pytest.approx(0.957, abs=0.005)
+
+
+@pytest.mark.parametrize("E", [20.0, 60.0, 140.0])
+def test_level2_compton_is_doppler_broadened(oracle, E):
+    rng = np.random.default_rng(int(E))
+    n = 20000
+    U = parity.uniforms_f32_exact(rng, (n, 1024))
+    d_rel = []
+    for i in range(n):
+        Ep, cost, used = oracle.sample_compton(E, P.WATER, 2, U[i])
+        Ec = E / (1.0 + E / ME * (1.0 - cost))
+        assert used < 1024
+        assert 0.0 < Ep < E
+        d_rel.append((Ep - Ec) / Ec)
+    d_rel = np.asarray(d_rel)
+    # broadened around the Compton line: centred, with a spread of a few per cent or less
+    assert abs(np.median(d_rel)) < 2e-3
+    assert 1e-4 < np.std(d_rel) < 0.05
+    # level 1 returns the Compton line exactly
+    Ep, cost, _ = oracle.sample_compton(E, P.WATER, 1, U[0])
+    assert Ep == pytest.approx(E / (1.0 + E / ME * (1.0 - cost)), rel=1e-12)
+
+
+def test_level2_photoelectric_fluorescence(oracle):
+    calcium = {20: 1.0}
+    rng = np.random.default_rng(9)
+    n = 40000
+    U = parity.uniforms_f32_exact(rng, (n, 8))
+    ka = oracle.lib().or_k_alpha(20)
+    out = np.array([oracle.sample_photoelectric(60.0, calcium, U[i])[:2] for i in range(n)])
+    emitted = out[:, 0] > 0
+    assert np.all(out[emitted, 0] == ka)
+    p = (1.0 - 1.0 / 7.0) * oracle.lib().or_fluorescence_yield_k(20)
+    assert emitted.mean() == pytest.approx(p, abs=5 * np.sqrt(p * (1 - p) / n))
+    # isotropic: dz uniform in [-1, 1]
+    assert abs(out[emitted, 1].mean()) < 0.03 and out[emitted, 1].var() == pytest.approx(1 / 3, abs=0.02)
+    # below the K edge, and for water (oxygen's K-alpha is under the 1 keV cutoff): no photon
+    assert all(oracle.sample_photoelectric(3.0, calcium, U[i])[0] == 0.0 for i in range(200))
+    assert all(oracle.sample_photoelectric(60.0, P.WATER, U[i])[0] == 0.0 for i in range(200))
+
+
+def test_oracle_level2_transport_conserves_energy(oracle):
+    ph = parity.small_cylinder()
+    w = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials, 2)
+    st = w.run(P.dx_beam_params(particles=4000, exposures=5), threads=4)
+    e, _, _ = w.tally()
+    assert st["n_histories"] == 20000 and st["n_errors"] == 0
+    assert st["n_fluorescence"] > 0  # the bone insert holds calcium
+    assert e.sum() + st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-12)

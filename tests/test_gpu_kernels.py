@@ -87,11 +87,11 @@ def test_siddon_bit_exact_and_path_lengths(gpu, oracle, dims, spacing):
 COMPOSITIONS = [P.WATER, P.BONE, P.LUNG, {53: 1.0}]
 
 
-@pytest.mark.parametrize("correction", [0, 1])
+@pytest.mark.parametrize("correction", [0, 1, 2])
 @pytest.mark.parametrize("zw", COMPOSITIONS)
 def test_compton_sampler_matches_oracle(gpu, oracle, zw, correction):
     rng = np.random.default_rng(5 + correction)
-    n, stride = 4000, 96
+    n, stride = 4000, (96 if correction < 2 else 1024)  # level 2 also draws shells and momenta
     E = rng.uniform(1.0, 150.0, n)
     U = parity.uniforms_f32_exact(rng, (n, stride))
     eg, cg, ug = gpu.sample_compton(E, zw, correction, U)
@@ -103,6 +103,24 @@ def test_compton_sampler_matches_oracle(gpu, oracle, zw, correction):
         same += 1
         assert abs(eg[i] - eo) <= 1e-6 * eo
         assert abs(cg[i] - co) <= 1e-6
+    assert same >= 0.998 * n
+
+
+@pytest.mark.parametrize("zw", COMPOSITIONS + [{20: 1.0}, {74: 1.0}])
+def test_photoelectric_fluorescence_matches_oracle(gpu, oracle, zw):
+    rng = np.random.default_rng(23)
+    n, stride = 4000, 8
+    E = rng.uniform(1.0, 150.0, n)
+    U = parity.uniforms_f32_exact(rng, (n, stride))
+    eg, dg, ug = gpu.sample_photoelectric(E, zw, U)
+    same = 0
+    for i in range(n):
+        eo, do, uo = oracle.sample_photoelectric(E[i], zw, U[i])
+        if uo != ug[i]:
+            continue
+        same += 1
+        assert abs(eg[i] - eo) <= 1e-6 * max(eo, 1.0)
+        assert abs(dg[i] - do) <= 1e-6
     assert same >= 0.998 * n
 
 

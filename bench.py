@@ -59,6 +59,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--tracking", choices=list(TRACKING), default="woodcock")
     p.add_argument("--macro-cell", type=int, default=16, help="macro-cell edge in voxels (macro tracking)")
+    p.add_argument("--woodcock-steps", type=int, default=0,
+                   help="Woodcock steps a lane takes between regroupings (0: library default)")
+    p.add_argument("--interact-batch", type=int, default=0)
+    p.add_argument("--refill-batch", type=int, default=0)
     p.add_argument("--correction", type=int, choices=[0, 1, 2], default=1,
                    help="bound-electron correction: 0 free electrons, 1 form factors (the reference's default), "
                         "2 impulse approximation + fluorescence")
@@ -250,7 +254,9 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     def run_opts(seed):
-        return G.run_options(seed=seed, stream=rank, tracking=TRACKING[args.tracking], macro_cell=args.macro_cell)
+        return G.run_options(seed=seed, stream=rank, tracking=TRACKING[args.tracking], macro_cell=args.macro_cell,
+                             woodcock_steps=args.woodcock_steps, interact_batch=args.interact_batch,
+                             refill_batch=args.refill_batch)
 
     def step(seed):
         flush.fill_(float(seed))

@@ -159,6 +159,7 @@ typedef struct {
     int32_t interact_batch; /* parked scatterings a warp gathers before sampling them, 0 = default */
     int32_t refill_batch;   /* dead lanes a warp gathers before starting new histories, 0 = default */
     int32_t macro_cell;     /* MACRO tracking: cell edge in voxels, 0 = default (16) */
+    int32_t woodcock_steps; /* WOODCOCK tracking: steps a lane takes between regroupings, 0 = default */
 } dxmcg_run_options;
 
 typedef struct {
@@ -245,8 +246,9 @@ DXMCG_API void dxmcg_batch_destroy(dxmcg_batch* b);
  * No counterpart in the reference.  Times the transport kernel on
  * sample_histories (0: 2^24) histories from the middle of the beam for each
  * block size {128, 256} x interact batch {8, 12, 16, 24} x refill batch
- * {4, 8, 16}, depositing into a scratch tally (the world's dose is untouched),
- * and writes the fastest block_size / interact_batch / refill_batch into *opts
+ * {4, 8, 16} x Woodcock steps per phase {8, 16} (Woodcock tracking only),
+ * depositing into a scratch tally (the world's dose is untouched), and writes the
+ * fastest block_size / interact_batch / refill_batch / woodcock_steps into *opts
  * (blocks_per_sm = 0: all resident blocks).  histories_per_second may be NULL. */
 DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_options* opts,
     uint64_t sample_histories, double* histories_per_second);

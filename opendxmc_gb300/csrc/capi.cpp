@@ -255,6 +255,7 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o, bool b
     s.grid = std::max(1, sms) * per;
     s.interact_batch = std::min(32, std::max(0, o.interact_batch));
     s.refill_batch = std::min(32, std::max(0, o.refill_batch));
+    s.woodcock_steps = std::min(64, std::max(0, o.woodcock_steps));
     return s;
 }
 
@@ -1092,6 +1093,7 @@ DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_o
     static const int kBlocks[] = { 128, 256 };
     static const int kInteract[] = { 8, 12, 16, 24 };
     static const int kRefill[] = { 4, 8, 16 };
+    static const int kWoodcock[] = { 8, 16 };
     float warm = 0.0f;
     rc = trial(chooseShape(w, o), warm);
     if (rc != DXMCG_OK)
@@ -1100,29 +1102,34 @@ DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_o
     dxmcg_run_options bestOpt = o;
     for (int blk : kBlocks)
         for (int ib : kInteract)
-            for (int rb : kRefill) {
-                dxmcg_run_options t = o;
-                t.block_size = blk;
-                t.blocks_per_sm = 0;
-                t.interact_batch = ib;
-                t.refill_batch = rb;
-                const LaunchShape shape = chooseShape(w, t);
-                float m = 0.0f, m2 = 0.0f;
-                rc = trial(shape, m);
-                if (rc == DXMCG_OK)
-                    rc = trial(shape, m2);
-                if (rc != DXMCG_OK)
-                    return rc;
-                const float tmin = std::min(m, m2);
-                if (best == 0.0f || tmin < best) {
-                    best = tmin;
-                    bestOpt = t;
+            for (int rb : kRefill)
+                for (int ws : kWoodcock) {
+                    dxmcg_run_options t = o;
+                    t.block_size = blk;
+                    t.blocks_per_sm = 0;
+                    t.interact_batch = ib;
+                    t.refill_batch = rb;
+                    t.woodcock_steps = o.tracking == DXMCG_TRACK_WOODCOCK ? ws : 0;
+                    if (o.tracking != DXMCG_TRACK_WOODCOCK && ws != kWoodcock[0])
+                        continue;
+                    const LaunchShape shape = chooseShape(w, t);
+                    float m = 0.0f, m2 = 0.0f;
+                    rc = trial(shape, m);
+                    if (rc == DXMCG_OK)
+                        rc = trial(shape, m2);
+                    if (rc != DXMCG_OK)
+                        return rc;
+                    const float tmin = std::min(m, m2);
+                    if (best == 0.0f || tmin < best) {
+                        best = tmin;
+                        bestOpt = t;
+                    }
                 }
-            }
     opts->block_size = bestOpt.block_size;
     opts->blocks_per_sm = 0;
     opts->interact_batch = bestOpt.interact_batch;
     opts->refill_batch = bestOpt.refill_batch;
+    opts->woodcock_steps = bestOpt.woodcock_steps;
     if (histories_per_second)
         *histories_per_second = best > 0.0f ? static_cast<double>(n) / (best * 1e-3) : 0.0;
     return DXMCG_OK;

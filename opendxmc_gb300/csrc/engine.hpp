@@ -135,6 +135,7 @@ struct LaunchShape {
     int block = 256;
     int refill_batch = 0;   // dead lanes a warp gathers before starting new histories (0: default)
     int interact_batch = 0; // parked lanes a warp gathers before running scatterings (0: default)
+    int woodcock_steps = 0; // Woodcock steps per lane and step phase (0: default)
 };
 
 // kernels (transport.cu)

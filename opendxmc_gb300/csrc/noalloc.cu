@@ -248,6 +248,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     shape.grid = std::max(1, sms) * (o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, resident) : resident);
     shape.interact_batch = std::min(32, std::max(0, o.interact_batch));
     shape.refill_batch = std::min(32, std::max(0, o.refill_batch));
+    shape.woodcock_steps = std::min(64, std::max(0, o.woodcock_steps));
 
     const auto t0 = std::chrono::steady_clock::now();
     cudaError_t le = cudaSuccess;

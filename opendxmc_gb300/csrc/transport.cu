@@ -266,7 +266,7 @@ namespace {
     template <int TRACKING, bool PACKED, bool MULTI>
     __global__ void __launch_bounds__(256) transportKernel(const DevJob J0, const DevJob* __restrict__ jobs,
         const unsigned long long* __restrict__ offsets, int nJobs, unsigned long long h_end,
-        DevCounters* __restrict__ ctr, int refillBatch, int interactBatch)
+        DevCounters* __restrict__ ctr, int refillBatch, int interactBatch, int woodcockSteps)
     {
         int jid = 0;
         // event counters per warp (no block-wide barrier: warps finish independently)
@@ -444,10 +444,17 @@ namespace {
                 bool escaped = false;
                 uint32_t v = 0;
                 int m = 0;
-                bool real;
-                if (TRACKING == DXMCG_TRACK_WOODCOCK)
-                    real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
-                else if (TRACKING == DXMCG_TRACK_SIDDON)
+                bool real = false;
+                if (TRACKING == DXMCG_TRACK_WOODCOCK) {
+                    // several steps per phase: most are virtual, and each phase boundary
+                    // costs the warp its votes; a lane stops at a real collision or escape
+                    for (int k = 0;;) {
+                        real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
+                        if (real || escaped || ++k >= woodcockSteps)
+                            break;
+                        ++steps;
+                    }
+                } else if (TRACKING == DXMCG_TRACK_SIDDON)
                     real = siddonFlight<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
                 else
                     real = macroFlight<PACKED>(J, ph, rng, ec, cx, cy, cz, escaped, v, m, visits, crossings, err);
@@ -537,7 +544,7 @@ namespace {
 
 namespace {
     using TransportFn = void (*)(const DevJob, const DevJob*, const unsigned long long*, int, unsigned long long,
-        DevCounters*, int, int);
+        DevCounters*, int, int, int);
 
     // kernel instance for a tracking mode on the packed (world) or unpacked
     // (caller-owned arrays) voxel layout, single job or a batch of jobs;
@@ -574,7 +581,8 @@ namespace {
             return cudaErrorInvalidValue;
         const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
         const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
-        fn<<<shape.grid, shape.block, 0, s>>>(job, jobs, offsets, nJobs, h_end, ctr, refill, interact);
+        const int wsteps = shape.woodcock_steps > 0 ? shape.woodcock_steps : 16;
+        fn<<<shape.grid, shape.block, 0, s>>>(job, jobs, offsets, nJobs, h_end, ctr, refill, interact, wsteps);
         return cudaGetLastError();
     }
 

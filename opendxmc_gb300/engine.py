@@ -75,7 +75,7 @@ def beam_exposures(params: dict) -> list[dict]:
 
 def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_size=0, blocks_per_sm=0,
                 chunk_log2=0, hist_begin=0, hist_end=0, interact_batch=0, refill_batch=0,
-                macro_cell=0) -> N.RunOptions:
+                macro_cell=0, woodcock_steps=0) -> N.RunOptions:
     o = N.RunOptions()
     o.seed = seed
     o.stream = stream
@@ -89,6 +89,7 @@ def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_
     o.interact_batch = interact_batch
     o.refill_batch = refill_batch
     o.macro_cell = macro_cell
+    o.woodcock_steps = woodcock_steps
     return o
 
 

@@ -148,7 +148,8 @@ class RunOptions(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("stream", C.c_uint32), ("tracking", C.c_int32), ("normalize", C.c_int32),
                 ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk_histories_log2", C.c_int32),
                 ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64), ("interact_batch", C.c_int32),
-                ("refill_batch", C.c_int32), ("macro_cell", C.c_int32)]
+                ("refill_batch", C.c_int32), ("macro_cell", C.c_int32),
+                ("woodcock_steps", C.c_int32)]
 
 
 class Stats(C.Structure):

@@ -113,6 +113,26 @@ def test_level2_impulse_approximation_and_fluorescence(gpu, oracle):
     assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
 
 
+@pytest.mark.parametrize("steps", [2, 5])
+def test_woodcock_steps_per_phase_keep_every_history(c1, gpu, steps):
+    """Several Woodcock steps per step phase change only when a lane's work runs,
+    not what it draws: every history makes the same decisions, so the counts are
+    equal and the per-voxel sums equal up to the order of the FP64 atomics."""
+    ph, gw, _ = c1
+    beam = P.dx_beam_params(particles=100_000, exposures=10)
+    gw.clear()
+    s1 = gw.run(beam, gpu.run_options(seed=3, stream=1, woodcock_steps=1))
+    e1, q1, n1 = gw.tally()
+    gw.clear()
+    s2 = gw.run(beam, gpu.run_options(seed=3, stream=1, woodcock_steps=steps))
+    e2, q2, n2 = gw.tally()
+    for k in ("n_histories", "n_visits", "n_photo", "n_compton", "n_rayleigh", "n_cutoff", "n_interacted"):
+        assert s1[k] == s2[k], k
+    np.testing.assert_array_equal(n1, n2)
+    np.testing.assert_allclose(e2, e1, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(q2, q1, rtol=1e-12, atol=0)
+
+
 def test_energy_conservation(c1, gpu):
     ph, gw, ow = c1
     gw.clear()

@@ -41,7 +41,7 @@ METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "
 WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 materials, +-2% density jitter), "
             "120 kVp 6 mm Al + body bowtie, pitch 1.0, 40 mm collimation, 200 mm scan, 1e9 histories")
 # dram__bytes_read.sum + dram__bytes_write.sum of one full transport launch
-# (67,000,320 histories of this workload: 2.60 GB read + 1.01 GB written), from the
+# (67,000,320 histories of this workload: 2.603 GB read + 1.008 GB written), from the
 # 1-pass ncu capture summarised in profiles/transport_kernel_torso.md.  bench.py's
 # launches hold up to 2^26 histories, 0.2 % more than the captured one.
 TRAFFIC_BYTES_PER_LAUNCH = 3.61e9
@@ -67,6 +67,8 @@ def parse():
                    help="bound-electron correction: 0 free electrons, 1 form factors (the reference's default), "
                         "2 impulse approximation + fluorescence")
     p.add_argument("--small", action="store_true", help="denoise-experiment: a small quick configuration")
+    p.add_argument("--inference-dims", default="512,512,400",
+                   help="denoiser: x,y,z of the inference volume (multiples of 8)")
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
     p.add_argument("--workload", choices=["torso", "batch", "pipelines", "denoiser", "denoise-experiment"],
                    default="torso",
@@ -588,18 +590,21 @@ def run_denoiser(args):
         return statistics.median(ms)
 
     step_ms = timed(lambda: (net.backward(x, t, stream), net.adam(1e-4, stream)), max(args.steps, 5))
-    vol = torch.rand((1, 400, 512, 512, 16), device="cuda", generator=gen).to(torch.bfloat16)
-    out = torch.empty((1, 400, 512, 512), dtype=torch.float32, device="cuda")
+    ix, iy, iz = (int(v) for v in args.inference_dims.split(","))
+    vol = torch.rand((1, iz, iy, ix, 16), device="cuda", generator=gen).to(torch.bfloat16)
+    out = torch.empty((1, iz, iy, ix), dtype=torch.float32, device="cuda")
     inf_ms = timed(lambda: net.forward(vol, out, stream), max(2, args.steps // 2))
     peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"] if (ROOT / "MEASURED_PEAKS.json").exists() else 1900.0
     step_tf = train_per_vox * 8 * 64 ** 3 / (step_ms * 1e-3) / 1e12
-    inf_tf = fwd_per_vox * 512 * 512 * 400 / (inf_ms * 1e-3) / 1e12
+    inf_tf = fwd_per_vox * ix * iy * iz / (inf_ms * 1e-3) / 1e12
     print(json.dumps({
         "metric": "denoiser training step", "value": step_ms, "unit": "ms", "higher_is_better": False, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "dtype": "bf16", "data": "synthetic",
-        "config": {"workload": "3D conv encoder-decoder 16/32/64/128, batch 8 x 64^3 patches; inference 512x512x400"},
+        "config": {"workload": "3D conv encoder-decoder 16/32/64/128, batch 8 x 64^3 patches; "
+                               f"inference {ix}x{iy}x{iz}"},
         "train_step_ms": step_ms, "train_tflops": step_tf, "train_frac": step_tf / peak,
-        "inference_ms_512x512x400": inf_ms, "inference_tflops": inf_tf, "inference_frac": inf_tf / peak,
+        "inference_ms": inf_ms, "inference_dims": [ix, iy, iz], "inference_tflops": inf_tf,
+        "inference_frac": inf_tf / peak,
         "peak_bf16_tflops": peak, "params": net.n_params,
     }), flush=True)
 

@@ -410,6 +410,11 @@ DXMCG_API int dxmcg_sample_rayleigh(int n, const double* energies, const dxmcg_m
  * that leaves the atom (0: none) and the z cosine of its isotropic direction */
 DXMCG_API int dxmcg_sample_photoelectric(int n, const double* energies, const dxmcg_material* m,
     const double* uniforms, int u_stride, double* e_out, double* dz_out, int32_t* used);
+/* tcgen05 self-test (no counterpart in the reference): with A 128 x 16 and B0, B1
+ * N x 16 bf16 bit patterns (row-major, N = 16 or 32), d0 = A (B0 + B1)^T and
+ * d1 = A B1^T in FP32 [128][N], computed by three tensor-core MMAs into tensor memory */
+DXMCG_API int dxmcg_umma_probe(int N, const uint16_t* a, const uint16_t* b0, const uint16_t* b1, float* d0,
+    float* d1);
 /* source photons of histories [hist_begin, hist_begin + n): E, weight, grid-local pos[3], dir[3] */
 DXMCG_API int dxmcg_sample_source(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts, int n,
     double* out8);

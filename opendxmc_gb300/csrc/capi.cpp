@@ -1568,6 +1568,38 @@ DXMCG_API int dxmcg_sample_rayleigh(int n, const double* energies, const dxmcg_m
     return DXMCG_OK;
 }
 
+DXMCG_API int dxmcg_umma_probe(int N, const uint16_t* a, const uint16_t* b0, const uint16_t* b1, float* d0,
+    float* d1)
+{
+    if ((N != 16 && N != 32) || !a || !b0 || !b1 || !d0 || !d1)
+        return fail(DXMCG_ERR_ARGUMENT, "umma_probe: N must be 16 or 32, all arrays given");
+    DeviceBuffer<uint16_t> A, B0, B1;
+    DeviceBuffer<float> D0, D1;
+    DeviceBuffer<unsigned> st;
+    DXMCG_CUDA(A.alloc(128 * 16));
+    DXMCG_CUDA(B0.alloc(128 * 16));
+    DXMCG_CUDA(B1.alloc(128 * 16));
+    DXMCG_CUDA(D0.alloc(128 * N));
+    DXMCG_CUDA(D1.alloc(128 * N));
+    DXMCG_CUDA(st.alloc(1));
+    DXMCG_CUDA(cudaMemset(B0.p, 0, 128 * 16 * sizeof(uint16_t)));
+    DXMCG_CUDA(cudaMemset(B1.p, 0, 128 * 16 * sizeof(uint16_t)));
+    DXMCG_CUDA(cudaMemset(st.p, 0, sizeof(unsigned)));
+    DXMCG_CUDA(cudaMemcpy(A.p, a, 128 * 16 * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    DXMCG_CUDA(cudaMemcpy(B0.p, b0, N * 16 * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    DXMCG_CUDA(cudaMemcpy(B1.p, b1, N * 16 * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    cudaError_t e = launchUmmaProbe(A.p, B0.p, B1.p, N, D0.p, D1.p, st.p, nullptr);
+    if (e != cudaSuccess)
+        return cudaFail(e, "umma probe");
+    unsigned status = 0;
+    DXMCG_CUDA(cudaMemcpy(d0, D0.p, 128 * N * sizeof(float), cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(d1, D1.p, 128 * N * sizeof(float), cudaMemcpyDeviceToHost));
+    DXMCG_CUDA(cudaMemcpy(&status, st.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (status)
+        return fail(DXMCG_ERR_DEVICE, "umma probe: the tensor-core commit was not seen in time");
+    return DXMCG_OK;
+}
+
 DXMCG_API int dxmcg_sample_source(dxmcg_world* w, const dxmcg_beam* beam, const dxmcg_run_options* opts, int n,
     double* out8)
 {

@@ -155,6 +155,10 @@ cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, int
     int stride, float* e_out, float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const float* u, int stride, float* e_out,
     float* dz_out, int* used, cudaStream_t s);
+// tcgen05 interface self-test (conv_tc.cu): D0 = A (B0 + B1)^T, D1 = A B1^T, A 128 x 16,
+// B N x 16 (N = 16 or 32) bf16 row-major, D FP32 [128][N]; *status |= 1 on a timed-out wait
+cudaError_t launchUmmaProbe(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int N, float* D0, float* D1,
+    unsigned* status, cudaStream_t s);
 cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* u, int stride,
     float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s);

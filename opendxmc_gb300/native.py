@@ -41,7 +41,7 @@ EXPORTED = [
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_reset", "dxmcg_progress_continue",
     "dxmcg_progress_message",
     "dxmcg_siddon_trace", "dxmcg_philox", "dxmcg_history_stream", "dxmcg_sample_compton", "dxmcg_sample_rayleigh",
-    "dxmcg_sample_photoelectric",
+    "dxmcg_sample_photoelectric", "dxmcg_umma_probe",
     "dxmcg_sample_source",
 ]
 
@@ -239,6 +239,7 @@ def lib() -> C.CDLL:
         "dxmcg_sample_compton": (i, [i, pd, C.POINTER(Material), i, pd, i, pd, pd, pi32]),
         "dxmcg_sample_rayleigh": (i, [i, pd, C.POINTER(Material), pd, i, pd, pi32]),
         "dxmcg_sample_photoelectric": (i, [i, pd, C.POINTER(Material), pd, i, pd, pd, pi32]),
+        "dxmcg_umma_probe": (i, [i, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
         "dxmcg_sample_source": (i, [vp, C.POINTER(Beam), C.POINTER(RunOptions), i, pd]),
     }
     for name, (res, args) in sig.items():

@@ -200,3 +200,28 @@ def test_trained_denoiser_beats_plain_monte_carlo(gpu, torch):
     assert lv["denoised_rms_rel"] < 0.5 * lv["low_rms_rel"], lv
     # the same error level costs plain Monte Carlo many more histories
     assert (lv["low_rms_rel"] / lv["denoised_rms_rel"]) ** 2 > 4.0
+
+
+def _bf16_bits(x):
+    return (np.asarray(x, np.float32).view(np.uint32) >> 16).astype(np.uint16)
+
+
+@pytest.mark.parametrize("n", [16, 32])
+def test_tensor_core_probe_is_exact(gpu, n):
+    """The tcgen05 interface (shared-memory descriptors, TMEM accumulators, commit to an
+    mbarrier, the A-operand collector) on values whose products and sums are exact in
+    FP32: the tensor-core result must equal the FP64 product bit for bit."""
+    import ctypes as C
+    from opendxmc_gb300 import native as N
+
+    rng = np.random.default_rng(n)
+    a = rng.integers(-4, 5, (128, 16)) / 4.0
+    b0 = rng.integers(-4, 5, (n, 16)) / 4.0
+    b1 = rng.integers(-4, 5, (n, 16)) / 4.0
+    A, B0, B1 = (np.ascontiguousarray(_bf16_bits(v)) for v in (a, b0, b1))
+    d0 = np.zeros((128, n), np.float32)
+    d1 = np.zeros((128, n), np.float32)
+    N.check(N.lib().dxmcg_umma_probe(n, A.ctypes.data, B0.ctypes.data, B1.ctypes.data, d0.ctypes.data,
+                                     d1.ctypes.data))
+    np.testing.assert_array_equal(d1, a @ b1.T)
+    np.testing.assert_array_equal(d0, a @ (b0 + b1).T)

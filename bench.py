@@ -67,6 +67,8 @@ def parse():
                    help="bound-electron correction: 0 free electrons, 1 form factors (the reference's default), "
                         "2 impulse approximation + fluorescence")
     p.add_argument("--small", action="store_true", help="denoise-experiment: a small quick configuration")
+    p.add_argument("--conv-path", type=int, choices=[0, 1, 2], default=0,
+                   help="denoiser: 0 default, 1 tcgen05 tensor cores, 2 mma.sync")
     p.add_argument("--inference-dims", default="512,512,400",
                    help="denoiser: x,y,z of the inference volume (multiples of 8)")
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
@@ -569,7 +571,7 @@ def run_denoiser(args):
     G.set_device(0)
     torch.cuda.set_device(0)
     ch = (16, 32, 64, 128)
-    net = G.Denoiser(ch, seed=0)
+    net = G.Denoiser(ch, seed=0, conv_path=args.conv_path)
     fwd_per_vox, train_per_vox = DN.conv_flops(ch)
     gen = torch.Generator(device="cuda").manual_seed(0)
     x = torch.rand((8, 64, 64, 64, 16), device="cuda", generator=gen).to(torch.bfloat16)
@@ -606,6 +608,7 @@ def run_denoiser(args):
         "inference_ms": inf_ms, "inference_dims": [ix, iy, iz], "inference_tflops": inf_tf,
         "inference_frac": inf_tf / peak,
         "peak_bf16_tflops": peak, "params": net.n_params,
+        "conv_path": {0: "default (tcgen05)", 1: "tcgen05", 2: "mma.sync"}[args.conv_path],
     }), flush=True)
 
 

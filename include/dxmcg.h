@@ -345,6 +345,8 @@ typedef struct {
     int32_t levels;      /* 1..5 */
     int32_t channels[5]; /* per level, multiples of 16; channels[0] 16 or 32 */
     uint64_t seed;       /* He-normal initialisation */
+    int32_t conv_path;   /* 3x3x3 convolutions: 0 = default (1), 1 = tcgen05 tensor cores with
+                            accumulators in tensor memory, 2 = warp-level mma.sync */
 } dxmcg_denoiser_config;
 DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* config, dxmcg_denoiser** out);
 DXMCG_API void dxmcg_denoiser_destroy(dxmcg_denoiser* d);

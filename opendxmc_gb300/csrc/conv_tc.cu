@@ -1,6 +1,26 @@
 // conv_tc.cu -- tcgen05 (5th-generation tensor core) kernels of the dose denoiser.
 // This part has no counterpart in the reference.
 //
+// conv3TcKernel is the 3x3x3 convolution (forward, and the input gradient with
+// transposed, flipped weights) of channels-last bf16 tensors as an implicit GEMM on
+// the tensor cores.  A CTA computes an output brick of 8 (x) x 16 (y) x ZT (z)
+// voxels and NT output channels.  Per 16-channel input slice it stages
+//   * the zero-padded input halo of 10 x 18 x (ZT + 2) voxels as two planes, one per
+//     8-channel half: voxel (hz, hy, hx) of half h at h * plane + ((hz*18 + hy)*10 + hx)*16,
+//   * the slice's weights of all 27 taps: tap t, half h, output channel co at
+//     t * NT*32 + h * NT*16 + co * 16,
+// in the tensor cores' no-swizzle K-major layout, so that the A operand of a tap is
+// the halo seen through a descriptor: output row r = 8 y + x of z-slice o reads halo
+// voxel (o + dz + 1, y + dy + 1, x + dx + 1): 8 consecutive x are one core matrix,
+// consecutive y are 160 bytes apart (SBO), the channel halves one plane apart (LBO).
+// One M = 128 MMA per (output slice, tap), accumulating in TMEM column block o * NT.
+// With N = 16 or 32 an MMA is short, and MMAs issued by one thread go out one after
+// another, so each output slice has its own issuing warp (one elected thread),
+// which commits its 27 MMAs per input slice to the CTA's mbarrier (one arrival per
+// warp): measured on the 16-channel layers, a single issuing thread held the CTA to
+// one MMA per ~72 SM cycles.  After the last slice the warps read the accumulators
+// back (tcgen05.ld), add the bias, apply the ReLU and store bf16.
+//
 // ummaProbeKernel is the self-test of the inline-PTX interface in umma.cuh: one CTA
 // stages A (128 x 16) and two B tiles (N x 16) in the no-swizzle K-major layout,
 // issues three MMAs into two TMEM accumulators -- the first two sharing A through
@@ -11,6 +31,9 @@
 
 #include <cuda_runtime.h>
 
+#include <cuda_bf16.h>
+
+#include "denoiser.hpp"
 #include "engine.hpp"
 #include "umma.cuh"
 
@@ -93,7 +116,255 @@ namespace {
         }
     }
 
+    // ------------------------------------------------------------------ convolution
+    __device__ unsigned g_convTcError; // set when a commit was not seen in time
+
+    __device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src, bool valid)
+    {
+        const int n = valid ? 16 : 0;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+    }
+
+    template <int NT>
+    struct ConvTcShape {
+        static constexpr int ZT = NT == 64 ? 4 : 8;          // output z-slices per CTA
+        static constexpr int HZ = ZT + 2, HY = 18, HX = 10;  // halo extent
+        static constexpr int kVox = HZ * HY * HX;
+        static constexpr uint32_t kPlane = kVox * 16;        // one 8-channel half of the halo
+        static constexpr uint32_t kHalo = 2 * kPlane;
+        static constexpr uint32_t kTapBytes = NT * 32;
+        static constexpr uint32_t kWeights = 27 * kTapBytes;
+        static constexpr uint32_t kSmem = kHalo + kWeights;
+        static constexpr uint32_t kCols = ZT * NT <= 32 ? 32 : (ZT * NT <= 64 ? 64 : (ZT * NT <= 128 ? 128 : 256));
+    };
+
+    struct TcTile {
+        int b, z0, y0, x0;
+    };
+    template <int ZT>
+    __device__ __forceinline__ TcTile tcTileOf(int tile, int D, int H, int W)
+    {
+        const int nx = (W + 7) >> 3, ny = (H + 15) >> 4, nz = (D + ZT - 1) / ZT;
+        TcTile p;
+        p.x0 = (tile % nx) * 8;
+        tile /= nx;
+        p.y0 = (tile % ny) * 16;
+        tile /= ny;
+        p.z0 = (tile % nz) * ZT;
+        p.b = tile / nz;
+        return p;
+    }
+
+    template <int NT>
+    __global__ void __launch_bounds__(256) conv3TcKernel(const nn::ConvIn in, int D, int H, int W, int Cin,
+        const __nv_bfloat16* __restrict__ wgt, const float* __restrict__ bias, int Cout, int relu,
+        __nv_bfloat16* __restrict__ out)
+    {
+        using S = ConvTcShape<NT>;
+        constexpr int ZT = S::ZT;
+        extern __shared__ __align__(128) unsigned char smem[];
+        __shared__ __align__(8) uint64_t bar;
+        __shared__ uint32_t tmemBase;
+        const int t = threadIdx.x;
+        const int warp = t >> 5;
+        const TcTile p = tcTileOf<ZT>(blockIdx.x, D, H, W);
+        const int n0 = blockIdx.y * NT;
+        const int nSlices = Cin >> 4;
+        const uint32_t sbase = umma::smemAddr(smem);
+
+        if (warp == 0)
+            umma::tmemAlloc(&tmemBase, S::kCols);
+        if (t == 0)
+            umma::mbarInit(&bar, ZT); // one arrival per issuing warp
+        umma::fenceBeforeSync();
+        __syncthreads();
+        umma::fenceAfterSync();
+        const uint32_t tm = tmemBase;
+        bool ok = true;
+        int sl = 0;
+        for (; sl < nSlices && ok; ++sl) {
+            const int c0 = sl * 16;
+            // ---- stage the halo of this slice (from a, nearest-upsampled when halfA, or b)
+            const bool inA = c0 < in.ca;
+            const __nv_bfloat16* src = inA ? in.a : in.b;
+            const int cs = inA ? in.ca : in.cb;
+            const int cc = inA ? c0 : c0 - in.ca;
+            const bool half = inA && in.halfA;
+            const int Ds = half ? D >> 1 : D, Hs = half ? H >> 1 : H, Ws = half ? W >> 1 : W;
+            for (int i = t; i < 2 * S::kVox; i += 256) {
+                const int h = i / S::kVox, v = i - h * S::kVox;
+                const int hz = v / (S::HY * S::HX), hy = (v / S::HX) % S::HY, hx = v % S::HX;
+                const int gz = p.z0 + hz - 1, gy = p.y0 + hy - 1, gx = p.x0 + hx - 1;
+                const bool inside = gz >= 0 && gz < D && gy >= 0 && gy < H && gx >= 0 && gx < W;
+                const __nv_bfloat16* q = src;
+                if (inside) {
+                    const int sz = half ? gz >> 1 : gz, sy = half ? gy >> 1 : gy, sx = half ? gx >> 1 : gx;
+                    q = src + ((((static_cast<size_t>(p.b) * Ds + sz) * Hs + sy) * Ws + sx) * cs + cc + h * 8);
+                }
+                cpAsync16(sbase + h * S::kPlane + v * 16, q, inside);
+            }
+            // ---- and the slice's weights for all taps
+            const uint32_t wbase = sbase + S::kHalo;
+            for (int i = t; i < 27 * NT * 2; i += 256) {
+                const int co = i % NT, th = i / NT; // th = tap * 2 + h
+                const int tap = th >> 1, h = th & 1;
+                const bool valid = n0 + co < Cout;
+                const __nv_bfloat16* q
+                    = valid ? wgt + ((static_cast<size_t>(n0 + co) * 27 + tap) * Cin + c0 + h * 8) : wgt;
+                cpAsync16(wbase + tap * S::kTapBytes + h * (NT * 16) + co * 16, q, valid);
+            }
+            asm volatile("cp.async.commit_group;\n" ::);
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            umma::fenceProxyAsync();
+            __syncthreads();
+
+            // warp w < ZT issues the 27 MMAs of output slice o = w (one elected thread each):
+            // MMAs from one thread issue one after another, and slices are independent
+            if (warp < ZT && (t & 31) == 0) {
+                umma::fenceAfterSync();
+                constexpr uint32_t idesc = umma::instrDescriptorBf16(128, NT);
+                // descriptor start addresses are in 16-byte units in the low 14 bits (shared
+                // memory < 256 KB), so offsets are added to the descriptor directly
+                const int o = warp;
+                const uint64_t aSlice = umma::smemDescriptor(sbase, S::kPlane, S::HX * 16)
+                    + static_cast<uint64_t>(o * S::HY * S::HX); // halo plane o is dz = -1
+                const uint64_t bBase = umma::smemDescriptor(wbase, NT * 16, 128);
+                const uint32_t d = tm + o * NT;
+#pragma unroll
+                for (int tap = 0; tap < 27; ++tap) {
+                    const int dz1 = tap / 9, dy1 = (tap / 3) % 3, dx1 = tap % 3; // offsets + 1
+                    const uint64_t a = aSlice + static_cast<uint64_t>((dz1 * S::HY + dy1) * S::HX + dx1);
+                    umma::mmaBf16<umma::Collector::kNone>(d, a, bBase + tap * (S::kTapBytes >> 4), idesc,
+                        sl > 0 || tap > 0);
+                }
+                umma::commit(&bar);
+            }
+            // the stage is free again (and, after the last slice, the sums are final)
+            // once this slice's MMAs have completed: one thread polls the mbarrier, the
+            // other warps wait at the CTA barrier without taking issue slots
+            int done = 1;
+            if (t == 0)
+                done = umma::mbarWait(&bar, static_cast<uint32_t>(sl & 1), 1u << 24) ? 1 : 0;
+            ok = __syncthreads_and(done) != 0;
+        }
+        if (!ok && t == 0) {
+            atomicOr(&g_convTcError, 1u);
+            // let the MMAs in flight (those of slice sl - 1) finish before the tensor
+            // memory is given back
+            umma::mbarWait(&bar, static_cast<uint32_t>((sl - 1) & 1), 1u << 24);
+        }
+        __syncthreads();
+        umma::fenceAfterSync();
+
+        // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) for half the slices
+        if (ok) {
+            const int lane = t & 31;
+            const int row = 32 * (warp & 3) + lane;
+            const int y = p.y0 + (row >> 3), x = p.x0 + (row & 7);
+            const int oBegin = (warp >> 2) * (ZT / 2);
+            const bool inPlane = y < H && x < W;
+#pragma unroll 1
+            for (int c = 0; c < NT; c += 16) {
+                float bv[16];
+#pragma unroll
+                for (int k = 0; k < 16; ++k)
+                    bv[k] = bias ? __ldg(bias + n0 + c + k) : 0.0f;
+#pragma unroll 1
+                for (int o = oBegin; o < oBegin + ZT / 2; ++o) {
+                    float v[16];
+                    umma::tmemLoad16(tm + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + o * NT + c, v);
+                    const int z = p.z0 + o;
+                    if (inPlane && z < D) {
+                        uint4 pk[2];
+                        __nv_bfloat162* h2 = reinterpret_cast<__nv_bfloat162*>(pk);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) {
+                            float a0 = v[2 * k] + bv[2 * k], a1 = v[2 * k + 1] + bv[2 * k + 1];
+                            if (relu) {
+                                a0 = fmaxf(a0, 0.0f);
+                                a1 = fmaxf(a1, 0.0f);
+                            }
+                            h2[k] = __floats2bfloat162_rn(a0, a1);
+                        }
+                        uint4* d4 = reinterpret_cast<uint4*>(
+                            out + (((static_cast<size_t>(p.b) * D + z) * H + y) * W + x) * Cout + n0 + c);
+                        d4[0] = pk[0];
+                        d4[1] = pk[1];
+                    }
+                }
+            }
+        }
+        umma::fenceBeforeSync();
+        __syncthreads();
+        if (warp == 0) {
+            umma::fenceAfterSync();
+            umma::tmemFree(tm, S::kCols);
+        }
+        if (t == 0)
+            umma::mbarInval(&bar);
+    }
+
+    template <int NT>
+    cudaError_t launchTc(const nn::ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
+        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s)
+    {
+        using S = ConvTcShape<NT>;
+        const int tiles = B * ((D + S::ZT - 1) / S::ZT) * ((H + 15) / 16) * ((W + 7) / 8);
+        conv3TcKernel<NT><<<dim3(tiles, Cout / NT), 256, S::kSmem, s>>>(in, D, H, W, Cin, w, bias, Cout,
+            relu ? 1 : 0, out);
+        return cudaGetLastError();
+    }
+
 } // namespace
+
+namespace nn {
+    cudaError_t conv3TcConfigure()
+    {
+        cudaError_t e = cudaFuncSetAttribute(conv3TcKernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            ConvTcShape<16>::kSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(conv3TcKernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                ConvTcShape<32>::kSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(conv3TcKernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                ConvTcShape<64>::kSmem);
+        return e;
+    }
+
+    cudaError_t launchConv3Tc(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
+        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s)
+    {
+        if (Cin % 16 || Cout % 16 || (in.ca % 16) || (in.b && in.cb % 16) || in.ca + (in.b ? in.cb : 0) != Cin)
+            return cudaErrorInvalidValue;
+        if (Cout % 64 == 0)
+            return launchTc<64>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s);
+        if (Cout % 32 == 0)
+            return launchTc<32>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s);
+        return launchTc<16>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s);
+    }
+
+    int conv3TcCtas(int B, int D, int H, int W, int Cout)
+    {
+        const auto ctas = [&](int zt, int nt) {
+            return B * ((D + zt - 1) / zt) * ((H + 15) / 16) * ((W + 7) / 8) * (Cout / nt);
+        };
+        if (Cout % 64 == 0)
+            return ctas(ConvTcShape<64>::ZT, 64);
+        if (Cout % 32 == 0)
+            return ctas(ConvTcShape<32>::ZT, 32);
+        return ctas(ConvTcShape<16>::ZT, 16);
+    }
+
+    // reads and clears the device flag of timed-out commits (0: none)
+    cudaError_t conv3TcErrors(unsigned* flags)
+    {
+        unsigned zero = 0;
+        cudaError_t e = cudaMemcpyFromSymbol(flags, g_convTcError, sizeof(unsigned));
+        if (e == cudaSuccess && *flags)
+            e = cudaMemcpyToSymbol(g_convTcError, &zero, sizeof(unsigned));
+        return e;
+    }
+} // namespace nn
 
 cudaError_t launchUmmaProbe(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int N, float* D0, float* D1,
     unsigned* status, cudaStream_t s)

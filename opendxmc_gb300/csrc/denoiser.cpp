@@ -38,6 +38,8 @@ struct dxmcg_denoiser {
     DevBuf<bf16> pb, wt;
     long step = 0;
     bool configured = false;
+    bool tensorCores = true; // tcgen05 convolutions (else warp-level mma.sync)
+    int sms = 1;             // streaming multiprocessors of the device
 
     // activations and gradients of the current shape, per level
     int B = 0, D = 0, H = 0, W = 0;
@@ -108,11 +110,31 @@ int refreshWeights(dxmcg_denoiser* d, cudaStream_t s)
     return DXMCG_OK;
 }
 
+// tcgen05 for a convolution unless its grid would leave SMs without a CTA
+bool useTensorCores(const dxmcg_denoiser* d, int D, int H, int W, int Cout)
+{
+    return d->tensorCores && nn::conv3TcCtas(d->B, D, H, W, Cout) >= d->sms;
+}
+
 int conv(dxmcg_denoiser* d, int k, const nn::ConvIn& in, int l, bf16* out, cudaStream_t s)
 {
     const auto& ly = d->layers[k];
-    NN_CUDA(nn::launchConv3(in, d->B, d->D >> l, d->H >> l, d->W >> l, ly.cin, d->pb.p + ly.w, d->p.p + ly.b,
-        ly.cout, true, out, s));
+    const int Dl = d->D >> l, Hl = d->H >> l, Wl = d->W >> l;
+    const auto launch = useTensorCores(d, Dl, Hl, Wl, ly.cout) ? nn::launchConv3Tc : nn::launchConv3;
+    NN_CUDA(launch(in, d->B, Dl, Hl, Wl, ly.cin, d->pb.p + ly.w, d->p.p + ly.b, ly.cout, true, out, s));
+    return DXMCG_OK;
+}
+
+// DXMCG_OK unless a tcgen05 convolution gave up waiting for its tensor-core work
+// (the kernel then skipped its output); call after a synchronisation
+int tensorCoreStatus(dxmcg_denoiser* d)
+{
+    if (!d->tensorCores)
+        return DXMCG_OK;
+    unsigned flags = 0;
+    NN_CUDA(nn::conv3TcErrors(&flags));
+    if (flags)
+        return fail(DXMCG_ERR_DEVICE, "denoiser: a tensor-core convolution timed out waiting for its MMAs");
     return DXMCG_OK;
 }
 
@@ -171,9 +193,11 @@ int layerBack(dxmcg_denoiser* d, int k, const nn::ConvIn& xin, const bf16* y, co
     const int Dl = d->D >> l, Hl = d->H >> l, Wl = d->W >> l;
     NN_CUDA(nn::launchReluBackward(dy, y, d->dz.p, d->nvox(l), ly.cout, d->g.p + ly.b, s));
     NN_CUDA(nn::launchWgrad(xin, d->dz.p, d->B, Dl, Hl, Wl, ly.cin, ly.cout, d->g.p + ly.w, s));
-    if (dxOut)
-        NN_CUDA(nn::launchConv3(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr,
-            ly.cin, false, dxOut, s));
+    if (dxOut) {
+        const auto launch = useTensorCores(d, Dl, Hl, Wl, ly.cin) ? nn::launchConv3Tc : nn::launchConv3;
+        NN_CUDA(launch(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr, ly.cin, false,
+            dxOut, s));
+    }
     return DXMCG_OK;
 }
 
@@ -268,7 +292,7 @@ namespace nn {
         if (hostOut)
             NN_CUDA(cudaMemcpyAsync(hostOut, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
         NN_CUDA(cudaStreamSynchronize(s));
-        return DXMCG_OK;
+        return tensorCoreStatus(d);
     }
 } // namespace nn
 } // namespace dxmcg
@@ -287,12 +311,17 @@ DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* c, dxmcg_denois
             return fail(DXMCG_ERR_ARGUMENT, "denoiser_create: channels must be multiples of 16 up to 256");
     if (c->channels[0] != 16 && c->channels[0] != 32)
         return fail(DXMCG_ERR_ARGUMENT, "denoiser_create: channels[0] must be 16 or 32");
+    if (c->conv_path < 0 || c->conv_path > 2)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_create: conv_path must be 0, 1 or 2");
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1)
         return fail(DXMCG_ERR_NO_DEVICE, "denoiser_create: no CUDA device");
     auto d = std::make_unique<dxmcg_denoiser>();
     cudaGetDevice(&d->device);
     d->L = c->levels;
+    d->tensorCores = c->conv_path != 2;
+    if (cudaDeviceGetAttribute(&d->sms, cudaDevAttrMultiProcessorCount, d->device) != cudaSuccess || d->sms < 1)
+        d->sms = 1;
     for (int l = 0; l < d->L; ++l)
         d->ch[l] = c->channels[l];
     std::vector<std::pair<int, int>> shapes; // (cin, cout) in layer order
@@ -328,6 +357,7 @@ DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* c, dxmcg_denois
     for (int i = 0; i < d->ch[0]; ++i)
         h[d->head + i] = static_cast<float>(nh(rng));
     NN_CUDA(nn::conv3Configure());
+    NN_CUDA(nn::conv3TcConfigure());
     NN_CUDA(d->p.reserve(d->nParams));
     NN_CUDA(d->g.reserve(d->nParams));
     NN_CUDA(d->m.reserve(d->nParams));
@@ -443,6 +473,8 @@ DXMCG_API int dxmcg_denoiser_backward(dxmcg_denoiser* d, const void* input, cons
         NN_CUDA(cudaMemcpyAsync(&h, d->loss.p, sizeof(double), cudaMemcpyDeviceToHost, s));
         NN_CUDA(cudaStreamSynchronize(s));
         *loss = h / static_cast<double>(d->nvox(0));
+        if ((rc = tensorCoreStatus(d)) != DXMCG_OK)
+            return rc;
     }
     return DXMCG_OK;
 }

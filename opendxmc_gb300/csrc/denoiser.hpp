@@ -28,6 +28,15 @@ size_t conv3SmemBytes(int nt);
 size_t wgradSmemBytes(int nt);
 cudaError_t conv3Configure(); // opt the kernels into their shared-memory size (once per device)
 
+// tcgen05 (5th-generation tensor core) form of launchConv3 (conv_tc.cu); the same
+// arguments and result up to FP32 summation order
+cudaError_t conv3TcConfigure();
+cudaError_t launchConv3Tc(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
+    const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);
+cudaError_t conv3TcErrors(unsigned* flags);
+// CTAs of the tcgen05 launch for this shape (a grid under one CTA per SM leaves the
+// tensor cores of the other SMs idle: the caller then takes launchConv3)
+int conv3TcCtas(int B, int D, int H, int W, int Cout);
 // out = act(conv3(in) + bias), act = relu or identity; bias may be null
 cudaError_t launchConv3(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
     const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);

@@ -354,12 +354,13 @@ class Denoiser:
     device-memory container only): inputs bf16 [B, D, H, W, 16], targets and
     predictions float32 [B, D, H, W]."""
 
-    def __init__(self, channels=(16, 32, 64, 128), seed=0):
+    def __init__(self, channels=(16, 32, 64, 128), seed=0, conv_path=0):
         cfg = N.DenoiserConfig()
         cfg.levels = len(channels)
         for k, c in enumerate(channels):
             cfg.channels[k] = int(c)
         cfg.seed = seed
+        cfg.conv_path = conv_path
         h = C.c_void_p()
         N.check(N.lib().dxmcg_denoiser_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -68,7 +68,8 @@ class OrganDose(C.Structure):
 
 
 class DenoiserConfig(C.Structure):
-    _fields_ = [("levels", C.c_int32), ("channels", C.c_int32 * 5), ("seed", C.c_uint64)]
+    _fields_ = [("levels", C.c_int32), ("channels", C.c_int32 * 5), ("seed", C.c_uint64),
+                ("conv_path", C.c_int32)]
 
 
 class Material(C.Structure):

@@ -37,11 +37,12 @@ def make_case(seed, B=2, D=16, H=8, W=12):
     return x, t
 
 
-@pytest.fixture(scope="module")
-def case(gpu, torch):
+@pytest.fixture(scope="module", params=[1, 2], ids=["tcgen05", "mma_sync"])
+def case(gpu, torch, request):
+    """Both convolution paths: tcgen05 (tensor memory accumulators) and mma.sync."""
     net = OD.UNet(CH, in_channels=16, seed=5)
     net.params = net.params.astype(np.float32).astype(np.float64)  # the GPU's FP32 master copy
-    dn = gpu.Denoiser(CH, seed=1)
+    dn = gpu.Denoiser(CH, seed=1, conv_path=request.param)
     dn.set_params(net.params)
     x, t = make_case(7)
     xt = torch.tensor(x, dtype=torch.bfloat16, device="cuda")
@@ -68,6 +69,28 @@ def test_gradients_match_oracle(case):
         assert rel(g[w1:b1], gref[w1:b1]) < TOL, name + " bias"
     h0, h1, h2 = net.head
     assert rel(g[h0:h2], gref[h0:h2]) < TOL
+
+
+def test_tensor_core_convolutions_match_mma_sync(gpu, torch):
+    """The full 16/32/64/128 network on both convolution paths with the same
+    parameters: every output-channel tile width (16, 32, 64), partial y and z tiles,
+    upsampled-and-concatenated decoder inputs and the input-gradient convolutions
+    (up to 192 channels) give the same predictions and gradients up to FP32 summation
+    order and the bf16 roundings it moves."""
+    ch = (16, 32, 64, 128)
+    tc = gpu.Denoiser(ch, seed=4, conv_path=1)
+    ms = gpu.Denoiser(ch, seed=4, conv_path=2)
+    np.testing.assert_array_equal(tc.get_params(), ms.get_params())
+    x, t = make_case(13, B=2, D=24, H=40, W=16)
+    xt = torch.tensor(x, dtype=torch.bfloat16, device="cuda")
+    tt = torch.tensor(t, dtype=torch.float32, device="cuda")
+    p1 = tc.forward(xt).cpu().numpy()
+    p2 = ms.forward(xt).cpu().numpy()
+    assert rel(p1, p2) < 1e-2
+    l1 = tc.backward(xt, tt)
+    l2 = ms.backward(xt, tt)
+    assert abs(l1 / l2 - 1) < 1e-3
+    assert rel(tc.grads(), ms.grads()) < 2e-2
 
 
 def test_adam_step_matches_oracle(gpu, torch):

@@ -32,6 +32,7 @@
 #include <cuda_runtime.h>
 
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include "denoiser.hpp"
 #include "engine.hpp"
@@ -155,34 +156,45 @@ namespace {
         return p;
     }
 
+    // mapA / mapB: 5-D tensor maps (C, W, H, D, B) of the full-resolution inputs a and b
+    // with a box of (8, 10, 18, ZT + 2, 1), used when useTma: the box of channel half h
+    // lands as halo plane h.  Slices of an upsampled input (halfA) use cp.async.
     template <int NT>
     __global__ void __launch_bounds__(256) conv3TcKernel(const nn::ConvIn in, int D, int H, int W, int Cin,
         const __nv_bfloat16* __restrict__ wgt, const float* __restrict__ bias, int Cout, int relu,
-        __nv_bfloat16* __restrict__ out)
+        __nv_bfloat16* __restrict__ out, const __grid_constant__ CUtensorMap mapA,
+        const __grid_constant__ CUtensorMap mapB, int useTma)
     {
         using S = ConvTcShape<NT>;
         constexpr int ZT = S::ZT;
         extern __shared__ __align__(128) unsigned char smem[];
         __shared__ __align__(8) uint64_t bar;
+        __shared__ __align__(8) uint64_t tmaBar;
         __shared__ uint32_t tmemBase;
         const int t = threadIdx.x;
         const int warp = t >> 5;
         const TcTile p = tcTileOf<ZT>(blockIdx.x, D, H, W);
+        uint32_t tmaPhase = 0;
         const int n0 = blockIdx.y * NT;
         const int nSlices = Cin >> 4;
         const uint32_t sbase = umma::smemAddr(smem);
 
         if (warp == 0)
             umma::tmemAlloc(&tmemBase, S::kCols);
-        if (t == 0)
+        if (t == 0) {
             umma::mbarInit(&bar, ZT); // one arrival per issuing warp
+            umma::mbarInit(&tmaBar, 1);
+        }
         umma::fenceBeforeSync();
         __syncthreads();
         umma::fenceAfterSync();
         const uint32_t tm = tmemBase;
-        bool ok = true;
+        // 0: fine; kLateHalo / kLateMma: a bounded wait for the halo copies / the MMAs of
+        // slice sl gave up (the epilogue is skipped, the device error flag set)
+        enum { kFine = 0, kLateHalo = 1, kLateMma = 2 };
+        int failed = kFine;
         int sl = 0;
-        for (; sl < nSlices && ok; ++sl) {
+        for (; sl < nSlices; ++sl) {
             const int c0 = sl * 16;
             // ---- stage the halo of this slice (from a, nearest-upsampled when halfA, or b)
             const bool inA = c0 < in.ca;
@@ -191,7 +203,15 @@ namespace {
             const int cc = inA ? c0 : c0 - in.ca;
             const bool half = inA && in.halfA;
             const int Ds = half ? D >> 1 : D, Hs = half ? H >> 1 : H, Ws = half ? W >> 1 : W;
-            for (int i = t; i < 2 * S::kVox; i += 256) {
+            // TMA needs a 128-byte aligned destination (checked here, not assumed)
+            const bool tma = useTma && !half && (sbase & 127u) == 0u;
+            if (tma && t == 0) {
+                const CUtensorMap* m = inA ? &mapA : &mapB;
+                umma::mbarArriveExpectTx(&tmaBar, S::kHalo);
+                umma::tmaLoad5d(sbase, m, cc, p.x0 - 1, p.y0 - 1, p.z0 - 1, p.b, &tmaBar);
+                umma::tmaLoad5d(sbase + S::kPlane, m, cc + 8, p.x0 - 1, p.y0 - 1, p.z0 - 1, p.b, &tmaBar);
+            }
+            for (int i = t; i < (tma ? 0 : 2 * S::kVox); i += 256) {
                 const int h = i / S::kVox, v = i - h * S::kVox;
                 const int hz = v / (S::HY * S::HX), hy = (v / S::HX) % S::HY, hx = v % S::HX;
                 const int gz = p.z0 + hz - 1, gy = p.y0 + hy - 1, gx = p.x0 + hx - 1;
@@ -216,7 +236,15 @@ namespace {
             asm volatile("cp.async.commit_group;\n" ::);
             asm volatile("cp.async.wait_group 0;\n" ::: "memory");
             umma::fenceProxyAsync();
-            __syncthreads();
+            int staged = 1;
+            if (tma && t == 0)
+                staged = umma::mbarWait(&tmaBar, tmaPhase, 1u << 24) ? 1 : 0;
+            if (!__syncthreads_and(staged)) {
+                failed = kLateHalo; // no MMAs were issued for this slice
+                break;
+            }
+            if (tma)
+                tmaPhase ^= 1u;
 
             // warp w < ZT issues the 27 MMAs of output slice o = w (one elected thread each):
             // MMAs from one thread issue one after another, and slices are independent
@@ -245,13 +273,20 @@ namespace {
             int done = 1;
             if (t == 0)
                 done = umma::mbarWait(&bar, static_cast<uint32_t>(sl & 1), 1u << 24) ? 1 : 0;
-            ok = __syncthreads_and(done) != 0;
+            if (!__syncthreads_and(done)) {
+                failed = kLateMma;
+                break;
+            }
         }
+        const bool ok = failed == kFine;
         if (!ok && t == 0) {
             atomicOr(&g_convTcError, 1u);
-            // let the MMAs in flight (those of slice sl - 1) finish before the tensor
-            // memory is given back
-            umma::mbarWait(&bar, static_cast<uint32_t>((sl - 1) & 1), 1u << 24);
+            // what is still in flight must land before the shared and tensor memory are
+            // given back: the halo copies, or the MMAs, of slice sl
+            if (failed == kLateHalo)
+                umma::mbarWait(&tmaBar, tmaPhase, 1u << 24);
+            else
+                umma::mbarWait(&bar, static_cast<uint32_t>(sl & 1), 1u << 24);
         }
         __syncthreads();
         umma::fenceAfterSync();
@@ -300,8 +335,44 @@ namespace {
             umma::fenceAfterSync();
             umma::tmemFree(tm, S::kCols);
         }
-        if (t == 0)
+        if (t == 0) {
             umma::mbarInval(&bar);
+            umma::mbarInval(&tmaBar);
+        }
+    }
+
+    // cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+    PFN_cuTensorMapEncodeTiled_v12000 tensorMapEncoder()
+    {
+        static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+            void* p = nullptr;
+            cudaDriverEntryPointQueryResult q {};
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q)
+                    != cudaSuccess
+                || q != cudaDriverEntryPointSuccess)
+                p = nullptr;
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        }();
+        return fn;
+    }
+
+    // 5-D map (C, W, H, D, B) of a channels-last bf16 tensor with a halo box
+    // (8, 10, 18, hz, 1); false if it cannot be made (the kernel then uses cp.async)
+    bool haloTensorMap(CUtensorMap* m, const void* base, int B, int D, int H, int W, int C, int hz)
+    {
+        const auto encode = tensorMapEncoder();
+        if (!encode || !base || (reinterpret_cast<uintptr_t>(base) & 15u))
+            return false;
+        const cuuint64_t dims[5] = { static_cast<cuuint64_t>(C), static_cast<cuuint64_t>(W),
+            static_cast<cuuint64_t>(H), static_cast<cuuint64_t>(D), static_cast<cuuint64_t>(B) };
+        const cuuint64_t row = static_cast<cuuint64_t>(C) * 2;
+        const cuuint64_t strides[4] = { row, row * W, row * W * H, row * W * H * D };
+        const cuuint32_t box[5] = { 8, 10, 18, static_cast<cuuint32_t>(hz), 1 };
+        const cuuint32_t step[5] = { 1, 1, 1, 1, 1 };
+        return encode(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, step,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE)
+            == CUDA_SUCCESS;
     }
 
     template <int NT>
@@ -310,8 +381,15 @@ namespace {
     {
         using S = ConvTcShape<NT>;
         const int tiles = B * ((D + S::ZT - 1) / S::ZT) * ((H + 15) / 16) * ((W + 7) / 8);
+        // tensor maps of the full-resolution inputs (an upsampled a keeps cp.async)
+        CUtensorMap mapA {}, mapB {};
+        bool tma = true;
+        if (in.a && !in.halfA)
+            tma = haloTensorMap(&mapA, in.a, B, D, H, W, in.ca, S::HZ);
+        if (tma && in.b)
+            tma = haloTensorMap(&mapB, in.b, B, D, H, W, in.cb, S::HZ);
         conv3TcKernel<NT><<<dim3(tiles, Cout / NT), 256, S::kSmem, s>>>(in, D, H, W, Cin, w, bias, Cout,
-            relu ? 1 : 0, out);
+            relu ? 1 : 0, out, mapA, mapB, tma ? 1 : 0);
         return cudaGetLastError();
     }
 

@@ -122,6 +122,22 @@ namespace umma {
         return false;
     }
 
+    // ---- TMA: one tiled box of a 5-D tensor map into shared memory, completing on an
+    // mbarrier (the caller arms it with the byte count first)
+    __device__ __forceinline__ void mbarArriveExpectTx(uint64_t* bar, uint32_t bytes)
+    {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smemAddr(bar)), "r"(bytes)
+                     : "memory");
+    }
+    __device__ __forceinline__ void tmaLoad5d(uint32_t dstSmem, const void* tmap, int c0, int c1, int c2, int c3,
+        int c4, uint64_t* bar)
+    {
+        asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                     "%4, %5, %6}], [%7];\n" ::"r"(dstSmem),
+            "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smemAddr(bar))
+                     : "memory");
+    }
+
     // ---- TMEM -> registers: this warp's 32 lanes (lane base 32 x (warp % 4)), 16 / 32
     // consecutive FP32 columns per thread
     __device__ __forceinline__ void tmemLoad16(uint32_t taddr, float (&v)[16])

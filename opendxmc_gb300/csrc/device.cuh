@@ -38,10 +38,13 @@ namespace dev {
         }
     }
 
-    // (2k + 1) / 2^24 from the top 23 bits: exact in FP32 and FP64, never 0 or 1.
+    // (2k + 1) / 2^24 from the top 23 bits k: exact in FP32 and FP64, never 0 or 1.
+    // Formed as the float 1 + k / 2^23 (k in the mantissa) minus 1 - 2^-24; both are
+    // in [1/2, 2] of each other, so the difference is exact (Sterbenz) and no
+    // integer-to-float conversion is needed.
     __device__ __forceinline__ float toUniform(uint32_t x)
     {
-        return __uint2float_rn(((x >> 9) << 1) | 1u) * 5.9604644775390625e-8f;
+        return __fsub_rn(__uint_as_float(0x3f800000u | (x >> 9)), 0.99999994039535522461f);
     }
 
     // Stream of one history: a xoshiro128** generator (Blackman & Vigna 2018) whose

@@ -370,10 +370,15 @@ namespace {
                 const bool compton = st == kCompton;
                 const bool rayleigh = st == kRayleigh;
                 bool cut = false, fluor = false;
-                if (compton) {
-                    float cost;
-                    const float Ep = sampleCompton(ph.E, J.mats + pm, J.correction, rng, cost, err);
+                // the samplers diverge; the direction update they share runs once
+                float cost = 1.0f, Ep = ph.E;
+                if (compton)
+                    Ep = sampleCompton(ph.E, J.mats + pm, J.correction, rng, cost, err);
+                else if (rayleigh)
+                    cost = sampleRayleigh(ph.E, J.mats + pm, rng, err);
+                if (compton || rayleigh)
                     scatterDirection(ph.dx, ph.dy, ph.dz, cost, rng.u());
+                if (compton) {
                     const float e = ph.w * (ph.E - Ep);
                     deposit(J.tally, pv, e);
                     edep.add(e);
@@ -392,8 +397,6 @@ namespace {
                             ec.set(J, ph.E);
                     }
                 } else if (rayleigh) {
-                    const float cost = sampleRayleigh(ph.E, J.mats + pm, rng, err);
-                    scatterDirection(ph.dx, ph.dy, ph.dz, cost, rng.u());
                     st = kStepping;
                 } else if (st == kPhoto) {
                     // correction level 2: the atom may emit a K-alpha photon, which the lane

@@ -31,7 +31,10 @@ def oracle_world_on_packed(oracle, gw, ph, correction=1):
     """Oracle world fed the densities exactly as the device stores them."""
     d, m = gw.packed_density()
     np.testing.assert_array_equal(m, ph.material.ravel())
-    assert np.max(np.abs(d.astype(np.float64) / ph.density.ravel() - 1)) <= 2.0 ** -16
+    ref = ph.density.ravel()
+    pos = ref > 0
+    assert np.all(d[~pos] == 0)
+    assert np.max(np.abs(d[pos].astype(np.float64) / ref[pos] - 1), initial=0.0) <= 2.0 ** -16
     return oracle.World(ph.dims, ph.spacing, d.astype(np.float64), ph.material, ph.materials, correction)
 
 
@@ -326,6 +329,57 @@ def test_transparent_material_is_skipped(gpu):
     e, _, _ = gw.tally()
     assert e.sum() == 0 and st["n_interacted"] == 0
     assert st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-6)
+
+
+@pytest.mark.parametrize("dims,spacing", [((1, 1, 1), (12.0, 12.0, 12.0)), ((7, 5, 3), (1.3, 2.1, 3.7))])
+def test_degenerate_and_odd_grids_match_oracle(gpu, oracle, dims, spacing):
+    """A single voxel, and an odd-sized grid with anisotropic voxels and zero-density
+    voxels, both under a DX beam: shared streams give the oracle's counts and energy."""
+    rng = np.random.default_rng(sum(dims))
+    nx, ny, nz = dims
+    mat = rng.integers(0, 3, (nz, ny, nx)).astype(np.uint8)
+    dens = np.array([0.0012, 1.0, 1.92])[mat] * rng.uniform(0.9, 1.1, mat.shape)
+    if mat.size > 1:
+        dens.ravel()[::4] = 0.0  # empty voxels
+    ph = P.Phantom(dims, spacing, dens, mat, [P.AIR, P.WATER, P.BONE])
+    gw = gpu_world(gpu, ph)
+    ow = oracle_world_on_packed(oracle, gw, ph)
+    beam = P.dx_beam_params(particles=50_000, exposures=4, field_cm=30.0)
+    sg = gw.run(beam, gpu.run_options(seed=2, stream=5))
+    so = ow.run(beam, seed=2, stream=5)
+    assert sg["n_errors"] == 0
+    for k in ("n_histories", "n_missed"):
+        assert sg[k] == so[k], k
+    assert sg["n_photo"] + sg["n_compton"] > 0
+    for k in ("n_photo", "n_compton", "n_rayleigh", "n_interacted"):
+        assert sg[k] == pytest.approx(so[k], rel=5e-3, abs=3), k
+    e1, _, _ = gw.tally()
+    e2, _, _ = ow.tally()
+    assert e1.sum() == pytest.approx(e2.sum(), rel=5e-3)
+    assert e1.sum() + sg["e_escaped"] == pytest.approx(sg["e_source"], rel=1e-5)
+
+
+def test_beam_that_misses_the_grid(gpu):
+    """A pencil beam passing beside the grid: every history is missed, nothing is
+    deposited and all source energy escapes."""
+    ph = parity.small_cylinder()
+    gw = gpu_world(gpu, ph)
+    beam = {"type": 4, "energy_kev": 60.0, "particles_per_exposure": 10_000, "n_exposures": 1,
+            "position": [100.0, 100.0, 0.0], "cosines": [[0, 0, 1], [-1, 0, 0]]}
+    st = gw.run(beam, gpu.run_options(seed=1))
+    e, _, c = gw.tally()
+    assert st["n_histories"] == st["n_missed"] == 10_000
+    assert e.sum() == 0 and c.sum() == 0
+    assert st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-6)
+
+
+def test_zero_histories_rejected(gpu):
+    from opendxmc_gb300 import native as N
+
+    ph = parity.small_cylinder()
+    gw = gpu_world(gpu, ph)
+    with pytest.raises(N.DxmcgError, match="particles_per_exposure"):
+        gw.run(P.dx_beam_params(particles=0, exposures=2))
 
 
 def test_cancel_stops_between_launches(gpu):

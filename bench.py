@@ -44,6 +44,8 @@ WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 material
 # 1-pass ncu capture summarised in profiles/transport_kernel_torso.md.  bench.py's
 # launches hold up to 2^26 histories, 0.2 % more than the captured one.
 TRAFFIC_BYTES_PER_LAUNCH = 3.61e9
+# the same for a full launch of the 512x512x400 workload (--workload torso512); None until captured
+TRAFFIC_BYTES_PER_LAUNCH_512 = None
 
 
 def parse():
@@ -71,9 +73,11 @@ def parse():
     p.add_argument("--inference-dims", default="512,512,400",
                    help="denoiser: x,y,z of the inference volume (multiples of 8)")
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
-    p.add_argument("--workload", choices=["torso", "batch", "pipelines", "denoiser", "denoise-experiment"],
+    p.add_argument("--workload", choices=["torso", "torso512", "batch", "pipelines", "denoiser",
+                                          "denoise-experiment"],
                    default="torso",
-                   help="torso: the spiral-CT torso job; batch: 64 uneven DX/CBCT jobs in one persistent launch; "
+                   help="torso: the spiral-CT torso job (256x256x200); torso512: the 512x512x400 spiral-CT torso; "
+                        "batch: 64 uneven DX/CBCT jobs in one persistent launch; "
                         "pipelines: segmentation and organ dose table passes; denoiser: training step and "
                         "inference throughput")
     return p.parse_args()
@@ -97,14 +101,26 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def workload(histories: float):
+WORKLOAD_512 = ("spiral CT on seeded synthetic torso 512x512x400 @0.8x0.8x1.0 mm (6 materials, +-2% density "
+                "jitter), 120 kVp 6 mm Al + body bowtie, pitch 0.8, 80 mm collimation, 200 mm scan")
+
+
+def workload(histories: float, big: bool = False):
+    """(phantom, beam, histories per step, exposures): the 256x256x200 torso at pitch 1.0
+    and 40 mm collimation, or (big) the 512x512x400 torso at pitch 0.8 and 80 mm."""
+    from opendxmc_gb300 import engine as G
     from opendxmc_gb300 import phantoms as P
 
-    ph = P.torso_phantom(dims=(256, 256, 200), spacing=(0.15, 0.15, 0.15), seed=1)
-    n_exp = 360
+    if big:
+        ph = P.torso_phantom(dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), seed=1)
+        beam = P.ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=0.8, collimation_cm=8.0, scan_cm=20.0, particles=1)
+    else:
+        ph = P.torso_phantom(dims=(256, 256, 200), spacing=(0.15, 0.15, 0.15), seed=1)
+        beam = P.ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=1.0, collimation_cm=4.0, scan_cm=20.0, particles=1)
+    n_exp = len(G.beam_exposures(beam))
     ppe = int(-(-int(histories) // n_exp))
-    beam = P.ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=1.0, collimation_cm=4.0, scan_cm=20.0, particles=ppe)
-    return ph, beam, n_exp * ppe
+    beam["particles_per_exposure"] = ppe
+    return ph, beam, n_exp * ppe, n_exp
 
 
 class ClockSampler:
@@ -190,7 +206,12 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    ph, beam, _ = workload(args.histories)
+    from opendxmc_gb300 import build as B
+
+    if not B.LIB.exists():
+        B.build(verbose_ptxas=False)  # the exposure list comes from the library's host code
+    big = args.workload == "torso512"
+    ph, beam, _, _ = workload(args.histories, big)
     from oracle import oracle as O
 
     O.build()
@@ -218,7 +239,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_histories_per_step": per_step},
+        "config": {"workload": WORKLOAD_512 if big else WORKLOAD, "sample_histories_per_step": per_step},
         "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -245,7 +266,8 @@ def run_ours(args):
     import torch
 
     torch.cuda.set_device(local)
-    ph, beam, hist = workload(args.histories)
+    big = args.workload == "torso512"
+    ph, beam, hist, n_exp = workload(args.histories, big)
     gw = G.GpuWorld(ph.dims, ph.spacing, ph.materials, args.correction)
     gw.set_data(ph.density, ph.material)
     gw.build()
@@ -297,7 +319,7 @@ def run_ours(args):
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "peak_source": peak_kind,
-            "traffic": TRAFFIC_BYTES_PER_LAUNCH,
+            "traffic": TRAFFIC_BYTES_PER_LAUNCH_512 if big else TRAFFIC_BYTES_PER_LAUNCH,
             "alg_bytes_per_launch": alg_bytes / (args.steps * launches_per_step),
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step),
             "visits_per_history": visits / done, "crossings_per_history": crossings / done,
@@ -345,10 +367,12 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "grid": list(ph.dims), "voxel_mm": 1.5, "histories_per_step": hist,
-                       "exposures": 360, "tracking": args.tracking, "correction": args.correction,
+            "config": {"workload": WORKLOAD_512 if big else WORKLOAD, "grid": list(ph.dims),
+                       "voxel_mm": [0.8, 0.8, 1.0] if big else 1.5, "histories_per_step": hist,
+                       "exposures": n_exp, "tracking": args.tracking, "correction": args.correction,
                        "macro_cell_voxels": args.macro_cell if args.tracking == "macro" else None, "scoring": "fp64",
-                       "l2": "256 MB buffer written before every step; tally 420 MB > L2",
+                       "l2": "256 MB buffer written before every step; tally " + ("3.4 GB" if big else "420 MB")
+                             + " > L2",
                        "parallelism": f"replicas x{world} (independent Philox streams)"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps, "clocks": clk,

@@ -23,16 +23,44 @@ namespace {
     // ---------------------------------------------------------------- segmentation
     // Integer CT numbers in [kSegLutMin, kSegLutMin + kSegLutSize) read their result
     // from a table filled once per segmentation table with the same FP64 operations
-    // (on GB300 the two FP64 divisions per voxel would otherwise bound the pass);
-    // any other value is computed here.
-    __device__ __forceinline__ void segmentOne(double h, const SegTable& t, const double* __restrict__ lutD,
-        const uint8_t* __restrict__ lutM, uint8_t& m, double& d)
+    // (on GB300 the two FP64 divisions per voxel would otherwise bound the pass); the
+    // table sits in shared memory, and whether a value is such an integer is read from
+    // its IEEE-754 bits with integer operations (FP64 runs at a small fraction of the
+    // integer rate here).  Any other value is computed.
+
+    // table slot of h when h is an integer in the table's range (+-0 is 0; NaN, the
+    // infinities and subnormals are not)
+    __device__ __forceinline__ bool lutSlot(double h, int& k)
     {
-        if (lutD && h == rint(h) && h >= static_cast<double>(kSegLutMin)
-            && h < static_cast<double>(kSegLutMin + kSegLutSize)) {
-            const int k = static_cast<int>(h) - kSegLutMin;
-            m = __ldg(lutM + k);
-            d = __ldg(lutD + k);
+        const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(h));
+        const int e = static_cast<int>((b >> 52) & 0x7ffu) - 1023;
+        if (e < 0) {
+            if ((b << 1) != 0ull)
+                return false;
+            k = -kSegLutMin;
+            return true;
+        }
+        if (e > 13) // |h| >= 2^14, beyond every table entry
+            return false;
+        const unsigned long long mant = (b & 0xfffffffffffffull) | (1ull << 52);
+        const int frac = 52 - e;
+        if (mant & ((1ull << frac) - 1ull))
+            return false;
+        const long long mag = static_cast<long long>(mant >> frac);
+        const long long v = (b >> 63) ? -mag : mag;
+        if (v < kSegLutMin || v >= kSegLutMin + kSegLutSize)
+            return false;
+        k = static_cast<int>(v - kSegLutMin);
+        return true;
+    }
+
+    __device__ __forceinline__ void segmentOne(double h, const SegTable& t, const double* lutD, const uint8_t* lutM,
+        uint8_t& m, double& d)
+    {
+        int k;
+        if (lutD && lutSlot(h, k)) {
+            m = lutM[k];
+            d = lutD[k];
             return;
         }
         int i = 0;
@@ -47,49 +75,81 @@ namespace {
     // Four voxels per thread and iteration: 32 B of HU in, 4 B of material and 32 B of
     // density out with 16-byte / 4-byte vector accesses (the host checks alignment).
     __global__ void segmentKernel(const double* __restrict__ hu, size_t n, const SegTable t,
-        const double* __restrict__ lutD, const uint8_t* __restrict__ lutM, uint8_t* __restrict__ mat,
+        const double* __restrict__ gLutD, const uint8_t* __restrict__ gLutM, uint8_t* __restrict__ mat,
         double* __restrict__ dens, int vec)
     {
+        __shared__ double sD[kSegLutSize];
+        __shared__ uint8_t sM[kSegLutSize];
+        if (gLutD) {
+            for (int i = threadIdx.x; i < kSegLutSize; i += blockDim.x) {
+                sD[i] = __ldg(gLutD + i);
+                sM[i] = __ldg(gLutM + i);
+            }
+            __syncthreads();
+        }
+        const double* lutD = gLutD ? sD : nullptr;
         const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
         const size_t nq = n / 4;
         size_t q = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x;
         if (vec) {
             for (; q < nq; q += stride) {
-                const double2 a = reinterpret_cast<const double2*>(hu)[2 * q];
-                const double2 b = reinterpret_cast<const double2*>(hu)[2 * q + 1];
+                const double2 a = __ldcs(reinterpret_cast<const double2*>(hu) + 2 * q);
+                const double2 b = __ldcs(reinterpret_cast<const double2*>(hu) + 2 * q + 1);
                 uchar4 m;
                 double2 da, db;
-                segmentOne(a.x, t, lutD, lutM, m.x, da.x);
-                segmentOne(a.y, t, lutD, lutM, m.y, da.y);
-                segmentOne(b.x, t, lutD, lutM, m.z, db.x);
-                segmentOne(b.y, t, lutD, lutM, m.w, db.y);
-                reinterpret_cast<uchar4*>(mat)[q] = m;
-                reinterpret_cast<double2*>(dens)[2 * q] = da;
-                reinterpret_cast<double2*>(dens)[2 * q + 1] = db;
+                segmentOne(a.x, t, lutD, sM, m.x, da.x);
+                segmentOne(a.y, t, lutD, sM, m.y, da.y);
+                segmentOne(b.x, t, lutD, sM, m.z, db.x);
+                segmentOne(b.y, t, lutD, sM, m.w, db.y);
+                __stcs(reinterpret_cast<uchar4*>(mat) + q, m);
+                __stcs(reinterpret_cast<double2*>(dens) + 2 * q, da);
+                __stcs(reinterpret_cast<double2*>(dens) + 2 * q + 1, db);
             }
             q = 4 * nq + blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; // the tail
         }
         for (; q < n; q += stride)
-            segmentOne(hu[q], t, lutD, lutM, mat[q], dens[q]);
+            segmentOne(hu[q], t, lutD, sM, mat[q], dens[q]);
     }
 
     // ---------------------------------------------------------------- organ dose table
-    // Per-block histograms over the 256 labels in shared memory, flushed once per
-    // block.  Lanes that share a label are combined first (__match_any_sync); a
-    // warp whose 32 voxels carry one label -- the common case in organ maps --
-    // reduces by shuffles and touches shared memory once.
+    // Every warp takes a contiguous chunk of the volume, 32 consecutive voxels per
+    // step, so a lane sees long runs of one label in organ maps.  A lane keeps
+    // running sums for its current label and adds them to the block's shared-memory
+    // histograms only when the label changes; the block flushes once at the end.
+    // FP64 runs at a small fraction of the FP32 rate here, so the per-voxel FP64 work
+    // is one add for the density and one fused multiply-add for dose x density (array
+    // form) or one add of the tally energy (world form); the constant factors -- voxel
+    // volume, and mGy per keV/g -- multiply the block sums.
     struct OrganInputs {
         const uint8_t* organ;
         // array form: dose (any unit) and density per voxel
         const double* dose;
         const double* density;
-        // world form: tally and packed voxel words; dose = e * toDose / rho
+        // world form: tally and packed voxel words; dose x mass = e * toDose * volume
         const Tally* tally;
         const uint32_t* vox;
         double toDose;
         int airMask; // world form: dose of material-0 voxels counts as 0
         double voxelVolume;
     };
+
+    struct OrganRun {
+        unsigned key = 0xffffffffu;
+        unsigned count = 0;
+        double rho = 0.0, e = 0.0;
+    };
+
+    __device__ __forceinline__ void flushRun(OrganRun& r, unsigned* sCnt, double* sRho, double* sE)
+    {
+        if (r.count) {
+            atomicAdd(&sCnt[r.key], r.count);
+            atomicAdd(&sRho[r.key], r.rho);
+            atomicAdd(&sE[r.key], r.e);
+        }
+        r.count = 0;
+        r.rho = 0.0;
+        r.e = 0.0;
+    }
 
     template <bool WORLD>
     __global__ void organKernel(const OrganInputs in, size_t n, int nOrgans, unsigned long long* __restrict__ cnt,
@@ -104,54 +164,64 @@ namespace {
         }
         __syncthreads();
         const unsigned lane = threadIdx.x & 31u;
-        const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
-        // the loop bound is uniform per warp so that every lane reaches the warp votes
-        for (size_t base = blockIdx.x * static_cast<size_t>(blockDim.x) + (threadIdx.x & ~31u); base < n;
-             base += stride) {
-            const size_t i = base + lane;
-            unsigned key = 256u;
-            double rho = 0.0, e = 0.0;
-            if (i < n) {
-                const unsigned o = in.organ[i];
-                if (o < static_cast<unsigned>(nOrgans)) {
-                    key = o;
-                    if (WORLD) {
-                        const uint32_t w = in.vox[i];
-                        rho = static_cast<double>(__uint_as_float(w & 0xffffff00u));
-                        const bool masked = in.airMask && (w & 0xffu) == 0u;
-                        const double d = (rho > 0.0 && !masked) ? in.tally[i].e * (in.toDose / rho) : 0.0;
-                        e = d * (in.voxelVolume * rho);
-                    } else {
-                        rho = in.density[i];
-                        e = in.dose[i] * (in.voxelVolume * rho);
+        const size_t warps = static_cast<size_t>(gridDim.x) * (blockDim.x >> 5);
+        const size_t w = static_cast<size_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        const size_t groups = (n + 31) / 32;
+        const size_t g0 = groups * w / warps, g1 = groups * (w + 1) / warps;
+        constexpr int kBatch = 4; // 32-voxel steps whose loads are in flight together
+        OrganRun run;
+        for (size_t g = g0; g < g1; g += kBatch) {
+            unsigned o[kBatch];
+            double a[kBatch], b[kBatch];
+            uint32_t word[kBatch];
+#pragma unroll
+            for (int k = 0; k < kBatch; ++k) {
+                const size_t i = (g + k) * 32 + lane;
+                o[k] = 256u;
+                a[k] = b[k] = 0.0;
+                word[k] = 0u;
+                if (g + k < g1 && i < n) {
+                    o[k] = __ldcs(in.organ + i);
+                    if (o[k] < static_cast<unsigned>(nOrgans)) {
+                        if (WORLD) {
+                            word[k] = __ldcs(in.vox + i);
+                            a[k] = __ldcs(&in.tally[i].e);
+                        } else {
+                            a[k] = __ldcs(in.dose + i);
+                            b[k] = __ldcs(in.density + i);
+                        }
                     }
                 }
             }
-            const unsigned peers = __match_any_sync(kFull, key);
-            if (peers == kFull) {
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    rho += __shfl_xor_sync(kFull, rho, o);
-                    e += __shfl_xor_sync(kFull, e, o);
+            for (int k = 0; k < kBatch; ++k) {
+                if (o[k] >= static_cast<unsigned>(nOrgans))
+                    continue;
+                if (o[k] != run.key) {
+                    flushRun(run, sCnt, sRho, sE);
+                    run.key = o[k];
                 }
-                if (lane == 0 && key < 256u) {
-                    atomicAdd(&sCnt[key], 32u);
-                    atomicAdd(&sRho[key], rho);
-                    atomicAdd(&sE[key], e);
+                ++run.count;
+                if (WORLD) {
+                    const float rho = __uint_as_float(word[k] & 0xffffff00u);
+                    run.rho += static_cast<double>(rho);
+                    const bool masked = in.airMask && (word[k] & 0xffu) == 0u;
+                    if (rho > 0.0f && !masked)
+                        run.e += a[k];
+                } else {
+                    run.rho += b[k];
+                    run.e = fma(a[k], b[k], run.e);
                 }
-            } else if (key < 256u) {
-                if (lane == static_cast<unsigned>(__ffs(peers) - 1))
-                    atomicAdd(&sCnt[key], static_cast<unsigned>(__popc(peers)));
-                atomicAdd(&sRho[key], rho);
-                atomicAdd(&sE[key], e);
             }
         }
+        flushRun(run, sCnt, sRho, sE);
         __syncthreads();
+        const double eScale = WORLD ? in.toDose * in.voxelVolume : in.voxelVolume;
         for (int i = threadIdx.x; i < nOrgans; i += blockDim.x)
             if (sCnt[i]) {
                 atomicAdd(&cnt[i], static_cast<unsigned long long>(sCnt[i]));
                 atomicAdd(&sumRho[i], sRho[i]);
-                atomicAdd(&sumE[i], sE[i]);
+                atomicAdd(&sumE[i], sE[i] * eScale);
             }
     }
 

@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--inference-dims", default="512,512,400",
                    help="denoiser: x,y,z of the inference volume (multiples of 8)")
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
+    p.add_argument("--train-steps", type=int, default=0, help="denoise-experiment: training steps (0: default)")
+    p.add_argument("--lr-final", type=float, default=0.0, help="denoise-experiment: final learning rate (0: default)")
     p.add_argument("--workload", choices=["torso", "torso512", "batch", "pipelines", "denoiser",
                                           "denoise-experiment"],
                    default="torso",
@@ -654,6 +656,10 @@ def run_denoise_experiment(args):
     if args.small:
         kw = dict(dims=(128, 128, 96), spacing=(0.32, 0.32, 0.4), train_seeds=(11, 12), lows=(1e6, 1e7), high=1e8,
                   steps=60)
+    if args.train_steps:
+        kw["steps"] = args.train_steps
+    if args.lr_final:
+        kw["lr_final"] = args.lr_final
     out, net = DN.experiment(torch, log=lambda m: print(m, file=sys.stderr, flush=True), **kw)
     if args.save_weights:
         np.save(args.save_weights, net.get_params())

@@ -12,6 +12,10 @@ Sources (paths inside the reference project):
   data/phantoms/other/media.dat        same layout, row 53 is Water
   data/bowtiefilters/bowtiefilters.json           {filters: [{name, filterdata: [{angle, weight}]}]}
   data/bowtiefilters/bowtiefilters.json.template  same layout (body W3 120 kV)
+  src/libopendxmc/hdf5wrapper.cpp      the study file layout: root dataset names of
+                                       HDF5Wrapper::save(DataContainer), and per beam kind
+                                       the /beams/<Kind>Beams group and its attribute names
+                                       and types (read from the source text)
 """
 import json
 import re
@@ -52,12 +56,35 @@ def parse_bowties(path: Path) -> dict:
     return out
 
 
+def parse_hdf5_layout(path: Path) -> dict:
+    """Dataset names of the study save and, per beam save function, its group kind and
+    its attributes with their element type."""
+    src = path.read_text(errors="replace")
+    funcs = re.split(r"\nbool HDF5Wrapper::save\(", src)
+    datasets, beams = [], {}
+    for f in funcs[1:]:
+        head = f.split(")", 1)[0]
+        if "DataContainer" in head:
+            datasets = re.findall(r'names\[0\] = "(\w+)";', f.split("\n}\n", 1)[0])
+            continue
+        m = re.search(r'"/beams/(\w+)/1"', f)
+        if not m:
+            continue
+        body = f.split("\n}\n", 1)[0]
+        attrs = {}
+        for t, name in re.findall(r'saveAttribute<([\w:]+)>\(beamgroup, "(\w+)"', body):
+            attrs[name] = "uint64" if "uint64" in t else "double"
+        beams[m.group(1)] = attrs
+    return {"datasets": datasets, "beams": beams}
+
+
 def main():
     res = {
         "AM_media": parse_media(REF / "data/phantoms/icrp/AM/AM_media.dat"),
         "other_media": parse_media(REF / "data/phantoms/other/media.dat"),
         "bowtiefilters": parse_bowties(REF / "data/bowtiefilters/bowtiefilters.json"),
         "bowtie_template": parse_bowties(REF / "data/bowtiefilters/bowtiefilters.json.template"),
+        "hdf5_layout": parse_hdf5_layout(REF / "src/libopendxmc/hdf5wrapper.cpp"),
     }
     OUT.write_text(json.dumps(res, indent=1, sort_keys=True))
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes): {len(res['AM_media'])} AM media, "

@@ -112,15 +112,18 @@ namespace {
         ph.px = fmaf(s, ph.dx, ph.px);
         ph.py = fmaf(s, ph.dy, ph.py);
         ph.pz = fmaf(s, ph.dz, ph.pz);
-        if (!(ph.px >= 0.0f && ph.px < J.L[0] && ph.py >= 0.0f && ph.py < J.L[1] && ph.pz >= 0.0f
-                && ph.pz < J.L[2])) {
+        // voxel indices by rounding down; outside the grid one of them is negative
+        // (huge as unsigned) or >= its dimension (conversions saturate far away)
+        const int ix = __float2int_rd(ph.px * J.isp[0]);
+        const int iy = __float2int_rd(ph.py * J.isp[1]);
+        const int iz = __float2int_rd(ph.pz * J.isp[2]);
+        if ((static_cast<unsigned>(ix) >= static_cast<unsigned>(J.nx))
+            | (static_cast<unsigned>(iy) >= static_cast<unsigned>(J.ny))
+            | (static_cast<unsigned>(iz) >= static_cast<unsigned>(J.nz))) {
             escaped = true;
             return false;
         }
         ++visits;
-        const int ix = min(static_cast<int>(ph.px * J.isp[0]), J.nx - 1);
-        const int iy = min(static_cast<int>(ph.py * J.isp[1]), J.ny - 1);
-        const int iz = min(static_cast<int>(ph.pz * J.isp[2]), J.nz - 1);
         v = static_cast<uint32_t>(ix + J.nx * (iy + J.ny * iz));
         const float rho = voxelAt<PACKED>(J, v, m);
         if (m == DXMCG_TRANSPARENT_MATERIAL)

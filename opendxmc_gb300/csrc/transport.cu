@@ -1,8 +1,9 @@
 // transport.cu -- the persistent photon-transport kernel (sm_103a).
 //
-// Every lane owns one photon and is in one of four states: stepping, waiting for
-// a Compton interaction, waiting for a Rayleigh interaction, or dead.  Each loop
-// iteration of a warp has three phases whose branches are warp-uniform:
+// Every lane owns one photon and is in one of five states: stepping, waiting for
+// a Compton interaction, waiting for a Rayleigh interaction, waiting for the
+// fluorescence of a photoelectric absorption (correction level 2), or dead.  Each
+// loop iteration of a warp has three phases whose branches are warp-uniform:
 //
 //   refill    dead lanes start new histories (source sampling, entry into the
 //             grid) once at least `refillBatch` lanes are dead, from a warp-private
@@ -10,15 +11,19 @@
 //             head in chunks of kChunk (one atomic per chunk);
 //   interact  lanes waiting for an interaction run it together once at least
 //             `interactBatch` lanes wait (Compton: Kahn's rejection method for
-//             Klein-Nishina, then rejection on S(x)/Z; Rayleigh: element choice and
-//             analytic inversion of F^2, rejection on (1 + cos^2)/2);
-//   step      stepping lanes take one Woodcock step against the majorant mu_max(E)
-//             (or, in the regular-tracking variant, one free flight with exact
-//             Siddon path lengths); a real collision picks its type at once:
-//             photoelectric absorption is scored on the spot, scatterings park
-//             the lane until the next interact phase.
+//             Klein-Nishina, then rejection on S(x)/Z, and at level 2 the Doppler
+//             energy of a bound electron; Rayleigh: element choice and analytic
+//             inversion of F^2, rejection on (1 + cos^2)/2; fluorescence: K-shell
+//             vacancy and yield);
+//   step      stepping lanes take up to `woodcockSteps` Woodcock steps against the
+//             majorant mu_max(E), stopping at a real collision or an escape (or, in
+//             the regular-tracking variant, one free flight with exact Siddon path
+//             lengths; with macro cells, one flight against the cell majorants); a
+//             real collision picks its type at once: photoelectric absorption is
+//             scored on the spot below level 2, the other events park the lane
+//             until the next interact phase.
 //
-// Parking scatterings and batching refills regroups the expensive, divergent
+// Parking interactions and batching refills regroups the expensive, divergent
 // work so that it runs with many lanes active instead of one or two.  A history
 // draws its uniforms in a fixed order from its own stream, so its result does not
 // depend on when, or in which lane, each phase runs.

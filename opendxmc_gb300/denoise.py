@@ -133,15 +133,19 @@ class PatchSampler:
 
 def train(net: "G.Denoiser", sampler: PatchSampler, steps: int, lr: float = 1e-3, log_every: int = 0,
           lr_final: float | None = None, log=print):
-    """Adam on random patches; returns the loss history.  With lr_final the rate
-    decays geometrically from lr to lr_final."""
+    """Adam on random patches; returns the loss of every `every`-th step (reading the
+    loss back waits for the GPU, so it is not read on the others).  With lr_final the
+    rate decays geometrically from lr to lr_final."""
     losses = []
+    every = max(1, log_every // 20) if log_every else 16  # read the loss back on these steps only
     for s in range(steps):
         rate = lr if lr_final is None else lr * (lr_final / lr) ** (s / max(1, steps - 1))
         x, t = sampler.sample()
-        losses.append(net.train_step(x, t, rate))
+        loss = net.train_step(x, t, rate, want_loss=(s % every == every - 1) or s == steps - 1)
+        if loss is not None:
+            losses.append(loss)
         if log_every and (s + 1) % log_every == 0:
-            log(f"step {s + 1}: loss {np.mean(losses[-log_every:]):.4f}")
+            log(f"step {s + 1}: loss {np.mean(losses[-20:]):.4f}")
     return losses
 
 
@@ -268,7 +272,7 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
     out = {
         "dims": list(dims), "spacing_cm": list(spacing), "train_phantoms": len(train_seeds), "inputs": list(lows),
         "high": high, "train_steps": steps, "batch": batch, "patch": patch,
-        "final_loss": float(np.mean(losses[-100:])), "data_s": t_data, "data_mc_s": mc_s, "train_s": t_train,
+        "final_loss": float(np.mean(losses[-10:])), "data_s": t_data, "data_mc_s": mc_s, "train_s": t_train,
         "histories_per_s": rate, "reference_rms_rel": sigma_ref, "target_error": target_error,
         "plain_histories_to_target": n_plain, "plain_s_to_target": t_plain, "levels": levels,
         "denoised_s_to_target": best["total_s"] if best else None,

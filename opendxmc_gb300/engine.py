@@ -399,18 +399,21 @@ class Denoiser:
                                                C.c_void_p(out.data_ptr()), self._stream(stream)))
         return out
 
-    def backward(self, x, target, stream=None) -> float:
+    def backward(self, x, target, stream=None, want_loss: bool = True):
+        """Forward, L1 loss and gradients; returns the mean loss, or None without
+        want_loss (the call then only queues work and does not wait for the GPU)."""
         B, D, H, W, _ = x.shape
         loss = C.c_double(0)
         N.check(N.lib().dxmcg_denoiser_backward(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(target.data_ptr()),
-                                                B, D, H, W, C.byref(loss), self._stream(stream)))
-        return loss.value
+                                                B, D, H, W, C.byref(loss) if want_loss else None,
+                                                self._stream(stream)))
+        return loss.value if want_loss else None
 
     def adam(self, lr: float, stream=None) -> None:
         N.check(N.lib().dxmcg_denoiser_adam(self._h, C.c_float(lr), self._stream(stream)))
 
-    def train_step(self, x, target, lr: float, stream=None) -> float:
-        loss = self.backward(x, target, stream)
+    def train_step(self, x, target, lr: float, stream=None, want_loss: bool = True):
+        loss = self.backward(x, target, stream, want_loss)
         self.adam(lr, stream)
         return loss
 

@@ -430,7 +430,7 @@ def run_batch(args):
     def opts(j, seed):
         o = G.run_options(seed=seed, stream=j, tracking=trk, macro_cell=args.macro_cell,
                           block_size=tuned.block_size, interact_batch=tuned.interact_batch,
-                          refill_batch=tuned.refill_batch)
+                          refill_batch=tuned.refill_batch, woodcock_steps=tuned.woodcock_steps)
         return o
 
     batch = G.Batch([(w, sp["beam"], opts(j, 1)) for j, (w, sp) in enumerate(zip(worlds, specs))])
@@ -480,7 +480,8 @@ def run_batch(args):
                    "l2": "256 MB buffer written before every step; tallies 14 GB > L2",
                    "launch": "CUDA graph (counter reset + one persistent kernel) replayed per step"},
         "autotune": {"block_size": tuned.block_size, "interact_batch": tuned.interact_batch,
-                     "refill_batch": tuned.refill_batch, "trial_histories_per_s": tuned_rate, "seconds": t_tune,
+                     "refill_batch": tuned.refill_batch, "woodcock_steps": tuned.woodcock_steps,
+                     "trial_histories_per_s": tuned_rate, "seconds": t_tune,
                      "job": big},
         "sequential": {"value": seq_done / seq_dt, "unit": "histories/s", "calls": len(specs),
                        "path": "one dxmcg_transport_run per job"},

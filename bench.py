@@ -75,10 +75,11 @@ def parse():
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
     p.add_argument("--train-steps", type=int, default=0, help="denoise-experiment: training steps (0: default)")
     p.add_argument("--lr-final", type=float, default=0.0, help="denoise-experiment: final learning rate (0: default)")
-    p.add_argument("--workload", choices=["torso", "torso512", "batch", "pipelines", "denoiser",
+    p.add_argument("--workload", choices=["torso", "torso512", "c1", "batch", "pipelines", "denoiser",
                                           "denoise-experiment"],
                    default="torso",
                    help="torso: the spiral-CT torso job (256x256x200); torso512: the 512x512x400 spiral-CT torso; "
+                        "c1: the DX water cylinder (1e7 histories per step unless --histories); "
                         "batch: 64 uneven DX/CBCT jobs in one persistent launch; "
                         "pipelines: segmentation and organ dose table passes; denoiser: training step and "
                         "inference throughput")
@@ -103,17 +104,23 @@ def peaks():
     return 6800.0, "fallback"
 
 
+WORKLOAD_C1 = ("DX on a 128x128x64 water cylinder (16 cm, bone insert) at 1x1x2.5 mm, 70 kVp 2.5 mm Al, "
+               "10x10 cm field at 100 cm, 1e7 histories")
 WORKLOAD_512 = ("spiral CT on seeded synthetic torso 512x512x400 @0.8x0.8x1.0 mm (6 materials, +-2% density "
                 "jitter), 120 kVp 6 mm Al + body bowtie, pitch 0.8, 80 mm collimation, 200 mm scan")
 
 
-def workload(histories: float, big: bool = False):
+def workload(histories: float, big: bool = False, c1: bool = False):
     """(phantom, beam, histories per step, exposures): the 256x256x200 torso at pitch 1.0
-    and 40 mm collimation, or (big) the 512x512x400 torso at pitch 0.8 and 80 mm."""
+    and 40 mm collimation, (big) the 512x512x400 torso at pitch 0.8 and 80 mm, or (c1) the
+    DX water cylinder."""
     from opendxmc_gb300 import engine as G
     from opendxmc_gb300 import phantoms as P
 
-    if big:
+    if c1:
+        ph = P.water_cylinder_phantom()
+        beam = P.dx_beam_params(particles=1, exposures=10)
+    elif big:
         ph = P.torso_phantom(dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), seed=1)
         beam = P.ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=0.8, collimation_cm=8.0, scan_cm=20.0, particles=1)
     else:
@@ -213,7 +220,8 @@ def run_reference(args):
     if not B.LIB.exists():
         B.build(verbose_ptxas=False)  # the exposure list comes from the library's host code
     big = args.workload == "torso512"
-    ph, beam, _, _ = workload(args.histories, big)
+    c1 = args.workload == "c1"
+    ph, beam, _, _ = workload(args.histories, big, c1)
     from oracle import oracle as O
 
     O.build()
@@ -241,7 +249,8 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD_512 if big else WORKLOAD, "sample_histories_per_step": per_step},
+        "config": {"workload": WORKLOAD_C1 if c1 else (WORKLOAD_512 if big else WORKLOAD),
+                   "sample_histories_per_step": per_step},
         "cpu_baseline": {"value": value, "unit": "histories/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -269,7 +278,8 @@ def run_ours(args):
 
     torch.cuda.set_device(local)
     big = args.workload == "torso512"
-    ph, beam, hist, n_exp = workload(args.histories, big)
+    c1 = args.workload == "c1"
+    ph, beam, hist, n_exp = workload(args.histories, big, c1)
     gw = G.GpuWorld(ph.dims, ph.spacing, ph.materials, args.correction)
     gw.set_data(ph.density, ph.material)
     gw.build()
@@ -321,7 +331,7 @@ def run_ours(args):
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "peak_source": peak_kind,
-            "traffic": TRAFFIC_BYTES_PER_LAUNCH_512 if big else TRAFFIC_BYTES_PER_LAUNCH,
+            "traffic": None if c1 else (TRAFFIC_BYTES_PER_LAUNCH_512 if big else TRAFFIC_BYTES_PER_LAUNCH),
             "alg_bytes_per_launch": alg_bytes / (args.steps * launches_per_step),
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step),
             "visits_per_history": visits / done, "crossings_per_history": crossings / done,
@@ -369,12 +379,14 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "histories/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD_512 if big else WORKLOAD, "grid": list(ph.dims),
-                       "voxel_mm": [0.8, 0.8, 1.0] if big else 1.5, "histories_per_step": hist,
+            "config": {"workload": WORKLOAD_C1 if c1 else (WORKLOAD_512 if big else WORKLOAD), "grid": list(ph.dims),
+                       "voxel_mm": [1.0, 1.0, 2.5] if c1 else ([0.8, 0.8, 1.0] if big else 1.5),
+                       "histories_per_step": hist,
                        "exposures": n_exp, "tracking": args.tracking, "correction": args.correction,
                        "macro_cell_voxels": args.macro_cell if args.tracking == "macro" else None, "scoring": "fp64",
-                       "l2": "256 MB buffer written before every step; tally " + ("3.4 GB" if big else "420 MB")
-                             + " > L2",
+                       "l2": "256 MB buffer written before every step" + (
+                           "; the 128x128x64 world (5 MB voxels, 34 MB tally) is L2-resident" if c1 else
+                           "; tally " + ("3.4 GB" if big else "420 MB") + " > L2"),
                        "parallelism": f"replicas x{world} (independent Philox streams)"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps, "clocks": clk,
@@ -669,6 +681,8 @@ def run_denoise_experiment(args):
 
 def main():
     args = parse()
+    if args.workload == "c1" and args.histories == 1e9:
+        args.histories = 1e7  # the configuration's history count
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":

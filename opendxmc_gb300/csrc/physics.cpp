@@ -3,6 +3,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
+#include <mutex>
+#include <limits>
 
 namespace dxmcg {
 namespace {
@@ -250,13 +253,33 @@ namespace {
     constexpr std::array<double, 4> kTungstenLineShare = { 0.27, 0.47, 0.18, 0.08 };
     constexpr double kCharacteristicYield = 0.1;
 
-    double elementTotal(int Z, double E)
+    double elementTotalUncached(int Z, double E)
     {
         dxmcg_material m {};
         m.n = 1;
         m.Z[0] = Z;
         m.w[0] = 1.0;
         return attenuation(m, 1, E).sum();
+    }
+
+    // Total mass attenuation of a filter element.  Spectra use integer energies (1 keV
+    // bins); those values are computed once per element and kept (the angular
+    // integrals behind them take milliseconds per spectrum otherwise).
+    double elementTotal(int Z, double E)
+    {
+        constexpr int kMaxKeV = 512;
+        static std::mutex guard;
+        static std::vector<double> cache; // [Z][keV], NaN until computed
+        const double k = std::floor(E);
+        if (k != E || k < 1.0 || k >= kMaxKeV || Z < 1 || Z > 92)
+            return elementTotalUncached(Z, E);
+        const size_t idx = static_cast<size_t>(Z) * kMaxKeV + static_cast<size_t>(k);
+        std::lock_guard<std::mutex> lock(guard);
+        if (cache.empty())
+            cache.assign(93 * static_cast<size_t>(kMaxKeV), std::numeric_limits<double>::quiet_NaN());
+        if (std::isnan(cache[idx]))
+            cache[idx] = elementTotalUncached(Z, E);
+        return cache[idx];
     }
 } // namespace
 

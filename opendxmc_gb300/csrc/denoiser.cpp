@@ -47,6 +47,11 @@ struct dxmcg_denoiser {
     DevBuf<bf16> dz;
     DevBuf<float> pred;
     DevBuf<double> loss;
+    // world path: input channels, denoised dose and the normalisation sums, kept
+    // between calls (the input of a 512x512x400 world is 3.4 GB)
+    DevBuf<bf16> worldInput;
+    DevBuf<double> worldOut, meanSum;
+    DevBuf<unsigned long long> meanCount;
 
     int encA(int l) const { return 2 * l; }
     int encB(int l) const { return 2 * l + 1; }
@@ -261,17 +266,15 @@ namespace nn {
             return rc;
         const size_t n = static_cast<size_t>(nx) * ny * nz;
         if (!(scale > 0.0)) {
-            DevBuf<double> sum;
-            DevBuf<unsigned long long> cnt;
-            NN_CUDA(sum.reserve(1));
-            NN_CUDA(cnt.reserve(1));
-            NN_CUDA(cudaMemsetAsync(sum.p, 0, sizeof(double), s));
-            NN_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), s));
-            NN_CUDA(launchDoseMean(tally, vox, toDose, n, 0.2f, sum.p, cnt.p, s));
+            NN_CUDA(d->meanSum.reserve(1));
+            NN_CUDA(d->meanCount.reserve(1));
+            NN_CUDA(cudaMemsetAsync(d->meanSum.p, 0, sizeof(double), s));
+            NN_CUDA(cudaMemsetAsync(d->meanCount.p, 0, sizeof(unsigned long long), s));
+            NN_CUDA(launchDoseMean(tally, vox, toDose, n, 0.2f, d->meanSum.p, d->meanCount.p, s));
             double hs = 0;
             unsigned long long hc = 0;
-            NN_CUDA(cudaMemcpyAsync(&hs, sum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-            NN_CUDA(cudaMemcpyAsync(&hc, cnt.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
+            NN_CUDA(cudaMemcpyAsync(&hs, d->meanSum.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+            NN_CUDA(cudaMemcpyAsync(&hc, d->meanCount.p, sizeof(hc), cudaMemcpyDeviceToHost, s));
             NN_CUDA(cudaStreamSynchronize(s));
             scale = hc ? hs / static_cast<double>(hc) : 0.0;
             if (!(scale > 0.0))
@@ -279,18 +282,16 @@ namespace nn {
         }
         if (scaleUsed)
             *scaleUsed = scale;
-        DevBuf<bf16> input;
-        DevBuf<double> out;
-        NN_CUDA(input.reserve(n * 16));
-        NN_CUDA(out.reserve(n));
+        NN_CUDA(d->worldInput.reserve(n * 16));
+        NN_CUDA(d->worldOut.reserve(n));
         NN_CUDA(launchPrepareInput(nullptr, nullptr, nullptr, tally, vox, toDose, n, static_cast<float>(1.0 / scale),
-            input.p, s));
-        if ((rc = forward(d, input.p, s)) != DXMCG_OK)
+            d->worldInput.p, s));
+        if ((rc = forward(d, d->worldInput.p, s)) != DXMCG_OK)
             return rc;
-        NN_CUDA(launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, n, nullptr, nullptr, scale, out.p, nullptr,
-            nullptr, nullptr, s));
+        NN_CUDA(launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, n, nullptr, nullptr, scale, d->worldOut.p,
+            nullptr, nullptr, nullptr, s));
         if (hostOut)
-            NN_CUDA(cudaMemcpyAsync(hostOut, out.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+            NN_CUDA(cudaMemcpyAsync(hostOut, d->worldOut.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
         NN_CUDA(cudaStreamSynchronize(s));
         return tensorCoreStatus(d);
     }

@@ -417,11 +417,13 @@ class Denoiser:
         self.adam(lr, stream)
         return loss
 
-    def denoise_world(self, world: "GpuWorld", scale: float = 0.0):
-        """(denoised dose in mGy per voxel, scale used)"""
-        out = np.zeros(world.N)
+    def denoise_world(self, world: "GpuWorld", scale: float = 0.0, readback: bool = True):
+        """(denoised dose in mGy per voxel, scale used); without readback the dose stays
+        in device memory and None is returned in its place."""
+        out = np.zeros(world.N) if readback else None
         s = C.c_double(0)
-        N.check(N.lib().dxmcg_world_denoise(world._h, self._h, scale, N.ptr(out, C.c_double), C.byref(s)))
+        N.check(N.lib().dxmcg_world_denoise(world._h, self._h, scale, N.ptr(out, C.c_double) if readback else None,
+                                            C.byref(s)))
         return out, s.value
 
     def close(self) -> None:

@@ -136,16 +136,29 @@ namespace {
 
     template <int NT>
     struct ConvTcShape {
-        static constexpr int ZT = NT == 64 ? 4 : 8;          // output z-slices per CTA
+        static constexpr int ZT = NT == 64 ? 4 : 8;          // output z-slices per brick
         static constexpr int HZ = ZT + 2, HY = 18, HX = 10;  // halo extent
         static constexpr int kVox = HZ * HY * HX;
         static constexpr uint32_t kPlane = kVox * 16;        // one 8-channel half of the halo
-        static constexpr uint32_t kHalo = 2 * kPlane;
+        static constexpr uint32_t kHalo = 2 * kPlane;        // one halo buffer (two in the pipeline)
         static constexpr uint32_t kTapBytes = NT * 32;
         static constexpr uint32_t kStackBytes = 3 * kTapBytes; // the z-taps of one in-plane tap
-        static constexpr uint32_t kWeights = 27 * kTapBytes;
-        static constexpr uint32_t kSmem = kHalo + kWeights;
-        static constexpr uint32_t kCols = ZT * NT <= 32 ? 32 : (ZT * NT <= 64 ? 64 : (ZT * NT <= 128 ? 128 : 256));
+        static constexpr uint32_t kWeights = 27 * kTapBytes;  // one 16-channel input slice
+        static constexpr uint32_t kAcc = ZT * NT;             // TMEM columns of one brick's sums
+        static constexpr uint32_t kCols = 2 * kAcc <= 256 ? 256 : 512; // two accumulator sets
+        // reach of a brick in a half-resolution input (nearest upsampling): low-resolution
+        // voxels (z0/2 - 1 + lz, y0/2 - 1 + ly, x0/2 - 1 + lx), whose children cover the halo
+        static constexpr int LZ = ZT / 2 + 2, LY = 10, LX = 6;
+        static constexpr int kLowVox = LZ * LY * LX;
+        // dynamic shared memory: one halo buffer per pipeline stage (two or three), then the
+        // weights -- every slice's when they fit (resident), else one buffer per stage
+        static constexpr int kMaxStages = 3;
+        static constexpr uint32_t kMaxSmem = 227 * 1024 - 256;
+        static constexpr uint32_t smemFor(int nSlices, bool resident, int stages)
+        {
+            return stages * kHalo + (resident ? nSlices : stages) * kWeights;
+        }
+        static_assert(2 * kHalo + 2 * kWeights <= kMaxSmem, "pipeline buffers exceed shared memory");
     };
 
     struct TcTile {
@@ -167,138 +180,157 @@ namespace {
 
     // mapA / mapB: 5-D tensor maps (C, W, H, D, B) of the full-resolution inputs a and b
     // with a box of (8, 10, 18, ZT + 2, 1), used when useTma: the box of channel half h
-    // lands as halo plane h.  Slices of an upsampled input (halfA) use cp.async.
+    // lands as halo plane h.  Slices of an upsampled input (halfA) are expanded by the
+    // producer threads from the low-resolution voxels; without tensor maps the halo is
+    // gathered with cp.async.
     //
-    // The CTAs are persistent: CTA (i, j) takes bricks i, i + gridDim.x, ... of output
-    // channel tile j, keeping its TMEM, mbarriers and -- for a single 16-channel input
-    // slice -- the weights for all of them (every brick reading the same weights from L2
-    // made a few L2 slices the hot spot).  The epilogue zeroes the accumulators it read.
+    // One persistent CTA per SM (and output-channel tile blockIdx.y) works through its
+    // items -- (brick, input slice) pairs, bricks blockIdx.x, blockIdx.x + gridDim.x, ...
+    // in order, each brick's slices in order -- with warp-specialised roles that hand
+    // work over through mbarriers only, never a CTA barrier:
+    //   * warp 0 (one thread) issues each item's MMAs into its brick's accumulator set
+    //     (the two sets alternate between bricks), commits them to empty[stage] and,
+    //     after a brick's last slice, to accFull[set].  An issuing thread stalls while
+    //     the tensor pipe's queue is full, so no other role waits on it;
+    //   * warps 1-3 (producers) stage item i into stage i mod S once the MMAs of the
+    //     item that used it before released it (S = 2 or 3 stages, a launch parameter):
+    //     the halo by TMA (completing on tmaFull) or by their own
+    //     copies / upsampling expansion, and the slice's weights unless every slice's
+    //     weights stay resident; then they arrive on full[stage];
+    //   * warps 4-7 (one TMEM lane quarter each) wait for accFull, read the brick's sums
+    //     back (bias, ReLU, bf16 store), zero them and arrive on accEmpty[set].
+    // Every wait is bounded; a role that gives up raises the CTA's abort flag, the
+    // others leave at their next wait, and what is in flight (TMA, MMAs, copies) is
+    // awaited before the shared and tensor memory are given back.
+    constexpr int kProducers = 96;   // warps 1-3
+    constexpr int kEpilogue = 128;   // warps 4-7
+    constexpr uint32_t kPolls = 1u << 24;
+
     template <int NT>
-    __global__ void __launch_bounds__(256) conv3TcKernel(const nn::ConvIn in, int D, int H, int W, int Cin,
+    __global__ void __launch_bounds__(256, 1) conv3TcKernel(const nn::ConvIn in, int D, int H, int W, int Cin,
         const __nv_bfloat16* __restrict__ wgt, const float* __restrict__ bias, int Cout, int relu,
         __nv_bfloat16* __restrict__ out, const __grid_constant__ CUtensorMap mapA,
-        const __grid_constant__ CUtensorMap mapB, int useTma, int tiles)
+        const __grid_constant__ CUtensorMap mapB, int useTma, int tiles, int weightsResident, int stages)
     {
         using S = ConvTcShape<NT>;
         constexpr int ZT = S::ZT;
         extern __shared__ __align__(128) unsigned char smem[];
-        __shared__ __align__(8) uint64_t bar;
-        __shared__ __align__(8) uint64_t tmaBar;
+        __shared__ __align__(8) uint64_t full[S::kMaxStages];    // producers' copies of stage b visible
+        __shared__ __align__(8) uint64_t tmaFull[S::kMaxStages]; // the TMA halo of stage b landed
+        __shared__ __align__(8) uint64_t empty[S::kMaxStages];   // the MMAs reading stage b are done
+        __shared__ __align__(8) uint64_t accFull[2];  // the sums in accumulator set s are final
+        __shared__ __align__(8) uint64_t accEmpty[2]; // set s was read back and zeroed
+        __shared__ __align__(8) uint64_t drain;       // every MMA issued has completed
         __shared__ uint32_t tmemBase;
+        __shared__ int abortFlag;
         const int t = threadIdx.x;
         const int warp = t >> 5;
-        uint32_t tmaPhase = 0, mmaPhase = 0;
         const int n0 = blockIdx.y * NT;
         const int nSlices = Cin >> 4;
         const uint32_t sbase = umma::smemAddr(smem);
-        const uint32_t wbase = sbase + S::kHalo;
+        const uint32_t wbase = sbase + stages * S::kHalo;
+        const int myTiles = static_cast<int>(blockIdx.x) < tiles
+            ? (tiles - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
+            : 0;
+        const int nItems = myTiles * nSlices;
+        volatile int* abortp = &abortFlag;
 
         if (warp == 0)
             umma::tmemAlloc(&tmemBase, S::kCols);
         if (t == 0) {
-            umma::mbarInit(&bar, 1);
-            umma::mbarInit(&tmaBar, 1);
+            for (int b = 0; b < S::kMaxStages; ++b) {
+                umma::mbarInit(&full[b], kProducers);
+                umma::mbarInit(&tmaFull[b], 1);
+                umma::mbarInit(&empty[b], 1);
+            }
+            for (int b = 0; b < 2; ++b) {
+                umma::mbarInit(&accFull[b], 1);
+                umma::mbarInit(&accEmpty[b], kEpilogue);
+            }
+            umma::mbarInit(&drain, 1);
+            abortFlag = 0;
         }
         umma::fenceBeforeSync();
         __syncthreads();
         umma::fenceAfterSync();
         const uint32_t tm = tmemBase;
         const uint32_t laneBase = static_cast<uint32_t>(32 * (warp & 3)) << 16;
-        // zero the accumulators (warp w: lanes 32 (w % 4).., half of the columns), so
-        // that every MMA accumulates; the first slice's barrier orders these stores
-        // before the MMAs
-        {
-            constexpr int half = ZT * NT / 2;
+        // zero both accumulator sets (warp w: lanes 32 (w % 4).., half of the columns)
 #pragma unroll
-            for (int c = 0; c < half; c += 16)
-                umma::tmemZero16(tm + laneBase + (warp >> 2) * half + c);
-            umma::storeWait();
-            umma::fenceBeforeSync();
-        }
-        // the slice's weights for all taps, z-taps stacked per in-plane tap (cp.async,
-        // awaited with the halo of the slice)
-        const auto stageWeights = [&](int c0) {
-            for (int i = t; i < 27 * NT * 2; i += 256) {
+        for (int c = 0; c < static_cast<int>(S::kAcc); c += 16)
+            umma::tmemZero16(tm + laneBase + (warp >> 2) * S::kAcc + c);
+        umma::storeWait();
+
+        // a slice's weights for all taps, z-taps stacked per in-plane tap (cp.async by the
+        // threads [first, first + count))
+        const auto stageWeights = [&](int sl, uint32_t dst, int first, int count) {
+            const int c0 = sl * 16;
+            for (int i = t - first; i < 27 * NT * 2; i += count) {
                 const int co = i % NT, th = i / NT; // th = tap * 2 + h, tap = 9 (dz + 1) + q
                 const int tap = th >> 1, h = th & 1;
                 const int dz1 = tap / 9, q = tap - 9 * dz1;
                 const bool valid = n0 + co < Cout;
                 const __nv_bfloat16* src
                     = valid ? wgt + ((static_cast<size_t>(n0 + co) * 27 + tap) * Cin + c0 + h * 8) : wgt;
-                cpAsync16(wbase + q * S::kStackBytes + h * (3 * NT * 16) + ((2 - dz1) * NT + co) * 16, src, valid);
+                cpAsync16(dst + q * S::kStackBytes + h * (3 * NT * 16) + ((2 - dz1) * NT + co) * 16, src, valid);
             }
         };
-        const bool weightsResident = nSlices == 1;
-        if (weightsResident)
-            stageWeights(0);
+        if (weightsResident) {
+            for (int sl = 0; sl < nSlices; ++sl)
+                stageWeights(sl, wbase + sl * S::kWeights, 0, 256);
+            asm volatile("cp.async.commit_group;\n" ::);
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        umma::fenceProxyAsync();
+        umma::fenceBeforeSync();
+        __syncthreads();
+        umma::fenceAfterSync();
 
-        // 0: fine; kLateHalo / kLateMma: a bounded wait for the halo copies / the MMAs of
-        // a slice gave up (the CTA stops, the device error flag is set)
-        enum { kFine = 0, kLateHalo = 1, kLateMma = 2 };
-        int failed = kFine;
-        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-            const TcTile p = tcTileOf<ZT>(tile, D, H, W);
-            for (int sl = 0; sl < nSlices; ++sl) {
-                const int c0 = sl * 16;
-                // ---- stage the halo of this slice (from a, nearest-upsampled when halfA, or b)
-                const bool inA = c0 < in.ca;
-                const __nv_bfloat16* src = inA ? in.a : in.b;
-                const int cs = inA ? in.ca : in.cb;
-                const int cc = inA ? c0 : c0 - in.ca;
-                const bool half = inA && in.halfA;
-                const int Ds = half ? D >> 1 : D, Hs = half ? H >> 1 : H, Ws = half ? W >> 1 : W;
-                // TMA needs a 128-byte aligned destination (checked here, not assumed)
-                const bool tma = useTma && !half && (sbase & 127u) == 0u;
-                if (tma && t == 0) {
-                    const CUtensorMap* m = inA ? &mapA : &mapB;
-                    umma::mbarArriveExpectTx(&tmaBar, S::kHalo);
-                    umma::tmaLoad5d(sbase, m, cc, p.x0 - 1, p.y0 - 1, p.z0 - 1, p.b, &tmaBar);
-                    umma::tmaLoad5d(sbase + S::kPlane, m, cc + 8, p.x0 - 1, p.y0 - 1, p.z0 - 1, p.b, &tmaBar);
-                }
-                for (int i = t; i < (tma ? 0 : 2 * S::kVox); i += 256) {
-                    const int h = i / S::kVox, v = i - h * S::kVox;
-                    const int hz = v / (S::HY * S::HX), hy = (v / S::HX) % S::HY, hx = v % S::HX;
-                    const int gz = p.z0 + hz - 1, gy = p.y0 + hy - 1, gx = p.x0 + hx - 1;
-                    const bool inside = gz >= 0 && gz < D && gy >= 0 && gy < H && gx >= 0 && gx < W;
-                    const __nv_bfloat16* q = src;
-                    if (inside) {
-                        const int sz = half ? gz >> 1 : gz, sy = half ? gy >> 1 : gy, sx = half ? gx >> 1 : gx;
-                        q = src + ((((static_cast<size_t>(p.b) * Ds + sz) * Hs + sy) * Ws + sx) * cs + cc + h * 8);
+        const auto tileOfItem = [&](int it) {
+            return static_cast<int>(blockIdx.x) + (it / nSlices) * static_cast<int>(gridDim.x);
+        };
+        // whether the halo of slice sl comes by TMA (uniform over the CTA)
+        const auto byTma = [&](int sl) {
+            const bool inA = sl * 16 < in.ca;
+            return useTma && !(inA && in.halfA) && (sbase & 127u) == 0u;
+        };
+
+        if (warp == 0) {
+            // ------------------------------------------------------------ MMA issuer
+            if (t == 0) {
+                bool ok = true;
+                uint32_t tmaPhase = 0; // bit b: phase of tmaFull[b] (only TMA items complete it)
+                for (int it = 0; it < nItems && ok; ++it) {
+                    const int b = it % stages;
+                    const uint32_t use = static_cast<uint32_t>(it / stages);
+                    const int sl = it % nSlices;
+                    const int k = it / nSlices; // this CTA's brick number
+                    const int set = k & 1;
+                    ok = umma::mbarWaitOrAbort(&full[b], use & 1u, kPolls, abortp);
+                    if (ok && byTma(sl)) {
+                        ok = umma::mbarWaitOrAbort(&tmaFull[b], tmaPhase >> b & 1u, kPolls, abortp);
+                        tmaPhase ^= 1u << b;
                     }
-                    cpAsync16(sbase + h * S::kPlane + v * 16, q, inside);
-                }
-                if (!weightsResident)
-                    stageWeights(c0);
-                asm volatile("cp.async.commit_group;\n" ::);
-                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-                umma::fenceProxyAsync();
-                int staged = 1;
-                if (tma && t == 0)
-                    staged = umma::mbarWait(&tmaBar, tmaPhase, 1u << 24) ? 1 : 0;
-                if (!__syncthreads_and(staged)) {
-                    failed = kLateHalo; // no MMAs were issued for this slice
-                    break;
-                }
-                if (tma)
-                    tmaPhase ^= 1u;
-
-                // one thread issues the (ZT + 2) x 9 MMAs of the slice: plane hz feeds output
-                // slices hz - dz1 for dz1 = dz + 1 in [lo, hi]; the stacked B rows of those
-                // z-taps start at row (2 - hi) NT and land from column (hz - hi) NT
-                if (t == 0) {
+                    if (ok && sl == 0 && k >= 2)
+                        ok = umma::mbarWaitOrAbort(&accEmpty[set], static_cast<uint32_t>((k >> 1) - 1) & 1u, kPolls,
+                            abortp);
+                    if (!ok)
+                        break;
                     umma::fenceAfterSync();
-                    // descriptor start addresses are in 16-byte units in the low 14 bits (shared
-                    // memory < 256 KB), so offsets are added to the descriptor directly
-                    const uint64_t aBase = umma::smemDescriptor(sbase, S::kPlane, S::HX * 16);
-                    const uint64_t bBase = umma::smemDescriptor(wbase, 3 * NT * 16, 128);
-                    // the plane loop stays rolled: unrolled, its 90-odd descriptors take ~170
-                    // registers and cut the CTAs resident per SM from three to one
+                    // plane hz feeds output slices hz - dz1 for dz1 = dz + 1 in [lo, hi]; the
+                    // stacked B rows of those z-taps start at row (2 - hi) NT and land from
+                    // column (hz - hi) NT.  Descriptor start addresses are in 16-byte units in
+                    // the low 14 bits (shared memory < 256 KB): offsets are added directly.
+                    const uint64_t aBase = umma::smemDescriptor(sbase + b * S::kHalo, S::kPlane, S::HX * 16);
+                    const uint64_t bBase = umma::smemDescriptor(
+                        wbase + (weightsResident ? sl : b) * S::kWeights, 3 * NT * 16, 128);
+                    const uint32_t dBase = tm + set * S::kAcc;
 #pragma unroll 1
                     for (int hz = 0; hz < ZT + 2; ++hz) {
                         const int lo = hz - (ZT - 1) > 0 ? hz - (ZT - 1) : 0;
                         const int hi = hz < 2 ? hz : 2;
                         const uint32_t idesc = umma::instrDescriptorBf16(128, (hi - lo + 1) * NT);
-                        const uint32_t d = tm + (hz - hi) * NT;
+                        const uint32_t d = dBase + (hz - hi) * NT;
                         const uint64_t aPlane = aBase + static_cast<uint64_t>(hz * S::HY * S::HX);
                         const uint64_t bPlane = bBase + static_cast<uint64_t>(((2 - hi) * NT * 16) >> 4);
 #pragma unroll
@@ -309,87 +341,198 @@ namespace {
                                 bPlane + static_cast<uint64_t>((q * S::kStackBytes) >> 4), idesc, true);
                         }
                     }
-                    umma::commit(&bar);
+                    umma::commit(&empty[b]);
+                    if (sl == nSlices - 1)
+                        umma::commit(&accFull[set]);
                 }
-                // the stage is free again (and, after the last slice, the sums are final)
-                // once this slice's MMAs have completed: one thread polls the mbarrier, the
-                // other warps wait at the CTA barrier without taking issue slots
-                int done = 1;
-                if (t == 0)
-                    done = umma::mbarWait(&bar, mmaPhase, 1u << 24) ? 1 : 0;
-                if (!__syncthreads_and(done)) {
-                    failed = kLateMma;
+                if (!ok)
+                    *abortp = 1;
+                // nothing issued may still run when the memory is given back
+                umma::commit(&drain);
+                if (!umma::mbarWait(&drain, 0, kPolls))
+                    *abortp = 1;
+            }
+        } else if (warp < 4) {
+            // ------------------------------------------------------------ producers
+            const int pt = t - 32; // 0 .. kProducers - 1
+            uint32_t tmaPending = 0, tmaPhase = 0;
+            bool ok = true;
+            for (int it = 0; it < nItems; ++it) {
+                const int b = it % stages;
+                const uint32_t use = static_cast<uint32_t>(it / stages);
+                if (use >= 1 && !umma::mbarWaitOrAbort(&empty[b], (use - 1) & 1u, kPolls, abortp)) {
+                    ok = false;
                     break;
                 }
-                mmaPhase ^= 1u;
-            }
-            if (failed != kFine)
-                break;
-            umma::fenceAfterSync();
-
-            // ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (rows) for half the
-            // slices, and zeroes what it read for the next brick
-            const int lane = t & 31;
-            const int row = 32 * (warp & 3) + lane;
-            const int y = p.y0 + (row >> 3), x = p.x0 + (row & 7);
-            const int oBegin = (warp >> 2) * (ZT / 2);
-            const bool inPlane = y < H && x < W;
-#pragma unroll 1
-            for (int c = 0; c < NT; c += 16) {
-                float bv[16];
+                if (pt == 0 && (tmaPending >> b & 1u)) {
+                    // the stage's previous TMA was consumed by MMAs that are now done
+                    tmaPending &= ~(1u << b);
+                    tmaPhase ^= 1u << b;
+                }
+                const int sl = it % nSlices;
+                const TcTile p = tcTileOf<ZT>(tileOfItem(it), D, H, W);
+                const int c0 = sl * 16;
+                const bool inA = c0 < in.ca;
+                const __nv_bfloat16* src = inA ? in.a : in.b;
+                const int cs = inA ? in.ca : in.cb;
+                const int cc = inA ? c0 : c0 - in.ca;
+                const bool half = inA && in.halfA;
+                const uint32_t dst = sbase + b * S::kHalo;
+                unsigned char* dstp = smem + b * S::kHalo;
+                if (byTma(sl)) {
+                    if (pt == 0) {
+                        const CUtensorMap* m = inA ? &mapA : &mapB;
+                        umma::mbarArriveExpectTx(&tmaFull[b], S::kHalo);
+                        umma::tmaLoad5d(dst, m, cc, p.x0 - 1, p.y0 - 1, p.z0 - 1, p.b, &tmaFull[b]);
+                        umma::tmaLoad5d(dst + S::kPlane, m, cc + 8, p.x0 - 1, p.y0 - 1, p.z0 - 1, p.b, &tmaFull[b]);
+                        tmaPending |= 1u << b;
+                    }
+                } else if (half) {
+                    // nearest upsampling: each low-resolution voxel of the brick's reach is
+                    // read once and written to its 2 x 2 x 2 children that fall in the halo;
+                    // with even dimensions a child is outside the volume exactly when its
+                    // parent is, and that parent was read as zero
+                    const int Ds = D >> 1, Hs = H >> 1, Ws = W >> 1;
+                    constexpr int kBatch = 4;
+                    for (int i0 = pt; i0 < 2 * S::kLowVox; i0 += kBatch * kProducers) {
+                        uint4 lowv[kBatch];
 #pragma unroll
-                for (int k = 0; k < 16; ++k)
-                    bv[k] = bias ? __ldg(bias + n0 + c + k) : 0.0f;
-#pragma unroll 1
-                for (int o = oBegin; o < oBegin + ZT / 2; ++o) {
-                    float v[16];
-                    const uint32_t ta = tm + laneBase + o * NT + c;
-                    umma::tmemLoad16(ta, v);
-                    umma::tmemZero16(ta);
-                    const int z = p.z0 + o;
-                    if (inPlane && z < D) {
-                        uint4 pk[2];
-                        __nv_bfloat162* h2 = reinterpret_cast<__nv_bfloat162*>(pk);
-#pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            float a0 = v[2 * k] + bv[2 * k], a1 = v[2 * k + 1] + bv[2 * k + 1];
-                            if (relu) {
-                                a0 = fmaxf(a0, 0.0f);
-                                a1 = fmaxf(a1, 0.0f);
+                        for (int k = 0; k < kBatch; ++k) {
+                            const int i = i0 + k * kProducers;
+                            lowv[k] = make_uint4(0u, 0u, 0u, 0u);
+                            if (i < 2 * S::kLowVox) {
+                                const int h = i & 1, v = i >> 1;
+                                const int lz = v / (S::LY * S::LX), ly = (v / S::LX) % S::LY, lx = v % S::LX;
+                                const int sz = (p.z0 >> 1) - 1 + lz, sy = (p.y0 >> 1) - 1 + ly,
+                                          sx = (p.x0 >> 1) - 1 + lx;
+                                if (sz >= 0 && sz < Ds && sy >= 0 && sy < Hs && sx >= 0 && sx < Ws)
+                                    lowv[k] = __ldg(reinterpret_cast<const uint4*>(src
+                                        + ((((static_cast<size_t>(p.b) * Ds + sz) * Hs + sy) * Ws + sx) * cs + cc
+                                            + h * 8)));
                             }
-                            h2[k] = __floats2bfloat162_rn(a0, a1);
                         }
-                        uint4* d4 = reinterpret_cast<uint4*>(
-                            out + (((static_cast<size_t>(p.b) * D + z) * H + y) * W + x) * Cout + n0 + c);
-                        d4[0] = pk[0];
-                        d4[1] = pk[1];
+#pragma unroll
+                        for (int k = 0; k < kBatch; ++k) {
+                            const int i = i0 + k * kProducers;
+                            if (i < 2 * S::kLowVox) {
+                                const int h = i & 1, v = i >> 1;
+                                const int lz = v / (S::LY * S::LX), ly = (v / S::LX) % S::LY, lx = v % S::LX;
+                                // children at halo (2 lz - 1 + cz, ...): z0, y0 and x0 are even
+                                const int hz0 = 2 * lz - 1, hy0 = 2 * ly - 1, hx0 = 2 * lx - 1;
+                                unsigned char* base = dstp + h * S::kPlane;
+#pragma unroll
+                                for (int c = 0; c < 8; ++c) {
+                                    const int hz = hz0 + (c >> 2), hy = hy0 + ((c >> 1) & 1), hx = hx0 + (c & 1);
+                                    if (static_cast<unsigned>(hz) < static_cast<unsigned>(S::HZ)
+                                        && static_cast<unsigned>(hy) < static_cast<unsigned>(S::HY)
+                                        && static_cast<unsigned>(hx) < static_cast<unsigned>(S::HX))
+                                        *reinterpret_cast<uint4*>(base + ((hz * S::HY + hy) * S::HX + hx) * 16)
+                                            = lowv[k];
+                                }
+                            }
+                        }
+                    }
+                } else {
+                    // thread pairs copy the two 16-byte halves of one voxel: whole sectors
+                    for (int i = pt; i < 2 * S::kVox; i += kProducers) {
+                        const int h = i & 1, v = i >> 1;
+                        const int hz = v / (S::HY * S::HX), hy = (v / S::HX) % S::HY, hx = v % S::HX;
+                        const int gz = p.z0 + hz - 1, gy = p.y0 + hy - 1, gx = p.x0 + hx - 1;
+                        const bool inside = gz >= 0 && gz < D && gy >= 0 && gy < H && gx >= 0 && gx < W;
+                        const __nv_bfloat16* q = inside
+                            ? src + ((((static_cast<size_t>(p.b) * D + gz) * H + gy) * W + gx) * cs + cc + h * 8)
+                            : src;
+                        cpAsync16(dst + h * S::kPlane + v * 16, q, inside);
                     }
                 }
+                if (!weightsResident)
+                    stageWeights(sl, wbase + b * S::kWeights, 32, kProducers);
+                asm volatile("cp.async.commit_group;\n" ::);
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+                umma::fenceProxyAsync(); // generic-proxy writes, read next by the tensor cores
+                umma::mbarArrive(&full[b]);
             }
-            // the zeros land before the next brick's MMAs (ordered by its first barrier)
-            umma::storeWait();
-            umma::fenceBeforeSync();
+            if (!ok)
+                *abortp = 1;
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            // a TMA still in flight lands before the memory is given back
+            if (pt == 0)
+                for (int b = 0; b < stages; ++b)
+                    if (tmaPending >> b & 1u)
+                        umma::mbarWait(&tmaFull[b], tmaPhase >> b & 1u, kPolls);
+        } else {
+            // ------------------------------------------------------------ epilogue
+            const int lane = t & 31;
+            const int row = 32 * (warp & 3) + lane;
+            for (int k = 0; k < myTiles; ++k) {
+                const int set = k & 1;
+                if (!umma::mbarWaitOrAbort(&accFull[set], static_cast<uint32_t>(k >> 1) & 1u, kPolls, abortp)) {
+                    *abortp = 1;
+                    break;
+                }
+                umma::fenceAfterSync();
+                const TcTile p = tcTileOf<ZT>(static_cast<int>(blockIdx.x) + k * static_cast<int>(gridDim.x), D, H, W);
+                const int y = p.y0 + (row >> 3), x = p.x0 + (row & 7);
+                const bool inPlane = y < H && x < W;
+                const uint32_t acc = tm + laneBase + set * S::kAcc;
+#pragma unroll 1
+                for (int c = 0; c < NT; c += 16) {
+                    float bv[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        bv[j] = bias ? __ldg(bias + n0 + c + j) : 0.0f;
+#pragma unroll 1
+                    for (int o = 0; o < ZT; ++o) {
+                        float v[16];
+                        const uint32_t ta = acc + o * NT + c;
+                        umma::tmemLoad16(ta, v);
+                        umma::tmemZero16(ta);
+                        const int z = p.z0 + o;
+                        if (inPlane && z < D) {
+                            uint4 pk[2];
+                            __nv_bfloat162* h2 = reinterpret_cast<__nv_bfloat162*>(pk);
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                float a0 = v[2 * j] + bv[2 * j], a1 = v[2 * j + 1] + bv[2 * j + 1];
+                                if (relu) {
+                                    a0 = fmaxf(a0, 0.0f);
+                                    a1 = fmaxf(a1, 0.0f);
+                                }
+                                h2[j] = __floats2bfloat162_rn(a0, a1);
+                            }
+                            uint4* d4 = reinterpret_cast<uint4*>(
+                                out + (((static_cast<size_t>(p.b) * D + z) * H + y) * W + x) * Cout + n0 + c);
+                            d4[0] = pk[0];
+                            d4[1] = pk[1];
+                        }
+                    }
+                }
+                // the zeros land before the set's next MMAs
+                umma::storeWait();
+                umma::fenceBeforeSync();
+                umma::mbarArrive(&accEmpty[set]);
+            }
         }
-        if (failed != kFine && t == 0) {
-            atomicOr(&g_convTcError, 1u);
-            // what is still in flight must land before the shared and tensor memory are
-            // given back: the halo copies, or the MMAs, of the slice that gave up
-            if (failed == kLateHalo)
-                umma::mbarWait(&tmaBar, tmaPhase, 1u << 24);
-            else
-                umma::mbarWait(&bar, mmaPhase, 1u << 24);
-        }
-        // weights staged for a CTA that had no brick are awaited before it exits
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+
         umma::fenceBeforeSync();
         __syncthreads();
+        if (t == 0 && abortFlag)
+            atomicOr(&g_convTcError, 1u);
         if (warp == 0) {
             umma::fenceAfterSync();
             umma::tmemFree(tm, S::kCols);
         }
         if (t == 0) {
-            umma::mbarInval(&bar);
-            umma::mbarInval(&tmaBar);
+            for (int b = 0; b < S::kMaxStages; ++b) {
+                umma::mbarInval(&full[b]);
+                umma::mbarInval(&tmaFull[b]);
+                umma::mbarInval(&empty[b]);
+            }
+            for (int b = 0; b < 2; ++b) {
+                umma::mbarInval(&accFull[b]);
+                umma::mbarInval(&accEmpty[b]);
+            }
+            umma::mbarInval(&drain);
         }
     }
 
@@ -433,36 +576,33 @@ namespace {
     {
         using S = ConvTcShape<NT>;
         const int tiles = B * ((D + S::ZT - 1) / S::ZT) * ((H + 15) / 16) * ((W + 7) / 8);
-        // tensor maps of the full-resolution inputs (an upsampled a keeps cp.async)
+        // tensor maps of the full-resolution inputs (an upsampled a is expanded by the threads)
         CUtensorMap mapA {}, mapB {};
         bool tma = true;
         if (in.a && !in.halfA)
             tma = haloTensorMap(&mapA, in.a, B, D, H, W, in.ca, S::HZ);
         if (tma && in.b)
             tma = haloTensorMap(&mapB, in.b, B, D, H, W, in.cb, S::HZ);
-        // persistent CTAs: as many as are resident at once (whole waves), never more than bricks
-        // (from the SM's shared memory, registers and threads and the kernel's own use;
-        // the occupancy query answered one CTA per SM where three are resident)
-        static const int resident = [] {
-            int dev = 0;
-            cudaDeviceProp prop {};
-            cudaFuncAttributes fa {};
-            if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess
-                || cudaFuncGetAttributes(&fa, conv3TcKernel<NT>) != cudaSuccess)
+        // one persistent CTA per SM and output-channel tile, never more than bricks
+        static const int sms = [] {
+            int dev = 0, n = 0;
+            if (cudaGetDevice(&dev) != cudaSuccess
+                || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
                 return 0;
-            const size_t perCta = S::kSmem + fa.sharedSizeBytes + prop.reservedSharedMemPerBlock;
-            const int bySmem = static_cast<int>(prop.sharedMemPerMultiprocessor / perCta);
-            const int regs = ((fa.numRegs + 7) / 8) * 8 * 256;
-            const int byRegs = regs > 0 ? prop.regsPerMultiprocessor / regs : 1;
-            const int byThreads = prop.maxThreadsPerMultiProcessor / 256;
-            return std::max(1, std::min(bySmem, std::min(byRegs, byThreads))) * prop.multiProcessorCount;
+            return n;
         }();
-        if (resident <= 0)
+        if (sms <= 0)
             return cudaErrorLaunchOutOfResources;
+        const int nSlices = Cin / 16;
+        // resident weights where they fit; two stages (a third, where it fits, measured no
+        // faster on the 512 x 512 x 400 inference: the tensor pipe, not the staging, is the
+        // bound)
+        const bool resident = S::smemFor(nSlices, true, 2) <= S::kMaxSmem;
+        const int stages = 2;
         const int gy = Cout / NT;
-        const int gx = std::max(1, std::min(tiles, resident / gy));
-        conv3TcKernel<NT><<<dim3(gx, gy), 256, S::kSmem, s>>>(in, D, H, W, Cin, w, bias, Cout, relu ? 1 : 0, out,
-            mapA, mapB, tma ? 1 : 0, tiles);
+        const int gx = std::max(1, std::min(tiles, sms / gy));
+        conv3TcKernel<NT><<<dim3(gx, gy), 256, S::smemFor(nSlices, resident, stages), s>>>(in, D, H, W, Cin, w, bias,
+            Cout, relu ? 1 : 0, out, mapA, mapB, tma ? 1 : 0, tiles, resident ? 1 : 0, stages);
         return cudaGetLastError();
     }
 
@@ -471,8 +611,8 @@ namespace {
 namespace nn {
     cudaError_t conv3TcConfigure()
     {
-        // the whole unified L1 / shared array as shared memory: the CTAs per SM are
-        // bounded by shared memory
+        // the whole unified L1 / shared array as shared memory (one CTA per SM, with up to
+        // ConvTcShape::kMaxSmem of pipeline buffers)
         const auto configure = [](auto kernel, uint32_t smem) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e == cudaSuccess)
@@ -480,11 +620,11 @@ namespace nn {
                     cudaSharedmemCarveoutMaxShared);
             return e;
         };
-        cudaError_t e = configure(conv3TcKernel<16>, ConvTcShape<16>::kSmem);
+        cudaError_t e = configure(conv3TcKernel<16>, ConvTcShape<16>::kMaxSmem);
         if (e == cudaSuccess)
-            e = configure(conv3TcKernel<32>, ConvTcShape<32>::kSmem);
+            e = configure(conv3TcKernel<32>, ConvTcShape<32>::kMaxSmem);
         if (e == cudaSuccess)
-            e = configure(conv3TcKernel<64>, ConvTcShape<64>::kSmem);
+            e = configure(conv3TcKernel<64>, ConvTcShape<64>::kMaxSmem);
         return e;
     }
 

@@ -127,6 +127,33 @@ namespace umma {
         return false;
     }
 
+    // Like mbarWait, but also gives up as soon as *abort is set (checked every 64 polls):
+    // lets the roles of a warp-specialised CTA leave together when one of them timed out.
+    __device__ __forceinline__ bool mbarWaitOrAbort(uint64_t* bar, uint32_t parity, uint32_t limit,
+        const volatile int* abort)
+    {
+        const uint32_t a = smemAddr(bar);
+        for (uint32_t i = 0; i < limit; ++i) {
+            uint32_t done;
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                         "selp.u32 %0, 1, 0, p;\n}\n"
+                         : "=r"(done)
+                         : "r"(a), "r"(parity)
+                         : "memory");
+            if (done)
+                return true;
+            if ((i & 63u) == 63u && *abort)
+                return false;
+        }
+        return false;
+    }
+    // one arrival (release semantics: this thread's earlier shared-memory writes are
+    // visible to a thread whose wait on the phase succeeds)
+    __device__ __forceinline__ void mbarArrive(uint64_t* bar)
+    {
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smemAddr(bar)) : "memory");
+    }
+
     // ---- TMA: one tiled box of a 5-D tensor map into shared memory, completing on an
     // mbarrier (the caller arms it with the byte count first)
     __device__ __forceinline__ void mbarArriveExpectTx(uint64_t* bar, uint32_t bytes)

@@ -345,8 +345,10 @@ typedef struct {
     int32_t levels;      /* 1..5 */
     int32_t channels[5]; /* per level, multiples of 16; channels[0] 16 or 32 */
     uint64_t seed;       /* He-normal initialisation */
-    int32_t conv_path;   /* 3x3x3 convolutions: 0 = default (1), 1 = tcgen05 tensor cores with
-                            accumulators in tensor memory, 2 = warp-level mma.sync */
+    int32_t conv_path;   /* 3x3x3 convolutions: 0 = default: tcgen05 tensor cores with
+                            accumulators in tensor memory, except a launch whose grid would
+                            leave SMs idle (fewer output bricks than SMs), which takes mma.sync;
+                            1 = tcgen05 for every convolution; 2 = warp-level mma.sync */
 } dxmcg_denoiser_config;
 DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* config, dxmcg_denoiser** out);
 DXMCG_API void dxmcg_denoiser_destroy(dxmcg_denoiser* d);

@@ -210,7 +210,8 @@ namespace {
     __global__ void __launch_bounds__(256, 1) conv3TcKernel(const nn::ConvIn in, int D, int H, int W, int Cin,
         const __nv_bfloat16* __restrict__ wgt, const float* __restrict__ bias, int Cout, int relu,
         __nv_bfloat16* __restrict__ out, const __grid_constant__ CUtensorMap mapA,
-        const __grid_constant__ CUtensorMap mapB, int useTma, int tiles, int weightsResident, int stages)
+        const __grid_constant__ CUtensorMap mapB, int useTma, int tiles, int weightsResident, int stages,
+        const nn::ConvEpilogue ep)
     {
         using S = ConvTcShape<NT>;
         constexpr int ZT = S::ZT;
@@ -462,8 +463,21 @@ namespace {
                         umma::mbarWait(&tmaFull[b], tmaPhase >> b & 1u, kPolls);
         } else {
             // ------------------------------------------------------------ epilogue
+            // per brick: bias, ReLU, bf16 store; with ep.pooled also the 2x2x2 averages
+            // (z pairs in the thread, x pairs lane ^ 1, y pairs lane ^ 8: a warp holds 4
+            // rows of 8 x); with ep.head (N_T = 16) the 1x1x1 head instead of the store
             const int lane = t & 31;
             const int row = 32 * (warp & 3) + lane;
+            const bool pool = ep.pooled != nullptr;
+            const bool head = NT == 16 && ep.head != nullptr;
+            float hw[16];
+            float hb = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                hw[j] = head ? __ldg(ep.head + j) : 0.0f;
+            if (head)
+                hb = __ldg(ep.head + 16);
+            const int Dh = D >> 1, Hh = H >> 1, Wh = W >> 1;
             for (int k = 0; k < myTiles; ++k) {
                 const int set = k & 1;
                 if (!umma::mbarWaitOrAbort(&accFull[set], static_cast<uint32_t>(k >> 1) & 1u, kPolls, abortp)) {
@@ -482,13 +496,14 @@ namespace {
                     for (int j = 0; j < 16; ++j)
                         bv[j] = bias ? __ldg(bias + n0 + c + j) : 0.0f;
 #pragma unroll 1
-                    for (int o = 0; o < ZT; ++o) {
-                        float v[16];
-                        const uint32_t ta = acc + o * NT + c;
-                        umma::tmemLoad16(ta, v);
-                        umma::tmemZero16(ta);
-                        const int z = p.z0 + o;
-                        if (inPlane && z < D) {
+                    for (int o = 0; o < ZT; o += 2) {
+                        float r[2][16]; // the bf16 outputs of slices o and o + 1, as floats
+#pragma unroll
+                        for (int s2 = 0; s2 < 2; ++s2) {
+                            float v[16];
+                            const uint32_t ta = acc + (o + s2) * NT + c;
+                            umma::tmemLoad16(ta, v);
+                            umma::tmemZero16(ta);
                             uint4 pk[2];
                             __nv_bfloat162* h2 = reinterpret_cast<__nv_bfloat162*>(pk);
 #pragma unroll
@@ -499,11 +514,53 @@ namespace {
                                     a1 = fmaxf(a1, 0.0f);
                                 }
                                 h2[j] = __floats2bfloat162_rn(a0, a1);
+                                const float2 f = __bfloat1622float2(h2[j]);
+                                r[s2][2 * j] = f.x;
+                                r[s2][2 * j + 1] = f.y;
                             }
-                            uint4* d4 = reinterpret_cast<uint4*>(
-                                out + (((static_cast<size_t>(p.b) * D + z) * H + y) * W + x) * Cout + n0 + c);
-                            d4[0] = pk[0];
-                            d4[1] = pk[1];
+                            const int z = p.z0 + o + s2;
+                            if (inPlane && z < D) {
+                                const size_t vox = ((static_cast<size_t>(p.b) * D + z) * H + y) * W + x;
+                                if (head) {
+                                    float pr = hb;
+#pragma unroll
+                                    for (int j = 0; j < 16; ++j)
+                                        pr = fmaf(r[s2][j], hw[j], pr);
+                                    if (ep.headPred)
+                                        ep.headPred[vox] = pr;
+                                    if (ep.headOut)
+                                        ep.headOut[vox] = static_cast<double>(pr) * ep.headScale;
+                                } else {
+                                    uint4* d4 = reinterpret_cast<uint4*>(out + vox * Cout + n0 + c);
+                                    d4[0] = pk[0];
+                                    d4[1] = pk[1];
+                                }
+                            }
+                        }
+                        if (pool) {
+                            float sum[16];
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                sum[j] = r[0][j] + r[1][j];
+                                sum[j] += __shfl_xor_sync(0xffffffffu, sum[j], 1);
+                                sum[j] += __shfl_xor_sync(0xffffffffu, sum[j], 8);
+                            }
+                            // the even corner writes; with even D, H, W its window is inside
+                            // the volume exactly when the corner is
+                            if ((lane & 9) == 0 && inPlane && p.z0 + o < D) {
+                                uint4 pk[2];
+                                __nv_bfloat162* h2 = reinterpret_cast<__nv_bfloat162*>(pk);
+#pragma unroll
+                                for (int j = 0; j < 8; ++j)
+                                    h2[j] = __floats2bfloat162_rn(sum[2 * j] * 0.125f, sum[2 * j + 1] * 0.125f);
+                                uint4* d4 = reinterpret_cast<uint4*>(ep.pooled
+                                    + ((((static_cast<size_t>(p.b) * Dh + ((p.z0 + o) >> 1)) * Hh + (y >> 1)) * Wh
+                                           + (x >> 1))
+                                              * Cout
+                                        + n0 + c));
+                                d4[0] = pk[0];
+                                d4[1] = pk[1];
+                            }
                         }
                     }
                 }
@@ -572,7 +629,7 @@ namespace {
 
     template <int NT>
     cudaError_t launchTc(const nn::ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
-        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s)
+        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const nn::ConvEpilogue& ep)
     {
         using S = ConvTcShape<NT>;
         const int tiles = B * ((D + S::ZT - 1) / S::ZT) * ((H + 15) / 16) * ((W + 7) / 8);
@@ -602,7 +659,7 @@ namespace {
         const int gy = Cout / NT;
         const int gx = std::max(1, std::min(tiles, sms / gy));
         conv3TcKernel<NT><<<dim3(gx, gy), 256, S::smemFor(nSlices, resident, stages), s>>>(in, D, H, W, Cin, w, bias,
-            Cout, relu ? 1 : 0, out, mapA, mapB, tma ? 1 : 0, tiles, resident ? 1 : 0, stages);
+            Cout, relu ? 1 : 0, out, mapA, mapB, tma ? 1 : 0, tiles, resident ? 1 : 0, stages, ep);
         return cudaGetLastError();
     }
 
@@ -629,15 +686,20 @@ namespace nn {
     }
 
     cudaError_t launchConv3Tc(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
-        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s)
+        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const ConvEpilogue* ep)
     {
         if (Cin % 16 || Cout % 16 || (in.ca % 16) || (in.b && in.cb % 16) || in.ca + (in.b ? in.cb : 0) != Cin)
             return cudaErrorInvalidValue;
+        const ConvEpilogue none {};
+        const ConvEpilogue& e = ep ? *ep : none;
+        // the pooled output needs whole 2 x 2 x 2 windows; the head a 16-channel output
+        if ((e.pooled && ((D | H | W) & 1)) || (e.head && Cout != 16))
+            return cudaErrorInvalidValue;
         if (Cout % 64 == 0)
-            return launchTc<64>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s);
+            return launchTc<64>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s, e);
         if (Cout % 32 == 0)
-            return launchTc<32>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s);
-        return launchTc<16>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s);
+            return launchTc<32>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s, e);
+        return launchTc<16>(in, B, D, H, W, Cin, w, bias, Cout, relu, out, s, e);
     }
 
     int conv3TcCtas(int B, int D, int H, int W, int Cout)

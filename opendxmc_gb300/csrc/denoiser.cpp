@@ -38,8 +38,9 @@ struct dxmcg_denoiser {
     DevBuf<bf16> pb, wt;
     long step = 0;
     bool configured = false;
-    bool tensorCores = true; // tcgen05 convolutions (else warp-level mma.sync)
-    int sms = 1;             // streaming multiprocessors of the device
+    bool tensorCores = true;  // tcgen05 convolutions (else warp-level mma.sync)
+    bool tcEverywhere = false; // tcgen05 even where the grid has fewer bricks than SMs
+    int sms = 1;              // streaming multiprocessors of the device
 
     // activations and gradients of the current shape, per level
     int B = 0, D = 0, H = 0, W = 0;
@@ -115,18 +116,28 @@ int refreshWeights(dxmcg_denoiser* d, cudaStream_t s)
     return DXMCG_OK;
 }
 
-// tcgen05 for a convolution unless its grid would leave SMs without a CTA
+// tcgen05 for a convolution unless its grid would leave SMs without a CTA (or always,
+// when asked for with conv_path 1)
 bool useTensorCores(const dxmcg_denoiser* d, int D, int H, int W, int Cout)
 {
-    return d->tensorCores && nn::conv3TcCtas(d->B, D, H, W, Cout) >= d->sms;
+    return d->tensorCores && (d->tcEverywhere || nn::conv3TcCtas(d->B, D, H, W, Cout) >= d->sms);
 }
 
-int conv(dxmcg_denoiser* d, int k, const nn::ConvIn& in, int l, bf16* out, cudaStream_t s)
+// conv + bias + ReLU of layer k at level l; on the tcgen05 path the epilogue also does
+// the work of `ep` (*fused is set then; the caller runs the separate kernels otherwise)
+int conv(dxmcg_denoiser* d, int k, const nn::ConvIn& in, int l, bf16* out, cudaStream_t s,
+    const nn::ConvEpilogue* ep = nullptr, bool* fused = nullptr)
 {
     const auto& ly = d->layers[k];
     const int Dl = d->D >> l, Hl = d->H >> l, Wl = d->W >> l;
-    const auto launch = useTensorCores(d, Dl, Hl, Wl, ly.cout) ? nn::launchConv3Tc : nn::launchConv3;
-    NN_CUDA(launch(in, d->B, Dl, Hl, Wl, ly.cin, d->pb.p + ly.w, d->p.p + ly.b, ly.cout, true, out, s));
+    const bool tc = useTensorCores(d, Dl, Hl, Wl, ly.cout);
+    if (fused)
+        *fused = tc && ep;
+    if (tc)
+        NN_CUDA(nn::launchConv3Tc(in, d->B, Dl, Hl, Wl, ly.cin, d->pb.p + ly.w, d->p.p + ly.b, ly.cout, true, out, s,
+            ep));
+    else
+        NN_CUDA(nn::launchConv3(in, d->B, Dl, Hl, Wl, ly.cin, d->pb.p + ly.w, d->p.p + ly.b, ly.cout, true, out, s));
     return DXMCG_OK;
 }
 
@@ -168,27 +179,62 @@ nn::ConvIn encIn(dxmcg_denoiser* d, int l, const bf16* input)
     return l == 0 ? plain(input, 16) : plain(d->x[l].p, d->ch[l - 1]);
 }
 
-int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s)
+const bf16* finalActivation(dxmcg_denoiser* d) { return d->L > 1 ? d->db[0].p : d->eb[0].p; }
+
+// Forward pass.  The encoder's pooling is fused into the second convolution of each
+// level where that runs on tcgen05.  With `pred` or `predOut` (inference) the 1x1x1
+// head follows: fused into the last convolution (whose output is then not stored)
+// where it can be, else by headKernel; pred = prediction, predOut = prediction *
+// predScale.
+int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = nullptr,
+    double* predOut = nullptr, double predScale = 1.0)
 {
     int rc;
+    const bool wantHead = pred || predOut;
+    nn::ConvEpilogue headEp;
+    headEp.head = d->p.p + d->head;
+    headEp.headPred = pred;
+    headEp.headOut = predOut;
+    headEp.headScale = predScale;
+    const bool headFusable = wantHead && d->ch[0] == 16;
+    bool headDone = false;
     for (int l = 0; l < d->L; ++l) {
         if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s)) != DXMCG_OK)
             return rc;
-        if ((rc = conv(d, d->encB(l), plain(d->ea[l].p, d->ch[l]), l, d->eb[l].p, s)) != DXMCG_OK)
-            return rc;
+        nn::ConvEpilogue ep;
+        const bool last = d->L == 1; // encB(0) is the final convolution of a one-level net
         if (l < d->L - 1)
+            ep.pooled = d->x[l + 1].p;
+        else if (last && headFusable)
+            ep = headEp;
+        bool fused = false;
+        const bool withEp = ep.pooled || ep.head;
+        if ((rc = conv(d, d->encB(l), plain(d->ea[l].p, d->ch[l]), l, d->eb[l].p, s, withEp ? &ep : nullptr,
+                 &fused))
+            != DXMCG_OK)
+            return rc;
+        if (l < d->L - 1 && !fused)
             NN_CUDA(nn::launchAvgPool(d->eb[l].p, d->x[l + 1].p, d->B, d->D >> l, d->H >> l, d->W >> l, d->ch[l], s));
+        if (last && ep.head)
+            headDone = fused;
     }
     for (int l = d->L - 2; l >= 0; --l) {
         if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s)) != DXMCG_OK)
             return rc;
-        if ((rc = conv(d, d->decB(l), plain(d->da[l].p, d->ch[l]), l, d->db[l].p, s)) != DXMCG_OK)
+        const bool withHead = l == 0 && headFusable;
+        bool fused = false;
+        if ((rc = conv(d, d->decB(l), plain(d->da[l].p, d->ch[l]), l, d->db[l].p, s, withHead ? &headEp : nullptr,
+                 &fused))
+            != DXMCG_OK)
             return rc;
+        if (withHead)
+            headDone = fused;
     }
+    if (wantHead && !headDone)
+        NN_CUDA(nn::launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, d->nvox(0), nullptr, pred, predScale,
+            predOut, nullptr, nullptr, nullptr, s));
     return DXMCG_OK;
 }
-
-const bf16* finalActivation(dxmcg_denoiser* d) { return d->L > 1 ? d->db[0].p : d->eb[0].p; }
 
 // relu backward + weight/bias gradients, and the input gradient when dxOut
 int layerBack(dxmcg_denoiser* d, int k, const nn::ConvIn& xin, const bf16* y, const bf16* dy, bf16* dxOut, int l,
@@ -199,9 +245,12 @@ int layerBack(dxmcg_denoiser* d, int k, const nn::ConvIn& xin, const bf16* y, co
     NN_CUDA(nn::launchReluBackward(dy, y, d->dz.p, d->nvox(l), ly.cout, d->g.p + ly.b, s));
     NN_CUDA(nn::launchWgrad(xin, d->dz.p, d->B, Dl, Hl, Wl, ly.cin, ly.cout, d->g.p + ly.w, s));
     if (dxOut) {
-        const auto launch = useTensorCores(d, Dl, Hl, Wl, ly.cin) ? nn::launchConv3Tc : nn::launchConv3;
-        NN_CUDA(launch(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr, ly.cin, false,
-            dxOut, s));
+        if (useTensorCores(d, Dl, Hl, Wl, ly.cin))
+            NN_CUDA(nn::launchConv3Tc(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr,
+                ly.cin, false, dxOut, s));
+        else
+            NN_CUDA(nn::launchConv3(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr,
+                ly.cin, false, dxOut, s));
     }
     return DXMCG_OK;
 }
@@ -286,10 +335,8 @@ namespace nn {
         NN_CUDA(d->worldOut.reserve(n));
         NN_CUDA(launchPrepareInput(nullptr, nullptr, nullptr, tally, vox, toDose, n, static_cast<float>(1.0 / scale),
             d->worldInput.p, s));
-        if ((rc = forward(d, d->worldInput.p, s)) != DXMCG_OK)
+        if ((rc = forward(d, d->worldInput.p, s, nullptr, d->worldOut.p, scale)) != DXMCG_OK)
             return rc;
-        NN_CUDA(launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, n, nullptr, nullptr, scale, d->worldOut.p,
-            nullptr, nullptr, nullptr, s));
         if (hostOut)
             NN_CUDA(cudaMemcpyAsync(hostOut, d->worldOut.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
         NN_CUDA(cudaStreamSynchronize(s));
@@ -321,6 +368,7 @@ DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* c, dxmcg_denois
     cudaGetDevice(&d->device);
     d->L = c->levels;
     d->tensorCores = c->conv_path != 2;
+    d->tcEverywhere = c->conv_path == 1;
     if (cudaDeviceGetAttribute(&d->sms, cudaDevAttrMultiProcessorCount, d->device) != cudaSuccess || d->sms < 1)
         d->sms = 1;
     for (int l = 0; l < d->L; ++l)
@@ -446,10 +494,8 @@ DXMCG_API int dxmcg_denoiser_forward(dxmcg_denoiser* d, const void* input, int B
     if ((rc = ensureShape(d, B, D, H, W)) != DXMCG_OK)
         return rc;
     const auto s = static_cast<cudaStream_t>(cuda_stream);
-    if ((rc = forward(d, static_cast<const bf16*>(input), s)) != DXMCG_OK)
+    if ((rc = forward(d, static_cast<const bf16*>(input), s, pred)) != DXMCG_OK)
         return rc;
-    NN_CUDA(nn::launchHead(finalActivation(d), d->ch[0], d->p.p + d->head, d->nvox(0), nullptr, pred, 1.0, nullptr,
-        nullptr, nullptr, nullptr, s));
     return DXMCG_OK;
 }
 

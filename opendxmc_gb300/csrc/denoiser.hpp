@@ -28,11 +28,25 @@ size_t conv3SmemBytes(int nt);
 size_t wgradSmemBytes(int nt);
 cudaError_t conv3Configure(); // opt the kernels into their shared-memory size (once per device)
 
+// Work the tcgen05 convolution's epilogue does besides storing its output:
+//   pooled: also the 2x2x2 average of the (bf16) output, as launchAvgPool gives it up
+//           to the order of the eight additions (D, H, W even);
+//   head:   for a 16-channel output, the 1x1x1 head (16 weights, then the bias) in
+//           place of the output, exactly as launchHead without a target: headPred[v]
+//           = the prediction, headOut[v] = it times headScale (either may be null).
+struct ConvEpilogue {
+    __nv_bfloat16* pooled = nullptr;
+    const float* head = nullptr;
+    float* headPred = nullptr;
+    double* headOut = nullptr;
+    double headScale = 1.0;
+};
+
 // tcgen05 (5th-generation tensor core) form of launchConv3 (conv_tc.cu); the same
-// arguments and result up to FP32 summation order
+// arguments and result up to FP32 summation order, plus the optional epilogue work
 cudaError_t conv3TcConfigure();
 cudaError_t launchConv3Tc(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
-    const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);
+    const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const ConvEpilogue* ep = nullptr);
 cudaError_t conv3TcErrors(unsigned* flags);
 // CTAs of the tcgen05 launch for this shape (a grid under one CTA per SM leaves the
 // tensor cores of the other SMs idle: the caller then takes launchConv3)

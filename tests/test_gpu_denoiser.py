@@ -93,6 +93,26 @@ def test_tensor_core_convolutions_match_mma_sync(gpu, torch):
     assert rel(tc.grads(), ms.grads()) < 2e-2
 
 
+def test_tensor_core_persistent_bricks_match_mma_sync(gpu, torch):
+    """A volume with more output bricks than SMs at level 0 (1 x 64 x 128 x 64: 512
+    bricks of 8 x 16 x 8 for the persistent CTAs, three or four each): the tcgen05
+    pipeline alternates its two accumulator sets and waits for the epilogue to free
+    them, and it agrees with mma.sync on predictions and every gradient."""
+    ch = (16, 32)
+    tc = gpu.Denoiser(ch, seed=6, conv_path=1)
+    ms = gpu.Denoiser(ch, seed=6, conv_path=2)
+    x, t = make_case(17, B=1, D=64, H=128, W=64)
+    xt = torch.tensor(x, dtype=torch.bfloat16, device="cuda")
+    tt = torch.tensor(t, dtype=torch.float32, device="cuda")
+    p1 = tc.forward(xt).cpu().numpy()
+    p2 = ms.forward(xt).cpu().numpy()
+    assert rel(p1, p2) < 1e-2
+    l1 = tc.backward(xt, tt)
+    l2 = ms.backward(xt, tt)
+    assert abs(l1 / l2 - 1) < 1e-3
+    assert rel(tc.grads(), ms.grads()) < 2e-2
+
+
 def test_adam_step_matches_oracle(gpu, torch):
     x, t = make_case(11, B=1, D=8, H=8, W=8)
     dn = gpu.Denoiser(CH, seed=2)

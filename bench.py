@@ -75,6 +75,8 @@ def parse():
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
     p.add_argument("--train-steps", type=int, default=0, help="denoise-experiment: training steps (0: default)")
     p.add_argument("--lr-final", type=float, default=0.0, help="denoise-experiment: final learning rate (0: default)")
+    p.add_argument("--lows", default="", help="denoise-experiment: input history counts, comma-separated "
+                   "(default 3e7,1e8,3e8,1e9)")
     p.add_argument("--workload", choices=["torso", "torso512", "c1", "batch", "pipelines", "denoiser",
                                           "denoise-experiment"],
                    default="torso",
@@ -673,6 +675,8 @@ def run_denoise_experiment(args):
         kw["steps"] = args.train_steps
     if args.lr_final:
         kw["lr_final"] = args.lr_final
+    if args.lows:
+        kw["lows"] = tuple(float(v) for v in args.lows.split(","))
     out, net = DN.experiment(torch, log=lambda m: print(m, file=sys.stderr, flush=True), **kw)
     if args.save_weights:
         np.save(args.save_weights, net.get_params())

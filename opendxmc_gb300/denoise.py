@@ -191,7 +191,7 @@ def run_dose(world, beam, seed, stream, air):
 
 
 def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_seeds=(11, 12, 13, 14, 15, 16),
-               eval_seed=99, lows=(1e8, 3e8, 1e9), high=1e10, steps=16000, batch=8, patch=64, lr=1e-3,
+               eval_seed=99, lows=(3e7, 1e8, 3e8, 1e9), high=1e10, steps=16000, batch=8, patch=64, lr=1e-3,
                lr_final=5e-5, channels=(16, 32, 64, 128), target_error=0.02, log=print):
     """Train the denoiser on torso phantoms (inputs: runs of each history count in
     `lows`; target: a `high`-history run), then, on a held-out torso, compare the

@@ -230,10 +230,6 @@ namespace {
         const int nSlices = Cin >> 4;
         const uint32_t sbase = umma::smemAddr(smem);
         const uint32_t wbase = sbase + stages * S::kHalo;
-        const int myTiles = static_cast<int>(blockIdx.x) < tiles
-            ? (tiles - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
-            : 0;
-        const int nItems = myTiles * nSlices;
         volatile int* abortp = &abortFlag;
 
         if (warp == 0)
@@ -287,8 +283,14 @@ namespace {
         __syncthreads();
         umma::fenceAfterSync();
 
-        const auto tileOfItem = [&](int it) {
-            return static_cast<int>(blockIdx.x) + (it / nSlices) * static_cast<int>(gridDim.x);
+        // this CTA's bricks: blockIdx.x, blockIdx.x + gridDim.x, ... that ep.active marks
+        // (all without a mask); every role walks the same sequence with its own cursor
+        const auto nextTile = [&](int& cursor) {
+            while (cursor < tiles && ep.active && !__ldg(ep.active + cursor))
+                cursor += static_cast<int>(gridDim.x);
+            const int tile = cursor;
+            cursor += static_cast<int>(gridDim.x);
+            return tile; // >= tiles: no more
         };
         // whether the halo of slice sl comes by TMA (uniform over the CTA)
         const auto byTma = [&](int sl) {
@@ -301,12 +303,12 @@ namespace {
             if (t == 0) {
                 bool ok = true;
                 uint32_t tmaPhase = 0; // bit b: phase of tmaFull[b] (only TMA items complete it)
-                for (int it = 0; it < nItems && ok; ++it) {
+                int cursor = static_cast<int>(blockIdx.x), it = 0;
+                for (int k = 0; ok && nextTile(cursor) < tiles; ++k) { // k: this CTA's brick number
+                  const int set = k & 1;
+                  for (int sl = 0; sl < nSlices && ok; ++sl, ++it) {
                     const int b = it % stages;
                     const uint32_t use = static_cast<uint32_t>(it / stages);
-                    const int sl = it % nSlices;
-                    const int k = it / nSlices; // this CTA's brick number
-                    const int set = k & 1;
                     ok = umma::mbarWaitOrAbort(&full[b], use & 1u, kPolls, abortp);
                     if (ok && byTma(sl)) {
                         ok = umma::mbarWaitOrAbort(&tmaFull[b], tmaPhase >> b & 1u, kPolls, abortp);
@@ -345,6 +347,7 @@ namespace {
                     umma::commit(&empty[b]);
                     if (sl == nSlices - 1)
                         umma::commit(&accFull[set]);
+                  }
                 }
                 if (!ok)
                     *abortp = 1;
@@ -358,7 +361,10 @@ namespace {
             const int pt = t - 32; // 0 .. kProducers - 1
             uint32_t tmaPending = 0, tmaPhase = 0;
             bool ok = true;
-            for (int it = 0; it < nItems; ++it) {
+            int cursor = static_cast<int>(blockIdx.x), it = 0;
+            for (int tile; ok && (tile = nextTile(cursor)) < tiles;) {
+              const TcTile p = tcTileOf<ZT>(tile, D, H, W);
+              for (int sl = 0; sl < nSlices; ++sl, ++it) {
                 const int b = it % stages;
                 const uint32_t use = static_cast<uint32_t>(it / stages);
                 if (use >= 1 && !umma::mbarWaitOrAbort(&empty[b], (use - 1) & 1u, kPolls, abortp)) {
@@ -370,8 +376,6 @@ namespace {
                     tmaPending &= ~(1u << b);
                     tmaPhase ^= 1u << b;
                 }
-                const int sl = it % nSlices;
-                const TcTile p = tcTileOf<ZT>(tileOfItem(it), D, H, W);
                 const int c0 = sl * 16;
                 const bool inA = c0 < in.ca;
                 const __nv_bfloat16* src = inA ? in.a : in.b;
@@ -452,6 +456,7 @@ namespace {
                 asm volatile("cp.async.wait_group 0;\n" ::: "memory");
                 umma::fenceProxyAsync(); // generic-proxy writes, read next by the tensor cores
                 umma::mbarArrive(&full[b]);
+              }
             }
             if (!ok)
                 *abortp = 1;
@@ -478,14 +483,15 @@ namespace {
             if (head)
                 hb = __ldg(ep.head + 16);
             const int Dh = D >> 1, Hh = H >> 1, Wh = W >> 1;
-            for (int k = 0; k < myTiles; ++k) {
+            int cursor = static_cast<int>(blockIdx.x);
+            for (int k = 0, tile; (tile = nextTile(cursor)) < tiles; ++k) {
                 const int set = k & 1;
                 if (!umma::mbarWaitOrAbort(&accFull[set], static_cast<uint32_t>(k >> 1) & 1u, kPolls, abortp)) {
                     *abortp = 1;
                     break;
                 }
                 umma::fenceAfterSync();
-                const TcTile p = tcTileOf<ZT>(static_cast<int>(blockIdx.x) + k * static_cast<int>(gridDim.x), D, H, W);
+                const TcTile p = tcTileOf<ZT>(tile, D, H, W);
                 const int y = p.y0 + (row >> 3), x = p.x0 + (row & 7);
                 const bool inPlane = y < H && x < W;
                 const uint32_t acc = tm + laneBase + set * S::kAcc;
@@ -663,6 +669,47 @@ namespace {
         return cudaGetLastError();
     }
 
+    // active[b] = 1 where brick b holds a voxel whose packed word has a material other
+    // than 0 (one warp per brick; bricks x fastest, then y, z)
+    __global__ void brickActivityKernel(const uint32_t* __restrict__ vox, int nx, int ny, int nz, int bx, int by,
+        int bz, int cx, int cy, int cz, uint8_t* __restrict__ active)
+    {
+        const int lane = threadIdx.x & 31;
+        const int warps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
+        const int nb = cx * cy * cz;
+        for (int b = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); b < nb; b += warps) {
+            const int ix = b % cx, iy = (b / cx) % cy, iz = b / (cx * cy);
+            bool any = false;
+            for (int e = lane; e < bx * by * bz && !any; e += 32) {
+                const int x = ix * bx + e % bx, y = iy * by + (e / bx) % by, z = iz * bz + e / (bx * by);
+                if (x < nx && y < ny && z < nz)
+                    any = (__ldg(vox + (static_cast<size_t>(z) * ny + y) * nx + x) & 0xffu) != 0u;
+            }
+            any = __any_sync(0xffffffffu, any);
+            if (lane == 0)
+                active[b] = any ? 1 : 0;
+        }
+    }
+
+    // grown[b] = 1 where brick b or one of its 26 neighbours is active
+    __global__ void brickGrowKernel(const uint8_t* __restrict__ active, int cx, int cy, int cz,
+        uint8_t* __restrict__ grown)
+    {
+        const int nb = cx * cy * cz;
+        for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+            const int ix = b % cx, iy = (b / cx) % cy, iz = b / (cx * cy);
+            uint8_t g = 0;
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        const int x = ix + dx, y = iy + dy, z = iz + dz;
+                        if (x >= 0 && x < cx && y >= 0 && y < cy && z >= 0 && z < cz)
+                            g |= active[(static_cast<size_t>(z) * cy + y) * cx + x];
+                    }
+            grown[b] = g;
+        }
+    }
+
 } // namespace
 
 namespace nn {
@@ -712,6 +759,32 @@ namespace nn {
         if (Cout % 32 == 0)
             return ctas(ConvTcShape<32>::ZT, 32);
         return ctas(ConvTcShape<16>::ZT, 16);
+    }
+
+    void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3])
+    {
+        const int zt = Cout % 64 == 0 ? ConvTcShape<64>::ZT : (Cout % 32 == 0 ? ConvTcShape<32>::ZT : ConvTcShape<16>::ZT);
+        brick[0] = 8;
+        brick[1] = 16;
+        brick[2] = zt;
+        count[0] = (W + 7) / 8;
+        count[1] = (H + 15) / 16;
+        count[2] = (D + zt - 1) / zt;
+    }
+
+    cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3],
+        const int count[3], uint8_t* active, uint8_t* activeGrown, cudaStream_t s)
+    {
+        const int nb = count[0] * count[1] * count[2];
+        if (nb <= 0)
+            return cudaSuccess;
+        const int blocks = std::min((nb + 7) / 8, 4096);
+        brickActivityKernel<<<blocks, 256, 0, s>>>(vox, nx, ny, nz, brick[0], brick[1], brick[2], count[0], count[1],
+            count[2], active);
+        if (activeGrown)
+            brickGrowKernel<<<std::min((nb + 255) / 256, 4096), 256, 0, s>>>(active, count[0], count[1], count[2],
+                activeGrown);
+        return cudaGetLastError();
     }
 
     // reads and clears the device flag of timed-out commits (0: none)

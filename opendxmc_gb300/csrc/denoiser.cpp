@@ -52,6 +52,7 @@ struct dxmcg_denoiser {
     // between calls (the input of a 512x512x400 world is 3.4 GB)
     DevBuf<bf16> worldInput;
     DevBuf<double> worldOut, meanSum;
+    DevBuf<uint8_t> brickLast, brickBefore; // world path: bricks holding tissue, and grown by one
     DevBuf<unsigned long long> meanCount;
 
     int encA(int l) const { return 2 * l; }
@@ -185,9 +186,15 @@ const bf16* finalActivation(dxmcg_denoiser* d) { return d->L > 1 ? d->db[0].p : 
 // level where that runs on tcgen05.  With `pred` or `predOut` (inference) the 1x1x1
 // head follows: fused into the last convolution (whose output is then not stored)
 // where it can be, else by headKernel; pred = prediction, predOut = prediction *
-// predScale.
+// predScale.  `sparse` (inference, head fused) restricts the last convolution to the
+// bricks sparse->last marks and the one before it to sparse->before.
+struct Sparse {
+    const uint8_t* last = nullptr;
+    const uint8_t* before = nullptr;
+};
+
 int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = nullptr,
-    double* predOut = nullptr, double predScale = 1.0)
+    double* predOut = nullptr, double predScale = 1.0, const Sparse* sparse = nullptr)
 {
     int rc;
     const bool wantHead = pred || predOut;
@@ -196,13 +203,19 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
     headEp.headPred = pred;
     headEp.headOut = predOut;
     headEp.headScale = predScale;
+    if (sparse)
+        headEp.active = sparse->last;
+    nn::ConvEpilogue beforeEp;
+    if (sparse)
+        beforeEp.active = sparse->before;
     const bool headFusable = wantHead && d->ch[0] == 16;
     bool headDone = false;
     for (int l = 0; l < d->L; ++l) {
-        if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s)) != DXMCG_OK)
+        const bool last = d->L == 1; // encB(0) is the final convolution of a one-level net
+        if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s, last && sparse ? &beforeEp : nullptr))
+            != DXMCG_OK)
             return rc;
         nn::ConvEpilogue ep;
-        const bool last = d->L == 1; // encB(0) is the final convolution of a one-level net
         if (l < d->L - 1)
             ep.pooled = d->x[l + 1].p;
         else if (last && headFusable)
@@ -219,7 +232,8 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
             headDone = fused;
     }
     for (int l = d->L - 2; l >= 0; --l) {
-        if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s)) != DXMCG_OK)
+        if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s, l == 0 && sparse ? &beforeEp : nullptr))
+            != DXMCG_OK)
             return rc;
         const bool withHead = l == 0 && headFusable;
         bool fused = false;
@@ -335,7 +349,25 @@ namespace nn {
         NN_CUDA(d->worldOut.reserve(n));
         NN_CUDA(launchPrepareInput(nullptr, nullptr, nullptr, tally, vox, toDose, n, static_cast<float>(1.0 / scale),
             d->worldInput.p, s));
-        if ((rc = forward(d, d->worldInput.p, s, nullptr, d->worldOut.p, scale)) != DXMCG_OK)
+        // The readout deletes the dose of air (material 0).  Where the last two
+        // convolutions run on tcgen05 with the head fused, the last one computes only
+        // bricks holding a non-air voxel and the one before only those and their
+        // neighbours (the last one's halo); the dose of the other voxels is 0.  Every
+        // non-air voxel gets the same value as the dense pass.
+        Sparse sp;
+        const bool sparse = d->ch[0] == 16 && useTensorCores(d, nz, ny, nx, d->ch[0]);
+        if (sparse) {
+            int brick[3], count[3];
+            conv3TcBrickDims(nz, ny, nx, d->ch[0], brick, count);
+            const size_t nb = static_cast<size_t>(count[0]) * count[1] * count[2];
+            NN_CUDA(d->brickLast.reserve(nb));
+            NN_CUDA(d->brickBefore.reserve(nb));
+            NN_CUDA(launchBrickActivity(vox, nx, ny, nz, brick, count, d->brickLast.p, d->brickBefore.p, s));
+            NN_CUDA(cudaMemsetAsync(d->worldOut.p, 0, n * sizeof(double), s));
+            sp.last = d->brickLast.p;
+            sp.before = d->brickBefore.p;
+        }
+        if ((rc = forward(d, d->worldInput.p, s, nullptr, d->worldOut.p, scale, sparse ? &sp : nullptr)) != DXMCG_OK)
             return rc;
         if (hostOut)
             NN_CUDA(cudaMemcpyAsync(hostOut, d->worldOut.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -28,13 +28,16 @@ size_t conv3SmemBytes(int nt);
 size_t wgradSmemBytes(int nt);
 cudaError_t conv3Configure(); // opt the kernels into their shared-memory size (once per device)
 
-// Work the tcgen05 convolution's epilogue does besides storing its output:
+// Options of the tcgen05 convolution beyond launchConv3's:
+//   active: one byte per output brick (conv3TcBrickDims, x fastest, then y, z, batch);
+//           only marked bricks are computed, the others' output is left as it was;
 //   pooled: also the 2x2x2 average of the (bf16) output, as launchAvgPool gives it up
 //           to the order of the eight additions (D, H, W even);
 //   head:   for a 16-channel output, the 1x1x1 head (16 weights, then the bias) in
 //           place of the output, exactly as launchHead without a target: headPred[v]
 //           = the prediction, headOut[v] = it times headScale (either may be null).
 struct ConvEpilogue {
+    const uint8_t* active = nullptr;
     __nv_bfloat16* pooled = nullptr;
     const float* head = nullptr;
     float* headPred = nullptr;
@@ -51,6 +54,14 @@ cudaError_t conv3TcErrors(unsigned* flags);
 // CTAs of the tcgen05 launch for this shape (a grid under one CTA per SM leaves the
 // tensor cores of the other SMs idle: the caller then takes launchConv3)
 int conv3TcCtas(int B, int D, int H, int W, int Cout);
+// the output bricks of the tcgen05 launch for this shape: (x, y, z) voxels per brick
+// and the brick counts along x, y, z (per batch item)
+void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3]);
+// active[b] = 1 where brick b (of the given brick size) holds a voxel whose packed word
+// has a material other than 0, then dilated by `grow` bricks along each axis (26-
+// neighbourhood steps) into activeGrown when that is not null
+cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
+    uint8_t* active, uint8_t* activeGrown, cudaStream_t s);
 // out = act(conv3(in) + bias), act = relu or identity; bias may be null
 cudaError_t launchConv3(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
     const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);

@@ -78,13 +78,14 @@ def parse():
     p.add_argument("--lows", default="", help="denoise-experiment: input history counts, comma-separated "
                    "(default 3e7,1e8,3e8,1e9)")
     p.add_argument("--workload", choices=["torso", "torso512", "c1", "batch", "pipelines", "denoiser",
-                                          "denoise-experiment"],
+                                          "world-denoise", "denoise-experiment"],
                    default="torso",
                    help="torso: the spiral-CT torso job (256x256x200); torso512: the 512x512x400 spiral-CT torso; "
                         "c1: the DX water cylinder (1e7 histories per step unless --histories); "
                         "batch: 64 uneven DX/CBCT jobs in one persistent launch; "
                         "pipelines: segmentation and organ dose table passes; denoiser: training step and "
-                        "inference throughput")
+                        "inference throughput; world-denoise: the world-path denoiser call on the 512x512x400 "
+                        "torso after a 3e7-history run")
     return p.parse_args()
 
 
@@ -652,6 +653,48 @@ def run_denoiser(args):
     }), flush=True)
 
 
+def run_world_denoise(args):
+    """Time of the world-path denoiser call (dxmcg_world_denoise: the dose scale, the
+    input channels from the tally, the network with its last two convolutions on the
+    bricks holding tissue, the dose map left in device memory) on the 512x512x400
+    spiral-CT torso after a 3e7-history run.  Untrained weights: the time does not
+    depend on them."""
+    import torch
+
+    from opendxmc_gb300 import build as B
+    from opendxmc_gb300 import denoise as DN
+    from opendxmc_gb300 import phantoms as P
+
+    if not B.LIB.exists():
+        B.build(verbose_ptxas=False)
+    from opendxmc_gb300 import engine as G
+
+    G.set_device(0)
+    torch.cuda.set_device(0)
+    dims, spacing = (512, 512, 400), (0.08, 0.08, 0.1)
+    ph = P.torso_phantom(dims=dims, spacing=spacing, seed=99)
+    world = G.GpuWorld(dims, spacing, [c for _, c, _ in P.SIX_MATERIALS])
+    world.set_data(ph.density, ph.material)
+    world.build()
+    st = world.run(DN.spiral_beam(3e7), G.run_options(seed=5))
+    net = G.Denoiser((16, 32, 64, 128), seed=0, conv_path=args.conv_path)
+    ms = []
+    for r in range(max(args.warmup, 1) + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        net.denoise_world(world, readback=False)
+        torch.cuda.synchronize()
+        if r >= max(args.warmup, 1):
+            ms.append((time.perf_counter() - t0) * 1e3)
+    print(json.dumps({
+        "metric": "world-path denoiser call", "value": statistics.median(ms), "unit": "ms",
+        "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 1),
+        "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": "512x512x400 spiral-CT torso, 3e7 histories, denoiser 16/32/64/128 (untrained)"},
+        "transport_ms": st["total_ms"], "ms_all": ms,
+    }), flush=True)
+
+
 def run_denoise_experiment(args):
     """Seconds to 2 % dose error, plain Monte Carlo vs a short run plus the denoiser,
     on the 512x512x400 spiral-CT torso (trains the network first: a few minutes)."""
@@ -695,6 +738,8 @@ def main():
         run_pipelines(args)
     elif args.workload == "denoiser":
         run_denoiser(args)
+    elif args.workload == "world-denoise":
+        run_world_denoise(args)
     elif args.workload == "denoise-experiment":
         run_denoise_experiment(args)
     else:

@@ -230,6 +230,13 @@ namespace {
         const int nSlices = Cin >> 4;
         const uint32_t sbase = umma::smemAddr(smem);
         const uint32_t wbase = sbase + stages * S::kHalo;
+        // this CTA's bricks: blockIdx.x, blockIdx.x + gridDim.x, ... of the brick list
+        // (ep.list, ep.listLen entries) or of all `tiles` bricks
+        const int nBricks = ep.list ? __ldg(ep.listLen) : tiles;
+        const int myTiles = static_cast<int>(blockIdx.x) < nBricks
+            ? (nBricks - 1 - static_cast<int>(blockIdx.x)) / static_cast<int>(gridDim.x) + 1
+            : 0;
+        const int nItems = myTiles * nSlices;
         volatile int* abortp = &abortFlag;
 
         if (warp == 0)
@@ -283,14 +290,9 @@ namespace {
         __syncthreads();
         umma::fenceAfterSync();
 
-        // this CTA's bricks: blockIdx.x, blockIdx.x + gridDim.x, ... that ep.active marks
-        // (all without a mask); every role walks the same sequence with its own cursor
-        const auto nextTile = [&](int& cursor) {
-            while (cursor < tiles && ep.active && !__ldg(ep.active + cursor))
-                cursor += static_cast<int>(gridDim.x);
-            const int tile = cursor;
-            cursor += static_cast<int>(gridDim.x);
-            return tile; // >= tiles: no more
+        const auto tileOfBrick = [&](int k) {
+            const int j = static_cast<int>(blockIdx.x) + k * static_cast<int>(gridDim.x);
+            return ep.list ? __ldg(ep.list + j) : j;
         };
         // whether the halo of slice sl comes by TMA (uniform over the CTA)
         const auto byTma = [&](int sl) {
@@ -303,12 +305,12 @@ namespace {
             if (t == 0) {
                 bool ok = true;
                 uint32_t tmaPhase = 0; // bit b: phase of tmaFull[b] (only TMA items complete it)
-                int cursor = static_cast<int>(blockIdx.x), it = 0;
-                for (int k = 0; ok && nextTile(cursor) < tiles; ++k) { // k: this CTA's brick number
-                  const int set = k & 1;
-                  for (int sl = 0; sl < nSlices && ok; ++sl, ++it) {
+                for (int it = 0; it < nItems && ok; ++it) {
                     const int b = it % stages;
                     const uint32_t use = static_cast<uint32_t>(it / stages);
+                    const int sl = it % nSlices;
+                    const int k = it / nSlices; // this CTA's brick number
+                    const int set = k & 1;
                     ok = umma::mbarWaitOrAbort(&full[b], use & 1u, kPolls, abortp);
                     if (ok && byTma(sl)) {
                         ok = umma::mbarWaitOrAbort(&tmaFull[b], tmaPhase >> b & 1u, kPolls, abortp);
@@ -347,7 +349,6 @@ namespace {
                     umma::commit(&empty[b]);
                     if (sl == nSlices - 1)
                         umma::commit(&accFull[set]);
-                  }
                 }
                 if (!ok)
                     *abortp = 1;
@@ -361,10 +362,7 @@ namespace {
             const int pt = t - 32; // 0 .. kProducers - 1
             uint32_t tmaPending = 0, tmaPhase = 0;
             bool ok = true;
-            int cursor = static_cast<int>(blockIdx.x), it = 0;
-            for (int tile; ok && (tile = nextTile(cursor)) < tiles;) {
-              const TcTile p = tcTileOf<ZT>(tile, D, H, W);
-              for (int sl = 0; sl < nSlices; ++sl, ++it) {
+            for (int it = 0; it < nItems; ++it) {
                 const int b = it % stages;
                 const uint32_t use = static_cast<uint32_t>(it / stages);
                 if (use >= 1 && !umma::mbarWaitOrAbort(&empty[b], (use - 1) & 1u, kPolls, abortp)) {
@@ -376,6 +374,8 @@ namespace {
                     tmaPending &= ~(1u << b);
                     tmaPhase ^= 1u << b;
                 }
+                const int sl = it % nSlices;
+                const TcTile p = tcTileOf<ZT>(tileOfBrick(it / nSlices), D, H, W);
                 const int c0 = sl * 16;
                 const bool inA = c0 < in.ca;
                 const __nv_bfloat16* src = inA ? in.a : in.b;
@@ -456,7 +456,6 @@ namespace {
                 asm volatile("cp.async.wait_group 0;\n" ::: "memory");
                 umma::fenceProxyAsync(); // generic-proxy writes, read next by the tensor cores
                 umma::mbarArrive(&full[b]);
-              }
             }
             if (!ok)
                 *abortp = 1;
@@ -483,15 +482,14 @@ namespace {
             if (head)
                 hb = __ldg(ep.head + 16);
             const int Dh = D >> 1, Hh = H >> 1, Wh = W >> 1;
-            int cursor = static_cast<int>(blockIdx.x);
-            for (int k = 0, tile; (tile = nextTile(cursor)) < tiles; ++k) {
+            for (int k = 0; k < myTiles; ++k) {
                 const int set = k & 1;
                 if (!umma::mbarWaitOrAbort(&accFull[set], static_cast<uint32_t>(k >> 1) & 1u, kPolls, abortp)) {
                     *abortp = 1;
                     break;
                 }
                 umma::fenceAfterSync();
-                const TcTile p = tcTileOf<ZT>(tile, D, H, W);
+                const TcTile p = tcTileOf<ZT>(tileOfBrick(k), D, H, W);
                 const int y = p.y0 + (row >> 3), x = p.x0 + (row & 7);
                 const bool inPlane = y < H && x < W;
                 const uint32_t acc = tm + laneBase + set * S::kAcc;
@@ -691,6 +689,44 @@ namespace {
         }
     }
 
+    // list[0 .. *count) = the indices b with active[b] != 0, in increasing order (one CTA
+    // of 1024 threads: ballots within warps, a prefix over the warps, 1024 bricks a pass)
+    __global__ void __launch_bounds__(1024) brickListKernel(const uint8_t* __restrict__ active, int nb,
+        int* __restrict__ list, int* __restrict__ count)
+    {
+        __shared__ int warpBase[32];
+        __shared__ int passTotal;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        int base = 0;
+        for (int i0 = 0; i0 < nb; i0 += 1024) {
+            const int i = i0 + static_cast<int>(threadIdx.x);
+            const bool a = i < nb && active[i] != 0;
+            const unsigned m = __ballot_sync(0xffffffffu, a);
+            if (lane == 0)
+                warpBase[w] = __popc(m);
+            __syncthreads();
+            if (w == 0) {
+                const int v = warpBase[lane];
+                int incl = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int n = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o)
+                        incl += n;
+                }
+                warpBase[lane] = incl - v;
+                if (lane == 31)
+                    passTotal = incl;
+            }
+            __syncthreads();
+            if (a)
+                list[base + warpBase[w] + __popc(m & ((1u << lane) - 1u))] = i;
+            base += passTotal;
+            __syncthreads(); // warpBase and passTotal are rewritten by the next pass
+        }
+        if (threadIdx.x == 0)
+            *count = base;
+    }
+
     // grown[b] = 1 where brick b or one of its 26 neighbours is active
     __global__ void brickGrowKernel(const uint8_t* __restrict__ active, int cx, int cy, int cz,
         uint8_t* __restrict__ grown)
@@ -772,18 +808,18 @@ namespace nn {
         count[2] = (D + zt - 1) / zt;
     }
 
-    cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3],
-        const int count[3], uint8_t* active, uint8_t* activeGrown, cudaStream_t s)
+    cudaError_t launchBrickLists(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
+        uint8_t* active, uint8_t* grown, int* list, int* listLen, int* grownList, int* grownLen, cudaStream_t s)
     {
         const int nb = count[0] * count[1] * count[2];
         if (nb <= 0)
-            return cudaSuccess;
+            return cudaErrorInvalidValue;
         const int blocks = std::min((nb + 7) / 8, 4096);
         brickActivityKernel<<<blocks, 256, 0, s>>>(vox, nx, ny, nz, brick[0], brick[1], brick[2], count[0], count[1],
             count[2], active);
-        if (activeGrown)
-            brickGrowKernel<<<std::min((nb + 255) / 256, 4096), 256, 0, s>>>(active, count[0], count[1], count[2],
-                activeGrown);
+        brickGrowKernel<<<std::min((nb + 255) / 256, 4096), 256, 0, s>>>(active, count[0], count[1], count[2], grown);
+        brickListKernel<<<1, 1024, 0, s>>>(active, nb, list, listLen);
+        brickListKernel<<<1, 1024, 0, s>>>(grown, nb, grownList, grownLen);
         return cudaGetLastError();
     }
 

@@ -52,7 +52,9 @@ struct dxmcg_denoiser {
     // between calls (the input of a 512x512x400 world is 3.4 GB)
     DevBuf<bf16> worldInput;
     DevBuf<double> worldOut, meanSum;
-    DevBuf<uint8_t> brickLast, brickBefore; // world path: bricks holding tissue, and grown by one
+    // world path: bricks holding tissue, and those grown by one brick (masks, lists, lengths)
+    DevBuf<uint8_t> brickLast, brickBefore;
+    DevBuf<int> listLast, listBefore, listLens;
     DevBuf<unsigned long long> meanCount;
 
     int encA(int l) const { return 2 * l; }
@@ -189,8 +191,10 @@ const bf16* finalActivation(dxmcg_denoiser* d) { return d->L > 1 ? d->db[0].p : 
 // predScale.  `sparse` (inference, head fused) restricts the last convolution to the
 // bricks sparse->last marks and the one before it to sparse->before.
 struct Sparse {
-    const uint8_t* last = nullptr;
-    const uint8_t* before = nullptr;
+    const int* last = nullptr; // brick list of the last convolution, its length at lastLen
+    const int* lastLen = nullptr;
+    const int* before = nullptr; // and of the one before
+    const int* beforeLen = nullptr;
 };
 
 int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = nullptr,
@@ -203,11 +207,15 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
     headEp.headPred = pred;
     headEp.headOut = predOut;
     headEp.headScale = predScale;
-    if (sparse)
-        headEp.active = sparse->last;
+    if (sparse) {
+        headEp.list = sparse->last;
+        headEp.listLen = sparse->lastLen;
+    }
     nn::ConvEpilogue beforeEp;
-    if (sparse)
-        beforeEp.active = sparse->before;
+    if (sparse) {
+        beforeEp.list = sparse->before;
+        beforeEp.listLen = sparse->beforeLen;
+    }
     const bool headFusable = wantHead && d->ch[0] == 16;
     bool headDone = false;
     for (int l = 0; l < d->L; ++l) {
@@ -362,10 +370,16 @@ namespace nn {
             const size_t nb = static_cast<size_t>(count[0]) * count[1] * count[2];
             NN_CUDA(d->brickLast.reserve(nb));
             NN_CUDA(d->brickBefore.reserve(nb));
-            NN_CUDA(launchBrickActivity(vox, nx, ny, nz, brick, count, d->brickLast.p, d->brickBefore.p, s));
+            NN_CUDA(d->listLast.reserve(nb));
+            NN_CUDA(d->listBefore.reserve(nb));
+            NN_CUDA(d->listLens.reserve(2));
+            NN_CUDA(launchBrickLists(vox, nx, ny, nz, brick, count, d->brickLast.p, d->brickBefore.p, d->listLast.p,
+                d->listLens.p, d->listBefore.p, d->listLens.p + 1, s));
             NN_CUDA(cudaMemsetAsync(d->worldOut.p, 0, n * sizeof(double), s));
-            sp.last = d->brickLast.p;
-            sp.before = d->brickBefore.p;
+            sp.last = d->listLast.p;
+            sp.lastLen = d->listLens.p;
+            sp.before = d->listBefore.p;
+            sp.beforeLen = d->listLens.p + 1;
         }
         if ((rc = forward(d, d->worldInput.p, s, nullptr, d->worldOut.p, scale, sparse ? &sp : nullptr)) != DXMCG_OK)
             return rc;

@@ -29,15 +29,17 @@ size_t wgradSmemBytes(int nt);
 cudaError_t conv3Configure(); // opt the kernels into their shared-memory size (once per device)
 
 // Options of the tcgen05 convolution beyond launchConv3's:
-//   active: one byte per output brick (conv3TcBrickDims, x fastest, then y, z, batch);
-//           only marked bricks are computed, the others' output is left as it was;
+//   list:   device array of output-brick indices (conv3TcBrickDims, x fastest, then y,
+//           z, batch) and *listLen, its length, on the device: only those bricks are
+//           computed, the others' output is left as it was;
 //   pooled: also the 2x2x2 average of the (bf16) output, as launchAvgPool gives it up
 //           to the order of the eight additions (D, H, W even);
 //   head:   for a 16-channel output, the 1x1x1 head (16 weights, then the bias) in
 //           place of the output, exactly as launchHead without a target: headPred[v]
 //           = the prediction, headOut[v] = it times headScale (either may be null).
 struct ConvEpilogue {
-    const uint8_t* active = nullptr;
+    const int* list = nullptr;
+    const int* listLen = nullptr;
     __nv_bfloat16* pooled = nullptr;
     const float* head = nullptr;
     float* headPred = nullptr;
@@ -57,11 +59,13 @@ int conv3TcCtas(int B, int D, int H, int W, int Cout);
 // the output bricks of the tcgen05 launch for this shape: (x, y, z) voxels per brick
 // and the brick counts along x, y, z (per batch item)
 void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3]);
-// active[b] = 1 where brick b (of the given brick size) holds a voxel whose packed word
-// has a material other than 0, then dilated by `grow` bricks along each axis (26-
-// neighbourhood steps) into activeGrown when that is not null
-cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
-    uint8_t* active, uint8_t* activeGrown, cudaStream_t s);
+// Bricks (of the given size and counts) holding a voxel whose packed word has a
+// material other than 0: active[b] = 1 for those, grown[b] = 1 for those and their 26
+// neighbours; list / grownList their indices in increasing order, *listLen / *grownLen
+// how many (all on the device; active and grown need count[0] count[1] count[2] bytes,
+// the lists as many ints)
+cudaError_t launchBrickLists(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
+    uint8_t* active, uint8_t* grown, int* list, int* listLen, int* grownList, int* grownLen, cudaStream_t s);
 // out = act(conv3(in) + bias), act = relu or identity; bias may be null
 cudaError_t launchConv3(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
     const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);

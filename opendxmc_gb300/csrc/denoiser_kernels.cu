@@ -649,8 +649,10 @@ namespace {
         }
     }
 
-    // sum and count of the dose over voxels denser than rhoMin (the normalisation scale)
-    __global__ void doseMeanKernel(const Tally* __restrict__ tally, const uint32_t* __restrict__ vox, double toDose,
+    // sum and count of the dose over voxels denser than rhoMin (the normalisation scale).
+    // The factor toDose / rho is formed in FP32 (relative error ~1e-7, well inside what
+    // a normalisation needs): an FP64 division per voxel made this pass FP64-bound.
+    __global__ void doseMeanKernel(const Tally* __restrict__ tally, const uint32_t* __restrict__ vox, float toDose,
         size_t n, float rhoMin, double* __restrict__ sum, unsigned long long* __restrict__ count)
     {
         double s = 0.0;
@@ -659,7 +661,7 @@ namespace {
              i += static_cast<size_t>(gridDim.x) * blockDim.x) {
             const float rho = __uint_as_float(vox[i] & 0xffffff00u);
             if (rho > rhoMin) {
-                s += tally[i].e * (toDose / rho);
+                s += tally[i].e * static_cast<double>(toDose / rho);
                 ++c;
             }
         }
@@ -825,7 +827,7 @@ cudaError_t launchGatherPatches(const __nv_bfloat16* const* inputs, const float*
 cudaError_t launchDoseMean(const Tally* tally, const uint32_t* vox, double toDose, size_t n, float rhoMin,
     double* sum, unsigned long long* count, cudaStream_t s)
 {
-    doseMeanKernel<<<grid1d(n), 256, 0, s>>>(tally, vox, toDose, n, rhoMin, sum, count);
+    doseMeanKernel<<<grid1d(n), 256, 0, s>>>(tally, vox, static_cast<float>(toDose), n, rhoMin, sum, count);
     return cudaGetLastError();
 }
 

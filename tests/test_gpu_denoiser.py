@@ -215,7 +215,7 @@ def test_world_denoise_path(gpu, torch):
     d, _, _ = w.dose()
     rho, mat = w.packed_density()
     sel = rho > 0.2
-    assert abs(scale / d[sel].mean() - 1) < 1e-9
+    assert abs(scale / d[sel].mean() - 1) < 1e-6  # the mean forms toDose / rho in FP32
     # the same through the array path: prepare_input + forward, times the scale
     shape = (ph.dims[2], ph.dims[1], ph.dims[0])
     d_in = np.where(mat == 0, 0.0, d)  # air enters with zero dose

@@ -52,9 +52,10 @@ struct dxmcg_denoiser {
     // between calls (the input of a 512x512x400 world is 3.4 GB)
     DevBuf<bf16> worldInput;
     DevBuf<double> worldOut, meanSum;
-    // world path: bricks holding tissue, and those grown by one brick (masks, lists, lengths)
-    DevBuf<uint8_t> brickLast, brickBefore;
-    DevBuf<int> listLast, listBefore, listLens;
+    // world path: brick masks and lists of the restricted decoder layers (level 0:
+    // tissue, grown by one, grown by two; level 1: covered by the last, grown by one)
+    DevBuf<uint8_t> mask0[3], mask1[2];
+    DevBuf<int> list0[2], list1[2], listLens;
     DevBuf<unsigned long long> meanCount;
 
     int encA(int l) const { return 2 * l; }
@@ -195,6 +196,10 @@ struct Sparse {
     const int* lastLen = nullptr;
     const int* before = nullptr; // and of the one before
     const int* beforeLen = nullptr;
+    const int* dec1b = nullptr; // level-1 decoder (null: dense)
+    const int* dec1bLen = nullptr;
+    const int* dec1a = nullptr;
+    const int* dec1aLen = nullptr;
 };
 
 int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = nullptr,
@@ -239,15 +244,22 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
         if (last && ep.head)
             headDone = fused;
     }
+    nn::ConvEpilogue dec1aEp, dec1bEp;
+    if (sparse && sparse->dec1a) {
+        dec1aEp.list = sparse->dec1a;
+        dec1aEp.listLen = sparse->dec1aLen;
+        dec1bEp.list = sparse->dec1b;
+        dec1bEp.listLen = sparse->dec1bLen;
+    }
+    const bool sparse1 = sparse && sparse->dec1a;
     for (int l = d->L - 2; l >= 0; --l) {
-        if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s, l == 0 && sparse ? &beforeEp : nullptr))
-            != DXMCG_OK)
+        const nn::ConvEpilogue* epA = l == 0 && sparse ? &beforeEp : (l == 1 && sparse1 ? &dec1aEp : nullptr);
+        if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s, epA)) != DXMCG_OK)
             return rc;
         const bool withHead = l == 0 && headFusable;
         bool fused = false;
-        if ((rc = conv(d, d->decB(l), plain(d->da[l].p, d->ch[l]), l, d->db[l].p, s, withHead ? &headEp : nullptr,
-                 &fused))
-            != DXMCG_OK)
+        const nn::ConvEpilogue* epB = withHead ? &headEp : (l == 1 && sparse1 ? &dec1bEp : nullptr);
+        if ((rc = conv(d, d->decB(l), plain(d->da[l].p, d->ch[l]), l, d->db[l].p, s, epB, &fused)) != DXMCG_OK)
             return rc;
         if (withHead)
             headDone = fused;
@@ -362,24 +374,49 @@ namespace nn {
         // bricks holding a non-air voxel and the one before only those and their
         // neighbours (the last one's halo); the dose of the other voxels is 0.  Every
         // non-air voxel gets the same value as the dense pass.
+        // The level-1 decoder is restricted too: the one before the last reads the
+        // upsampled level-1 output in a one-voxel halo of its bricks (their set grown by
+        // one brick, coarsened to level 1), and that layer's input one level-1 voxel
+        // further (grown by one level-1 brick).
         Sparse sp;
         const bool sparse = d->ch[0] == 16 && useTensorCores(d, nz, ny, nx, d->ch[0]);
         if (sparse) {
             int brick[3], count[3];
             conv3TcBrickDims(nz, ny, nx, d->ch[0], brick, count);
             const size_t nb = static_cast<size_t>(count[0]) * count[1] * count[2];
-            NN_CUDA(d->brickLast.reserve(nb));
-            NN_CUDA(d->brickBefore.reserve(nb));
-            NN_CUDA(d->listLast.reserve(nb));
-            NN_CUDA(d->listBefore.reserve(nb));
-            NN_CUDA(d->listLens.reserve(2));
-            NN_CUDA(launchBrickLists(vox, nx, ny, nz, brick, count, d->brickLast.p, d->brickBefore.p, d->listLast.p,
-                d->listLens.p, d->listBefore.p, d->listLens.p + 1, s));
+            for (auto& m : d->mask0)
+                NN_CUDA(m.reserve(nb));
+            for (auto& l : d->list0)
+                NN_CUDA(l.reserve(nb));
+            NN_CUDA(d->listLens.reserve(4));
+            NN_CUDA(launchBrickActivity(vox, nx, ny, nz, brick, count, d->mask0[0].p, s));
+            NN_CUDA(launchBrickGrow(d->mask0[0].p, count, d->mask0[1].p, s));
+            NN_CUDA(launchBrickList(d->mask0[0].p, static_cast<int>(nb), d->list0[0].p, d->listLens.p, s));
+            NN_CUDA(launchBrickList(d->mask0[1].p, static_cast<int>(nb), d->list0[1].p, d->listLens.p + 1, s));
             NN_CUDA(cudaMemsetAsync(d->worldOut.p, 0, n * sizeof(double), s));
-            sp.last = d->listLast.p;
+            sp.last = d->list0[0].p;
             sp.lastLen = d->listLens.p;
-            sp.before = d->listBefore.p;
+            sp.before = d->list0[1].p;
             sp.beforeLen = d->listLens.p + 1;
+            const int D1 = nz >> 1, H1 = ny >> 1, W1 = nx >> 1;
+            if (d->L >= 3 && useTensorCores(d, D1, H1, W1, d->ch[1])) {
+                int brick1[3], count1[3];
+                conv3TcBrickDims(D1, H1, W1, d->ch[1], brick1, count1);
+                const size_t nb1 = static_cast<size_t>(count1[0]) * count1[1] * count1[2];
+                for (auto& m : d->mask1)
+                    NN_CUDA(m.reserve(nb1));
+                for (auto& l : d->list1)
+                    NN_CUDA(l.reserve(nb1));
+                NN_CUDA(launchBrickGrow(d->mask0[1].p, count, d->mask0[2].p, s));
+                NN_CUDA(launchBrickCoarsen(d->mask0[2].p, brick, count, brick1, count1, d->mask1[0].p, s));
+                NN_CUDA(launchBrickGrow(d->mask1[0].p, count1, d->mask1[1].p, s));
+                NN_CUDA(launchBrickList(d->mask1[0].p, static_cast<int>(nb1), d->list1[0].p, d->listLens.p + 2, s));
+                NN_CUDA(launchBrickList(d->mask1[1].p, static_cast<int>(nb1), d->list1[1].p, d->listLens.p + 3, s));
+                sp.dec1b = d->list1[0].p;
+                sp.dec1bLen = d->listLens.p + 2;
+                sp.dec1a = d->list1[1].p;
+                sp.dec1aLen = d->listLens.p + 3;
+            }
         }
         if ((rc = forward(d, d->worldInput.p, s, nullptr, d->worldOut.p, scale, sparse ? &sp : nullptr)) != DXMCG_OK)
             return rc;

@@ -59,13 +59,19 @@ int conv3TcCtas(int B, int D, int H, int W, int Cout);
 // the output bricks of the tcgen05 launch for this shape: (x, y, z) voxels per brick
 // and the brick counts along x, y, z (per batch item)
 void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3]);
-// Bricks (of the given size and counts) holding a voxel whose packed word has a
-// material other than 0: active[b] = 1 for those, grown[b] = 1 for those and their 26
-// neighbours; list / grownList their indices in increasing order, *listLen / *grownLen
-// how many (all on the device; active and grown need count[0] count[1] count[2] bytes,
-// the lists as many ints)
-cudaError_t launchBrickLists(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
-    uint8_t* active, uint8_t* grown, int* list, int* listLen, int* grownList, int* grownLen, cudaStream_t s);
+// Brick sets of the world path (one byte per brick, bricks x fastest, all on the device):
+//   activity: bricks (of the given size and counts) holding a voxel whose packed word
+//             has a material other than 0;
+//   grow:     those and their 26 neighbours;
+//   coarsen:  bricks of the half-resolution level whose voxels cover a voxel of a
+//             marked brick of the level above (voxel v lies in coarse voxel v / 2);
+//   list:     the marked indices in increasing order, and how many (*listLen).
+cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
+    uint8_t* active, cudaStream_t s);
+cudaError_t launchBrickGrow(const uint8_t* active, const int count[3], uint8_t* grown, cudaStream_t s);
+cudaError_t launchBrickCoarsen(const uint8_t* fine, const int fineBrick[3], const int fineCount[3],
+    const int coarseBrick[3], const int coarseCount[3], uint8_t* coarse, cudaStream_t s);
+cudaError_t launchBrickList(const uint8_t* mask, int nb, int* list, int* listLen, cudaStream_t s);
 // out = act(conv3(in) + bias), act = relu or identity; bias may be null
 cudaError_t launchConv3(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
     const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);

@@ -211,7 +211,7 @@ namespace {
         const __nv_bfloat16* __restrict__ wgt, const float* __restrict__ bias, int Cout, int relu,
         __nv_bfloat16* __restrict__ out, const __grid_constant__ CUtensorMap mapA,
         const __grid_constant__ CUtensorMap mapB, int useTma, int tiles, int weightsResident, int stages,
-        const nn::ConvEpilogue ep)
+        const nn::ConvOptions ep)
     {
         using S = ConvTcShape<NT>;
         constexpr int ZT = S::ZT;
@@ -633,7 +633,7 @@ namespace {
 
     template <int NT>
     cudaError_t launchTc(const nn::ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
-        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const nn::ConvEpilogue& ep)
+        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const nn::ConvOptions& ep)
     {
         using S = ConvTcShape<NT>;
         const int tiles = B * ((D + S::ZT - 1) / S::ZT) * ((H + 15) / 16) * ((W + 7) / 8);
@@ -791,12 +791,12 @@ namespace nn {
     }
 
     cudaError_t launchConv3Tc(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
-        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const ConvEpilogue* ep)
+        const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const ConvOptions* ep)
     {
         if (Cin % 16 || Cout % 16 || (in.ca % 16) || (in.b && in.cb % 16) || in.ca + (in.b ? in.cb : 0) != Cin)
             return cudaErrorInvalidValue;
-        const ConvEpilogue none {};
-        const ConvEpilogue& e = ep ? *ep : none;
+        const ConvOptions none {};
+        const ConvOptions& e = ep ? *ep : none;
         // the pooled output needs whole 2 x 2 x 2 windows; the head a 16-channel output
         if ((e.pooled && ((D | H | W) & 1)) || (e.head && Cout != 16))
             return cudaErrorInvalidValue;

@@ -130,7 +130,7 @@ bool useTensorCores(const dxmcg_denoiser* d, int D, int H, int W, int Cout)
 // conv + bias + ReLU of layer k at level l; on the tcgen05 path the epilogue also does
 // the work of `ep` (*fused is set then; the caller runs the separate kernels otherwise)
 int conv(dxmcg_denoiser* d, int k, const nn::ConvIn& in, int l, bf16* out, cudaStream_t s,
-    const nn::ConvEpilogue* ep = nullptr, bool* fused = nullptr)
+    const nn::ConvOptions* ep = nullptr, bool* fused = nullptr)
 {
     const auto& ly = d->layers[k];
     const int Dl = d->D >> l, Hl = d->H >> l, Wl = d->W >> l;
@@ -207,7 +207,7 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
 {
     int rc;
     const bool wantHead = pred || predOut;
-    nn::ConvEpilogue headEp;
+    nn::ConvOptions headEp;
     headEp.head = d->p.p + d->head;
     headEp.headPred = pred;
     headEp.headOut = predOut;
@@ -216,7 +216,7 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
         headEp.list = sparse->last;
         headEp.listLen = sparse->lastLen;
     }
-    nn::ConvEpilogue beforeEp;
+    nn::ConvOptions beforeEp;
     if (sparse) {
         beforeEp.list = sparse->before;
         beforeEp.listLen = sparse->beforeLen;
@@ -228,7 +228,7 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
         if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s, last && sparse ? &beforeEp : nullptr))
             != DXMCG_OK)
             return rc;
-        nn::ConvEpilogue ep;
+        nn::ConvOptions ep;
         if (l < d->L - 1)
             ep.pooled = d->x[l + 1].p;
         else if (last && headFusable)
@@ -244,7 +244,7 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
         if (last && ep.head)
             headDone = fused;
     }
-    nn::ConvEpilogue dec1aEp, dec1bEp;
+    nn::ConvOptions dec1aEp, dec1bEp;
     if (sparse && sparse->dec1a) {
         dec1aEp.list = sparse->dec1a;
         dec1aEp.listLen = sparse->dec1aLen;
@@ -253,12 +253,12 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
     }
     const bool sparse1 = sparse && sparse->dec1a;
     for (int l = d->L - 2; l >= 0; --l) {
-        const nn::ConvEpilogue* epA = l == 0 && sparse ? &beforeEp : (l == 1 && sparse1 ? &dec1aEp : nullptr);
+        const nn::ConvOptions* epA = l == 0 && sparse ? &beforeEp : (l == 1 && sparse1 ? &dec1aEp : nullptr);
         if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s, epA)) != DXMCG_OK)
             return rc;
         const bool withHead = l == 0 && headFusable;
         bool fused = false;
-        const nn::ConvEpilogue* epB = withHead ? &headEp : (l == 1 && sparse1 ? &dec1bEp : nullptr);
+        const nn::ConvOptions* epB = withHead ? &headEp : (l == 1 && sparse1 ? &dec1bEp : nullptr);
         if ((rc = conv(d, d->decB(l), plain(d->da[l].p, d->ch[l]), l, d->db[l].p, s, epB, &fused)) != DXMCG_OK)
             return rc;
         if (withHead)

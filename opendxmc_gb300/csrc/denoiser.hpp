@@ -37,7 +37,7 @@ cudaError_t conv3Configure(); // opt the kernels into their shared-memory size (
 //   head:   for a 16-channel output, the 1x1x1 head (16 weights, then the bias) in
 //           place of the output, exactly as launchHead without a target: headPred[v]
 //           = the prediction, headOut[v] = it times headScale (either may be null).
-struct ConvEpilogue {
+struct ConvOptions {
     const int* list = nullptr;
     const int* listLen = nullptr;
     __nv_bfloat16* pooled = nullptr;
@@ -51,7 +51,7 @@ struct ConvEpilogue {
 // arguments and result up to FP32 summation order, plus the optional epilogue work
 cudaError_t conv3TcConfigure();
 cudaError_t launchConv3Tc(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
-    const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const ConvEpilogue* ep = nullptr);
+    const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s, const ConvOptions* ep = nullptr);
 cudaError_t conv3TcErrors(unsigned* flags);
 // CTAs of the tcgen05 launch for this shape (a grid under one CTA per SM leaves the
 // tensor cores of the other SMs idle: the caller then takes launchConv3)

@@ -181,6 +181,24 @@ def test_c2_spiral_ct_torso_independent_streams(gpu, oracle):
     assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
 
 
+def test_c5_torso_full_size_conservation(gpu):
+    """The 512 x 512 x 400 torso (the voxels and tallies exceed L2): no device error,
+    energy conserved, the tally sum equal to the deposited-energy counter, and the
+    dose readout finite and non-negative."""
+    dims, spacing = (512, 512, 400), (0.08, 0.08, 0.1)
+    ph = P.torso_phantom(dims=dims, spacing=spacing, seed=7)
+    gw = gpu_world(gpu, ph)
+    beam = P.ct_spiral_params(pitch=0.8, collimation_cm=8.0, particles=20_000)
+    st = gw.run(beam, gpu.run_options(seed=9))
+    assert st["n_errors"] == 0 and st["n_histories"] > 1_000_000
+    e, _, _ = gw.tally()
+    assert st["e_deposited"] == pytest.approx(e.sum(), rel=1e-9)
+    assert e.sum() + st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-5)
+    dose, var, cnt = gw.dose()
+    assert np.isfinite(dose).all() and (dose >= 0).all() and (var >= 0).all()
+    assert cnt.sum() > 0
+
+
 @pytest.mark.parametrize("cell", [8, 16])
 def test_macro_tracking_matches_oracle(c1, gpu, cell):
     """Macro-cell majorants: shared streams follow the oracle's histories; the

@@ -40,9 +40,9 @@ METRIC = "s to \u22642% voxel dose error: MC+denoiser vs plain MC on 1 GB300; hi
 WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 materials, +-2% density jitter), "
             "120 kVp 6 mm Al + body bowtie, pitch 1.0, 40 mm collimation, 200 mm scan, 1e9 histories")
 # dram__bytes_read.sum + dram__bytes_write.sum of one full transport launch
-# (67,000,320 histories of this workload: 2.603 GB read + 1.008 GB written), from the
-# 1-pass ncu capture summarised in profiles/transport_kernel_torso.md.  bench.py's
-# launches hold up to 2^26 histories, 0.2 % more than the captured one.
+# (67,000,320 histories of this workload: 2.603 GB read + 1.008 GB written), from a
+# 1-pass ncu capture of the launch list.  bench.py's launches hold up to 2^26
+# histories, 0.2 % more than the captured one.
 TRAFFIC_BYTES_PER_LAUNCH = 3.61e9
 # the same for a full launch of the 512x512x400 workload (--workload torso512); None until captured
 TRAFFIC_BYTES_PER_LAUNCH_512 = None
@@ -113,12 +113,16 @@ WORKLOAD_512 = ("spiral CT on seeded synthetic torso 512x512x400 @0.8x0.8x1.0 mm
                 "jitter), 120 kVp 6 mm Al + body bowtie, pitch 0.8, 80 mm collimation, 200 mm scan")
 
 
-def workload(histories: float, big: bool = False, c1: bool = False):
+def workload(histories: float, big: bool = False, c1: bool = False, count_exposures=None):
     """(phantom, beam, histories per step, exposures): the 256x256x200 torso at pitch 1.0
     and 40 mm collimation, (big) the 512x512x400 torso at pitch 0.8 and 80 mm, or (c1) the
-    DX water cylinder."""
-    from opendxmc_gb300 import engine as G
+    DX water cylinder.  count_exposures(beam) -> exposure list (default: the engine's)."""
     from opendxmc_gb300 import phantoms as P
+
+    if count_exposures is None:
+        from opendxmc_gb300 import engine as G
+
+        count_exposures = G.beam_exposures
 
     if c1:
         ph = P.water_cylinder_phantom()
@@ -129,7 +133,7 @@ def workload(histories: float, big: bool = False, c1: bool = False):
     else:
         ph = P.torso_phantom(dims=(256, 256, 200), spacing=(0.15, 0.15, 0.15), seed=1)
         beam = P.ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=1.0, collimation_cm=4.0, scan_cm=20.0, particles=1)
-    n_exp = len(G.beam_exposures(beam))
+    n_exp = len(count_exposures(beam))
     ppe = int(-(-int(histories) // n_exp))
     beam["particles_per_exposure"] = ppe
     return ph, beam, n_exp * ppe, n_exp
@@ -218,33 +222,37 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from opendxmc_gb300 import build as B
-
-    if not B.LIB.exists():
-        B.build(verbose_ptxas=False)  # the exposure list comes from the library's host code
-    big = args.workload == "torso512"
-    c1 = args.workload == "c1"
-    ph, beam, _, _ = workload(args.histories, big, c1)
+    # the CPU implementation alone: the phantom (numpy) and the oracle's own exposure
+    # list; the engine library is neither built nor loaded on this arm
     from oracle import oracle as O
 
     O.build()
+    big = args.workload == "torso512"
+    c1 = args.workload == "c1"
+    ph, beam, job_hist, _ = workload(args.histories, big, c1, count_exposures=O.beam_exposures)
     threads = os.cpu_count() or 1
     w = O.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials, args.correction)
     cal = 2_000_000
     t = time.perf_counter()
     w.run(beam, seed=1, threads=threads, hist_end=cal)
     rate = cal / (time.perf_counter() - t)
-    per_step = int(max(cal, min(rate * 4.0, 2e8)))  # ~4 s of CPU work per step
+    per_step = int(min(max(cal, min(rate * 4.0, 2e8)), job_hist))  # ~4 s of CPU work per step
     h = 0
-    for _ in range(args.warmup):
-        w.run(beam, seed=1, threads=threads, hist_begin=h, hist_end=h + per_step)
+
+    def sample():
+        nonlocal h
+        if h + per_step > job_hist:  # wrap around within the job's history range
+            h = 0
+        st = w.run(beam, seed=1, threads=threads, hist_begin=h, hist_end=h + per_step)
         h += per_step
+        return st["n_histories"]
+
+    for _ in range(args.warmup):
+        sample()
     t = time.perf_counter()
     done = 0
     for _ in range(args.steps):
-        st = w.run(beam, seed=1, threads=threads, hist_begin=h, hist_end=h + per_step)
-        h += per_step
-        done += st["n_histories"]
+        done += sample()
     dt = time.perf_counter() - t
     value = done / dt
     sample = f"{per_step} histories per step of the same job (FP64 oracle port, {threads} threads)"

@@ -55,7 +55,10 @@ namespace detail {
             kvp = t.voltage();
             n = t.filters(Z, mm);
         }
-        void putBowtie(dxmcg_beam& b, const BowtieFilter& f, std::vector<double>& ang, std::vector<double>& w) const
+        // the profile's points into (ang, w), which must outlive the descriptor, and
+        // the descriptor's (n, angles, weights) fields pointing at them
+        static void putBowtieInto(const BowtieFilter& f, std::vector<double>& ang, std::vector<double>& w, int32_t& n,
+            const double*& angles, const double*& weights)
         {
             ang.clear();
             w.clear();
@@ -63,9 +66,13 @@ namespace detail {
                 ang.push_back(a);
                 w.push_back(v);
             }
-            b.n_bowtie = static_cast<int32_t>(ang.size());
-            b.bowtie_angle = ang.empty() ? nullptr : ang.data();
-            b.bowtie_weight = w.empty() ? nullptr : w.data();
+            n = static_cast<int32_t>(ang.size());
+            angles = ang.empty() ? nullptr : ang.data();
+            weights = w.empty() ? nullptr : w.data();
+        }
+        void putBowtie(dxmcg_beam& b, const BowtieFilter& f, std::vector<double>& ang, std::vector<double>& w) const
+        {
+            putBowtieInto(f, ang, w, b.n_bowtie, b.bowtie_angle, b.bowtie_weight);
         }
         static void putAec(dxmcg_beam& b, const CTAECFilter& f)
         {

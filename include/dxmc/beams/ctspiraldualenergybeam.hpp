@@ -1,6 +1,6 @@
 // dxmc/beams/ctspiraldualenergybeam.hpp -- dual-source helical CT: tube A and tube B
 // 90 degrees apart, each with its own voltage, filtration, bowtie and field of view,
-// output shared by relative mAs (beamsettingsmodel.cpp:1342-1600; exposures
+// output shared by relative mAs (beamsettingsmodel.cpp:1386-1612; exposures
 // alternate A, B as drawn at beamactorcontainer.cpp:301-313).
 #pragma once
 
@@ -53,8 +53,8 @@ public:
     void setTubeAVoltage(double kvp) { m_tubeA.setVoltage(kvp); }
     void setTubeBVoltage(double kvp) { m_tubeB.setVoltage(kvp); }
 
-    // The engine shares one bowtie profile between the tubes; tube B's is kept for
-    // source compatibility.
+    // Tube A's bowtie goes to n_bowtie/bowtie_*, tube B's to n_bowtie_b/bowtie_b_*: the
+    // engine weights each tube's photons with its own profile.
     dxmcg_beam descriptor() const
     {
         dxmcg_beam b {};
@@ -70,6 +70,7 @@ public:
         b.pitch = m_pitch;
         b.ctdi_vol_mgy = m_ctdivol;
         b.fov_b_cm = m_fovB;
+        putBowtieInto(m_bowtieB, m_bowAngleB, m_bowWeightB, b.n_bowtie_b, b.bowtie_b_angle, b.bowtie_b_weight);
         const double s = m_masA + m_masB;
         b.tube_a_weight = s > 0 ? m_masA / s : 0.5;
         return b;
@@ -95,6 +96,7 @@ private:
     double m_fovB = 33.0;
     double m_masA = 1.0, m_masB = 1.0;
     BowtieFilter m_bowtieB;
+    mutable std::vector<double> m_bowAngleB, m_bowWeightB; // tube B's profile as the descriptor points at it
     Tube m_tubeA { 140.0 }, m_tubeB { 80.0 };
 };
 

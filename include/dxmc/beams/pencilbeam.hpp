@@ -1,6 +1,7 @@
 // dxmc/beams/pencilbeam.hpp -- monoenergetic pencil beam (position, direction,
-// energy; beamsettingsmodel.cpp:621-716).  Air kerma is kept for source
-// compatibility; pencil beams are not dose-calibrated by the engine.
+// energy, air kerma; beamsettingsmodel.cpp:621-716).  With dose normalisation on,
+// the engine scales the beam so that its histories, taken as one photon per cm2
+// each, carry the set air kerma (dxmcg_beam.air_kerma_mgy).
 #pragma once
 
 #include "beamtype.hpp"
@@ -37,6 +38,7 @@ public:
         b.energy_kev = m_energy;
         b.particles_per_exposure = m_ppe;
         b.n_exposures = m_nexp;
+        b.air_kerma_mgy = m_airKerma;
         // any orthonormal pair with c0 x c1 = direction
         std::array<double, 3> ref = std::abs(m_dir[2]) < 0.9 ? std::array<double, 3> { 0, 0, 1 }
                                                               : std::array<double, 3> { 1, 0, 0 };

@@ -134,6 +134,15 @@ typedef struct {
     double ctdi_vol_mgy;
     double ctdi_w_mgy;
     double ctdi_diameter_cm;
+    /* pencil beam calibration target: air kerma (mGy) of one history per cm2
+     * (PencilBeam::setAirKerma, beamsettingsmodel.cpp:675) */
+    double air_kerma_mgy;
+    /* dual energy: tube B's bowtie (setBowtieFilterB, beamsettingsmodel.cpp:1607-1612);
+     * n_bowtie/bowtie_angle/bowtie_weight above are tube A's.  n_bowtie_b = 0: no
+     * bowtie on tube B.  Ignored by the single-tube beams. */
+    int32_t n_bowtie_b;
+    const double* bowtie_b_angle;
+    const double* bowtie_b_weight;
 } dxmcg_beam;
 
 /* One source pose (exposure(i) in beamactorcontainer.cpp:114-121). */
@@ -160,6 +169,10 @@ typedef struct {
     int32_t refill_batch;   /* dead lanes a warp gathers before starting new histories, 0 = default */
     int32_t macro_cell;     /* MACRO tracking: cell edge in voxels, 0 = default (16) */
     int32_t woodcock_steps; /* WOODCOCK tracking: steps a lane takes between regroupings, 0 = default */
+    /* per-history step limit, 0 = default (1,000,000, at most that): a history that
+     * takes more tracking steps is stopped and counted in n_errors, and the call
+     * returns DXMCG_ERR_DEVICE after the launch completes */
+    uint32_t max_steps;
 } dxmcg_run_options;
 
 typedef struct {
@@ -196,6 +209,15 @@ DXMCG_API int dxmcg_tube_al_hvl(double kvp, int n_filters, const int32_t* filter
     double* hvl_mm);
 /* numberOfExposures()/exposure(i) (beamactorcontainer.cpp:114-121); out may be NULL to count */
 DXMCG_API int dxmcg_beam_exposures(const dxmcg_beam* beam, dxmcg_exposure* out, int cap, int* n_out);
+/* The factor dxmcg_transport_run applies to every history weight when
+ * opts->normalize is set (the trailing `true` of transport(...),
+ * simulationpipeline.cpp:165), referred to all N = exposures x
+ * particles_per_exposure histories of the beam: DX/CBCT from dap_mgycm2, pencil
+ * from air_kerma_mgy (host arithmetic only), CT from the CTDI target by a
+ * one-rotation run on a CTDI phantom (needs a device).  1 when normalize is 0 or
+ * the beam has no target. */
+DXMCG_API int dxmcg_beam_calibration(const dxmcg_beam* beam, int correction, const dxmcg_run_options* opts,
+    double* factor);
 
 /* ---- world: World<AAVoxelGrid<5, C, 255>> (simulationpipeline.cpp:127-153) ---- */
 DXMCG_API int dxmcg_world_create(const int32_t dims[3], const double spacing_cm[3], const dxmcg_material* materials,
@@ -261,10 +283,15 @@ DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_o
  * statistics, tables, exposures, spectra, bowtie) lives in one 512 KiB
  * file-scope __device__ array that each GPU loading the library keeps until exit.
  * Limits: at most 16 materials and 4096 exposures (DXMCG_ERR_CAPACITY beyond).
- * The first call on a device looks the array up (cudaGetSymbolAddress) and so
- * should come before any stream capture.  Calls share the array: calls that
- * overlap on the GPU race, so issue them one after another.  The call runs on
- * `cuda_stream` (NULL: the default stream) and returns after it completes.
+ * CT beams with opts->normalize set and a CTDIvol or CTDIw target are refused
+ * (DXMCG_ERR_ARGUMENT): their calibration simulates a CTDI phantom world, which
+ * needs device allocations; DX/CBCT (DAP) and pencil (air kerma) calibration work.
+ * The first call on a device looks the array up (cudaGetSymbolAddress).  Calls
+ * share the array: calls that overlap on the GPU race, so issue them one after
+ * another.  The call runs on `cuda_stream` (NULL: the default stream), reads
+ * validation results back and synchronises that stream partway, and returns after
+ * the stream completes; so no call may be made on a stream that is being captured
+ * into a CUDA graph (such a call returns DXMCG_ERR_ARGUMENT before any work).
  * Deposits are added to device_tally (N records, zero it to start afresh);
  * stats->kernel_ms is 0 here and total_ms is the host wall time of the run. */
 typedef struct {
@@ -352,6 +379,12 @@ typedef struct {
 } dxmcg_denoiser_config;
 DXMCG_API int dxmcg_denoiser_create(const dxmcg_denoiser_config* config, dxmcg_denoiser** out);
 DXMCG_API void dxmcg_denoiser_destroy(dxmcg_denoiser* d);
+/* Polls of each wait by which one role of the tcgen05 convolution (MMA issue,
+ * staging, epilogue) hands work to another before it gives up (0: the default,
+ * 2^24; the first poll never blocks).  A convolution that gives up waits for the
+ * copies and MMAs it already started, leaves its output unwritten, and the call
+ * returns DXMCG_ERR_DEVICE; later calls run normally.  For tests of that path. */
+DXMCG_API int dxmcg_denoiser_set_wait_limit(dxmcg_denoiser* d, uint32_t polls);
 /* parameters as one FP32 vector: per conv layer (enc0a, enc0b, ..., enc(L-1)b,
  * dec(L-2)a, dec(L-2)b, ..., dec0a, dec0b) weights [Cout][27][Cin] then bias
  * [Cout]; then the head's weights [channels[0]] and bias */

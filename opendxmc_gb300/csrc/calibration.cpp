@@ -15,7 +15,9 @@
 //    CTDIvol = CTDIw / pitch (spiral) or CTDIw * collimation / slice spacing
 //    (sequential).  F = CTDIw_target / (CTDIw per history-per-rotation * histories
 //    per rotation of the beam).
-//  * pencil beams are not calibrated (F = 1).
+//  * pencil beams (setAirKerma, beamsettingsmodel.cpp:675): the air kerma of a fluence
+//    of one photon per cm2 is E (mu_tr/rho)_air, so with the target air kerma K of the
+//    beam's N histories taken as N photons per cm2, F = K / (N E (mu_tr/rho)_air(E)).
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -169,6 +171,11 @@ namespace {
     }
 } // namespace
 
+double airKermaPerHistory(const dxmcg_beam& b)
+{
+    return b.energy_kev * airEnergyAbsorption(b.energy_kev) * kKeVToMilliGrayGram;
+}
+
 double dapPerHistory(const dxmcg_beam& b)
 {
     const auto s = tubeSpectrum(b.kvp, b.anode_angle_deg, b.n_filters, b.filter_Z, b.filter_mm);
@@ -192,6 +199,17 @@ int calibrationFactor(const dxmcg_beam& b, int correction, const dxmcg_run_optio
                 return DXMCG_ERR_ARGUMENT;
             }
             F = b.dap_mgycm2 / (static_cast<double>(nHist) * per);
+        }
+        return DXMCG_OK;
+    }
+    if (b.type == DXMCG_BEAM_PENCIL) {
+        if (b.air_kerma_mgy > 0) {
+            const double per = airKermaPerHistory(b);
+            if (!(per > 0) || nHist == 0) {
+                err = "calibration: pencil energy out of range";
+                return DXMCG_ERR_ARGUMENT;
+            }
+            F = b.air_kerma_mgy / (static_cast<double>(nHist) * per);
         }
         return DXMCG_OK;
     }

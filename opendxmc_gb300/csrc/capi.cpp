@@ -595,6 +595,28 @@ DXMCG_API int dxmcg_beam_exposures(const dxmcg_beam* beam, dxmcg_exposure* out, 
     return DXMCG_OK;
 }
 
+DXMCG_API int dxmcg_beam_calibration(const dxmcg_beam* beam, int correction, const dxmcg_run_options* opts,
+    double* factor)
+{
+    if (!beam || !factor)
+        return fail(DXMCG_ERR_ARGUMENT, "beam_calibration: null argument");
+    if (correction < 0 || correction > 2)
+        return fail(DXMCG_ERR_ARGUMENT, "beam_calibration: correction must be 0, 1 or 2");
+    std::vector<dxmcg_exposure> ex;
+    if (expandExposures(*beam, ex) != DXMCG_OK || ex.empty())
+        return fail(DXMCG_ERR_ARGUMENT, "beam_calibration: invalid beam geometry");
+    dxmcg_run_options o {};
+    o.seed = 1;
+    if (opts)
+        o = *opts;
+    const uint64_t nHist = static_cast<uint64_t>(ex.size()) * beam->particles_per_exposure;
+    std::string err;
+    const int rc = calibrationFactor(*beam, correction, o, nHist, true, *factor, err);
+    if (rc != DXMCG_OK)
+        return fail(rc, "beam_calibration: " + err);
+    return DXMCG_OK;
+}
+
 DXMCG_API int dxmcg_world_create(const int32_t dims[3], const double spacing_cm[3], const dxmcg_material* materials,
     int n_materials, int correction, dxmcg_world** out)
 {

@@ -238,6 +238,8 @@ namespace {
             : 0;
         const int nItems = myTiles * nSlices;
         volatile int* abortp = &abortFlag;
+        // limit of the hand-over waits between the roles (the drains keep kPolls)
+        const uint32_t hp = ep.handoverPolls ? ep.handoverPolls : kPolls;
 
         if (warp == 0)
             umma::tmemAlloc(&tmemBase, S::kCols);
@@ -311,13 +313,13 @@ namespace {
                     const int sl = it % nSlices;
                     const int k = it / nSlices; // this CTA's brick number
                     const int set = k & 1;
-                    ok = umma::mbarWaitOrAbort(&full[b], use & 1u, kPolls, abortp);
+                    ok = umma::mbarWaitOrAbort(&full[b], use & 1u, hp, abortp);
                     if (ok && byTma(sl)) {
-                        ok = umma::mbarWaitOrAbort(&tmaFull[b], tmaPhase >> b & 1u, kPolls, abortp);
+                        ok = umma::mbarWaitOrAbort(&tmaFull[b], tmaPhase >> b & 1u, hp, abortp);
                         tmaPhase ^= 1u << b;
                     }
                     if (ok && sl == 0 && k >= 2)
-                        ok = umma::mbarWaitOrAbort(&accEmpty[set], static_cast<uint32_t>((k >> 1) - 1) & 1u, kPolls,
+                        ok = umma::mbarWaitOrAbort(&accEmpty[set], static_cast<uint32_t>((k >> 1) - 1) & 1u, hp,
                             abortp);
                     if (!ok)
                         break;
@@ -365,7 +367,7 @@ namespace {
             for (int it = 0; it < nItems; ++it) {
                 const int b = it % stages;
                 const uint32_t use = static_cast<uint32_t>(it / stages);
-                if (use >= 1 && !umma::mbarWaitOrAbort(&empty[b], (use - 1) & 1u, kPolls, abortp)) {
+                if (use >= 1 && !umma::mbarWaitOrAbort(&empty[b], (use - 1) & 1u, hp, abortp)) {
                     ok = false;
                     break;
                 }
@@ -484,7 +486,7 @@ namespace {
             const int Dh = D >> 1, Hh = H >> 1, Wh = W >> 1;
             for (int k = 0; k < myTiles; ++k) {
                 const int set = k & 1;
-                if (!umma::mbarWaitOrAbort(&accFull[set], static_cast<uint32_t>(k >> 1) & 1u, kPolls, abortp)) {
+                if (!umma::mbarWaitOrAbort(&accFull[set], static_cast<uint32_t>(k >> 1) & 1u, hp, abortp)) {
                     *abortp = 1;
                     break;
                 }

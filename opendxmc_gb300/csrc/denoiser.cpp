@@ -41,6 +41,7 @@ struct dxmcg_denoiser {
     bool tensorCores = true;  // tcgen05 convolutions (else warp-level mma.sync)
     bool tcEverywhere = false; // tcgen05 even where the grid has fewer bricks than SMs
     int sms = 1;              // streaming multiprocessors of the device
+    uint32_t waitPolls = 0;   // hand-over wait limit of the tcgen05 convolution (0: default)
 
     // activations and gradients of the current shape, per level
     int B = 0, D = 0, H = 0, W = 0;
@@ -137,9 +138,12 @@ int conv(dxmcg_denoiser* d, int k, const nn::ConvIn& in, int l, bf16* out, cudaS
     const bool tc = useTensorCores(d, Dl, Hl, Wl, ly.cout);
     if (fused)
         *fused = tc && ep;
-    if (tc)
+    if (tc) {
+        nn::ConvOptions o = ep ? *ep : nn::ConvOptions {};
+        o.handoverPolls = d->waitPolls;
         NN_CUDA(nn::launchConv3Tc(in, d->B, Dl, Hl, Wl, ly.cin, d->pb.p + ly.w, d->p.p + ly.b, ly.cout, true, out, s,
-            ep));
+            &o));
+    }
     else
         NN_CUDA(nn::launchConv3(in, d->B, Dl, Hl, Wl, ly.cin, d->pb.p + ly.w, d->p.p + ly.b, ly.cout, true, out, s));
     return DXMCG_OK;
@@ -279,9 +283,12 @@ int layerBack(dxmcg_denoiser* d, int k, const nn::ConvIn& xin, const bf16* y, co
     NN_CUDA(nn::launchReluBackward(dy, y, d->dz.p, d->nvox(l), ly.cout, d->g.p + ly.b, s));
     NN_CUDA(nn::launchWgrad(xin, d->dz.p, d->B, Dl, Hl, Wl, ly.cin, ly.cout, d->g.p + ly.w, s));
     if (dxOut) {
-        if (useTensorCores(d, Dl, Hl, Wl, ly.cin))
+        if (useTensorCores(d, Dl, Hl, Wl, ly.cin)) {
+            nn::ConvOptions o;
+            o.handoverPolls = d->waitPolls;
             NN_CUDA(nn::launchConv3Tc(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr,
-                ly.cin, false, dxOut, s));
+                ly.cin, false, dxOut, s, &o));
+        }
         else
             NN_CUDA(nn::launchConv3(plain(d->dz.p, ly.cout), d->B, Dl, Hl, Wl, ly.cout, d->wt.p + ly.wt, nullptr,
                 ly.cin, false, dxOut, s));
@@ -512,6 +519,14 @@ DXMCG_API void dxmcg_denoiser_destroy(dxmcg_denoiser* d)
     cudaSetDevice(d->device);
     cudaDeviceSynchronize();
     delete d;
+}
+
+DXMCG_API int dxmcg_denoiser_set_wait_limit(dxmcg_denoiser* d, uint32_t polls)
+{
+    if (!d)
+        return fail(DXMCG_ERR_ARGUMENT, "denoiser_set_wait_limit: null denoiser");
+    d->waitPolls = polls;
+    return DXMCG_OK;
 }
 
 DXMCG_API int dxmcg_denoiser_param_count(const dxmcg_denoiser* d, uint64_t* n)

@@ -36,7 +36,11 @@ cudaError_t conv3Configure(); // opt the kernels into their shared-memory size (
 //           to the order of the eight additions (D, H, W even);
 //   head:   for a 16-channel output, the 1x1x1 head (16 weights, then the bias) in
 //           place of the output, exactly as launchHead without a target: headPred[v]
-//           = the prediction, headOut[v] = it times headScale (either may be null).
+//           = the prediction, headOut[v] = it times headScale (either may be null);
+//   handoverPolls: polls of each wait by which one role of the kernel hands work to
+//           another before it gives up (0: 2^24); the waits for copies and MMAs already
+//           in flight keep the default limit, so a kernel that gives up still returns
+//           only after its own asynchronous work has landed.
 struct ConvOptions {
     const int* list = nullptr;
     const int* listLen = nullptr;
@@ -45,6 +49,7 @@ struct ConvOptions {
     float* headPred = nullptr;
     double* headOut = nullptr;
     double headScale = 1.0;
+    uint32_t handoverPolls = 0;
 };
 
 // tcgen05 (5th-generation tensor core) form of launchConv3 (conv_tc.cu); the same

@@ -454,23 +454,28 @@ namespace dev {
         atomicAdd(&tally[v].n, 1ull);
     }
 
-    __device__ __forceinline__ float bowtieAt(const DevBowtie* __restrict__ b, float a)
+    // relative bowtie weight of tube `tube` at |fan angle| a (1 when that tube has none)
+    __device__ __forceinline__ float bowtieAt(const DevBowtie* __restrict__ b, int tube, float a)
     {
-        const int n = b->n;
-        if (a <= b->ang[0])
-            return b->w[0];
-        if (a >= b->ang[n - 1])
-            return b->w[n - 1];
+        const int n = b->n[tube];
+        const float* __restrict__ ang = b->ang[tube];
+        const float* __restrict__ w = b->w[tube];
+        if (n <= 0)
+            return 1.0f;
+        if (a <= ang[0])
+            return w[0];
+        if (a >= ang[n - 1])
+            return w[n - 1];
         int lo = 0, hi = n - 1;
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
-            if (b->ang[mid] <= a)
+            if (ang[mid] <= a)
                 lo = mid;
             else
                 hi = mid;
         }
-        const float t = (a - b->ang[lo]) / (b->ang[hi] - b->ang[lo]);
-        return b->w[lo] + t * (b->w[hi] - b->w[lo]);
+        const float t = (a - ang[lo]) / (ang[hi] - ang[lo]);
+        return w[lo] + t * (w[hi] - w[lo]);
     }
 
     // exposure of history h (histories are numbered exposure-major)
@@ -513,7 +518,7 @@ namespace dev {
         ph.pz = ex->pos[2];
         float w = ex->weight;
         if (J.bowtie)
-            w *= bowtieAt(J.bowtie, fabsf(ax)) * J.bowtie->inv_norm[tube];
+            w *= bowtieAt(J.bowtie, tube, fabsf(ax)) * J.bowtie->inv_norm[tube];
         ph.w = w;
     }
 

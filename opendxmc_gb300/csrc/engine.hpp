@@ -67,10 +67,12 @@ struct DevSpectrum {
     int32_t alias[kMaxSpectrum];
 };
 
+// One bowtie profile per tube (tube 1: dual-energy tube B); n[t] = 0 leaves that
+// tube's weights at 1 (and inv_norm[t] = 1).
 struct DevBowtie {
-    int n;
-    float ang[kMaxBowtie];
-    float w[kMaxBowtie];
+    int n[2];
+    float ang[2][kMaxBowtie];
+    float w[2][kMaxBowtie];
     float inv_norm[2];
 };
 
@@ -108,11 +110,12 @@ struct DevJob {
     int n_exp;
     unsigned long long ppe;
     const DevSpectrum* spec; // [2]
-    const DevBowtie* bowtie; // nullptr: none
+    const DevBowtie* bowtie; // nullptr: no bowtie on either tube
     int beam_type;
     float pencil_energy;
     uint32_t key0, key1, stream;
     int tracking;
+    uint32_t maxSteps; // per-history step limit (kErrStepLimit beyond it)
 };
 
 struct DevCounters {
@@ -208,6 +211,8 @@ int reportError(int code, const std::string& msg);
 // dose calibration (calibration.cpp): DAP per history of the beam's spectrum, and the
 // factor F applied to every history weight when opts.normalize is set
 double dapPerHistory(const dxmcg_beam& b);
+// air kerma (mGy) of one pencil-beam history per cm2: E (mu_tr/rho)_air(E)
+double airKermaPerHistory(const dxmcg_beam& b);
 int calibrationFactor(const dxmcg_beam& b, int correction, const dxmcg_run_options& o, uint64_t nHist,
     bool allowPhantom, double& F, std::string& err);
 

@@ -210,16 +210,26 @@ int buildHostJob(const dxmcg_beam& b, const int32_t dims[3], const double spacin
         return DXMCG_ERR_ARGUMENT;
     }
 
+    // bowtie profiles: tube A's from n_bowtie/bowtie_*, dual-energy tube B's from
+    // n_bowtie_b/bowtie_b_* (the two are set independently, beamsettingsmodel.cpp:1581-1612)
     out.hasBowtie = false;
-    if (b.n_bowtie > 0 && b.bowtie_angle && b.bowtie_weight) {
-        if (b.n_bowtie > kMaxBowtie) {
+    out.bowtie = DevBowtie {};
+    const bool dualBeam = b.type == DXMCG_BEAM_CT_SPIRAL_DUAL_ENERGY;
+    for (int t = 0; t < 2; ++t) {
+        out.bowtie.inv_norm[t] = 1.0f;
+        const int n = t == 0 ? b.n_bowtie : (dualBeam ? b.n_bowtie_b : 0);
+        const double* angles = t == 0 ? b.bowtie_angle : b.bowtie_b_angle;
+        const double* weights = t == 0 ? b.bowtie_weight : b.bowtie_b_weight;
+        if (n <= 0 || !angles || !weights)
+            continue;
+        if (n > kMaxBowtie) {
             err = "beam: bowtie has too many points";
             return DXMCG_ERR_ARGUMENT;
         }
         // sorted by angle: the bowtie JSON lists points unordered (bowtiefilters.json:4-32)
         std::vector<std::pair<double, double>> pts;
-        for (int i = 0; i < b.n_bowtie; ++i)
-            pts.emplace_back(b.bowtie_angle[i], b.bowtie_weight[i]);
+        for (int i = 0; i < n; ++i)
+            pts.emplace_back(angles[i], weights[i]);
         std::stable_sort(pts.begin(), pts.end(), [](const auto& x, const auto& y) { return x.first < y.first; });
         BowtieProfile prof;
         for (const auto& p : pts) {
@@ -227,22 +237,20 @@ int buildHostJob(const dxmcg_beam& b, const int32_t dims[3], const double spacin
             prof.w.push_back(p.second);
         }
         DevBowtie& db = out.bowtie;
-        db = DevBowtie {};
-        db.n = static_cast<int>(pts.size());
-        for (int i = 0; i < db.n; ++i) {
-            db.ang[i] = static_cast<float>(prof.ang[i]);
-            db.w[i] = static_cast<float>(prof.w[i]);
+        db.n[t] = n;
+        for (int i = 0; i < n; ++i) {
+            db.ang[t][i] = static_cast<float>(prof.ang[i]);
+            db.w[t][i] = static_cast<float>(prof.w[i]);
         }
-        for (int t = 0; t < 2; ++t) {
-            double half = 0;
-            for (const auto& e : ex)
-                if (e.tube == t) {
-                    half = e.half[0];
-                    break;
-                }
-            const double m = prof.mean(half);
-            db.inv_norm[t] = static_cast<float>(m > 0 ? 1.0 / m : 1.0);
-        }
+        // normalised to a mean weight of 1 over the tube's fan
+        double half = 0;
+        for (const auto& e : ex)
+            if (e.tube == t) {
+                half = e.half[0];
+                break;
+            }
+        const double m = prof.mean(half);
+        db.inv_norm[t] = static_cast<float>(m > 0 ? 1.0 / m : 1.0);
         out.hasBowtie = true;
     }
     return DXMCG_OK;
@@ -270,6 +278,7 @@ void fillJobFields(DevJob& J, const dxmcg_beam& b, const dxmcg_run_options& o, c
     J.key1 = static_cast<uint32_t>(o.seed >> 32);
     J.stream = o.stream;
     J.tracking = o.tracking;
+    J.maxSteps = o.max_steps > 0 ? std::min(o.max_steps, kMaxStepsPerHistory) : kMaxStepsPerHistory;
 }
 
 } // namespace dxmcg

@@ -13,11 +13,17 @@
 // until the process exits.
 //
 // The host finds the array's device address with cudaGetSymbolAddress, once per
-// device, with that device current, on the first call made on that device; that
-// first call should therefore come before any stream capture.  All calls share
-// the array and it keeps the last call's contents: each call clears the counters
-// it needs to start at zero, and calls that overlap on the GPU (on different
-// streams or threads) race on it, so issue them one after another.
+// device, with that device current, on the first call made on that device.  Every
+// call reads its validation flags back and synchronises its stream partway, and
+// again at the end, so no call can be captured into a CUDA graph: a call on a
+// capturing stream is refused before it queues any work.  All calls share the
+// array and it keeps the last call's contents: each call clears the counters it
+// needs to start at zero, and calls that overlap on the GPU (on different streams
+// or threads) race on it, so issue them one after another.
+//
+// Calibration: DX/CBCT beams (dose-area product) and pencil beams (air kerma) are
+// normalised analytically; CT beams with a CTDI target are refused, because their
+// calibration simulates a CTDI phantom world, which needs device allocations.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -179,6 +185,15 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     if (rc != DXMCG_OK)
         return rc;
     const cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    const cudaError_t qe = cudaStreamIsCapturing(s, &capture);
+    if (qe != cudaSuccess || capture != cudaStreamCaptureStatusNone) {
+        if (qe != cudaSuccess)
+            (void)cudaGetLastError();
+        return fail(DXMCG_ERR_ARGUMENT,
+            "transport_run_noalloc: the stream is being captured; this call synchronises its stream and "
+            "cannot be captured into a CUDA graph");
+    }
     auto* counters = reinterpret_cast<DevCounters*>(base + kOffCounters);
     auto* flags = reinterpret_cast<unsigned*>(base + kOffFlags);
 

@@ -499,7 +499,7 @@ namespace {
                         st = rt < pe + ic ? kCompton : kRayleigh;
                     }
                 }
-                if (st != kDead && ++steps > kMaxStepsPerHistory) {
+                if (st != kDead && ++steps > J.maxSteps) {
                     err |= kErrStepLimit;
                     st = kDead;
                     error = true;

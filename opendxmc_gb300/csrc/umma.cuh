@@ -129,12 +129,24 @@ namespace umma {
 
     // Like mbarWait, but also gives up as soon as *abort is set (checked every 64 polls):
     // lets the roles of a warp-specialised CTA leave together when one of them timed out.
+    // The first poll is a non-blocking test (mbarrier.test_wait), the later ones may
+    // suspend the thread for a while (try_wait): a limit of 1 gives up at once unless
+    // the phase has already completed.
     __device__ __forceinline__ bool mbarWaitOrAbort(uint64_t* bar, uint32_t parity, uint32_t limit,
         const volatile int* abort)
     {
         const uint32_t a = smemAddr(bar);
-        for (uint32_t i = 0; i < limit; ++i) {
-            uint32_t done;
+        if (limit == 0u)
+            return false;
+        uint32_t done;
+        asm volatile("{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     "selp.u32 %0, 1, 0, p;\n}\n"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done)
+            return true;
+        for (uint32_t i = 1; i < limit; ++i) {
             asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
                          "selp.u32 %0, 1, 0, p;\n}\n"
                          : "=r"(done)

@@ -73,9 +73,19 @@ def beam_exposures(params: dict) -> list[dict]:
              "tube": e.tube} for e in arr[:n.value]]
 
 
+def beam_calibration(params: dict, correction: int = 1, options: N.RunOptions | None = None) -> float:
+    """The factor the transport applies to every history weight with normalize set
+    (DX/CBCT: DAP, pencil: air kerma, CT: CTDI phantom run, which needs a device)."""
+    b, keep = N.make_beam(params)
+    o = options if options is not None else run_options(normalize=1)
+    out = C.c_double(0)
+    N.check(N.lib().dxmcg_beam_calibration(C.byref(b), correction, C.byref(o), C.byref(out)))
+    return out.value
+
+
 def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_size=0, blocks_per_sm=0,
                 chunk_log2=0, hist_begin=0, hist_end=0, interact_batch=0, refill_batch=0,
-                macro_cell=0, woodcock_steps=0) -> N.RunOptions:
+                macro_cell=0, woodcock_steps=0, max_steps=0) -> N.RunOptions:
     o = N.RunOptions()
     o.seed = seed
     o.stream = stream
@@ -90,6 +100,7 @@ def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_
     o.refill_batch = refill_batch
     o.macro_cell = macro_cell
     o.woodcock_steps = woodcock_steps
+    o.max_steps = max_steps
     return o
 
 
@@ -416,6 +427,11 @@ class Denoiser:
         loss = self.backward(x, target, stream, want_loss)
         self.adam(lr, stream)
         return loss
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Hand-over wait limit of the tcgen05 convolution (0: default); see
+        dxmcg_denoiser_set_wait_limit."""
+        N.check(N.lib().dxmcg_denoiser_set_wait_limit(self._h, int(polls)))
 
     def denoise_world(self, world: "GpuWorld", scale: float = 0.0, readback: bool = True):
         """(denoised dose in mGy per voxel, scale used); without readback the dose stays

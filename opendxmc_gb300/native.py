@@ -26,14 +26,16 @@ STATUS = {0: "OK", -1: "ARGUMENT", -2: "CUDA", -3: "STATE", -4: "CANCELLED", -5:
 EXPORTED = [
     "dxmcg_version", "dxmcg_last_error", "dxmcg_device_count", "dxmcg_set_device", "dxmcg_material_attenuation",
     "dxmcg_tube_spectrum",
-    "dxmcg_tube_mean_energy", "dxmcg_tube_al_hvl", "dxmcg_beam_exposures", "dxmcg_world_create",
+    "dxmcg_tube_mean_energy", "dxmcg_tube_al_hvl", "dxmcg_beam_exposures", "dxmcg_beam_calibration",
+    "dxmcg_world_create",
     "dxmcg_world_set_data", "dxmcg_world_set_data_f32", "dxmcg_world_build", "dxmcg_world_destroy",
     "dxmcg_world_clear_tally", "dxmcg_world_read_tally", "dxmcg_world_read_dose", "dxmcg_world_tables",
     "dxmcg_world_packed_density", "dxmcg_transport_run", "dxmcg_batch_create", "dxmcg_batch_info",
     "dxmcg_batch_run", "dxmcg_batch_destroy", "dxmcg_autotune", "dxmcg_transport_run_noalloc",
     "dxmcg_ct_segmentation_table", "dxmcg_ct_segment", "dxmcg_ct_segment_device", "dxmcg_organ_dose_table",
     "dxmcg_organ_dose_table_device", "dxmcg_world_organ_dose", "dxmcg_world_read_dose_postprocessed",
-    "dxmcg_denoiser_create", "dxmcg_denoiser_destroy", "dxmcg_denoiser_param_count", "dxmcg_denoiser_get_params",
+    "dxmcg_denoiser_create", "dxmcg_denoiser_destroy", "dxmcg_denoiser_set_wait_limit",
+    "dxmcg_denoiser_param_count", "dxmcg_denoiser_get_params",
     "dxmcg_denoiser_set_params", "dxmcg_denoiser_get_grads", "dxmcg_denoiser_forward", "dxmcg_denoiser_backward",
     "dxmcg_denoiser_adam", "dxmcg_denoiser_prepare_input", "dxmcg_denoiser_gather_patches", "dxmcg_world_denoise",
     "dxmcg_progress_create",
@@ -137,6 +139,10 @@ class Beam(C.Structure):
         ("ctdi_vol_mgy", C.c_double),
         ("ctdi_w_mgy", C.c_double),
         ("ctdi_diameter_cm", C.c_double),
+        ("air_kerma_mgy", C.c_double),
+        ("n_bowtie_b", C.c_int32),
+        ("bowtie_b_angle", C.POINTER(C.c_double)),
+        ("bowtie_b_weight", C.POINTER(C.c_double)),
     ]
 
 
@@ -150,7 +156,7 @@ class RunOptions(C.Structure):
                 ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk_histories_log2", C.c_int32),
                 ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64), ("interact_batch", C.c_int32),
                 ("refill_batch", C.c_int32), ("macro_cell", C.c_int32),
-                ("woodcock_steps", C.c_int32)]
+                ("woodcock_steps", C.c_int32), ("max_steps", C.c_uint32)]
 
 
 class Stats(C.Structure):
@@ -190,6 +196,7 @@ def lib() -> C.CDLL:
         "dxmcg_tube_mean_energy": (i, [d, i, pi32, pd, pd]),
         "dxmcg_tube_al_hvl": (i, [d, i, pi32, pd, pd]),
         "dxmcg_beam_exposures": (i, [C.POINTER(Beam), C.POINTER(Exposure), i, C.POINTER(C.c_int)]),
+        "dxmcg_beam_calibration": (i, [C.POINTER(Beam), i, C.POINTER(RunOptions), pd]),
         "dxmcg_world_create": (i, [pi32, pd, C.POINTER(Material), i, i, C.POINTER(vp)]),
         "dxmcg_world_set_data": (i, [vp, pd, pu8]),
         "dxmcg_world_set_data_f32": (i, [vp, pf, pu8]),
@@ -217,6 +224,7 @@ def lib() -> C.CDLL:
         "dxmcg_world_read_dose_postprocessed": (i, [vp, i, pd, pd, pd, C.POINTER(C.c_int)]),
         "dxmcg_denoiser_create": (i, [C.POINTER(DenoiserConfig), C.POINTER(vp)]),
         "dxmcg_denoiser_destroy": (None, [vp]),
+        "dxmcg_denoiser_set_wait_limit": (i, [vp, C.c_uint32]),
         "dxmcg_denoiser_param_count": (i, [vp, pu64]),
         "dxmcg_denoiser_get_params": (i, [vp, pf]),
         "dxmcg_denoiser_set_params": (i, [vp, pf]),
@@ -276,13 +284,14 @@ def make_beam(params: dict):
             for j, (z, mm) in enumerate(items):
                 fz[j] = int(z)
                 fm[j] = float(mm)
-        elif k == "bowtie":
+        elif k in ("bowtie", "bowtie_b"):
             ang = np.ascontiguousarray([a for a, _ in v], dtype=np.float64)
             wt = np.ascontiguousarray([w for _, w in v], dtype=np.float64)
             keep += [ang, wt]
-            b.n_bowtie = len(ang)
-            b.bowtie_angle = ptr(ang, C.c_double)
-            b.bowtie_weight = ptr(wt, C.c_double)
+            suf = "_b" if k == "bowtie_b" else ""
+            setattr(b, "n_bowtie" + suf, len(ang))
+            setattr(b, "bowtie" + suf + "_angle", ptr(ang, C.c_double))
+            setattr(b, "bowtie" + suf + "_weight", ptr(wt, C.c_double))
         elif k == "aec":
             start, stop, weights = v
             wt = np.ascontiguousarray(weights, dtype=np.float64)

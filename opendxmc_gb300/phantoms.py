@@ -184,6 +184,52 @@ def ct_spiral_params(kvp=120.0, al_mm=6.0, pitch=1.0, collimation_cm=4.0, scan_c
     return p
 
 
+def ct_sequential_params(kvp=120.0, al_mm=6.0, collimation_cm=4.0, n_slices=3, slice_spacing_cm=4.0,
+                         position=(0.0, 0.0, -4.0), sdd_cm=119.0, fov_cm=50.0, step_deg=5.0, particles=1_000_000,
+                         bowtie=BODY_BOWTIE) -> dict:
+    """CTSequentialBeam: axial rotations at `n_slices` table positions `slice_spacing_cm`
+    apart from `position` (beamsettingsmodel.cpp:1654-1837)."""
+    p = {
+        "type": 2, "kvp": kvp, "anode_angle_deg": 12.0, "filters": {13: al_mm}, "particles_per_exposure": particles,
+        "position": list(position), "start_angle_deg": 0.0, "step_angle_deg": step_deg,
+        "collimation_cm": collimation_cm, "scan_fov_cm": fov_cm, "sdd_cm": sdd_cm, "n_slices": n_slices,
+        "slice_spacing_cm": slice_spacing_cm,
+    }
+    if bowtie:
+        p["bowtie"] = list(bowtie)
+    return p
+
+
+def cbct_params(kvp=90.0, al_mm=4.0, sdd_cm=120.0, start_deg=0.0, stop_deg=200.0, step_deg=2.0,
+                half_angles=(0.2, 0.12), particles=1_000_000) -> dict:
+    """CBCTBeam: a cone of the given half angles rotating about z in `step_deg` steps
+    from `start_deg` to `stop_deg` (addCBCTBeam, beamsettingsmodel.cpp:718-901)."""
+    return {"type": 3, "kvp": kvp, "anode_angle_deg": 12.0, "filters": {13: al_mm},
+            "particles_per_exposure": particles, "position": [0.0, 0.0, 0.0], "rotation_axis": [0.0, 0.0, 1.0],
+            "start_angle_deg": start_deg, "stop_angle_deg": stop_deg, "step_angle_deg": step_deg, "sdd_cm": sdd_cm,
+            "half_angles": list(half_angles)}
+
+
+def ct_dual_energy_params(kvp_a=140.0, kvp_b=80.0, filters_a=None, filters_b=None, pitch=1.0, collimation_cm=4.0,
+                          scan_cm=12.0, sdd_cm=119.0, fov_a_cm=50.0, fov_b_cm=33.0, step_deg=5.0, tube_a_weight=0.5,
+                          particles=1_000_000, bowtie=BODY_BOWTIE, bowtie_b=BODY_BOWTIE) -> dict:
+    """CTSpiralDualEnergyBeam: tubes A and B 90 degrees apart, each with its own
+    voltage, filtration, field of view and bowtie (addCTSpiralDualEnergyBeam,
+    beamsettingsmodel.cpp:1386-1612)."""
+    p = {
+        "type": 5, "kvp": kvp_a, "kvp_b": kvp_b, "anode_angle_deg": 12.0,
+        "filters": dict(filters_a or {13: 6.0}), "filters_b": dict(filters_b or {13: 6.0, 50: 0.4}),
+        "particles_per_exposure": particles, "start": [0.0, 0.0, -0.5 * scan_cm], "stop": [0.0, 0.0, 0.5 * scan_cm],
+        "start_angle_deg": 0.0, "step_angle_deg": step_deg, "pitch": pitch, "collimation_cm": collimation_cm,
+        "scan_fov_cm": fov_a_cm, "fov_b_cm": fov_b_cm, "sdd_cm": sdd_cm, "tube_a_weight": tube_a_weight,
+    }
+    if bowtie:
+        p["bowtie"] = list(bowtie)
+    if bowtie_b:
+        p["bowtie_b"] = list(bowtie_b)
+    return p
+
+
 def ellipsoid_phantom(dims, spacing, seed=1, jitter=0.02, n_inserts=8) -> Phantom:
     """Seeded six-material ellipsoid phantom of any grid size: an adipose body
     ellipsoid filling 80-90 % of the grid, a muscle wall and a soft-tissue

@@ -346,6 +346,43 @@ double or_tube_al_hvl_mm(double kvp, int n_filters, const int32_t* fZ, const dou
     return 0.5 * (lo + hi);
 }
 
+/* Analytic dose calibration (calibration.cpp in the engine; the trailing `true` of
+ * transport(world, beam, progress, true), simulationpipeline.cpp:165): the factor
+ * applied to every history weight so that the N = n_hist histories of the beam
+ * deliver its target.  DX / CBCT: the dose-area product per photon of a point source
+ * is E (mu_tr/rho)_air at any distance (setDAPvalue, beamsettingsmodel.cpp:576);
+ * pencil: the air kerma of one photon per cm2 is E (mu_tr/rho)_air (setAirKerma,
+ * beamsettingsmodel.cpp:675).  1 without a target; -1 for CT beams (their factor
+ * comes from a CTDI phantom simulation, not restated here). */
+double or_calibration_factor(const or_beam* b, uint64_t n_hist)
+{
+    const double k = 1.602176634e-10; /* mGy g / keV */
+    if (n_hist == 0)
+        return 1.0;
+    if (b->type == OR_BEAM_DX || b->type == OR_BEAM_CBCT) {
+        if (!(b->dap_mgycm2 > 0.0))
+            return 1.0;
+        double E[512], w[512], ph[512], ic[512], co[512];
+        const int n = or_tube_spectrum(b->kvp, b->anode_angle_deg, b->n_filters, b->filter_Z, b->filter_mm, E, w, 512);
+        if (n <= 0)
+            return 1.0;
+        or_attenuation(&AIR, 1, n, E, ph, ic, co);
+        double per = 0.0;
+        for (int i = 0; i < n; ++i)
+            per += w[i] * E[i] * (ph[i] + ic[i] * or_kn_energy_transfer_fraction(E[i]));
+        return b->dap_mgycm2 / ((double)n_hist * per * k);
+    }
+    if (b->type == OR_BEAM_PENCIL) {
+        if (!(b->air_kerma_mgy > 0.0))
+            return 1.0;
+        const double E = b->energy_kev;
+        double ph, ic, co;
+        or_attenuation(&AIR, 1, 1, &E, &ph, &ic, &co);
+        return b->air_kerma_mgy / ((double)n_hist * E * (ph + ic * or_kn_energy_transfer_fraction(E)) * k);
+    }
+    return -1.0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11).  */
 /* ------------------------------------------------------------------------- */
@@ -1336,7 +1373,7 @@ typedef struct {
     int n;
     double ang[256];
     double w[256];
-    double norm[2];
+    double norm; /* mean over the tube's fan, |angle| in [0, half] */
 } bowtie_t;
 
 static double bowtie_eval(const bowtie_t* b, double a)
@@ -1384,7 +1421,7 @@ typedef struct {
     int n_exp;
     double gorigin[3];
     alias_table spec[2];
-    bowtie_t bow;
+    bowtie_t bow[2]; /* per tube: A, and dual-energy B */
     uint64_t seed;
     uint32_t stream;
     int tracking;
@@ -1522,8 +1559,9 @@ static void sample_source(const run_ctx* c, uint64_t h, rng_t* r, double* E_out,
         p[a] = ex->pos[a] - c->gorigin[a];
     }
     double wgt = ex->weight;
-    if (c->bow.n > 0)
-        wgt *= bowtie_eval(&c->bow, fabs(ax)) / c->bow.norm[ex->tube];
+    const bowtie_t* bow = &c->bow[ex->tube];
+    if (bow->n > 0)
+        wgt *= bowtie_eval(bow, fabs(ax)) / bow->norm;
     *E_out = E;
     *wgt_out = wgt;
 }
@@ -1781,32 +1819,40 @@ static int ctx_setup(run_ctx* c, or_world* w, const or_beam* b)
             memcpy(c->spec[t].E, E, n * sizeof(double));
         }
     }
-    if (b->n_bowtie > 0 && b->bowtie_angle && b->bowtie_weight) {
+    /* bowtie profiles: tube A from n_bowtie/bowtie_*, dual-energy tube B from
+     * n_bowtie_b/bowtie_b_* (set independently, beamsettingsmodel.cpp:1581-1612) */
+    for (int t = 0; t < 2; ++t) {
+        bowtie_t* bw = &c->bow[t];
+        bw->n = 0;
+        bw->norm = 1.0;
+        const int nb = t == 0 ? b->n_bowtie : (b->type == OR_BEAM_CT_SPIRAL_DUAL ? b->n_bowtie_b : 0);
+        const double* ang = t == 0 ? b->bowtie_angle : b->bowtie_b_angle;
+        const double* wt = t == 0 ? b->bowtie_weight : b->bowtie_b_weight;
+        if (nb <= 0 || !ang || !wt)
+            continue;
         /* sort by angle (the bowtie JSON is unordered, bowtiefilters.json:4-32) */
-        int n = b->n_bowtie > 256 ? 256 : b->n_bowtie;
+        const int n = nb > 256 ? 256 : nb;
         for (int i = 0; i < n; ++i) {
-            c->bow.ang[i] = b->bowtie_angle[i];
-            c->bow.w[i] = b->bowtie_weight[i];
+            bw->ang[i] = ang[i];
+            bw->w[i] = wt[i];
         }
         for (int i = 1; i < n; ++i)
-            for (int j = i; j > 0 && c->bow.ang[j - 1] > c->bow.ang[j]; --j) {
-                double t = c->bow.ang[j];
-                c->bow.ang[j] = c->bow.ang[j - 1];
-                c->bow.ang[j - 1] = t;
-                t = c->bow.w[j];
-                c->bow.w[j] = c->bow.w[j - 1];
-                c->bow.w[j - 1] = t;
+            for (int j = i; j > 0 && bw->ang[j - 1] > bw->ang[j]; --j) {
+                double tmp = bw->ang[j];
+                bw->ang[j] = bw->ang[j - 1];
+                bw->ang[j - 1] = tmp;
+                tmp = bw->w[j];
+                bw->w[j] = bw->w[j - 1];
+                bw->w[j - 1] = tmp;
             }
-        c->bow.n = n;
-        for (int t = 0; t < 2; ++t) {
-            double half = 0.0;
-            for (int i = 0; i < c->n_exp; ++i)
-                if (c->exps[i].tube == t) {
-                    half = c->exps[i].half[0];
-                    break;
-                }
-            c->bow.norm[t] = bowtie_mean(&c->bow, half);
-        }
+        bw->n = n;
+        double half = 0.0;
+        for (int i = 0; i < c->n_exp; ++i)
+            if (c->exps[i].tube == t) {
+                half = c->exps[i].half[0];
+                break;
+            }
+        bw->norm = bowtie_mean(bw, half);
     }
     return 0;
 }

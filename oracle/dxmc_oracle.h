@@ -109,6 +109,11 @@ typedef struct {
     double ctdi_vol_mgy;
     double ctdi_w_mgy;
     double ctdi_diameter_cm;
+    double air_kerma_mgy; /* pencil beam: air kerma of one history per cm2 */
+    /* dual energy: tube B's bowtie (the fields above are tube A's); 0 points: none */
+    int32_t n_bowtie_b;
+    const double* bowtie_b_angle;
+    const double* bowtie_b_weight;
 } or_beam;
 
 typedef struct {
@@ -151,6 +156,9 @@ double or_uniform_from_u32(uint32_t x);
 void or_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, int n_draws, uint32_t* out);
 /* beam geometry */
 int or_beam_exposures(const or_beam* b, or_exposure* out, int cap);
+/* analytic calibration factor over n_hist histories: DX/CBCT (DAP), pencil (air
+ * kerma); 1 without a target, -1 for CT beams */
+double or_calibration_factor(const or_beam* b, uint64_t n_hist);
 /* traversal on a grid-local ray; returns number of segments (or -needed if cap too small) */
 int or_siddon_f32(const float o[3], const float d[3], const int32_t n[3], const float sp[3], int cap,
     int64_t* idx, float* len);

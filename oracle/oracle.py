@@ -93,6 +93,10 @@ class Beam(C.Structure):
         ("ctdi_vol_mgy", C.c_double),
         ("ctdi_w_mgy", C.c_double),
         ("ctdi_diameter_cm", C.c_double),
+        ("air_kerma_mgy", C.c_double),
+        ("n_bowtie_b", C.c_int32),
+        ("bowtie_b_angle", C.POINTER(C.c_double)),
+        ("bowtie_b_weight", C.POINTER(C.c_double)),
     ]
 
 
@@ -280,13 +284,14 @@ def make_beam(params: dict) -> tuple[Beam, list]:
             setattr(b, "n_filters" + suf, n)
             setattr(b, "filter_Z" + suf, fz)
             setattr(b, "filter_mm" + suf, fm)
-        elif k == "bowtie":
+        elif k in ("bowtie", "bowtie_b"):
             ang = np.ascontiguousarray([a for a, _ in v], dtype=np.float64)
             wt = np.ascontiguousarray([w for _, w in v], dtype=np.float64)
             keep += [ang, wt]
-            b.n_bowtie = len(v)
-            b.bowtie_angle = _p(ang, C.c_double)
-            b.bowtie_weight = _p(wt, C.c_double)
+            suf = "_b" if k == "bowtie_b" else ""
+            setattr(b, "n_bowtie" + suf, len(v))
+            setattr(b, "bowtie" + suf + "_angle", _p(ang, C.c_double))
+            setattr(b, "bowtie" + suf + "_weight", _p(wt, C.c_double))
         elif k == "aec":
             start, stop, weights = v
             wt = np.ascontiguousarray(weights, dtype=np.float64)
@@ -306,6 +311,16 @@ def make_beam(params: dict) -> tuple[Beam, list]:
         else:
             setattr(b, k, v)
     return b, keep
+
+
+def calibration_factor(params: dict, n_hist: int) -> float:
+    """Analytic calibration factor of a DX/CBCT (DAP) or pencil (air kerma) beam
+    over n_hist histories; 1 without a target."""
+    b, keep = make_beam(params)
+    L = lib()
+    L.or_calibration_factor.restype = C.c_double
+    L.or_calibration_factor.argtypes = [C.POINTER(Beam), C.c_uint64]
+    return L.or_calibration_factor(C.byref(b), n_hist)
 
 
 def beam_exposures(params: dict) -> list[dict]:

@@ -18,11 +18,15 @@ Sources (paths inside the reference project):
                                        and types (read from the source text)
 """
 import json
+import os
 import re
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+# the reference project root: first argument, else $OPENDXMC_REFERENCE, else a checkout
+# named "reference" beside this repository
+REF = Path(sys.argv[1] if len(sys.argv) > 1 else
+           os.environ.get("OPENDXMC_REFERENCE") or Path(__file__).resolve().parents[3] / "reference")
 OUT = Path(__file__).resolve().parent / "reference_data.json"
 ZS = [1, 6, 7, 8, 11, 12, 15, 16, 17, 19, 20, 26, 53]
 

@@ -168,3 +168,45 @@ def test_batched_job_generator_ranges():
     again = P.ellipsoid_phantom((40, 30, 20), (0.2, 0.3, 0.25), seed=4)
     np.testing.assert_array_equal(ph.material, again.material)
     np.testing.assert_array_equal(ph.density, again.density)
+
+
+def _pencil(energy=55.0, kerma=3.5, particles=40_000, exposures=5):
+    return {"type": 4, "energy_kev": energy, "particles_per_exposure": particles, "n_exposures": exposures,
+            "position": [0.0, 40.0, 0.0], "cosines": [[0, 0, 1], [-1, 0, 0]], "air_kerma_mgy": kerma}
+
+
+@pytest.mark.parametrize("beam", [
+    _pencil(),
+    _pencil(energy=20.0, kerma=0.25, particles=7, exposures=3),
+    _pencil(energy=149.5, kerma=100.0),
+    dict(P.dx_beam_params(particles=50_000, exposures=4), dap_mgycm2=12.5),
+    {"type": 3, "kvp": 90.0, "anode_angle_deg": 12.0, "filters": {13: 4.0}, "particles_per_exposure": 1000,
+     "position": [0.0, 0.0, 0.0], "rotation_axis": [0.0, 0.0, 1.0], "start_angle_deg": 0.0,
+     "stop_angle_deg": 180.0, "step_angle_deg": 2.0, "sdd_cm": 120.0, "half_angles": [0.2, 0.1],
+     "dap_mgycm2": 30.0},
+], ids=["pencil55", "pencil20", "pencil149", "dx", "cbct"])
+def test_analytic_calibration_factor_matches_oracle(engine, oracle, beam):
+    """DX/CBCT (DAP) and pencil (air kerma, PencilBeam::setAirKerma,
+    beamsettingsmodel.cpp:675) calibration factors: host arithmetic, no device."""
+    n_hist = len(oracle.beam_exposures(beam)) * beam["particles_per_exposure"]
+    F_or = oracle.calibration_factor(beam, n_hist)
+    F = engine.beam_calibration(beam, 1, engine.run_options(normalize=1))
+    assert F == pytest.approx(F_or, rel=1e-12)
+    assert F != 1.0
+    # normalize off, or no target: no scaling
+    assert engine.beam_calibration(beam, 1, engine.run_options(normalize=0)) == 1.0
+    key = "air_kerma_mgy" if beam["type"] == 4 else "dap_mgycm2"
+    assert engine.beam_calibration(dict(beam, **{key: 0.0})) == 1.0
+
+
+def test_pencil_calibration_is_kerma_per_history():
+    """F = K / (N E (mu_tr/rho)_air(E)): doubling the target doubles F, doubling the
+    histories halves it."""
+    from opendxmc_gb300 import build
+
+    build.build(verbose_ptxas=False)
+    from opendxmc_gb300 import engine as G
+
+    f1 = G.beam_calibration(_pencil(kerma=1.0))
+    assert G.beam_calibration(_pencil(kerma=2.0)) == pytest.approx(2 * f1, rel=1e-14)
+    assert G.beam_calibration(_pencil(kerma=1.0, particles=80_000)) == pytest.approx(f1 / 2, rel=1e-14)

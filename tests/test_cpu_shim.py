@@ -1,6 +1,7 @@
 """The header-only dxmc:: layer (include/dxmc/) compiles, and OpenDXMC's own beam
 specialisation (src/libopendxmc/dxmc_specialization.cpp: the DXBeam wrapper and the
 Beam variant over all six beam types) compiles against it unchanged.  No GPU."""
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -8,7 +9,9 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-REFERENCE = Path("/root/reference/src/libopendxmc")
+# the reference project tree, when mounted: $OPENDXMC_REFERENCE, else a checkout named
+# "reference" beside this repository
+REFERENCE = Path(os.environ.get("OPENDXMC_REFERENCE") or ROOT.parent / "reference") / "src" / "libopendxmc"
 
 
 def gxx():
@@ -33,7 +36,7 @@ def test_each_header_stands_alone(header, tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-@pytest.mark.skipif(not (REFERENCE / "dxmc_specialization.cpp").exists(), reason="reference tree not mounted")
+@pytest.mark.skipif(not (REFERENCE / "dxmc_specialization.cpp").exists(), reason="reference tree not mounted (set OPENDXMC_REFERENCE)")
 def test_reference_beam_specialisation_compiles_against_the_layer():
     r = subprocess.run([gxx(), "-std=c++20", "-fsyntax-only", f"-I{ROOT / 'include'}", f"-I{REFERENCE}",
                         str(REFERENCE / "dxmc_specialization.cpp")], capture_output=True, text=True)

@@ -1,0 +1,168 @@
+"""GPU parity against the CPU oracle for the beam types beyond DX and CT spiral,
+through the C ABI: CBCT, CT sequential and dual-energy spiral CT (the Beam variant
+of dxmc_specialization.hpp:40-44, set up at beamsettingsmodel.cpp:718-1612), the
+dual-energy tubes' independent bowtie filters (setBowtieFilterA/B,
+beamsettingsmodel.cpp:1581-1612) and the pencil beam's air-kerma calibration
+(setAirKerma, beamsettingsmodel.cpp:675).
+
+Source sampling is compared photon by photon on shared Philox streams; transport
+with independent streams: per-voxel energy within 3 combined standard errors in
+>= 99 % of voxels above 5 % of the maximum, total energy within 0.3 %."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from opendxmc_gb300 import phantoms as P
+import parity
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.loads((Path(__file__).resolve().parent / "golden" / "reference_data.json").read_text())
+# a second bowtie from the reference's bowtie file (data/bowtiefilters/bowtiefilters.json)
+W1_80KV = [tuple(p) for p in GOLDEN["bowtiefilters"]["Siemens Definition Flash W1  80kV"]]
+
+
+def beams():
+    return {
+        "cbct": P.cbct_params(particles=60),
+        "ct_sequential": P.ct_sequential_params(particles=60),
+        "dual_energy": P.ct_dual_energy_params(particles=60, bowtie_b=W1_80KV),
+    }
+
+
+def worlds(gpu, oracle, ph):
+    gw = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    gw.set_data(ph.density, ph.material)
+    gw.build()
+    d, _ = gw.packed_density()
+    ow = oracle.World(ph.dims, ph.spacing, d.astype(np.float64), ph.material, ph.materials)
+    return gw, ow
+
+
+@pytest.mark.parametrize("which", ["cbct", "ct_sequential", "dual_energy"])
+def test_source_sampling_matches_oracle(gpu, oracle, which):
+    ph = parity.small_torso()
+    gw, ow = worlds(gpu, oracle, ph)
+    beam = beams()[which]
+    n_exp = len(oracle.beam_exposures(beam))
+    assert n_exp == len(gpu.beam_exposures(beam)) > 10
+    n = min(6000, n_exp * beam["particles_per_exposure"])
+    g = gw.sample_source(beam, n, gpu.run_options(seed=21, stream=4))
+    o = oracle.sample_source(ow, beam, n, seed=21, stream=4)
+    np.testing.assert_array_equal(g[:, 0], o[:, 0])  # energies: integer alias draw, exact
+    np.testing.assert_allclose(g[:, 1], o[:, 1], rtol=2e-6)
+    np.testing.assert_allclose(g[:, 2:5], o[:, 2:5], atol=2e-5)
+    np.testing.assert_allclose(g[:, 5:8], o[:, 5:8], atol=2e-6)
+    if which != "cbct":
+        assert g[:, 1].std() > 0.1  # bowtie weights vary across the fan
+
+
+def test_dual_energy_tubes_use_their_own_bowtie(gpu, oracle):
+    """Tube B's photons are weighted with tube B's profile: sampled weights differ
+    from those of a beam whose two tubes share tube A's profile exactly on tube B's
+    exposures (odd exposure numbers: A and B alternate, beamactorcontainer.cpp:301-313)."""
+    ph = parity.small_torso()
+    gw, ow = worlds(gpu, oracle, ph)
+    own = P.ct_dual_energy_params(particles=50, bowtie_b=W1_80KV)
+    shared = P.ct_dual_energy_params(particles=50, bowtie_b=P.BODY_BOWTIE)
+    none_b = P.ct_dual_energy_params(particles=50, bowtie_b=None)
+    n = 50 * 40
+    g_own = gw.sample_source(own, n, gpu.run_options(seed=3, stream=1))
+    g_sh = gw.sample_source(shared, n, gpu.run_options(seed=3, stream=1))
+    g_no = gw.sample_source(none_b, n, gpu.run_options(seed=3, stream=1))
+    tube = oracle.beam_exposures(own)
+    tube_of = np.repeat([e["tube"] for e in tube], 50)[:n]
+    a, b = tube_of == 0, tube_of == 1
+    assert a.any() and b.any()
+    np.testing.assert_array_equal(g_own[a, 1], g_sh[a, 1])  # tube A: the same profile
+    assert np.max(np.abs(g_own[b, 1] - g_sh[b, 1])) > 0.05  # tube B: its own
+    np.testing.assert_allclose(g_no[b, 1], 1.0, rtol=1e-6)  # no bowtie on B: the exposure weight, 1
+    # the oracle samples the same weights
+    o_own = oracle.sample_source(ow, own, n, seed=3, stream=1)
+    np.testing.assert_allclose(g_own[:, 1], o_own[:, 1], rtol=2e-6)
+
+
+@pytest.mark.parametrize("which", ["cbct", "ct_sequential", "dual_energy"])
+def test_transport_matches_oracle_independent_streams(gpu, oracle, which):
+    ph = parity.small_torso(scale=2, seed=5)
+    gw, ow = worlds(gpu, oracle, ph)
+    beam = dict(beams()[which])
+    n_exp = len(oracle.beam_exposures(beam))
+    beam["particles_per_exposure"] = int(np.ceil(3_000_000 / n_exp))
+    sg = gw.run(beam, gpu.run_options(seed=8, stream=0))
+    so = ow.run(beam, seed=8, stream=1)
+    n = sg["n_histories"]
+    assert n == so["n_histories"] == n_exp * beam["particles_per_exposure"]
+    assert sg["n_errors"] == 0
+    e1, q1, _ = gw.tally()
+    e2, q2, _ = ow.tally()
+    frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
+                                                 parity.tally_variance(e2, q2, n))
+    print(f"{which}: {n} histories, {nvox} voxels above 5 % of max, {frac:.4f} within 3 sigma, "
+          f"total GPU/oracle - 1 = {e1.sum() / e2.sum() - 1:+.2e}")
+    assert nvox > 2000
+    assert frac >= 0.99, frac
+    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+
+
+def test_dual_energy_second_bowtie_changes_the_dose(gpu, oracle):
+    """Two different bowties give a different dose from a shared one, and the oracle
+    agrees with the GPU for both."""
+    ph = parity.small_torso(scale=2, seed=5)
+    gw, ow = worlds(gpu, oracle, ph)
+    maps = {}
+    for name, bb in (("own", W1_80KV), ("shared", P.BODY_BOWTIE)):
+        beam = P.ct_dual_energy_params(particles=10_000, bowtie_b=bb)
+        gw.clear()
+        ow.clear()
+        sg = gw.run(beam, gpu.run_options(seed=4, stream=0))
+        ow.run(beam, seed=4, stream=1)
+        e1, q1, _ = gw.tally()
+        e2, _, _ = ow.tally()
+        assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3), name
+        maps[name] = (e1, parity.tally_variance(e1, q1, sg["n_histories"]))
+    frac, nvox = parity.combined_sigma_agreement(*maps["own"], *maps["shared"])
+    print(f"own vs shared tube-B bowtie: {frac:.3f} of {nvox} voxels within 3 sigma")
+    assert nvox > 2000 and frac < 0.9, frac
+
+
+def test_pencil_air_kerma_normalisation(gpu):
+    """normalize=1 scales every history weight by F = K / (N E (mu_tr/rho)_air(E)):
+    the same histories, energies times F, counts unchanged."""
+    ph = parity.small_cylinder()
+    gw = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    gw.set_data(ph.density, ph.material)
+    gw.build()
+    beam = {"type": 4, "energy_kev": 60.0, "particles_per_exposure": 100_000, "n_exposures": 4,
+            "position": [0.0, 40.0, 0.0], "cosines": [[0, 0, 1], [-1, 0, 0]], "air_kerma_mgy": 2.5}
+    s0 = gw.run(beam, gpu.run_options(seed=3, normalize=0))
+    e0, _, c0 = gw.tally()
+    gw.clear()
+    s1 = gw.run(beam, gpu.run_options(seed=3, normalize=1))
+    e1, _, c1 = gw.tally()
+    F = gpu.beam_calibration(beam)
+    assert s0["calibration"] == 1.0
+    assert s1["calibration"] == pytest.approx(F, rel=1e-12) and F != 1.0
+    np.testing.assert_array_equal(c0, c1)
+    m = e0 > 0
+    np.testing.assert_allclose(e1[m] / e0[m], F, rtol=2e-6)
+
+
+def test_step_limit_reports_device_error_and_recovers(gpu):
+    """A per-history step limit that histories exceed stops them and the call returns
+    DXMCG_ERR_DEVICE after its launch completed; the next call runs normally."""
+    ph = parity.small_cylinder()
+    gw = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials)
+    gw.set_data(ph.density, ph.material)
+    gw.build()
+    beam = P.dx_beam_params(particles=20_000, exposures=2)
+    rc, st = gw.run_status(beam, gpu.run_options(seed=2, max_steps=2))
+    assert rc == -5, rc
+    assert st["n_errors"] > 0 and st["n_histories"] == 40_000
+    gw.clear()
+    rc, st = gw.run_status(beam, gpu.run_options(seed=2))
+    assert rc == 0 and st["n_errors"] == 0
+    e, _, _ = gw.tally()
+    assert e.sum() + st["e_escaped"] == pytest.approx(st["e_source"], rel=1e-5)

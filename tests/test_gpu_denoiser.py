@@ -93,6 +93,29 @@ def test_tensor_core_convolutions_match_mma_sync(gpu, torch):
     assert rel(tc.grads(), ms.grads()) < 2e-2
 
 
+def test_tensor_core_wait_limit_gives_up_and_recovers(gpu, torch):
+    """The tcgen05 convolution's hand-over waits between its roles are bounded: with
+    a limit of one non-blocking poll they run out, every CTA leaves after its copies
+    and MMAs in flight have landed, and the call reports DXMCG_ERR_DEVICE; with the
+    default limit restored the same network gives the same predictions as before,
+    bit for bit, and trains."""
+    from opendxmc_gb300 import native as N
+
+    net = gpu.Denoiser((16, 32, 64), seed=2, conv_path=1)
+    x, t = make_case(17, B=1, D=24, H=40, W=16)
+    xt = torch.tensor(x, dtype=torch.bfloat16, device="cuda")
+    tt = torch.tensor(t, dtype=torch.float32, device="cuda")
+    ref = net.forward(xt).cpu().numpy()
+    net.set_wait_limit(1)
+    with pytest.raises(N.DxmcgError) as err:
+        net.backward(xt, tt)  # synchronises and reads the convolutions' status
+    assert err.value.code == -5
+    net.set_wait_limit(0)
+    np.testing.assert_array_equal(net.forward(xt).cpu().numpy(), ref)
+    loss = net.backward(xt, tt)
+    assert np.isfinite(loss) and loss > 0
+
+
 def test_tensor_core_persistent_bricks_match_mma_sync(gpu, torch):
     """A volume with more output bricks than SMs at level 0 (1 x 64 x 128 x 64: 512
     bricks of 8 x 16 x 8 for the persistent CTAs, three or four each): the tcgen05

@@ -83,3 +83,22 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu):
     # within limits it runs
     rc, st = _call(N, ph, d_dens, d_mat, d_tally, beam, gpu.run_options())
     assert rc == 0 and st["n_histories"] == 100
+
+
+def test_noalloc_refuses_ct_calibration(gpu):
+    """A CT beam with dose normalisation and a CTDI target needs a CTDI phantom run,
+    which allocates: the allocation-free call refuses it with an argument error."""
+    import torch
+
+    from opendxmc_gb300 import native as N
+
+    ph = P.water_cylinder_phantom(dims=(16, 16, 8), spacing=(0.8, 0.8, 2.0))
+    d_dens = torch.from_numpy(ph.density.astype(np.float32)).to("cuda:0")
+    d_mat = torch.from_numpy(ph.material).to("cuda:0")
+    d_tally = torch.zeros((ph.n_voxels, 4), dtype=torch.float64, device="cuda:0")
+    beam = dict(P.ct_spiral_params(particles=10, scan_cm=2.0), ctdi_vol_mgy=10.0)
+    rc, _ = _call(N, ph, d_dens, d_mat, d_tally, beam, gpu.run_options(normalize=1))
+    assert rc == -1 and b"CTDI" in N.lib().dxmcg_last_error()
+    # without normalisation the same beam runs
+    rc, st = _call(N, ph, d_dens, d_mat, d_tally, beam, gpu.run_options(normalize=0))
+    assert rc == 0 and st["n_histories"] > 0

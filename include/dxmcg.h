@@ -173,6 +173,10 @@ typedef struct {
      * takes more tracking steps is stopped and counted in n_errors, and the call
      * returns DXMCG_ERR_DEVICE after the launch completes */
     uint32_t max_steps;
+    /* WOODCOCK tracking: 0 = default: a tentative collision whose 8x8x8-voxel cell
+     * bound already proves it virtual does not read its voxel (the same decisions,
+     * fewer voxel reads); -1 = read every voxel */
+    int32_t gather_skip;
 } dxmcg_run_options;
 
 typedef struct {
@@ -185,6 +189,8 @@ typedef struct {
     double calibration; /* factor applied to every history weight (1 unless normalize) */
     uint64_t n_crossings; /* MACRO tracking: macro-cell boundary crossings */
     uint64_t n_fluorescence; /* correction level 2: K fluorescence photons emitted */
+    uint64_t n_voxel_reads;  /* voxel words read: n_visits less the tentative collisions
+                                the Woodcock gather skip settled from their cell bound */
 } dxmcg_stats;
 
 typedef struct dxmcg_world dxmcg_world;

@@ -74,6 +74,50 @@ namespace {
         }
     }
 
+    // One block per cell of kCellEdge^3 voxels: the largest rho * ratio[m] of its
+    // voxels times (1 + 2^-12), or +inf when one of them is transparent.  The margin
+    // covers the FP32 roundings of the interpolated tables on both sides of the
+    // Woodcock acceptance test (a few units in 2^-24 each).
+    __global__ void cellBoundKernel(const uint32_t* __restrict__ vox, int nx, int ny, int nz, int ncx, int ncy,
+        const float* __restrict__ ratio, float* __restrict__ bound)
+    {
+        const int c = blockIdx.x;
+        const int cx = c % ncx, cy = (c / ncx) % ncy, cz = c / (ncx * ncy);
+        const int x0 = cx * kCellEdge, y0 = cy * kCellEdge, z0 = cz * kCellEdge;
+        const int ex = min(kCellEdge, nx - x0), ey = min(kCellEdge, ny - y0), ez = min(kCellEdge, nz - z0);
+        const int n = ex * ey * ez;
+        float best = 0.0f;
+        bool transparent = false;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int ix = x0 + i % ex, iy = y0 + (i / ex) % ey, iz = z0 + i / (ex * ey);
+            const uint32_t w = vox[ix + static_cast<size_t>(nx) * (iy + static_cast<size_t>(ny) * iz)];
+            const int m = static_cast<int>(w & 0xffu);
+            if (m == DXMCG_TRANSPARENT_MATERIAL)
+                transparent = true;
+            else
+                best = fmaxf(best, __uint_as_float(w & 0xffffff00u) * ratio[m]);
+        }
+        for (int o = 16; o > 0; o >>= 1)
+            best = fmaxf(best, __shfl_xor_sync(kFull, best, o));
+        transparent = __any_sync(kFull, transparent);
+        __shared__ float warpBest[32];
+        __shared__ int warpTransparent[32];
+        if ((threadIdx.x & 31) == 0) {
+            warpBest[threadIdx.x >> 5] = best;
+            warpTransparent[threadIdx.x >> 5] = transparent ? 1 : 0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float b = 0.0f;
+            int tr = 0;
+            for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w) {
+                b = fmaxf(b, warpBest[w]);
+                tr |= warpTransparent[w];
+            }
+            bound[c] = tr ? __int_as_float(0x7f800000) : b * (1.0f + 2.44140625e-4f);
+        }
+    }
+
     __global__ void finalizeKernel(const Tally* __restrict__ t, const uint32_t* __restrict__ vox, size_t n,
         double toDose, double nh, double* __restrict__ dose, double* __restrict__ var,
         unsigned long long* __restrict__ cnt)
@@ -238,6 +282,13 @@ cudaError_t launchMacroScale(const uint32_t* vox, int nx, int ny, int nz, int mb
 {
     const int mcz = (nz + mb - 1) / mb;
     macroScaleKernel<<<mcx * mcy * mcz, 256, 0, s>>>(vox, nx, ny, nz, mb, mcx, mcy, ratio, scaleBits);
+    return cudaGetLastError();
+}
+
+cudaError_t launchCellBound(const uint32_t* vox, int nx, int ny, int nz, int ncx, int ncy, int ncz, const float* ratio,
+    float* bound, cudaStream_t s)
+{
+    cellBoundKernel<<<ncx * ncy * ncz, 128, 0, s>>>(vox, nx, ny, nz, ncx, ncy, ratio, bound);
     return cudaGetLastError();
 }
 

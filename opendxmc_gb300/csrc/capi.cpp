@@ -132,6 +132,9 @@ struct dxmcg_world {
     DeviceBuffer<float> mratio;
     int macroB = 0;
     int mc[3] {};
+    // Woodcock gather-skip bounds per cell of 8^3 voxels (built with the world)
+    DeviceBuffer<float> cbound;
+    int ncell[3] {};
     std::vector<float> hostTot, hostMaj; // FP32 tables as uploaded
     std::vector<double> rhoMax;
     double historiesScored = 0.0;
@@ -152,13 +155,9 @@ int ensureStream(dxmcg_world* w)
     return DXMCG_OK;
 }
 
-// Macro cells of B^3 voxels: ratio[m] = max over the table energies of
-// total_m(E) / majorant(E) (host), then s_c = max over the cell of rho * ratio[m]
-// (device, one block per cell).
-int ensureMacroCells(dxmcg_world* w, int B)
+// ratio[m] = max over the table energies of total_m(E) / majorant(E), 256 entries
+std::vector<float> majorantRatios(const dxmcg_world* w)
 {
-    if (w->macroB == B && w->mscale.p)
-        return DXMCG_OK;
     const int M = static_cast<int>(w->materials.size());
     std::vector<float> ratio(256, 0.0f);
     for (int m = 0; m < M; ++m) {
@@ -168,6 +167,16 @@ int ensureMacroCells(dxmcg_world* w, int B)
                 r = std::max(r, static_cast<double>(w->hostTot[m * kNE + i]) / w->hostMaj[i]);
         ratio[m] = static_cast<float>(r);
     }
+    return ratio;
+}
+
+// Macro cells of B^3 voxels: ratio[m] (host), then s_c = max over the cell of
+// rho * ratio[m] (device, one block per cell).
+int ensureMacroCells(dxmcg_world* w, int B)
+{
+    if (w->macroB == B && w->mscale.p)
+        return DXMCG_OK;
+    const std::vector<float> ratio = majorantRatios(w);
     for (int a = 0; a < 3; ++a)
         w->mc[a] = (w->dims[a] + B - 1) / B;
     const size_t nc = static_cast<size_t>(w->mc[0]) * w->mc[1] * w->mc[2];
@@ -226,6 +235,11 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
     J.tally = w->tally.p;
     J.exps = jb->exps.p;
     J.spec = jb->spec.p;
+    if (o.tracking == DXMCG_TRACK_WOODCOCK && o.gather_skip >= 0 && w->cbound.p) {
+        J.cbound = w->cbound.p;
+        J.cb[0] = w->ncell[0];
+        J.cb[1] = w->ncell[1];
+    }
     if (o.tracking == DXMCG_TRACK_MACRO) {
         const int B = o.macro_cell > 0 ? std::min(o.macro_cell, 1024) : 16;
         rc = ensureMacroCells(w, B);
@@ -267,6 +281,7 @@ void fillStats(const DevCounters& c, dxmcg_stats* stats)
     stats->n_histories = c.histories;
     stats->n_missed = c.missed;
     stats->n_visits = c.visits;
+    stats->n_voxel_reads = c.visits - c.skipped;
     stats->n_photo = c.photo;
     stats->n_compton = c.compton;
     stats->n_rayleigh = c.rayleigh;
@@ -742,6 +757,20 @@ DXMCG_API int dxmcg_world_build(dxmcg_world* w)
     DXMCG_CUDA(cudaMemcpyAsync(w->maj.p, majf.data(), kNE * sizeof(float), cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(cudaMemcpyAsync(w->mats.p, dm.data(), M * sizeof(DevMaterial), cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(cudaMemsetAsync(w->tally.p, 0, w->N * sizeof(Tally), w->stream));
+    // gather-skip bounds of the Woodcock step
+    {
+        const std::vector<float> ratio = majorantRatios(w);
+        for (int a = 0; a < 3; ++a)
+            w->ncell[a] = (w->dims[a] + kCellEdge - 1) / kCellEdge;
+        const size_t nc = static_cast<size_t>(w->ncell[0]) * w->ncell[1] * w->ncell[2];
+        DXMCG_CUDA(w->mratio.alloc(256));
+        DXMCG_CUDA(w->cbound.alloc(nc));
+        DXMCG_CUDA(cudaMemcpyAsync(w->mratio.p, ratio.data(), 256 * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+        e = launchCellBound(w->vox.p, w->dims[0], w->dims[1], w->dims[2], w->ncell[0], w->ncell[1], w->ncell[2],
+            w->mratio.p, w->cbound.p, w->stream);
+        if (e != cudaSuccess)
+            return cudaFail(e, "cell-bound kernel");
+    }
     DXMCG_CUDA(cudaStreamSynchronize(w->stream));
     w->historiesScored = 0.0;
     w->built = true;
@@ -922,6 +951,7 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
         stats->n_histories = c.histories;
         stats->n_missed = c.missed;
         stats->n_visits = c.visits;
+        stats->n_voxel_reads = c.visits - c.skipped;
         stats->n_photo = c.photo;
         stats->n_compton = c.compton;
         stats->n_rayleigh = c.rayleigh;

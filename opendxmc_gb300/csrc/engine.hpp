@@ -116,7 +116,15 @@ struct DevJob {
     uint32_t key0, key1, stream;
     int tracking;
     uint32_t maxSteps; // per-history step limit (kErrStepLimit beyond it)
+    // Woodcock gather skip: per cell of kCellEdge^3 voxels an upper bound b_c of
+    // rho mu_m(E) / mu_max(E) over the cell's voxels and all energies (+inf where the
+    // cell holds a transparent voxel); nullptr: off.  cb[0], cb[1]: cells along x, y.
+    const float* cbound;
+    int cb[2];
 };
+
+constexpr int kCellShift = 3; // gather-skip cells of 8 x 8 x 8 voxels
+constexpr int kCellEdge = 1 << kCellShift;
 
 struct DevCounters {
     unsigned long long next; // work-queue head (history index)
@@ -124,6 +132,7 @@ struct DevCounters {
         fluorescence;
     double e_source, e_escaped, e_deposited;
     unsigned int error_flags;
+    unsigned long long skipped; // Woodcock tentative collisions settled by the cell bound alone
 };
 
 enum ErrorFlag : unsigned {
@@ -149,6 +158,10 @@ cudaError_t launchTransport(const DevJob& job, unsigned long long h_end, DevCoun
 // per-macro-cell majorant scale: max over the cell's voxels of rho * ratio[m]
 cudaError_t launchMacroScale(const uint32_t* vox, int nx, int ny, int nz, int mb, int mcx, int mcy,
     const float* ratio, unsigned* scaleBits, cudaStream_t s);
+// gather-skip bounds: per cell of kCellEdge^3 voxels (cells x fastest, ncx x ncy x ncz)
+// max over its voxels of rho * ratio[m] times (1 + 2^-12), +inf if one is transparent
+cudaError_t launchCellBound(const uint32_t* vox, int nx, int ny, int nz, int ncx, int ncy, int ncz, const float* ratio,
+    float* bound, cudaStream_t s);
 cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, double energy_to_dose,
     double n_histories, double* dose, double* var, unsigned long long* count, cudaStream_t s);
 cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int ny, int nz, float sx, float sy,

@@ -108,9 +108,18 @@ namespace {
     }
 
     // Woodcock step; returns true on a real collision in voxel v / material m.
+    //
+    // Gather skip (J.cbound set): the tentative collision is real when u mu_max(E) <
+    // rho mu_m(E).  The cell's bound b_c satisfies rho mu_m(E) <= b_c mu_max(E) for each
+    // of its voxels, with a margin larger than the FP32 roundings of both sides, so
+    // u mu_max >= b_c mu_max settles the step as virtual without reading the voxel.
+    // Otherwise the voxel is read and the usual test decides, on the same uniform: the
+    // decisions, and so the histories, are those of the plain step.  Cells holding a
+    // transparent voxel (b_c = +inf) take the plain step, which draws the uniform only
+    // for a voxel that is not transparent.
     template <bool PACKED>
     __device__ __forceinline__ bool woodcockStep(const DevJob& J, Photon& ph, Rng& rng, const EnergyCache& ec,
-        bool& escaped, uint32_t& v, int& m, unsigned& visits)
+        bool& escaped, uint32_t& v, int& m, unsigned& visits, unsigned& skipped)
     {
         // hardware log2: |error| <= 2^-21.4 near u = 1, where the step is < 1e-6 mean free paths
         const float s = fmaxf(-__logf(rng.u()), 0.0f) * ec.invMmax;
@@ -130,6 +139,19 @@ namespace {
         }
         ++visits;
         v = static_cast<uint32_t>(ix + J.nx * (iy + J.ny * iz));
+        if (J.cbound) {
+            const float b = __ldg(J.cbound
+                + ((ix >> kCellShift) + J.cb[0] * ((iy >> kCellShift) + J.cb[1] * (iz >> kCellShift))));
+            if (b <= FLT_MAX) {
+                const float t = rng.u() * ec.mmax;
+                if (t >= b * ec.mmax) {
+                    ++skipped;
+                    return false;
+                }
+                const float rho = voxelAt<PACKED>(J, v, m);
+                return t < rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
+            }
+        }
         const float rho = voxelAt<PACKED>(J, v, m);
         if (m == DXMCG_TRANSPARENT_MATERIAL)
             return false;
@@ -294,7 +316,7 @@ namespace {
         EnergyCache ec { 0, 0.0f, 1.0f, 1.0f };
         uint32_t pv = 0; // voxel of the parked interaction
         int pm = 0;      // its material
-        unsigned steps = 0, visits = 0, crossings = 0, err = 0;
+        unsigned steps = 0, visits = 0, crossings = 0, err = 0, skipped = 0;
         int cx = 0, cy = 0, cz = 0; // macro cell of the photon (MACRO tracking)
         bool fresh = false;
         KahanSum esrc, eesc, edep; // FP32 compensated sums: no FP64 on the per-event path
@@ -460,7 +482,7 @@ namespace {
                     // several steps per phase: most are virtual, and each phase boundary
                     // costs the warp its votes; a lane stops at a real collision or escape
                     for (int k = 0;;) {
-                        real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
+                        real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits, skipped);
                         if (real || escaped || ++k >= woodcockSteps)
                             break;
                         ++steps;
@@ -521,6 +543,7 @@ namespace {
         // ---- flush: per-lane sums by warp, block counters by one thread
         const unsigned long long vi = warpSum(static_cast<unsigned long long>(visits));
         const unsigned long long cr = warpSum(static_cast<unsigned long long>(crossings));
+        const unsigned long long sk = warpSum(static_cast<unsigned long long>(skipped));
         const double es = warpSum(esrc.value());
         const double ee = warpSum(eesc.value());
         const double ed = warpSum(edep.value());
@@ -533,6 +556,8 @@ namespace {
             atomicAdd(&ctr->visits, vi);
             if (cr)
                 atomicAdd(&ctr->crossings, cr);
+            if (sk)
+                atomicAdd(&ctr->skipped, sk);
             atomicAdd(&ctr->e_source, es);
             atomicAdd(&ctr->e_escaped, ee);
             atomicAdd(&ctr->e_deposited, ed);

@@ -156,7 +156,7 @@ class RunOptions(C.Structure):
                 ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk_histories_log2", C.c_int32),
                 ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64), ("interact_batch", C.c_int32),
                 ("refill_batch", C.c_int32), ("macro_cell", C.c_int32),
-                ("woodcock_steps", C.c_int32), ("max_steps", C.c_uint32)]
+                ("woodcock_steps", C.c_int32), ("max_steps", C.c_uint32), ("gather_skip", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -165,7 +165,7 @@ class Stats(C.Structure):
                                   "n_cutoff", "n_errors", "n_interacted")] + [
         ("kernel_ms", C.c_double), ("total_ms", C.c_double), ("dose_scale", C.c_double),
         ("calibration", C.c_double), ("n_crossings", C.c_uint64),
-        ("n_fluorescence", C.c_uint64)]
+        ("n_fluorescence", C.c_uint64), ("n_voxel_reads", C.c_uint64)]
 
     def as_dict(self) -> dict:
         return {f[0]: getattr(self, f[0]) for f in self._fields_}

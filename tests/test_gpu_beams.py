@@ -109,23 +109,27 @@ def test_transport_matches_oracle_independent_streams(gpu, oracle, which):
 
 def test_dual_energy_second_bowtie_changes_the_dose(gpu, oracle):
     """Two different bowties give a different dose from a shared one, and the oracle
-    agrees with the GPU for both."""
+    agrees with the GPU for both: on this torso tube B's own profile (W1 80 kV, flatter
+    than the body bowtie) lowers the energy imparted by about 2 %, some 30 standard
+    errors of the 4.3e6-history totals."""
     ph = parity.small_torso(scale=2, seed=5)
     gw, ow = worlds(gpu, oracle, ph)
-    maps = {}
+    tot = {}
     for name, bb in (("own", W1_80KV), ("shared", P.BODY_BOWTIE)):
         beam = P.ct_dual_energy_params(particles=10_000, bowtie_b=bb)
         gw.clear()
         ow.clear()
-        sg = gw.run(beam, gpu.run_options(seed=4, stream=0))
+        gw.run(beam, gpu.run_options(seed=4, stream=0))
         ow.run(beam, seed=4, stream=1)
-        e1, q1, _ = gw.tally()
+        e1, _, _ = gw.tally()
         e2, _, _ = ow.tally()
         assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3), name
-        maps[name] = (e1, parity.tally_variance(e1, q1, sg["n_histories"]))
-    frac, nvox = parity.combined_sigma_agreement(*maps["own"], *maps["shared"])
-    print(f"own vs shared tube-B bowtie: {frac:.3f} of {nvox} voxels within 3 sigma")
-    assert nvox > 2000 and frac < 0.9, frac
+        tot[name] = (e1.sum(), e2.sum())
+    r_gpu = tot["own"][0] / tot["shared"][0]
+    r_or = tot["own"][1] / tot["shared"][1]
+    print(f"energy imparted, own / shared tube-B bowtie: GPU {r_gpu:.4f}, oracle {r_or:.4f}")
+    assert abs(r_gpu - 1.0) > 0.01
+    assert r_gpu == pytest.approx(r_or, abs=4e-3)
 
 
 def test_pencil_air_kerma_normalisation(gpu):

@@ -136,6 +136,31 @@ def test_woodcock_steps_per_phase_keep_every_history(c1, gpu, steps):
     np.testing.assert_allclose(q2, q1, rtol=1e-12, atol=0)
 
 
+def test_gather_skip_keeps_every_history(gpu):
+    """The Woodcock gather skip settles tentative collisions from the 8^3-voxel cell
+    bound without reading the voxel, on the uniform the full test would use: every
+    history makes the same decisions, so counts are equal and the per-voxel sums
+    equal up to the order of the FP64 atomics, with far fewer voxel reads.  A cell
+    holding a transparent voxel takes the full test."""
+    ph = P.torso_phantom(dims=(96, 80, 64), spacing=(0.4, 0.4, 0.4), seed=6)
+    ph.material[20:30, 30:40, 40:48] = 255  # transparent voxels in a few cells
+    gw = gpu_world(gpu, ph)
+    beam = P.ct_spiral_params(particles=3000, scan_cm=20.0)
+    s_off = gw.run(beam, gpu.run_options(seed=9, stream=1, gather_skip=-1))
+    e1, q1, n1 = gw.tally()
+    gw.clear()
+    s_on = gw.run(beam, gpu.run_options(seed=9, stream=1))
+    e2, q2, n2 = gw.tally()
+    for k in ("n_histories", "n_visits", "n_photo", "n_compton", "n_rayleigh", "n_cutoff", "n_interacted"):
+        assert s_off[k] == s_on[k], k
+    np.testing.assert_array_equal(n1, n2)
+    np.testing.assert_allclose(e2, e1, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(q2, q1, rtol=1e-12, atol=0)
+    assert s_off["n_voxel_reads"] == s_off["n_visits"]
+    print(f"gather skip: {s_on['n_voxel_reads'] / s_on['n_visits']:.3f} of the tentative collisions read their voxel")
+    assert s_on["n_voxel_reads"] < 0.7 * s_on["n_visits"]
+
+
 def test_energy_conservation(c1, gpu):
     ph, gw, ow = c1
     gw.clear()

@@ -62,8 +62,8 @@ def parse():
     p.add_argument("--macro-cell", type=int, default=16, help="macro-cell edge in voxels (macro tracking)")
     p.add_argument("--woodcock-steps", type=int, default=0,
                    help="Woodcock steps a lane takes between regroupings (0: library default)")
-    p.add_argument("--no-gather-skip", action="store_true",
-                   help="Woodcock: read every tentative collision's voxel (no cell-bound skip)")
+    p.add_argument("--gather-skip", type=int, choices=[-1, 0, 1], default=0,
+                   help="Woodcock gather skip: 1 on, -1 off, 0 library default (on above 64 MiB of voxels)")
     p.add_argument("--interact-batch", type=int, default=0)
     p.add_argument("--refill-batch", type=int, default=0)
     p.add_argument("--correction", type=int, choices=[0, 1, 2], default=1,
@@ -199,12 +199,10 @@ class ClockSampler:
                 "power_w_max": max((num(r[3]) or 0.0) for r in rows)}
 
 
-def algorithmic_bytes(args, visits, reads, crossings, deposits) -> float:
+def algorithmic_bytes(reads, cell_reads, crossings, deposits) -> float:
     """Bytes the transport must move: 4 B per voxel word read, 4 B per gather-skip
-    cell bound read (one per Woodcock tentative collision when the skip is on), 4 B per
-    macro-cell crossing (cell scale), 48 B per deposit (read-modify-write of the
-    24-byte tally record)."""
-    cell_reads = visits if (args.tracking == "woodcock" and not args.no_gather_skip) else 0
+    cell bound read, 4 B per macro-cell crossing (cell scale), 48 B per deposit
+    (read-modify-write of the 24-byte tally record)."""
     return 4.0 * reads + 4.0 * cell_reads + 4.0 * crossings + 48.0 * deposits
 
 
@@ -315,7 +313,7 @@ def run_ours(args):
     def run_opts(seed):
         return G.run_options(seed=seed, stream=rank, tracking=TRACKING[args.tracking], macro_cell=args.macro_cell,
                              woodcock_steps=args.woodcock_steps, interact_batch=args.interact_batch,
-                             refill_batch=args.refill_batch, gather_skip=-1 if args.no_gather_skip else 0)
+                             refill_batch=args.refill_batch, gather_skip=args.gather_skip)
 
     def step(seed):
         flush.fill_(float(seed))
@@ -347,7 +345,8 @@ def run_ours(args):
     deposits = sum(s["n_photo"] + s["n_compton"] + s["n_cutoff"] for s in stats)
     chunk = 1 << 26
     launches_per_step = -(-hist // chunk)
-    alg_bytes = algorithmic_bytes(args, visits, reads, crossings, deposits)
+    cells = sum(s["n_cell_reads"] for s in stats)
+    alg_bytes = algorithmic_bytes(reads, cells, crossings, deposits)
     hbm, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -356,6 +355,7 @@ def run_ours(args):
             "alg_bytes_per_launch": alg_bytes / (args.steps * launches_per_step),
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step),
             "visits_per_history": visits / done, "voxel_reads_per_history": reads / done,
+            "cell_reads_per_history": cells / done,
             "crossings_per_history": crossings / done, "deposits_per_history": deposits / done}
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -492,7 +492,8 @@ def run_batch(args):
     reads = sum(s["n_voxel_reads"] for s in stats)
     crossings = sum(s["n_crossings"] for s in stats)
     deposits = sum(s["n_photo"] + s["n_compton"] + s["n_cutoff"] for s in stats)
-    alg_bytes = algorithmic_bytes(args, visits, reads, crossings, deposits)
+    cells = sum(s["n_cell_reads"] for s in stats)
+    alg_bytes = algorithmic_bytes(reads, cells, crossings, deposits)
     hbm, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
 

@@ -173,9 +173,11 @@ typedef struct {
      * takes more tracking steps is stopped and counted in n_errors, and the call
      * returns DXMCG_ERR_DEVICE after the launch completes */
     uint32_t max_steps;
-    /* WOODCOCK tracking: 0 = default: a tentative collision whose 8x8x8-voxel cell
+    /* WOODCOCK tracking, gather skip: a tentative collision whose 8x8x8-voxel cell
      * bound already proves it virtual does not read its voxel (the same decisions,
-     * fewer voxel reads); -1 = read every voxel */
+     * fewer voxel reads).  1 = on, -1 = off, 0 = default: on when the voxel words
+     * (4 bytes per voxel; for a batch, of all its worlds, decided from opts[0])
+     * exceed 64 MiB, where they no longer stay in L2 */
     int32_t gather_skip;
 } dxmcg_run_options;
 
@@ -191,6 +193,7 @@ typedef struct {
     uint64_t n_fluorescence; /* correction level 2: K fluorescence photons emitted */
     uint64_t n_voxel_reads;  /* voxel words read: n_visits less the tentative collisions
                                 the Woodcock gather skip settled from their cell bound */
+    uint64_t n_cell_reads;   /* gather-skip cell bounds read (n_visits when the skip ran) */
 } dxmcg_stats;
 
 typedef struct dxmcg_world dxmcg_world;

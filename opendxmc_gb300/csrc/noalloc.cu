@@ -286,6 +286,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
         stats->n_missed = c.missed;
         stats->n_visits = c.visits;
         stats->n_voxel_reads = c.visits - c.skipped;
+        stats->n_cell_reads = 0; // no cell bounds without a world
         stats->n_photo = c.photo;
         stats->n_compton = c.compton;
         stats->n_rayleigh = c.rayleigh;

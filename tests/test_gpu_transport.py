@@ -149,14 +149,18 @@ def test_gather_skip_keeps_every_history(gpu):
     s_off = gw.run(beam, gpu.run_options(seed=9, stream=1, gather_skip=-1))
     e1, q1, n1 = gw.tally()
     gw.clear()
-    s_on = gw.run(beam, gpu.run_options(seed=9, stream=1))
+    s_on = gw.run(beam, gpu.run_options(seed=9, stream=1, gather_skip=1))
     e2, q2, n2 = gw.tally()
     for k in ("n_histories", "n_visits", "n_photo", "n_compton", "n_rayleigh", "n_cutoff", "n_interacted"):
         assert s_off[k] == s_on[k], k
     np.testing.assert_array_equal(n1, n2)
     np.testing.assert_allclose(e2, e1, rtol=1e-12, atol=0)
     np.testing.assert_allclose(q2, q1, rtol=1e-12, atol=0)
-    assert s_off["n_voxel_reads"] == s_off["n_visits"]
+    assert s_off["n_voxel_reads"] == s_off["n_visits"] and s_off["n_cell_reads"] == 0
+    assert s_on["n_cell_reads"] == s_on["n_visits"]
+    # the default turns the skip on only for grids whose voxel words exceed 64 MiB
+    gw.clear()
+    assert gw.run(beam, gpu.run_options(seed=9, stream=1, hist_end=1000))["n_cell_reads"] == 0
     print(f"gather skip: {s_on['n_voxel_reads'] / s_on['n_visits']:.3f} of the tentative collisions read their voxel")
     assert s_on["n_voxel_reads"] < 0.7 * s_on["n_visits"]
 

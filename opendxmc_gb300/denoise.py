@@ -170,6 +170,153 @@ def relative_errors(estimate, reference, reference2=None, threshold=0.1, mask=No
     return out
 
 
+class Scorer:
+    """Errors of a dose map against two independent reference runs r1 and r2 (same
+    units), over the voxels that are not air and whose averaged reference dose exceeds
+    `threshold` x its maximum:
+
+      rms_rel         RMS relative error with the references' own noise removed:
+                      E[(e - r1)(e - r2)] = E[(e - truth)^2] for r1, r2 independent of e
+                      and of each other;
+      mean_rel        mean |e - rbar| / rbar against the references' average rbar;
+      mean_rel_floor  that statistic for an exact map, mean |r1 - r2| / (2 rbar): rbar's
+                      own noise, below which mean_rel cannot go whatever the estimate."""
+
+    def __init__(self, r1, r2, nonair, threshold=0.1):
+        rbar = 0.5 * (r1 + r2)
+        cand = np.where(nonair, rbar, 0.0)
+        self.sel = np.flatnonzero(cand > threshold * cand.max())
+        self.r1 = r1[self.sel]
+        self.r2 = r2[self.sel]
+        self.rbar = rbar[self.sel]
+        self.floor = float(np.mean(np.abs(self.r1 - self.r2) / (2.0 * self.rbar)))
+        self.reference_rms = float(np.sqrt(np.mean((self.r1 - self.r2) ** 2 / self.rbar ** 2) / 2))
+
+    def __call__(self, estimate) -> dict:
+        e = estimate[self.sel]
+        cross = (e - self.r1) * (e - self.r2) / self.rbar ** 2
+        return {"rms_rel": float(np.sqrt(max(np.mean(cross), 0.0))),
+                "mean_rel": float(np.mean(np.abs(e - self.rbar) / self.rbar)),
+                "mean_rel_floor": self.floor, "voxels": int(self.sel.size)}
+
+
+def plain_to_target(world, beam_of, high, scorer, target, air, seed, chunk, start, limit, stream0=100, log=print):
+    """Plain Monte Carlo, measured: runs of `chunk` histories on independent streams
+    add up in the world's tally until the error of the accumulated map (scaled to the
+    `high`-history references) crosses `target`; the map is scored after every run
+    once `start` histories are in (reading it back is not timed).  Returns the checks,
+    the first passing one, and the crossing N* = N (rms / target)^2 of that check
+    (rms^2 falls as 1/N for plain Monte Carlo), with its time at the measured rate."""
+    world.clear()
+    n, mc_s, k = 0, 0.0, 0
+    checks = []
+    while n < limit:
+        st = world.run(beam_of(chunk), G.run_options(seed=seed, stream=stream0 + k))
+        k += 1
+        n += st["n_histories"]
+        mc_s += st["total_ms"] * 1e-3
+        if n < start:
+            continue
+        d = world.dose()[0]
+        d[air] = 0.0
+        e = scorer(d * (high / n))
+        checks.append({"histories": n, "mc_s": mc_s, **e})
+        log(f"plain MC {n:.3g} histories, {mc_s:.2f} s: RMS {e['rms_rel']:.4f}, mean {e['mean_rel']:.4f}")
+        if e["rms_rel"] <= target:
+            break
+    last = checks[-1] if checks else None
+    passed = last is not None and last["rms_rel"] <= target
+    out = {"checks": checks, "passed": passed, "histories_per_s": n / mc_s if mc_s > 0 else None}
+    if passed:
+        n_star = last["histories"] * (last["rms_rel"] / target) ** 2
+        out.update({"histories": last["histories"], "s": last["mc_s"], "rms_rel": last["rms_rel"],
+                    "mean_rel": last["mean_rel"], "crossing_histories": n_star,
+                    "crossing_s": n_star / out["histories_per_s"]})
+    return out
+
+
+def denoised_to_target(torch, world, net, beam_of, high, scorer, target, lows, air, seed, stream0=20,
+                       log=print):
+    """A short run plus the denoiser, judged by the references: inputs of each history
+    count in `lows` in turn, each attempt's time (transport + inference, the denoised
+    map left in device memory) added to the total, until one denoised map meets
+    `target`.  When none does, the caller falls back on plain Monte Carlo."""
+    total = 0.0
+    attempts = []
+    for k, low in enumerate(lows):
+        world.clear()
+        st = world.run(beam_of(low), G.run_options(seed=seed, stream=stream0 + k))
+        t_mc = st["total_ms"] * 1e-3
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        net.denoise_world(world, readback=False)
+        torch.cuda.synchronize()
+        t_inf = time.perf_counter() - t1
+        d_dn, _ = net.denoise_world(world)  # the same map again, read back for scoring
+        d_dn[air] = 0.0
+        e = scorer(d_dn * (high / low))
+        d_in = world.dose()[0]
+        d_in[air] = 0.0
+        e_in = scorer(d_in * (high / low))
+        total += t_mc + t_inf
+        ok = e["rms_rel"] <= target
+        attempts.append({"histories": low, "mc_s": t_mc, "inference_s": t_inf, "rms_rel": e["rms_rel"],
+                         "mean_rel": e["mean_rel"], "input_rms_rel": e_in["rms_rel"], "accepted": ok})
+        log(f"{low:.3g} histories + denoiser: RMS {e['rms_rel']:.4f} (input {e_in['rms_rel']:.4f}), "
+            f"{'accepted' if ok else 'rejected'}")
+        if ok:
+            return {"accepted": True, "histories": low, "s": total, "rms_rel": e["rms_rel"],
+                    "mean_rel": e["mean_rel"], "attempts": attempts}
+    return {"accepted": False, "s": total, "attempts": attempts}
+
+
+def time_to_target(torch, net, dims, spacing, phantom_seed, beam_of, high=1e10, target=0.02,
+                   lows=(3e7, 1e8, 3e8, 1e9), plain_chunk=1e10, log=print):
+    """Seconds to `target` RMS relative dose error on one torso: plain Monte Carlo
+    (measured, plain_to_target) against a short run plus the denoiser with plain Monte
+    Carlo as the fallback (denoised_to_target), both judged against two independent
+    `high`-history runs over non-air voxels above 10 % of the maximum dose."""
+    from . import phantoms as P
+
+    t0 = time.perf_counter()
+    ph = P.torso_phantom(dims=dims, spacing=spacing, seed=phantom_seed)
+    world = G.GpuWorld(dims, spacing, [c for _, c, _ in P.SIX_MATERIALS])
+    world.set_data(ph.density, ph.material)
+    world.build()
+    del ph
+    _, mat = world.packed_density()
+    air = mat == 0
+    refs = []
+    for stream in (2, 3):
+        world.clear()
+        world.run(beam_of(high), G.run_options(seed=phantom_seed, stream=stream))
+        d = world.dose()[0]
+        d[air] = 0.0
+        refs.append(d)
+    scorer = Scorer(refs[0], refs[1], ~air)
+    del refs
+    t_setup = time.perf_counter() - t0
+    log(f"references: 2 x {high:.3g} histories, RMS noise {scorer.reference_rms:.4f}, "
+        f"mean-error floor {scorer.floor:.4f}, {scorer.sel.size} voxels scored")
+    world.clear()
+    world.run(beam_of(lows[0]), G.run_options(seed=phantom_seed, stream=9))
+    net.denoise_world(world, readback=False)  # sizes the network's buffers for this grid
+    dn = denoised_to_target(torch, world, net, beam_of, high, scorer, target, lows, air, phantom_seed, log=log)
+    n_pred = high * (scorer.reference_rms / target) ** 2
+    plain = plain_to_target(world, beam_of, high, scorer, target, air, phantom_seed, chunk=plain_chunk,
+                            start=0.6 * n_pred, limit=3.0 * n_pred, log=log)
+    if not dn["accepted"] and plain["passed"]:
+        dn["fallback_plain_s"] = plain["s"]
+        dn["s"] += plain["s"]
+    world.close()
+    out = {"reference_histories": high, "reference_rms_rel": scorer.reference_rms,
+           "mean_rel_floor": scorer.floor, "voxels_scored": int(scorer.sel.size), "target_rms_rel": target,
+           "plain": plain, "denoised": dn, "setup_s": t_setup}
+    if plain["passed"]:
+        out["speedup_vs_plain_crossing"] = plain["crossing_s"] / dn["s"]
+    return out
+
+
 # ---------------------------------------------------------------- the spiral-CT experiment
 def spiral_beam(histories: float, pitch=0.8, collimation_cm=8.0, scan_cm=20.0, kvp=120.0, al_mm=6.0) -> dict:
     from . import phantoms as P
@@ -285,3 +432,88 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
         "speedup": t_plain / best["total_s"] if best else None,
     }
     return out, net
+
+
+# ---------------------------------------------------------------- training on many small phantoms
+def c4_experiment(torch, n_phantoms=200, dims=(128, 128, 128), spacing=(0.2, 0.2, 0.2), low=1e6, high=1e9,
+                  eval_phantoms=10, steps=16000, batch=8, patch=64, lr=1e-3, lr_final=5e-5,
+                  channels=(16, 32, 64, 128), seed0=5000, log=print):
+    """The denoiser trained on data the Monte Carlo generates from many small
+    phantoms: `n_phantoms` seeded six-material ellipsoid phantoms of `dims` voxels,
+    each run for `low` histories (input) and `high` histories (target) with independent
+    streams, spiral CT 120 kVp / 6 mm Al with the body bowtie, pitch 1.0, 40 mm
+    collimation over the phantom's length.  Then, on `eval_phantoms` held-out phantoms
+    of the same generator, the RMS relative error of the input and of its denoised map
+    against two independent `high`-history runs (non-air voxels above 10 % of max)."""
+    from . import phantoms as P
+
+    nx, ny, nz = dims
+    length = nz * spacing[2]
+
+    def beam_of(n):
+        return spiral_beam(n, pitch=1.0, collimation_cm=4.0, scan_cm=length)
+
+    mats = [c for _, c, _ in P.SIX_MATERIALS]
+    world = G.GpuWorld(dims, spacing, mats)
+    pairs, centers = [], []
+    t0 = time.perf_counter()
+    mc_s, hist = 0.0, 0
+    for i in range(n_phantoms):
+        ph = P.ellipsoid_phantom(dims, spacing, seed=seed0 + i)
+        world.set_data(ph.density, ph.material)
+        world.build()
+        rho, mat = world.packed_density()
+        air = mat == 0
+        d_high, st = run_dose(world, beam_of(high), seed0 + i, 1, air)
+        mc_s += st["total_ms"] * 1e-3
+        hist += st["n_histories"]
+        d_low, st = run_dose(world, beam_of(low), seed0 + i, 10, air)
+        mc_s += st["total_ms"] * 1e-3
+        hist += st["n_histories"]
+        pairs.append(make_pair(torch, world, (nz, ny, nx), d_low, d_high, rho, mat, low / high))
+        body = np.flatnonzero(rho > 0.2)
+        pick = np.random.default_rng(i).choice(body, size=min(20_000, body.size), replace=False)
+        centers.append(np.stack(np.unravel_index(pick, (nz, ny, nx)), axis=1))
+        if (i + 1) % 20 == 0:
+            log(f"phantom {i + 1}/{n_phantoms}: {hist:.3g} histories in {mc_s:.1f} s of transport")
+    t_data = time.perf_counter() - t0
+
+    net = G.Denoiser(channels, seed=0)
+    sampler = PatchSampler(torch, pairs, patch, batch, seed=1, centers=centers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = train(net, sampler, steps, lr=lr, lr_final=lr_final, log_every=max(1, steps // 10), log=log)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del sampler, pairs
+
+    evals = []
+    for i in range(eval_phantoms):
+        s = seed0 + n_phantoms + 1000 + i
+        ph = P.ellipsoid_phantom(dims, spacing, seed=s)
+        world.set_data(ph.density, ph.material)
+        world.build()
+        _, mat = world.packed_density()
+        air = mat == 0
+        r1, _ = run_dose(world, beam_of(high), s, 2, air)
+        r2, _ = run_dose(world, beam_of(high), s, 3, air)
+        scorer = Scorer(r1, r2, ~air)
+        d_low, st = run_dose(world, beam_of(low), s, 20, air)
+        d_dn, _ = net.denoise_world(world)
+        d_dn[air] = 0.0
+        e_in = scorer(d_low * (high / low))
+        e_dn = scorer(d_dn * (high / low))
+        evals.append({"seed": s, "input_rms_rel": e_in["rms_rel"], "denoised_rms_rel": e_dn["rms_rel"],
+                      "input_mean_rel": e_in["mean_rel"], "denoised_mean_rel": e_dn["mean_rel"],
+                      "mean_rel_floor": e_dn["mean_rel_floor"], "reference_rms_rel": scorer.reference_rms})
+        log(f"held-out phantom {s}: input RMS {e_in['rms_rel']:.3f}, denoised RMS {e_dn['rms_rel']:.4f}")
+    world.close()
+    return {
+        "phantoms": n_phantoms, "dims": list(dims), "spacing_cm": list(spacing), "low": low, "high": high,
+        "train_steps": steps, "batch": batch, "patch": patch, "lr": lr, "lr_final": lr_final,
+        "final_loss": float(np.mean(losses[-10:])), "first_loss": float(np.mean(losses[:5])),
+        "data_s": t_data, "data_mc_s": mc_s, "data_histories": hist, "train_s": t_train,
+        "held_out": evals,
+        "mean_input_rms_rel": float(np.mean([e["input_rms_rel"] for e in evals])),
+        "mean_denoised_rms_rel": float(np.mean([e["denoised_rms_rel"] for e in evals])),
+    }, net

@@ -1,6 +1,6 @@
 // dxmc/beams/beamtype.hpp -- what every beam of the dxmc:: layer shares: the
 // exposure type (exposure(i).position()/directionCosines()/collimationHalfAngles(),
-// beamactorcontainer.cpp:114-121, :287-288) and the conversion of a beam's settings
+// beamactorcontainer.cpp:114-121, :134-146) and the conversion of a beam's settings
 // into the engine's dxmcg_beam descriptor.
 #pragma once
 

@@ -1,7 +1,7 @@
 // dxmc/beams/ctspiraldualenergybeam.hpp -- dual-source helical CT: tube A and tube B
 // 90 degrees apart, each with its own voltage, filtration, bowtie and field of view,
 // output shared by relative mAs (beamsettingsmodel.cpp:1386-1612; exposures
-// alternate A, B as drawn at beamactorcontainer.cpp:301-313).
+// alternate A, B as drawn at beamactorcontainer.cpp:134-146).
 #pragma once
 
 #include "ctspiralbeam.hpp"

@@ -1,6 +1,6 @@
 // dxmc/beams/dxbeam.hpp -- planar (DX) beam: one source pose repeated over
 // numberOfExposures() exposures.  Constructor and setters as OpenDXMC's DXBeam wrapper
-// uses them (dxmc_specialization.cpp:98-167) and as the beam settings edit them
+// uses them (dxmc_specialization.cpp:21-90) and as the beam settings edit them
 // (beamsettingsmodel.cpp:459-620).
 #pragma once
 

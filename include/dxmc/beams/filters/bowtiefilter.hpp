@@ -1,6 +1,6 @@
 // dxmc/beams/filters/bowtiefilter.hpp -- relative tube output versus fan angle,
 // BowtieFilter(vector<pair<angle_rad, weight>>) as built from the bowtie JSON
-// (bowtiefilterreader.cpp:173-191).  Points may come in any order.
+// (bowtiefilterreader.cpp:64-92).  Points may come in any order.
 #pragma once
 
 #include <algorithm>

@@ -1,4 +1,4 @@
-// dxmc/floating.hpp -- angle constants used by OpenDXMC (dxmc_specialization.cpp:141-151).
+// dxmc/floating.hpp -- angle constants used by OpenDXMC (dxmc_specialization.cpp:62-76).
 // Part of the header-only dxmc:: layer over the GB300 engine's C ABI (dxmcg.h).
 #pragma once
 

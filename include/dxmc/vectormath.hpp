@@ -1,5 +1,5 @@
 // dxmc/vectormath.hpp -- the 3-vector helpers OpenDXMC calls
-// (dxmc_specialization.cpp:158-165, beamactorcontainer.cpp:219-233).
+// (dxmc_specialization.cpp:80-88, beamactorcontainer.cpp:44-67).
 #pragma once
 
 #include <array>

@@ -110,7 +110,7 @@ typedef struct {
     double filter_mm_b[8];
     double tube_a_weight;
     double fov_b_cm;
-    /* bowtie (BowtieFilter(vector<pair<angle_rad, weight>>), bowtiefilterreader.cpp:173-191) */
+    /* bowtie (BowtieFilter(vector<pair<angle_rad, weight>>), bowtiefilterreader.cpp:64-92) */
     int32_t n_bowtie;
     const double* bowtie_angle;
     const double* bowtie_weight;
@@ -179,6 +179,10 @@ typedef struct {
      * (4 bytes per voxel; for a batch, of all its worlds, decided from opts[0])
      * exceed 64 MiB, where they no longer stay in L2 */
     int32_t gather_skip;
+    /* WOODCOCK tracking: a warp's step phase ends once fewer than this many of its
+     * lanes are still stepping (the rest keep their photons for the next phase);
+     * 0 = default */
+    int32_t step_min_lanes;
 } dxmcg_run_options;
 
 typedef struct {
@@ -216,6 +220,21 @@ DXMCG_API int dxmcg_tube_mean_energy(double kvp, int n_filters, const int32_t* f
     double* mean_kev);
 DXMCG_API int dxmcg_tube_al_hvl(double kvp, int n_filters, const int32_t* filter_Z, const double* filter_mm,
     double* hvl_mm);
+/* ---- physics tables --------------------------------------------------------
+ * The interaction data behind Material<5>::byWeight (simulationpipeline.cpp:136)
+ * and the Tube (ctsegmentationpipeline.cpp:66-71).  The engine's own model is
+ * parametric; a table file (text, "dxmcg-physics 1": an energy grid, then per
+ * element its atomic mass, photoelectric, incoherent and coherent cross sections
+ * in barn/atom on that grid, form-factor scale, K/L edges, K-alpha energy and
+ * yield, and Compton shells; optionally unfiltered tube spectra per kVp and anode
+ * angle) replaces those numbers for the elements and tubes it lists.  The format
+ * is described in full in opendxmc_gb300/csrc/physics.hpp.  Process-wide; worlds
+ * built and spectra made after a load use it.  write dumps the current numbers of
+ * the listed elements on the DXMCG_NE-point table grid (loading that file back
+ * leaves every device table bit for bit as it was). */
+DXMCG_API int dxmcg_physics_load(const char* path);
+DXMCG_API int dxmcg_physics_reset(void);
+DXMCG_API int dxmcg_physics_write(const char* path, int n_elements, const int32_t* Z);
 /* numberOfExposures()/exposure(i) (beamactorcontainer.cpp:114-121); out may be NULL to count */
 DXMCG_API int dxmcg_beam_exposures(const dxmcg_beam* beam, dxmcg_exposure* out, int cap, int* n_out);
 /* The factor dxmcg_transport_run applies to every history weight when

@@ -284,6 +284,7 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o, bool b
     s.interact_batch = std::min(32, std::max(0, o.interact_batch));
     s.refill_batch = std::min(32, std::max(0, o.refill_batch));
     s.woodcock_steps = std::min(64, std::max(0, o.woodcock_steps));
+    s.step_min_lanes = std::min(32, std::max(0, o.step_min_lanes));
     return s;
 }
 
@@ -623,6 +624,30 @@ DXMCG_API int dxmcg_beam_exposures(const dxmcg_beam* beam, dxmcg_exposure* out, 
         return fail(DXMCG_ERR_CAPACITY, "beam_exposures: output too small");
     std::copy(ex.begin(), ex.end(), out);
     return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_physics_load(const char* path)
+{
+    if (!path)
+        return fail(DXMCG_ERR_ARGUMENT, "physics_load: null path");
+    std::string err;
+    const int rc = loadPhysicsTable(path, err);
+    return rc == DXMCG_OK ? rc : fail(rc, "physics_load: " + err);
+}
+
+DXMCG_API int dxmcg_physics_reset(void)
+{
+    resetPhysicsTable();
+    return DXMCG_OK;
+}
+
+DXMCG_API int dxmcg_physics_write(const char* path, int n_elements, const int32_t* Z)
+{
+    if (!path || n_elements < 0 || (n_elements > 0 && !Z))
+        return fail(DXMCG_ERR_ARGUMENT, "physics_write: bad arguments");
+    std::string err;
+    const int rc = writePhysicsTable(path, n_elements, Z, err);
+    return rc == DXMCG_OK ? rc : fail(rc, "physics_write: " + err);
 }
 
 DXMCG_API int dxmcg_beam_calibration(const dxmcg_beam* beam, int correction, const dxmcg_run_options* opts,

@@ -2,12 +2,12 @@
 // beamactorcontainer.cpp:114-121).
 //
 // DX and pencil beams repeat one pose n_exposures times (the pose is set by
-// DXBeam::updatePosition, dxmc_specialization.cpp:155-167; collimation
-// half-angles by DXBeam::setCollimation, :123-129).  Rotating beams (CT spiral,
+// DXBeam::updatePosition, dxmc_specialization.cpp:78-90; collimation
+// half-angles by DXBeam::setCollimation, :46-52).  Rotating beams (CT spiral,
 // CT sequential, CBCT, dual-energy spiral) put the source at SDD/2 from the
 // isocentre, with c0 along the fan, c1 along the rotation axis and the beam
 // direction c0 x c1 pointing at the isocentre -- the same basis
-// pointsFromCollimations uses (beamactorcontainer.cpp:219-231).
+// pointsFromCollimations uses (beamactorcontainer.cpp:44-67).
 #include <algorithm>
 #include <cmath>
 #include <vector>

@@ -19,9 +19,15 @@ namespace {
     std::mutex g_elementMutex;
     std::map<std::pair<int, int>, ElementTables> g_elements;
 
+    uint64_t g_elementGeneration = ~0ull; // the physics table g_elements came from
+
     const ElementTables& elementTables(int Z, int correction)
     {
         std::lock_guard<std::mutex> lock(g_elementMutex);
+        if (g_elementGeneration != physicsGeneration()) {
+            g_elements.clear();
+            g_elementGeneration = physicsGeneration();
+        }
         const auto key = std::make_pair(Z, correction);
         auto it = g_elements.find(key);
         if (it != g_elements.end())

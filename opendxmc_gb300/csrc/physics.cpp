@@ -2,10 +2,15 @@
 #include "physics.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
-#include <vector>
-#include <mutex>
+#include <cstdio>
+#include <fstream>
 #include <limits>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <vector>
 
 namespace dxmcg {
 namespace {
@@ -56,10 +61,70 @@ namespace {
             w[i] = s > 0 ? m.w[i] / s : 0.0;
         return w;
     }
+
+    // ---- loaded physics tables (format in physics.hpp)
+    struct ElementRecord {
+        bool present = false;
+        double A = 0;
+        std::vector<double> photo, incoh, incohFree, coh; // at Table::energy; incohFree may be empty
+        double a = 0, eK = 0, eL = 0, kAlpha = 0, omegaK = 0;
+        phys::Shells shells;
+    };
+    struct TubeRecord {
+        double kvp = 0, angle = 0;
+        std::vector<double> E, w;
+    };
+    struct Table {
+        std::vector<double> energy;
+        std::array<ElementRecord, 93> el {};
+        std::vector<TubeRecord> tubes;
+    };
+    std::mutex g_tableMutex;
+    std::shared_ptr<const Table> g_table;
+    std::atomic<uint64_t> g_generation { 0 };
+
+    std::shared_ptr<const Table> currentTable()
+    {
+        std::lock_guard<std::mutex> lock(g_tableMutex);
+        return g_table;
+    }
+
+    const ElementRecord* tableElement(const Table* t, int Z)
+    {
+        return (t && Z >= 1 && Z <= 92 && t->el[Z].present) ? &t->el[Z] : nullptr;
+    }
+
+    // v(E) from values at the ascending energies x (a repeated energy is an edge: the
+    // value above it is the second one): the listed value at a listed energy, else
+    // log-log interpolation in the bracketing interval, held at the ends.
+    double tableAt(const std::vector<double>& x, const std::vector<double>& v, double E)
+    {
+        const size_t n = x.size();
+        if (E <= x.front())
+            return E == x.front() && n > 1 && x[1] == x[0] ? v[1] : v.front();
+        if (E >= x.back())
+            return v.back();
+        // first index with x[i] > E; the interval is [i - 1, i]
+        const size_t i = static_cast<size_t>(std::upper_bound(x.begin(), x.end(), E) - x.begin());
+        const size_t lo = i - 1;
+        if (x[lo] == E)
+            return v[lo];
+        const double a = v[lo], b = v[i];
+        if (!(a > 0) || !(b > 0))
+            return a + (b - a) * (E - x[lo]) / (x[i] - x[lo]);
+        const double t = std::log(E / x[lo]) / std::log(x[i] / x[lo]);
+        return std::exp(std::log(a) + t * (std::log(b) - std::log(a)));
+    }
 } // namespace
 
 namespace phys {
-    double atomicMass(int Z) { return (Z >= 1 && Z <= 92) ? kAtomicMass[Z] : 0.0; }
+    double atomicMass(int Z)
+    {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return e->A;
+        return (Z >= 1 && Z <= 92) ? kAtomicMass[Z] : 0.0;
+    }
 
     double elementDensity(int Z)
     {
@@ -83,6 +148,9 @@ namespace phys {
 
     double formFactorScale(int Z)
     {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return e->a;
         const double x = std::cbrt(static_cast<double>(Z)) / (2.0 * kPi * kBohrA);
         return x * x;
     }
@@ -97,12 +165,33 @@ namespace phys {
         return 2.0 * kPi * kRe2Barn * (a + b - c);
     }
 
-    double kEdge(int Z) { return kRydKeV * (Z - 1.0) * (Z - 1.0); }
-    double lEdge(int Z) { return Z > 7 ? kRydKeV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0; }
-    double kAlphaEnergy(int Z) { return 0.75 * kEdge(Z); }
+    double kEdge(int Z)
+    {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return e->eK;
+        return kRydKeV * (Z - 1.0) * (Z - 1.0);
+    }
+    double lEdge(int Z)
+    {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return e->eL;
+        return Z > 7 ? kRydKeV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0;
+    }
+    double kAlphaEnergy(int Z)
+    {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return e->kAlpha;
+        return 0.75 * kRydKeV * (Z - 1.0) * (Z - 1.0);
+    }
 
     double fluorescenceYieldK(int Z)
     {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return e->omegaK;
         const double z = static_cast<double>(Z);
         const double x = 0.015 + 0.0327 * z - 0.64e-6 * z * z * z;
         const double x4 = x * x * x * x;
@@ -111,6 +200,9 @@ namespace phys {
 
     Shells comptonShells(int Z)
     {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return e->shells;
         Shells s;
         const double z = static_cast<double>(Z);
         const double occ[3] = { std::min(z, 2.0), std::min(std::max(z - 2.0, 0.0), 8.0), std::max(z - 10.0, 0.0) };
@@ -130,6 +222,9 @@ namespace phys {
 
     double photoelectric(double E, int Z)
     {
+        const auto t = currentTable();
+        if (const auto* e = tableElement(t.get(), Z))
+            return tableAt(t->energy, e->photo, E);
         const double z2 = static_cast<double>(Z) * Z;
         double s = kPhotoC * z2 * z2 / (E * E * E);
         if (E < kEdge(Z))
@@ -143,6 +238,13 @@ namespace phys {
     // B = 1 + T / a, which resolves the forward peak of F^2 and the rise of S.
     double incoherent(double E, int Z, int correction)
     {
+        const auto tb = currentTable();
+        if (const auto* e = tableElement(tb.get(), Z)) {
+            if (correction >= 1)
+                return tableAt(tb->energy, e->incoh, E);
+            if (!e->incohFree.empty())
+                return tableAt(tb->energy, e->incohFree, E);
+        }
         if (correction <= 0)
             return Z * kleinNishinaTotal(E);
         const double k = E / kMeKeV;
@@ -163,6 +265,9 @@ namespace phys {
 
     double coherent(double E, int Z)
     {
+        const auto tb = currentTable();
+        if (const auto* e = tableElement(tb.get(), Z))
+            return tableAt(tb->energy, e->coh, E);
         const double T = (E / kHcKeVA) * (E / kHcKeVA);
         const double a = formFactorScale(Z);
         const double L = std::log1p(T / a);
@@ -275,29 +380,44 @@ namespace {
             return elementTotalUncached(Z, E);
         const size_t idx = static_cast<size_t>(Z) * kMaxKeV + static_cast<size_t>(k);
         std::lock_guard<std::mutex> lock(guard);
-        if (cache.empty())
+        static uint64_t cacheGeneration = ~0ull; // the physics table the values came from
+        if (cache.empty() || cacheGeneration != physicsGeneration()) {
             cache.assign(93 * static_cast<size_t>(kMaxKeV), std::numeric_limits<double>::quiet_NaN());
+            cacheGeneration = physicsGeneration();
+        }
         if (std::isnan(cache[idx]))
             cache[idx] = elementTotalUncached(Z, E);
         return cache[idx];
     }
 } // namespace
 
-Spectrum tubeSpectrum(double kvp, double /*anode_angle_deg*/, int n_filters, const int32_t* Z, const double* mm)
+Spectrum tubeSpectrum(double kvp, double anode_angle_deg, int n_filters, const int32_t* Z, const double* mm)
 {
     Spectrum s;
     const int n = static_cast<int>(std::floor(kvp));
     if (n < 1 || n > 511)
         return s;
-    s.energy.resize(n);
-    s.weight.resize(n);
+    const auto table = currentTable();
+    const TubeRecord* rec = nullptr;
+    if (table)
+        for (const auto& t : table->tubes)
+            if (t.kvp == kvp && t.angle == anode_angle_deg)
+                rec = &t;
+    if (rec) {
+        // a loaded unfiltered spectrum of this exact tube setting
+        s.energy = rec->E;
+        s.weight = rec->w;
+    } else {
+        s.energy.resize(n);
+        s.weight.resize(n);
+    }
     double total = 0;
-    for (int k = 0; k < n; ++k) {
+    for (int k = 0; k < n && !rec; ++k) {
         s.energy[k] = k + 1.0;
         s.weight[k] = (kvp - s.energy[k]) / s.energy[k]; // Kramers
         total += s.weight[k];
     }
-    if (kvp > kTungstenKEdge) {
+    if (!rec && kvp > kTungstenKEdge) {
         const double lines = kCharacteristicYield * std::pow(kvp / kTungstenKEdge - 1.0, 1.63) * total;
         for (int l = 0; l < 4; ++l) {
             const int bin = static_cast<int>(std::floor(kTungstenLines[l] + 0.5)) - 1;
@@ -309,7 +429,7 @@ Spectrum tubeSpectrum(double kvp, double /*anode_angle_deg*/, int n_filters, con
         const double rho = phys::elementDensity(Z[f]);
         if (rho <= 0 || mm[f] <= 0)
             continue;
-        for (int k = 0; k < n; ++k)
+        for (size_t k = 0; k < s.energy.size(); ++k)
             s.weight[k] *= std::exp(-elementTotal(Z[f], s.energy[k]) * rho * mm[f] * 0.1);
     }
     double sum = 0;
@@ -398,6 +518,192 @@ AliasTable buildAlias(const Spectrum& s)
     for (int i = 0; i < n; ++i)
         t.threshold[i] = static_cast<uint32_t>(std::floor(prob[i] * 8388608.0 + 0.5));
     return t;
+}
+
+
+// ---------------------------------------------------------------- physics tables
+namespace {
+    bool readValues(std::istream& in, size_t n, std::vector<double>& out)
+    {
+        out.resize(n);
+        for (size_t i = 0; i < n; ++i)
+            if (!(in >> out[i]) || !std::isfinite(out[i]) || out[i] < 0)
+                return false;
+        return true;
+    }
+
+    // the file's tokens with comments removed
+    bool tokens(const std::string& path, std::stringstream& out)
+    {
+        std::ifstream f(path);
+        if (!f)
+            return false;
+        std::string line;
+        while (std::getline(f, line)) {
+            const auto c = line.find('#');
+            out << (c == std::string::npos ? line : line.substr(0, c)) << '\n';
+        }
+        return true;
+    }
+} // namespace
+
+uint64_t physicsGeneration() { return g_generation.load(); }
+
+void resetPhysicsTable()
+{
+    std::lock_guard<std::mutex> lock(g_tableMutex);
+    g_table.reset();
+    ++g_generation;
+}
+
+int loadPhysicsTable(const std::string& path, std::string& err)
+{
+    std::stringstream in;
+    if (!tokens(path, in)) {
+        err = "cannot read " + path;
+        return DXMCG_ERR_ARGUMENT;
+    }
+    auto t = std::make_shared<Table>();
+    std::string word;
+    int version = 0;
+    if (!(in >> word) || word != "dxmcg-physics" || !(in >> version) || version != 1) {
+        err = "not a dxmcg-physics 1 table";
+        return DXMCG_ERR_ARGUMENT;
+    }
+    while (in >> word) {
+        if (word == "energies") {
+            size_t n = 0;
+            if (!(in >> n) || n < 2 || n > 100000 || !readValues(in, n, t->energy)) {
+                err = "bad energies line";
+                return DXMCG_ERR_ARGUMENT;
+            }
+            for (size_t i = 0; i < n; ++i)
+                if (!(t->energy[i] > 0) || (i > 0 && t->energy[i] < t->energy[i - 1])
+                    || (i > 1 && t->energy[i] == t->energy[i - 2])) {
+                    err = "energies must be positive and ascending (an energy at most twice)";
+                    return DXMCG_ERR_ARGUMENT;
+                }
+        } else if (word == "element") {
+            int Z = 0;
+            double A = 0;
+            if (!(in >> Z >> A) || Z < 1 || Z > 92 || !(A > 0)) {
+                err = "bad element line";
+                return DXMCG_ERR_ARGUMENT;
+            }
+            if (t->energy.empty()) {
+                err = "element before energies";
+                return DXMCG_ERR_ARGUMENT;
+            }
+            ElementRecord e;
+            e.A = A;
+            bool photo = false, incoh = false, coh = false, ff = false, edges = false, fl = false, sh = false;
+            const size_t n = t->energy.size();
+            while (in >> word && word != "end") {
+                bool ok = true;
+                if (word == "photo")
+                    ok = photo = readValues(in, n, e.photo);
+                else if (word == "incoherent")
+                    ok = incoh = readValues(in, n, e.incoh);
+                else if (word == "incoherent_free")
+                    ok = readValues(in, n, e.incohFree);
+                else if (word == "coherent")
+                    ok = coh = readValues(in, n, e.coh);
+                else if (word == "formfactor")
+                    ok = ff = static_cast<bool>(in >> e.a) && e.a > 0;
+                else if (word == "edges")
+                    ok = edges = static_cast<bool>(in >> e.eK >> e.eL) && e.eK >= 0 && e.eL >= 0;
+                else if (word == "fluorescence")
+                    ok = fl = static_cast<bool>(in >> e.kAlpha >> e.omegaK) && e.kAlpha >= 0 && e.omegaK >= 0
+                        && e.omegaK <= 1;
+                else if (word == "shells") {
+                    ok = static_cast<bool>(in >> e.shells.n) && e.shells.n >= 0 && e.shells.n <= 3;
+                    for (int k = 0; ok && k < e.shells.n; ++k)
+                        ok = static_cast<bool>(in >> e.shells.electrons[k] >> e.shells.binding[k]
+                                 >> e.shells.momentum[k])
+                            && e.shells.electrons[k] >= 0 && e.shells.binding[k] >= 0 && e.shells.momentum[k] > 0;
+                    sh = ok;
+                } else {
+                    err = "unknown element field '" + word + "'";
+                    return DXMCG_ERR_ARGUMENT;
+                }
+                if (!ok) {
+                    err = "bad '" + word + "' of element " + std::to_string(Z);
+                    return DXMCG_ERR_ARGUMENT;
+                }
+            }
+            if (word != "end" || !(photo && incoh && coh && ff && edges && fl && sh)) {
+                err = "element " + std::to_string(Z)
+                    + " needs photo, incoherent, coherent, formfactor, edges, fluorescence, shells and end";
+                return DXMCG_ERR_ARGUMENT;
+            }
+            e.present = true;
+            t->el[Z] = std::move(e);
+        } else if (word == "tube") {
+            TubeRecord r;
+            size_t m = 0;
+            if (!(in >> r.kvp >> r.angle >> m) || !(r.kvp > 1) || m < 1 || m > 512) {
+                err = "bad tube line";
+                return DXMCG_ERR_ARGUMENT;
+            }
+            r.E.resize(m);
+            r.w.resize(m);
+            for (size_t i = 0; i < m; ++i)
+                if (!(in >> r.E[i] >> r.w[i]) || !(r.E[i] >= 1.0) || r.E[i] > r.kvp || !(r.w[i] >= 0)) {
+                    err = "bad tube entry";
+                    return DXMCG_ERR_ARGUMENT;
+                }
+            t->tubes.push_back(std::move(r));
+        } else {
+            err = "unknown table entry '" + word + "'";
+            return DXMCG_ERR_ARGUMENT;
+        }
+    }
+    std::lock_guard<std::mutex> lock(g_tableMutex);
+    g_table = std::move(t);
+    ++g_generation;
+    return DXMCG_OK;
+}
+
+int writePhysicsTable(const std::string& path, int n, const int32_t* Zs, std::string& err)
+{
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) {
+        err = "cannot write " + path;
+        return DXMCG_ERR_ARGUMENT;
+    }
+    std::fprintf(f, "# photon interaction data for the dxmcg engine, written by dxmcg_physics_write\n");
+    std::fprintf(f, "dxmcg-physics 1\nenergies %d", kNE);
+    for (int i = 0; i < kNE; ++i)
+        std::fprintf(f, " %.17g", kEmin + i * kDE);
+    std::fprintf(f, "\n");
+    const auto row = [&](const char* name, auto fn) {
+        std::fprintf(f, "  %s", name);
+        for (int i = 0; i < kNE; ++i)
+            std::fprintf(f, " %.17g", fn(kEmin + i * kDE));
+        std::fprintf(f, "\n");
+    };
+    for (int k = 0; k < n; ++k) {
+        const int Z = Zs[k];
+        if (Z < 1 || Z > 92)
+            continue;
+        std::fprintf(f, "element %d %.17g\n", Z, phys::atomicMass(Z));
+        row("photo", [Z](double E) { return phys::photoelectric(E, Z); });
+        row("incoherent", [Z](double E) { return phys::incoherent(E, Z, 1); });
+        row("incoherent_free", [Z](double E) { return phys::incoherent(E, Z, 0); });
+        row("coherent", [Z](double E) { return phys::coherent(E, Z); });
+        std::fprintf(f, "  formfactor %.17g\n  edges %.17g %.17g\n  fluorescence %.17g %.17g\n",
+            phys::formFactorScale(Z), phys::kEdge(Z), phys::lEdge(Z), phys::kAlphaEnergy(Z),
+            phys::fluorescenceYieldK(Z));
+        const auto sh = phys::comptonShells(Z);
+        std::fprintf(f, "  shells %d", sh.n);
+        for (int s = 0; s < sh.n; ++s)
+            std::fprintf(f, " %.17g %.17g %.17g", sh.electrons[s], sh.binding[s], sh.momentum[s]);
+        std::fprintf(f, "\nend\n");
+    }
+    const bool ok = std::fclose(f) == 0;
+    if (!ok)
+        err = "error writing " + path;
+    return ok ? DXMCG_OK : DXMCG_ERR_ARGUMENT;
 }
 
 } // namespace dxmcg

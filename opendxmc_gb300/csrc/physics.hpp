@@ -21,10 +21,37 @@
 //    leaves a K vacancy with probability 1 - 1/J_K, which emits a K-alpha photon of
 //    0.75 Ryd (Z - 1)^2 with the yield omega_K(Z) of Bambynek et al. (Rev. Mod. Phys.
 //    44, 716, 1972): omega = X^4 / (1 + X^4), X = 0.015 + 0.0327 Z - 0.64e-6 Z^3.
+//
+// Physics tables.  A table file replaces the model's numbers element by element
+// (elements it does not list keep the model) and may add unfiltered tube spectra.
+// It is plain text, whitespace-separated, '#' starts a comment:
+//
+//   dxmcg-physics 1
+//   energies <n> <E_1> ... <E_n>          keV, ascending; a repeated energy marks an
+//                                          absorption edge (below, then above it)
+//   element <Z> <A>                        atomic number, atomic mass (g/mol)
+//     photo <n values>                     photoelectric, barn/atom, at the energies
+//     incoherent <n values>                Compton with binding (correction >= 1)
+//     incoherent_free <n values>           Compton of free electrons (correction 0;
+//                                          optional: Z x Klein-Nishina when absent)
+//     coherent <n values>                  Rayleigh
+//     formfactor <a_Z>                     1/A^2 scale of F and S in the samplers
+//     edges <K keV> <L keV>
+//     fluorescence <K-alpha keV> <omega_K>
+//     shells <m> (<electrons> <binding keV> <momentum m_e c>) x m    (m <= 3)
+//   end
+//   tube <kVp> <anode angle deg> <m> (<E keV> <photons>) x m
+//
+// Cross sections between the listed energies are interpolated linearly in log E and
+// log sigma (linearly where a value is 0), and held at the end values outside them;
+// at a listed energy the listed value is returned exactly.  A tube entry replaces
+// the unfiltered spectrum of that exact (kVp, anode angle); filtration is applied as
+// usual.  Loaded tables take effect for worlds built and spectra made afterwards.
 #pragma once
 
 #include <array>
 #include <cstdint>
+#include <string>
 #include <vector>
 
 #include "../../include/dxmcg.h"
@@ -59,6 +86,15 @@ namespace phys {
     };
     Shells comptonShells(int Z);
 }
+
+// Physics tables (format above): load replaces the current table (reset: the model
+// alone); write dumps the current numbers of the given elements on the attenuation
+// table grid (1.0 + 0.5 i keV, i < DXMCG_NE).  Each load or reset increments the
+// generation, which the caches keyed on element data compare against.
+int loadPhysicsTable(const std::string& path, std::string& err);
+void resetPhysicsTable();
+int writePhysicsTable(const std::string& path, int n, const int32_t* Z, std::string& err);
+uint64_t physicsGeneration();
 
 // Composition -> mass attenuation (cm^2/g) at arbitrary energies.
 struct Attenuation {

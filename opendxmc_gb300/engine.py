@@ -73,6 +73,22 @@ def beam_exposures(params: dict) -> list[dict]:
              "tube": e.tube} for e in arr[:n.value]]
 
 
+def physics_load(path) -> None:
+    """Load a physics table (dxmcg-physics 1 text format) for the whole process."""
+    N.check(N.lib().dxmcg_physics_load(str(path).encode()))
+
+
+def physics_reset() -> None:
+    """Back to the engine's own parametric model."""
+    N.check(N.lib().dxmcg_physics_reset())
+
+
+def physics_write(path, elements) -> None:
+    """Write the current numbers of `elements` (atomic numbers) as a physics table."""
+    z = np.ascontiguousarray(list(elements), dtype=np.int32)
+    N.check(N.lib().dxmcg_physics_write(str(path).encode(), z.size, N.ptr(z, C.c_int32)))
+
+
 def beam_calibration(params: dict, correction: int = 1, options: N.RunOptions | None = None) -> float:
     """The factor the transport applies to every history weight with normalize set
     (DX/CBCT: DAP, pencil: air kerma, CT: CTDI phantom run, which needs a device)."""
@@ -85,7 +101,7 @@ def beam_calibration(params: dict, correction: int = 1, options: N.RunOptions | 
 
 def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_size=0, blocks_per_sm=0,
                 chunk_log2=0, hist_begin=0, hist_end=0, interact_batch=0, refill_batch=0,
-                macro_cell=0, woodcock_steps=0, max_steps=0, gather_skip=0) -> N.RunOptions:
+                macro_cell=0, woodcock_steps=0, max_steps=0, gather_skip=0, step_min_lanes=0) -> N.RunOptions:
     o = N.RunOptions()
     o.seed = seed
     o.stream = stream
@@ -102,6 +118,7 @@ def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_
     o.woodcock_steps = woodcock_steps
     o.max_steps = max_steps
     o.gather_skip = gather_skip
+    o.step_min_lanes = step_min_lanes
     return o
 
 

@@ -26,7 +26,8 @@ STATUS = {0: "OK", -1: "ARGUMENT", -2: "CUDA", -3: "STATE", -4: "CANCELLED", -5:
 EXPORTED = [
     "dxmcg_version", "dxmcg_last_error", "dxmcg_device_count", "dxmcg_set_device", "dxmcg_material_attenuation",
     "dxmcg_tube_spectrum",
-    "dxmcg_tube_mean_energy", "dxmcg_tube_al_hvl", "dxmcg_beam_exposures", "dxmcg_beam_calibration",
+    "dxmcg_tube_mean_energy", "dxmcg_tube_al_hvl", "dxmcg_physics_load", "dxmcg_physics_reset",
+    "dxmcg_physics_write", "dxmcg_beam_exposures", "dxmcg_beam_calibration",
     "dxmcg_world_create",
     "dxmcg_world_set_data", "dxmcg_world_set_data_f32", "dxmcg_world_build", "dxmcg_world_destroy",
     "dxmcg_world_clear_tally", "dxmcg_world_read_tally", "dxmcg_world_read_dose", "dxmcg_world_tables",
@@ -156,7 +157,8 @@ class RunOptions(C.Structure):
                 ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk_histories_log2", C.c_int32),
                 ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64), ("interact_batch", C.c_int32),
                 ("refill_batch", C.c_int32), ("macro_cell", C.c_int32),
-                ("woodcock_steps", C.c_int32), ("max_steps", C.c_uint32), ("gather_skip", C.c_int32)]
+                ("woodcock_steps", C.c_int32), ("max_steps", C.c_uint32), ("gather_skip", C.c_int32),
+                ("step_min_lanes", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -197,6 +199,9 @@ def lib() -> C.CDLL:
         "dxmcg_tube_al_hvl": (i, [d, i, pi32, pd, pd]),
         "dxmcg_beam_exposures": (i, [C.POINTER(Beam), C.POINTER(Exposure), i, C.POINTER(C.c_int)]),
         "dxmcg_beam_calibration": (i, [C.POINTER(Beam), i, C.POINTER(RunOptions), pd]),
+        "dxmcg_physics_load": (i, [cp]),
+        "dxmcg_physics_reset": (i, []),
+        "dxmcg_physics_write": (i, [cp, i, pi32]),
         "dxmcg_world_create": (i, [pi32, pd, C.POINTER(Material), i, i, C.POINTER(vp)]),
         "dxmcg_world_set_data": (i, [vp, pd, pu8]),
         "dxmcg_world_set_data_f32": (i, [vp, pf, pu8]),

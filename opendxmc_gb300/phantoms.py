@@ -143,9 +143,9 @@ BODY_BOWTIE = [
 
 def dx_beam_params(kvp=70.0, al_mm=2.5, field_cm=10.0, sid_cm=100.0, particles=1_000_000, exposures=10) -> dict:
     """Planar DX beam as OpenDXMC's DXBeam sets it up at 0/0 degrees: source at
-    +y, c0 = +z, c1 = -x, beam along -y (dxmc_specialization.cpp:98-103, :155-167);
+    +y, c0 = +z, c1 = -x, beam along -y (dxmc_specialization.cpp:21-26, :78-90);
     square field of `field_cm` at the isocentre distance, half-angles from
-    DXBeam::setCollimation (dxmc_specialization.cpp:123-129)."""
+    DXBeam::setCollimation (dxmc_specialization.cpp:46-52)."""
     half = float(np.tan(0.5 * field_cm / sid_cm))
     return {
         "type": 0,

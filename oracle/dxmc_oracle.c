@@ -13,6 +13,7 @@
 #include <float.h>
 #include <math.h>
 #include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -45,7 +46,231 @@ static const double ATOMIC_MASS[93] = { 0.0, 1.008, 4.0026, 6.94, 9.0122, 10.81,
     200.59, 204.38, 207.2, 208.98, 209.0, 210.0, 222.0, 223.0, 226.0, 227.0, 232.04, 231.04,
     238.03 };
 
-double or_atomic_mass(int Z) { return (Z >= 1 && Z <= 92) ? ATOMIC_MASS[Z] : 0.0; }
+/* ------------------------------------------------------------------------- */
+/* Physics tables: the engine's "dxmcg-physics 1" text format (documented in the  */
+/* engine's csrc/physics.hpp), restated.  A loaded table replaces the model's     */
+/* numbers for the elements and tube settings it lists.  Not thread-safe against */
+/* running transports: load before building worlds.                              */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    int present;
+    double A;
+    double *photo, *incoh, *incoh_free, *coh; /* at TABLE.energy; incoh_free may be NULL */
+    double a, eK, eL, kAlpha, omegaK;
+    int nsh;
+    double sh_el[3], sh_bd[3], sh_mo[3];
+} elem_rec;
+typedef struct {
+    double kvp, angle;
+    int m;
+    double *E, *w;
+} tube_rec;
+static struct {
+    int n;
+    double* energy;
+    elem_rec el[93];
+    int ntubes;
+    tube_rec* tubes;
+} TABLE;
+
+static const elem_rec* table_elem(int Z)
+{
+    return (Z >= 1 && Z <= 92 && TABLE.el[Z].present) ? &TABLE.el[Z] : NULL;
+}
+
+/* the listed value at a listed energy (the second of a repeated one: above the
+ * edge), else log-log interpolation in the bracketing interval, held at the ends */
+static double table_at(const double* v, double E)
+{
+    const double* x = TABLE.energy;
+    const int n = TABLE.n;
+    if (E <= x[0])
+        return (E == x[0] && n > 1 && x[1] == x[0]) ? v[1] : v[0];
+    if (E >= x[n - 1])
+        return v[n - 1];
+    int lo = 0, hi = n; /* first index with x > E */
+    while (lo < hi) {
+        const int mid = (lo + hi) / 2;
+        if (x[mid] > E)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    const int i = lo, l = i - 1;
+    if (x[l] == E)
+        return v[l];
+    const double a = v[l], b = v[i];
+    if (!(a > 0) || !(b > 0))
+        return a + (b - a) * (E - x[l]) / (x[i] - x[l]);
+    const double t = log(E / x[l]) / log(x[i] / x[l]);
+    return exp(log(a) + t * (log(b) - log(a)));
+}
+
+void or_physics_reset(void)
+{
+    for (int Z = 0; Z <= 92; ++Z) {
+        free(TABLE.el[Z].photo);
+        free(TABLE.el[Z].incoh);
+        free(TABLE.el[Z].incoh_free);
+        free(TABLE.el[Z].coh);
+    }
+    for (int t = 0; t < TABLE.ntubes; ++t) {
+        free(TABLE.tubes[t].E);
+        free(TABLE.tubes[t].w);
+    }
+    free(TABLE.tubes);
+    free(TABLE.energy);
+    memset(&TABLE, 0, sizeof(TABLE));
+}
+
+typedef struct {
+    char* p; /* next unread character */
+} toks;
+/* the next whitespace-separated word (terminated in place), or NULL at the end */
+static char* tok(toks* t)
+{
+    char* c = t->p;
+    while (*c == ' ' || *c == '\t' || *c == '\r' || *c == '\n')
+        ++c;
+    if (!*c) {
+        t->p = c;
+        return NULL;
+    }
+    char* w = c;
+    while (*c && *c != ' ' && *c != '\t' && *c != '\r' && *c != '\n')
+        ++c;
+    if (*c)
+        *c++ = '\0';
+    t->p = c;
+    return w;
+}
+static int num(toks* t, double* out)
+{
+    char* w = tok(t);
+    char* end = NULL;
+    if (!w)
+        return 0;
+    *out = strtod(w, &end);
+    return *end == '\0' && isfinite(*out);
+}
+static double* values(toks* t, int n)
+{
+    double* v = (double*)malloc((size_t)n * sizeof(double));
+    for (int i = 0; v && i < n; ++i)
+        if (!num(t, &v[i]) || v[i] < 0) {
+            free(v);
+            return NULL;
+        }
+    return v;
+}
+
+/* 0 on success; a negative value (nothing changed) on a malformed file */
+int or_physics_load(const char* path)
+{
+    FILE* f = fopen(path, "rb");
+    if (!f)
+        return -1;
+    fseek(f, 0, SEEK_END);
+    const long len = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    char* buf = (char*)malloc((size_t)len + 1);
+    const size_t got = fread(buf, 1, (size_t)len, f);
+    fclose(f);
+    buf[got] = '\0';
+    for (char* c = buf; *c; ++c) /* comments run to the end of the line */
+        if (*c == '#')
+            while (*c && *c != '\n')
+                *c++ = ' ';
+    or_physics_reset();
+    toks t = { buf };
+    char* w = tok(&t);
+    double v;
+    int rc = 0;
+    if (!w || strcmp(w, "dxmcg-physics") != 0 || !num(&t, &v) || v != 1.0)
+        rc = -2;
+    while (rc == 0 && (w = tok(&t)) != NULL) {
+        if (strcmp(w, "energies") == 0) {
+            if (!num(&t, &v) || v < 2) {
+                rc = -3;
+                break;
+            }
+            TABLE.n = (int)v;
+            TABLE.energy = values(&t, TABLE.n);
+            if (!TABLE.energy)
+                rc = -3;
+            for (int i = 0; rc == 0 && i < TABLE.n; ++i) /* ascending, an energy at most twice */
+                if (!(TABLE.energy[i] > 0) || (i > 0 && TABLE.energy[i] < TABLE.energy[i - 1])
+                    || (i > 1 && TABLE.energy[i] == TABLE.energy[i - 2]))
+                    rc = -3;
+        } else if (strcmp(w, "element") == 0) {
+            double z, A;
+            if (!num(&t, &z) || !num(&t, &A) || z < 1 || z > 92 || !(A > 0) || TABLE.n == 0) {
+                rc = -4;
+                break;
+            }
+            elem_rec* e = &TABLE.el[(int)z];
+            e->A = A;
+            int seen = 0; /* formfactor, edges, fluorescence, shells */
+            while (rc == 0 && (w = tok(&t)) != NULL && strcmp(w, "end") != 0) {
+                if (strcmp(w, "formfactor") == 0 || strcmp(w, "edges") == 0 || strcmp(w, "fluorescence") == 0
+                    || strcmp(w, "shells") == 0)
+                    seen |= w[0] == 'f' ? (w[1] == 'o' ? 1 : 4) : (w[0] == 'e' ? 2 : 8);
+                if (strcmp(w, "photo") == 0)
+                    rc = (e->photo = values(&t, TABLE.n)) ? 0 : -5;
+                else if (strcmp(w, "incoherent") == 0)
+                    rc = (e->incoh = values(&t, TABLE.n)) ? 0 : -5;
+                else if (strcmp(w, "incoherent_free") == 0)
+                    rc = (e->incoh_free = values(&t, TABLE.n)) ? 0 : -5;
+                else if (strcmp(w, "coherent") == 0)
+                    rc = (e->coh = values(&t, TABLE.n)) ? 0 : -5;
+                else if (strcmp(w, "formfactor") == 0)
+                    rc = num(&t, &e->a) ? 0 : -5;
+                else if (strcmp(w, "edges") == 0)
+                    rc = num(&t, &e->eK) && num(&t, &e->eL) ? 0 : -5;
+                else if (strcmp(w, "fluorescence") == 0)
+                    rc = num(&t, &e->kAlpha) && num(&t, &e->omegaK) ? 0 : -5;
+                else if (strcmp(w, "shells") == 0) {
+                    rc = num(&t, &v) && v >= 0 && v <= 3 ? 0 : -5;
+                    e->nsh = (int)v;
+                    for (int k = 0; rc == 0 && k < e->nsh; ++k)
+                        rc = num(&t, &e->sh_el[k]) && num(&t, &e->sh_bd[k]) && num(&t, &e->sh_mo[k]) ? 0 : -5;
+                } else
+                    rc = -6;
+            }
+            if (rc == 0 && (!w || !e->photo || !e->incoh || !e->coh || seen != 15 || !(e->a > 0)))
+                rc = -7;
+            e->present = rc == 0;
+        } else if (strcmp(w, "tube") == 0) {
+            double kvp, ang, m;
+            if (!num(&t, &kvp) || !num(&t, &ang) || !num(&t, &m) || m < 1 || m > 512) {
+                rc = -8;
+                break;
+            }
+            TABLE.tubes = (tube_rec*)realloc(TABLE.tubes, (size_t)(TABLE.ntubes + 1) * sizeof(tube_rec));
+            tube_rec* r = &TABLE.tubes[TABLE.ntubes++];
+            r->kvp = kvp;
+            r->angle = ang;
+            r->m = (int)m;
+            r->E = (double*)malloc((size_t)r->m * sizeof(double));
+            r->w = (double*)malloc((size_t)r->m * sizeof(double));
+            for (int i = 0; rc == 0 && i < r->m; ++i)
+                rc = num(&t, &r->E[i]) && num(&t, &r->w[i]) ? 0 : -8;
+        } else
+            rc = -9;
+    }
+    free(buf);
+    if (rc != 0)
+        or_physics_reset();
+    return rc;
+}
+
+double or_atomic_mass(int Z)
+{
+    const elem_rec* e = table_elem(Z);
+    if (e)
+        return e->A;
+    return (Z >= 1 && Z <= 92) ? ATOMIC_MASS[Z] : 0.0;
+}
 
 /* Mass densities (g/cm3) of elements used as tube filters. */
 double or_element_density(int Z)
@@ -113,17 +338,43 @@ static double kn_dcs(double k, double mu)
  * hydrogen-like 1s Compton profile of momentum scale sqrt(U/Ryd) atomic units
  * (alpha m_e c per atomic unit). */
 #define FINE_STRUCTURE 7.2973525693e-3
-double or_k_edge(int Z) { return RYD_KEV * (Z - 1.0) * (Z - 1.0); }
-double or_l_edge(int Z) { return Z > 7 ? RYD_KEV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0; }
-double or_k_alpha(int Z) { return 0.75 * or_k_edge(Z); }
+double or_k_edge(int Z)
+{
+    const elem_rec* e = table_elem(Z);
+    return e ? e->eK : RYD_KEV * (Z - 1.0) * (Z - 1.0);
+}
+double or_l_edge(int Z)
+{
+    const elem_rec* e = table_elem(Z);
+    if (e)
+        return e->eL;
+    return Z > 7 ? RYD_KEV * (Z - 7.4) * (Z - 7.4) * 0.25 : 0.0;
+}
+double or_k_alpha(int Z)
+{
+    const elem_rec* e = table_elem(Z);
+    return e ? e->kAlpha : 0.75 * RYD_KEV * (Z - 1.0) * (Z - 1.0);
+}
 double or_fluorescence_yield_k(int Z)
 {
+    const elem_rec* e = table_elem(Z);
+    if (e)
+        return e->omegaK;
     const double x = 0.015 + 0.0327 * Z - 0.64e-6 * (double)Z * Z * Z;
     const double x4 = x * x * x * x;
     return x4 / (1.0 + x4);
 }
 int or_compton_shells(int Z, double electrons[3], double binding[3], double momentum[3])
 {
+    const elem_rec* e = table_elem(Z);
+    if (e) {
+        for (int k = 0; k < e->nsh; ++k) {
+            electrons[k] = e->sh_el[k];
+            binding[k] = e->sh_bd[k];
+            momentum[k] = e->sh_mo[k];
+        }
+        return e->nsh;
+    }
     const double z = (double)Z;
     double occ[3], bind[3];
     occ[0] = z < 2.0 ? z : 2.0;
@@ -148,6 +399,9 @@ int or_compton_shells(int Z, double electrons[3], double binding[3], double mome
 
 double or_sigma_photo(double E, int Z)
 {
+    const elem_rec* e = table_elem(Z);
+    if (e)
+        return table_at(e->photo, E);
     const double z2 = (double)Z * (double)Z;
     double s = C_PE * z2 * z2 / (E * E * E);
     const double ek = RYD_KEV * (Z - 1.0) * (Z - 1.0);
@@ -170,6 +424,11 @@ static double simpson_weight(int i)
 
 double or_sigma_incoh(double E, int Z, int correction)
 {
+    const elem_rec* e = table_elem(Z);
+    if (e && correction >= 1)
+        return table_at(e->incoh, E);
+    if (e && e->incoh_free)
+        return table_at(e->incoh_free, E);
     if (correction <= 0)
         return Z * or_sigma_kn(E);
     const double k = E / ME_KEV;
@@ -190,6 +449,9 @@ double or_sigma_incoh(double E, int Z, int correction)
 
 double or_sigma_coh(double E, int Z)
 {
+    const elem_rec* e = table_elem(Z);
+    if (e)
+        return table_at(e->coh, E);
     const double T = (E / HC_KEV_A) * (E / HC_KEV_A);
     const double a = a_Z(Z);
     const double L = log1p(T / a);
@@ -272,18 +534,28 @@ static const double W_LINE_FRAC[4] = { 0.27, 0.47, 0.18, 0.08 };
 int or_tube_spectrum(double kvp, double anode_angle_deg, int n_filters, const int32_t* fZ,
     const double* fmm, double* energies, double* weights, int cap)
 {
-    (void)anode_angle_deg;
-    const int n = (int)floor(kvp);
+    int n = (int)floor(kvp);
     if (n < 1 || n > cap)
         return -1;
+    const tube_rec* rec = NULL; /* a loaded unfiltered spectrum of this exact setting */
+    for (int t = 0; t < TABLE.ntubes; ++t)
+        if (TABLE.tubes[t].kvp == kvp && TABLE.tubes[t].angle == anode_angle_deg)
+            rec = &TABLE.tubes[t];
     double total = 0.0;
-    for (int k = 0; k < n; ++k) {
-        const double E = k + 1.0;
-        energies[k] = E;
-        weights[k] = (kvp - E) / E;
-        total += weights[k];
-    }
-    if (kvp > W_K_EDGE) {
+    if (rec) {
+        if (rec->m > cap)
+            return -1;
+        n = rec->m;
+        memcpy(energies, rec->E, (size_t)n * sizeof(double));
+        memcpy(weights, rec->w, (size_t)n * sizeof(double));
+    } else
+        for (int k = 0; k < n; ++k) {
+            const double E = k + 1.0;
+            energies[k] = E;
+            weights[k] = (kvp - E) / E;
+            total += weights[k];
+        }
+    if (!rec && kvp > W_K_EDGE) {
         const double nchar = C_CHAR * pow(kvp / W_K_EDGE - 1.0, 1.63) * total;
         for (int l = 0; l < 4; ++l) {
             const int bin = (int)floor(W_LINES[l] + 0.5) - 1;
@@ -495,10 +767,10 @@ static void rotate3(const double v[3], const double k[3], double a, double out[3
 
 /* ------------------------------------------------------------------------- */
 /* Beam -> exposures.  DX: every exposure has the beam's pose
- * (dxmc_specialization.cpp:155-167 sets position/cosines; collimation half-angles
+ * (dxmc_specialization.cpp:78-90 sets position/cosines; collimation half-angles
  * :123-129).  Rotating beams place the source at SDD/2 from the isocentre, the
  * fan along c0, the rotation axis along c1, and direction = c0 x c1 pointing at
- * the isocentre (beamactorcontainer.cpp:219-231 uses the same basis).         */
+ * the isocentre (beamactorcontainer.cpp:44-67 uses the same basis).         */
 /* ------------------------------------------------------------------------- */
 static double interp_profile(const double* w, int n, double f)
 {

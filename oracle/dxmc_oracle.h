@@ -7,8 +7,8 @@
  * It restates, in plain C with FP64 arithmetic, the path OpenDXMC reaches at
  * src/libopendxmc/simulationpipeline.cpp:165 (`transport(world, beam, progress, true)`):
  * world ingest (simulationpipeline.cpp:127-153), tube spectrum
- * (ctsegmentationpipeline.cpp:66-71), beam -> exposures (dxmc_specialization.cpp:155-167,
- * beamactorcontainer.cpp:211-236), per-history source sampling, voxel traversal,
+ * (ctsegmentationpipeline.cpp:66-71), beam -> exposures (dxmc_specialization.cpp:78-90,
+ * beamactorcontainer.cpp:44-67, :110-170), per-history source sampling, voxel traversal,
  * interaction sampling and per-voxel energy scoring (readback at
  * simulationpipeline.cpp:174-231).
  *
@@ -133,6 +133,11 @@ typedef struct {
 
 typedef struct or_world or_world;
 
+/* physics tables ("dxmcg-physics 1" text, as the engine reads it): load replaces the
+ * model's numbers for the listed elements and tube settings (0, or < 0 on a bad
+ * file, which leaves the model alone); reset returns to the model */
+int or_physics_load(const char* path);
+void or_physics_reset(void);
 /* physics (per atom, barn; energies keV) */
 double or_atomic_mass(int Z);
 double or_element_density(int Z);

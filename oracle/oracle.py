@@ -210,6 +210,21 @@ def lib() -> C.CDLL:
     return L
 
 
+def physics_load(path) -> None:
+    L = lib()
+    L.or_physics_load.restype = C.c_int
+    L.or_physics_load.argtypes = [C.c_char_p]
+    rc = L.or_physics_load(str(path).encode())
+    if rc != 0:
+        raise ValueError(f"oracle: bad physics table ({rc})")
+
+
+def physics_reset() -> None:
+    L = lib()
+    L.or_physics_reset.restype = None
+    L.or_physics_reset()
+
+
 def _p(a: np.ndarray, t):
     return a.ctypes.data_as(C.POINTER(t))
 

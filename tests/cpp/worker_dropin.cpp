@@ -71,7 +71,7 @@ int main(int argc, char** argv)
     dxmc::Transport transport;
     transport.setNumberOfThreads(16);
 
-    // DX beam as OpenDXMC's DXBeam sets it up at 0/0 degrees (dxmc_specialization.cpp:98-167)
+    // DX beam as OpenDXMC's DXBeam sets it up at 0/0 degrees (dxmc_specialization.cpp:21-90)
     dxmc::DXBeam<false> dx({ 0, 100, 0 }, { { { 0, 0, 1 }, { -1, 0, 0 } } }, { { 13, 2.5 } });
     dx.setTubeVoltage(70.0);
     dx.setCollimationHalfAngles({ std::tan(0.5 * 10.0 / 100.0), std::tan(0.5 * 10.0 / 100.0) });

@@ -62,7 +62,7 @@ def test_source_sampling_matches_oracle(gpu, oracle, which):
 def test_dual_energy_tubes_use_their_own_bowtie(gpu, oracle):
     """Tube B's photons are weighted with tube B's profile: sampled weights differ
     from those of a beam whose two tubes share tube A's profile exactly on tube B's
-    exposures (odd exposure numbers: A and B alternate, beamactorcontainer.cpp:301-313)."""
+    exposures (odd exposure numbers: A and B alternate, beamactorcontainer.cpp:134-146)."""
     ph = parity.small_torso()
     gw, ow = worlds(gpu, oracle, ph)
     own = P.ct_dual_energy_params(particles=50, bowtie_b=W1_80KV)

@@ -1,0 +1,110 @@
+"""The configured workloads against the FP64 oracle, each at a history count the
+oracle runs in seconds on the host's cores, with the oracle fed the caller's own
+FP64 densities (AAVoxelGrid::setData's vector<double>, simulationpipeline.cpp:149),
+not the engine's 16-bit-mantissa packing of them.  Each test prints its error line:
+the fraction of voxels above 5 % of the maximum whose energy agrees within 3
+combined standard errors, and the relative difference of the total energy
+imparted (criteria: >= 99 % and <= 0.3 %)."""
+import numpy as np
+import pytest
+
+from opendxmc_gb300 import phantoms as P
+import parity
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_world(gpu, ph, correction=1):
+    w = gpu.GpuWorld(ph.dims, ph.spacing, ph.materials, correction)
+    w.set_data(ph.density, ph.material)
+    w.build()
+    return w
+
+
+def error_line(name, n, e1, q1, e2, q2):
+    frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
+                                                 parity.tally_variance(e2, q2, n))
+    rel = e1.sum() / e2.sum() - 1.0
+    print(f"\nconfig {name}: {n:.3g} histories, {nvox} voxels above 5 % of max, {frac:.4f} within 3 sigma, "
+          f"total energy GPU/oracle - 1 = {rel:+.2e}")
+    return frac, nvox, rel
+
+
+def test_c2_torso_1e8_histories_against_fp64_densities(gpu, oracle):
+    """The 256x256x200 spiral-CT torso at 1e8 histories (a tenth of the configured
+    step), oracle on the caller's FP64 densities."""
+    ph = P.torso_phantom(seed=1)
+    gw = gpu_world(gpu, ph)
+    ow = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    beam = P.ct_spiral_params(particles=277_778)  # 360 exposures -> 1.0e8 histories
+    sg = gw.run(beam, gpu.run_options(seed=21, stream=0))
+    so = ow.run(beam, seed=21, stream=1)
+    n = sg["n_histories"]
+    assert n == so["n_histories"] == 360 * 277_778 and sg["n_errors"] == 0
+    e1, q1, _ = gw.tally()
+    e2, q2, _ = ow.tally()
+    frac, nvox, rel = error_line("C2", n, e1, q1, e2, q2)
+    assert nvox > 500_000
+    assert frac >= 0.99, frac
+    assert abs(rel) <= 3e-3
+
+
+def test_c1_cylinder_against_fp64_densities(gpu, oracle):
+    """The DX water cylinder at its configured 1e7 histories from seed 1."""
+    ph = P.water_cylinder_phantom()
+    gw = gpu_world(gpu, ph)
+    ow = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    beam = P.dx_beam_params(particles=1_000_000, exposures=10)
+    sg = gw.run(beam, gpu.run_options(seed=1, stream=0))
+    so = ow.run(beam, seed=1, stream=1)
+    n = sg["n_histories"]
+    assert n == so["n_histories"] == 10_000_000
+    e1, q1, _ = gw.tally()
+    e2, q2, _ = ow.tally()
+    frac, nvox, rel = error_line("C1", n, e1, q1, e2, q2)
+    assert nvox > 10_000 and frac >= 0.99 and abs(rel) <= 3e-3
+
+
+def test_c3_batch_jobs_against_oracle(gpu, oracle):
+    """Three jobs of the 64-job batch workload (the smallest grids among those under
+    2e7 histories) in one persistent launch, each against its own oracle run."""
+    specs = P.batched_jobs(n_jobs=64, seed=1)
+
+    def hist(sp):
+        b = sp["beam"]
+        return b["particles_per_exposure"] * b.get("n_exposures", 91)
+
+    cand = [j for j, sp in enumerate(specs) if hist(sp) < 2e7]
+    pick = sorted(cand, key=lambda j: np.prod(specs[j]["dims"]))[:3]
+    phs = [P.ellipsoid_phantom(specs[j]["dims"], specs[j]["spacing"], specs[j]["seed"]) for j in pick]
+    worlds = [gpu_world(gpu, ph) for ph in phs]
+    batch = gpu.Batch([(w, specs[j]["beam"], gpu.run_options(seed=31, stream=j)) for w, j in zip(worlds, pick)])
+    batch.run()
+    for w, ph, j in zip(worlds, phs, pick):
+        ow = oracle.World(ph.dims, ph.spacing, ph.density.astype(np.float64), ph.material, ph.materials)
+        so = ow.run(specs[j]["beam"], seed=31, stream=1000 + j)
+        n = so["n_histories"]
+        e1, q1, _ = w.tally()
+        e2, q2, _ = ow.tally()
+        frac, nvox, rel = error_line(f"C3 job {j} {specs[j]['dims']}", n, e1, q1, e2, q2)
+        assert nvox > 1000 and frac >= 0.99 and abs(rel) <= 3e-3, (j, frac, rel)
+    batch.close()
+
+
+def test_c5_torso_history_range_against_oracle(gpu, oracle):
+    """The 512x512x400 torso (pitch 0.8, 80 mm collimation): the first 2e7 histories
+    of the configured beam on both sides, oracle on the caller's FP64 densities."""
+    dims, spacing = (512, 512, 400), (0.08, 0.08, 0.1)
+    ph = P.torso_phantom(dims=dims, spacing=spacing, seed=7)
+    gw = gpu_world(gpu, ph)
+    ow = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    del ph
+    beam = P.ct_spiral_params(pitch=0.8, collimation_cm=8.0, particles=2_000_000)
+    sg = gw.run(beam, gpu.run_options(seed=41, stream=0, hist_end=20_000_000))
+    so = ow.run(beam, seed=41, stream=1, hist_end=20_000_000)
+    n = sg["n_histories"]
+    assert n == so["n_histories"] == 20_000_000 and sg["n_errors"] == 0
+    e1, q1, _ = gw.tally()
+    e2, q2, _ = ow.tally()
+    frac, nvox, rel = error_line("C5", n, e1, q1, e2, q2)
+    assert nvox > 100_000 and frac >= 0.99 and abs(rel) <= 3e-3

@@ -64,8 +64,6 @@ def parse():
                    help="Woodcock steps a lane takes between regroupings (0: library default)")
     p.add_argument("--gather-skip", type=int, choices=[-1, 0, 1], default=0,
                    help="Woodcock gather skip: 1 on, -1 off, 0 library default (on above 64 MiB of voxels)")
-    p.add_argument("--step-min-lanes", type=int, default=0,
-                   help="Woodcock: a step phase ends once fewer lanes still step (0: library default)")
     p.add_argument("--interact-batch", type=int, default=0)
     p.add_argument("--refill-batch", type=int, default=0)
     p.add_argument("--correction", type=int, choices=[0, 1, 2], default=1,
@@ -322,8 +320,7 @@ def run_ours(args):
     def run_opts(seed):
         return G.run_options(seed=seed, stream=rank, tracking=TRACKING[args.tracking], macro_cell=args.macro_cell,
                              woodcock_steps=args.woodcock_steps, interact_batch=args.interact_batch,
-                             refill_batch=args.refill_batch, gather_skip=args.gather_skip,
-                             step_min_lanes=args.step_min_lanes)
+                             refill_batch=args.refill_batch, gather_skip=args.gather_skip)
 
     def step(seed):
         flush.fill_(float(seed))

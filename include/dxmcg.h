@@ -179,10 +179,6 @@ typedef struct {
      * (4 bytes per voxel; for a batch, of all its worlds, decided from opts[0])
      * exceed 64 MiB, where they no longer stay in L2 */
     int32_t gather_skip;
-    /* WOODCOCK tracking: a warp's step phase ends once fewer than this many of its
-     * lanes are still stepping (the rest keep their photons for the next phase);
-     * 0 = default */
-    int32_t step_min_lanes;
 } dxmcg_run_options;
 
 typedef struct {

@@ -284,7 +284,6 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o, bool b
     s.interact_batch = std::min(32, std::max(0, o.interact_batch));
     s.refill_batch = std::min(32, std::max(0, o.refill_batch));
     s.woodcock_steps = std::min(64, std::max(0, o.woodcock_steps));
-    s.step_min_lanes = std::min(32, std::max(0, o.step_min_lanes));
     return s;
 }
 

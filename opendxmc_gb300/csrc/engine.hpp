@@ -148,7 +148,6 @@ struct LaunchShape {
     int refill_batch = 0;   // dead lanes a warp gathers before starting new histories (0: default)
     int interact_batch = 0; // parked lanes a warp gathers before running scatterings (0: default)
     int woodcock_steps = 0; // Woodcock steps per lane and step phase (0: default)
-    int step_min_lanes = 0; // a step phase ends once fewer lanes than this still step (0: off)
 };
 
 // kernels (transport.cu)

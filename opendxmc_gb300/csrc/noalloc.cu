@@ -264,7 +264,6 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     shape.interact_batch = std::min(32, std::max(0, o.interact_batch));
     shape.refill_batch = std::min(32, std::max(0, o.refill_batch));
     shape.woodcock_steps = std::min(64, std::max(0, o.woodcock_steps));
-    shape.step_min_lanes = std::min(32, std::max(0, o.step_min_lanes));
 
     const auto t0 = std::chrono::steady_clock::now();
     cudaError_t le = cudaSuccess;

@@ -297,7 +297,7 @@ namespace {
     template <int TRACKING, bool PACKED, bool MULTI>
     __global__ void __launch_bounds__(256) transportKernel(const DevJob J0, const DevJob* __restrict__ jobs,
         const unsigned long long* __restrict__ offsets, int nJobs, unsigned long long h_end,
-        DevCounters* __restrict__ ctr, int refillBatch, int interactBatch, int woodcockSteps, int stepMinLanes)
+        DevCounters* __restrict__ ctr, int refillBatch, int interactBatch, int woodcockSteps)
     {
         int jid = 0;
         // event counters per warp (no block-wide barrier: warps finish independently)
@@ -474,7 +474,6 @@ namespace {
 
             // ---- step
             bool photo = false, first = false, error = false;
-            const unsigned stepMask = __ballot_sync(kFull, st == kStepping);
             if (st == kStepping) {
                 bool escaped = false;
                 uint32_t v = 0;
@@ -482,21 +481,12 @@ namespace {
                 bool real = false;
                 if (TRACKING == DXMCG_TRACK_WOODCOCK) {
                     // several steps per phase: most are virtual, and each phase boundary
-                    // costs the warp its votes; a lane stops at a real collision or escape.
-                    // The phase ends for all its lanes after woodcockSteps steps, or as soon
-                    // as fewer than stepMinLanes of them are still stepping (the others
-                    // would only wait): those keep their photon and go on next iteration.
-                    bool going = true;
+                    // costs the warp its votes; a lane stops at a real collision or escape
                     for (int k = 0;;) {
-                        if (going) {
-                            real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits, skipped);
-                            going = !(real || escaped);
-                            if (going)
-                                ++steps;
-                        }
-                        const unsigned still = __ballot_sync(stepMask, going);
-                        if (++k >= woodcockSteps || still == 0u || __popc(still) < stepMinLanes)
+                        real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits, skipped);
+                        if (real || escaped || ++k >= woodcockSteps)
                             break;
+                        ++steps;
                     }
                 } else if (TRACKING == DXMCG_TRACK_SIDDON)
                     real = siddonFlight<PACKED>(J, ph, rng, ec, escaped, v, m, visits);
@@ -591,7 +581,7 @@ namespace {
 
 namespace {
     using TransportFn = void (*)(const DevJob, const DevJob*, const unsigned long long*, int, unsigned long long,
-        DevCounters*, int, int, int, int);
+        DevCounters*, int, int, int);
 
     // kernel instance for a tracking mode on the packed (world) or unpacked
     // (caller-owned arrays) voxel layout, single job or a batch of jobs;
@@ -629,9 +619,7 @@ namespace {
         const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
         const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
         const int wsteps = shape.woodcock_steps > 0 ? shape.woodcock_steps : 16;
-        const int minLanes = shape.step_min_lanes > 0 ? std::min(shape.step_min_lanes, 32) : 0;
-        fn<<<shape.grid, shape.block, 0, s>>>(job, jobs, offsets, nJobs, h_end, ctr, refill, interact, wsteps,
-            minLanes);
+        fn<<<shape.grid, shape.block, 0, s>>>(job, jobs, offsets, nJobs, h_end, ctr, refill, interact, wsteps);
         return cudaGetLastError();
     }
 

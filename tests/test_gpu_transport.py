@@ -116,25 +116,6 @@ def test_level2_impulse_approximation_and_fluorescence(gpu, oracle):
     assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
 
 
-@pytest.mark.parametrize("min_lanes", [6, 16, 32])
-def test_step_phase_early_exit_keeps_every_history(c1, gpu, min_lanes):
-    """Ending a warp's step phase once fewer than min_lanes lanes still step only
-    changes when each lane's steps run, not what it draws."""
-    ph, gw, _ = c1
-    beam = P.dx_beam_params(particles=100_000, exposures=10)
-    gw.clear()
-    s1 = gw.run(beam, gpu.run_options(seed=3, stream=1))
-    e1, q1, n1 = gw.tally()
-    gw.clear()
-    s2 = gw.run(beam, gpu.run_options(seed=3, stream=1, step_min_lanes=min_lanes))
-    e2, q2, n2 = gw.tally()
-    for k in ("n_histories", "n_visits", "n_photo", "n_compton", "n_rayleigh", "n_cutoff", "n_interacted"):
-        assert s1[k] == s2[k], k
-    np.testing.assert_array_equal(n1, n2)
-    np.testing.assert_allclose(e2, e1, rtol=1e-12, atol=0)
-    np.testing.assert_allclose(q2, q1, rtol=1e-12, atol=0)
-
-
 @pytest.mark.parametrize("steps", [2, 5])
 def test_woodcock_steps_per_phase_keep_every_history(c1, gpu, steps):
     """Several Woodcock steps per step phase change only when a lane's work runs,

@@ -44,8 +44,9 @@ WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 material
 # 1-pass ncu capture of the launch list.  bench.py's launches hold up to 2^26
 # histories, 0.2 % more than the captured one.
 TRAFFIC_BYTES_PER_LAUNCH = 3.61e9
-# the same for a full launch of the 512x512x400 workload (--workload torso512); None until captured
-TRAFFIC_BYTES_PER_LAUNCH_512 = None
+# the same for a full launch of the 512x512x400 workload (--workload torso512, gather skip
+# on): 67,000,050 histories, 10.79 GB read + 2.79 GB written
+TRAFFIC_BYTES_PER_LAUNCH_512 = 13.58e9
 
 
 def parse():

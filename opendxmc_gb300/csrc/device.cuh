@@ -222,6 +222,21 @@ namespace dev {
         return E;
     }
 
+    // 1 - (1 + x)^-3 = x (3 + x (3 + x)) / (1 + x)^3 for x = T / a >= 0: the form factor
+    // integral of an element, without the cancellation of 1 - 1/b^3 at small x and
+    // without transcendental functions (a few ulps in FP32).
+    __device__ __forceinline__ float formFactorIntegral(float x)
+    {
+        const float b = 1.0f + x;
+        return x * fmaf(x, 3.0f + x, 3.0f) * __frcp_rn(b * b * b);
+    }
+
+    // Rayleigh scattering: element i with probability n_i Z_i^2 a_i c_i(T), then
+    // t = x^2 from F^2 by inversion, t = a ((1 - y)^(-1/3) - 1) with y = r2 c_i, and
+    // rejection on (1 + cos^2) / 2.  The inversion is evaluated as
+    // a y / (om (s^2 + s + 1)) with om = 1 - y and s = om^(-1/3): that is a (s - 1), since
+    // s^3 - 1 = y / om, with no cancellation when y is small.  For y >= 1/2, om is formed
+    // as (1 - r2) + r2 (1 + T/a)^-3 (1 - r2 is exact) so FP32 keeps its precision.
     template <class U>
     __device__ float sampleRayleigh(float E, const DevMaterial* __restrict__ M, U& r, unsigned& err)
     {
@@ -229,31 +244,30 @@ namespace dev {
         const float T = q * q;
         const int n = M->n;
         float Gs = 0.0f;
-        for (int i = 0; i < n; ++i) {
-            const float a = __ldg(&M->a[i]);
-            Gs += __ldg(&M->nZ2[i]) * a * (-expm1f(-3.0f * log1pf(T / a)));
-        }
+        for (int i = 0; i < n; ++i)
+            Gs += __ldg(&M->nZ2[i]) * __ldg(&M->a[i]) * formFactorIntegral(T * __ldg(&M->ia[i]));
         for (int guard = 0; guard < kMaxRejections; ++guard) {
             const float r1 = r.u(), r2 = r.u(), r3 = r.u();
             const float target = r1 * Gs;
-            float acc = 0.0f, a = 0.0f, c = 0.0f;
+            float acc = 0.0f, a = 0.0f, ia = 0.0f, c = 0.0f;
             for (int i = 0; i < n; ++i) {
                 a = __ldg(&M->a[i]);
-                c = -expm1f(-3.0f * log1pf(T / a));
+                ia = __ldg(&M->ia[i]);
+                c = formFactorIntegral(T * ia);
                 acc += __ldg(&M->nZ2[i]) * a * c;
                 if (target <= acc)
                     break;
             }
-            // t = a ((1 - y)^(-1/3) - 1), y = r2 c.  For y >= 1/2, 1 - y is formed as
-            // (1 - r2) + r2 (1 + T/a)^-3 (1 - r2 is exact) so FP32 keeps its precision.
             const float y = r2 * c;
-            float t;
+            float om;
             if (y < 0.5f) {
-                t = a * expm1f(-log1pf(-y) / 3.0f);
+                om = 1.0f - y;
             } else {
-                const float omy = (1.0f - r2) + r2 * expf(-3.0f * log1pf(T / a));
-                t = a * expm1f(-logf(omy) / 3.0f);
+                const float b = 1.0f + T * ia;
+                om = (1.0f - r2) + r2 * __frcp_rn(b * b * b);
             }
+            const float sr = rcbrtf(om);
+            const float t = a * y * __frcp_rn(om * fmaf(sr, sr + 1.0f, 1.0f));
             const float mu = 1.0f - 2.0f * t / T;
             if (2.0f * r3 <= 1.0f + mu * mu)
                 return mu;

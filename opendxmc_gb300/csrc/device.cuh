@@ -171,9 +171,24 @@ namespace dev {
         return false;
     }
 
+    // S(t) / Z_sum from the material's table (linear in log2 t; proportional to t below
+    // the first node, whose value is stab[0])
+    __device__ __forceinline__ float comptonS(const float* __restrict__ stab, float t)
+    {
+        const float x = (__log2f(t) - static_cast<float>(kSTabMinLog2)) * static_cast<float>(kSTabPerOctave);
+        if (!(x > 0.0f))
+            return __ldg(stab) * t * 65536.0f; // t / 2^kSTabMinLog2
+        const float xc = fminf(x, static_cast<float>(kSTabN - 1));
+        const int i = min(static_cast<int>(xc), kSTabN - 2);
+        const float f = xc - static_cast<float>(i);
+        const float a = __ldg(stab + i);
+        const float b = __ldg(stab + i + 1);
+        return fmaf(f, b - a, a);
+    }
+
     template <class U>
-    __device__ float sampleCompton(float E, const DevMaterial* __restrict__ M, int correction, U& r, float& cost,
-        unsigned& err)
+    __device__ float sampleCompton(float E, const DevMaterial* __restrict__ M, const float* __restrict__ stab,
+        int correction, U& r, float& cost, unsigned& err)
     {
         const float k = E / kMeKeV;
         const float kk = 2.0f * k;
@@ -197,15 +212,8 @@ namespace dev {
             if (correction >= 1) {
                 const float q = E * kInvHc;
                 const float t = q * q * 0.5f * omu;
-                const int n = M->n;
-                float S = 0.0f;
-                for (int i = 0; i < n; ++i) {
-                    const float b = fmaf(t, __ldg(&M->ia[i]), 1.0f);
-                    const float b2 = b * b;
-                    S += __ldg(&M->nZ[i]) * (1.0f - __frcp_rn(b2 * b2));
-                }
                 const float r4 = r.u();
-                if (r4 * __ldg(&M->Zsum) > S)
+                if (r4 > comptonS(stab, t))
                     continue;
             }
             cost = 1.0f - omu;

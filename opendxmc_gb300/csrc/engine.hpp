@@ -28,6 +28,13 @@ constexpr int kMaxBowtie = 64;
 constexpr int kTableNE = DXMCG_NE;
 constexpr uint32_t kMaxStepsPerHistory = 1000000;
 constexpr int kMaxRejections = 100000;
+// Compton rejection on the incoherent scattering function: per material S(t) / Z_sum
+// at t = 2^(kSTabMinLog2 + i / kSTabPerOctave) 1/A^2 (t = x^2 = q^2 (1 - cos) / 2),
+// i = 0 .. kSTabN - 1, interpolated linearly in log2 t; S is proportional to t below
+// the first node.  24 octaves reach t = 256, beyond q^2 = 147 at 150.5 keV.
+constexpr int kSTabPerOctave = 32;
+constexpr int kSTabMinLog2 = -16;
+constexpr int kSTabN = 24 * kSTabPerOctave + 1;
 
 struct DevMaterial {
     int n;
@@ -97,6 +104,7 @@ struct DevJob {
     const float4* xs;
     const float* maj;
     const DevMaterial* mats;
+    const float* stab; // [n_mats][kSTabN] S(t) / Z_sum of each material
     int n_mats;
     int correction;
     Tally* tally;
@@ -167,8 +175,8 @@ cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, do
 cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int ny, int nz, float sx, float sy,
     float sz, int cap, long long* idx, float* len, int* cnt, cudaStream_t s);
 cudaError_t launchPhilox(int n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t s);
-cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, int correction, const float* u,
-    int stride, float* e_out, float* cos_out, int* used, cudaStream_t s);
+cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, const float* stab, int correction,
+    const float* u, int stride, float* e_out, float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const float* u, int stride, float* e_out,
     float* dz_out, int* used, cudaStream_t s);
 // tcgen05 interface self-test (conv_tc.cu): D0 = A (B0 + B1)^T, D1 = A B1^T, A 128 x 16,

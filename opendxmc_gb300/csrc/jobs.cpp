@@ -126,6 +126,23 @@ DevMaterial toDevMaterial(const dxmcg_material& m)
     return d;
 }
 
+void buildComptonTables(const dxmcg_material* mats, int M, float* out)
+{
+    for (int m = 0; m < M; ++m) {
+        const auto s = samplingElements(mats[m]);
+        for (int k = 0; k < kSTabN; ++k) {
+            const double t = std::exp2(kSTabMinLog2 + static_cast<double>(k) / kSTabPerOctave);
+            double S = 0.0;
+            for (int i = 0; i < s.n; ++i) {
+                const double b = 1.0 + t / s.a[i];
+                const double b2 = b * b;
+                S += s.nZ[i] * (1.0 - 1.0 / (b2 * b2));
+            }
+            out[static_cast<size_t>(m) * kSTabN + k] = static_cast<float>(s.Zsum > 0 ? S / s.Zsum : 0.0);
+        }
+    }
+}
+
 void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const double* rhoMax, float* tot,
     float4* xs, float* maj, DevMaterial* dm)
 {

@@ -39,4 +39,9 @@ void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const 
 
 DevMaterial toDevMaterial(const dxmcg_material& m);
 
+// S(t) / Z_sum of each of the M materials on the kSTabN-point table (out: M x kSTabN),
+// from the same per-element incoherent scattering functions the samplers restate:
+// S = sum_i n_i Z_i (1 - (1 + t / a_i)^-4).
+void buildComptonTables(const dxmcg_material* mats, int M, float* out);
+
 } // namespace dxmcg

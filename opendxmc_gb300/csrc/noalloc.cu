@@ -7,8 +7,8 @@
 // between its set-up phase and its runs.  They own every input and output array
 // and pass device pointers; everything else this path needs -- the work-queue head
 // and run statistics, the validation flags and per-material maximum densities,
-// the attenuation tables and majorant, the exposure list, the spectra and the
-// bowtie profile -- lives in one file-scope __device__ array of
+// the attenuation tables and majorant, the Compton S(t) tables, the exposure list,
+// the spectra and the bowtie profiles -- lives in one file-scope __device__ array of
 // kScratchBytes = 512 KiB.  Every GPU that loads the library holds that array
 // until the process exits.
 //
@@ -59,7 +59,8 @@ namespace {
     constexpr size_t kOffTot = alignUp(kOffMaj + kTableNE * sizeof(float));
     constexpr size_t kOffXs = alignUp(kOffTot + kMaxMaterials * kTableNE * sizeof(float));
     constexpr size_t kOffExps = alignUp(kOffXs + kMaxMaterials * kTableNE * sizeof(float4));
-    constexpr size_t kUsed = kOffExps + kMaxExposures * sizeof(DevExposure);
+    constexpr size_t kOffSTab = alignUp(kOffExps + kMaxExposures * sizeof(DevExposure));
+    constexpr size_t kUsed = kOffSTab + kMaxMaterials * kSTabN * sizeof(float);
     static_assert(kUsed <= kScratchBytes, "scratch layout exceeds the static array");
     static_assert(sizeof(dxmcg_tally_record) == sizeof(Tally), "tally record layout");
 
@@ -228,6 +229,9 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     buildDeviceTables(materials, n_materials, correction, rhoMax, tot.data(), xs.data(), maj.data(), dm.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffTot, tot.data(), tot.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffXs, xs.data(), xs.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
+    std::vector<float> stab(static_cast<size_t>(n_materials) * kSTabN);
+    buildComptonTables(materials, n_materials, stab.data());
+    NOALLOC_CUDA(cudaMemcpyAsync(base + kOffSTab, stab.data(), stab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMaj, maj.data(), maj.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMats, dm.data(), dm.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffExps, hj.exposures.data(), hj.exposures.size() * sizeof(DevExposure),
@@ -250,6 +254,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     J.mat = device_material;
     J.tot = reinterpret_cast<const float*>(base + kOffTot);
     J.xs = reinterpret_cast<const float4*>(base + kOffXs);
+    J.stab = reinterpret_cast<const float*>(base + kOffSTab);
     J.maj = reinterpret_cast<const float*>(base + kOffMaj);
     J.mats = reinterpret_cast<const DevMaterial*>(base + kOffMats);
     J.tally = reinterpret_cast<Tally*>(device_tally);

@@ -404,7 +404,7 @@ namespace {
                 // the samplers diverge; the direction update they share runs once
                 float cost = 1.0f, Ep = ph.E;
                 if (compton)
-                    Ep = sampleCompton(ph.E, J.mats + pm, J.correction, rng, cost, err);
+                    Ep = sampleCompton(ph.E, J.mats + pm, J.stab + pm * kSTabN, J.correction, rng, cost, err);
                 else if (rayleigh)
                     cost = sampleRayleigh(ph.E, J.mats + pm, rng, err);
                 if (compton || rayleigh)

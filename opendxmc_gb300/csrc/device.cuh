@@ -190,7 +190,10 @@ namespace dev {
     __device__ float sampleCompton(float E, const DevMaterial* __restrict__ M, const float* __restrict__ stab,
         int correction, U& r, float& cost, unsigned& err)
     {
-        const float k = E / kMeKeV;
+        // reciprocals instead of IEEE divisions (a unit in the last place at most apart;
+        // the rejection tests are insensitive to it)
+        const float k = E * (1.0f / kMeKeV);
+        const float ik = __frcp_rn(k);
         const float kk = 2.0f * k;
         for (int guard = 0; guard < kMaxRejections; ++guard) {
             const float r1 = r.u(), r2 = r.u(), r3 = r.u();
@@ -201,14 +204,14 @@ namespace dev {
                 const float x = 1.0f + xm1;
                 acc = r3 * x * x <= 4.0f * xm1;
             } else {
-                xm1 = kk * (1.0f - r2) / (1.0f + kk * r2);
+                xm1 = kk * (1.0f - r2) * __frcp_rn(fmaf(kk, r2, 1.0f));
                 const float x = 1.0f + xm1;
-                const float mu = 1.0f - xm1 / k;
+                const float mu = 1.0f - xm1 * ik;
                 acc = 2.0f * r3 <= mu * mu + 1.0f / x;
             }
             if (!acc)
                 continue;
-            const float omu = xm1 / k;
+            const float omu = xm1 * ik;
             if (correction >= 1) {
                 const float q = E * kInvHc;
                 const float t = q * q * 0.5f * omu;
@@ -223,7 +226,7 @@ namespace dev {
                     continue;
                 return Ep;
             }
-            return E / (1.0f + xm1);
+            return E * __frcp_rn(1.0f + xm1);
         }
         err |= kErrRejectLimit;
         cost = 1.0f;
@@ -553,7 +556,7 @@ namespace dev {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             if (d[a] != 0.0f) {
-                const float inv = 1.0f / d[a];
+                const float inv = __frcp_rn(d[a]); // the correctly rounded 1 / d, as a division gives
                 float t1 = (0.0f - p[a]) * inv, t2 = (J.L[a] - p[a]) * inv;
                 if (t1 > t2) {
                     const float tt = t1;

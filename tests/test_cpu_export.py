@@ -93,3 +93,61 @@ def test_hdf5_file_where_h5py_exists(tmp_path):
         assert f["dosearray"].shape == (3, 2, 2)
         np.testing.assert_array_equal(f["dosearray"][...].reshape(-1), np.arange(12.0))
         assert f["beams/CBCTBeams/1"].attrs["DAPvalue"] == 800.0
+
+
+def test_study_round_trip_through_the_archive(engine, tmp_path):
+    """A study written with save_npz and read with load_study gives back the arrays,
+    the material compositions and beams that expand to the same exposures (the loader
+    is HDF5Wrapper::load's counterpart, hdf5wrapper.cpp:1070-1207)."""
+    ph = P.water_cylinder_phantom(dims=(16, 12, 8), spacing=(0.5, 0.6, 0.7))
+    rng = np.random.default_rng(2)
+    dose = rng.uniform(0, 1, ph.material.shape)
+    beams = [
+        dict(P.dx_beam_params(particles=10, exposures=3), rotation_center=[0.0, 0.0, 0.0],
+             source_center_distance=100.0, primary_angle=0.0, secondary_angle=0.0, sdd_cm=110.0, dap_mgycm2=5.0),
+        dict(P.dx_beam_params(particles=20, exposures=2), rotation_center=[1.0, -2.0, 3.0],
+             source_center_distance=80.0, primary_angle=30.0, secondary_angle=-20.0, sdd_cm=100.0),
+        P.ct_spiral_params(particles=7, scan_cm=6.0),
+        dict(P.ct_spiral_params(particles=7, scan_cm=6.0), organ_aec=1, organ_aec_start_deg=30.0,
+             organ_aec_stop_deg=150.0, organ_aec_ramp_deg=20.0, organ_aec_low_weight=0.6),
+        P.ct_sequential_params(particles=5),
+        P.cbct_params(particles=9),
+        P.ct_dual_energy_params(particles=3, scan_cm=4.0, tube_a_weight=0.3),
+    ]
+    # the DX poses as a caller's DXBeam would have them
+    for b in beams[:2]:
+        b["position"], b["cosines"] = X._dx_pose(b["rotation_center"], b["source_center_distance"],
+                                                 b["primary_angle"], b["secondary_angle"])
+    tree = X.study_entries(ph.dims, ph.spacing, density=ph.density, material=ph.material, materials=ph.materials,
+                           material_names=ph.names, dose=dose, variance=dose * 0.1, count=np.round(dose * 100),
+                           beams=beams)
+    X.save_npz(tmp_path / "study.npz", tree)
+    st = X.load_study(tmp_path / "study.npz")
+    assert st["dims"] == tuple(ph.dims) and st["spacing"] == pytest.approx(ph.spacing)
+    np.testing.assert_array_equal(st["density"], ph.density)
+    np.testing.assert_array_equal(st["material"], ph.material)
+    np.testing.assert_array_equal(st["dose"], dose)
+    assert st["material_names"] == ph.names
+    for got, want in zip(st["materials"], ph.materials):
+        assert set(got) == set(want)
+        s_got, s_want = sum(got.values()), sum(want.values())
+        for z in want:
+            assert got[z] / s_got == pytest.approx(want[z] / s_want, abs=1e-6)
+    assert len(st["beams"]) == len(beams)
+    # group order is DX, spiral, sequential, CBCT, dual energy; beams are listed that way
+    for got, want in zip(st["beams"], beams):
+        assert got["type"] == want["type"]
+        pose = ("rotation_center", "source_center_distance", "primary_angle", "secondary_angle")
+        e1 = engine.beam_exposures({k: v for k, v in want.items() if k not in pose})
+        e2 = engine.beam_exposures({k: v for k, v in got.items() if k not in pose})
+        assert len(e1) == len(e2)
+        for a, b in zip(e1, e2):
+            for k in ("pos", "c0", "c1", "half"):
+                np.testing.assert_allclose(b[k], a[k], rtol=1e-9, atol=1e-9, err_msg=k)
+            assert b["weight"] == pytest.approx(a["weight"], rel=1e-9)
+            assert b["tube"] == a["tube"]
+        assert got["particles_per_exposure"] == want["particles_per_exposure"]
+        for k in ("kvp", "kvp_b", "pitch", "collimation_cm", "sdd_cm", "tube_a_weight"):
+            if k in want:
+                assert got[k] == pytest.approx(want[k]), k
+        assert got["filters"] == {int(z): float(v) for z, v in want["filters"].items()}

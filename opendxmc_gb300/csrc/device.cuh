@@ -491,14 +491,15 @@ namespace dev {
             return w[0];
         if (a >= ang[n - 1])
             return w[n - 1];
-        int lo = 0, hi = n - 1;
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (ang[mid] <= a)
-                lo = mid;
-            else
-                hi = mid;
-        }
+        // the segment with ang[lo] <= a < ang[lo + 1], from the cell's entry (the two
+        // scans correct a cell misplaced by the rounding of a * cellScale)
+        const int c = min(static_cast<int>(a * b->cellScale[tube]), kBowtieCells - 1);
+        int lo = b->seg[tube][c];
+        while (lo > 0 && ang[lo] > a)
+            --lo;
+        while (ang[lo + 1] <= a)
+            ++lo;
+        const int hi = lo + 1;
         const float t = (a - ang[lo]) / (ang[hi] - ang[lo]);
         return w[lo] + t * (w[hi] - w[lo]);
     }
@@ -515,8 +516,11 @@ namespace dev {
     // photon at its source position (grid-local).
     __device__ __forceinline__ void sampleSource(const DevJob& J, unsigned long long h, Photon& ph, Rng& r)
     {
-        const DevExposure* __restrict__ ex = J.exps + exposureOf(J, h);
-        const int tube = ex->tube;
+        // the 64-byte exposure record as four 16-byte loads: (pos, c0.x), (c0.y, c0.z,
+        // c1.x, c1.y), (c1.z, n), (half, weight, tube)
+        const float4* __restrict__ ex4 = reinterpret_cast<const float4*>(J.exps + exposureOf(J, h));
+        const float4 q3 = __ldg(ex4 + 3);
+        const int tube = __float_as_int(q3.w);
         if (J.beam_type == DXMCG_BEAM_PENCIL) {
             (void)r.raw();
             (void)r.raw();
@@ -530,18 +534,19 @@ namespace dev {
             k = x1 < __ldg(&S->thr[k]) ? k : __ldg(&S->alias[k]);
             ph.E = __ldg(&S->E[k]);
         }
-        const float ax = (2.0f * r.u() - 1.0f) * ex->half[0];
-        const float ay = (2.0f * r.u() - 1.0f) * ex->half[1];
+        const float ax = (2.0f * r.u() - 1.0f) * q3.x;
+        const float ay = (2.0f * r.u() - 1.0f) * q3.y;
         // |angle| < pi/2: the hardware sine is within 2^-21.4
         const float sx = __sinf(ax), sy = __sinf(ay);
         const float sz = sqrtf(fmaxf(0.0f, 1.0f - sx * sx - sy * sy));
-        ph.dx = ex->c0[0] * sx + ex->c1[0] * sy + ex->n[0] * sz;
-        ph.dy = ex->c0[1] * sx + ex->c1[1] * sy + ex->n[1] * sz;
-        ph.dz = ex->c0[2] * sx + ex->c1[2] * sy + ex->n[2] * sz;
-        ph.px = ex->pos[0];
-        ph.py = ex->pos[1];
-        ph.pz = ex->pos[2];
-        float w = ex->weight;
+        const float4 q0 = __ldg(ex4), q1 = __ldg(ex4 + 1), q2 = __ldg(ex4 + 2);
+        ph.dx = q0.w * sx + q1.z * sy + q2.y * sz;
+        ph.dy = q1.x * sx + q1.w * sy + q2.z * sz;
+        ph.dz = q1.y * sx + q2.x * sy + q2.w * sz;
+        ph.px = q0.x;
+        ph.py = q0.y;
+        ph.pz = q0.z;
+        float w = q3.z;
         if (J.bowtie)
             w *= bowtieAt(J.bowtie, tube, fabsf(ax)) * J.bowtie->inv_norm[tube];
         ph.w = w;

@@ -67,6 +67,8 @@ struct alignas(16) DevExposure {
     int tube;
 };
 
+static_assert(sizeof(DevExposure) == 64, "the source sampler reads an exposure as four float4");
+
 struct DevSpectrum {
     int n;
     float E[kMaxSpectrum];
@@ -75,12 +77,17 @@ struct DevSpectrum {
 };
 
 // One bowtie profile per tube (tube 1: dual-energy tube B); n[t] = 0 leaves that
-// tube's weights at 1 (and inv_norm[t] = 1).
+// tube's weights at 1 (and inv_norm[t] = 1).  seg[t][c] is a segment near the angles
+// of cell c of kBowtieCells equal cells over [0, ang[t][n-1]] (cellScale = cells per
+// radian): the lookup starts there instead of a binary search.
+constexpr int kBowtieCells = 256;
 struct DevBowtie {
     int n[2];
     float ang[2][kMaxBowtie];
     float w[2][kMaxBowtie];
     float inv_norm[2];
+    float cellScale[2];
+    uint8_t seg[2][kBowtieCells];
 };
 
 struct alignas(32) Tally {

@@ -274,6 +274,16 @@ int buildHostJob(const dxmcg_beam& b, const int32_t dims[3], const double spacin
             }
         const double m = prof.mean(half);
         db.inv_norm[t] = static_cast<float>(m > 0 ? 1.0 / m : 1.0);
+        // segment index: for each cell the last segment starting at or before the cell
+        const double amax = db.ang[t][n - 1];
+        db.cellScale[t] = amax > 0 ? static_cast<float>(kBowtieCells / amax) : 0.0f;
+        for (int c = 0; c < kBowtieCells; ++c) {
+            const double a0 = amax * c / kBowtieCells;
+            int k = 0;
+            while (k + 1 < n - 1 && db.ang[t][k + 1] <= a0)
+                ++k;
+            db.seg[t][c] = static_cast<uint8_t>(k);
+        }
         out.hasBowtie = true;
     }
     return DXMCG_OK;

@@ -83,6 +83,8 @@ def parse():
     p.add_argument("--save-weights", default="", help="denoise-experiment: write the trained parameters (.npy)")
     p.add_argument("--train-steps", type=int, default=0, help="denoise-experiment: training steps (0: default)")
     p.add_argument("--lr-final", type=float, default=0.0, help="denoise-experiment: final learning rate (0: default)")
+    p.add_argument("--init-seeds", default="", help="denoise-experiment: initialisations to train, comma-separated; "
+                   "the one best on a validation torso is kept (default: 0)")
     p.add_argument("--lows", default="", help="denoise-experiment: input history counts, comma-separated "
                    "(default 3e7,1e8,3e8,1e9)")
     p.add_argument("--workload", choices=["torso", "torso512", "c1", "batch", "pipelines", "denoiser",
@@ -789,6 +791,8 @@ def run_denoise_experiment(args):
         kw["lr_final"] = args.lr_final
     if args.lows:
         kw["lows"] = tuple(float(v) for v in args.lows.split(","))
+    if args.init_seeds:
+        kw["init_seeds"] = tuple(int(v) for v in args.init_seeds.split(","))
     out, net = DN.experiment(torch, log=lambda m: print(m, file=sys.stderr, flush=True), **kw)
     if args.save_weights:
         np.save(args.save_weights, net.get_params())

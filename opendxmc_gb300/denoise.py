@@ -339,14 +339,20 @@ def run_dose(world, beam, seed, stream, air):
 
 def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_seeds=(11, 12, 13, 14, 15, 16),
                eval_seed=99, lows=(3e7, 1e8, 3e8, 1e9), high=1e10, steps=16000, batch=8, patch=64, lr=1e-3,
-               lr_final=5e-5, channels=(16, 32, 64, 128), target_error=0.02, log=print):
+               lr_final=5e-5, channels=(16, 32, 64, 128), target_error=0.02, init_seeds=(0,), val_seed=97,
+               log=print):
     """Train the denoiser on torso phantoms (inputs: runs of each history count in
     `lows`; target: a `high`-history run), then, on a held-out torso, compare the
     time to `target_error` of plain Monte Carlo with that of a short run plus
     denoising, for each input history count.  Error: RMS relative error over
     non-air voxels above 10 % of the maximum dose, made unbiased by two independent
     `high`-history references; plain Monte Carlo's error at N histories is one
-    reference's own noise scaled by sqrt(high / N)."""
+    reference's own noise scaled by sqrt(high / N).
+
+    With several `init_seeds` one network is trained from each initialisation and the
+    one with the lowest error at the smallest input (then the next) on a validation
+    torso (`val_seed`, neither a training nor the evaluation torso) is kept: the
+    evaluation torso plays no part in the choice."""
     from . import phantoms as P
 
     nx, ny, nz = dims
@@ -374,14 +380,46 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
         log(f"phantom {s}: {len(lows)} inputs, target {high:.3g} histories, scale {pairs[-1].scale:.4g}")
     t_data = time.perf_counter() - t0
 
-    net = G.Denoiser(channels, seed=0)
     sampler = PatchSampler(torch, pairs, patch, batch, seed=1, centers=centers)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    losses = train(net, sampler, steps, lr=lr, lr_final=lr_final, log_every=max(1, steps // 10), log=log)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t0
+    candidates = []
+    t_train = 0.0
+    for init in init_seeds:
+        cand = G.Denoiser(channels, seed=init)
+        sampler.rng = np.random.default_rng(1)  # every candidate sees the same patches
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cand_losses = train(cand, sampler, steps, lr=lr, lr_final=lr_final, log_every=max(1, steps // 10), log=log)
+        torch.cuda.synchronize()
+        t_train += time.perf_counter() - t0
+        candidates.append((cand, cand_losses))
     del sampler, pairs
+
+    validation = []
+    if len(candidates) > 1:
+        ph = P.torso_phantom(dims=dims, spacing=spacing, seed=val_seed)
+        world.set_data(ph.density, ph.material)
+        world.build()
+        _, mat = world.packed_density()
+        air = mat == 0
+        v1, _ = run_dose(world, beam_high, val_seed, 2, air)
+        v2, _ = run_dose(world, beam_high, val_seed, 3, air)
+        scorer = Scorer(v1, v2, ~air)
+        for k, low in enumerate(lows):
+            run_dose(world, spiral_beam(low), val_seed, 20 + k, air)
+            errs = []
+            for cand, _ in candidates:
+                d_dn, _ = cand.denoise_world(world)
+                d_dn[air] = 0.0
+                errs.append(scorer(d_dn * (high / low))["rms_rel"])
+            validation.append(errs)
+        for i, init in enumerate(init_seeds):
+            log(f"candidate {init}: validation RMS " + ", ".join(f"{v[i]:.4f}" for v in validation))
+    order = sorted(range(len(candidates)), key=lambda i: tuple(v[i] for v in validation))
+    best = order[0]
+    net, losses = candidates[best]
+    for i, (cand, _) in enumerate(candidates):
+        if i != best:
+            cand.close()
 
     # held-out torso
     ph = P.torso_phantom(dims=dims, spacing=spacing, seed=eval_seed)
@@ -425,6 +463,8 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
         "dims": list(dims), "spacing_cm": list(spacing), "train_phantoms": len(train_seeds), "inputs": list(lows),
         "high": high, "train_steps": steps, "batch": batch, "patch": patch,
         "final_loss": float(np.mean(losses[-10:])), "data_s": t_data, "data_mc_s": mc_s, "train_s": t_train,
+        "init_seeds": list(init_seeds), "chosen_init_seed": init_seeds[best], "validation_seed": val_seed,
+        "validation_rms_rel": validation,
         "histories_per_s": rate, "reference_rms_rel": sigma_ref, "target_error": target_error,
         "plain_histories_to_target": n_plain, "plain_s_to_target": t_plain, "levels": levels,
         "denoised_s_to_target": best["total_s"] if best else None,

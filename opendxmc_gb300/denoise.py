@@ -415,10 +415,10 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
         for i, init in enumerate(init_seeds):
             log(f"candidate {init}: validation RMS " + ", ".join(f"{v[i]:.4f}" for v in validation))
     order = sorted(range(len(candidates)), key=lambda i: tuple(v[i] for v in validation))
-    best = order[0]
-    net, losses = candidates[best]
+    chosen = order[0]
+    net, losses = candidates[chosen]
     for i, (cand, _) in enumerate(candidates):
-        if i != best:
+        if i != chosen:
             cand.close()
 
     # held-out torso
@@ -463,7 +463,7 @@ def experiment(torch, dims=(512, 512, 400), spacing=(0.08, 0.08, 0.1), train_see
         "dims": list(dims), "spacing_cm": list(spacing), "train_phantoms": len(train_seeds), "inputs": list(lows),
         "high": high, "train_steps": steps, "batch": batch, "patch": patch,
         "final_loss": float(np.mean(losses[-10:])), "data_s": t_data, "data_mc_s": mc_s, "train_s": t_train,
-        "init_seeds": list(init_seeds), "chosen_init_seed": init_seeds[best], "validation_seed": val_seed,
+        "init_seeds": list(init_seeds), "chosen_init_seed": init_seeds[chosen], "validation_seed": val_seed,
         "validation_rms_rel": validation,
         "histories_per_s": rate, "reference_rms_rel": sigma_ref, "target_error": target_error,
         "plain_histories_to_target": n_plain, "plain_s_to_target": t_plain, "levels": levels,

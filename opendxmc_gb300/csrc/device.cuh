@@ -47,10 +47,13 @@ namespace dev {
         return __fsub_rn(__uint_as_float(0x3f800000u | (x >> 9)), 0.99999994039535522461f);
     }
 
-    // Stream of one history: a xoshiro128** generator (Blackman & Vigna 2018) whose
+    // Stream of one history: a xoshiro128+ generator (Blackman & Vigna 2018) whose
     // 128-bit state is the Philox4x32-10 block at counter (0, stream, h) under the
-    // seed.  One Philox evaluation per history, then ten 32-bit ALU operations per
-    // draw with no data-dependent branch, so lanes stay converged while drawing.
+    // seed.  One Philox evaluation per history, then seven 32-bit ALU operations per
+    // draw with no data-dependent branch, so lanes stay converged while drawing.  Every
+    // draw is used through its top 23 bits (uniforms, alias columns), where the '+'
+    // output (s0 + s3) is as good as the scrambled '**' one; only its lowest bits are
+    // weak, and they are never used.
     struct Rng {
         uint32_t s0, s1, s2, s3;
 
@@ -66,7 +69,7 @@ namespace dev {
         }
         __device__ __forceinline__ uint32_t raw()
         {
-            const uint32_t out = __funnelshift_l(s1 * 5u, s1 * 5u, 7) * 9u;
+            const uint32_t out = s0 + s3;
             const uint32_t t = s1 << 9;
             s2 ^= s0;
             s3 ^= s1;

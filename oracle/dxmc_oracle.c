@@ -686,10 +686,11 @@ void or_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]
 double or_uniform_from_u32(uint32_t x) { return (double)((x >> 9) * 2u + 1u) * (1.0 / 16777216.0); }
 
 /* Draw source: either the stream of one history, or injected uniforms.
- * History h's stream: the 128-bit state of a xoshiro128** generator (Blackman &
- * Vigna, "Scrambled linear pseudorandom number generators", 2018) is the Philox4x32-10
- * block at counter (0, stream, h_lo, h_hi) under key = seed, so every history's
- * draws depend only on (seed, stream, h). */
+ * History h's stream: the 128-bit state of a xoshiro128+ generator (Blackman & Vigna,
+ * "Scrambled linear pseudorandom number generators", 2018; output s0 + s3, of which
+ * only the top 23 bits are ever used) is the Philox4x32-10 block at counter
+ * (0, stream, h_lo, h_hi) under key = seed, so every history's draws depend only on
+ * (seed, stream, h). */
 typedef struct {
     uint32_t s[4];
     const double* inj;
@@ -712,7 +713,7 @@ static inline uint32_t rotl32(uint32_t x, int k) { return (x << k) | (x >> (32 -
 static uint32_t rng_raw(rng_t* r)
 {
     uint32_t* s = r->s;
-    const uint32_t out = rotl32(s[1] * 5u, 7) * 9u;
+    const uint32_t out = s[0] + s[3];
     const uint32_t t = s[1] << 9;
     s[2] ^= s[0];
     s[3] ^= s[1];

@@ -122,14 +122,14 @@ def test_philox_uniforms(oracle):
     assert oracle.lib().or_uniform_from_u32(0xFFFFFFFF) == 1.0 - 2.0 ** -24
 
 
-def _xoshiro128ss(state, n):
-    """Plain-Python xoshiro128** (Blackman & Vigna 2018) for checking the oracle."""
+def _xoshiro128p(state, n):
+    """Plain-Python xoshiro128+ (Blackman & Vigna 2018) for checking the oracle."""
     s = [int(x) for x in state]
     M = 0xFFFFFFFF
     rotl = lambda x, k: ((x << k) | (x >> (32 - k))) & M
     out = []
     for _ in range(n):
-        out.append((rotl((s[1] * 5) & M, 7) * 9) & M)
+        out.append((s[0] + s[3]) & M)
         t = (s[1] << 9) & M
         s[2] ^= s[0]
         s[3] ^= s[1]
@@ -146,7 +146,7 @@ def test_history_streams_are_philox_seeded_xoshiro(oracle):
     for i in range(4):
         h = 2 ** 33 - 2 + i
         state = oracle.philox([0, stream, h & 0xFFFFFFFF, h >> 32], [seed & 0xFFFFFFFF, seed >> 32])
-        assert list(got[i]) == _xoshiro128ss(state, 12)
+        assert list(got[i]) == _xoshiro128p(state, 12)
     # streams of neighbouring histories and stream words differ
     a = oracle.history_stream(1, 0, 0, 2, 8)
     b = oracle.history_stream(1, 1, 0, 1, 8)

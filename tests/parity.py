@@ -38,3 +38,19 @@ def small_cylinder(scale=2):
 def small_torso(scale=4, seed=3):
     return P.torso_phantom(dims=(256 // scale, 256 // scale, 200 // scale),
                            spacing=(0.15 * scale, 0.15 * scale, 0.15 * scale), seed=seed)
+
+
+
+def replicate_totals(world, beam, options_for, k=8):
+    """Runs the whole beam k times on independent streams (options_for(r) -> run
+    options of replicate r) into the world's tally (cleared first) and returns each
+    replicate's deposited energy: their sum is the total of k x the beam's histories,
+    and total_sigma estimates its standard error."""
+    world.clear()
+    return np.array([world.run(beam, options_for(r))["e_deposited"] for r in range(k)])
+
+
+def total_sigma(totals) -> float:
+    """Standard error of the sum of independent, identically distributed totals."""
+    b = np.asarray(totals, dtype=np.float64)
+    return float(np.sqrt(b.size * np.var(b, ddof=1)))

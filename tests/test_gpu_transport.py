@@ -276,19 +276,30 @@ def test_macro_tracking_c2_torso(gpu, oracle):
 
 
 def test_siddon_tracking_matches_woodcock(gpu):
+    """Regular tracking with exact path lengths and Woodcock tracking sample the same
+    transport: per-voxel energy within 3 combined standard errors, and total energy
+    within 4 standard errors of the difference, estimated from eight independent
+    replicates of the beam with each method (at a few 1e5 histories a total scatters
+    by a few 0.1 %, so a fixed relative tolerance would be a coin toss)."""
     ph = parity.small_torso(scale=2)
     gw = gpu_world(gpu, ph)
     beam = P.ct_spiral_params(particles=2000, scan_cm=10.0)
-    s1 = gw.run(beam, gpu.run_options(seed=1, tracking=0))
+    k = 8
+    n = k * len(gpu.beam_exposures(beam)) * beam["particles_per_exposure"]
+    tw = parity.replicate_totals(gw, beam, lambda r: gpu.run_options(seed=1, stream=100 + r, tracking=0), k)
     e1, q1, _ = gw.tally()
-    gw.clear()
-    s2 = gw.run(beam, gpu.run_options(seed=1, stream=9, tracking=1))
+    ts = parity.replicate_totals(gw, beam, lambda r: gpu.run_options(seed=1, stream=200 + r, tracking=1), k)
     e2, q2, _ = gw.tally()
-    n = s1["n_histories"]
     frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
                                                  parity.tally_variance(e2, q2, n))
     assert nvox > 500 and frac >= 0.99
-    assert e1.sum() == pytest.approx(e2.sum(), rel=5e-3)
+    sigma = np.hypot(parity.total_sigma(tw), parity.total_sigma(ts))
+    print(f"Woodcock - Siddon total: {tw.sum() - ts.sum():+.4g} keV, {(tw.sum() - ts.sum()) / sigma:+.2f} sigma "
+          f"({sigma / ts.sum():.2e} relative)")
+    assert abs(tw.sum() - ts.sum()) <= 4.0 * sigma
+    gw.clear()
+    s1 = gw.run(beam, gpu.run_options(seed=1, tracking=0, hist_end=100_000))
+    s2 = gw.run(beam, gpu.run_options(seed=1, stream=9, tracking=1, hist_end=100_000))
     assert s2["n_visits"] > s1["n_visits"]  # exact stepping visits every voxel on the path
 
 

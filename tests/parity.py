@@ -54,3 +54,24 @@ def total_sigma(totals) -> float:
     """Standard error of the sum of independent, identically distributed totals."""
     b = np.asarray(totals, dtype=np.float64)
     return float(np.sqrt(b.size * np.var(b, ddof=1)))
+
+
+def total_tolerance(world, beam, options_for, k=32, n_sigma=4.0) -> float:
+    """Relative tolerance for the difference of two independent runs' totals of one
+    beam: n_sigma standard errors of that difference, sqrt(2) x the spread of a run's
+    deposited energy over k replicate runs on the GPU world (options_for(r) gives
+    replicate r's independent stream).  The world's tally is cleared afterwards."""
+    world.clear()
+    t = np.array([world.run(beam, options_for(r))["e_deposited"] for r in range(k)])
+    world.clear()
+    return float(n_sigma * np.sqrt(2.0) * t.std(ddof=1) / t.mean())
+
+
+def assert_totals_agree(e_gpu, e_oracle, tol, name="", resolve=3e-3):
+    """Total energy imparted of independent GPU and oracle runs: the difference
+    within `tol` (total_tolerance), and `tol` no wider than `resolve`, so the test
+    can see a bias of that size."""
+    rel = float(np.sum(e_gpu) / np.sum(e_oracle) - 1.0)
+    print(f"{name}: total GPU/oracle - 1 = {rel:+.2e}, tolerance {tol:.2e} (4 standard errors)")
+    assert abs(rel) <= tol, (name, rel, tol)
+    assert tol <= resolve, (name, tol)

@@ -7,7 +7,9 @@ beamsettingsmodel.cpp:1581-1612) and the pencil beam's air-kerma calibration
 
 Source sampling is compared photon by photon on shared Philox streams; transport
 with independent streams: per-voxel energy within 3 combined standard errors in
->= 99 % of voxels above 5 % of the maximum, total energy within 0.3 %."""
+>= 99 % of voxels above 5 % of the maximum, total energy within 4 standard errors of
+the difference (the spread of 32 replicate GPU runs), at history counts where that is
+at most 0.3 %."""
 import json
 from pathlib import Path
 
@@ -90,7 +92,7 @@ def test_transport_matches_oracle_independent_streams(gpu, oracle, which):
     gw, ow = worlds(gpu, oracle, ph)
     beam = dict(beams()[which])
     n_exp = len(oracle.beam_exposures(beam))
-    beam["particles_per_exposure"] = int(np.ceil(3_000_000 / n_exp))
+    beam["particles_per_exposure"] = int(np.ceil(20_000_000 / n_exp))
     sg = gw.run(beam, gpu.run_options(seed=8, stream=0))
     so = ow.run(beam, seed=8, stream=1)
     n = sg["n_histories"]
@@ -100,30 +102,31 @@ def test_transport_matches_oracle_independent_streams(gpu, oracle, which):
     e2, q2, _ = ow.tally()
     frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
                                                  parity.tally_variance(e2, q2, n))
-    print(f"{which}: {n} histories, {nvox} voxels above 5 % of max, {frac:.4f} within 3 sigma, "
-          f"total GPU/oracle - 1 = {e1.sum() / e2.sum() - 1:+.2e}")
+    print(f"{which}: {n} histories, {nvox} voxels above 5 % of max, {frac:.4f} within 3 sigma")
     assert nvox > 2000
     assert frac >= 0.99, frac
-    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+    parity.assert_totals_agree(e1, e2, tol, which)
 
 
 def test_dual_energy_second_bowtie_changes_the_dose(gpu, oracle):
     """Two different bowties give a different dose from a shared one, and the oracle
     agrees with the GPU for both: on this torso tube B's own profile (W1 80 kV, flatter
-    than the body bowtie) lowers the energy imparted by about 2 %, some 30 standard
-    errors of the 4.3e6-history totals."""
+    than the body bowtie) lowers the energy imparted by about 2 %, some 40 standard
+    errors of the ratio of the 1.2e7-history totals."""
     ph = parity.small_torso(scale=2, seed=5)
     gw, ow = worlds(gpu, oracle, ph)
     tot = {}
     for name, bb in (("own", W1_80KV), ("shared", P.BODY_BOWTIE)):
-        beam = P.ct_dual_energy_params(particles=10_000, bowtie_b=bb)
+        beam = P.ct_dual_energy_params(particles=27_000, bowtie_b=bb)
         gw.clear()
         ow.clear()
         gw.run(beam, gpu.run_options(seed=4, stream=0))
         ow.run(beam, seed=4, stream=1)
         e1, _, _ = gw.tally()
         e2, _, _ = ow.tally()
-        assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3), name
+        tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+        parity.assert_totals_agree(e1, e2, tol, name)
         tot[name] = (e1.sum(), e2.sum())
     r_gpu = tot["own"][0] / tot["shared"][0]
     r_or = tot["own"][1] / tot["shared"][1]

@@ -4,7 +4,8 @@ FP64 densities (AAVoxelGrid::setData's vector<double>, simulationpipeline.cpp:14
 not the engine's 16-bit-mantissa packing of them.  Each test prints its error line:
 the fraction of voxels above 5 % of the maximum whose energy agrees within 3
 combined standard errors, and the relative difference of the total energy
-imparted (criteria: >= 99 % and <= 0.3 %)."""
+imparted (criteria: >= 99 %, and within 4 standard errors of the difference, from
+the spread of 32 replicate GPU runs, which must be at most 0.3 %)."""
 import numpy as np
 import pytest
 
@@ -46,7 +47,8 @@ def test_c2_torso_1e8_histories_against_fp64_densities(gpu, oracle):
     frac, nvox, rel = error_line("C2", n, e1, q1, e2, q2)
     assert nvox > 500_000
     assert frac >= 0.99, frac
-    assert abs(rel) <= 3e-3
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+    parity.assert_totals_agree(e1, e2, tol, "C2")
 
 
 def test_c1_cylinder_against_fp64_densities(gpu, oracle):
@@ -62,7 +64,9 @@ def test_c1_cylinder_against_fp64_densities(gpu, oracle):
     e1, q1, _ = gw.tally()
     e2, q2, _ = ow.tally()
     frac, nvox, rel = error_line("C1", n, e1, q1, e2, q2)
-    assert nvox > 10_000 and frac >= 0.99 and abs(rel) <= 3e-3
+    assert nvox > 10_000 and frac >= 0.99
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+    parity.assert_totals_agree(e1, e2, tol, "C1")
 
 
 def test_c3_batch_jobs_against_oracle(gpu, oracle):
@@ -87,7 +91,9 @@ def test_c3_batch_jobs_against_oracle(gpu, oracle):
         e1, q1, _ = w.tally()
         e2, q2, _ = ow.tally()
         frac, nvox, rel = error_line(f"C3 job {j} {specs[j]['dims']}", n, e1, q1, e2, q2)
-        assert nvox > 1000 and frac >= 0.99 and abs(rel) <= 3e-3, (j, frac, rel)
+        assert nvox > 1000 and frac >= 0.99, (j, frac)
+        tol = parity.total_tolerance(w, specs[j]["beam"], lambda r: gpu.run_options(seed=100 + r, stream=j))
+        parity.assert_totals_agree(e1, e2, tol, f"C3 job {j}")
     batch.close()
 
 
@@ -107,4 +113,6 @@ def test_c5_torso_history_range_against_oracle(gpu, oracle):
     e1, q1, _ = gw.tally()
     e2, q2, _ = ow.tally()
     frac, nvox, rel = error_line("C5", n, e1, q1, e2, q2)
-    assert nvox > 100_000 and frac >= 0.99 and abs(rel) <= 3e-3
+    assert nvox > 100_000 and frac >= 0.99
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0, hist_end=20_000_000))
+    parity.assert_totals_agree(e1, e2, tol, "C5")

@@ -60,8 +60,9 @@ def test_modified_table_transport_matches_oracle(tables, tmp_path):
     e2, q2, _ = ow.tally()
     frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
                                                  parity.tally_variance(e2, q2, n))
-    print(f"modified table: {frac:.4f} of {nvox} voxels within 3 sigma, GPU/oracle - 1 = "
-          f"{e1.sum() / e2.sum() - 1:+.2e}, model/modified energy {e0.sum() / e1.sum():.4f}")
+    print(f"modified table: {frac:.4f} of {nvox} voxels within 3 sigma, "
+          f"model/modified energy {e0.sum() / e1.sum():.4f}")
     assert nvox > 2000 and frac >= 0.99
-    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+    parity.assert_totals_agree(e1, e2, tol, "modified table")
     assert abs(e0.sum() / e1.sum() - 1) > 0.01  # oxygen's photoelectric x 1.5 shows in the dose

@@ -3,7 +3,9 @@
 Two kinds of comparison:
   * independent streams (different Philox stream words): per-voxel energy
     imparted within 3 combined standard errors in >= 99 % of voxels above 5 % of
-    the maximum, total energy within 0.3 %;
+    the maximum; total energy within 4 standard errors of the difference (the
+    spread of 32 replicate GPU runs of the beam), at history counts where that is
+    at most 0.3 %;
   * shared streams (same seed and stream): the GPU (FP32 tracking) and the
     oracle (FP64) draw the same uniforms per history, so totals agree far more
     tightly; what is left is FP32 vs FP64 rounding flipping a few decisions.
@@ -67,7 +69,8 @@ def test_c1_dx_independent_streams(c1, gpu):
     frac, nvox, e1, e2 = compare(gw, ow, 10_000_000)
     assert nvox > 10000
     assert frac >= 0.99, frac
-    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+    parity.assert_totals_agree(e1, e2, tol, "C1 DX")
 
 
 def test_c1_dx_shared_streams(c1, gpu):
@@ -106,14 +109,16 @@ def test_level2_impulse_approximation_and_fluorescence(gpu, oracle):
     e2, _, _ = ow.tally()
     assert e1.sum() == pytest.approx(e2.sum(), rel=2e-3)
     assert e1.sum() + sg["e_escaped"] == pytest.approx(sg["e_source"], rel=1e-5)
-    # independent streams
+    # independent streams, 7e6 histories
     gw.clear()
     ow.clear()
+    beam = P.dx_beam_params(particles=700_000, exposures=10)
     sg = gw.run(beam, gpu.run_options(seed=1, stream=0))
     ow.run(beam, seed=1, stream=1)
     frac, nvox, e1, e2 = compare(gw, ow, sg["n_histories"])
     assert nvox > 1000 and frac >= 0.99, frac
-    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+    parity.assert_totals_agree(e1, e2, tol, "level 2")
 
 
 @pytest.mark.parametrize("steps", [2, 5])
@@ -199,15 +204,16 @@ def test_c2_spiral_ct_torso_independent_streams(gpu, oracle):
     ph = P.torso_phantom(seed=1)
     gw = gpu_world(gpu, ph)
     ow = oracle_world_on_packed(oracle, gw, ph)
-    beam = P.ct_spiral_params(particles=8000)  # 360 exposures -> 2.88e6 histories
+    beam = P.ct_spiral_params(particles=54_000)  # 360 exposures -> 1.94e7 histories
     sg = gw.run(beam, gpu.run_options(seed=11, stream=0))
     so = ow.run(beam, seed=11, stream=1)
     n = sg["n_histories"]
-    assert n == so["n_histories"] == 360 * 8000
+    assert n == so["n_histories"] == 360 * 54_000
     frac, nvox, e1, e2 = compare(gw, ow, n)
     assert nvox > 2000
     assert frac >= 0.99, frac
-    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, stream=0))
+    parity.assert_totals_agree(e1, e2, tol, "C2 torso")
 
 
 def test_c5_torso_full_size_conservation(gpu):
@@ -249,11 +255,13 @@ def test_macro_tracking_matches_oracle(c1, gpu, cell):
     assert e1.sum() == pytest.approx(e2.sum(), rel=2e-3)
     gw.clear()
     ow.clear()
+    beam = P.dx_beam_params(particles=800_000, exposures=5)
     sg = gw.run(beam, gpu.run_options(seed=14, stream=0, tracking=2, macro_cell=cell))
     ow.run(beam, seed=14, stream=1, tracking=0)
     frac, nvox, e1, e2 = compare(gw, ow, sg["n_histories"])
     assert nvox > 5000 and frac >= 0.99
-    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, tracking=2, macro_cell=cell))
+    parity.assert_totals_agree(e1, e2, tol, f"macro cells {cell}")
 
 
 def oracle_macro():
@@ -266,13 +274,14 @@ def test_macro_tracking_c2_torso(gpu, oracle):
     ph = P.torso_phantom(seed=2)
     gw = gpu_world(gpu, ph)
     ow = oracle_world_on_packed(oracle, gw, ph)
-    beam = P.ct_spiral_params(particles=5000)
+    beam = P.ct_spiral_params(particles=67_000)  # 2.4e7 histories
     sg = gw.run(beam, gpu.run_options(seed=3, stream=0, tracking=2))
     ow.run(beam, seed=3, stream=1)
     assert sg["n_visits"] < 0.4 * 20.5 * sg["n_histories"]  # far fewer voxel lookups than global Woodcock
     frac, nvox, e1, e2 = compare(gw, ow, sg["n_histories"])
     assert nvox > 2000 and frac >= 0.99
-    assert e1.sum() == pytest.approx(e2.sum(), rel=3e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, tracking=2))
+    parity.assert_totals_agree(e1, e2, tol, "macro cells, C2 torso")
 
 
 def test_siddon_tracking_matches_woodcock(gpu):
@@ -307,12 +316,13 @@ def test_siddon_tracking_matches_oracle(gpu, oracle):
     ph = parity.small_cylinder()
     gw = gpu_world(gpu, ph)
     ow = oracle_world_on_packed(oracle, gw, ph)
-    beam = P.dx_beam_params(particles=100_000, exposures=4)
+    beam = P.dx_beam_params(particles=850_000, exposures=4)
     sg = gw.run(beam, gpu.run_options(seed=2, stream=0, tracking=1))
     ow.run(beam, seed=2, stream=1, tracking=oracle.TRACK_SIDDON)
     frac, nvox, e1, e2 = compare(gw, ow, sg["n_histories"])
     assert nvox > 500 and frac >= 0.99
-    assert e1.sum() == pytest.approx(e2.sum(), rel=5e-3)
+    tol = parity.total_tolerance(gw, beam, lambda r: gpu.run_options(seed=100 + r, tracking=1))
+    parity.assert_totals_agree(e1, e2, tol, "Siddon")
 
 
 def test_beer_lambert_transmission(gpu, oracle):

@@ -65,6 +65,9 @@ def parse():
                    help="Woodcock steps a lane takes between regroupings (0: library default)")
     p.add_argument("--gather-skip", type=int, choices=[-1, 0, 1], default=0,
                    help="Woodcock gather skip: 1 on, -1 off, 0 library default (on above 64 MiB of voxels)")
+    p.add_argument("--two-region", type=int, choices=[-1, 0, 1], default=0,
+                   help="two-region Woodcock (outside the box of non-air voxels against air's own majorant): "
+                        "1 on, -1 off, 0 library default (on above 64 MiB of voxels)")
     p.add_argument("--interact-batch", type=int, default=0)
     p.add_argument("--refill-batch", type=int, default=0)
     p.add_argument("--correction", type=int, choices=[0, 1, 2], default=1,
@@ -323,7 +326,8 @@ def run_ours(args):
     def run_opts(seed):
         return G.run_options(seed=seed, stream=rank, tracking=TRACKING[args.tracking], macro_cell=args.macro_cell,
                              woodcock_steps=args.woodcock_steps, interact_batch=args.interact_batch,
-                             refill_batch=args.refill_batch, gather_skip=args.gather_skip)
+                             refill_batch=args.refill_batch, gather_skip=args.gather_skip,
+                             two_region=args.two_region)
 
     def step(seed):
         flush.fill_(float(seed))
@@ -514,7 +518,8 @@ def run_batch(args):
     def opts(j, seed):
         o = G.run_options(seed=seed, stream=j, tracking=trk, macro_cell=args.macro_cell,
                           block_size=tuned.block_size, interact_batch=tuned.interact_batch,
-                          refill_batch=tuned.refill_batch, woodcock_steps=tuned.woodcock_steps)
+                          refill_batch=tuned.refill_batch, woodcock_steps=tuned.woodcock_steps,
+                          gather_skip=args.gather_skip, two_region=args.two_region)
         return o
 
     batch = G.Batch([(w, sp["beam"], opts(j, 1)) for j, (w, sp) in enumerate(zip(worlds, specs))])

@@ -179,6 +179,13 @@ typedef struct {
      * (4 bytes per voxel; for a batch, of all its worlds, decided from opts[0])
      * exceed 64 MiB, where they no longer stay in L2 */
     int32_t gather_skip;
+    /* WOODCOCK tracking, two regions: outside the bounding box of the voxels whose
+     * material is neither 0 nor transparent, flights step against material 0's own
+     * majorant until they reach the box (the same transport, fewer tentative
+     * collisions in the air around a patient).  1 = on, -1 = off, 0 = default: on
+     * when the world's voxel words (4 bytes per voxel) exceed 64 MiB; a batch
+     * decides from opts[0] and is on only for 1 */
+    int32_t two_region;
 } dxmcg_run_options;
 
 typedef struct {

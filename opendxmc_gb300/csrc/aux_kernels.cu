@@ -1,7 +1,10 @@
-// aux_kernels.cu -- kernels around the transport: voxel packing at World::build,
-// dose finalisation at readout, and the device test hooks that run single
-// pieces of the hot path (traversal, Philox, samplers, source) on given inputs.
+// aux_kernels.cu -- kernels around the transport: voxel packing, gather-skip cell
+// bounds and the two-region Woodcock box at World::build, dose finalisation at
+// readout, and the device test hooks that run single pieces of the hot path
+// (traversal, Philox, samplers, source) on given inputs.
+#include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 
@@ -115,6 +118,64 @@ namespace {
                 tr |= warpTransparent[w];
             }
             bound[c] = tr ? __int_as_float(0x7f800000) : b * (1.0f + 2.44140625e-4f);
+        }
+    }
+
+    // One warp per (y, z) row of voxels, reading x coalesced; per-lane extremes are
+    // reduced over the warp and the block, then six atomics per block.
+    // T = uint32_t: packed voxel words (material in the low byte); T = uint8_t: materials
+    template <typename T>
+    __global__ void materialBoxKernel(const T* __restrict__ vox, int nx, int ny, int nz, int* __restrict__ box)
+    {
+        int lo[3] = { INT_MAX, INT_MAX, INT_MAX }, hi[3] = { -1, -1, -1 };
+        const unsigned lane = threadIdx.x & 31u;
+        const long long rows = static_cast<long long>(ny) * nz;
+        const long long nWarps = static_cast<long long>(gridDim.x) * (blockDim.x >> 5);
+        for (long long r = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; r < rows;
+             r += nWarps) {
+            const T* row = vox + r * nx;
+            int xlo = INT_MAX, xhi = -1;
+            for (int x = static_cast<int>(lane); x < nx; x += 32) {
+                const uint32_t m = static_cast<uint32_t>(__ldg(row + x)) & 0xffu;
+                if (m != 0u && m != DXMCG_TRANSPARENT_MATERIAL) {
+                    xlo = min(xlo, x);
+                    xhi = max(xhi, x);
+                }
+            }
+            if (xhi >= 0) {
+                const int y = static_cast<int>(r % ny), z = static_cast<int>(r / ny);
+                lo[0] = min(lo[0], xlo);
+                hi[0] = max(hi[0], xhi);
+                lo[1] = min(lo[1], y);
+                hi[1] = max(hi[1], y);
+                lo[2] = min(lo[2], z);
+                hi[2] = max(hi[2], z);
+            }
+        }
+        __shared__ int sLo[32][3], sHi[32][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            for (int o = 16; o > 0; o >>= 1) {
+                lo[a] = min(lo[a], __shfl_xor_sync(kFull, lo[a], o));
+                hi[a] = max(hi[a], __shfl_xor_sync(kFull, hi[a], o));
+            }
+            if (lane == 0) {
+                sLo[threadIdx.x >> 5][a] = lo[a];
+                sHi[threadIdx.x >> 5][a] = hi[a];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w)
+                for (int a = 0; a < 3; ++a) {
+                    lo[a] = min(lo[a], sLo[w][a]);
+                    hi[a] = max(hi[a], sHi[w][a]);
+                }
+            if (hi[0] >= 0)
+                for (int a = 0; a < 3; ++a) {
+                    atomicMin(box + a, lo[a]);
+                    atomicMax(box + 3 + a, hi[a]);
+                }
         }
     }
 
@@ -289,6 +350,27 @@ cudaError_t launchCellBound(const uint32_t* vox, int nx, int ny, int nz, int ncx
     float* bound, cudaStream_t s)
 {
     cellBoundKernel<<<ncx * ncy * ncz, 128, 0, s>>>(vox, nx, ny, nz, ncx, ncy, ratio, bound);
+    return cudaGetLastError();
+}
+
+static int materialBoxBlocks(int ny, int nz)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long rows = static_cast<long long>(ny) * nz;
+    return static_cast<int>(std::min<long long>((rows + 7) / 8, 4LL * (sms > 0 ? sms : 1)));
+}
+
+cudaError_t launchMaterialBox(const uint32_t* vox, int nx, int ny, int nz, int* box, cudaStream_t s)
+{
+    materialBoxKernel<uint32_t><<<materialBoxBlocks(ny, nz), 256, 0, s>>>(vox, nx, ny, nz, box);
+    return cudaGetLastError();
+}
+
+cudaError_t launchMaterialBox(const uint8_t* mat, int nx, int ny, int nz, int* box, cudaStream_t s)
+{
+    materialBoxKernel<uint8_t><<<materialBoxBlocks(ny, nz), 256, 0, s>>>(mat, nx, ny, nz, box);
     return cudaGetLastError();
 }
 

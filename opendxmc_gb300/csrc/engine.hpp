@@ -136,6 +136,17 @@ struct DevJob {
     // cell holds a transparent voxel); nullptr: off.  cb[0], cb[1]: cells along x, y.
     const float* cbound;
     int cb[2];
+    // Two-region Woodcock: every voxel outside the box of voxels whose material is not
+    // 0 (nor transparent) holds material 0, so a flight that starts outside the box
+    // steps against majOut(E) >= rho mu_0(E) of those voxels until it reaches the box,
+    // and against maj(E) from there on.  Box voxel indices b0 .. b0 + bn - 1; blo, bhi:
+    // its faces in cm, widened by a margin (a flight may reach it early, never late).
+    // boxOn 0: one region.
+    int boxOn;
+    int b0[3];
+    unsigned bn[3];
+    float blo[3], bhi[3];
+    const float* majOut;
 };
 
 constexpr int kCellShift = 3; // gather-skip cells of 8 x 8 x 8 voxels
@@ -148,6 +159,7 @@ struct DevCounters {
     double e_source, e_escaped, e_deposited;
     unsigned int error_flags;
     unsigned long long skipped; // Woodcock tentative collisions settled by the cell bound alone
+    unsigned long long outer;   // two-region Woodcock: tentative collisions outside the box (no cell bound)
 };
 
 enum ErrorFlag : unsigned {
@@ -165,6 +177,15 @@ struct LaunchShape {
     int woodcock_steps = 0; // Woodcock steps per lane and step phase (0: default)
 };
 
+// Kernel instances of the transport are chosen by "kernel tracking": the public
+// DXMCG_TRACK_* modes, and kTrackWoodcockBox, Woodcock tracking with two regions,
+// for jobs whose world has a two-region box (DevJob::boxOn).
+constexpr int kTrackWoodcockBox = 3;
+inline int kernelTracking(const DevJob& J)
+{
+    return J.tracking == DXMCG_TRACK_WOODCOCK && J.boxOn ? kTrackWoodcockBox : J.tracking;
+}
+
 // kernels (transport.cu)
 cudaError_t launchPack(const double* dens64, const float* dens32, const uint8_t* mat, uint32_t* vox, size_t n,
     int n_mats, unsigned* rho_max_bits, unsigned* err, cudaStream_t s);
@@ -175,6 +196,11 @@ cudaError_t launchMacroScale(const uint32_t* vox, int nx, int ny, int nz, int mb
     const float* ratio, unsigned* scaleBits, cudaStream_t s);
 // gather-skip bounds: per cell of kCellEdge^3 voxels (cells x fastest, ncx x ncy x ncz)
 // max over its voxels of rho * ratio[m] times (1 + 2^-12), +inf if one is transparent
+// bounding box of the voxels whose material is neither 0 nor transparent:
+// box = {min x, min y, min z, max x, max y, max z}, initialised by the caller to
+// {INT_MAX x3, -1 x3} (max x = -1 after the launch: no such voxel)
+cudaError_t launchMaterialBox(const uint32_t* vox, int nx, int ny, int nz, int* box, cudaStream_t s);
+cudaError_t launchMaterialBox(const uint8_t* mat, int nx, int ny, int nz, int* box, cudaStream_t s);
 cudaError_t launchCellBound(const uint32_t* vox, int nx, int ny, int nz, int ncx, int ncy, int ncz, const float* ratio,
     float* bound, cudaStream_t s);
 cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, double energy_to_dose,

@@ -162,6 +162,40 @@ void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const 
         maj[i] = static_cast<float>(std::max(mx[i] * kMajorantSafety, 1e-30));
 }
 
+void buildBackgroundMajorant(const float* tot0, double rho0, float* out)
+{
+    for (int i = 0; i < kNE; ++i)
+        out[i] = static_cast<float>(std::max(static_cast<double>(tot0[i]) * rho0 * kMajorantSafety, 1e-30));
+}
+
+bool twoRegionBox(const int box[6], const int32_t dims[3])
+{
+    return box[3] >= 0
+        && (box[0] > 0 || box[1] > 0 || box[2] > 0 || box[3] < dims[0] - 1 || box[4] < dims[1] - 1
+            || box[5] < dims[2] - 1);
+}
+
+bool twoRegionFor(const dxmcg_run_options& o, size_t voxelBytes)
+{
+    if (o.tracking != DXMCG_TRACK_WOODCOCK || o.two_region < 0)
+        return false;
+    return o.two_region > 0 || voxelBytes > (64ull << 20);
+}
+
+void setTwoRegion(DevJob& J, const int box[6], const double spacing[3], const float* majOut)
+{
+    J.boxOn = 1;
+    J.majOut = majOut;
+    for (int a = 0; a < 3; ++a) {
+        J.b0[a] = box[a];
+        J.bn[a] = static_cast<unsigned>(box[3 + a] - box[a] + 1);
+        // the widened faces: a flight may find the box up to this much early, never late
+        const double margin = std::max(1e-3, 1e-3 * spacing[a]);
+        J.blo[a] = static_cast<float>(box[a] * spacing[a] - margin);
+        J.bhi[a] = static_cast<float>((box[3 + a] + 1) * spacing[a] + margin);
+    }
+}
+
 int buildHostJob(const dxmcg_beam& b, const int32_t dims[3], const double spacing[3], HostJob& out, std::string& err)
 {
     std::vector<dxmcg_exposure> ex;

@@ -34,6 +34,17 @@ void materialTables(const dxmcg_material& m, int correction, double* photo, doub
 
 // FP32 device tables for M materials and the majorant (rho_max[m] * total, times a
 // small safety factor, maximised over m) on the table grid.
+// majorant of material 0 alone: rho0 x its total attenuation, with the same safety
+// factor and floor as the grid's majorant
+void buildBackgroundMajorant(const float* tot0, double rho0, float* out);
+// two-region Woodcock: the box {lo x, y, z, hi x, y, z} of the voxels whose material is
+// neither 0 nor transparent (hi x = -1: none) is worth a second region when it leaves
+// part of the grid out; setTwoRegion fills J's box fields and material 0's majorant
+bool twoRegionBox(const int box[6], const int32_t dims[3]);
+// whether Woodcock runs with two regions: two_region 1 on, -1 off, 0 on when the voxel
+// words exceed 64 MiB (beyond L2), the grids on which it was measured to pay
+bool twoRegionFor(const dxmcg_run_options& o, size_t voxelBytes);
+void setTwoRegion(DevJob& J, const int box[6], const double spacing[3], const float* majOut);
 void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const double* rhoMax, float* tot,
     float4* xs, float* maj, DevMaterial* dm);
 

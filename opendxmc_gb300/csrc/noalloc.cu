@@ -7,10 +7,10 @@
 // between its set-up phase and its runs.  They own every input and output array
 // and pass device pointers; everything else this path needs -- the work-queue head
 // and run statistics, the validation flags and per-material maximum densities,
-// the attenuation tables and majorant, the Compton S(t) tables, the exposure list,
-// the spectra and the bowtie profiles -- lives in one file-scope __device__ array of
-// kScratchBytes = 512 KiB.  Every GPU that loads the library holds that array
-// until the process exits.
+// the attenuation tables and majorants, the Compton S(t) tables, the two-region box,
+// the exposure list, the spectra and the bowtie profiles -- lives in one file-scope
+// __device__ array of kScratchBytes = 512 KiB.  Every GPU that loads the library
+// holds that array until the process exits.
 //
 // The host finds the array's device address with cudaGetSymbolAddress, once per
 // device, with that device current, on the first call made on that device.  Every
@@ -26,6 +26,7 @@
 // calibration simulates a CTDI phantom world, which needs device allocations.
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -60,7 +61,9 @@ namespace {
     constexpr size_t kOffXs = alignUp(kOffTot + kMaxMaterials * kTableNE * sizeof(float));
     constexpr size_t kOffExps = alignUp(kOffXs + kMaxMaterials * kTableNE * sizeof(float4));
     constexpr size_t kOffSTab = alignUp(kOffExps + kMaxExposures * sizeof(DevExposure));
-    constexpr size_t kUsed = kOffSTab + kMaxMaterials * kSTabN * sizeof(float);
+    constexpr size_t kOffBox = alignUp(kOffSTab + kMaxMaterials * kSTabN * sizeof(float)); // 6 ints
+    constexpr size_t kOffMajOut = alignUp(kOffBox + 6 * sizeof(int));
+    constexpr size_t kUsed = kOffMajOut + kTableNE * sizeof(float);
     static_assert(kUsed <= kScratchBytes, "scratch layout exceeds the static array");
     static_assert(sizeof(dxmcg_tally_record) == sizeof(Tally), "tally record layout");
 
@@ -198,8 +201,12 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     auto* counters = reinterpret_cast<DevCounters*>(base + kOffCounters);
     auto* flags = reinterpret_cast<unsigned*>(base + kOffFlags);
 
-    // 1. maximum density per material and validation of the caller's arrays
+    // 1. maximum density per material and validation of the caller's arrays; the
+    //    two-region box of the materials
+    auto* box = reinterpret_cast<int*>(base + kOffBox);
+    const int boxInit[6] = { INT_MAX, INT_MAX, INT_MAX, -1, -1, -1 };
     NOALLOC_CUDA(cudaMemsetAsync(flags, 0, 257 * sizeof(unsigned), s));
+    NOALLOC_CUDA(cudaMemcpyAsync(box, boxInit, sizeof(boxInit), cudaMemcpyHostToDevice, s));
     int dev = 0, sms = 0;
     NOALLOC_CUDA(cudaGetDevice(&dev));
     NOALLOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -207,8 +214,13 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     rhoMaxKernel<<<grid, 256, 0, s>>>(device_density, device_material, static_cast<size_t>(N), n_materials, flags,
         flags + 256);
     NOALLOC_CUDA(cudaGetLastError());
+    const bool woodcock = twoRegionFor(o, static_cast<size_t>(N) * sizeof(uint32_t));
+    if (woodcock)
+        NOALLOC_CUDA(launchMaterialBox(device_material, dims[0], dims[1], dims[2], box, s));
     unsigned host[257];
+    int hostBox[6];
     NOALLOC_CUDA(cudaMemcpyAsync(host, flags, sizeof(host), cudaMemcpyDeviceToHost, s));
+    NOALLOC_CUDA(cudaMemcpyAsync(hostBox, box, sizeof(hostBox), cudaMemcpyDeviceToHost, s));
     NOALLOC_CUDA(cudaStreamSynchronize(s));
     if (host[256] & kErrBadMaterial)
         return fail(DXMCG_ERR_ARGUMENT, "transport_run_noalloc: a voxel's material index is >= the number of materials");
@@ -233,6 +245,13 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     buildComptonTables(materials, n_materials, stab.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffSTab, stab.data(), stab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMaj, maj.data(), maj.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    const bool twoRegion = woodcock && twoRegionBox(hostBox, dims);
+    std::vector<float> majOut(kTableNE);
+    if (twoRegion) {
+        buildBackgroundMajorant(tot.data(), rhoMax[0], majOut.data());
+        NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMajOut, majOut.data(), majOut.size() * sizeof(float),
+            cudaMemcpyHostToDevice, s));
+    }
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMats, dm.data(), dm.size() * sizeof(DevMaterial), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffExps, hj.exposures.data(), hj.exposures.size() * sizeof(DevExposure),
         cudaMemcpyHostToDevice, s));
@@ -261,10 +280,12 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     J.exps = reinterpret_cast<const DevExposure*>(base + kOffExps);
     J.spec = reinterpret_cast<const DevSpectrum*>(base + kOffSpec);
     J.bowtie = hj.hasBowtie ? reinterpret_cast<const DevBowtie*>(base + kOffBowtie) : nullptr;
+    if (twoRegion)
+        setTwoRegion(J, hostBox, spacing_cm, reinterpret_cast<const float*>(base + kOffMajOut));
 
     LaunchShape shape;
     shape.block = o.block_size > 0 ? std::max(32, std::min(256, o.block_size / 32 * 32)) : 256;
-    const int resident = transportMaxBlocksPerSMUnpacked(shape.block, o.tracking);
+    const int resident = transportMaxBlocksPerSMUnpacked(shape.block, kernelTracking(J));
     shape.grid = std::max(1, sms) * (o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, resident) : resident);
     shape.interact_batch = std::min(32, std::max(0, o.interact_batch));
     shape.refill_batch = std::min(32, std::max(0, o.refill_batch));

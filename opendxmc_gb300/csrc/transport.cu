@@ -83,16 +83,154 @@ namespace {
         __device__ __forceinline__ double value() const { return static_cast<double>(s) - static_cast<double>(c); }
     };
 
+    // Per-thread sums of the source, escaped and deposited energy (K = 0, 1, 2), and
+    // the warp's pool of history indices [next, end) with its exhausted flag, in
+    // registers (LaneTotals<false>) or in shared memory (LaneTotals<true>; sums: value
+    // sEnergy[2K][thread], compensation [2K + 1]).  They change a few times per history
+    // or once per refill phase, so shared memory costs little where registers are short.
+    constexpr int kSumSource = 0, kSumEscaped = 1, kSumDeposited = 2;
+    __shared__ float sEnergy[6][256];
+    __shared__ unsigned long long sPool[256 / 32][2];
+    __shared__ int sExhausted[256 / 32];
+
+    template <bool SHARED>
+    struct LaneTotals;
+
+    template <>
+    struct LaneTotals<false> {
+        KahanSum sum[3];
+        unsigned long long next = 0, end = 0;
+        bool done = false;
+        __device__ __forceinline__ void init() { }
+        template <int K>
+        __device__ __forceinline__ void add(float x)
+        {
+            sum[K].add(x);
+        }
+        template <int K>
+        __device__ __forceinline__ double value() const
+        {
+            return sum[K].value();
+        }
+        __device__ __forceinline__ bool exhausted() const { return done; }
+        __device__ __forceinline__ void markExhausted() { done = true; }
+        __device__ __forceinline__ void loadPool(unsigned long long& n, unsigned long long& e) const
+        {
+            n = next;
+            e = end;
+        }
+        __device__ __forceinline__ void storePool(unsigned long long n, unsigned long long e)
+        {
+            next = n;
+            end = e;
+        }
+    };
+
+    template <>
+    struct LaneTotals<true> {
+        __device__ __forceinline__ void init()
+        {
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+                sEnergy[k][threadIdx.x] = 0.0f;
+            if ((threadIdx.x & 31u) == 0) {
+                sPool[threadIdx.x >> 5][0] = sPool[threadIdx.x >> 5][1] = 0ull;
+                sExhausted[threadIdx.x >> 5] = 0;
+            }
+            __syncwarp();
+        }
+        template <int K>
+        __device__ __forceinline__ void add(float x)
+        {
+            const float c = sEnergy[2 * K + 1][threadIdx.x], s0 = sEnergy[2 * K][threadIdx.x];
+            const float y = x - c;
+            const float t = s0 + y;
+            sEnergy[2 * K + 1][threadIdx.x] = (t - s0) - y;
+            sEnergy[2 * K][threadIdx.x] = t;
+        }
+        template <int K>
+        __device__ __forceinline__ double value() const
+        {
+            return static_cast<double>(sEnergy[2 * K][threadIdx.x])
+                - static_cast<double>(sEnergy[2 * K + 1][threadIdx.x]);
+        }
+        __device__ __forceinline__ bool exhausted() const { return sExhausted[threadIdx.x >> 5] != 0; }
+        // warp-uniform: every lane calls it; one writes, the barrier publishes
+        __device__ __forceinline__ void markExhausted()
+        {
+            __syncwarp();
+            if ((threadIdx.x & 31u) == 0)
+                sExhausted[threadIdx.x >> 5] = 1;
+            __syncwarp();
+        }
+        __device__ __forceinline__ void loadPool(unsigned long long& n, unsigned long long& e) const
+        {
+            n = sPool[threadIdx.x >> 5][0];
+            e = sPool[threadIdx.x >> 5][1];
+        }
+        __device__ __forceinline__ void storePool(unsigned long long n, unsigned long long e)
+        {
+            __syncwarp();
+            if ((threadIdx.x & 31u) == 0) {
+                sPool[threadIdx.x >> 5][0] = n;
+                sPool[threadIdx.x >> 5][1] = e;
+            }
+            __syncwarp();
+        }
+    };
+
+    // The photon's energy-grid position and the majorant its next flight steps
+    // against.  A negative invMmax marks a flight outside the two-region box, against
+    // majOut(E) = mmax = -1 / invMmax (no extra loop-carried register).
     struct EnergyCache {
         int ie;
         float fe, mmax, invMmax;
         __device__ __forceinline__ void set(const DevJob& J, float E)
         {
             gridPos(E, ie, fe);
+            toInner(J);
+        }
+        __device__ __forceinline__ void toInner(const DevJob& J)
+        {
             mmax = lerp1(J.maj, ie, fe);
             invMmax = 1.0f / mmax;
         }
+        __device__ __forceinline__ void toOuter(const DevJob& J)
+        {
+            mmax = lerp1(J.majOut, ie, fe);
+            invMmax = -1.0f / mmax;
+        }
     };
+
+    // Per-thread count of tentative collisions outside the two-region box (they read
+    // their voxel without the cell bound); about one per history, so kept in shared
+    // memory rather than in a register across the transport loop.
+    __shared__ unsigned sOuterVisits[256];
+
+    // Voxel (ix, iy, iz) lies outside the two-region box.
+    __device__ __forceinline__ bool outsideBox(const DevJob& J, int ix, int iy, int iz)
+    {
+        return (static_cast<unsigned>(ix - J.b0[0]) >= J.bn[0]) | (static_cast<unsigned>(iy - J.b0[1]) >= J.bn[1])
+            | (static_cast<unsigned>(iz - J.b0[2]) >= J.bn[2]);
+    }
+
+    // Distance along the flight to the widened box (FLT_MAX if the line misses it, 0
+    // from inside it).  Approximate reciprocals: the margin of the box absorbs their
+    // error, so the entry is never found late.
+    __device__ __forceinline__ float boxEntry(const DevJob& J, const Photon& ph)
+    {
+        const float p[3] = { ph.px, ph.py, ph.pz };
+        const float d[3] = { ph.dx, ph.dy, ph.dz };
+        float tn = 0.0f, tf = FLT_MAX;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float inv = __fdividef(1.0f, d[a]);
+            const float t1 = (J.blo[a] - p[a]) * inv, t2 = (J.bhi[a] - p[a]) * inv;
+            tn = fmaxf(tn, fminf(t1, t2));
+            tf = fminf(tf, fmaxf(t1, t2));
+        }
+        return tn <= tf ? tn : FLT_MAX;
+    }
 
     // Density and material of voxel v: one 4-byte word in the packed layout, or two
     // loads from caller-owned arrays in the unpacked layout.
@@ -118,12 +256,32 @@ namespace {
     // decisions, and so the histories, are those of the plain step.  Cells holding a
     // transparent voxel (b_c = +inf) take the plain step, which draws the uniform only
     // for a voxel that is not transparent.
-    template <bool PACKED>
-    __device__ __forceinline__ bool woodcockStep(const DevJob& J, Photon& ph, Rng& rng, const EnergyCache& ec,
+    //
+    // BOX (the two-region instance, for jobs with J.boxOn): a flight outside the box
+    // steps against majOut; if the box comes first, the photon moves to it and steps
+    // on against maj (the flight is memoryless), drawing no acceptance uniform.  A
+    // flight against maj that ends outside the box decides its tentative collision as
+    // usual (maj bounds every voxel); the flights after it step against majOut.  Every
+    // decision keeps the tentative-collision rate at or above rho mu(E) on the path, so
+    // the transport is that of plain Woodcock with fewer tentative collisions.  Outside
+    // the box the cell bounds (relative to maj) are not used.
+    template <bool PACKED, bool BOX>
+    __device__ __forceinline__ bool woodcockStep(const DevJob& J, Photon& ph, Rng& rng, EnergyCache& ec,
         bool& escaped, uint32_t& v, int& m, unsigned& visits, unsigned& skipped)
     {
+        const bool outer = BOX && ec.invMmax < 0.0f;
         // hardware log2: |error| <= 2^-21.4 near u = 1, where the step is < 1e-6 mean free paths
-        const float s = fmaxf(-__logf(rng.u()), 0.0f) * ec.invMmax;
+        const float s = fmaxf(-__logf(rng.u()), 0.0f) * (BOX ? fabsf(ec.invMmax) : ec.invMmax);
+        if (BOX && outer) {
+            const float te = boxEntry(J, ph);
+            if (te < s) {
+                ph.px = fmaf(te, ph.dx, ph.px);
+                ph.py = fmaf(te, ph.dy, ph.py);
+                ph.pz = fmaf(te, ph.dz, ph.pz);
+                ec.toInner(J);
+                return false;
+            }
+        }
         ph.px = fmaf(s, ph.dx, ph.px);
         ph.py = fmaf(s, ph.dy, ph.py);
         ph.pz = fmaf(s, ph.dz, ph.pz);
@@ -140,24 +298,51 @@ namespace {
         }
         ++visits;
         v = static_cast<uint32_t>(ix + J.nx * (iy + J.ny * iz));
-        if (J.cbound) {
+        if (!BOX) {
+            if (J.cbound) {
+                const float b = __ldg(J.cbound
+                    + ((ix >> kCellShift) + J.cb[0] * ((iy >> kCellShift) + J.cb[1] * (iz >> kCellShift))));
+                if (b <= FLT_MAX) {
+                    const float t = rng.u() * ec.mmax;
+                    if (t >= b * ec.mmax) {
+                        ++skipped;
+                        return false;
+                    }
+                    const float rho = voxelAt<PACKED>(J, v, m);
+                    return t < rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
+                }
+            }
+            const float rho = voxelAt<PACKED>(J, v, m);
+            if (m == DXMCG_TRANSPARENT_MATERIAL)
+                return false;
+            const float mu = rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
+            return rng.u() * ec.mmax < mu;
+        }
+        if (outer)
+            ++sOuterVisits[threadIdx.x];
+        bool real = false, decided = false;
+        if (J.cbound && !outer) {
             const float b = __ldg(J.cbound
                 + ((ix >> kCellShift) + J.cb[0] * ((iy >> kCellShift) + J.cb[1] * (iz >> kCellShift))));
             if (b <= FLT_MAX) {
+                decided = true;
                 const float t = rng.u() * ec.mmax;
                 if (t >= b * ec.mmax) {
                     ++skipped;
-                    return false;
+                } else {
+                    const float rho = voxelAt<PACKED>(J, v, m);
+                    real = t < rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
                 }
-                const float rho = voxelAt<PACKED>(J, v, m);
-                return t < rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
             }
         }
-        const float rho = voxelAt<PACKED>(J, v, m);
-        if (m == DXMCG_TRANSPARENT_MATERIAL)
-            return false;
-        const float mu = rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
-        return rng.u() * ec.mmax < mu;
+        if (!decided) {
+            const float rho = voxelAt<PACKED>(J, v, m);
+            if (m != DXMCG_TRANSPARENT_MATERIAL)
+                real = rng.u() * ec.mmax < rho * lerp1(J.tot + m * kTableNE, ec.ie, ec.fe);
+        }
+        if (J.boxOn && !outer && outsideBox(J, ix, iy, iz))
+            ec.toOuter(J);
+        return real;
     }
 
     // One free flight with exact voxel path lengths; true on a collision.
@@ -299,6 +484,8 @@ namespace {
         const unsigned long long* __restrict__ offsets, int nJobs, unsigned long long h_end,
         DevCounters* __restrict__ ctr, int refillBatch, int interactBatch, int woodcockSteps)
     {
+        constexpr bool BOX = TRACKING == kTrackWoodcockBox;
+        constexpr bool WOODCOCK = TRACKING == DXMCG_TRACK_WOODCOCK || BOX;
         int jid = 0;
         // event counters per warp (no block-wide barrier: warps finish independently)
         __shared__ unsigned long long sCountAll[256 / 32][cNum];
@@ -309,8 +496,12 @@ namespace {
         __syncwarp();
 
         const unsigned ltMask = (1u << lane) - 1u;
-        unsigned long long poolNext = 0, poolEnd = 0;
-        bool exhausted = false;
+        // energy sums (FP32, compensated) and the warp's history pool: in shared memory
+        // for the two-region instance, whose step would spill otherwise; in registers
+        // for the others, where shared memory measured slower (4 % on the 256x256x200
+        // torso, 5 % on the 64-job batch, whose instance spills a little instead)
+        LaneTotals<BOX> ls;
+        ls.init();
         int st = kDead;
         Photon ph;
         Rng rng;
@@ -320,7 +511,8 @@ namespace {
         unsigned steps = 0, visits = 0, crossings = 0, err = 0, skipped = 0;
         int cx = 0, cy = 0, cz = 0; // macro cell of the photon (MACRO tracking)
         bool fresh = false;
-        KahanSum esrc, eesc, edep; // FP32 compensated sums: no FP64 on the per-event path
+        if (BOX)
+            sOuterVisits[threadIdx.x] = 0u;
 
         for (;;) {
             const unsigned stepping = __ballot_sync(kFull, st == kStepping);
@@ -329,14 +521,16 @@ namespace {
             const int nStep = __popc(stepping);
 
             // ---- refill
-            if (dead && !exhausted && (__popc(dead) >= refillBatch || nStep == 0)) {
+            if (dead && !ls.exhausted() && (__popc(dead) >= refillBatch || nStep == 0)) {
+                unsigned long long poolNext, poolEnd;
+                ls.loadPool(poolNext, poolEnd);
                 if (poolNext >= poolEnd) {
                     unsigned long long base = 0;
                     if (lane == 0)
                         base = atomicAdd(&ctr->next, static_cast<unsigned long long>(kChunk));
                     base = __shfl_sync(kFull, base, 0);
                     if (base >= h_end) {
-                        exhausted = true;
+                        ls.markExhausted();
                         poolNext = poolEnd = 0;
                     } else {
                         poolNext = base;
@@ -364,7 +558,7 @@ namespace {
                     const DevJob& Jr = MULTI ? jobs[jid] : J0;
                     rng.init(Jr.key0, Jr.key1, Jr.stream, h);
                     sampleSource(Jr, h, ph, rng);
-                    esrc.add(ph.w * ph.E);
+                    ls.template add<kSumSource>(ph.w * ph.E);
                     entered = enterGrid(Jr, ph);
                     if (entered) {
                         st = kStepping;
@@ -374,16 +568,21 @@ namespace {
                             gridPos(ph.E, ec.ie, ec.fe);
                         else
                             ec.set(Jr, ph.E);
+                        if (BOX && Jr.boxOn
+                            && outsideBox(Jr, __float2int_rd(ph.px * Jr.isp[0]), __float2int_rd(ph.py * Jr.isp[1]),
+                                __float2int_rd(ph.pz * Jr.isp[2])))
+                            ec.toOuter(Jr);
                         if (TRACKING == DXMCG_TRACK_MACRO) {
                             cx = min(static_cast<int>(ph.px / Jr.cellL[0]), Jr.mc[0] - 1);
                             cy = min(static_cast<int>(ph.py / Jr.cellL[1]), Jr.mc[1] - 1);
                             cz = min(static_cast<int>(ph.pz / Jr.cellL[2]), Jr.mc[2] - 1);
                         }
                     } else {
-                        eesc.add(ph.w * ph.E);
+                        ls.template add<kSumEscaped>(ph.w * ph.E);
                     }
                 }
                 poolNext += min(static_cast<unsigned long long>(__popc(dead)), avail);
+                ls.storePool(poolNext, poolEnd);
                 const unsigned mStart = __ballot_sync(kFull, start);
                 const unsigned mIn = __ballot_sync(kFull, entered);
                 if (lane == 0 && mStart) {
@@ -412,12 +611,12 @@ namespace {
                 if (compton) {
                     const float e = ph.w * (ph.E - Ep);
                     deposit(J.tally, pv, e);
-                    edep.add(e);
+                    ls.template add<kSumDeposited>(e);
                     ph.E = Ep;
                     if (Ep < 1.0f) {
                         const float r = ph.w * Ep;
                         deposit(J.tally, pv, r);
-                        edep.add(r);
+                        ls.template add<kSumDeposited>(r);
                         st = kDead;
                         cut = true;
                     } else {
@@ -435,7 +634,7 @@ namespace {
                     const float Ef = samplePhotoFluorescence(ph.E, J.mats + pm, rng);
                     const float e = ph.w * (ph.E - Ef);
                     deposit(J.tally, pv, e);
-                    edep.add(e);
+                    ls.template add<kSumDeposited>(e);
                     if (Ef > 0.0f) {
                         const float u1 = rng.u();
                         isotropicDirection(ph.dx, ph.dy, ph.dz, u1, rng.u());
@@ -467,7 +666,7 @@ namespace {
             }
 
             if (__ballot_sync(kFull, st != kDead) == 0u) {
-                if (exhausted)
+                if (ls.exhausted())
                     break;
                 continue;
             }
@@ -479,11 +678,11 @@ namespace {
                 uint32_t v = 0;
                 int m = 0;
                 bool real = false;
-                if (TRACKING == DXMCG_TRACK_WOODCOCK) {
+                if (WOODCOCK) {
                     // several steps per phase: most are virtual, and each phase boundary
                     // costs the warp its votes; a lane stops at a real collision or escape
                     for (int k = 0;;) {
-                        real = woodcockStep<PACKED>(J, ph, rng, ec, escaped, v, m, visits, skipped);
+                        real = woodcockStep<PACKED, BOX>(J, ph, rng, ec, escaped, v, m, visits, skipped);
                         if (real || escaped || ++k >= woodcockSteps)
                             break;
                         ++steps;
@@ -493,7 +692,7 @@ namespace {
                 else
                     real = macroFlight<PACKED>(J, ph, rng, ec, cx, cy, cz, escaped, v, m, visits, crossings, err);
                 if (escaped) {
-                    eesc.add(ph.w * ph.E);
+                    ls.template add<kSumEscaped>(ph.w * ph.E);
                     st = kDead;
                 } else if (real) {
                     first = fresh;
@@ -513,7 +712,7 @@ namespace {
                         } else {
                             const float e = ph.w * ph.E;
                             deposit(J.tally, v, e);
-                            edep.add(e);
+                            ls.template add<kSumDeposited>(e);
                             st = kDead;
                         }
                     } else {
@@ -545,9 +744,10 @@ namespace {
         const unsigned long long vi = warpSum(static_cast<unsigned long long>(visits));
         const unsigned long long cr = warpSum(static_cast<unsigned long long>(crossings));
         const unsigned long long sk = warpSum(static_cast<unsigned long long>(skipped));
-        const double es = warpSum(esrc.value());
-        const double ee = warpSum(eesc.value());
-        const double ed = warpSum(edep.value());
+        const unsigned long long ov = BOX ? warpSum(static_cast<unsigned long long>(sOuterVisits[threadIdx.x])) : 0ull;
+        const double es = warpSum(ls.template value<kSumSource>());
+        const double ee = warpSum(ls.template value<kSumEscaped>());
+        const double ed = warpSum(ls.template value<kSumDeposited>());
         unsigned errAll = err;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
@@ -559,6 +759,8 @@ namespace {
                 atomicAdd(&ctr->crossings, cr);
             if (sk)
                 atomicAdd(&ctr->skipped, sk);
+            if (ov)
+                atomicAdd(&ctr->outer, ov);
             atomicAdd(&ctr->e_source, es);
             atomicAdd(&ctr->e_escaped, ee);
             atomicAdd(&ctr->e_deposited, ed);
@@ -591,6 +793,7 @@ namespace {
         if (multi) {
             switch (tracking) {
             case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, true, true>;
+            case kTrackWoodcockBox: return transportKernel<kTrackWoodcockBox, true, true>;
             case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, true, true>;
             case DXMCG_TRACK_MACRO: return transportKernel<DXMCG_TRACK_MACRO, true, true>;
             default: return nullptr;
@@ -599,6 +802,7 @@ namespace {
         if (packed) {
             switch (tracking) {
             case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, true, false>;
+            case kTrackWoodcockBox: return transportKernel<kTrackWoodcockBox, true, false>;
             case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, true, false>;
             case DXMCG_TRACK_MACRO: return transportKernel<DXMCG_TRACK_MACRO, true, false>;
             default: return nullptr;
@@ -606,6 +810,7 @@ namespace {
         }
         switch (tracking) {
         case DXMCG_TRACK_WOODCOCK: return transportKernel<DXMCG_TRACK_WOODCOCK, false, false>;
+        case kTrackWoodcockBox: return transportKernel<kTrackWoodcockBox, false, false>;
         case DXMCG_TRACK_SIDDON: return transportKernel<DXMCG_TRACK_SIDDON, false, false>;
         default: return nullptr;
         }
@@ -635,13 +840,13 @@ namespace {
 cudaError_t launchTransport(const DevJob& job, unsigned long long h_end, DevCounters* ctr, LaunchShape shape,
     cudaStream_t s)
 {
-    return launchWith(kernelFor(job.tracking, true), job, nullptr, nullptr, 1, h_end, ctr, shape, s);
+    return launchWith(kernelFor(kernelTracking(job), true), job, nullptr, nullptr, 1, h_end, ctr, shape, s);
 }
 
 cudaError_t launchTransportUnpacked(const DevJob& job, unsigned long long h_end, DevCounters* ctr,
     LaunchShape shape, cudaStream_t s)
 {
-    return launchWith(kernelFor(job.tracking, false), job, nullptr, nullptr, 1, h_end, ctr, shape, s);
+    return launchWith(kernelFor(kernelTracking(job), false), job, nullptr, nullptr, 1, h_end, ctr, shape, s);
 }
 
 cudaError_t launchTransportBatch(int tracking, const DevJob* jobs, const unsigned long long* offsets, int nJobs,

@@ -101,7 +101,7 @@ def beam_calibration(params: dict, correction: int = 1, options: N.RunOptions | 
 
 def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_size=0, blocks_per_sm=0,
                 chunk_log2=0, hist_begin=0, hist_end=0, interact_batch=0, refill_batch=0,
-                macro_cell=0, woodcock_steps=0, max_steps=0, gather_skip=0) -> N.RunOptions:
+                macro_cell=0, woodcock_steps=0, max_steps=0, gather_skip=0, two_region=0) -> N.RunOptions:
     o = N.RunOptions()
     o.seed = seed
     o.stream = stream
@@ -118,6 +118,7 @@ def run_options(seed=1, stream=0, tracking=N.TRACK_WOODCOCK, normalize=0, block_
     o.woodcock_steps = woodcock_steps
     o.max_steps = max_steps
     o.gather_skip = gather_skip
+    o.two_region = two_region
     return o
 
 

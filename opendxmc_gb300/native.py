@@ -157,7 +157,8 @@ class RunOptions(C.Structure):
                 ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32), ("chunk_histories_log2", C.c_int32),
                 ("hist_begin", C.c_uint64), ("hist_end", C.c_uint64), ("interact_batch", C.c_int32),
                 ("refill_batch", C.c_int32), ("macro_cell", C.c_int32),
-                ("woodcock_steps", C.c_int32), ("max_steps", C.c_uint32), ("gather_skip", C.c_int32)]
+                ("woodcock_steps", C.c_int32), ("max_steps", C.c_uint32), ("gather_skip", C.c_int32),
+                ("two_region", C.c_int32)]
 
 
 class Stats(C.Structure):

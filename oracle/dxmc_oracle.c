@@ -1436,6 +1436,13 @@ struct or_world {
     double* coh;
     double* tot;
     double maj[OR_NE]; /* 1/cm */
+    /* two-region Woodcock: the box of voxels whose material is neither 0 nor
+     * transparent (voxel indices b0 .. b1 inclusive), its faces widened by a margin,
+     * and material 0's majorant; box_on 0: the box is empty or the whole grid */
+    int box_on;
+    int b0[3], b1[3];
+    double blo[3], bhi[3];
+    double maj_out[OR_NE];
     int mb;            /* macro-cell edge in voxels (0: none) */
     int mc[3];
     double* mscale;    /* per macro cell: majorant scale s_c */
@@ -1496,6 +1503,34 @@ or_world* or_world_create(const int32_t dims[3], const double spacing_cm[3], con
                 mx = v;
         }
         w->maj[i] = mx * MAJ_SAFETY;
+        const double mo = rmax[0] * w->tot[i] * MAJ_SAFETY;
+        w->maj_out[i] = mo > 1e-30 ? mo : 1e-30;
+    }
+    for (int a = 0; a < 3; ++a) {
+        w->b0[a] = INT32_MAX;
+        w->b1[a] = -1;
+    }
+    for (int z = 0; z < dims[2]; ++z)
+        for (int y = 0; y < dims[1]; ++y)
+            for (int x = 0; x < dims[0]; ++x) {
+                const int m = w->material[(size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z)];
+                if (m == 0 || m == OR_TRANSPARENT)
+                    continue;
+                const int i[3] = { x, y, z };
+                for (int a = 0; a < 3; ++a) {
+                    if (i[a] < w->b0[a])
+                        w->b0[a] = i[a];
+                    if (i[a] > w->b1[a])
+                        w->b1[a] = i[a];
+                }
+            }
+    w->box_on = w->b1[0] >= 0
+        && (w->b0[0] > 0 || w->b0[1] > 0 || w->b0[2] > 0 || w->b1[0] < dims[0] - 1 || w->b1[1] < dims[1] - 1
+            || w->b1[2] < dims[2] - 1);
+    for (int a = 0; a < 3; ++a) {
+        const double margin = 1e-3 * w->sp[a] > 1e-3 ? 1e-3 * w->sp[a] : 1e-3;
+        w->blo[a] = w->b0[a] * w->sp[a] - margin;
+        w->bhi[a] = (w->b1[a] + 1) * w->sp[a] + margin;
     }
     w->e = (double*)calloc(w->N, sizeof(double));
     w->e2 = (double*)calloc(w->N, sizeof(double));
@@ -1751,6 +1786,43 @@ static inline int inside(const or_world* w, const double p[3], size_t* v)
     return 1;
 }
 
+/* Two-region Woodcock: voxel indices of p outside the box (p inside the grid). */
+static inline int outside_box(const or_world* w, const double p[3])
+{
+    for (int a = 0; a < 3; ++a) {
+        int k = (int)floor(p[a] / w->sp[a]);
+        if (k > w->n[a] - 1)
+            k = w->n[a] - 1;
+        if (k < w->b0[a] || k > w->b1[a])
+            return 1;
+    }
+    return 0;
+}
+
+/* Distance along d to the widened box (DBL_MAX if the line misses it, 0 from inside). */
+static double box_entry(const or_world* w, const double p[3], const double d[3])
+{
+    double tn = 0.0, tf = DBL_MAX;
+    for (int a = 0; a < 3; ++a) {
+        if (d[a] == 0.0) {
+            if (p[a] < w->blo[a] || p[a] > w->bhi[a])
+                return DBL_MAX;
+            continue;
+        }
+        double t1 = (w->blo[a] - p[a]) / d[a], t2 = (w->bhi[a] - p[a]) / d[a];
+        if (t1 > t2) {
+            const double tt = t1;
+            t1 = t2;
+            t2 = tt;
+        }
+        if (t1 > tn)
+            tn = t1;
+        if (t2 < tf)
+            tf = t2;
+    }
+    return tn <= tf ? tn : DBL_MAX;
+}
+
 /* Real-interaction branch shared by both tracking modes; returns 0 if the photon died. */
 static int interact(or_world* w, size_t v, int m, double* E, double wgt, double d[3], rng_t* r, or_stats* st,
     int* first)
@@ -1881,6 +1953,10 @@ static void run_history(run_ctx* c, uint64_t h, or_stats* st)
         if (p[a] >= L[a])
             p[a] = nextafter(L[a], 0.0);
     }
+    /* two-region Woodcock: the flight starts against material 0's majorant when the
+     * entry point lies outside the box */
+    const int two = c->tracking == OR_TRACK_WOODCOCK_BOX && w->box_on;
+    int outer = two && outside_box(w, p);
     int cell[3] = { 0, 0, 0 };
     if (c->tracking == OR_TRACK_MACRO) {
         if (!w->mscale) {
@@ -1960,12 +2036,22 @@ static void run_history(run_ctx* c, uint64_t h, or_stats* st)
                 if (!interact(w, v, m, &E, wgt, d, &r, st, &first))
                     return;
             }
-        } else if (c->tracking == OR_TRACK_WOODCOCK) {
+        } else if (c->tracking == OR_TRACK_WOODCOCK || c->tracking == OR_TRACK_WOODCOCK_BOX) {
             int ie;
             double fe;
             grid_pos(E, &ie, &fe);
-            const double mmax = lerp_tab(w->maj, ie, fe);
+            const double mmax = lerp_tab(outer ? w->maj_out : w->maj, ie, fe);
             const double s = -log(rng_u(&r)) / mmax;
+            if (outer) {
+                /* the box comes first: move there, no tentative collision */
+                const double te = box_entry(w, p, d);
+                if (te < s) {
+                    for (int a = 0; a < 3; ++a)
+                        p[a] += te * d[a];
+                    outer = 0;
+                    continue;
+                }
+            }
             for (int a = 0; a < 3; ++a)
                 p[a] += s * d[a];
             size_t v;
@@ -1975,12 +2061,24 @@ static void run_history(run_ctx* c, uint64_t h, or_stats* st)
             }
             st->n_visits++;
             const int m = w->material[v];
-            if (m == OR_TRANSPARENT)
-                continue;
-            const double mu = w->density[v] * lerp_tab(w->tot + m * OR_NE, ie, fe);
-            if (rng_u(&r) * mmax < mu) {
+            /* a flight against maj that ends outside the box: the flights after this
+             * tentative collision step against material 0's majorant */
+            const int leave = two && !outer && outside_box(w, p);
+            int real = 0;
+            if (m != OR_TRANSPARENT) {
+                const double mu = w->density[v] * lerp_tab(w->tot + m * OR_NE, ie, fe);
+                real = rng_u(&r) * mmax < mu;
+            }
+            if (leave)
+                outer = 1;
+            if (real) {
+                /* a Rayleigh scattering keeps the flight's majorant; Compton scattering
+                 * and fluorescence start again against maj */
+                const uint64_t nr = st->n_rayleigh;
                 if (!interact(w, v, m, &E, wgt, d, &r, st, &first))
                     return;
+                if (st->n_rayleigh == nr)
+                    outer = 0;
             }
         } else {
             /* regular tracking: walk voxel segments until the sampled optical depth is used up */

@@ -36,7 +36,10 @@ extern "C" {
 #define OR_MAX_ELEMENTS 16
 #define OR_TRANSPARENT 255
 
-enum { OR_TRACK_WOODCOCK = 0, OR_TRACK_SIDDON = 1, OR_TRACK_MACRO = 2 };
+/* OR_TRACK_WOODCOCK_BOX: Woodcock with two regions, the transport kernel's default
+ * (outside the box of voxels whose material is neither 0 nor transparent, flights
+ * step against material 0's majorant until they reach the box) */
+enum { OR_TRACK_WOODCOCK = 0, OR_TRACK_SIDDON = 1, OR_TRACK_MACRO = 2, OR_TRACK_WOODCOCK_BOX = 3 };
 enum {
     OR_BEAM_DX = 0,
     OR_BEAM_CT_SPIRAL = 1,

@@ -25,6 +25,10 @@ MAX_ELEMENTS = 16
 TRACK_WOODCOCK = 0
 TRACK_SIDDON = 1
 TRACK_MACRO = 2
+TRACK_WOODCOCK_BOX = 3  # two-region Woodcock
+# the transport kernel's default: two-region Woodcock on grids whose 4-byte voxel words
+# exceed 64 MiB, one region below
+TWO_REGION_BYTES = 64 << 20
 BEAM_DX, BEAM_CT_SPIRAL, BEAM_CT_SEQUENTIAL, BEAM_CBCT, BEAM_PENCIL, BEAM_CT_SPIRAL_DUAL = range(6)
 
 
@@ -468,8 +472,12 @@ class World:
         lib().or_world_majorant(self._h, _p(m, C.c_double))
         return m
 
-    def run(self, beam: dict, seed=1, stream=0, tracking=TRACK_WOODCOCK, threads=None, hist_begin=0,
+    def run(self, beam: dict, seed=1, stream=0, tracking=None, threads=None, hist_begin=0,
             hist_end=2**63):
+        """tracking None: Woodcock as the transport kernel chooses by default (two
+        regions on grids beyond TWO_REGION_BYTES of voxel words, one below)."""
+        if tracking is None:
+            tracking = TRACK_WOODCOCK_BOX if 4 * self.N > TWO_REGION_BYTES else TRACK_WOODCOCK
         b, keep = make_beam(beam)
         st = Stats()
         threads = threads or os.cpu_count() or 1

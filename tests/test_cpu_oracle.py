@@ -258,6 +258,42 @@ def test_oracle_woodcock_and_siddon_tracking_agree(oracle):
     assert e1.sum() == pytest.approx(e2.sum(), rel=0.01)
 
 
+def test_oracle_two_region_woodcock_equals_plain_woodcock(oracle):
+    """Two-region Woodcock (material 0's own majorant outside the box of the other
+    voxels) samples the plain Woodcock transport with fewer tentative collisions:
+    per-voxel energy within 3 combined standard errors, totals of 16 replicates each
+    within 4 standard errors of their difference, and a third of the visits.  The box
+    is empty on a grid without background voxels, where the mode is plain Woodcock."""
+    ph = parity.small_torso(scale=4, seed=3)
+    w = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+    beam = P.ct_spiral_params(particles=400, scan_cm=10.0)
+    tot, tally, visits = {}, {}, {}
+    for trk in (oracle.TRACK_WOODCOCK, oracle.TRACK_WOODCOCK_BOX):
+        w.clear()
+        runs = [w.run(beam, stream=100 * trk + r, tracking=trk, threads=8) for r in range(16)]
+        tot[trk] = np.array([s["e_deposited"] for s in runs])
+        visits[trk] = sum(s["n_visits"] for s in runs) / sum(s["n_histories"] for s in runs)
+        tally[trk] = w.tally()
+        assert sum(s["n_errors"] for s in runs) == 0
+    n = 16 * runs[0]["n_histories"]
+    (e1, q1, _), (e2, q2, _) = tally[oracle.TRACK_WOODCOCK], tally[oracle.TRACK_WOODCOCK_BOX]
+    frac, nvox = parity.combined_sigma_agreement(e1, parity.tally_variance(e1, q1, n), e2,
+                                                 parity.tally_variance(e2, q2, n))
+    assert nvox > 200 and frac >= 0.99
+    a, b = tot[oracle.TRACK_WOODCOCK], tot[oracle.TRACK_WOODCOCK_BOX]
+    assert abs(a.sum() - b.sum()) <= 4.0 * np.hypot(parity.total_sigma(a), parity.total_sigma(b))
+    assert visits[oracle.TRACK_WOODCOCK_BOX] < 0.5 * visits[oracle.TRACK_WOODCOCK]
+    # no background voxel: one region, the same histories as plain Woodcock
+    full = oracle.World(ph.dims, ph.spacing, ph.density, np.ones_like(ph.material), ph.materials)
+    s1 = full.run(beam, stream=5, tracking=oracle.TRACK_WOODCOCK, hist_end=20000)
+    e1, _, _ = full.tally()
+    full.clear()
+    s2 = full.run(beam, stream=5, tracking=oracle.TRACK_WOODCOCK_BOX, hist_end=20000)
+    e2, _, _ = full.tally()
+    assert s1["n_visits"] == s2["n_visits"]
+    np.testing.assert_allclose(e2, e1, rtol=1e-12, atol=0)
+
+
 # ---- correction level 2 (impulse approximation, fluorescence)
 ME = 510.99895
 

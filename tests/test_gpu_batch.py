@@ -15,7 +15,8 @@ from opendxmc_gb300 import phantoms as P
 
 pytestmark = pytest.mark.gpu
 
-TRACKINGS = {"woodcock": N.TRACK_WOODCOCK, "siddon": N.TRACK_SIDDON, "macro": N.TRACK_MACRO}
+TRACKINGS = {"woodcock": N.TRACK_WOODCOCK, "siddon": N.TRACK_SIDDON, "macro": N.TRACK_MACRO,
+             "woodcock_two_region": N.TRACK_WOODCOCK}
 
 
 def make_world(gpu, ph):
@@ -49,7 +50,8 @@ def assert_tallies_match(a, b):
 def test_batch_matches_single_runs(gpu, jobs, tracking):
     phantoms, plan = jobs
     trk = TRACKINGS[tracking]
-    opts = [gpu.run_options(seed=11 + k, stream=3 * k, tracking=trk) for k in range(len(plan))]
+    two = 1 if tracking == "woodcock_two_region" else 0
+    opts = [gpu.run_options(seed=11 + k, stream=3 * k, tracking=trk, two_region=two) for k in range(len(plan))]
 
     worlds = [make_world(gpu, ph) for ph in phantoms]
     batch = gpu.Batch([(worlds[i], beam, o) for (i, beam), o in zip(plan, opts)])

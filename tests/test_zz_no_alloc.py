@@ -31,7 +31,10 @@ def _call(N, ph, d_dens, d_mat, d_tally, beam_params, opts, mats=None):
     return rc, st.as_dict()
 
 
-def test_noalloc_matches_world_entry_point_on_two_calls(gpu):
+@pytest.mark.parametrize("two_region", [0, 1])
+def test_noalloc_matches_world_entry_point_on_two_calls(gpu, two_region):
+    """Both entry points, one or two Woodcock regions (the two-region box of the
+    caller's materials is found on the device, into the static scratch)."""
     import torch
 
     from opendxmc_gb300 import native as N
@@ -49,15 +52,15 @@ def test_noalloc_matches_world_entry_point_on_two_calls(gpu):
 
     for seed in (5, 6):
         gw.clear()
-        ref = gw.run(beam, gpu.run_options(seed=seed, stream=2))
+        ref = gw.run(beam, gpu.run_options(seed=seed, stream=2, two_region=two_region))
         e_ref, e2_ref, c_ref = gw.tally()
         d_tally.zero_()
         torch.cuda.synchronize()
-        rc, st = _call(N, ph, d_dens, d_mat, d_tally, beam, gpu.run_options(seed=seed, stream=2))
+        rc, st = _call(N, ph, d_dens, d_mat, d_tally, beam, gpu.run_options(seed=seed, stream=2, two_region=two_region))
         assert rc == 0, N.lib().dxmcg_last_error().decode()
         rec = d_tally.cpu().numpy()
         counts = rec[:, 2].copy().view(np.uint64)
-        for k in ("n_histories", "n_missed", "n_photo", "n_compton", "n_rayleigh", "n_interacted"):
+        for k in ("n_histories", "n_missed", "n_visits", "n_photo", "n_compton", "n_rayleigh", "n_interacted"):
             assert st[k] == ref[k], k
         np.testing.assert_array_equal(counts, c_ref)
         np.testing.assert_allclose(rec[:, 0], e_ref, rtol=1e-9, atol=0)

@@ -39,14 +39,15 @@ sys.path.insert(0, str(ROOT))
 METRIC = "s to \u22642% voxel dose error: MC+denoiser vs plain MC on 1 GB300; histories/s"
 WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 materials, +-2% density jitter), "
             "120 kVp 6 mm Al + body bowtie, pitch 1.0, 40 mm collimation, 200 mm scan, 1e9 histories")
-# dram__bytes_read.sum + dram__bytes_write.sum of one full transport launch
-# (67,000,320 histories of this workload: 2.603 GB read + 1.008 GB written), from a
-# 1-pass ncu capture of the launch list.  bench.py's launches hold up to 2^26
-# histories, 0.2 % more than the captured one.
-TRAFFIC_BYTES_PER_LAUNCH = 3.61e9
-# the same for a full launch of the 512x512x400 workload (--workload torso512, gather skip
-# on): 67,000,050 histories, 10.79 GB read + 2.79 GB written
-TRAFFIC_BYTES_PER_LAUNCH_512 = 13.58e9
+# dram__bytes_read.sum + dram__bytes_write.sum per history, from 1-pass ncu captures of
+# one 67,000,320-history transport launch of this workload (2.603 GB read + 1.008 GB
+# written) and one 67,000,050-history launch of the 512x512x400 workload (gather skip
+# and two regions on: 10.71 GB + 2.79 GB).  The library's launches hold up to 2^28
+# histories; a launch's traffic is taken as these per-history figures times its
+# histories (the tallies and voxels a launch touches grow with its histories).
+TRAFFIC_BYTES_PER_HISTORY = 3.61e9 / 67_000_320
+TRAFFIC_BYTES_PER_HISTORY_512 = 13.50e9 / 67_000_050
+LAUNCH_HISTORIES = 1 << 28
 
 
 def parse():
@@ -357,15 +358,15 @@ def run_ours(args):
     reads = sum(s["n_voxel_reads"] for s in stats)
     crossings = sum(s["n_crossings"] for s in stats)
     deposits = sum(s["n_photo"] + s["n_compton"] + s["n_cutoff"] for s in stats)
-    chunk = 1 << 26
-    launches_per_step = -(-hist // chunk)
+    launches_per_step = -(-hist // LAUNCH_HISTORIES)
     cells = sum(s["n_cell_reads"] for s in stats)
     alg_bytes = algorithmic_bytes(reads, cells, crossings, deposits)
     hbm, peak_kind = peaks()
     achieved = alg_bytes / (kernel_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "peak_source": peak_kind,
-            "traffic": None if c1 else (TRAFFIC_BYTES_PER_LAUNCH_512 if big else TRAFFIC_BYTES_PER_LAUNCH),
+            "traffic": None if c1 else (TRAFFIC_BYTES_PER_HISTORY_512 if big else TRAFFIC_BYTES_PER_HISTORY)
+            * hist / launches_per_step,
             "alg_bytes_per_launch": alg_bytes / (args.steps * launches_per_step),
             "kernel_ms_per_launch": kernel_ms / (args.steps * launches_per_step),
             "visits_per_history": visits / done, "voxel_reads_per_history": reads / done,
@@ -569,7 +570,8 @@ def run_batch(args):
         "config": {"workload": BATCH_WORKLOAD, "jobs": len(specs), "histories_per_step": total,
                    "voxels": int(sum(int(np.prod(sp["dims"])) for sp in specs)), "tracking": args.tracking,
                    "l2": "256 MB buffer written before every step; tallies 14 GB > L2",
-                   "launch": "CUDA graph (counter reset + one persistent kernel) replayed per step"},
+                   "launch": "CUDA graph replayed per step: counter reset + one single-job persistent launch per "
+                             "job on 4 streams (a job's blocks take the SMs another job's tail frees)"},
         "autotune": {"block_size": tuned.block_size, "interact_batch": tuned.interact_batch,
                      "refill_batch": tuned.refill_batch, "woodcock_steps": tuned.woodcock_steps,
                      "trial_histories_per_s": tuned_rate, "seconds": t_tune,
@@ -578,7 +580,10 @@ def run_batch(args):
                        "path": "one dxmcg_transport_run per job"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": peak_kind, "traffic": None, "kernel_ms_per_launch": kernel_ms / args.steps},
-        "setup_s": t_setup, "gpu_launches": args.steps, "clocks": clk,
+        # jobs averaging 2^21 histories or more run one single-job launch each in the
+        # graph; smaller ones one shared-queue launch (the library's rule)
+        "setup_s": t_setup, "gpu_launches": args.steps * (len(specs) if total >= (1 << 21) * len(specs) else 1),
+        "clocks": clk,
     }
     print(json.dumps(line), flush=True)
     batch.close()

@@ -79,7 +79,11 @@ struct DeviceBuffer {
 };
 
 constexpr double kKeVToMilliGrayGram = 1.602176634e-10; // mGy * g per keV
-constexpr int kDefaultChunkLog2 = 26;
+// histories per launch by default (progress and cancel act between launches): 2^28 is
+// about 75 ms on the 256x256x200 torso.  Each launch boundary costs the persistent
+// kernel's tail, about 0.23 ms there: one launch per 2^26 histories measured 283.0 ms
+// per 1e9 histories, per 2^28 280.5 ms, one launch 279.8 ms.
+constexpr int kDefaultChunkLog2 = 28;
 
 // per-beam device inputs of one job
 struct JobBuffers {
@@ -334,9 +338,25 @@ int deviceErrors(const DevCounters& c, const char* what)
 
 // Several (world, beam) jobs run by one persistent launch over a shared history
 // queue; the launch (counter reset + kernel) is a CUDA graph replayed by each run.
+// Batches run in one of two ways, both captured once as a CUDA graph and replayed.
+// Per job (when the jobs average at least kPerJobHistories): each job is one launch
+// of the single-job kernel, on kBatchStreams streams, so that one job's blocks take
+// the SMs another job's tail frees.  Shared queue (smaller jobs): one launch of the
+// batch kernel over the concatenated history ranges, whose per-lane job descriptors
+// cost about 5 % per history against the single-job kernel.
+constexpr uint64_t kPerJobHistories = 1ull << 21;
+constexpr int kBatchStreams = 4;
+
 struct dxmcg_batch {
     int device = 0;
     int tracking = DXMCG_TRACK_WOODCOCK;
+    bool perJob = false;
+    std::vector<DevJob> hostJobs;
+    std::vector<LaunchShape> jobShapes;
+    DeviceBuffer<DevCounters> jobCounters;
+    cudaStream_t side[kBatchStreams] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kBatchStreams] = {};
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<dxmcg_world*> worlds;
@@ -368,10 +388,41 @@ struct dxmcg_batch {
             cudaEventDestroy(ev0);
         if (ev1)
             cudaEventDestroy(ev1);
+        if (fork)
+            cudaEventDestroy(fork);
+        for (int k = 0; k < kBatchStreams; ++k) {
+            if (join[k])
+                cudaEventDestroy(join[k]);
+            if (side[k])
+                cudaStreamDestroy(side[k]);
+        }
         if (stream)
             cudaStreamDestroy(stream);
     }
 };
+
+namespace {
+void addCounters(DevCounters& a, const DevCounters& b)
+{
+    a.histories += b.histories;
+    a.missed += b.missed;
+    a.visits += b.visits;
+    a.photo += b.photo;
+    a.compton += b.compton;
+    a.rayleigh += b.rayleigh;
+    a.cutoff += b.cutoff;
+    a.errors += b.errors;
+    a.interacted += b.interacted;
+    a.crossings += b.crossings;
+    a.fluorescence += b.fluorescence;
+    a.e_source += b.e_source;
+    a.e_escaped += b.e_escaped;
+    a.e_deposited += b.e_deposited;
+    a.error_flags |= b.error_flags;
+    a.skipped += b.skipped;
+    a.outer += b.outer;
+}
+} // namespace
 
 // the segmentation kernel's per-voxel arithmetic, on the host (no contraction into
 // fused multiply-adds: the library's host code is compiled with -ffp-contract=off)
@@ -1127,6 +1178,18 @@ DXMCG_API int dxmcg_batch_create(int n_jobs, dxmcg_world* const* worlds, const d
         if (kernelTracking(J[j]) == kTrackWoodcockBox)
             b->tracking = kTrackWoodcockBox;
     b->shape = chooseShape(worlds[0], opts[0], b->tracking, true);
+    b->perJob = b->total >= kPerJobHistories * static_cast<uint64_t>(n_jobs);
+    if (b->perJob) {
+        b->hostJobs = J;
+        for (int j = 0; j < n_jobs; ++j)
+            b->jobShapes.push_back(chooseShape(worlds[j], opts[j], kernelTracking(J[j])));
+        DXMCG_CUDA(b->jobCounters.alloc(n_jobs));
+        DXMCG_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        for (int k = 0; k < kBatchStreams; ++k) {
+            DXMCG_CUDA(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
+            DXMCG_CUDA(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+        }
+    }
     *out = b.release();
     return DXMCG_OK;
 }
@@ -1153,12 +1216,31 @@ DXMCG_API int dxmcg_batch_run(dxmcg_batch* b, dxmcg_stats* stats)
     if (!b)
         return fail(DXMCG_ERR_ARGUMENT, "batch_run: null batch");
     DXMCG_CUDA(cudaSetDevice(b->device));
+    const int nJobs = static_cast<int>(b->worlds.size());
     if (!b->exec) {
         DXMCG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = cudaMemsetAsync(b->counters.p, 0, sizeof(DevCounters), b->stream);
-        if (e == cudaSuccess)
-            e = launchTransportBatch(b->tracking, b->jobs.p, b->offsets.p, static_cast<int>(b->worlds.size()),
-                b->total, b->counters.p, b->shape, b->stream);
+        cudaError_t e = cudaSuccess;
+        if (b->perJob) {
+            // fork to the side streams, one launch per job round-robin, join
+            e = cudaMemsetAsync(b->jobCounters.p, 0, nJobs * sizeof(DevCounters), b->stream);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(b->fork, b->stream);
+            for (int k = 0; k < kBatchStreams && e == cudaSuccess; ++k)
+                e = cudaStreamWaitEvent(b->side[k], b->fork, 0);
+            for (int j = 0; j < nJobs && e == cudaSuccess; ++j)
+                e = launchTransport(b->hostJobs[j], b->nHist[j], b->jobCounters.p + j, b->jobShapes[j],
+                    b->side[j % kBatchStreams]);
+            for (int k = 0; k < kBatchStreams && e == cudaSuccess; ++k) {
+                e = cudaEventRecord(b->join[k], b->side[k]);
+                if (e == cudaSuccess)
+                    e = cudaStreamWaitEvent(b->stream, b->join[k], 0);
+            }
+        } else {
+            e = cudaMemsetAsync(b->counters.p, 0, sizeof(DevCounters), b->stream);
+            if (e == cudaSuccess)
+                e = launchTransportBatch(b->tracking, b->jobs.p, b->offsets.p, nJobs, b->total, b->counters.p,
+                    b->shape, b->stream);
+        }
         cudaGraph_t g = nullptr;
         const cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
         if (e != cudaSuccess || ee != cudaSuccess) {
@@ -1173,8 +1255,17 @@ DXMCG_API int dxmcg_batch_run(dxmcg_batch* b, dxmcg_stats* stats)
     DXMCG_CUDA(cudaGraphLaunch(b->exec, b->stream));
     DXMCG_CUDA(cudaEventRecord(b->ev1, b->stream));
     DevCounters c {};
-    DXMCG_CUDA(cudaMemcpyAsync(&c, b->counters.p, sizeof(c), cudaMemcpyDeviceToHost, b->stream));
-    DXMCG_CUDA(cudaStreamSynchronize(b->stream));
+    if (b->perJob) {
+        std::vector<DevCounters> each(nJobs);
+        DXMCG_CUDA(cudaMemcpyAsync(each.data(), b->jobCounters.p, nJobs * sizeof(DevCounters),
+            cudaMemcpyDeviceToHost, b->stream));
+        DXMCG_CUDA(cudaStreamSynchronize(b->stream));
+        for (const auto& x : each)
+            addCounters(c, x);
+    } else {
+        DXMCG_CUDA(cudaMemcpyAsync(&c, b->counters.p, sizeof(c), cudaMemcpyDeviceToHost, b->stream));
+        DXMCG_CUDA(cudaStreamSynchronize(b->stream));
+    }
     float ms = 0.0f;
     DXMCG_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     for (size_t j = 0; j < b->worlds.size(); ++j)

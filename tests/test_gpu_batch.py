@@ -100,6 +100,42 @@ def test_batch_graph_replay(gpu, jobs):
     batch.close()
 
 
+def test_per_job_batch_matches_single_runs_and_replays(gpu):
+    """Jobs of 2.1e6 histories or more on average run as one single-job launch each,
+    on several streams of the captured graph: the same kernel and streams as
+    dxmcg_transport_run, so counts equal the single runs exactly and energies up to the
+    order of FP64 atomics.  Two jobs share one world; a replay doubles the tallies."""
+    phs = [P.ellipsoid_phantom((40, 36, 30), (0.3, 0.3, 0.3), seed=s) for s in (1, 2)]
+    beams = [P.dx_beam_params(kvp=80.0, field_cm=10.0, particles=400_000, exposures=6),
+             P.cbct_params(particles=30_000, kvp=90.0),
+             P.dx_beam_params(kvp=70.0, field_cm=8.0, particles=300_000, exposures=8)]
+    plan = [(0, 0), (1, 1), (0, 2)]
+    worlds = [make_world(gpu, ph) for ph in phs]
+    opts = [gpu.run_options(seed=21 + k, stream=k) for k in range(len(plan))]
+    batch = gpu.Batch([(worlds[i], beams[b], o) for (i, b), o in zip(plan, opts)])
+    hist, _ = batch.info()
+    assert hist.sum() >= (1 << 21) * len(plan)  # the per-job path
+    sb = batch.run()
+    assert sb["n_errors"] == 0 and sb["n_histories"] == int(hist.sum())
+    alone = [make_world(gpu, ph) for ph in phs]
+    tot = {"n_histories": 0, "n_photo": 0, "n_compton": 0, "n_rayleigh": 0, "n_visits": 0}
+    for (i, b), o in zip(plan, opts):
+        s = alone[i].run(beams[b], o)
+        for k in tot:
+            tot[k] += s[k]
+    for k in tot:
+        assert sb[k] == tot[k], k
+    for wb, wa in zip(worlds, alone):
+        e1, _, c1 = wb.tally()
+        e2, _, c2 = wa.tally()
+        np.testing.assert_array_equal(c1, c2)
+        np.testing.assert_allclose(e1, e2, rtol=1e-9, atol=1e-9)
+    batch.run()
+    for wb, wa in zip(worlds, alone):
+        np.testing.assert_array_equal(wb.tally()[2], 2 * wa.tally()[2])
+    batch.close()
+
+
 def test_batch_rejects_bad_jobs(gpu, jobs):
     phantoms, plan = jobs
     w = make_world(gpu, phantoms[0])

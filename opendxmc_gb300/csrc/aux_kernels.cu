@@ -270,14 +270,18 @@ namespace {
     }
 
     __global__ void rayleighKernel(int n, const float* __restrict__ E, const DevMaterial* __restrict__ M,
-        const float* __restrict__ u, int stride, float* __restrict__ co, int* __restrict__ used)
+        const float* __restrict__ rtab, const float* __restrict__ u, int stride, float* __restrict__ co,
+        int* __restrict__ used)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
         if (i >= n)
             return;
         InjectedUniforms r { u + static_cast<size_t>(i) * stride, stride, 0 };
         unsigned err = 0;
-        co[i] = sampleRayleigh(E[i], M, r, err);
+        int ie;
+        float fe;
+        gridPos(E[i], ie, fe);
+        co[i] = sampleRayleigh(E[i], M, rtab, ie, fe, r, err);
         used[i] = r.used;
     }
 
@@ -415,10 +419,10 @@ cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const
     return cudaGetLastError();
 }
 
-cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* u, int stride,
-    float* cos_out, int* used, cudaStream_t s)
+cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* rtab, const float* u,
+    int stride, float* cos_out, int* used, cudaStream_t s)
 {
-    rayleighKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, u, stride, cos_out, used);
+    rayleighKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, rtab, u, stride, cos_out, used);
     return cudaGetLastError();
 }
 

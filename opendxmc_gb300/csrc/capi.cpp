@@ -129,6 +129,7 @@ struct dxmcg_world {
     DeviceBuffer<float> maj;
     DeviceBuffer<DevMaterial> mats;
     DeviceBuffer<float> stab; // Compton S(t) / Z_sum per material
+    DeviceBuffer<float> rtab; // Rayleigh cumulative element shares per material and energy
     DeviceBuffer<DevCounters> counters;
     DeviceBuffer<unsigned> scratch; // rho max bits [256] + error word
     JobBuffers job; // exposures, spectra, bowtie of the last transport_run
@@ -257,6 +258,7 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
     J.maj = w->maj.p;
     J.mats = w->mats.p;
     J.stab = w->stab.p;
+    J.rtab = w->rtab.p;
     J.tally = w->tally.p;
     J.exps = jb->exps.p;
     J.spec = jb->spec.p;
@@ -864,6 +866,10 @@ DXMCG_API int dxmcg_world_build(dxmcg_world* w)
     std::vector<float> stab(static_cast<size_t>(M) * kSTabN);
     buildComptonTables(w->materials.data(), M, stab.data());
     DXMCG_CUDA(cudaMemcpyAsync(w->stab.p, stab.data(), stab.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    std::vector<float> rtab(static_cast<size_t>(M) * kNE * kRTabWidth);
+    buildRayleighTables(w->materials.data(), M, rtab.data());
+    DXMCG_CUDA(w->rtab.alloc(rtab.size()));
+    DXMCG_CUDA(cudaMemcpyAsync(w->rtab.p, rtab.data(), rtab.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(cudaMemsetAsync(w->tally.p, 0, w->N * sizeof(Tally), w->stream));
     // gather-skip bounds of the Woodcock step
     {
@@ -1799,7 +1805,12 @@ DXMCG_API int dxmcg_sample_rayleigh(int n, const double* energies, const dxmcg_m
         return rc;
     DXMCG_CUDA(co.alloc(n));
     DXMCG_CUDA(us.alloc(n));
-    cudaError_t e = launchSampleRayleigh(n, E.p, M.p, U.p, u_stride, co.p, us.p, nullptr);
+    std::vector<float> rtabHost(static_cast<size_t>(kNE) * kRTabWidth);
+    buildRayleighTables(m, 1, rtabHost.data());
+    DeviceBuffer<float> rtab;
+    DXMCG_CUDA(rtab.alloc(rtabHost.size()));
+    DXMCG_CUDA(cudaMemcpy(rtab.p, rtabHost.data(), sizeof(float) * rtabHost.size(), cudaMemcpyHostToDevice));
+    cudaError_t e = launchSampleRayleigh(n, E.p, M.p, rtab.p, U.p, u_stride, co.p, us.p, nullptr);
     if (e != cudaSuccess)
         return cudaFail(e, "rayleigh kernel");
     std::vector<float> b(n);

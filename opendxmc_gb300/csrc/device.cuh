@@ -247,31 +247,33 @@ namespace dev {
 
     // Rayleigh scattering: element i with probability n_i Z_i^2 a_i c_i(T), then
     // t = x^2 from F^2 by inversion, t = a ((1 - y)^(-1/3) - 1) with y = r2 c_i, and
-    // rejection on (1 + cos^2) / 2.  The inversion is evaluated as
+    // rejection on (1 + cos^2) / 2.  The element is the first whose cumulative share,
+    // interpolated from the material's table rtab at the photon's energy-grid position
+    // (ie, fe), reaches r1: at most 9e-5 from the exact shares in soft tissue, so the
+    // choice differs from the exact sum's for a few uniforms in 1e4.  The inversion is evaluated as
     // a y / (om (s^2 + s + 1)) with om = 1 - y and s = om^(-1/3): that is a (s - 1), since
     // s^3 - 1 = y / om, with no cancellation when y is small.  For y >= 1/2, om is formed
     // as (1 - r2) + r2 (1 + T/a)^-3 (1 - r2 is exact) so FP32 keeps its precision.
     template <class U>
-    __device__ float sampleRayleigh(float E, const DevMaterial* __restrict__ M, U& r, unsigned& err)
+    __device__ float sampleRayleigh(float E, const DevMaterial* __restrict__ M, const float* __restrict__ rtab,
+        int ie, float fe, U& r, unsigned& err)
     {
         const float q = E * kInvHc;
         const float T = q * q;
         const int n = M->n;
-        float Gs = 0.0f;
-        for (int i = 0; i < n; ++i)
-            Gs += __ldg(&M->nZ2[i]) * __ldg(&M->a[i]) * formFactorIntegral(T * __ldg(&M->ia[i]));
+        const float* c0 = rtab + ie * kRTabWidth;
         for (int guard = 0; guard < kMaxRejections; ++guard) {
             const float r1 = r.u(), r2 = r.u(), r3 = r.u();
-            const float target = r1 * Gs;
-            float acc = 0.0f, a = 0.0f, ia = 0.0f, c = 0.0f;
-            for (int i = 0; i < n; ++i) {
-                a = __ldg(&M->a[i]);
-                ia = __ldg(&M->ia[i]);
-                c = formFactorIntegral(T * ia);
-                acc += __ldg(&M->nZ2[i]) * a * c;
-                if (target <= acc)
+            int e = n - 1;
+            for (int i = 0; i < n - 1; ++i) {
+                const float lo = __ldg(c0 + i), hi = __ldg(c0 + kRTabWidth + i);
+                if (r1 <= fmaf(fe, hi - lo, lo)) {
+                    e = i;
                     break;
+                }
             }
+            const float a = __ldg(&M->a[e]), ia = __ldg(&M->ia[e]);
+            const float c = formFactorIntegral(T * ia);
             const float y = r2 * c;
             float om;
             if (y < 0.5f) {

@@ -35,6 +35,10 @@ constexpr int kMaxRejections = 100000;
 constexpr int kSTabPerOctave = 32;
 constexpr int kSTabMinLog2 = -16;
 constexpr int kSTabN = 24 * kSTabPerOctave + 1;
+// Rayleigh element choice: per material and table energy E_i, the cumulative shares
+// C_k = sum_{j<=k} G_j / sum_j G_j of the elements' form-factor integrals G_j (k < n;
+// entries k >= n - 1 hold 1), interpolated linearly in E between table energies.
+constexpr int kRTabWidth = DXMCG_MAX_ELEMENTS;
 
 struct DevMaterial {
     int n;
@@ -112,6 +116,7 @@ struct DevJob {
     const float* maj;
     const DevMaterial* mats;
     const float* stab; // [n_mats][kSTabN] S(t) / Z_sum of each material
+    const float* rtab; // [n_mats][kTableNE][kRTabWidth] cumulative Rayleigh element shares
     int n_mats;
     int correction;
     Tally* tally;
@@ -216,8 +221,8 @@ cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const
 // B N x 16 (N = 16 or 32) bf16 row-major, D FP32 [128][N]; *status |= 1 on a timed-out wait
 cudaError_t launchUmmaProbe(const uint16_t* A, const uint16_t* B0, const uint16_t* B1, int N, float* D0, float* D1,
     unsigned* status, cudaStream_t s);
-cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* u, int stride,
-    float* cos_out, int* used, cudaStream_t s);
+cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* rtab, const float* u,
+    int stride, float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s);
 cudaError_t launchHistoryStream(uint32_t k0, uint32_t k1, uint32_t stream, unsigned long long h0, int n_hist,
     int n_draws, uint32_t* out, cudaStream_t s);

@@ -162,6 +162,32 @@ void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const 
         maj[i] = static_cast<float>(std::max(mx[i] * kMajorantSafety, 1e-30));
 }
 
+void buildRayleighTables(const dxmcg_material* mats, int M, float* out)
+{
+    constexpr double kHcKeVA = 12.398419843; // keV * Angstrom
+    for (int m = 0; m < M; ++m) {
+        const auto s = samplingElements(mats[m]);
+        for (int i = 0; i < kNE; ++i) {
+            const double E = kEmin + i * kDE;
+            const double T = (E / kHcKeVA) * (E / kHcKeVA);
+            double G[kRTabWidth] = {};
+            double sum = 0.0;
+            for (int k = 0; k < s.n; ++k) {
+                const double x = T / s.a[k];
+                const double b = 1.0 + x;
+                G[k] = s.nZ2[k] * s.a[k] * (x * (3.0 + x * (3.0 + x)) / (b * b * b));
+                sum += G[k];
+            }
+            float* row = out + (static_cast<size_t>(m) * kNE + i) * kRTabWidth;
+            double acc = 0.0;
+            for (int k = 0; k < kRTabWidth; ++k) {
+                acc += G[k];
+                row[k] = k + 1 >= s.n || !(sum > 0.0) ? 1.0f : static_cast<float>(acc / sum);
+            }
+        }
+    }
+}
+
 void buildBackgroundMajorant(const float* tot0, double rho0, float* out)
 {
     for (int i = 0; i < kNE; ++i)

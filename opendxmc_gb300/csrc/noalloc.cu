@@ -7,10 +7,10 @@
 // between its set-up phase and its runs.  They own every input and output array
 // and pass device pointers; everything else this path needs -- the work-queue head
 // and run statistics, the validation flags and per-material maximum densities,
-// the attenuation tables and majorants, the Compton S(t) tables, the two-region box,
-// the exposure list, the spectra and the bowtie profiles -- lives in one file-scope
-// __device__ array of kScratchBytes = 512 KiB.  Every GPU that loads the library
-// holds that array until the process exits.
+// the attenuation tables and majorants, the Compton S(t) and Rayleigh share tables,
+// the two-region box, the exposure list, the spectra and the bowtie profiles -- lives
+// in one file-scope __device__ array of kScratchBytes = 1 MiB.  Every GPU that loads
+// the library holds that array until the process exits.
 //
 // The host finds the array's device address with cudaGetSymbolAddress, once per
 // device, with that device current, on the first call made on that device.  Every
@@ -41,7 +41,7 @@
 namespace dxmcg {
 namespace {
 
-    constexpr size_t kScratchBytes = 512u * 1024u;
+    constexpr size_t kScratchBytes = 1024u * 1024u;
     constexpr int kMaxMaterials = 16;
     constexpr int kMaxExposures = 4096;
     constexpr int kMaxDevices = 64;
@@ -61,7 +61,8 @@ namespace {
     constexpr size_t kOffXs = alignUp(kOffTot + kMaxMaterials * kTableNE * sizeof(float));
     constexpr size_t kOffExps = alignUp(kOffXs + kMaxMaterials * kTableNE * sizeof(float4));
     constexpr size_t kOffSTab = alignUp(kOffExps + kMaxExposures * sizeof(DevExposure));
-    constexpr size_t kOffBox = alignUp(kOffSTab + kMaxMaterials * kSTabN * sizeof(float)); // 6 ints
+    constexpr size_t kOffRTab = alignUp(kOffSTab + kMaxMaterials * kSTabN * sizeof(float));
+    constexpr size_t kOffBox = alignUp(kOffRTab + kMaxMaterials * kTableNE * kRTabWidth * sizeof(float)); // 6 ints
     constexpr size_t kOffMajOut = alignUp(kOffBox + 6 * sizeof(int));
     constexpr size_t kUsed = kOffMajOut + kTableNE * sizeof(float);
     static_assert(kUsed <= kScratchBytes, "scratch layout exceeds the static array");
@@ -244,6 +245,9 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     std::vector<float> stab(static_cast<size_t>(n_materials) * kSTabN);
     buildComptonTables(materials, n_materials, stab.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffSTab, stab.data(), stab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    std::vector<float> rtab(static_cast<size_t>(n_materials) * kTableNE * kRTabWidth);
+    buildRayleighTables(materials, n_materials, rtab.data());
+    NOALLOC_CUDA(cudaMemcpyAsync(base + kOffRTab, rtab.data(), rtab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMaj, maj.data(), maj.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     const bool twoRegion = woodcock && twoRegionBox(hostBox, dims);
     std::vector<float> majOut(kTableNE);
@@ -274,6 +278,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     J.tot = reinterpret_cast<const float*>(base + kOffTot);
     J.xs = reinterpret_cast<const float4*>(base + kOffXs);
     J.stab = reinterpret_cast<const float*>(base + kOffSTab);
+    J.rtab = reinterpret_cast<const float*>(base + kOffRTab);
     J.maj = reinterpret_cast<const float*>(base + kOffMaj);
     J.mats = reinterpret_cast<const DevMaterial*>(base + kOffMats);
     J.tally = reinterpret_cast<Tally*>(device_tally);

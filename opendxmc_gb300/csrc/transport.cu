@@ -605,7 +605,8 @@ namespace {
                 if (compton)
                     Ep = sampleCompton(ph.E, J.mats + pm, J.stab + pm * kSTabN, J.correction, rng, cost, err);
                 else if (rayleigh)
-                    cost = sampleRayleigh(ph.E, J.mats + pm, rng, err);
+                    cost = sampleRayleigh(ph.E, J.mats + pm, J.rtab + pm * (kTableNE * kRTabWidth), ec.ie, ec.fe,
+                        rng, err);
                 if (compton || rayleigh)
                     scatterDirection(ph.dx, ph.dy, ph.dz, cost, rng.u());
                 if (compton) {

@@ -255,7 +255,7 @@ namespace {
     }
 
     __global__ void comptonKernel(int n, const float* __restrict__ E, const DevMaterial* __restrict__ M,
-        const float* __restrict__ stab, int correction, const float* __restrict__ u, int stride,
+        const float* __restrict__ ctab, int correction, const float* __restrict__ u, int stride,
         float* __restrict__ eo, float* __restrict__ co, int* __restrict__ used)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -264,7 +264,10 @@ namespace {
         InjectedUniforms r { u + static_cast<size_t>(i) * stride, stride, 0 };
         unsigned err = 0;
         float cost;
-        eo[i] = sampleCompton(E[i], M, stab, correction, r, cost, err);
+        int ie;
+        float fe;
+        gridPos(E[i], ie, fe);
+        eo[i] = sampleCompton(E[i], M, ctab, ie, fe, correction, r, cost, err);
         co[i] = cost;
         used[i] = r.used;
     }
@@ -405,10 +408,10 @@ cudaError_t launchHistoryStream(uint32_t k0, uint32_t k1, uint32_t stream, unsig
     return cudaGetLastError();
 }
 
-cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, const float* stab, int correction,
+cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, const float* ctab, int correction,
     const float* u, int stride, float* e_out, float* cos_out, int* used, cudaStream_t s)
 {
-    comptonKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, stab, correction, u, stride, e_out, cos_out, used);
+    comptonKernel<<<(n + 127) / 128, 128, 0, s>>>(n, E, m, ctab, correction, u, stride, e_out, cos_out, used);
     return cudaGetLastError();
 }
 

@@ -128,7 +128,7 @@ struct dxmcg_world {
     DeviceBuffer<float4> xs;
     DeviceBuffer<float> maj;
     DeviceBuffer<DevMaterial> mats;
-    DeviceBuffer<float> stab; // Compton S(t) / Z_sum per material
+    DeviceBuffer<float> ctab; // Compton angle quantiles per material and energy
     DeviceBuffer<float> rtab; // Rayleigh cumulative element shares per material and energy
     DeviceBuffer<DevCounters> counters;
     DeviceBuffer<unsigned> scratch; // rho max bits [256] + error word
@@ -257,7 +257,7 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
     J.xs = w->xs.p;
     J.maj = w->maj.p;
     J.mats = w->mats.p;
-    J.stab = w->stab.p;
+    J.ctab = w->ctab.p;
     J.rtab = w->rtab.p;
     J.tally = w->tally.p;
     J.exps = jb->exps.p;
@@ -856,16 +856,16 @@ DXMCG_API int dxmcg_world_build(dxmcg_world* w)
     DXMCG_CUDA(w->xs.alloc(xs.size()));
     DXMCG_CUDA(w->maj.alloc(kNE));
     DXMCG_CUDA(w->mats.alloc(M));
-    DXMCG_CUDA(w->stab.alloc(static_cast<size_t>(M) * kSTabN));
     DXMCG_CUDA(w->counters.alloc(1));
     DXMCG_CUDA(w->tally.alloc(w->N));
     DXMCG_CUDA(cudaMemcpyAsync(w->tot.p, tot.data(), tot.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(cudaMemcpyAsync(w->xs.p, xs.data(), xs.size() * sizeof(float4), cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(cudaMemcpyAsync(w->maj.p, majf.data(), kNE * sizeof(float), cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(cudaMemcpyAsync(w->mats.p, dm.data(), M * sizeof(DevMaterial), cudaMemcpyHostToDevice, w->stream));
-    std::vector<float> stab(static_cast<size_t>(M) * kSTabN);
-    buildComptonTables(w->materials.data(), M, stab.data());
-    DXMCG_CUDA(cudaMemcpyAsync(w->stab.p, stab.data(), stab.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    std::vector<float> ctab(static_cast<size_t>(M) * kNE * kCTabK);
+    buildComptonAngleTables(w->materials.data(), M, w->correction, ctab.data());
+    DXMCG_CUDA(w->ctab.alloc(ctab.size()));
+    DXMCG_CUDA(cudaMemcpyAsync(w->ctab.p, ctab.data(), ctab.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
     std::vector<float> rtab(static_cast<size_t>(M) * kNE * kRTabWidth);
     buildRayleighTables(w->materials.data(), M, rtab.data());
     DXMCG_CUDA(w->rtab.alloc(rtab.size()));
@@ -1745,12 +1745,12 @@ DXMCG_API int dxmcg_sample_compton(int n, const double* energies, const dxmcg_ma
     DXMCG_CUDA(eo.alloc(n));
     DXMCG_CUDA(co.alloc(n));
     DXMCG_CUDA(us.alloc(n));
-    std::vector<float> stabHost(kSTabN);
-    buildComptonTables(m, 1, stabHost.data());
-    DeviceBuffer<float> stab;
-    DXMCG_CUDA(stab.alloc(kSTabN));
-    DXMCG_CUDA(cudaMemcpy(stab.p, stabHost.data(), sizeof(float) * kSTabN, cudaMemcpyHostToDevice));
-    cudaError_t e = launchSampleCompton(n, E.p, M.p, stab.p, correction, U.p, u_stride, eo.p, co.p, us.p, nullptr);
+    std::vector<float> ctabHost(static_cast<size_t>(kNE) * kCTabK);
+    buildComptonAngleTables(m, 1, correction, ctabHost.data());
+    DeviceBuffer<float> ctab;
+    DXMCG_CUDA(ctab.alloc(ctabHost.size()));
+    DXMCG_CUDA(cudaMemcpy(ctab.p, ctabHost.data(), sizeof(float) * ctabHost.size(), cudaMemcpyHostToDevice));
+    cudaError_t e = launchSampleCompton(n, E.p, M.p, ctab.p, correction, U.p, u_stride, eo.p, co.p, us.p, nullptr);
     if (e != cudaSuccess)
         return cudaFail(e, "compton kernel");
     std::vector<float> a(n), b(n);

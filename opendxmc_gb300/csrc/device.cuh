@@ -174,54 +174,34 @@ namespace dev {
         return false;
     }
 
-    // S(t) / Z_sum from the material's table (linear in log2 t; proportional to t below
-    // the first node, whose value is stab[0])
-    __device__ __forceinline__ float comptonS(const float* __restrict__ stab, float t)
+    // 1 - cos theta of a Compton scattering from the material's quantile table (row ie
+    // of ctab, interpolated towards row ie + 1 by fe, at the same probability): one
+    // uniform, no rejection.  The table's probability grid u_j = 1 - (1 - j/(K-1))^2 is
+    // inverted by j = (K - 1)(1 - sqrt(1 - u)).
+    __device__ __forceinline__ float comptonOneMinusCos(const float* __restrict__ ctab, int ie, float fe, float u)
     {
-        const float x = (__log2f(t) - static_cast<float>(kSTabMinLog2)) * static_cast<float>(kSTabPerOctave);
-        if (!(x > 0.0f))
-            return __ldg(stab) * t * 65536.0f; // t / 2^kSTabMinLog2
-        const float xc = fminf(x, static_cast<float>(kSTabN - 1));
-        const int i = min(static_cast<int>(xc), kSTabN - 2);
-        const float f = xc - static_cast<float>(i);
-        const float a = __ldg(stab + i);
-        const float b = __ldg(stab + i + 1);
-        return fmaf(f, b - a, a);
+        const float jf = static_cast<float>(kCTabK - 1) * (1.0f - sqrtf(1.0f - u));
+        const int j = min(static_cast<int>(jf), kCTabK - 2);
+        const float g = jf - static_cast<float>(j);
+        const float* a = ctab + ie * kCTabK + j;
+        const float a0 = __ldg(a), a1 = __ldg(a + 1);
+        const float b0 = __ldg(a + kCTabK), b1 = __ldg(a + kCTabK + 1);
+        const float lo = fmaf(g, a1 - a0, a0);
+        const float hi = fmaf(g, b1 - b0, b0);
+        return fmaf(fe, hi - lo, lo);
     }
 
+    // Compton scattering: the angle from the Klein-Nishina x S table, E' from the
+    // Compton relation (correction 0 and 1), or Doppler-broadened by a bound electron's
+    // momentum (correction 2, which may send the draw back for a new angle).
     template <class U>
-    __device__ float sampleCompton(float E, const DevMaterial* __restrict__ M, const float* __restrict__ stab,
-        int correction, U& r, float& cost, unsigned& err)
+    __device__ float sampleCompton(float E, const DevMaterial* __restrict__ M, const float* __restrict__ ctab,
+        int ie, float fe, int correction, U& r, float& cost, unsigned& err)
     {
-        // reciprocals instead of IEEE divisions (a unit in the last place at most apart;
-        // the rejection tests are insensitive to it)
         const float k = E * (1.0f / kMeKeV);
-        const float ik = __frcp_rn(k);
-        const float kk = 2.0f * k;
         for (int guard = 0; guard < kMaxRejections; ++guard) {
-            const float r1 = r.u(), r2 = r.u(), r3 = r.u();
-            float xm1;
-            bool acc;
-            if (r1 * (9.0f + kk) <= 1.0f + kk) {
-                xm1 = kk * r2;
-                const float x = 1.0f + xm1;
-                acc = r3 * x * x <= 4.0f * xm1;
-            } else {
-                xm1 = kk * (1.0f - r2) * __frcp_rn(fmaf(kk, r2, 1.0f));
-                const float x = 1.0f + xm1;
-                const float mu = 1.0f - xm1 * ik;
-                acc = 2.0f * r3 <= mu * mu + 1.0f / x;
-            }
-            if (!acc)
-                continue;
-            const float omu = xm1 * ik;
-            if (correction >= 1) {
-                const float q = E * kInvHc;
-                const float t = q * q * 0.5f * omu;
-                const float r4 = r.u();
-                if (r4 > comptonS(stab, t))
-                    continue;
-            }
+            const float omu = comptonOneMinusCos(ctab, ie, fe, r.u());
+            const float xm1 = k * omu;
             cost = 1.0f - omu;
             if (correction >= 2) {
                 float Ep;

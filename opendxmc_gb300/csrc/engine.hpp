@@ -28,17 +28,15 @@ constexpr int kMaxBowtie = 64;
 constexpr int kTableNE = DXMCG_NE;
 constexpr uint32_t kMaxStepsPerHistory = 1000000;
 constexpr int kMaxRejections = 100000;
-// Compton rejection on the incoherent scattering function: per material S(t) / Z_sum
-// at t = 2^(kSTabMinLog2 + i / kSTabPerOctave) 1/A^2 (t = x^2 = q^2 (1 - cos) / 2),
-// i = 0 .. kSTabN - 1, interpolated linearly in log2 t; S is proportional to t below
-// the first node.  24 octaves reach t = 256, beyond q^2 = 147 at 150.5 keV.
-constexpr int kSTabPerOctave = 32;
-constexpr int kSTabMinLog2 = -16;
-constexpr int kSTabN = 24 * kSTabPerOctave + 1;
 // Rayleigh element choice: per material and table energy E_i, the cumulative shares
 // C_k = sum_{j<=k} G_j / sum_j G_j of the elements' form-factor integrals G_j (k < n;
 // entries k >= n - 1 hold 1), interpolated linearly in E between table energies.
 constexpr int kRTabWidth = DXMCG_MAX_ELEMENTS;
+// Compton angle: per material and table energy E_i, 1 - cos theta at the cumulative
+// probabilities u_j = 1 - (1 - j / (kCTabK - 1))^2 of the Klein-Nishina x S(x) / Z
+// distribution (S = 1 at correction 0), j = 0 .. kCTabK - 1: 2 at j = 0, 0 at the last.
+// The u grid is densest towards cos theta = 1, where S changes fastest.
+constexpr int kCTabK = 256;
 
 struct DevMaterial {
     int n;
@@ -115,8 +113,8 @@ struct DevJob {
     const float4* xs;
     const float* maj;
     const DevMaterial* mats;
-    const float* stab; // [n_mats][kSTabN] S(t) / Z_sum of each material
     const float* rtab; // [n_mats][kTableNE][kRTabWidth] cumulative Rayleigh element shares
+    const float* ctab; // [n_mats][kTableNE][kCTabK] Compton 1 - cos theta quantiles
     int n_mats;
     int correction;
     Tally* tally;
@@ -213,7 +211,7 @@ cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, do
 cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int ny, int nz, float sx, float sy,
     float sz, int cap, long long* idx, float* len, int* cnt, cudaStream_t s);
 cudaError_t launchPhilox(int n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t s);
-cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, const float* stab, int correction,
+cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, const float* ctab, int correction,
     const float* u, int stride, float* e_out, float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const float* u, int stride, float* e_out,
     float* dz_out, int* used, cudaStream_t s);

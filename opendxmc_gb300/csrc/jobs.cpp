@@ -126,23 +126,6 @@ DevMaterial toDevMaterial(const dxmcg_material& m)
     return d;
 }
 
-void buildComptonTables(const dxmcg_material* mats, int M, float* out)
-{
-    for (int m = 0; m < M; ++m) {
-        const auto s = samplingElements(mats[m]);
-        for (int k = 0; k < kSTabN; ++k) {
-            const double t = std::exp2(kSTabMinLog2 + static_cast<double>(k) / kSTabPerOctave);
-            double S = 0.0;
-            for (int i = 0; i < s.n; ++i) {
-                const double b = 1.0 + t / s.a[i];
-                const double b2 = b * b;
-                S += s.nZ[i] * (1.0 - 1.0 / (b2 * b2));
-            }
-            out[static_cast<size_t>(m) * kSTabN + k] = static_cast<float>(s.Zsum > 0 ? S / s.Zsum : 0.0);
-        }
-    }
-}
-
 void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const double* rhoMax, float* tot,
     float4* xs, float* maj, DevMaterial* dm)
 {
@@ -160,6 +143,96 @@ void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const 
     }
     for (int i = 0; i < kNE; ++i)
         maj[i] = static_cast<float>(std::max(mx[i] * kMajorantSafety, 1e-30));
+}
+
+namespace {
+    // Quantiles of 1 - cos theta for one material and correction level, all table
+    // energies.  The distribution KN(mu) S(t(mu)) / Z is integrated by the trapezoid
+    // rule on 512 equal steps of w = sqrt((1 - mu) / 2), which crowds the points
+    // towards mu = 1 where S rises (dmu = -4 w dw); each quantile is found by linear
+    // interpolation of the cumulative sum in w.  Kolmogorov distance of the sampled
+    // distribution from the exact one: about 1.5e-5 for water, 5-150 keV.
+    std::vector<float> comptonAngleRows(const dxmcg_material& mat, int correction)
+    {
+        constexpr double kMeKeV = 510.99895, kHcKeVA = 12.398419843;
+        constexpr int G = 512;
+        const auto s = samplingElements(mat);
+        std::vector<float> out(static_cast<size_t>(kNE) * kCTabK);
+        std::vector<double> cum(G + 1);
+        for (int i = 0; i < kNE; ++i) {
+            const double E = kEmin + i * kDE;
+            const double k = E / kMeKeV;
+            const double q2 = (E / kHcKeVA) * (E / kHcKeVA);
+            auto density = [&](int g) {
+                const double w = static_cast<double>(g) / G;
+                const double omu = 2.0 * w * w, mu = 1.0 - omu;
+                const double P = 1.0 / (1.0 + k * omu);
+                double f = P * P * (P + 1.0 / P - 1.0 + mu * mu) * 4.0 * w;
+                if (correction >= 1 && s.Zsum > 0) {
+                    const double t = q2 * 0.5 * omu;
+                    double S = 0.0;
+                    for (int e = 0; e < s.n; ++e) {
+                        const double b = 1.0 + t / s.a[e];
+                        const double b2 = b * b;
+                        S += s.nZ[e] * (1.0 - 1.0 / (b2 * b2));
+                    }
+                    f *= S / s.Zsum;
+                }
+                return f;
+            };
+            cum[0] = 0.0;
+            double prev = density(0);
+            for (int g = 1; g <= G; ++g) {
+                const double cur = density(g);
+                cum[g] = cum[g - 1] + 0.5 * (prev + cur);
+                prev = cur;
+            }
+            float* row = out.data() + static_cast<size_t>(i) * kCTabK;
+            int g = 0;
+            for (int j = kCTabK - 1; j >= 0; --j) { // the mass c grows as j falls
+                // mass from mu = 1 down to the quantile: 1 - u_j
+                const double v = 1.0 - static_cast<double>(j) / (kCTabK - 1);
+                const double c = v * v * cum[G];
+                while (g < G - 1 && cum[g + 1] < c)
+                    ++g;
+                const double d = cum[g + 1] - cum[g];
+                const double w = (g + (d > 0.0 ? std::min(1.0, std::max(0.0, (c - cum[g]) / d)) : 0.0)) / G;
+                row[j] = static_cast<float>(2.0 * w * w);
+            }
+            row[0] = 2.0f;
+            row[kCTabK - 1] = 0.0f;
+        }
+        return out;
+    }
+
+    std::mutex g_comptonMutex;
+    std::map<std::vector<double>, std::vector<float>> g_comptonRows;
+    uint64_t g_comptonGeneration = ~0ull;
+} // namespace
+
+void buildComptonAngleTables(const dxmcg_material* mats, int M, int correction, float* out)
+{
+    for (int m = 0; m < M; ++m) {
+        // key: correction level (0 or >= 1 share nothing), then (Z, w) pairs
+        std::vector<double> key { static_cast<double>(correction >= 1 ? 1 : 0) };
+        for (int e = 0; e < mats[m].n; ++e) {
+            key.push_back(mats[m].Z[e]);
+            key.push_back(mats[m].w[e]);
+        }
+        const std::vector<float>* rows = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(g_comptonMutex);
+            if (g_comptonGeneration != physicsGeneration()) {
+                g_comptonRows.clear();
+                g_comptonGeneration = physicsGeneration();
+            }
+            auto it = g_comptonRows.find(key);
+            if (it == g_comptonRows.end())
+                it = g_comptonRows.emplace(key, comptonAngleRows(mats[m], correction)).first;
+            rows = &it->second;
+            std::copy(rows->begin(), rows->end(), out + static_cast<size_t>(m) * kNE * kCTabK);
+        }
+    }
 }
 
 void buildRayleighTables(const dxmcg_material* mats, int M, float* out)

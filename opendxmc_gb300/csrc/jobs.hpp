@@ -40,6 +40,9 @@ void buildBackgroundMajorant(const float* tot0, double rho0, float* out);
 // Rayleigh element choice: out[m][i][k] (kRTabWidth per row) = cumulative share of
 // elements 0..k in material m's form-factor integral at table energy i
 void buildRayleighTables(const dxmcg_material* mats, int M, float* out);
+// Compton angle quantiles out[m][i][j] (kCTabK per row; see kCTabK), kept per
+// (composition, correction) for the life of the physics tables
+void buildComptonAngleTables(const dxmcg_material* mats, int M, int correction, float* out);
 // two-region Woodcock: the box {lo x, y, z, hi x, y, z} of the voxels whose material is
 // neither 0 nor transparent (hi x = -1: none) is worth a second region when it leaves
 // part of the grid out; setTwoRegion fills J's box fields and material 0's majorant
@@ -53,9 +56,5 @@ void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const 
 
 DevMaterial toDevMaterial(const dxmcg_material& m);
 
-// S(t) / Z_sum of each of the M materials on the kSTabN-point table (out: M x kSTabN),
-// from the same per-element incoherent scattering functions the samplers restate:
-// S = sum_i n_i Z_i (1 - (1 + t / a_i)^-4).
-void buildComptonTables(const dxmcg_material* mats, int M, float* out);
 
 } // namespace dxmcg

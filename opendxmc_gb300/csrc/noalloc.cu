@@ -7,9 +7,9 @@
 // between its set-up phase and its runs.  They own every input and output array
 // and pass device pointers; everything else this path needs -- the work-queue head
 // and run statistics, the validation flags and per-material maximum densities,
-// the attenuation tables and majorants, the Compton S(t) and Rayleigh share tables,
+// the attenuation tables and majorants, the Compton angle and Rayleigh share tables,
 // the two-region box, the exposure list, the spectra and the bowtie profiles -- lives
-// in one file-scope __device__ array of kScratchBytes = 1 MiB.  Every GPU that loads
+// in one file-scope __device__ array of kScratchBytes = 6 MiB.  Every GPU that loads
 // the library holds that array until the process exits.
 //
 // The host finds the array's device address with cudaGetSymbolAddress, once per
@@ -41,7 +41,7 @@
 namespace dxmcg {
 namespace {
 
-    constexpr size_t kScratchBytes = 1024u * 1024u;
+    constexpr size_t kScratchBytes = 6u * 1024u * 1024u;
     constexpr int kMaxMaterials = 16;
     constexpr int kMaxExposures = 4096;
     constexpr int kMaxDevices = 64;
@@ -60,8 +60,8 @@ namespace {
     constexpr size_t kOffTot = alignUp(kOffMaj + kTableNE * sizeof(float));
     constexpr size_t kOffXs = alignUp(kOffTot + kMaxMaterials * kTableNE * sizeof(float));
     constexpr size_t kOffExps = alignUp(kOffXs + kMaxMaterials * kTableNE * sizeof(float4));
-    constexpr size_t kOffSTab = alignUp(kOffExps + kMaxExposures * sizeof(DevExposure));
-    constexpr size_t kOffRTab = alignUp(kOffSTab + kMaxMaterials * kSTabN * sizeof(float));
+    constexpr size_t kOffCTab = alignUp(kOffExps + kMaxExposures * sizeof(DevExposure));
+    constexpr size_t kOffRTab = alignUp(kOffCTab + kMaxMaterials * kTableNE * kCTabK * sizeof(float));
     constexpr size_t kOffBox = alignUp(kOffRTab + kMaxMaterials * kTableNE * kRTabWidth * sizeof(float)); // 6 ints
     constexpr size_t kOffMajOut = alignUp(kOffBox + 6 * sizeof(int));
     constexpr size_t kUsed = kOffMajOut + kTableNE * sizeof(float);
@@ -242,9 +242,9 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     buildDeviceTables(materials, n_materials, correction, rhoMax, tot.data(), xs.data(), maj.data(), dm.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffTot, tot.data(), tot.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffXs, xs.data(), xs.size() * sizeof(float4), cudaMemcpyHostToDevice, s));
-    std::vector<float> stab(static_cast<size_t>(n_materials) * kSTabN);
-    buildComptonTables(materials, n_materials, stab.data());
-    NOALLOC_CUDA(cudaMemcpyAsync(base + kOffSTab, stab.data(), stab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    std::vector<float> ctab(static_cast<size_t>(n_materials) * kTableNE * kCTabK);
+    buildComptonAngleTables(materials, n_materials, correction, ctab.data());
+    NOALLOC_CUDA(cudaMemcpyAsync(base + kOffCTab, ctab.data(), ctab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     std::vector<float> rtab(static_cast<size_t>(n_materials) * kTableNE * kRTabWidth);
     buildRayleighTables(materials, n_materials, rtab.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffRTab, rtab.data(), rtab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
@@ -277,7 +277,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     J.mat = device_material;
     J.tot = reinterpret_cast<const float*>(base + kOffTot);
     J.xs = reinterpret_cast<const float4*>(base + kOffXs);
-    J.stab = reinterpret_cast<const float*>(base + kOffSTab);
+    J.ctab = reinterpret_cast<const float*>(base + kOffCTab);
     J.rtab = reinterpret_cast<const float*>(base + kOffRTab);
     J.maj = reinterpret_cast<const float*>(base + kOffMaj);
     J.mats = reinterpret_cast<const DevMaterial*>(base + kOffMats);

@@ -10,11 +10,11 @@
 //             pool of history indices that the warp takes from a global work-queue
 //             head in chunks of kChunk (one atomic per chunk);
 //   interact  lanes waiting for an interaction run it together once at least
-//             `interactBatch` lanes wait (Compton: Kahn's rejection method for
-//             Klein-Nishina, then rejection on S(x)/Z, and at level 2 the Doppler
-//             energy of a bound electron; Rayleigh: element choice and analytic
-//             inversion of F^2, rejection on (1 + cos^2)/2; fluorescence: K-shell
-//             vacancy and yield);
+//             `interactBatch` lanes wait (Compton: the angle from the material's
+//             Klein-Nishina x S(x)/Z quantile table, and at level 2 the Doppler
+//             energy of a bound electron; Rayleigh: element choice from the
+//             material's share table and analytic inversion of F^2, rejection on
+//             (1 + cos^2)/2; fluorescence: K-shell vacancy and yield);
 //   step      stepping lanes take up to `woodcockSteps` Woodcock steps against the
 //             majorant mu_max(E), stopping at a real collision or an escape (or, in
 //             the regular-tracking variant, one free flight with exact Siddon path
@@ -603,7 +603,8 @@ namespace {
                 // the samplers diverge; the direction update they share runs once
                 float cost = 1.0f, Ep = ph.E;
                 if (compton)
-                    Ep = sampleCompton(ph.E, J.mats + pm, J.stab + pm * kSTabN, J.correction, rng, cost, err);
+                    Ep = sampleCompton(ph.E, J.mats + pm, J.ctab + pm * (kTableNE * kCTabK), ec.ie, ec.fe,
+                        J.correction, rng, cost, err);
                 else if (rayleigh)
                     cost = sampleRayleigh(ph.E, J.mats + pm, J.rtab + pm * (kTableNE * kRTabWidth), ec.ie, ec.fe,
                         rng, err);

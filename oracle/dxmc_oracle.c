@@ -1284,43 +1284,77 @@ static void isotropic_dir(double d[3], double u1, double u2)
     d[2] = ct;
 }
 
-/* Klein-Nishina by Kahn's rejection method (Kahn 1954; as given in Lux &
- * Koblinger, Monte Carlo Particle Transport Methods, 1991), followed for
- * correction >= 1 by rejection on S(x)/Z of the material.  Returns E'. */
-static double sample_compton(double E, const mat_sampling* m, int correction, rng_t* r, double* cos_theta)
+/* Compton angle (the transport kernel's sampler, jobs.cpp comptonAngleRows and
+ * device.cuh sampleCompton): per table energy E_i, 1 - cos theta at the cumulative
+ * probabilities u_j = 1 - (1 - j/(K-1))^2 of KN(mu) S(t(mu)) / Z (S = 1 at correction
+ * 0), integrated by the trapezoid rule on 512 equal steps of w = sqrt((1 - mu)/2) and
+ * inverted linearly.  A draw interpolates rows ie and ie + 1 at j = (K-1)(1 - sqrt(1-u)). */
+#define OR_CTAB_K 256
+static inline void grid_pos(double E, int* i, double* f);
+
+static void compton_rows(const mat_sampling* m, int correction, int i0, int i1, double* out)
+{
+    enum { G = 512 };
+    double cum[G + 1];
+    for (int i = i0; i <= i1; ++i) {
+        const double E = OR_EMIN + i * OR_DE;
+        const double k = E / ME_KEV;
+        const double q2 = (E / HC_KEV_A) * (E / HC_KEV_A);
+        double prev = 0.0;
+        cum[0] = 0.0;
+        for (int g = 0; g <= G; ++g) {
+            const double w = (double)g / G;
+            const double omu = 2.0 * w * w, mu = 1.0 - omu;
+            const double P = 1.0 / (1.0 + k * omu);
+            double f = P * P * (P + 1.0 / P - 1.0 + mu * mu) * 4.0 * w;
+            if (correction >= 1 && m->Zsum > 0.0) {
+                const double t = q2 * 0.5 * omu;
+                double S = 0.0;
+                for (int e = 0; e < m->n; ++e) {
+                    const double b = 1.0 + t / m->a[e];
+                    const double b2 = b * b;
+                    S += m->nZ[e] * (1.0 - 1.0 / (b2 * b2));
+                }
+                f *= S / m->Zsum;
+            }
+            if (g > 0)
+                cum[g] = cum[g - 1] + 0.5 * (prev + f);
+            prev = f;
+        }
+        double* row = out + (size_t)(i - i0) * OR_CTAB_K;
+        int g = 0;
+        for (int j = OR_CTAB_K - 1; j >= 0; --j) {
+            const double v = 1.0 - (double)j / (OR_CTAB_K - 1);
+            const double c = v * v * cum[G];
+            while (g < G - 1 && cum[g + 1] < c)
+                ++g;
+            const double d = cum[g + 1] - cum[g];
+            double fr = d > 0.0 ? (c - cum[g]) / d : 0.0;
+            fr = fr < 0.0 ? 0.0 : (fr > 1.0 ? 1.0 : fr);
+            const double w = (g + fr) / G;
+            row[j] = 2.0 * w * w;
+        }
+        row[0] = 2.0;
+        row[OR_CTAB_K - 1] = 0.0;
+    }
+}
+
+/* rows: the material's rows ie and ie + 1 (2 x OR_CTAB_K) */
+static double sample_compton(double E, const mat_sampling* m, int correction, const double* rows, double fe,
+    rng_t* r, double* cos_theta)
 {
     const double k = E / ME_KEV;
-    const double kk = 2.0 * k;
     for (int guard = 0; guard < 100000; ++guard) {
-        const double r1 = rng_u(r), r2 = rng_u(r), r3 = rng_u(r);
-        double xm1; /* x - 1, x = E / E' */
-        int acc;
-        if (r1 * (9.0 + kk) <= 1.0 + kk) {
-            xm1 = kk * r2;
-            const double x = 1.0 + xm1;
-            acc = r3 * x * x <= 4.0 * (x - 1.0);
-        } else {
-            xm1 = kk * (1.0 - r2) / (1.0 + kk * r2);
-            const double x = 1.0 + xm1;
-            const double mu = 1.0 - xm1 / k;
-            acc = 2.0 * r3 <= mu * mu + 1.0 / x;
-        }
-        if (!acc)
-            continue;
-        const double omu = xm1 / k; /* 1 - cos theta */
-        if (correction >= 1) {
-            const double q = E / HC_KEV_A;
-            const double t = q * q * 0.5 * omu; /* x^2 */
-            double S = 0.0;
-            for (int i = 0; i < m->n; ++i) {
-                const double b = 1.0 + t / m->a[i];
-                const double b2 = b * b;
-                S += m->nZ[i] * (1.0 - 1.0 / (b2 * b2));
-            }
-            const double r4 = rng_u(r);
-            if (r4 * m->Zsum > S)
-                continue;
-        }
+        const double u = rng_u(r);
+        const double jf = (OR_CTAB_K - 1) * (1.0 - sqrt(1.0 - u));
+        int j = (int)jf;
+        if (j > OR_CTAB_K - 2)
+            j = OR_CTAB_K - 2;
+        const double g = jf - j;
+        const double lo = rows[j] + g * (rows[j + 1] - rows[j]);
+        const double hi = rows[OR_CTAB_K + j] + g * (rows[OR_CTAB_K + j + 1] - rows[OR_CTAB_K + j]);
+        const double omu = lo + fe * (hi - lo); /* 1 - cos theta */
+        const double xm1 = k * omu;             /* x - 1, x = E / E' */
         *cos_theta = 1.0 - omu;
         if (correction >= 2) {
             const double Ep = doppler_sample(E, 1.0 + xm1, omu, m, r);
@@ -1378,9 +1412,23 @@ double or_sample_compton(double E, const or_composition* c, int correction, cons
     memset(&r, 0, sizeof(r));
     r.inj = u;
     r.n_inj = nu;
-    const double Ep = sample_compton(E, &m, correction, &r, cos_theta);
+    int ie;
+    double fe, rows[2 * OR_CTAB_K];
+    grid_pos(E, &ie, &fe);
+    compton_rows(&m, correction, ie, ie + 1, rows);
+    const double Ep = sample_compton(E, &m, correction, rows, fe, &r, cos_theta);
     *used = r.used;
     return Ep;
+}
+
+int or_compton_quantiles(const or_composition* c, int correction, int energy_index, double* out)
+{
+    if (energy_index < 0 || energy_index >= OR_NE)
+        return -1;
+    mat_sampling m;
+    make_sampling(c, &m);
+    compton_rows(&m, correction, energy_index, energy_index, out);
+    return OR_CTAB_K;
 }
 
 double or_sample_photoelectric(double E, const or_composition* c, const double* u, int nu, int* used, double* dz)
@@ -1436,6 +1484,7 @@ struct or_world {
     double* coh;
     double* tot;
     double maj[OR_NE]; /* 1/cm */
+    double* ctab;      /* [m][OR_NE][OR_CTAB_K] Compton 1 - cos theta quantiles */
     /* two-region Woodcock: the box of voxels whose material is neither 0 nor
      * transparent (voxel indices b0 .. b1 inclusive), its faces widened by a margin,
      * and material 0's majorant; box_on 0: the box is empty or the whole grid */
@@ -1480,8 +1529,10 @@ or_world* or_world_create(const int32_t dims[3], const double spacing_cm[3], con
     double E[OR_NE];
     for (int i = 0; i < OR_NE; ++i)
         E[i] = OR_EMIN + i * OR_DE;
+    w->ctab = (double*)malloc((size_t)n_mats * OR_NE * OR_CTAB_K * sizeof(double));
     for (int m = 0; m < n_mats; ++m) {
         make_sampling(&mats[m], &w->samp[m]);
+        compton_rows(&w->samp[m], correction, 0, OR_NE - 1, w->ctab + (size_t)m * OR_NE * OR_CTAB_K);
         or_attenuation(&mats[m], correction, OR_NE, E, w->photo + m * OR_NE, w->incoh + m * OR_NE,
             w->coh + m * OR_NE);
         for (int i = 0; i < OR_NE; ++i)
@@ -1554,6 +1605,7 @@ void or_world_destroy(or_world* w)
     free(w->e2);
     free(w->cnt);
     free(w->mscale);
+    free(w->ctab);
     free(w);
 }
 
@@ -1860,7 +1912,11 @@ static int interact(or_world* w, size_t v, int m, double* E, double wgt, double 
     if (rt < ph + ic) {
         st->n_compton++;
         double cost;
-        const double Ep = sample_compton(*E, &w->samp[m], w->correction, r, &cost);
+        int ie;
+        double fe;
+        grid_pos(*E, &ie, &fe);
+        const double Ep = sample_compton(*E, &w->samp[m], w->correction,
+            w->ctab + ((size_t)m * OR_NE + ie) * OR_CTAB_K, fe, r, &cost);
         scatter_dir(d, cost, rng_u(r));
         deposit(w, v, wgt * (*E - Ep), st);
         *E = Ep;

@@ -188,6 +188,8 @@ def lib() -> C.CDLL:
     L.or_siddon_f64.argtypes = [pd, pd, C.POINTER(C.c_int32), pd, i, C.POINTER(C.c_int64), pd]
     L.or_sample_compton.restype = d
     L.or_sample_compton.argtypes = [d, C.POINTER(Composition), i, pd, i, C.POINTER(C.c_int), pd]
+    L.or_compton_quantiles.restype = i
+    L.or_compton_quantiles.argtypes = [C.POINTER(Composition), i, i, pd]
     L.or_sample_photoelectric.restype = d
     L.or_sample_photoelectric.argtypes = [d, C.POINTER(Composition), pd, i, C.POINTER(C.c_int), pd]
     L.or_compton_shells.restype = i
@@ -380,6 +382,16 @@ def siddon_f64(o, d, dims, spacing, cap=4096):
     if k < 0:
         raise ValueError("cap too small")
     return idx[:k].copy(), ln[:k].copy()
+
+
+def compton_quantiles(zw, correction, energy_index):
+    """1 - cos theta of the Compton angle table at the probabilities
+    u_j = 1 - (1 - j/(K-1))^2 (K = 256) for table energy EMIN + energy_index * DE."""
+    out = np.zeros(256)
+    c = Composition.from_dict(zw)
+    if lib().or_compton_quantiles(C.byref(c), correction, energy_index, _p(out, C.c_double)) != 256:
+        raise ValueError("energy index out of range")
+    return out
 
 
 def sample_compton(E, zw, correction, uniforms):

@@ -101,7 +101,11 @@ def test_compton_sampler_matches_oracle(gpu, oracle, zw, correction):
         if uo != ug[i]:
             continue  # a comparison rounded the other way: different branch
         same += 1
-        assert abs(eg[i] - eo) <= 1e-6 * eo
+        # the angle comes from the same table, FP32 on the GPU and FP64 here; at level 2
+        # the Doppler-broadened E' can be a small difference of large terms, so its
+        # error scales with E rather than E'
+        tol = 1e-6 * eo + (1e-5 * E[i] if correction >= 2 else 0.0)
+        assert abs(eg[i] - eo) <= tol, (E[i], eg[i], eo)
         assert abs(cg[i] - co) <= 1e-6
     assert same >= 0.998 * n
 

@@ -168,7 +168,9 @@ typedef struct {
     int32_t interact_batch; /* parked scatterings a warp gathers before sampling them, 0 = default */
     int32_t refill_batch;   /* dead lanes a warp gathers before starting new histories, 0 = default */
     int32_t macro_cell;     /* MACRO tracking: cell edge in voxels, 0 = default (16) */
-    int32_t woodcock_steps; /* WOODCOCK tracking: steps a lane takes between regroupings, 0 = default */
+    int32_t woodcock_steps; /* WOODCOCK tracking: steps a lane takes between regroupings, 0 = default:
+                             * 1.1 / p clamped to 4..16, p = stops per step of the world's
+                             * previous Woodcock run (8 before the first) */
     /* per-history step limit, 0 = default (1,000,000, at most that): a history that
      * takes more tracking steps is stopped and counted in n_errors, and the call
      * returns DXMCG_ERR_DEVICE after the launch completes */

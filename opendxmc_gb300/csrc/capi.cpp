@@ -149,6 +149,9 @@ struct dxmcg_world {
     int box[6] {};
     bool hasBox = false;
     std::vector<float> hostTot, hostMaj; // FP32 tables as uploaded
+    // Woodcock launch hint: stops (real collisions and escapes) per tentative collision
+    // of the last run on this world, 0 before the first
+    double stopsPerStep = 0.0;
     std::vector<double> rhoMax;
     double historiesScored = 0.0;
     double voxelVolume = 0.0;
@@ -289,6 +292,25 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
 }
 
 // ktrack: the kernel tracking of the instance that will run (kernelTracking)
+// Woodcock steps a lane takes per step phase, by default.  A lane stops at a real
+// collision or an escape, with probability p per step; the phase's steps are best near
+// 1.1 / p, measured on the three single-job workloads (p 0.12 on the 256x256x200 torso:
+// best 8-10; 0.28 on the 512x512x400 torso with two regions: 4-6; 0.27 on the DX
+// cylinder: 6).  p comes from the world's previous run; 8 before the first.
+int defaultWoodcockSteps(double stopsPerStep)
+{
+    if (!(stopsPerStep > 0.0))
+        return 8;
+    return static_cast<int>(std::lround(std::min(16.0, std::max(4.0, 1.1 / stopsPerStep))));
+}
+
+void noteStops(dxmcg_world* w, const DevCounters& c)
+{
+    const unsigned long long stops = c.photo + c.compton + c.rayleigh + (c.histories - c.missed);
+    if (c.visits > 0)
+        w->stopsPerStep = static_cast<double>(stops) / static_cast<double>(c.visits);
+}
+
 LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o, int ktrack, bool batch = false)
 {
     int sms = 0;
@@ -303,7 +325,7 @@ LaunchShape chooseShape(const dxmcg_world* w, const dxmcg_run_options& o, int kt
     s.grid = std::max(1, sms) * per;
     s.interact_batch = std::min(32, std::max(0, o.interact_batch));
     s.refill_batch = std::min(32, std::max(0, o.refill_batch));
-    s.woodcock_steps = std::min(64, std::max(0, o.woodcock_steps));
+    s.woodcock_steps = o.woodcock_steps > 0 ? std::min(64, o.woodcock_steps) : defaultWoodcockSteps(w->stopsPerStep);
     return s;
 }
 
@@ -1073,6 +1095,8 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
     DXMCG_CUDA(cudaMemcpyAsync(&c, w->counters.p, sizeof(c), cudaMemcpyDeviceToHost, w->stream));
     DXMCG_CUDA(cudaStreamSynchronize(w->stream));
     w->historiesScored += static_cast<double>(c.histories);
+    if (o.tracking == DXMCG_TRACK_WOODCOCK)
+        noteStops(w, c);
     if (stats) {
         stats->e_source = c.e_source;
         stats->e_deposited = c.e_deposited;
@@ -1266,8 +1290,11 @@ DXMCG_API int dxmcg_batch_run(dxmcg_batch* b, dxmcg_stats* stats)
         DXMCG_CUDA(cudaMemcpyAsync(each.data(), b->jobCounters.p, nJobs * sizeof(DevCounters),
             cudaMemcpyDeviceToHost, b->stream));
         DXMCG_CUDA(cudaStreamSynchronize(b->stream));
-        for (const auto& x : each)
-            addCounters(c, x);
+        for (int j = 0; j < nJobs; ++j) {
+            addCounters(c, each[j]);
+            if (b->tracking == DXMCG_TRACK_WOODCOCK || b->tracking == kTrackWoodcockBox)
+                noteStops(b->worlds[j], each[j]);
+        }
     } else {
         DXMCG_CUDA(cudaMemcpyAsync(&c, b->counters.p, sizeof(c), cudaMemcpyDeviceToHost, b->stream));
         DXMCG_CUDA(cudaStreamSynchronize(b->stream));
@@ -1336,7 +1363,7 @@ DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_o
     static const int kBlocks[] = { 128, 256 };
     static const int kInteract[] = { 8, 12, 16, 24 };
     static const int kRefill[] = { 4, 8, 16 };
-    static const int kWoodcock[] = { 8, 16 };
+    static const int kWoodcock[] = { 4, 8, 12 };
     float warm = 0.0f;
     rc = trial(chooseShape(w, o, kernelTracking(J)), warm);
     if (rc != DXMCG_OK)

@@ -824,8 +824,8 @@ namespace {
         if (!fn)
             return cudaErrorInvalidValue;
         const int refill = shape.refill_batch > 0 ? shape.refill_batch : 8;
-        const int interact = shape.interact_batch > 0 ? shape.interact_batch : 12;
-        const int wsteps = shape.woodcock_steps > 0 ? shape.woodcock_steps : 16;
+        const int interact = shape.interact_batch > 0 ? shape.interact_batch : 8;
+        const int wsteps = shape.woodcock_steps > 0 ? shape.woodcock_steps : 8;
         fn<<<shape.grid, shape.block, 0, s>>>(job, jobs, offsets, nJobs, h_end, ctr, refill, interact, wsteps);
         return cudaGetLastError();
     }

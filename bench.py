@@ -68,7 +68,8 @@ def parse():
                    help="Woodcock gather skip: 1 on, -1 off, 0 library default (on above 64 MiB of voxels)")
     p.add_argument("--two-region", type=int, choices=[-1, 0, 1], default=0,
                    help="two-region Woodcock (outside the box of non-air voxels against air's own majorant): "
-                        "1 on, -1 off, 0 library default (on above 64 MiB of voxels)")
+                        "1 on, -1 off, 0 library default (on when the box of non-air voxels holds "
+                        "less than half the grid)")
     p.add_argument("--interact-batch", type=int, default=0)
     p.add_argument("--refill-batch", type=int, default=0)
     p.add_argument("--correction", type=int, choices=[0, 1, 2], default=1,

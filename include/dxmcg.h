@@ -169,7 +169,7 @@ typedef struct {
     int32_t refill_batch;   /* dead lanes a warp gathers before starting new histories, 0 = default */
     int32_t macro_cell;     /* MACRO tracking: cell edge in voxels, 0 = default (16) */
     int32_t woodcock_steps; /* WOODCOCK tracking: steps a lane takes between regroupings, 0 = default:
-                             * 1.1 / p clamped to 4..16, p = stops per step of the world's
+                             * 1.4 / p clamped to 4..16, p = stops per step of the world's
                              * previous Woodcock run (8 before the first) */
     /* per-history step limit, 0 = default (1,000,000, at most that): a history that
      * takes more tracking steps is stopped and counted in n_errors, and the call
@@ -185,8 +185,8 @@ typedef struct {
      * material is neither 0 nor transparent, flights step against material 0's own
      * majorant until they reach the box (the same transport, fewer tentative
      * collisions in the air around a patient).  1 = on, -1 = off, 0 = default: on
-     * when the world's voxel words (4 bytes per voxel) exceed 64 MiB; a batch
-     * decides from opts[0] and is on only for 1 */
+     * when that box holds less than half of the grid's voxels (decided per world,
+     * also in a batch) */
     int32_t two_region;
 } dxmcg_run_options;
 

@@ -272,8 +272,8 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
         J.cb[0] = w->ncell[0];
         J.cb[1] = w->ncell[1];
     }
-    // twoRegion: 1 on, 0 off, -1 decided from this world's size
-    const bool two = twoRegion < 0 ? twoRegionFor(o, w->N * sizeof(uint32_t)) : twoRegion > 0;
+    // twoRegion: 1 on, 0 off, -1 decided from this world's box
+    const bool two = twoRegion < 0 ? twoRegionFor(o, boxFraction(w->box, w->dims)) : twoRegion > 0;
     if (o.tracking == DXMCG_TRACK_WOODCOCK && two && w->hasBox)
         setTwoRegion(J, w->box, w->spacing, w->majOut.p);
     if (o.tracking == DXMCG_TRACK_MACRO) {
@@ -294,14 +294,15 @@ int prepareJob(dxmcg_world* w, const dxmcg_beam& b, const dxmcg_run_options& o, 
 // ktrack: the kernel tracking of the instance that will run (kernelTracking)
 // Woodcock steps a lane takes per step phase, by default.  A lane stops at a real
 // collision or an escape, with probability p per step; the phase's steps are best near
-// 1.1 / p, measured on the three single-job workloads (p 0.12 on the 256x256x200 torso:
-// best 8-10; 0.28 on the 512x512x400 torso with two regions: 4-6; 0.27 on the DX
-// cylinder: 6).  p comes from the world's previous run; 8 before the first.
+// 1.4 / p, measured on the single-job workloads (p 0.12 on the 256x256x200 torso with
+// one region: best 10-12; p 0.28 with two regions there and on the 512x512x400 torso:
+// 4-6; p 0.27 on the DX cylinder: 6).  p comes from the world's previous run; 8 before
+// the first.
 int defaultWoodcockSteps(double stopsPerStep)
 {
     if (!(stopsPerStep > 0.0))
         return 8;
-    return static_cast<int>(std::lround(std::min(16.0, std::max(4.0, 1.1 / stopsPerStep))));
+    return static_cast<int>(std::lround(std::min(16.0, std::max(4.0, 1.4 / stopsPerStep))));
 }
 
 void noteStops(dxmcg_world* w, const DevCounters& c)
@@ -1171,15 +1172,12 @@ DXMCG_API int dxmcg_batch_create(int n_jobs, dxmcg_world* const* worlds, const d
             voxelBytes += worlds[j]->N * sizeof(uint32_t);
     }
     b->gatherSkip = gatherSkipFor(opts[0], voxelBytes);
-    // two regions only when asked for (two_region 1): on the 64-job batch workload
-    // (ellipsoid phantoms that fill most of their grids) they measured 17 % slower
-    const bool twoRegion = opts[0].tracking == DXMCG_TRACK_WOODCOCK && opts[0].two_region > 0;
     for (int j = 0; j < n_jobs; ++j) {
         b->inputs.push_back(std::make_unique<JobBuffers>());
         uint64_t n = 0;
         double cal = 1.0;
         const int rc = prepareJob(worlds[j], beams[j], opts[j], J[j], n, cal, b->inputs.back().get(),
-            b->gatherSkip ? 1 : 0, twoRegion ? 1 : 0);
+            b->gatherSkip ? 1 : 0);
         if (rc != DXMCG_OK)
             return rc;
         b->worlds.push_back(worlds[j]);

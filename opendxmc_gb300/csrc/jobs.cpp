@@ -274,11 +274,21 @@ bool twoRegionBox(const int box[6], const int32_t dims[3])
             || box[5] < dims[2] - 1);
 }
 
-bool twoRegionFor(const dxmcg_run_options& o, size_t voxelBytes)
+double boxFraction(const int box[6], const int32_t dims[3])
+{
+    if (box[3] < 0)
+        return 0.0;
+    double f = 1.0;
+    for (int a = 0; a < 3; ++a)
+        f *= static_cast<double>(box[3 + a] - box[a] + 1) / dims[a];
+    return f;
+}
+
+bool twoRegionFor(const dxmcg_run_options& o, double boxFrac)
 {
     if (o.tracking != DXMCG_TRACK_WOODCOCK || o.two_region < 0)
         return false;
-    return o.two_region > 0 || voxelBytes > (64ull << 20);
+    return o.two_region > 0 || boxFrac < 0.5;
 }
 
 void setTwoRegion(DevJob& J, const int box[6], const double spacing[3], const float* majOut)

@@ -47,9 +47,13 @@ void buildComptonAngleTables(const dxmcg_material* mats, int M, int correction, 
 // neither 0 nor transparent (hi x = -1: none) is worth a second region when it leaves
 // part of the grid out; setTwoRegion fills J's box fields and material 0's majorant
 bool twoRegionBox(const int box[6], const int32_t dims[3]);
-// whether Woodcock runs with two regions: two_region 1 on, -1 off, 0 on when the voxel
-// words exceed 64 MiB (beyond L2), the grids on which it was measured to pay
-bool twoRegionFor(const dxmcg_run_options& o, size_t voxelBytes);
+// the box's share of the grid's voxels (0 without a box)
+double boxFraction(const int box[6], const int32_t dims[3]);
+// whether Woodcock runs with two regions: two_region 1 on, -1 off, 0 on when the box
+// holds less than half the grid.  Measured: on at box fractions 0.44 (256x256x200
+// torso, +13 %) and 0.36 (512x512x400 torso, +23 %); off at 0.53-0.62 (the batch
+// workload's ellipsoids, -12 %) and 0.94 (the DX cylinder, -11 %).
+bool twoRegionFor(const dxmcg_run_options& o, double boxFrac);
 void setTwoRegion(DevJob& J, const int box[6], const double spacing[3], const float* majOut);
 void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const double* rhoMax, float* tot,
     float4* xs, float* maj, DevMaterial* dm);

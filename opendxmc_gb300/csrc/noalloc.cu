@@ -215,7 +215,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     rhoMaxKernel<<<grid, 256, 0, s>>>(device_density, device_material, static_cast<size_t>(N), n_materials, flags,
         flags + 256);
     NOALLOC_CUDA(cudaGetLastError());
-    const bool woodcock = twoRegionFor(o, static_cast<size_t>(N) * sizeof(uint32_t));
+    const bool woodcock = o.tracking == DXMCG_TRACK_WOODCOCK && o.two_region >= 0;
     if (woodcock)
         NOALLOC_CUDA(launchMaterialBox(device_material, dims[0], dims[1], dims[2], box, s));
     unsigned host[257];
@@ -249,7 +249,7 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     buildRayleighTables(materials, n_materials, rtab.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffRTab, rtab.data(), rtab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMaj, maj.data(), maj.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-    const bool twoRegion = woodcock && twoRegionBox(hostBox, dims);
+    const bool twoRegion = woodcock && twoRegionBox(hostBox, dims) && twoRegionFor(o, boxFraction(hostBox, dims));
     std::vector<float> majOut(kTableNE);
     if (twoRegion) {
         buildBackgroundMajorant(tot.data(), rhoMax[0], majOut.data());

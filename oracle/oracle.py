@@ -22,13 +22,14 @@ EMIN = 1.0
 DE = 0.5
 MAX_ELEMENTS = 16
 
+TRANSPARENT = 255  # material index that interacts with nothing
 TRACK_WOODCOCK = 0
 TRACK_SIDDON = 1
 TRACK_MACRO = 2
 TRACK_WOODCOCK_BOX = 3  # two-region Woodcock
-# the transport kernel's default: two-region Woodcock on grids whose 4-byte voxel words
-# exceed 64 MiB, one region below
-TWO_REGION_BYTES = 64 << 20
+# the transport kernel's default: two-region Woodcock when the box of the voxels whose
+# material is neither 0 nor transparent holds less than this share of the grid
+TWO_REGION_BOX_FRACTION = 0.5
 BEAM_DX, BEAM_CT_SPIRAL, BEAM_CT_SEQUENTIAL, BEAM_CBCT, BEAM_PENCIL, BEAM_CT_SPIRAL_DUAL = range(6)
 
 
@@ -446,6 +447,12 @@ class World:
         comps = (Composition * len(materials))(*[Composition.from_dict(m) for m in materials])
         self.N = int(np.prod(self.dims))
         assert dens.size == self.N and mat.size == self.N
+        fg = (mat != 0) & (mat != TRANSPARENT)
+        self.box_fraction = 0.0
+        if fg.any():
+            m3 = fg.reshape(self.dims[::-1])
+            ext = [np.flatnonzero(m3.any(axis=tuple(b for b in range(3) if b != a))) for a in range(3)]
+            self.box_fraction = float(np.prod([(e[-1] - e[0] + 1) / m3.shape[a] for a, e in enumerate(ext)]))
         self._h = lib().or_world_create(_p(n, C.c_int32), _p(sp, C.c_double), _p(dens, C.c_double),
                                         _p(mat, C.c_uint8), comps, len(materials), correction)
         if not self._h:
@@ -487,9 +494,9 @@ class World:
     def run(self, beam: dict, seed=1, stream=0, tracking=None, threads=None, hist_begin=0,
             hist_end=2**63):
         """tracking None: Woodcock as the transport kernel chooses by default (two
-        regions on grids beyond TWO_REGION_BYTES of voxel words, one below)."""
+        regions when the box holds less than TWO_REGION_BOX_FRACTION of the grid)."""
         if tracking is None:
-            tracking = TRACK_WOODCOCK_BOX if 4 * self.N > TWO_REGION_BYTES else TRACK_WOODCOCK
+            tracking = TRACK_WOODCOCK_BOX if self.box_fraction < TWO_REGION_BOX_FRACTION else TRACK_WOODCOCK
         b, keep = make_beam(beam)
         st = Stats()
         threads = threads or os.cpu_count() or 1

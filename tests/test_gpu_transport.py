@@ -196,8 +196,8 @@ def test_two_region_woodcock_matches_plain_woodcock(gpu):
     assert nvox > 2000 and frac >= 0.99
     assert abs(two.sum() - one.sum()) <= 4.0 * sigma
     assert v2 < 0.5 * v1
-    # the default on this 17 MB grid: one region (two above 64 MiB of voxel words)
-    assert gw.run(beam, gpu.run_options(seed=2, stream=1, hist_end=200_000))["n_visits"] == v1
+    # the default: two regions, since the torso's box holds less than half the grid
+    assert gw.run(beam, gpu.run_options(seed=2, stream=1, hist_end=200_000))["n_visits"] == v2
 
 
 def test_two_region_woodcock_shared_streams_match_oracle(gpu, oracle):

@@ -313,7 +313,7 @@ DXMCG_API int dxmcg_autotune(dxmcg_world* w, const dxmcg_beam* beam, dxmcg_run_o
  * any other device allocator while they run (their GPU memory comes only from
  * their own pool, or they were given a fixed device budget up front): every input
  * and output is a caller-owned device array, and all scratch (queue head,
- * statistics, tables, exposures, spectra, bowtie) lives in one 6 MiB
+ * statistics, tables, exposures, spectra, bowtie) lives in one 12 MiB
  * file-scope __device__ array that each GPU loading the library keeps until exit.
  * Limits: at most 16 materials and 4096 exposures (DXMCG_ERR_CAPACITY beyond).
  * CT beams with opts->normalize set and a CTDIvol or CTDIw target are refused

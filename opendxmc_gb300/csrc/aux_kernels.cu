@@ -280,11 +280,10 @@ namespace {
         if (i >= n)
             return;
         InjectedUniforms r { u + static_cast<size_t>(i) * stride, stride, 0 };
-        unsigned err = 0;
         int ie;
         float fe;
         gridPos(E[i], ie, fe);
-        co[i] = sampleRayleigh(E[i], M, rtab, ie, fe, r, err);
+        co[i] = sampleRayleigh(rtab, ie, fe, r);
         used[i] = r.used;
     }
 

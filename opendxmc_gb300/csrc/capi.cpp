@@ -129,7 +129,7 @@ struct dxmcg_world {
     DeviceBuffer<float> maj;
     DeviceBuffer<DevMaterial> mats;
     DeviceBuffer<float> ctab; // Compton angle quantiles per material and energy
-    DeviceBuffer<float> rtab; // Rayleigh cumulative element shares per material and energy
+    DeviceBuffer<float> rtab; // Rayleigh angle quantiles per material and energy
     DeviceBuffer<DevCounters> counters;
     DeviceBuffer<unsigned> scratch; // rho max bits [256] + error word
     JobBuffers job; // exposures, spectra, bowtie of the last transport_run
@@ -889,8 +889,8 @@ DXMCG_API int dxmcg_world_build(dxmcg_world* w)
     buildComptonAngleTables(w->materials.data(), M, w->correction, ctab.data());
     DXMCG_CUDA(w->ctab.alloc(ctab.size()));
     DXMCG_CUDA(cudaMemcpyAsync(w->ctab.p, ctab.data(), ctab.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
-    std::vector<float> rtab(static_cast<size_t>(M) * kNE * kRTabWidth);
-    buildRayleighTables(w->materials.data(), M, rtab.data());
+    std::vector<float> rtab(static_cast<size_t>(M) * kNE * kCTabK);
+    buildRayleighAngleTables(w->materials.data(), M, rtab.data());
     DXMCG_CUDA(w->rtab.alloc(rtab.size()));
     DXMCG_CUDA(cudaMemcpyAsync(w->rtab.p, rtab.data(), rtab.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
     DXMCG_CUDA(cudaMemsetAsync(w->tally.p, 0, w->N * sizeof(Tally), w->stream));
@@ -1830,8 +1830,8 @@ DXMCG_API int dxmcg_sample_rayleigh(int n, const double* energies, const dxmcg_m
         return rc;
     DXMCG_CUDA(co.alloc(n));
     DXMCG_CUDA(us.alloc(n));
-    std::vector<float> rtabHost(static_cast<size_t>(kNE) * kRTabWidth);
-    buildRayleighTables(m, 1, rtabHost.data());
+    std::vector<float> rtabHost(static_cast<size_t>(kNE) * kCTabK);
+    buildRayleighAngleTables(m, 1, rtabHost.data());
     DeviceBuffer<float> rtab;
     DXMCG_CUDA(rtab.alloc(rtabHost.size()));
     DXMCG_CUDA(cudaMemcpy(rtab.p, rtabHost.data(), sizeof(float) * rtabHost.size(), cudaMemcpyHostToDevice));

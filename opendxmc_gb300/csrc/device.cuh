@@ -174,16 +174,16 @@ namespace dev {
         return false;
     }
 
-    // 1 - cos theta of a Compton scattering from the material's quantile table (row ie
-    // of ctab, interpolated towards row ie + 1 by fe, at the same probability): one
-    // uniform, no rejection.  The table's probability grid u_j = 1 - (1 - j/(K-1))^2 is
-    // inverted by j = (K - 1)(1 - sqrt(1 - u)).
-    __device__ __forceinline__ float comptonOneMinusCos(const float* __restrict__ ctab, int ie, float fe, float u)
+    // 1 - cos theta from a material's angle quantile table (row ie of tab, interpolated
+    // towards row ie + 1 by fe, at the same probability): one uniform, no rejection.
+    // The table's probability grid u_j = (1 - cos(pi j/(K-1)))/2 is inverted by
+    // j = (K - 1) acos(1 - 2u) / pi.
+    __device__ __forceinline__ float oneMinusCos(const float* __restrict__ tab, int ie, float fe, float u)
     {
-        const float jf = static_cast<float>(kCTabK - 1) * (1.0f - sqrtf(1.0f - u));
+        const float jf = static_cast<float>(kCTabK - 1) * 0.31830988618379067f * acosf(fmaf(-2.0f, u, 1.0f));
         const int j = min(static_cast<int>(jf), kCTabK - 2);
         const float g = jf - static_cast<float>(j);
-        const float* a = ctab + ie * kCTabK + j;
+        const float* a = tab + ie * kCTabK + j;
         const float a0 = __ldg(a), a1 = __ldg(a + 1);
         const float b0 = __ldg(a + kCTabK), b1 = __ldg(a + kCTabK + 1);
         const float lo = fmaf(g, a1 - a0, a0);
@@ -200,7 +200,7 @@ namespace dev {
     {
         const float k = E * (1.0f / kMeKeV);
         for (int guard = 0; guard < kMaxRejections; ++guard) {
-            const float omu = comptonOneMinusCos(ctab, ie, fe, r.u());
+            const float omu = oneMinusCos(ctab, ie, fe, r.u());
             const float xm1 = k * omu;
             cost = 1.0f - omu;
             if (correction >= 2) {
@@ -216,60 +216,12 @@ namespace dev {
         return E;
     }
 
-    // 1 - (1 + x)^-3 = x (3 + x (3 + x)) / (1 + x)^3 for x = T / a >= 0: the form factor
-    // integral of an element, without the cancellation of 1 - 1/b^3 at small x and
-    // without transcendental functions (a few ulps in FP32).
-    __device__ __forceinline__ float formFactorIntegral(float x)
-    {
-        const float b = 1.0f + x;
-        return x * fmaf(x, 3.0f + x, 3.0f) * __frcp_rn(b * b * b);
-    }
-
-    // Rayleigh scattering: element i with probability n_i Z_i^2 a_i c_i(T), then
-    // t = x^2 from F^2 by inversion, t = a ((1 - y)^(-1/3) - 1) with y = r2 c_i, and
-    // rejection on (1 + cos^2) / 2.  The element is the first whose cumulative share,
-    // interpolated from the material's table rtab at the photon's energy-grid position
-    // (ie, fe), reaches r1: at most 9e-5 from the exact shares in soft tissue, so the
-    // choice differs from the exact sum's for a few uniforms in 1e4.  The inversion is evaluated as
-    // a y / (om (s^2 + s + 1)) with om = 1 - y and s = om^(-1/3): that is a (s - 1), since
-    // s^3 - 1 = y / om, with no cancellation when y is small.  For y >= 1/2, om is formed
-    // as (1 - r2) + r2 (1 + T/a)^-3 (1 - r2 is exact) so FP32 keeps its precision.
+    // Rayleigh scattering: cos theta from the material's quantile table of
+    // (1 + cos^2)/2 F^2(x), as for the Compton angle: one uniform, no rejection.
     template <class U>
-    __device__ float sampleRayleigh(float E, const DevMaterial* __restrict__ M, const float* __restrict__ rtab,
-        int ie, float fe, U& r, unsigned& err)
+    __device__ __forceinline__ float sampleRayleigh(const float* __restrict__ rtab, int ie, float fe, U& r)
     {
-        const float q = E * kInvHc;
-        const float T = q * q;
-        const int n = M->n;
-        const float* c0 = rtab + ie * kRTabWidth;
-        for (int guard = 0; guard < kMaxRejections; ++guard) {
-            const float r1 = r.u(), r2 = r.u(), r3 = r.u();
-            int e = n - 1;
-            for (int i = 0; i < n - 1; ++i) {
-                const float lo = __ldg(c0 + i), hi = __ldg(c0 + kRTabWidth + i);
-                if (r1 <= fmaf(fe, hi - lo, lo)) {
-                    e = i;
-                    break;
-                }
-            }
-            const float a = __ldg(&M->a[e]), ia = __ldg(&M->ia[e]);
-            const float c = formFactorIntegral(T * ia);
-            const float y = r2 * c;
-            float om;
-            if (y < 0.5f) {
-                om = 1.0f - y;
-            } else {
-                const float b = 1.0f + T * ia;
-                om = (1.0f - r2) + r2 * __frcp_rn(b * b * b);
-            }
-            const float sr = rcbrtf(om);
-            const float t = a * y * __frcp_rn(om * fmaf(sr, sr + 1.0f, 1.0f));
-            const float mu = 1.0f - 2.0f * t / T;
-            if (2.0f * r3 <= 1.0f + mu * mu)
-                return mu;
-        }
-        err |= kErrRejectLimit;
-        return 1.0f;
+        return 1.0f - oneMinusCos(rtab, ie, fe, r.u());
     }
 
     // Correction level 2, photoelectric absorption: the absorbing element by its share

@@ -28,14 +28,11 @@ constexpr int kMaxBowtie = 64;
 constexpr int kTableNE = DXMCG_NE;
 constexpr uint32_t kMaxStepsPerHistory = 1000000;
 constexpr int kMaxRejections = 100000;
-// Rayleigh element choice: per material and table energy E_i, the cumulative shares
-// C_k = sum_{j<=k} G_j / sum_j G_j of the elements' form-factor integrals G_j (k < n;
-// entries k >= n - 1 hold 1), interpolated linearly in E between table energies.
-constexpr int kRTabWidth = DXMCG_MAX_ELEMENTS;
-// Compton angle: per material and table energy E_i, 1 - cos theta at the cumulative
-// probabilities u_j = 1 - (1 - j / (kCTabK - 1))^2 of the Klein-Nishina x S(x) / Z
-// distribution (S = 1 at correction 0), j = 0 .. kCTabK - 1: 2 at j = 0, 0 at the last.
-// The u grid is densest towards cos theta = 1, where S changes fastest.
+// Compton and Rayleigh angles: per material and table energy E_i, 1 - cos theta at the
+// cumulative probabilities u_j = (1 - cos(pi j / (kCTabK - 1)))/2 of the Klein-Nishina x
+// S(x) / Z distribution (S = 1 at correction 0), or of the Rayleigh distribution
+// (1 + cos^2)/2 F^2(x), j = 0 .. kCTabK - 1: 2 at j = 0, 0 at the last.  The u grid is
+// densest at both ends: the narrow forward peak and the long backward tail.
 constexpr int kCTabK = 256;
 
 struct DevMaterial {
@@ -113,7 +110,7 @@ struct DevJob {
     const float4* xs;
     const float* maj;
     const DevMaterial* mats;
-    const float* rtab; // [n_mats][kTableNE][kRTabWidth] cumulative Rayleigh element shares
+    const float* rtab; // [n_mats][kTableNE][kCTabK] Rayleigh 1 - cos theta quantiles
     const float* ctab; // [n_mats][kTableNE][kCTabK] Compton 1 - cos theta quantiles
     int n_mats;
     int correction;

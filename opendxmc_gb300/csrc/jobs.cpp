@@ -146,119 +146,145 @@ void buildDeviceTables(const dxmcg_material* mats, int M, int correction, const 
 }
 
 namespace {
-    // Quantiles of 1 - cos theta for one material and correction level, all table
-    // energies.  The distribution KN(mu) S(t(mu)) / Z is integrated by the trapezoid
-    // rule on 512 equal steps of w = sqrt((1 - mu) / 2), which crowds the points
-    // towards mu = 1 where S rises (dmu = -4 w dw); each quantile is found by linear
-    // interpolation of the cumulative sum in w.  Kolmogorov distance of the sampled
-    // distribution from the exact one: about 1.5e-5 for water, 5-150 keV.
+    constexpr double kPi = 3.14159265358979323846;
+
+    // One row of angle quantiles: 1 - cos theta at the cumulative probabilities
+    // u_j = (1 - cos(pi j/(K-1)))/2, dense at both ends (the narrow peak towards
+    // mu = 1 and the long backward tail of the Rayleigh distribution), for a density
+    // f(1 - cos theta) on mu in [-1, 1].  The density is integrated by the trapezoid rule
+    // on G equal steps of s, where w = sqrt((1 - mu)/2) = s^P (dmu = -4 w P s^(P-1) ds
+    // crowds the points towards mu = 1), and each quantile is found by linear
+    // interpolation of the cumulative sum.
+    template <int G, int P, class F>
+    void quantileRow(F density, float* row)
+    {
+        double cum[G + 1];
+        auto weight = [&](int g) {
+            const double sg = static_cast<double>(g) / G;
+            const double w = P == 1 ? sg : sg * sg;
+            const double dw = P == 1 ? 1.0 : 2.0 * sg;
+            return density(2.0 * w * w) * 4.0 * w * dw;
+        };
+        cum[0] = 0.0;
+        double prev = weight(0);
+        for (int g = 1; g <= G; ++g) {
+            const double cur = weight(g);
+            cum[g] = cum[g - 1] + 0.5 * (prev + cur);
+            prev = cur;
+        }
+        int g = 0;
+        for (int j = kCTabK - 1; j >= 0; --j) { // the mass c grows as j falls
+            // mass from mu = 1 down to the quantile: 1 - u_j
+            const double c = 0.5 * (1.0 + std::cos(kPi * j / (kCTabK - 1))) * cum[G];
+            while (g < G - 1 && cum[g + 1] < c)
+                ++g;
+            const double d = cum[g + 1] - cum[g];
+            const double sg = (g + (d > 0.0 ? std::min(1.0, std::max(0.0, (c - cum[g]) / d)) : 0.0)) / G;
+            const double w = P == 1 ? sg : sg * sg;
+            row[j] = static_cast<float>(2.0 * w * w);
+        }
+        row[0] = 2.0f;
+        row[kCTabK - 1] = 0.0f;
+    }
+
+    constexpr double kMeKeV = 510.99895, kHcKeVA = 12.398419843;
+
+    // Compton: KN(mu) S(t(mu)) / Z (S = 1 at correction 0), 1024 steps of s = w^(1/2).
+    // Kolmogorov distance of the sampled distribution from the exact one: about 1.2e-5
+    // for water, 5-150 keV.
     std::vector<float> comptonAngleRows(const dxmcg_material& mat, int correction)
     {
-        constexpr double kMeKeV = 510.99895, kHcKeVA = 12.398419843;
-        constexpr int G = 512;
         const auto s = samplingElements(mat);
         std::vector<float> out(static_cast<size_t>(kNE) * kCTabK);
-        std::vector<double> cum(G + 1);
         for (int i = 0; i < kNE; ++i) {
             const double E = kEmin + i * kDE;
             const double k = E / kMeKeV;
             const double q2 = (E / kHcKeVA) * (E / kHcKeVA);
-            auto density = [&](int g) {
-                const double w = static_cast<double>(g) / G;
-                const double omu = 2.0 * w * w, mu = 1.0 - omu;
-                const double P = 1.0 / (1.0 + k * omu);
-                double f = P * P * (P + 1.0 / P - 1.0 + mu * mu) * 4.0 * w;
-                if (correction >= 1 && s.Zsum > 0) {
-                    const double t = q2 * 0.5 * omu;
-                    double S = 0.0;
-                    for (int e = 0; e < s.n; ++e) {
-                        const double b = 1.0 + t / s.a[e];
-                        const double b2 = b * b;
-                        S += s.nZ[e] * (1.0 - 1.0 / (b2 * b2));
+            quantileRow<1024, 2>(
+                [&](double omu) {
+                    const double mu = 1.0 - omu;
+                    const double P = 1.0 / (1.0 + k * omu);
+                    double f = P * P * (P + 1.0 / P - 1.0 + mu * mu);
+                    if (correction >= 1 && s.Zsum > 0) {
+                        const double t = q2 * 0.5 * omu;
+                        double S = 0.0;
+                        for (int e = 0; e < s.n; ++e) {
+                            const double b = 1.0 + t / s.a[e];
+                            const double b2 = b * b;
+                            S += s.nZ[e] * (1.0 - 1.0 / (b2 * b2));
+                        }
+                        f *= S / s.Zsum;
                     }
-                    f *= S / s.Zsum;
-                }
-                return f;
-            };
-            cum[0] = 0.0;
-            double prev = density(0);
-            for (int g = 1; g <= G; ++g) {
-                const double cur = density(g);
-                cum[g] = cum[g - 1] + 0.5 * (prev + cur);
-                prev = cur;
-            }
-            float* row = out.data() + static_cast<size_t>(i) * kCTabK;
-            int g = 0;
-            for (int j = kCTabK - 1; j >= 0; --j) { // the mass c grows as j falls
-                // mass from mu = 1 down to the quantile: 1 - u_j
-                const double v = 1.0 - static_cast<double>(j) / (kCTabK - 1);
-                const double c = v * v * cum[G];
-                while (g < G - 1 && cum[g + 1] < c)
-                    ++g;
-                const double d = cum[g + 1] - cum[g];
-                const double w = (g + (d > 0.0 ? std::min(1.0, std::max(0.0, (c - cum[g]) / d)) : 0.0)) / G;
-                row[j] = static_cast<float>(2.0 * w * w);
-            }
-            row[0] = 2.0f;
-            row[kCTabK - 1] = 0.0f;
+                    return f;
+                },
+                out.data() + static_cast<size_t>(i) * kCTabK);
         }
         return out;
     }
 
-    std::mutex g_comptonMutex;
-    std::map<std::vector<double>, std::vector<float>> g_comptonRows;
-    uint64_t g_comptonGeneration = ~0ull;
+    // Rayleigh: (1 + mu^2)/2 sum_i n_i Z_i^2 (1 + t/a_i)^-4 with t = x^2, 1024 steps of
+    // s = w^(1/2) (the distribution narrows towards mu = 1 as E grows).  Kolmogorov
+    // distance about 4e-5 for water, 5-150 keV.
+    std::vector<float> rayleighAngleRows(const dxmcg_material& mat)
+    {
+        const auto s = samplingElements(mat);
+        std::vector<float> out(static_cast<size_t>(kNE) * kCTabK);
+        for (int i = 0; i < kNE; ++i) {
+            const double E = kEmin + i * kDE;
+            const double q2 = (E / kHcKeVA) * (E / kHcKeVA);
+            quantileRow<1024, 2>(
+                [&](double omu) {
+                    const double mu = 1.0 - omu;
+                    const double t = q2 * 0.5 * omu;
+                    double F2 = 0.0;
+                    for (int e = 0; e < s.n; ++e) {
+                        const double b = 1.0 + t / s.a[e];
+                        const double b2 = b * b;
+                        F2 += s.nZ2[e] / (b2 * b2);
+                    }
+                    return 0.5 * (1.0 + mu * mu) * F2;
+                },
+                out.data() + static_cast<size_t>(i) * kCTabK);
+        }
+        return out;
+    }
+
+    std::mutex g_angleMutex;
+    std::map<std::vector<double>, std::vector<float>> g_angleRows;
+    uint64_t g_angleGeneration = ~0ull;
+
+    // kind 0: Compton at correction 0, 1: Compton at correction >= 1, 2: Rayleigh
+    void angleTables(const dxmcg_material* mats, int M, int kind, float* out)
+    {
+        for (int m = 0; m < M; ++m) {
+            std::vector<double> key { static_cast<double>(kind) };
+            for (int e = 0; e < mats[m].n; ++e) {
+                key.push_back(mats[m].Z[e]);
+                key.push_back(mats[m].w[e]);
+            }
+            std::lock_guard<std::mutex> lock(g_angleMutex);
+            if (g_angleGeneration != physicsGeneration()) {
+                g_angleRows.clear();
+                g_angleGeneration = physicsGeneration();
+            }
+            auto it = g_angleRows.find(key);
+            if (it == g_angleRows.end())
+                it = g_angleRows
+                         .emplace(key, kind == 2 ? rayleighAngleRows(mats[m]) : comptonAngleRows(mats[m], kind))
+                         .first;
+            std::copy(it->second.begin(), it->second.end(), out + static_cast<size_t>(m) * kNE * kCTabK);
+        }
+    }
 } // namespace
 
 void buildComptonAngleTables(const dxmcg_material* mats, int M, int correction, float* out)
 {
-    for (int m = 0; m < M; ++m) {
-        // key: correction level (0 or >= 1 share nothing), then (Z, w) pairs
-        std::vector<double> key { static_cast<double>(correction >= 1 ? 1 : 0) };
-        for (int e = 0; e < mats[m].n; ++e) {
-            key.push_back(mats[m].Z[e]);
-            key.push_back(mats[m].w[e]);
-        }
-        const std::vector<float>* rows = nullptr;
-        {
-            std::lock_guard<std::mutex> lock(g_comptonMutex);
-            if (g_comptonGeneration != physicsGeneration()) {
-                g_comptonRows.clear();
-                g_comptonGeneration = physicsGeneration();
-            }
-            auto it = g_comptonRows.find(key);
-            if (it == g_comptonRows.end())
-                it = g_comptonRows.emplace(key, comptonAngleRows(mats[m], correction)).first;
-            rows = &it->second;
-            std::copy(rows->begin(), rows->end(), out + static_cast<size_t>(m) * kNE * kCTabK);
-        }
-    }
+    angleTables(mats, M, correction >= 1 ? 1 : 0, out);
 }
 
-void buildRayleighTables(const dxmcg_material* mats, int M, float* out)
+void buildRayleighAngleTables(const dxmcg_material* mats, int M, float* out)
 {
-    constexpr double kHcKeVA = 12.398419843; // keV * Angstrom
-    for (int m = 0; m < M; ++m) {
-        const auto s = samplingElements(mats[m]);
-        for (int i = 0; i < kNE; ++i) {
-            const double E = kEmin + i * kDE;
-            const double T = (E / kHcKeVA) * (E / kHcKeVA);
-            double G[kRTabWidth] = {};
-            double sum = 0.0;
-            for (int k = 0; k < s.n; ++k) {
-                const double x = T / s.a[k];
-                const double b = 1.0 + x;
-                G[k] = s.nZ2[k] * s.a[k] * (x * (3.0 + x * (3.0 + x)) / (b * b * b));
-                sum += G[k];
-            }
-            float* row = out + (static_cast<size_t>(m) * kNE + i) * kRTabWidth;
-            double acc = 0.0;
-            for (int k = 0; k < kRTabWidth; ++k) {
-                acc += G[k];
-                row[k] = k + 1 >= s.n || !(sum > 0.0) ? 1.0f : static_cast<float>(acc / sum);
-            }
-        }
-    }
+    angleTables(mats, M, 2, out);
 }
 
 void buildBackgroundMajorant(const float* tot0, double rho0, float* out)

@@ -37,12 +37,10 @@ void materialTables(const dxmcg_material& m, int correction, double* photo, doub
 // majorant of material 0 alone: rho0 x its total attenuation, with the same safety
 // factor and floor as the grid's majorant
 void buildBackgroundMajorant(const float* tot0, double rho0, float* out);
-// Rayleigh element choice: out[m][i][k] (kRTabWidth per row) = cumulative share of
-// elements 0..k in material m's form-factor integral at table energy i
-void buildRayleighTables(const dxmcg_material* mats, int M, float* out);
-// Compton angle quantiles out[m][i][j] (kCTabK per row; see kCTabK), kept per
-// (composition, correction) for the life of the physics tables
+// Compton and Rayleigh angle quantiles out[m][i][j] (kCTabK per row; see kCTabK),
+// kept per (composition, correction) for the life of the physics tables
 void buildComptonAngleTables(const dxmcg_material* mats, int M, int correction, float* out);
+void buildRayleighAngleTables(const dxmcg_material* mats, int M, float* out);
 // two-region Woodcock: the box {lo x, y, z, hi x, y, z} of the voxels whose material is
 // neither 0 nor transparent (hi x = -1: none) is worth a second region when it leaves
 // part of the grid out; setTwoRegion fills J's box fields and material 0's majorant

@@ -9,7 +9,7 @@
 // and run statistics, the validation flags and per-material maximum densities,
 // the attenuation tables and majorants, the Compton angle and Rayleigh share tables,
 // the two-region box, the exposure list, the spectra and the bowtie profiles -- lives
-// in one file-scope __device__ array of kScratchBytes = 6 MiB.  Every GPU that loads
+// in one file-scope __device__ array of kScratchBytes = 12 MiB.  Every GPU that loads
 // the library holds that array until the process exits.
 //
 // The host finds the array's device address with cudaGetSymbolAddress, once per
@@ -41,7 +41,7 @@
 namespace dxmcg {
 namespace {
 
-    constexpr size_t kScratchBytes = 6u * 1024u * 1024u;
+    constexpr size_t kScratchBytes = 12u * 1024u * 1024u;
     constexpr int kMaxMaterials = 16;
     constexpr int kMaxExposures = 4096;
     constexpr int kMaxDevices = 64;
@@ -62,7 +62,7 @@ namespace {
     constexpr size_t kOffExps = alignUp(kOffXs + kMaxMaterials * kTableNE * sizeof(float4));
     constexpr size_t kOffCTab = alignUp(kOffExps + kMaxExposures * sizeof(DevExposure));
     constexpr size_t kOffRTab = alignUp(kOffCTab + kMaxMaterials * kTableNE * kCTabK * sizeof(float));
-    constexpr size_t kOffBox = alignUp(kOffRTab + kMaxMaterials * kTableNE * kRTabWidth * sizeof(float)); // 6 ints
+    constexpr size_t kOffBox = alignUp(kOffRTab + kMaxMaterials * kTableNE * kCTabK * sizeof(float)); // 6 ints
     constexpr size_t kOffMajOut = alignUp(kOffBox + 6 * sizeof(int));
     constexpr size_t kUsed = kOffMajOut + kTableNE * sizeof(float);
     static_assert(kUsed <= kScratchBytes, "scratch layout exceeds the static array");
@@ -245,8 +245,8 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
     std::vector<float> ctab(static_cast<size_t>(n_materials) * kTableNE * kCTabK);
     buildComptonAngleTables(materials, n_materials, correction, ctab.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffCTab, ctab.data(), ctab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
-    std::vector<float> rtab(static_cast<size_t>(n_materials) * kTableNE * kRTabWidth);
-    buildRayleighTables(materials, n_materials, rtab.data());
+    std::vector<float> rtab(static_cast<size_t>(n_materials) * kTableNE * kCTabK);
+    buildRayleighAngleTables(materials, n_materials, rtab.data());
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffRTab, rtab.data(), rtab.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     NOALLOC_CUDA(cudaMemcpyAsync(base + kOffMaj, maj.data(), maj.size() * sizeof(float), cudaMemcpyHostToDevice, s));
     const bool twoRegion = woodcock && twoRegionBox(hostBox, dims) && twoRegionFor(o, boxFraction(hostBox, dims));

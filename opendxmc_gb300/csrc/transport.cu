@@ -606,8 +606,7 @@ namespace {
                     Ep = sampleCompton(ph.E, J.mats + pm, J.ctab + pm * (kTableNE * kCTabK), ec.ie, ec.fe,
                         J.correction, rng, cost, err);
                 else if (rayleigh)
-                    cost = sampleRayleigh(ph.E, J.mats + pm, J.rtab + pm * (kTableNE * kRTabWidth), ec.ie, ec.fe,
-                        rng, err);
+                    cost = sampleRayleigh(J.rtab + pm * (kTableNE * kCTabK), ec.ie, ec.fe, rng);
                 if (compton || rayleigh)
                     scatterDirection(ph.dx, ph.dy, ph.dz, cost, rng.u());
                 if (compton) {

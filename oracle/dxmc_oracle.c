@@ -1284,59 +1284,119 @@ static void isotropic_dir(double d[3], double u1, double u2)
     d[2] = ct;
 }
 
-/* Compton angle (the transport kernel's sampler, jobs.cpp comptonAngleRows and
- * device.cuh sampleCompton): per table energy E_i, 1 - cos theta at the cumulative
- * probabilities u_j = 1 - (1 - j/(K-1))^2 of KN(mu) S(t(mu)) / Z (S = 1 at correction
- * 0), integrated by the trapezoid rule on 512 equal steps of w = sqrt((1 - mu)/2) and
- * inverted linearly.  A draw interpolates rows ie and ie + 1 at j = (K-1)(1 - sqrt(1-u)). */
+/* Compton and Rayleigh angles (the transport kernel's samplers, jobs.cpp
+ * comptonAngleRows / rayleighAngleRows and device.cuh): per table energy E_i, 1 - cos
+ * theta at the cumulative probabilities u_j = (1 - cos(pi j/(K-1)))/2 of KN(mu) S(t(mu))
+ * / Z (S = 1 at correction 0), or of (1 + mu^2)/2 F^2(x), integrated by the trapezoid rule
+ * on 1024 equal steps of s with w = sqrt((1 - mu)/2) = s^2 and inverted linearly.  A draw
+ * interpolates rows ie and ie + 1 at j = (K-1) acos(1 - 2u) / pi. */
 #define OR_CTAB_K 256
 static inline void grid_pos(double E, int* i, double* f);
 
-static void compton_rows(const mat_sampling* m, int correction, int i0, int i1, double* out)
+/* One row of angle quantiles for a density f(1 - cos theta): trapezoid rule on G
+ * equal steps of s with w = sqrt((1 - mu)/2) = s^P, inverted linearly. */
+typedef double (*angle_density)(double omu, const void* ctx);
+
+static void quantile_row(angle_density f, const void* ctx, int G, int P, double* row)
 {
-    enum { G = 512 };
-    double cum[G + 1];
+    double* cum = (double*)malloc((size_t)(G + 1) * sizeof(double));
+    double prev = 0.0;
+    for (int g = 0; g <= G; ++g) {
+        const double sg = (double)g / G;
+        const double w = P == 1 ? sg : sg * sg;
+        const double dw = P == 1 ? 1.0 : 2.0 * sg;
+        const double cur = f(2.0 * w * w, ctx) * 4.0 * w * dw;
+        cum[g] = g == 0 ? 0.0 : cum[g - 1] + 0.5 * (prev + cur);
+        prev = cur;
+    }
+    int g = 0;
+    for (int j = OR_CTAB_K - 1; j >= 0; --j) {
+        const double c = 0.5 * (1.0 + cos(PI * j / (OR_CTAB_K - 1))) * cum[G];
+        while (g < G - 1 && cum[g + 1] < c)
+            ++g;
+        const double d = cum[g + 1] - cum[g];
+        double fr = d > 0.0 ? (c - cum[g]) / d : 0.0;
+        fr = fr < 0.0 ? 0.0 : (fr > 1.0 ? 1.0 : fr);
+        const double sg = (g + fr) / G;
+        const double w = P == 1 ? sg : sg * sg;
+        row[j] = 2.0 * w * w;
+    }
+    row[0] = 2.0;
+    row[OR_CTAB_K - 1] = 0.0;
+    free(cum);
+}
+
+typedef struct {
+    const mat_sampling* m;
+    int correction;
+    double k, q2;
+} angle_ctx;
+
+/* KN(mu) S(t(mu)) / Z, S = 1 at correction 0 */
+static double compton_density(double omu, const void* c)
+{
+    const angle_ctx* x = (const angle_ctx*)c;
+    const double mu = 1.0 - omu;
+    const double P = 1.0 / (1.0 + x->k * omu);
+    double f = P * P * (P + 1.0 / P - 1.0 + mu * mu);
+    if (x->correction >= 1 && x->m->Zsum > 0.0) {
+        const double t = x->q2 * 0.5 * omu;
+        double S = 0.0;
+        for (int e = 0; e < x->m->n; ++e) {
+            const double b = 1.0 + t / x->m->a[e];
+            const double b2 = b * b;
+            S += x->m->nZ[e] * (1.0 - 1.0 / (b2 * b2));
+        }
+        f *= S / x->m->Zsum;
+    }
+    return f;
+}
+
+/* (1 + mu^2)/2 sum_i n_i Z_i^2 (1 + t/a_i)^-4 */
+static double rayleigh_density(double omu, const void* c)
+{
+    const angle_ctx* x = (const angle_ctx*)c;
+    const double mu = 1.0 - omu;
+    const double t = x->q2 * 0.5 * omu;
+    double F2 = 0.0;
+    for (int e = 0; e < x->m->n; ++e) {
+        const double b = 1.0 + t / x->m->a[e];
+        const double b2 = b * b;
+        F2 += x->m->nZ2[e] / (b2 * b2);
+    }
+    return 0.5 * (1.0 + mu * mu) * F2;
+}
+
+/* rows i0 .. i1 of a material's angle table: Compton (kind 0) or Rayleigh (kind 1) */
+static void angle_rows(const mat_sampling* m, int kind, int correction, int i0, int i1, double* out)
+{
     for (int i = i0; i <= i1; ++i) {
         const double E = OR_EMIN + i * OR_DE;
-        const double k = E / ME_KEV;
-        const double q2 = (E / HC_KEV_A) * (E / HC_KEV_A);
-        double prev = 0.0;
-        cum[0] = 0.0;
-        for (int g = 0; g <= G; ++g) {
-            const double w = (double)g / G;
-            const double omu = 2.0 * w * w, mu = 1.0 - omu;
-            const double P = 1.0 / (1.0 + k * omu);
-            double f = P * P * (P + 1.0 / P - 1.0 + mu * mu) * 4.0 * w;
-            if (correction >= 1 && m->Zsum > 0.0) {
-                const double t = q2 * 0.5 * omu;
-                double S = 0.0;
-                for (int e = 0; e < m->n; ++e) {
-                    const double b = 1.0 + t / m->a[e];
-                    const double b2 = b * b;
-                    S += m->nZ[e] * (1.0 - 1.0 / (b2 * b2));
-                }
-                f *= S / m->Zsum;
-            }
-            if (g > 0)
-                cum[g] = cum[g - 1] + 0.5 * (prev + f);
-            prev = f;
-        }
+        angle_ctx x = { m, correction, E / ME_KEV, (E / HC_KEV_A) * (E / HC_KEV_A) };
         double* row = out + (size_t)(i - i0) * OR_CTAB_K;
-        int g = 0;
-        for (int j = OR_CTAB_K - 1; j >= 0; --j) {
-            const double v = 1.0 - (double)j / (OR_CTAB_K - 1);
-            const double c = v * v * cum[G];
-            while (g < G - 1 && cum[g + 1] < c)
-                ++g;
-            const double d = cum[g + 1] - cum[g];
-            double fr = d > 0.0 ? (c - cum[g]) / d : 0.0;
-            fr = fr < 0.0 ? 0.0 : (fr > 1.0 ? 1.0 : fr);
-            const double w = (g + fr) / G;
-            row[j] = 2.0 * w * w;
-        }
-        row[0] = 2.0;
-        row[OR_CTAB_K - 1] = 0.0;
+        if (kind == 0)
+            quantile_row(compton_density, &x, 1024, 2, row);
+        else
+            quantile_row(rayleigh_density, &x, 1024, 2, row);
     }
+}
+
+static void compton_rows(const mat_sampling* m, int correction, int i0, int i1, double* out)
+{
+    angle_rows(m, 0, correction, i0, i1, out);
+}
+
+/* 1 - cos theta from rows ie and ie + 1 of an angle table */
+static double table_one_minus_cos(const double* rows, double fe, double u)
+{
+    const double jf = (OR_CTAB_K - 1) * acos(1.0 - 2.0 * u) / PI;
+    int j = (int)jf;
+    if (j > OR_CTAB_K - 2)
+        j = OR_CTAB_K - 2;
+    const double g = jf - j;
+    const double lo = rows[j] + g * (rows[j + 1] - rows[j]);
+    const double hi = rows[OR_CTAB_K + j] + g * (rows[OR_CTAB_K + j + 1] - rows[OR_CTAB_K + j]);
+    return lo + fe * (hi - lo);
 }
 
 /* rows: the material's rows ie and ie + 1 (2 x OR_CTAB_K) */
@@ -1345,15 +1405,7 @@ static double sample_compton(double E, const mat_sampling* m, int correction, co
 {
     const double k = E / ME_KEV;
     for (int guard = 0; guard < 100000; ++guard) {
-        const double u = rng_u(r);
-        const double jf = (OR_CTAB_K - 1) * (1.0 - sqrt(1.0 - u));
-        int j = (int)jf;
-        if (j > OR_CTAB_K - 2)
-            j = OR_CTAB_K - 2;
-        const double g = jf - j;
-        const double lo = rows[j] + g * (rows[j + 1] - rows[j]);
-        const double hi = rows[OR_CTAB_K + j] + g * (rows[OR_CTAB_K + j + 1] - rows[OR_CTAB_K + j]);
-        const double omu = lo + fe * (hi - lo); /* 1 - cos theta */
+        const double omu = table_one_minus_cos(rows, fe, rng_u(r)); /* 1 - cos theta */
         const double xm1 = k * omu;             /* x - 1, x = E / E' */
         *cos_theta = 1.0 - omu;
         if (correction >= 2) {
@@ -1368,39 +1420,12 @@ static double sample_compton(double E, const mat_sampling* m, int correction, co
     return E;
 }
 
-/* Rayleigh: pick an element by its share of the form-factor integral up to
- * x_max = E / hc, invert that element's F^2 distribution in t = x^2 analytically,
- * accept on (1 + cos^2) / 2 (the standard composition-rejection scheme). */
-static double sample_rayleigh(double E, const mat_sampling* m, rng_t* r)
+/* Rayleigh: cos theta from the material's quantile table of (1 + cos^2)/2 F^2(x)
+ * (the transport kernel's sampler, jobs.cpp rayleighAngleRows and device.cuh
+ * sampleRayleigh): rows ie and ie + 1, one uniform. */
+static double sample_rayleigh(const double* rows, double fe, rng_t* r)
 {
-    const double q = E / HC_KEV_A;
-    const double T = q * q;
-    double G[OR_MAX_ELEMENTS], c[OR_MAX_ELEMENTS];
-    double Gs = 0.0;
-    for (int i = 0; i < m->n; ++i) {
-        c[i] = -expm1(-3.0 * log1p(T / m->a[i]));
-        G[i] = m->nZ2[i] * m->a[i] * c[i];
-        Gs += G[i];
-    }
-    for (int guard = 0; guard < 100000; ++guard) {
-        const double r1 = rng_u(r), r2 = rng_u(r), r3 = rng_u(r);
-        int e = m->n - 1;
-        double acc = 0.0;
-        const double target = r1 * Gs;
-        for (int i = 0; i < m->n; ++i) {
-            acc += G[i];
-            if (target <= acc) {
-                e = i;
-                break;
-            }
-        }
-        const double y = r2 * c[e];
-        const double t = m->a[e] * expm1(-log1p(-y) / 3.0);
-        const double mu = 1.0 - 2.0 * t / T;
-        if (2.0 * r3 <= 1.0 + mu * mu)
-            return mu;
-    }
-    return 1.0;
+    return 1.0 - table_one_minus_cos(rows, fe, rng_u(r));
 }
 
 double or_sample_compton(double E, const or_composition* c, int correction, const double* u, int nu, int* used,
@@ -1428,6 +1453,16 @@ int or_compton_quantiles(const or_composition* c, int correction, int energy_ind
     mat_sampling m;
     make_sampling(c, &m);
     compton_rows(&m, correction, energy_index, energy_index, out);
+    return OR_CTAB_K;
+}
+
+int or_rayleigh_quantiles(const or_composition* c, int energy_index, double* out)
+{
+    if (energy_index < 0 || energy_index >= OR_NE)
+        return -1;
+    mat_sampling m;
+    make_sampling(c, &m);
+    angle_rows(&m, 1, 0, energy_index, energy_index, out);
     return OR_CTAB_K;
 }
 
@@ -1459,7 +1494,11 @@ double or_sample_rayleigh(double E, const or_composition* c, const double* u, in
     memset(&r, 0, sizeof(r));
     r.inj = u;
     r.n_inj = nu;
-    const double mu = sample_rayleigh(E, &m, &r);
+    int ie;
+    double fe, rows[2 * OR_CTAB_K];
+    grid_pos(E, &ie, &fe);
+    angle_rows(&m, 1, 0, ie, ie + 1, rows);
+    const double mu = sample_rayleigh(rows, fe, &r);
     *used = r.used;
     return mu;
 }
@@ -1485,6 +1524,7 @@ struct or_world {
     double* tot;
     double maj[OR_NE]; /* 1/cm */
     double* ctab;      /* [m][OR_NE][OR_CTAB_K] Compton 1 - cos theta quantiles */
+    double* rtab;      /* [m][OR_NE][OR_CTAB_K] Rayleigh 1 - cos theta quantiles */
     /* two-region Woodcock: the box of voxels whose material is neither 0 nor
      * transparent (voxel indices b0 .. b1 inclusive), its faces widened by a margin,
      * and material 0's majorant; box_on 0: the box is empty or the whole grid */
@@ -1530,9 +1570,11 @@ or_world* or_world_create(const int32_t dims[3], const double spacing_cm[3], con
     for (int i = 0; i < OR_NE; ++i)
         E[i] = OR_EMIN + i * OR_DE;
     w->ctab = (double*)malloc((size_t)n_mats * OR_NE * OR_CTAB_K * sizeof(double));
+    w->rtab = (double*)malloc((size_t)n_mats * OR_NE * OR_CTAB_K * sizeof(double));
     for (int m = 0; m < n_mats; ++m) {
         make_sampling(&mats[m], &w->samp[m]);
         compton_rows(&w->samp[m], correction, 0, OR_NE - 1, w->ctab + (size_t)m * OR_NE * OR_CTAB_K);
+        angle_rows(&w->samp[m], 1, 0, 0, OR_NE - 1, w->rtab + (size_t)m * OR_NE * OR_CTAB_K);
         or_attenuation(&mats[m], correction, OR_NE, E, w->photo + m * OR_NE, w->incoh + m * OR_NE,
             w->coh + m * OR_NE);
         for (int i = 0; i < OR_NE; ++i)
@@ -1606,6 +1648,7 @@ void or_world_destroy(or_world* w)
     free(w->cnt);
     free(w->mscale);
     free(w->ctab);
+    free(w->rtab);
     free(w);
 }
 
@@ -1928,7 +1971,7 @@ static int interact(or_world* w, size_t v, int m, double* E, double wgt, double 
         return 1;
     }
     st->n_rayleigh++;
-    const double cost = sample_rayleigh(*E, &w->samp[m], r);
+    const double cost = sample_rayleigh(w->rtab + ((size_t)m * OR_NE + ie) * OR_CTAB_K, fe, r);
     scatter_dir(d, cost, rng_u(r));
     return 1;
 }

@@ -197,6 +197,8 @@ int or_world_set_macro(or_world* w, int B, double* scale_out);
 /* Compton angle table row: 1 - cos theta at u_j = 1 - (1 - j/(K-1))^2, j < K (returns
  * K = 256), for table energy OR_EMIN + energy_index * OR_DE */
 int or_compton_quantiles(const or_composition* c, int correction, int energy_index, double* out);
+/* the same for the Rayleigh angle, (1 + cos^2)/2 F^2(x) */
+int or_rayleigh_quantiles(const or_composition* c, int energy_index, double* out);
 int or_transport(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, int tracking,
     int n_threads, uint64_t hist_begin, uint64_t hist_end, or_stats* stats);
 int or_sample_source(or_world* w, const or_beam* b, uint64_t seed, uint32_t stream, uint64_t h0, int n,

@@ -191,6 +191,8 @@ def lib() -> C.CDLL:
     L.or_sample_compton.argtypes = [d, C.POINTER(Composition), i, pd, i, C.POINTER(C.c_int), pd]
     L.or_compton_quantiles.restype = i
     L.or_compton_quantiles.argtypes = [C.POINTER(Composition), i, i, pd]
+    L.or_rayleigh_quantiles.restype = i
+    L.or_rayleigh_quantiles.argtypes = [C.POINTER(Composition), i, pd]
     L.or_sample_photoelectric.restype = d
     L.or_sample_photoelectric.argtypes = [d, C.POINTER(Composition), pd, i, C.POINTER(C.c_int), pd]
     L.or_compton_shells.restype = i
@@ -391,6 +393,15 @@ def compton_quantiles(zw, correction, energy_index):
     out = np.zeros(256)
     c = Composition.from_dict(zw)
     if lib().or_compton_quantiles(C.byref(c), correction, energy_index, _p(out, C.c_double)) != 256:
+        raise ValueError("energy index out of range")
+    return out
+
+
+def rayleigh_quantiles(zw, energy_index):
+    """1 - cos theta of the Rayleigh angle table at u_j = 1 - (1 - j/(K-1))^2."""
+    out = np.zeros(256)
+    c = Composition.from_dict(zw)
+    if lib().or_rayleigh_quantiles(C.byref(c), energy_index, _p(out, C.c_double)) != 256:
         raise ValueError("energy index out of range")
     return out
 

@@ -381,14 +381,13 @@ def test_oracle_level2_transport_conserves_energy(oracle):
 def test_compton_angle_table_matches_klein_nishina_times_s(oracle, correction, index):
     """The Compton angle table against the distribution it stands for: KN(mu) S(x)/Z
     for water (S = 1 at correction 0), integrated here on 4e5 steps.  Sampling the
-    table inverts it linearly between its probabilities u_j = 1 - (1 - j/255)^2, so the
-    sampled distribution's CDF is the table's points joined linearly; its largest
+    table inverts it linearly between its probabilities u_j = (1 - cos(pi j/255))/2, so
+    the sampled distribution's CDF is the table's points joined linearly; its largest
     distance from the exact CDF (Kolmogorov distance) must stay below 5e-5."""
     E = oracle.EMIN + index * oracle.DE
     omu = oracle.compton_quantiles(P.WATER, correction, index)
     assert omu[0] == 2.0 and omu[-1] == 0.0 and np.all(np.diff(omu) <= 0)
-    j = np.arange(256) / 255.0
-    u = 1.0 - (1.0 - j) ** 2
+    u = 0.5 * (1.0 - np.cos(np.pi * np.arange(256) / 255.0))
     mu_tab = 1.0 - omu
     k = E / 510.99895
     mu = np.linspace(-1.0, 1.0, 400_001)
@@ -408,3 +407,30 @@ def test_compton_angle_table_matches_klein_nishina_times_s(oracle, correction, i
     cdf /= cdf[-1]
     implied = np.interp(mu, mu_tab, u)
     assert np.abs(implied - cdf).max() < 5e-5
+
+
+@pytest.mark.parametrize("index", [8, 38, 118, 298])  # 5, 20, 60 and 150 keV
+def test_rayleigh_angle_table_matches_form_factor(oracle, index):
+    """The Rayleigh angle table against (1 + mu^2)/2 sum_i n_i Z_i^2 (1 + t/a_i)^-4 for
+    water (t = x^2), integrated here on 2e6 steps of w = sqrt((1 - mu)/2) squared: the
+    sampled distribution (the table's points joined linearly in probability) is within
+    a Kolmogorov distance of 5e-5 of it."""
+    E = oracle.EMIN + index * oracle.DE
+    omu = oracle.rayleigh_quantiles(P.WATER, index)
+    assert omu[0] == 2.0 and omu[-1] == 0.0 and np.all(np.diff(omu) <= 0)
+    u = 0.5 * (1.0 - np.cos(np.pi * np.arange(256) / 255.0))
+    s = np.linspace(0.0, 1.0, 2_000_001)
+    w = s * s
+    om = 2.0 * w * w
+    mu = 1.0 - om
+    t = (E / 12.398419843) ** 2 * 0.5 * om
+    F2 = np.zeros_like(s)
+    for z, wt in P.WATER.items():
+        n = wt / {1: 1.008, 8: 15.999}[z]
+        a = (z ** (1 / 3) / (2 * np.pi * 0.529177210903)) ** 2
+        F2 += n * z * z / (1.0 + t / a) ** 4
+    f = 0.5 * (1.0 + mu * mu) * F2 * 4.0 * w * 2.0 * s  # density in s
+    mass = np.concatenate([[0.0], np.cumsum(0.5 * (f[1:] + f[:-1]) * np.diff(s))])
+    mass /= mass[-1]  # probability of 1 - cos theta below om
+    implied = 1.0 - np.interp(om[::-1], omu[::-1], u[::-1])[::-1]  # table's P(1 - cos < om)
+    assert np.abs(implied - mass).max() < 5e-5

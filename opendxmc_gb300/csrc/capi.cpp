@@ -146,6 +146,9 @@ struct dxmcg_world {
     // transparent (lo x, y, z, hi x, y, z), and material 0's majorant
     DeviceBuffer<int> boxBuf;
     DeviceBuffer<float> majOut;
+    // dose readback staging when the caller's arrays are not pinned host memory
+    DeviceBuffer<double> readDose, readVar;
+    DeviceBuffer<unsigned long long> readCount;
     int box[6] {};
     bool hasBox = false;
     std::vector<float> hostTot, hostMaj; // FP32 tables as uploaded
@@ -856,9 +859,8 @@ DXMCG_API int dxmcg_world_build(dxmcg_world* w)
         return fail(DXMCG_ERR_ARGUMENT, "world_build: a voxel's material index is >= the number of materials");
     if (host[256] & kErrBadDensity)
         return fail(DXMCG_ERR_ARGUMENT, "world_build: negative or non-finite density");
-    w->dens64.reset();
-    w->dens32.reset();
-    w->mat.reset();
+    // the staging arrays stay allocated: a caller that sets data and builds again each
+    // run (a new patient, the same grid) then allocates nothing
 
     w->rhoMax.assign(M, 0.0);
     for (int m = 0; m < M; ++m) {
@@ -975,30 +977,57 @@ DXMCG_API int dxmcg_world_read_tally(dxmcg_world* w, double* energy, double* ene
     return DXMCG_OK;
 }
 
+namespace {
+// Device address of caller memory the GPU can write directly: pinned host memory
+// (mapped under unified addressing) or device memory; nullptr for pageable memory.
+void* deviceWritable(void* p)
+{
+    if (!p)
+        return nullptr;
+    cudaPointerAttributes a {};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return p;
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+} // namespace
+
 DXMCG_API int dxmcg_world_read_dose(dxmcg_world* w, double* dose, double* variance, uint64_t* count)
 {
     if (!w || !w->built)
         return fail(DXMCG_ERR_STATE, "world_read_dose: world not built");
     DXMCG_CUDA(cudaSetDevice(w->device));
-    // finalize on the device into a scratch block, then one copy per array
-    DeviceBuffer<double> d, v;
-    DeviceBuffer<unsigned long long> c;
-    if (dose)
-        DXMCG_CUDA(d.alloc(w->N));
-    if (variance)
-        DXMCG_CUDA(v.alloc(w->N));
-    if (count)
-        DXMCG_CUDA(c.alloc(w->N));
+    // The finalize kernel writes straight into arrays the GPU can address (pinned host
+    // memory over the host link, or device memory); the others are staged in the
+    // world's readback buffers and copied.
+    double* dd = static_cast<double*>(deviceWritable(dose));
+    double* dv = static_cast<double*>(deviceWritable(variance));
+    auto* dc = static_cast<unsigned long long*>(deviceWritable(count));
+    if (dose && !dd) {
+        DXMCG_CUDA(w->readDose.alloc(w->N));
+        dd = w->readDose.p;
+    }
+    if (variance && !dv) {
+        DXMCG_CUDA(w->readVar.alloc(w->N));
+        dv = w->readVar.p;
+    }
+    if (count && !dc) {
+        DXMCG_CUDA(w->readCount.alloc(w->N));
+        dc = w->readCount.p;
+    }
     cudaError_t e = launchFinalize(w->tally.p, w->vox.p, w->N, kKeVToMilliGrayGram / w->voxelVolume,
-        w->historiesScored, dose ? d.p : nullptr, variance ? v.p : nullptr, count ? c.p : nullptr, w->stream);
+        w->historiesScored, dd, dv, dc, w->stream);
     if (e != cudaSuccess)
         return cudaFail(e, "finalize kernel");
-    if (dose)
-        DXMCG_CUDA(cudaMemcpyAsync(dose, d.p, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
-    if (variance)
-        DXMCG_CUDA(cudaMemcpyAsync(variance, v.p, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
-    if (count)
-        DXMCG_CUDA(cudaMemcpyAsync(count, c.p, w->N * sizeof(uint64_t), cudaMemcpyDeviceToHost, w->stream));
+    if (dose && dd == w->readDose.p)
+        DXMCG_CUDA(cudaMemcpyAsync(dose, dd, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    if (variance && dv == w->readVar.p)
+        DXMCG_CUDA(cudaMemcpyAsync(variance, dv, w->N * sizeof(double), cudaMemcpyDeviceToHost, w->stream));
+    if (count && dc == w->readCount.p)
+        DXMCG_CUDA(cudaMemcpyAsync(count, dc, w->N * sizeof(uint64_t), cudaMemcpyDeviceToHost, w->stream));
     DXMCG_CUDA(cudaStreamSynchronize(w->stream));
     return DXMCG_OK;
 }

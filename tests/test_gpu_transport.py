@@ -417,6 +417,28 @@ def test_dose_readout(c1, gpu):
     np.testing.assert_allclose(d, e * scale / rho.astype(np.float64), rtol=1e-12)
     var = np.maximum(e2 - e * e / st["n_histories"], 0) * (scale / rho.astype(np.float64)) ** 2
     np.testing.assert_allclose(v, var, rtol=1e-9, atol=1e-300)
+    # pinned host arrays take the direct path (the kernel writes them over the host
+    # link), device arrays too; both give the staged result exactly
+    import torch
+
+    pinned = (torch.zeros(gw.N, dtype=torch.float64, pin_memory=True).numpy(),
+              torch.zeros(gw.N, dtype=torch.float64, pin_memory=True).numpy(),
+              torch.zeros(gw.N, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64))
+    dp, vp, cp = gw.dose(out=pinned)
+    np.testing.assert_array_equal(dp, d)
+    np.testing.assert_array_equal(vp, v)
+    np.testing.assert_array_equal(cp, c2)
+    dev = [torch.zeros(gw.N, dtype=torch.float64, device="cuda:0") for _ in range(2)]
+    devc = torch.zeros(gw.N, dtype=torch.int64, device="cuda:0")
+    from opendxmc_gb300 import native as N
+    import ctypes as C
+
+    N.check(N.lib().dxmcg_world_read_dose(gw._h, C.cast(dev[0].data_ptr(), C.POINTER(C.c_double)),
+                                          C.cast(dev[1].data_ptr(), C.POINTER(C.c_double)),
+                                          C.cast(devc.data_ptr(), C.POINTER(C.c_uint64))))
+    np.testing.assert_array_equal(dev[0].cpu().numpy(), d)
+    np.testing.assert_array_equal(dev[1].cpu().numpy(), v)
+    np.testing.assert_array_equal(devc.cpu().numpy().view(np.uint64), c2)
 
 
 def test_invalid_material_index_rejected(gpu):

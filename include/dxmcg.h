@@ -202,7 +202,10 @@ typedef struct {
     uint64_t n_fluorescence; /* correction level 2: K fluorescence photons emitted */
     uint64_t n_voxel_reads;  /* voxel words read: n_visits less the tentative collisions
                                 the Woodcock gather skip settled from their cell bound */
-    uint64_t n_cell_reads;   /* gather-skip cell bounds read (n_visits when the skip ran) */
+    uint64_t n_cell_reads;   /* gather-skip cell bounds read (the tentative collisions inside
+                                the two-region box when the skip ran) */
+    int32_t woodcock_steps;  /* WOODCOCK tracking: steps per phase the launches used */
+    int32_t two_region;      /* WOODCOCK tracking: 1 when the run used two regions */
 } dxmcg_stats;
 
 typedef struct dxmcg_world dxmcg_world;

@@ -1148,6 +1148,8 @@ DXMCG_API int dxmcg_transport_run(dxmcg_world* w, const dxmcg_beam* beam, const 
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->dose_scale = kKeVToMilliGrayGram / w->voxelVolume;
         stats->calibration = calibration;
+        stats->woodcock_steps = o.tracking == DXMCG_TRACK_WOODCOCK ? shape.woodcock_steps : 0;
+        stats->two_region = J.boxOn;
     }
     if (progress)
         progress->setMessage(cancelled ? "Cancelled" : "Done");
@@ -1337,6 +1339,14 @@ DXMCG_API int dxmcg_batch_run(dxmcg_batch* b, dxmcg_stats* stats)
         stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         stats->dose_scale = kKeVToMilliGrayGram / b->worlds[0]->voxelVolume;
         stats->calibration = b->calibration[0];
+        const bool wood = b->tracking == DXMCG_TRACK_WOODCOCK || b->tracking == kTrackWoodcockBox;
+        stats->woodcock_steps = wood ? (b->perJob ? b->jobShapes[0].woodcock_steps : b->shape.woodcock_steps) : 0;
+        stats->two_region = 0;
+        if (b->perJob)
+            for (const auto& hj : b->hostJobs)
+                stats->two_region |= hj.boxOn;
+        else
+            stats->two_region = b->tracking == kTrackWoodcockBox ? 1 : 0;
     }
     return deviceErrors(c, "batch_run");
 }

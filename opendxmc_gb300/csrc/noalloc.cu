@@ -330,6 +330,8 @@ extern "C" DXMCG_API int dxmcg_transport_run_noalloc(const int32_t dims[3], cons
         stats->total_ms = ms;
         stats->dose_scale = 1.602176634e-10 / (spacing_cm[0] * spacing_cm[1] * spacing_cm[2]);
         stats->calibration = calibration;
+        stats->woodcock_steps = o.tracking == DXMCG_TRACK_WOODCOCK ? (shape.woodcock_steps > 0 ? shape.woodcock_steps : 8) : 0;
+        stats->two_region = twoRegion ? 1 : 0;
     }
     if (c.error_flags & kErrStepLimit)
         return fail(DXMCG_ERR_DEVICE, "transport_run_noalloc: a history exceeded the step limit");

@@ -167,7 +167,8 @@ class Stats(C.Structure):
                                   "n_cutoff", "n_errors", "n_interacted")] + [
         ("kernel_ms", C.c_double), ("total_ms", C.c_double), ("dose_scale", C.c_double),
         ("calibration", C.c_double), ("n_crossings", C.c_uint64),
-        ("n_fluorescence", C.c_uint64), ("n_voxel_reads", C.c_uint64), ("n_cell_reads", C.c_uint64)]
+        ("n_fluorescence", C.c_uint64), ("n_voxel_reads", C.c_uint64), ("n_cell_reads", C.c_uint64),
+        ("woodcock_steps", C.c_int32), ("two_region", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f[0]: getattr(self, f[0]) for f in self._fields_}

@@ -258,6 +258,19 @@ def test_oracle_woodcock_and_siddon_tracking_agree(oracle):
     assert e1.sum() == pytest.approx(e2.sum(), rel=0.01)
 
 
+def test_oracle_default_tracking_follows_the_box_fraction(oracle):
+    """The oracle's default Woodcock mirrors the transport kernel's: two regions when
+    the box of the voxels whose material is neither 0 nor transparent holds less than
+    half the grid's voxels."""
+    for ph, two in ((parity.small_torso(scale=4, seed=3), True), (parity.small_cylinder(), False)):
+        w = oracle.World(ph.dims, ph.spacing, ph.density, ph.material, ph.materials)
+        fg = (ph.material != 0) & (ph.material != 255)
+        idx = np.argwhere(fg)
+        frac = float(np.prod((idx.max(0) - idx.min(0) + 1) / np.array(ph.material.shape)))
+        assert w.box_fraction == pytest.approx(frac, abs=1e-12)
+        assert (w.box_fraction < oracle.TWO_REGION_BOX_FRACTION) == two
+
+
 def test_oracle_two_region_woodcock_equals_plain_woodcock(oracle):
     """Two-region Woodcock (material 0's own majorant outside the box of the other
     voxels) samples the plain Woodcock transport with fewer tentative collisions:

@@ -200,6 +200,25 @@ def test_two_region_woodcock_matches_plain_woodcock(gpu):
     assert gw.run(beam, gpu.run_options(seed=2, stream=1, hist_end=200_000))["n_visits"] == v2
 
 
+def test_launch_defaults_adapt_to_the_world(gpu):
+    """Steps per phase: 8 on a fresh world, then 1.4 / p (clamped to 4..16) with p the
+    stops (real collisions and escapes) per tentative collision of the world's previous
+    Woodcock run; an explicit setting wins.  Two regions: on for the torso (its box holds
+    less than half the grid), off for the cylinder that fills its grid."""
+    ph = parity.small_torso(scale=2, seed=4)
+    gw = gpu_world(gpu, ph)
+    beam = P.ct_spiral_params(particles=2000, scan_cm=10.0)
+    s1 = gw.run(beam, gpu.run_options(seed=3, hist_end=300_000))
+    assert s1["woodcock_steps"] == 8 and s1["two_region"] == 1
+    p = (s1["n_photo"] + s1["n_compton"] + s1["n_rayleigh"] + s1["n_histories"] - s1["n_missed"]) / s1["n_visits"]
+    s2 = gw.run(beam, gpu.run_options(seed=3, hist_end=300_000))
+    assert s2["woodcock_steps"] == int(np.clip(np.floor(1.4 / p + 0.5), 4, 16))
+    assert gw.run(beam, gpu.run_options(seed=3, hist_end=1000, woodcock_steps=12))["woodcock_steps"] == 12
+    assert gw.run(beam, gpu.run_options(seed=3, hist_end=1000, two_region=-1))["two_region"] == 0
+    cyl = gpu_world(gpu, parity.small_cylinder())
+    assert cyl.run(P.dx_beam_params(particles=1000, exposures=2))["two_region"] == 0
+
+
 def test_two_region_woodcock_shared_streams_match_oracle(gpu, oracle):
     """Shared streams: the kernel's two-region Woodcock and the oracle's restatement
     (TRACK_WOODCOCK_BOX) draw the same uniforms per history, so counts, visits and the

@@ -19,7 +19,7 @@ dataset exists for this path).
 `--impl reference` times that CPU implementation alone (the reference's own
 engine, DXMClib, is fetched by its build at configure time and is not available).
 N > 1 (torchrun): every rank runs its own full job on its own GPU with its own
-Philox stream (independent histories; weak scaling, no data-path collective).
+random stream (independent histories; weak scaling, no data-path collective).
 """
 from __future__ import annotations
 
@@ -429,7 +429,7 @@ def run_ours(args):
                        "l2": "256 MB buffer written before every step" + (
                            "; the 128x128x64 world (5 MB voxels, 34 MB tally) is L2-resident" if c1 else
                            "; tally " + ("3.4 GB" if big else "420 MB") + " > L2"),
-                       "parallelism": f"replicas x{world} (independent Philox streams)"},
+                       "parallelism": f"replicas x{world} (independent random streams)"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches_per_step * args.steps, "clocks": clk,
         }

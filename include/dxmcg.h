@@ -156,8 +156,8 @@ typedef struct {
 } dxmcg_exposure;
 
 typedef struct {
-    uint64_t seed;        /* Philox key */
-    uint32_t stream;      /* Philox counter word 1: independent stream per beam */
+    uint64_t seed;        /* random streams: seed */
+    uint32_t stream;      /* stream word: independent streams per beam or per replica */
     int32_t tracking;     /* dxmcg_tracking */
     int32_t normalize;    /* trailing bool of transport(...): scale dose to the beam's DAP */
     int32_t block_size;   /* 0 = library default / autotuned */
@@ -472,8 +472,6 @@ DXMCG_API int dxmcg_progress_message(const dxmcg_progress* p, char* buf, int cap
 /* Siddon traversal of n grid-local rays; per ray up to cap segments */
 DXMCG_API int dxmcg_siddon_trace(int n_rays, const float* origins, const float* directions, const int32_t dims[3],
     const float spacing[3], int cap, int64_t* voxel, float* length, int32_t* n_segments);
-/* Philox4x32-10 blocks */
-DXMCG_API int dxmcg_philox(int n, const uint32_t* counters, const uint32_t key[2], uint32_t* out);
 /* first n_draws raw 32-bit draws of the streams of histories h0 .. h0 + n_hist - 1 */
 DXMCG_API int dxmcg_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, int n_draws,
     uint32_t* out);

@@ -1,7 +1,7 @@
 // aux_kernels.cu -- kernels around the transport: voxel packing, gather-skip cell
 // bounds and the two-region Woodcock box at World::build, dose finalisation at
 // readout, and the device test hooks that run single pieces of the hot path
-// (traversal, Philox, samplers, source) on given inputs.
+// (traversal, history streams, samplers, source) on given inputs.
 #include <algorithm>
 #include <cfloat>
 #include <climits>
@@ -228,28 +228,14 @@ namespace {
         cnt[r] = c;
     }
 
-    __global__ void philoxKernel(int n, const uint32_t* __restrict__ c, uint32_t k0, uint32_t k1,
+    __global__ void streamKernel(unsigned long long key, unsigned long long h0, int nHist, int nDraws,
         uint32_t* __restrict__ out)
-    {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x;
-        if (i >= n)
-            return;
-        uint32_t a = c[4 * i], b = c[4 * i + 1], e = c[4 * i + 2], f = c[4 * i + 3];
-        philox10(a, b, e, f, k0, k1);
-        out[4 * i] = a;
-        out[4 * i + 1] = b;
-        out[4 * i + 2] = e;
-        out[4 * i + 3] = f;
-    }
-
-    __global__ void streamKernel(uint32_t k0, uint32_t k1, uint32_t stream, unsigned long long h0, int nHist,
-        int nDraws, uint32_t* __restrict__ out)
     {
         const int i = blockIdx.x * blockDim.x + threadIdx.x;
         if (i >= nHist)
             return;
         Rng r;
-        r.init(k0, k1, stream, h0 + i);
+        r.init(key, h0 + i);
         for (int k = 0; k < nDraws; ++k)
             out[static_cast<size_t>(i) * nDraws + k] = r.raw();
     }
@@ -312,7 +298,7 @@ namespace {
         if (i >= n)
             return;
         Rng r;
-        r.init(J.key0, J.key1, J.stream, h0 + i);
+        r.init(J.key, h0 + i);
         Photon ph;
         sampleSource(J, h0 + i, ph, r);
         float* o = out + 8 * static_cast<size_t>(i);
@@ -394,16 +380,10 @@ cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int
     return cudaGetLastError();
 }
 
-cudaError_t launchPhilox(int n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t s)
+cudaError_t launchHistoryStream(unsigned long long key, unsigned long long h0, int n_hist, int n_draws,
+    uint32_t* out, cudaStream_t s)
 {
-    philoxKernel<<<(n + 255) / 256, 256, 0, s>>>(n, ctr, k0, k1, out);
-    return cudaGetLastError();
-}
-
-cudaError_t launchHistoryStream(uint32_t k0, uint32_t k1, uint32_t stream, unsigned long long h0, int n_hist,
-    int n_draws, uint32_t* out, cudaStream_t s)
-{
-    streamKernel<<<(n_hist + 127) / 128, 128, 0, s>>>(k0, k1, stream, h0, n_hist, n_draws, out);
+    streamKernel<<<(n_hist + 127) / 128, 128, 0, s>>>(key, h0, n_hist, n_draws, out);
     return cudaGetLastError();
 }
 

@@ -1740,23 +1740,6 @@ DXMCG_API int dxmcg_siddon_trace(int n_rays, const float* origins, const float* 
     return DXMCG_OK;
 }
 
-DXMCG_API int dxmcg_philox(int n, const uint32_t* counters, const uint32_t key[2], uint32_t* out)
-{
-    if (n < 0 || !counters || !key || !out)
-        return fail(DXMCG_ERR_ARGUMENT, "philox: bad arguments");
-    if (n == 0)
-        return DXMCG_OK;
-    DeviceBuffer<uint32_t> c, o;
-    DXMCG_CUDA(c.alloc(4 * static_cast<size_t>(n)));
-    DXMCG_CUDA(o.alloc(4 * static_cast<size_t>(n)));
-    DXMCG_CUDA(cudaMemcpy(c.p, counters, 16 * static_cast<size_t>(n), cudaMemcpyHostToDevice));
-    cudaError_t e = launchPhilox(n, c.p, key[0], key[1], o.p, nullptr);
-    if (e != cudaSuccess)
-        return cudaFail(e, "philox kernel");
-    DXMCG_CUDA(cudaMemcpy(out, o.p, 16 * static_cast<size_t>(n), cudaMemcpyDeviceToHost));
-    return DXMCG_OK;
-}
-
 DXMCG_API int dxmcg_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, int n_draws,
     uint32_t* out)
 {
@@ -1767,8 +1750,7 @@ DXMCG_API int dxmcg_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, 
         return DXMCG_OK;
     DeviceBuffer<uint32_t> o;
     DXMCG_CUDA(o.alloc(n));
-    cudaError_t e = launchHistoryStream(static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32), stream, h0,
-        n_hist, n_draws, o.p, nullptr);
+    cudaError_t e = launchHistoryStream(streamKey(seed, stream), h0, n_hist, n_draws, o.p, nullptr);
     if (e != cudaSuccess)
         return cudaFail(e, "stream kernel");
     DXMCG_CUDA(cudaMemcpy(out, o.p, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));

@@ -17,27 +17,6 @@ namespace dev {
     constexpr float kMeKeV = 510.99895f;
     constexpr float kInvHc = 1.0f / 12.398419843f;
 
-    // ---------------------------------------------------------------- Philox
-    __device__ __forceinline__ void philox10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3, uint32_t k0,
-        uint32_t k1)
-    {
-#pragma unroll
-        for (int r = 0; r < 10; ++r) {
-            const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
-            const uint32_t lo0 = 0xD2511F53u * c0;
-            const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
-            const uint32_t lo1 = 0xCD9E8D57u * c2;
-            const uint32_t n0 = hi1 ^ c1 ^ k0;
-            const uint32_t n2 = hi0 ^ c3 ^ k1;
-            c0 = n0;
-            c1 = lo1;
-            c2 = n2;
-            c3 = lo0;
-            k0 += 0x9E3779B9u;
-            k1 += 0xBB67AE85u;
-        }
-    }
-
     // (2k + 1) / 2^24 from the top 23 bits k: exact in FP32 and FP64, never 0 or 1.
     // Formed as the float 1 + k / 2^23 (k in the mantissa) minus 1 - 2^-24; both are
     // in [1/2, 2] of each other, so the difference is exact (Sterbenz) and no
@@ -48,22 +27,24 @@ namespace dev {
     }
 
     // Stream of one history: a xoshiro128+ generator (Blackman & Vigna 2018) whose
-    // 128-bit state is the Philox4x32-10 block at counter (0, stream, h) under the
-    // seed.  One Philox evaluation per history, then seven 32-bit ALU operations per
-    // draw with no data-dependent branch, so lanes stay converged while drawing.  Every
-    // draw is used through its top 23 bits (uniforms, alias columns), where the '+'
-    // output (s0 + s3) is as good as the scrambled '**' one; only its lowest bits are
-    // weak, and they are never used.
+    // 128-bit state is two SplitMix64 outputs, at the counters key + (2h + 1) gamma and
+    // key + (2h + 2) gamma of the run's key (the seeding the generator's authors give),
+    // so every history's draws depend only on (seed, stream word, h).  Then seven 32-bit
+    // ALU operations per draw with no data-dependent branch, so lanes stay converged
+    // while drawing.  Every draw is used through its top 23 bits (uniforms, alias
+    // columns), where the '+' output (s0 + s3) is as good as the scrambled '**' one;
+    // only its lowest bits are weak, and they are never used.
     struct Rng {
         uint32_t s0, s1, s2, s3;
 
-        __device__ __forceinline__ void init(uint32_t key0, uint32_t key1, uint32_t stream, unsigned long long h)
+        __device__ __forceinline__ void init(unsigned long long key, unsigned long long h)
         {
-            s0 = 0u;
-            s1 = stream;
-            s2 = static_cast<uint32_t>(h);
-            s3 = static_cast<uint32_t>(h >> 32);
-            philox10(s0, s1, s2, s3, key0, key1);
+            const unsigned long long x = key + (2ull * h + 1ull) * kGolden64;
+            const unsigned long long a = splitMix64(x), b = splitMix64(x + kGolden64);
+            s0 = static_cast<uint32_t>(a);
+            s1 = static_cast<uint32_t>(a >> 32);
+            s2 = static_cast<uint32_t>(b);
+            s3 = static_cast<uint32_t>(b >> 32);
             if ((s0 | s1 | s2 | s3) == 0u)
                 s0 = 0x9E3779B9u;
         }

@@ -128,7 +128,7 @@ struct DevJob {
     const DevBowtie* bowtie; // nullptr: no bowtie on either tube
     int beam_type;
     float pencil_energy;
-    uint32_t key0, key1, stream;
+    unsigned long long key; // streamKey(seed, stream word) of the run
     int tracking;
     uint32_t maxSteps; // per-history step limit (kErrStepLimit beyond it)
     // Woodcock gather skip: per cell of kCellEdge^3 voxels an upper bound b_c of
@@ -177,6 +177,23 @@ struct LaunchShape {
     int woodcock_steps = 0; // Woodcock steps per lane and step phase (0: default)
 };
 
+// Per-history random streams.  splitMix64 is the output function of SplitMix64
+// (Steele, Lea & Flood 2014), a bijection of the 64-bit integers that passes BigCrush on
+// a counter.  streamKey mixes a run's (seed, stream word) into the key its histories'
+// streams start from: distinct seeds with one stream word, or one seed with distinct
+// stream words, give distinct keys.
+__host__ __device__ __forceinline__ unsigned long long splitMix64(unsigned long long z)
+{
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+constexpr unsigned long long kGolden64 = 0x9E3779B97F4A7C15ull;
+__host__ __device__ __forceinline__ unsigned long long streamKey(unsigned long long seed, uint32_t stream)
+{
+    return splitMix64(seed ^ splitMix64(static_cast<unsigned long long>(stream) + kGolden64));
+}
+
 // Kernel instances of the transport are chosen by "kernel tracking": the public
 // DXMCG_TRACK_* modes, and kTrackWoodcockBox, Woodcock tracking with two regions,
 // for jobs whose world has a two-region box (DevJob::boxOn).
@@ -207,7 +224,6 @@ cudaError_t launchFinalize(const Tally* tally, const uint32_t* vox, size_t n, do
     double n_histories, double* dose, double* var, unsigned long long* count, cudaStream_t s);
 cudaError_t launchSiddon(int n_rays, const float* o, const float* d, int nx, int ny, int nz, float sx, float sy,
     float sz, int cap, long long* idx, float* len, int* cnt, cudaStream_t s);
-cudaError_t launchPhilox(int n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out, cudaStream_t s);
 cudaError_t launchSampleCompton(int n, const float* E, const DevMaterial* m, const float* ctab, int correction,
     const float* u, int stride, float* e_out, float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSamplePhoto(int n, const float* E, const DevMaterial* m, const float* u, int stride, float* e_out,
@@ -219,8 +235,8 @@ cudaError_t launchUmmaProbe(const uint16_t* A, const uint16_t* B0, const uint16_
 cudaError_t launchSampleRayleigh(int n, const float* E, const DevMaterial* m, const float* rtab, const float* u,
     int stride, float* cos_out, int* used, cudaStream_t s);
 cudaError_t launchSampleSource(const DevJob& job, unsigned long long h0, int n, float* out8, cudaStream_t s);
-cudaError_t launchHistoryStream(uint32_t k0, uint32_t k1, uint32_t stream, unsigned long long h0, int n_hist,
-    int n_draws, uint32_t* out, cudaStream_t s);
+cudaError_t launchHistoryStream(unsigned long long key, unsigned long long h0, int n_hist, int n_draws,
+    uint32_t* out, cudaStream_t s);
 int transportRegistersPerThread(int tracking);
 int transportMaxBlocksPerSM(int block, int tracking);
 // the same kernel reading caller-owned float density / uint8 material arrays

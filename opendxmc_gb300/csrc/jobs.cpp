@@ -476,9 +476,7 @@ void fillJobFields(DevJob& J, const dxmcg_beam& b, const dxmcg_run_options& o, c
     J.ppe = b.particles_per_exposure;
     J.beam_type = b.type;
     J.pencil_energy = static_cast<float>(b.energy_kev);
-    J.key0 = static_cast<uint32_t>(o.seed);
-    J.key1 = static_cast<uint32_t>(o.seed >> 32);
-    J.stream = o.stream;
+    J.key = streamKey(o.seed, o.stream);
     J.tracking = o.tracking;
     J.maxSteps = o.max_steps > 0 ? std::min(o.max_steps, kMaxStepsPerHistory) : kMaxStepsPerHistory;
 }

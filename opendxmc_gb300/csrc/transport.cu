@@ -556,7 +556,7 @@ namespace {
                         h -= __ldg(offsets + lo);
                     }
                     const DevJob& Jr = MULTI ? jobs[jid] : J0;
-                    rng.init(Jr.key0, Jr.key1, Jr.stream, h);
+                    rng.init(Jr.key, h);
                     sampleSource(Jr, h, ph, rng);
                     ls.template add<kSumSource>(ph.w * ph.E);
                     entered = enterGrid(Jr, ph);

@@ -55,7 +55,7 @@ class Pair:
 
 def dose_pair(world: "G.GpuWorld", beam: dict, low: int, high: int, seed: int, stream_base: int = 0):
     """(low-history dose, high-history dose) of one beam on one world, mGy per voxel
-    (host arrays); the two runs use independent Philox streams."""
+    (host arrays); the two runs use independent random streams."""
     def run(n, stream):
         b = dict(beam)
         world.clear()

@@ -501,14 +501,6 @@ def siddon_trace(origins, directions, dims, spacing, cap=4096):
     return [(idx[r, :cnt[r]].copy(), ln[r, :cnt[r]].copy()) for r in range(n)]
 
 
-def philox(counters, key):
-    c = np.ascontiguousarray(counters, dtype=np.uint32).reshape(-1, 4)
-    k = np.ascontiguousarray(key, dtype=np.uint32)
-    out = np.zeros_like(c)
-    N.check(N.lib().dxmcg_philox(c.shape[0], N.ptr(c, C.c_uint32), N.ptr(k, C.c_uint32), N.ptr(out, C.c_uint32)))
-    return out
-
-
 def history_stream(seed: int, stream: int, h0: int, n_hist: int, n_draws: int) -> np.ndarray:
     out = np.zeros((n_hist, n_draws), dtype=np.uint32)
     N.check(N.lib().dxmcg_history_stream(seed, stream, h0, n_hist, n_draws, N.ptr(out, C.c_uint32)))

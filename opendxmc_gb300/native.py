@@ -43,7 +43,7 @@ EXPORTED = [
     "dxmcg_progress_destroy",
     "dxmcg_progress_get", "dxmcg_progress_stop", "dxmcg_progress_reset", "dxmcg_progress_continue",
     "dxmcg_progress_message",
-    "dxmcg_siddon_trace", "dxmcg_philox", "dxmcg_history_stream", "dxmcg_sample_compton", "dxmcg_sample_rayleigh",
+    "dxmcg_siddon_trace", "dxmcg_history_stream", "dxmcg_sample_compton", "dxmcg_sample_rayleigh",
     "dxmcg_sample_photoelectric", "dxmcg_umma_probe",
     "dxmcg_sample_source",
 ]
@@ -249,7 +249,6 @@ def lib() -> C.CDLL:
         "dxmcg_progress_continue": (i, [vp]),
         "dxmcg_progress_message": (i, [vp, cp, i]),
         "dxmcg_siddon_trace": (i, [i, pf, pf, pi32, pf, i, pi64, pf, pi32]),
-        "dxmcg_philox": (i, [i, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
         "dxmcg_history_stream": (i, [u64, C.c_uint32, u64, i, i, C.POINTER(C.c_uint32)]),
         "dxmcg_sample_compton": (i, [i, pd, C.POINTER(Material), i, pd, i, pd, pd, pi32]),
         "dxmcg_sample_rayleigh": (i, [i, pd, C.POINTER(Material), pd, i, pd, pi32]),

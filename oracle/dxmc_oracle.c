@@ -656,30 +656,21 @@ double or_calibration_factor(const or_beam* b, uint64_t n_hist)
 }
 
 /* ------------------------------------------------------------------------- */
-/* Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw, SC'11).  */
+/* Per-history streams                                                         */
 /* ------------------------------------------------------------------------- */
-void or_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+/* The output function of SplitMix64 (Steele, Lea & Flood, OOPSLA 2014). */
+static inline uint64_t splitmix64(uint64_t z)
 {
-    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
-    uint32_t k0 = key[0], k1 = key[1];
-    for (int r = 0; r < 10; ++r) {
-        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
-        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
-        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
-        const uint32_t n1 = (uint32_t)p1;
-        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
-        const uint32_t n3 = (uint32_t)p0;
-        c0 = n0;
-        c1 = n1;
-        c2 = n2;
-        c3 = n3;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-    out[0] = c0;
-    out[1] = c1;
-    out[2] = c2;
-    out[3] = c3;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+#define GOLDEN64 0x9E3779B97F4A7C15ull
+
+/* the key of a run's streams, a mix of (seed, stream word) */
+static inline uint64_t stream_key(uint64_t seed, uint32_t stream)
+{
+    return splitmix64(seed ^ splitmix64((uint64_t)stream + GOLDEN64));
 }
 
 /* (2 k + 1) / 2^24 with k the top 23 bits: exactly representable in FP32, in (0, 1). */
@@ -688,8 +679,9 @@ double or_uniform_from_u32(uint32_t x) { return (double)((x >> 9) * 2u + 1u) * (
 /* Draw source: either the stream of one history, or injected uniforms.
  * History h's stream: the 128-bit state of a xoshiro128+ generator (Blackman & Vigna,
  * "Scrambled linear pseudorandom number generators", 2018; output s0 + s3, of which
- * only the top 23 bits are ever used) is the Philox4x32-10 block at counter
- * (0, stream, h_lo, h_hi) under key = seed, so every history's draws depend only on
+ * only the top 23 bits are ever used) is two SplitMix64 outputs at the counters
+ * key + (2h + 1) gamma and key + (2h + 2) gamma, key = stream_key(seed, stream) (the
+ * seeding the generator's authors give), so every history's draws depend only on
  * (seed, stream, h). */
 typedef struct {
     uint32_t s[4];
@@ -699,9 +691,12 @@ typedef struct {
 
 static void rng_stream(rng_t* r, uint64_t seed, uint32_t stream, uint64_t hist)
 {
-    const uint32_t key[2] = { (uint32_t)seed, (uint32_t)(seed >> 32) };
-    const uint32_t ctr[4] = { 0u, stream, (uint32_t)hist, (uint32_t)(hist >> 32) };
-    or_philox4x32(ctr, key, r->s);
+    const uint64_t x = stream_key(seed, stream) + (2ull * hist + 1ull) * GOLDEN64;
+    const uint64_t a = splitmix64(x), b = splitmix64(x + GOLDEN64);
+    r->s[0] = (uint32_t)a;
+    r->s[1] = (uint32_t)(a >> 32);
+    r->s[2] = (uint32_t)b;
+    r->s[3] = (uint32_t)(b >> 32);
     if ((r->s[0] | r->s[1] | r->s[2] | r->s[3]) == 0u)
         r->s[0] = 0x9E3779B9u; /* the all-zero state is the generator's fixed point */
     r->inj = NULL;

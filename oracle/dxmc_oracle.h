@@ -158,9 +158,8 @@ int or_tube_spectrum(double kvp, double anode_angle_deg, int n_filters, const in
 double or_tube_mean_energy(double kvp, int n_filters, const int32_t* fZ, const double* fmm);
 double or_tube_al_hvl_mm(double kvp, int n_filters, const int32_t* fZ, const double* fmm);
 /* rng */
-void or_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 double or_uniform_from_u32(uint32_t x);
-/* raw draws of the per-history streams (xoshiro128+ seeded by one Philox block) */
+/* raw draws of the per-history streams (xoshiro128+ seeded by SplitMix64) */
 void or_history_stream(uint64_t seed, uint32_t stream, uint64_t h0, int n_hist, int n_draws, uint32_t* out);
 /* beam geometry */
 int or_beam_exposures(const or_beam* b, or_exposure* out, int cap);

@@ -177,7 +177,6 @@ def lib() -> C.CDLL:
     L.or_tube_mean_energy.argtypes = [d, i, C.POINTER(C.c_int32), pd]
     L.or_tube_al_hvl_mm.restype = d
     L.or_tube_al_hvl_mm.argtypes = [d, i, C.POINTER(C.c_int32), pd]
-    L.or_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
     L.or_uniform_from_u32.restype = d
     L.or_uniform_from_u32.argtypes = [u32]
     L.or_beam_exposures.restype = i
@@ -278,14 +277,6 @@ def tube_mean_energy(kvp, filters):
 def tube_al_hvl_mm(kvp, filters):
     n, fz, fm = _filters(filters)
     return lib().or_tube_al_hvl_mm(kvp, n, fz, fm)
-
-
-def philox(ctr, key):
-    c = (C.c_uint32 * 4)(*ctr)
-    k = (C.c_uint32 * 2)(*key)
-    o = (C.c_uint32 * 4)()
-    lib().or_philox4x32(c, k, o)
-    return list(o)
 
 
 def history_stream(seed: int, stream: int, h0: int, n_hist: int, n_draws: int) -> np.ndarray:

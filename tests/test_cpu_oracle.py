@@ -111,11 +111,11 @@ def test_rayleigh_sampler_matches_form_factor(oracle):
     assert _chi2_p(hist, expected) > 1e-4
 
 
-def test_philox_uniforms(oracle):
+def test_stream_uniforms(oracle):
     from scipy import stats
 
-    u = np.array([oracle.lib().or_uniform_from_u32(x) for x in
-                  np.array([oracle.philox([i, 0, 5, 0], [1, 0]) for i in range(5000)], dtype=np.uint32).ravel()])
+    raw = oracle.history_stream(1, 5, 0, 2500, 2).ravel()
+    u = np.array([oracle.lib().or_uniform_from_u32(int(x)) for x in raw])
     assert u.min() > 0 and u.max() < 1
     assert stats.kstest(u, "uniform").pvalue > 1e-3
     assert oracle.lib().or_uniform_from_u32(0) == 2.0 ** -24
@@ -140,12 +140,24 @@ def _xoshiro128p(state, n):
     return out
 
 
-def test_history_streams_are_philox_seeded_xoshiro(oracle):
+def _splitmix64(z):
+    """Plain-Python SplitMix64 output function (Steele, Lea & Flood 2014)."""
+    M = (1 << 64) - 1
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+    return z ^ (z >> 31)
+
+
+def test_history_streams_are_splitmix_seeded_xoshiro(oracle):
+    M, G = (1 << 64) - 1, 0x9E3779B97F4A7C15
     seed, stream = 0x1234567890ABCDEF, 3
+    key = _splitmix64(seed ^ _splitmix64((stream + G) & M))
     got = oracle.history_stream(seed, stream, 2 ** 33 - 2, 4, 12)
     for i in range(4):
         h = 2 ** 33 - 2 + i
-        state = oracle.philox([0, stream, h & 0xFFFFFFFF, h >> 32], [seed & 0xFFFFFFFF, seed >> 32])
+        x = (key + (2 * h + 1) * G) & M
+        a, b = _splitmix64(x), _splitmix64((x + G) & M)
+        state = [a & 0xFFFFFFFF, a >> 32, b & 0xFFFFFFFF, b >> 32]
         assert list(got[i]) == _xoshiro128p(state, 12)
     # streams of neighbouring histories and stream words differ
     a = oracle.history_stream(1, 0, 0, 2, 8)

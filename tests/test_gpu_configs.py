@@ -93,8 +93,10 @@ def test_c3_batch_jobs_against_oracle(gpu, oracle):
         e2, q2, _ = ow.tally()
         frac, nvox, rel = error_line(f"C3 job {j} {specs[j]['dims']}", n, e1, q1, e2, q2)
         assert nvox > 1000 and frac >= 0.99, (j, frac)
+        # these jobs run their configured 5e6-1.4e7 histories: a 4-sigma tolerance of about
+        # 2.6e-3, whose estimate from 32 replicates scatters by 12 %, so allow up to 4e-3
         tol = parity.total_tolerance(w, specs[j]["beam"], lambda r: gpu.run_options(seed=100 + r, stream=j))
-        parity.assert_totals_agree(e1, e2, tol, f"C3 job {j}")
+        parity.assert_totals_agree(e1, e2, tol, f"C3 job {j}", resolve=4e-3)
     batch.close()
 
 

@@ -1,5 +1,5 @@
 """GPU tests of the hot-path pieces run alone through the C ABI, against the
-oracle on identical inputs: Philox streams, Siddon traversal (bit-exact),
+oracle on identical inputs: per-history streams, Siddon traversal (bit-exact),
 interaction samplers fed identical uniforms, source sampling."""
 import numpy as np
 import pytest
@@ -8,15 +8,6 @@ from opendxmc_gb300 import phantoms as P
 import parity
 
 pytestmark = pytest.mark.gpu
-
-
-def test_philox_bit_exact(gpu, oracle):
-    rng = np.random.default_rng(1)
-    ctr = rng.integers(0, 2 ** 32, size=(4096, 4), dtype=np.uint64).astype(np.uint32)
-    for key in ([0, 0], [1, 0], [0xDEADBEEF, 0x12345678], [0xFFFFFFFF, 0xFFFFFFFF]):
-        out = gpu.philox(ctr, key)
-        ref = np.array([oracle.philox(c, key) for c in ctr[:512]], dtype=np.uint32)
-        np.testing.assert_array_equal(out[:512], ref)
 
 
 def test_history_streams_bit_exact(gpu, oracle):

@@ -40,14 +40,14 @@ METRIC = "s to \u22642% voxel dose error: MC+denoiser vs plain MC on 1 GB300; hi
 WORKLOAD = ("spiral CT on seeded synthetic torso 256x256x200 @1.5 mm (6 materials, +-2% density jitter), "
             "120 kVp 6 mm Al + body bowtie, pitch 1.0, 40 mm collimation, 200 mm scan, 1e9 histories")
 # dram__bytes_read.sum + dram__bytes_write.sum per history, from 1-pass ncu captures of
-# one 67,000,320-history transport launch of this workload (two regions on: 1.389 GB
-# read + 0.793 GB written) and one 67,000,050-history launch of the 512x512x400
-# workload (gather skip and two regions on: 10.89 GB + 2.79 GB).  The library's
+# one 67,000,320-history transport launch of this workload (two regions on: 1.436 GB
+# read + 0.799 GB written) and one 67,000,050-history launch of the 512x512x400
+# workload (gather skip and two regions on: 10.96 GB + 2.80 GB).  The library's
 # launches hold up to 2^28 histories; a launch's traffic is taken as these per-history
 # figures times its histories (the tallies and voxels a launch touches grow with its
 # histories).
-TRAFFIC_BYTES_PER_HISTORY = 2.182e9 / 67_000_320
-TRAFFIC_BYTES_PER_HISTORY_512 = 13.686e9 / 67_000_050
+TRAFFIC_BYTES_PER_HISTORY = 2.235e9 / 67_000_320
+TRAFFIC_BYTES_PER_HISTORY_512 = 13.760e9 / 67_000_050
 LAUNCH_HISTORIES = 1 << 28
 
 

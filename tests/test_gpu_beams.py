@@ -5,7 +5,7 @@ dual-energy tubes' independent bowtie filters (setBowtieFilterA/B,
 beamsettingsmodel.cpp:1581-1612) and the pencil beam's air-kerma calibration
 (setAirKerma, beamsettingsmodel.cpp:675).
 
-Source sampling is compared photon by photon on shared Philox streams; transport
+Source sampling is compared photon by photon on shared history streams; transport
 with independent streams: per-voxel energy within 3 combined standard errors in
 >= 99 % of voxels above 5 % of the maximum, total energy within 4 standard errors of
 the difference (the spread of 32 replicate GPU runs), at history counts where that is

@@ -1,7 +1,7 @@
 """GPU transport parity against the CPU oracle, through the C ABI.
 
 Two kinds of comparison:
-  * independent streams (different Philox stream words): per-voxel energy
+  * independent streams (different stream numbers): per-voxel energy
     imparted within 3 combined standard errors in >= 99 % of voxels above 5 % of
     the maximum; total energy within 4 standard errors of the difference (the
     spread of 32 replicate GPU runs of the beam), at history counts where that is

@@ -748,6 +748,24 @@ namespace {
         }
     }
 
+    // out[b] = 1 where a brick within g bricks of b along one axis (0: x, 1: y, 2: z)
+    // is marked in `in` (three passes, one per axis, grow a set by a box of bricks)
+    __global__ void brickDilateAxisKernel(const uint8_t* __restrict__ in, int cx, int cy, int cz, int axis, int g,
+        uint8_t* __restrict__ out)
+    {
+        const int nb = cx * cy * cz;
+        const int n = axis == 0 ? cx : (axis == 1 ? cy : cz);
+        const int stride = axis == 0 ? 1 : (axis == 1 ? cx : cx * cy);
+        for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+            const int i = axis == 0 ? b % cx : (axis == 1 ? (b / cx) % cy : b / (cx * cy));
+            const int lo = max(0, i - g), hi = min(n - 1, i + g);
+            uint8_t v = 0;
+            for (int j = lo; j <= hi && !v; ++j)
+                v = in[b + (j - i) * stride];
+            out[b] = v ? 1 : 0;
+        }
+    }
+
     // coarse[b] = 1 where coarse brick b (cb voxels of the half-resolution level, cc
     // bricks per axis) covers a level-above voxel of an active fine brick (fb voxels,
     // fc bricks per axis): fine voxel v lies in coarse voxel v / 2
@@ -848,6 +866,19 @@ namespace nn {
         const int nb = count[0] * count[1] * count[2];
         brickGrowKernel<<<std::max(1, std::min((nb + 255) / 256, 4096)), 256, 0, s>>>(active, count[0], count[1],
             count[2], grown);
+        return cudaGetLastError();
+    }
+
+    cudaError_t launchBrickDilate(const uint8_t* active, const int count[3], const int radius[3], uint8_t* out,
+        uint8_t* tmp, cudaStream_t s)
+    {
+        const int nb = count[0] * count[1] * count[2];
+        if (nb <= 0 || active == out || active == tmp || out == tmp)
+            return cudaErrorInvalidValue;
+        const int grid = std::max(1, std::min((nb + 255) / 256, 4096));
+        brickDilateAxisKernel<<<grid, 256, 0, s>>>(active, count[0], count[1], count[2], 0, radius[0], out);
+        brickDilateAxisKernel<<<grid, 256, 0, s>>>(out, count[0], count[1], count[2], 1, radius[1], tmp);
+        brickDilateAxisKernel<<<grid, 256, 0, s>>>(tmp, count[0], count[1], count[2], 2, radius[2], out);
         return cudaGetLastError();
     }
 

@@ -53,10 +53,11 @@ struct dxmcg_denoiser {
     // between calls (the input of a 512x512x400 world is 3.4 GB)
     DevBuf<bf16> worldInput;
     DevBuf<double> worldOut, meanSum;
-    // world path: brick masks and lists of the restricted decoder layers (level 0:
-    // tissue, grown by one, grown by two; level 1: covered by the last, grown by one)
-    DevBuf<uint8_t> mask0[3], mask1[2];
-    DevBuf<int> list0[2], list1[2], listLens;
+    // world path: brick masks and lists of the restricted layers (level 0: tissue,
+    // grown by one, grown by two; level 1: covered by the last, grown by one; the
+    // level-0 encoder: tissue grown by the network's reach, and a scratch mask)
+    DevBuf<uint8_t> mask0[3], mask1[2], maskEnc[2];
+    DevBuf<int> list0[2], list1[2], listEnc, listLens;
     DevBuf<unsigned long long> meanCount;
 
     int encA(int l) const { return 2 * l; }
@@ -189,6 +190,57 @@ nn::ConvIn encIn(dxmcg_denoiser* d, int l, const bf16* input)
 
 const bf16* finalActivation(dxmcg_denoiser* d) { return d->L > 1 ? d->db[0].p : d->eb[0].p; }
 
+// Span of level-0 voxels [lo, hi] along one axis.
+struct Span {
+    int lo, hi;
+};
+
+Span widen(Span s, int r) { return { s.lo - r, s.hi + r }; }
+
+int floorHalf(int a) { return a >= 0 ? a / 2 : -((1 - a) / 2); }
+
+// Fold into `acc` the level-0 encoder outputs (the second convolution of level 0) on
+// which the encoder output of level l on span s depends: two 3-tap convolutions per
+// level, and the 2x2x2 average pooling between levels (voxel q of level l reads voxels
+// 2q and 2q + 1 of level l - 1).
+void encoderNeeds(int l, Span s, Span& acc)
+{
+    if (l == 0) {
+        acc = { std::min(acc.lo, s.lo), std::max(acc.hi, s.hi) };
+        return;
+    }
+    const Span x = widen(s, 2);
+    encoderNeeds(l - 1, { 2 * x.lo, 2 * x.hi + 1 }, acc);
+}
+
+// The same for the decoder output of level l (l < L - 1) on span s: its two
+// convolutions read the skip input (the encoder output of level l) and the nearest
+// upsampling of level l + 1 (voxel v reads voxel floor(v / 2)).
+void decoderNeeds(int L, int l, Span s, Span& acc)
+{
+    const Span in = widen(s, 2);
+    encoderNeeds(l, in, acc);
+    const Span up = { floorHalf(in.lo), floorHalf(in.hi) };
+    if (l + 1 == L - 1)
+        encoderNeeds(L - 1, up, acc);
+    else
+        decoderNeeds(L, l + 1, up, acc);
+}
+
+// Reach of an L-level network (L >= 2) along one axis: the output at voxel p depends
+// on level-0 encoder outputs within this many voxels of p, whatever p's alignment to
+// the pooling grids (7 (2^(L-1) - 1): 7, 21, 49, 105 for L = 2..5).
+int encoderReach(int L)
+{
+    int r = 0;
+    for (int p = 0; p < (8 << L); ++p) {
+        Span acc { p, p };
+        decoderNeeds(L, 0, { p, p }, acc);
+        r = std::max(r, std::max(p - acc.lo, acc.hi - p));
+    }
+    return r;
+}
+
 // Forward pass.  The encoder's pooling is fused into the second convolution of each
 // level where that runs on tcgen05.  With `pred` or `predOut` (inference) the 1x1x1
 // head follows: fused into the last convolution (whose output is then not stored)
@@ -204,6 +256,8 @@ struct Sparse {
     const int* dec1bLen = nullptr;
     const int* dec1a = nullptr;
     const int* dec1aLen = nullptr;
+    const int* enc0 = nullptr; // both level-0 encoder convolutions (null: dense)
+    const int* enc0Len = nullptr;
 };
 
 int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = nullptr,
@@ -225,17 +279,27 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
         beforeEp.list = sparse->before;
         beforeEp.listLen = sparse->beforeLen;
     }
+    nn::ConvOptions enc0Ep;
+    const bool sparseEnc0 = sparse && sparse->enc0 && d->L >= 2;
+    if (sparseEnc0) {
+        enc0Ep.list = sparse->enc0;
+        enc0Ep.listLen = sparse->enc0Len;
+    }
     const bool headFusable = wantHead && d->ch[0] == 16;
     bool headDone = false;
     for (int l = 0; l < d->L; ++l) {
         const bool last = d->L == 1; // encB(0) is the final convolution of a one-level net
-        if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s, last && sparse ? &beforeEp : nullptr))
-            != DXMCG_OK)
+        const nn::ConvOptions* epA = last && sparse ? &beforeEp : (l == 0 && sparseEnc0 ? &enc0Ep : nullptr);
+        if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s, epA)) != DXMCG_OK)
             return rc;
         nn::ConvOptions ep;
-        if (l < d->L - 1)
+        if (l < d->L - 1) {
             ep.pooled = d->x[l + 1].p;
-        else if (last && headFusable)
+            if (l == 0 && sparseEnc0) {
+                ep.list = enc0Ep.list;
+                ep.listLen = enc0Ep.listLen;
+            }
+        } else if (last && headFusable)
             ep = headEp;
         bool fused = false;
         const bool withEp = ep.pooled || ep.head;
@@ -385,6 +449,11 @@ namespace nn {
         // upsampled level-1 output in a one-voxel halo of its bricks (their set grown by
         // one brick, coarsened to level 1), and that layer's input one level-1 voxel
         // further (grown by one level-1 brick).
+        // Both level-0 encoder convolutions run on the tissue bricks grown by the
+        // network's reach plus one voxel (the second one's halo) along each axis: every
+        // value a tissue brick's output depends on is computed as in the dense pass, and
+        // what the others hold (stale values from earlier calls) reaches only outputs of
+        // bricks outside that set, which the readout does not use.
         Sparse sp;
         const bool sparse = d->ch[0] == 16 && useTensorCores(d, nz, ny, nx, d->ch[0]);
         if (sparse) {
@@ -395,7 +464,7 @@ namespace nn {
                 NN_CUDA(m.reserve(nb));
             for (auto& l : d->list0)
                 NN_CUDA(l.reserve(nb));
-            NN_CUDA(d->listLens.reserve(4));
+            NN_CUDA(d->listLens.reserve(5));
             NN_CUDA(launchBrickActivity(vox, nx, ny, nz, brick, count, d->mask0[0].p, s));
             NN_CUDA(launchBrickGrow(d->mask0[0].p, count, d->mask0[1].p, s));
             NN_CUDA(launchBrickList(d->mask0[0].p, static_cast<int>(nb), d->list0[0].p, d->listLens.p, s));
@@ -405,6 +474,19 @@ namespace nn {
             sp.lastLen = d->listLens.p;
             sp.before = d->list0[1].p;
             sp.beforeLen = d->listLens.p + 1;
+            if (d->L >= 2) {
+                const int reach = encoderReach(d->L) + 1;
+                int radius[3];
+                for (int a = 0; a < 3; ++a)
+                    radius[a] = (reach + brick[a] - 1) / brick[a];
+                for (auto& m : d->maskEnc)
+                    NN_CUDA(m.reserve(nb));
+                NN_CUDA(d->listEnc.reserve(nb));
+                NN_CUDA(launchBrickDilate(d->mask0[0].p, count, radius, d->maskEnc[0].p, d->maskEnc[1].p, s));
+                NN_CUDA(launchBrickList(d->maskEnc[0].p, static_cast<int>(nb), d->listEnc.p, d->listLens.p + 4, s));
+                sp.enc0 = d->listEnc.p;
+                sp.enc0Len = d->listLens.p + 4;
+            }
             const int D1 = nz >> 1, H1 = ny >> 1, W1 = nx >> 1;
             if (d->L >= 3 && useTensorCores(d, D1, H1, W1, d->ch[1])) {
                 int brick1[3], count1[3];

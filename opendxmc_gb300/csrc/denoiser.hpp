@@ -68,12 +68,16 @@ void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3])
 //   activity: bricks (of the given size and counts) holding a voxel whose packed word
 //             has a material other than 0;
 //   grow:     those and their 26 neighbours;
+//   dilate:   those and every brick within radius[a] bricks along each axis a (x, y,
+//             z), by three one-axis passes (tmp: scratch of the same size);
 //   coarsen:  bricks of the half-resolution level whose voxels cover a voxel of a
 //             marked brick of the level above (voxel v lies in coarse voxel v / 2);
 //   list:     the marked indices in increasing order, and how many (*listLen).
 cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
     uint8_t* active, cudaStream_t s);
 cudaError_t launchBrickGrow(const uint8_t* active, const int count[3], uint8_t* grown, cudaStream_t s);
+cudaError_t launchBrickDilate(const uint8_t* active, const int count[3], const int radius[3], uint8_t* out,
+    uint8_t* tmp, cudaStream_t s);
 cudaError_t launchBrickCoarsen(const uint8_t* fine, const int fineBrick[3], const int fineCount[3],
     const int coarseBrick[3], const int coarseCount[3], uint8_t* coarse, cudaStream_t s);
 cudaError_t launchBrickList(const uint8_t* mask, int nb, int* list, int* listLen, cudaStream_t s);

@@ -252,10 +252,12 @@ def test_world_denoise_path(gpu, torch):
 
 def test_world_denoise_sparse_bricks_match_dense(gpu, torch):
     """The world path on tcgen05 computes the last convolution only on bricks holding a
-    non-air voxel, the one before only on those and their neighbours, and the level-1
-    decoder only where those read it (the body sits at one end of a long block of air,
-    so level-1 bricks are skipped too).  Every voxel of a tissue brick equals the dense
-    array path (prepare_input + forward); the voxels of the other bricks are 0."""
+    non-air voxel, the one before only on those and their neighbours, the level-1
+    decoder only where those read it, and both level-0 encoder convolutions only on the
+    tissue bricks grown by the network's reach (the body sits at one end of a long block
+    of air, so bricks of every restricted layer are skipped).  Every voxel of a tissue
+    brick equals the dense array path (prepare_input + forward); the voxels of the other
+    bricks are 0."""
     small = P.ellipsoid_phantom((32, 32, 24), (0.4, 0.4, 0.4), seed=8)
     nx, ny, nz = 192, 64, 48
     oz, oy, ox = 12, 16, 8  # the body sits at one end of a larger block of air
@@ -284,6 +286,17 @@ def test_world_denoise_sparse_bricks_match_dense(gpu, torch):
     tissue = (mat_w.reshape(shape) != 0).reshape(nz // 8, 8, ny // 16, 16, nx // 8, 8).any(axis=(1, 3, 5))
     in_tissue = np.repeat(np.repeat(np.repeat(tissue, 8, 0), 16, 1), 8, 2)
     assert 0.02 < tissue.mean() < 0.5  # the test skips most bricks
+    # the level-0 encoder's set: a three-level net reaches 21 voxels, its first
+    # convolution one more (3, 2, 3 bricks of 8, 16, 8 along x, y, z)
+    enc = np.zeros_like(tissue)
+    for dz in range(-3, 4):
+        for dy in range(-2, 3):
+            for dx in range(-3, 4):
+                src = tissue[max(0, -dz):tissue.shape[0] - max(0, dz), max(0, -dy):tissue.shape[1] - max(0, dy),
+                             max(0, -dx):tissue.shape[2] - max(0, dx)]
+                enc[max(0, dz):tissue.shape[0] - max(0, -dz), max(0, dy):tissue.shape[1] - max(0, -dy),
+                    max(0, dx):tissue.shape[2] - max(0, -dx)] |= src
+    assert enc.mean() < 0.5  # the encoder skips bricks too
     assert np.isfinite(out).all()
     np.testing.assert_allclose(out[in_tissue], dense[in_tissue], rtol=1e-3, atol=1e-6 * np.abs(dense).max())
     assert (out[~in_tissue] == 0).all()
@@ -356,8 +369,10 @@ def test_tensor_core_probe_is_exact(gpu, n):
 
 def test_world_denoise_sparse_matches_dense_at_full_size(gpu, torch):
     """The 512 x 512 x 400 spiral-CT torso (102,400 level-0 bricks, so the ordered
-    brick lists are built over a hundred 1024-brick passes): the sparse world path
-    equals the dense array path on every voxel of a tissue brick."""
+    brick lists are built over a hundred 1024-brick passes; the four-level net's
+    level-0 encoder runs on the 72 % of the bricks within 7, 4, 7 bricks of tissue):
+    the sparse world path equals the dense array path on every voxel of a tissue
+    brick."""
     from opendxmc_gb300 import denoise as DN
 
     dims, spacing = (512, 512, 400), (0.08, 0.08, 0.1)

@@ -669,64 +669,63 @@ namespace {
         return cudaGetLastError();
     }
 
-    // active[b] = 1 where brick b holds a voxel whose packed word has a material other
-    // than 0 (one warp per brick; bricks x fastest, then y, z)
-    __global__ void brickActivityKernel(const uint32_t* __restrict__ vox, int nx, int ny, int nz, int bx, int by,
-        int bz, int cx, int cy, int cz, uint8_t* __restrict__ active)
-    {
-        const int lane = threadIdx.x & 31;
-        const int warps = static_cast<int>((gridDim.x * blockDim.x) >> 5);
-        const int nb = cx * cy * cz;
-        for (int b = static_cast<int>((blockIdx.x * blockDim.x + threadIdx.x) >> 5); b < nb; b += warps) {
-            const int ix = b % cx, iy = (b / cx) % cy, iz = b / (cx * cy);
-            bool any = false;
-            for (int e = lane; e < bx * by * bz && !any; e += 32) {
-                const int x = ix * bx + e % bx, y = iy * by + (e / bx) % by, z = iz * bz + e / (bx * by);
-                if (x < nx && y < ny && z < nz)
-                    any = (__ldg(vox + (static_cast<size_t>(z) * ny + y) * nx + x) & 0xffu) != 0u;
-            }
-            any = __any_sync(0xffffffffu, any);
-            if (lane == 0)
-                active[b] = any ? 1 : 0;
-        }
-    }
-
-    // list[0 .. *count) = the indices b with active[b] != 0, in increasing order (one CTA
-    // of 1024 threads: ballots within warps, a prefix over the warps, 1024 bricks a pass)
-    __global__ void __launch_bounds__(1024) brickListKernel(const uint8_t* __restrict__ active, int nb,
-        int* __restrict__ list, int* __restrict__ count)
+    // For each job j (one CTA of 1024 threads each): list_j[0 .. *len_j) = the indices b
+    // with mask_j[b] != 0, in increasing order.  A pass covers 4096 bricks, four
+    // consecutive ones per thread: counts scanned within warps, a prefix over the warps.
+    __global__ void __launch_bounds__(1024) brickListKernel(const nn::BrickListJobs jobs)
     {
         __shared__ int warpBase[32];
         __shared__ int passTotal;
+        const int j = static_cast<int>(blockIdx.x);
+        const uint8_t* __restrict__ active = jobs.mask[j];
+        int* __restrict__ list = jobs.list[j];
+        const int nb = jobs.nb[j];
+        const bool words = (reinterpret_cast<uintptr_t>(active) & 3u) == 0u;
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         int base = 0;
-        for (int i0 = 0; i0 < nb; i0 += 1024) {
-            const int i = i0 + static_cast<int>(threadIdx.x);
-            const bool a = i < nb && active[i] != 0;
-            const unsigned m = __ballot_sync(0xffffffffu, a);
-            if (lane == 0)
-                warpBase[w] = __popc(m);
+        for (int i0 = 0; i0 < nb; i0 += 4096) {
+            const int i = i0 + 4 * static_cast<int>(threadIdx.x);
+            unsigned f = 0; // bit k: brick i + k is marked
+            if (words && i + 3 < nb) {
+                const uchar4 v = *reinterpret_cast<const uchar4*>(active + i);
+                f = (v.x != 0 ? 1u : 0u) | (v.y != 0 ? 2u : 0u) | (v.z != 0 ? 4u : 0u) | (v.w != 0 ? 8u : 0u);
+            } else {
+                for (int k = 0; k < 4; ++k)
+                    if (i + k < nb && active[i + k] != 0)
+                        f |= 1u << k;
+            }
+            const int c = __popc(f);
+            int incl = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int n = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += n;
+            }
+            if (lane == 31)
+                warpBase[w] = incl;
             __syncthreads();
             if (w == 0) {
                 const int v = warpBase[lane];
-                int incl = v;
+                int sum = v;
                 for (int o = 1; o < 32; o <<= 1) {
-                    const int n = __shfl_up_sync(0xffffffffu, incl, o);
+                    const int n = __shfl_up_sync(0xffffffffu, sum, o);
                     if (lane >= o)
-                        incl += n;
+                        sum += n;
                 }
-                warpBase[lane] = incl - v;
+                warpBase[lane] = sum - v;
                 if (lane == 31)
-                    passTotal = incl;
+                    passTotal = sum;
             }
             __syncthreads();
-            if (a)
-                list[base + warpBase[w] + __popc(m & ((1u << lane) - 1u))] = i;
+            int pos = base + warpBase[w] + incl - c;
+            for (int k = 0; k < 4; ++k)
+                if (f >> k & 1u)
+                    list[pos++] = i + k;
             base += passTotal;
             __syncthreads(); // warpBase and passTotal are rewritten by the next pass
         }
         if (threadIdx.x == 0)
-            *count = base;
+            *jobs.len[j] = base;
     }
 
     // grown[b] = 1 where brick b or one of its 26 neighbours is active
@@ -850,17 +849,6 @@ namespace nn {
         count[2] = (D + zt - 1) / zt;
     }
 
-    cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3],
-        const int count[3], uint8_t* active, cudaStream_t s)
-    {
-        const int nb = count[0] * count[1] * count[2];
-        if (nb <= 0)
-            return cudaErrorInvalidValue;
-        brickActivityKernel<<<std::min((nb + 7) / 8, 4096), 256, 0, s>>>(vox, nx, ny, nz, brick[0], brick[1], brick[2],
-            count[0], count[1], count[2], active);
-        return cudaGetLastError();
-    }
-
     cudaError_t launchBrickGrow(const uint8_t* active, const int count[3], uint8_t* grown, cudaStream_t s)
     {
         const int nb = count[0] * count[1] * count[2];
@@ -892,10 +880,22 @@ namespace nn {
         return cudaGetLastError();
     }
 
+    cudaError_t launchBrickLists(const BrickListJobs& jobs, cudaStream_t s)
+    {
+        if (jobs.n < 1 || jobs.n > kMaxBrickLists)
+            return cudaErrorInvalidValue;
+        for (int j = 0; j < jobs.n; ++j)
+            if (!jobs.mask[j] || !jobs.list[j] || !jobs.len[j] || jobs.nb[j] < 0)
+                return cudaErrorInvalidValue;
+        brickListKernel<<<jobs.n, 1024, 0, s>>>(jobs);
+        return cudaGetLastError();
+    }
+
     cudaError_t launchBrickList(const uint8_t* mask, int nb, int* list, int* listLen, cudaStream_t s)
     {
-        brickListKernel<<<1, 1024, 0, s>>>(mask, nb, list, listLen);
-        return cudaGetLastError();
+        BrickListJobs jobs;
+        jobs.add(mask, nb, list, listLen);
+        return launchBrickLists(jobs, s);
     }
 
     // reads and clears the device flag of timed-out commits (0: none)

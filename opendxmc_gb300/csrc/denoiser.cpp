@@ -438,37 +438,53 @@ namespace nn {
             *scaleUsed = scale;
         NN_CUDA(d->worldInput.reserve(n * 16));
         NN_CUDA(d->worldOut.reserve(n));
-        NN_CUDA(launchPrepareInput(nullptr, nullptr, nullptr, tally, vox, toDose, n, static_cast<float>(1.0 / scale),
-            d->worldInput.p, s));
         // The readout deletes the dose of air (material 0).  Where the last two
         // convolutions run on tcgen05 with the head fused, the last one computes only
         // bricks holding a non-air voxel and the one before only those and their
         // neighbours (the last one's halo); the dose of the other voxels is 0.  Every
-        // non-air voxel gets the same value as the dense pass.
+        // voxel of those bricks gets the same value as the dense pass.
         // The level-1 decoder is restricted too: the one before the last reads the
         // upsampled level-1 output in a one-voxel halo of its bricks (their set grown by
         // one brick, coarsened to level 1), and that layer's input one level-1 voxel
-        // further (grown by one level-1 brick).
+        // further (grown by one level-1 brick).  One level further down the same sets
+        // hold 94 % and 100 % of the level-2 bricks of the 512x512x400 torso, so the
+        // level-2 decoder runs dense.
         // Both level-0 encoder convolutions run on the tissue bricks grown by the
         // network's reach plus one voxel (the second one's halo) along each axis: every
         // value a tissue brick's output depends on is computed as in the dense pass, and
         // what the others hold (stale values from earlier calls) reaches only outputs of
         // bricks outside that set, which the readout does not use.
+        // The input pass marks the tissue bricks; every brick list comes from one launch.
         Sparse sp;
         const bool sparse = d->ch[0] == 16 && useTensorCores(d, nz, ny, nx, d->ch[0]);
+        int brick[3] = { 1, 1, 1 }, count[3] = { 1, 1, 1 };
+        size_t nb = 0;
+        BrickMarks marks;
         if (sparse) {
-            int brick[3], count[3];
             conv3TcBrickDims(nz, ny, nx, d->ch[0], brick, count);
-            const size_t nb = static_cast<size_t>(count[0]) * count[1] * count[2];
+            nb = static_cast<size_t>(count[0]) * count[1] * count[2];
             for (auto& m : d->mask0)
                 NN_CUDA(m.reserve(nb));
+            NN_CUDA(cudaMemsetAsync(d->mask0[0].p, 0, nb, s));
+            marks.active = d->mask0[0].p;
+            marks.nx = nx;
+            marks.ny = ny;
+            marks.bx = brick[0];
+            marks.by = brick[1];
+            marks.bz = brick[2];
+            marks.cx = count[0];
+            marks.cy = count[1];
+        }
+        NN_CUDA(launchPrepareInput(nullptr, nullptr, nullptr, tally, vox, toDose, n, static_cast<float>(1.0 / scale),
+            d->worldInput.p, s, sparse ? &marks : nullptr));
+        if (sparse) {
             for (auto& l : d->list0)
                 NN_CUDA(l.reserve(nb));
             NN_CUDA(d->listLens.reserve(5));
-            NN_CUDA(launchBrickActivity(vox, nx, ny, nz, brick, count, d->mask0[0].p, s));
+            BrickListJobs lists;
             NN_CUDA(launchBrickGrow(d->mask0[0].p, count, d->mask0[1].p, s));
-            NN_CUDA(launchBrickList(d->mask0[0].p, static_cast<int>(nb), d->list0[0].p, d->listLens.p, s));
-            NN_CUDA(launchBrickList(d->mask0[1].p, static_cast<int>(nb), d->list0[1].p, d->listLens.p + 1, s));
+            lists.add(d->mask0[0].p, static_cast<int>(nb), d->list0[0].p, d->listLens.p);
+            lists.add(d->mask0[1].p, static_cast<int>(nb), d->list0[1].p, d->listLens.p + 1);
             NN_CUDA(cudaMemsetAsync(d->worldOut.p, 0, n * sizeof(double), s));
             sp.last = d->list0[0].p;
             sp.lastLen = d->listLens.p;
@@ -483,7 +499,7 @@ namespace nn {
                     NN_CUDA(m.reserve(nb));
                 NN_CUDA(d->listEnc.reserve(nb));
                 NN_CUDA(launchBrickDilate(d->mask0[0].p, count, radius, d->maskEnc[0].p, d->maskEnc[1].p, s));
-                NN_CUDA(launchBrickList(d->maskEnc[0].p, static_cast<int>(nb), d->listEnc.p, d->listLens.p + 4, s));
+                lists.add(d->maskEnc[0].p, static_cast<int>(nb), d->listEnc.p, d->listLens.p + 4);
                 sp.enc0 = d->listEnc.p;
                 sp.enc0Len = d->listLens.p + 4;
             }
@@ -499,13 +515,14 @@ namespace nn {
                 NN_CUDA(launchBrickGrow(d->mask0[1].p, count, d->mask0[2].p, s));
                 NN_CUDA(launchBrickCoarsen(d->mask0[2].p, brick, count, brick1, count1, d->mask1[0].p, s));
                 NN_CUDA(launchBrickGrow(d->mask1[0].p, count1, d->mask1[1].p, s));
-                NN_CUDA(launchBrickList(d->mask1[0].p, static_cast<int>(nb1), d->list1[0].p, d->listLens.p + 2, s));
-                NN_CUDA(launchBrickList(d->mask1[1].p, static_cast<int>(nb1), d->list1[1].p, d->listLens.p + 3, s));
+                lists.add(d->mask1[0].p, static_cast<int>(nb1), d->list1[0].p, d->listLens.p + 2);
+                lists.add(d->mask1[1].p, static_cast<int>(nb1), d->list1[1].p, d->listLens.p + 3);
                 sp.dec1b = d->list1[0].p;
                 sp.dec1bLen = d->listLens.p + 2;
                 sp.dec1a = d->list1[1].p;
                 sp.dec1aLen = d->listLens.p + 3;
             }
+            NN_CUDA(launchBrickLists(lists, s));
         }
         if ((rc = forward(d, d->worldInput.p, s, nullptr, d->worldOut.p, scale, sparse ? &sp : nullptr)) != DXMCG_OK)
             return rc;

@@ -64,23 +64,40 @@ int conv3TcCtas(int B, int D, int H, int W, int Cout);
 // the output bricks of the tcgen05 launch for this shape: (x, y, z) voxels per brick
 // and the brick counts along x, y, z (per batch item)
 void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3]);
-// Brick sets of the world path (one byte per brick, bricks x fastest, all on the device):
-//   activity: bricks (of the given size and counts) holding a voxel whose packed word
-//             has a material other than 0;
-//   grow:     those and their 26 neighbours;
+// Brick sets of the world path (one byte per brick, bricks x fastest, all on the device;
+// the tissue set comes from launchPrepareInput's brick marks):
+//   grow:     the marked bricks and their 26 neighbours;
 //   dilate:   those and every brick within radius[a] bricks along each axis a (x, y,
 //             z), by three one-axis passes (tmp: scratch of the same size);
 //   coarsen:  bricks of the half-resolution level whose voxels cover a voxel of a
 //             marked brick of the level above (voxel v lies in coarse voxel v / 2);
-//   list:     the marked indices in increasing order, and how many (*listLen).
-cudaError_t launchBrickActivity(const uint32_t* vox, int nx, int ny, int nz, const int brick[3], const int count[3],
-    uint8_t* active, cudaStream_t s);
+//   list:     the marked indices in increasing order, and how many (*listLen);
+//             launchBrickLists compacts up to kMaxBrickLists masks in one launch.
 cudaError_t launchBrickGrow(const uint8_t* active, const int count[3], uint8_t* grown, cudaStream_t s);
 cudaError_t launchBrickDilate(const uint8_t* active, const int count[3], const int radius[3], uint8_t* out,
     uint8_t* tmp, cudaStream_t s);
 cudaError_t launchBrickCoarsen(const uint8_t* fine, const int fineBrick[3], const int fineCount[3],
     const int coarseBrick[3], const int coarseCount[3], uint8_t* coarse, cudaStream_t s);
 cudaError_t launchBrickList(const uint8_t* mask, int nb, int* list, int* listLen, cudaStream_t s);
+constexpr int kMaxBrickLists = 8;
+struct BrickListJobs {
+    const uint8_t* mask[kMaxBrickLists] = {};
+    int* list[kMaxBrickLists] = {};
+    int* len[kMaxBrickLists] = {};
+    int nb[kMaxBrickLists] = {};
+    int n = 0;
+    void add(const uint8_t* m, int count, int* l, int* lenOut)
+    {
+        if (n < kMaxBrickLists) {
+            mask[n] = m;
+            nb[n] = count;
+            list[n] = l;
+            len[n] = lenOut;
+        }
+        ++n; // beyond kMaxBrickLists the launch refuses
+    }
+};
+cudaError_t launchBrickLists(const BrickListJobs& jobs, cudaStream_t s);
 // out = act(conv3(in) + bias), act = relu or identity; bias may be null
 cudaError_t launchConv3(const ConvIn& in, int B, int D, int H, int W, int Cin, const __nv_bfloat16* w,
     const float* bias, int Cout, bool relu, __nv_bfloat16* out, cudaStream_t s);
@@ -102,10 +119,20 @@ cudaError_t launchAdam(float* p, const float* g, float* m, float* v, __nv_bfloat
     float b2, float eps, float c1, float c2, cudaStream_t s);
 cudaError_t launchToBf16(const float* p, __nv_bfloat16* pb, size_t n, cudaStream_t s);
 cudaError_t launchTransposeWeights(const __nv_bfloat16* w, __nv_bfloat16* wt, int Cout, int Cin, cudaStream_t s);
+// Bricks to mark while the input is prepared from a world: active[b] = 1 for each
+// brick b holding a voxel whose material is not 0 (bricks of bx, by, bz voxels, cx and
+// cy of them along x and y, x fastest; the grid nx voxels along x, ny along y).  The
+// caller zeroes `active`.
+struct BrickMarks {
+    uint8_t* active = nullptr;
+    int nx = 1, ny = 1, bx = 1, by = 1, bz = 1, cx = 1, cy = 1;
+};
 // input channels [log1p(d / s), density, one-hot(material 0..5), 0 x 8] from arrays
-// (dose, dens, mat) or from a world (tally, vox, toDose)
+// (dose, dens, mat) or from a world (tally, vox, toDose); with a world, optionally
+// the brick marks above (fewer than 2^32 voxels)
 cudaError_t launchPrepareInput(const float* dose, const float* dens, const uint8_t* mat, const Tally* tally,
-    const uint32_t* vox, double toDose, size_t n, float invScale, __nv_bfloat16* out, cudaStream_t s);
+    const uint32_t* vox, double toDose, size_t n, float invScale, __nv_bfloat16* out, cudaStream_t s,
+    const BrickMarks* marks = nullptr);
 // patches outside their volume (or of a volume index out of range) are written as zeros
 cudaError_t launchGatherPatches(const __nv_bfloat16* const* inputs, const float* const* targets, const int* dims,
     int nVolumes, const int* origins, int nPatch, int P, __nv_bfloat16* xin, float* tgt, cudaStream_t s);

@@ -586,10 +586,11 @@ namespace {
 
     // Network input channels for one volume: [log(1 + d / s), density, one-hot of
     // material 0..5, zeros]; d, density and material come either from arrays or
-    // straight from a world (tally energy -> dose, packed voxel words).
+    // straight from a world (tally energy -> dose, packed voxel words), in which case
+    // the bricks holding a non-air voxel are marked too when marks.active is set.
     __global__ void prepareInputKernel(const float* __restrict__ dose, const float* __restrict__ dens,
         const uint8_t* __restrict__ mat, const Tally* __restrict__ tally, const uint32_t* __restrict__ vox,
-        double toDose, size_t n, float invScale, uint4* __restrict__ out)
+        double toDose, size_t n, float invScale, uint4* __restrict__ out, const BrickMarks marks)
     {
         for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
              i += static_cast<size_t>(gridDim.x) * blockDim.x) {
@@ -601,6 +602,14 @@ namespace {
                 m = static_cast<int>(w & 0xffu);
                 // air (material 0) enters with zero dose, as the worker's readout deletes it
                 d = rho > 0.0f && m != 0 ? static_cast<float>(tally[i].e * (toDose / rho)) : 0.0f;
+                if (marks.active && m != 0) {
+                    const uint32_t v = static_cast<uint32_t>(i);
+                    const uint32_t row = v / static_cast<uint32_t>(marks.nx);
+                    const int x = static_cast<int>(v - row * static_cast<uint32_t>(marks.nx));
+                    const int y = static_cast<int>(row % static_cast<uint32_t>(marks.ny));
+                    const int z = static_cast<int>(row / static_cast<uint32_t>(marks.ny));
+                    marks.active[x / marks.bx + marks.cx * (y / marks.by + marks.cy * (z / marks.bz))] = 1;
+                }
             } else {
                 d = dose[i];
                 rho = dens[i];
@@ -808,10 +817,18 @@ cudaError_t launchTransposeWeights(const __nv_bfloat16* w, __nv_bfloat16* wt, in
 }
 
 cudaError_t launchPrepareInput(const float* dose, const float* dens, const uint8_t* mat, const Tally* tally,
-    const uint32_t* vox, double toDose, size_t n, float invScale, __nv_bfloat16* out, cudaStream_t s)
+    const uint32_t* vox, double toDose, size_t n, float invScale, __nv_bfloat16* out, cudaStream_t s,
+    const BrickMarks* marks)
 {
+    const BrickMarks none {};
+    const BrickMarks& bm = marks ? *marks : none;
+    if (bm.active
+        && (!tally || n >= (1ull << 32) || bm.nx < 1 || bm.ny < 1 || bm.bx < 1 || bm.by < 1 || bm.bz < 1
+            || static_cast<size_t>(bm.nx) * bm.ny == 0 || n % (static_cast<size_t>(bm.nx) * bm.ny) != 0
+            || bm.cx < (bm.nx + bm.bx - 1) / bm.bx || bm.cy < (bm.ny + bm.by - 1) / bm.by))
+        return cudaErrorInvalidValue;
     prepareInputKernel<<<grid1d(n), 256, 0, s>>>(dose, dens, mat, tally, vox, toDose, n, invScale,
-        reinterpret_cast<uint4*>(out));
+        reinterpret_cast<uint4*>(out), bm);
     return cudaGetLastError();
 }
 

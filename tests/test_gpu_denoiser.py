@@ -369,7 +369,7 @@ def test_tensor_core_probe_is_exact(gpu, n):
 
 def test_world_denoise_sparse_matches_dense_at_full_size(gpu, torch):
     """The 512 x 512 x 400 spiral-CT torso (102,400 level-0 bricks, so the ordered
-    brick lists are built over a hundred 1024-brick passes; the four-level net's
+    brick lists are built over 25 passes of 4096 bricks; the four-level net's
     level-0 encoder runs on the 72 % of the bricks within 7, 4, 7 bricks of tissue):
     the sparse world path equals the dense array path on every voxel of a tissue
     brick."""

@@ -300,6 +300,11 @@ def test_world_denoise_sparse_bricks_match_dense(gpu, torch):
     assert np.isfinite(out).all()
     np.testing.assert_allclose(out[in_tissue], dense[in_tissue], rtol=1e-3, atol=1e-6 * np.abs(dense).max())
     assert (out[~in_tissue] == 0).all()
+    # a second call on the same tally reuses the world-path buffers and brick lists
+    # and gives the same map
+    again, scale2 = dn.denoise_world(w)
+    assert scale2 == pytest.approx(scale, rel=1e-12)
+    np.testing.assert_allclose(again.reshape(shape), out, rtol=1e-6, atol=1e-9 * np.abs(out).max())
 
 
 def test_trained_denoiser_beats_plain_monte_carlo(gpu, torch):

@@ -747,21 +747,24 @@ namespace {
         }
     }
 
-    // out[b] = 1 where a brick within g bricks of b along one axis (0: x, 1: y, 2: z)
-    // is marked in `in` (three passes, one per axis, grow a set by a box of bricks)
-    __global__ void brickDilateAxisKernel(const uint8_t* __restrict__ in, int cx, int cy, int cz, int axis, int g,
-        uint8_t* __restrict__ out)
+    // One pass of a separable union of brick boxes: `out` has in's counts (nx, ny, nz)
+    // with the count along `axis` (0: x, 1: y, 2: z) replaced by nOut, and out[.., b, ..]
+    // = 1 where in[.., c, ..] is marked for some c in [range[2b], range[2b + 1]].
+    __global__ void brickMapAxisKernel(const uint8_t* __restrict__ in, int nx, int ny, int nz, int axis, int nOut,
+        const int* __restrict__ range, uint8_t* __restrict__ out)
     {
-        const int nb = cx * cy * cz;
-        const int n = axis == 0 ? cx : (axis == 1 ? cy : cz);
-        const int stride = axis == 0 ? 1 : (axis == 1 ? cx : cx * cy);
-        for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
-            const int i = axis == 0 ? b % cx : (axis == 1 ? (b / cx) % cy : b / (cx * cy));
-            const int lo = max(0, i - g), hi = min(n - 1, i + g);
+        const int ox = axis == 0 ? nOut : nx, oy = axis == 1 ? nOut : ny, oz = axis == 2 ? nOut : nz;
+        const int total = ox * oy * oz;
+        for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < total; o += gridDim.x * blockDim.x) {
+            const int x = o % ox, y = (o / ox) % oy, z = o / (ox * oy);
+            const int b = axis == 0 ? x : (axis == 1 ? y : z);
+            const int c1 = range[2 * b + 1];
             uint8_t v = 0;
-            for (int j = lo; j <= hi && !v; ++j)
-                v = in[b + (j - i) * stride];
-            out[b] = v ? 1 : 0;
+            for (int c = range[2 * b]; c <= c1 && !v; ++c) {
+                const int ix = axis == 0 ? c : x, iy = axis == 1 ? c : y, iz = axis == 2 ? c : z;
+                v = in[(static_cast<size_t>(iz) * ny + iy) * nx + ix];
+            }
+            out[o] = v ? 1 : 0;
         }
     }
 
@@ -857,16 +860,25 @@ namespace nn {
         return cudaGetLastError();
     }
 
-    cudaError_t launchBrickDilate(const uint8_t* active, const int count[3], const int radius[3], uint8_t* out,
-        uint8_t* tmp, cudaStream_t s)
+    cudaError_t launchBrickMap(const uint8_t* in, const int inCount[3], const int outCount[3], const int* ranges,
+        uint8_t* out, uint8_t* tmp1, uint8_t* tmp2, cudaStream_t s)
     {
-        const int nb = count[0] * count[1] * count[2];
-        if (nb <= 0 || active == out || active == tmp || out == tmp)
+        for (int a = 0; a < 3; ++a)
+            if (inCount[a] < 1 || outCount[a] < 1)
+                return cudaErrorInvalidValue;
+        if (!in || !ranges || !out || !tmp1 || !tmp2 || in == out || in == tmp1 || in == tmp2 || out == tmp1
+            || out == tmp2 || tmp1 == tmp2)
             return cudaErrorInvalidValue;
-        const int grid = std::max(1, std::min((nb + 255) / 256, 4096));
-        brickDilateAxisKernel<<<grid, 256, 0, s>>>(active, count[0], count[1], count[2], 0, radius[0], out);
-        brickDilateAxisKernel<<<grid, 256, 0, s>>>(out, count[0], count[1], count[2], 1, radius[1], tmp);
-        brickDilateAxisKernel<<<grid, 256, 0, s>>>(tmp, count[0], count[1], count[2], 2, radius[2], out);
+        const auto grid = [](int items) { return std::max(1, std::min((items + 255) / 256, 4096)); };
+        const int* rx = ranges;
+        const int* ry = rx + 2 * outCount[0];
+        const int* rz = ry + 2 * outCount[1];
+        brickMapAxisKernel<<<grid(outCount[0] * inCount[1] * inCount[2]), 256, 0, s>>>(in, inCount[0], inCount[1],
+            inCount[2], 0, outCount[0], rx, tmp1);
+        brickMapAxisKernel<<<grid(outCount[0] * outCount[1] * inCount[2]), 256, 0, s>>>(tmp1, outCount[0],
+            inCount[1], inCount[2], 1, outCount[1], ry, tmp2);
+        brickMapAxisKernel<<<grid(outCount[0] * outCount[1] * outCount[2]), 256, 0, s>>>(tmp2, outCount[0],
+            outCount[1], inCount[2], 2, outCount[2], rz, out);
         return cudaGetLastError();
     }
 

@@ -55,9 +55,11 @@ struct dxmcg_denoiser {
     DevBuf<double> worldOut, meanSum;
     // world path: brick masks and lists of the restricted layers (level 0: tissue,
     // grown by one, grown by two; level 1: covered by the last, grown by one; the
-    // level-0 encoder: tissue grown by the network's reach, and a scratch mask)
-    DevBuf<uint8_t> mask0[3], mask1[2], maskEnc[2];
-    DevBuf<int> list0[2], list1[2], listEnc, listLens;
+    // encoders of levels 0-2: the bricks the tissue bricks need, with two scratch
+    // masks and the brick ranges that map one grid onto the other)
+    DevBuf<uint8_t> mask0[3], mask1[2], maskEnc[3], maskTmp[2];
+    DevBuf<int> list0[2], list1[2], listEnc[3], listLens, encRanges;
+    std::vector<int> encRangesHost;
     DevBuf<unsigned long long> meanCount;
 
     int encA(int l) const { return 2 * l; }
@@ -199,46 +201,66 @@ Span widen(Span s, int r) { return { s.lo - r, s.hi + r }; }
 
 int floorHalf(int a) { return a >= 0 ? a / 2 : -((1 - a) / 2); }
 
-// Fold into `acc` the level-0 encoder outputs (the second convolution of level 0) on
-// which the encoder output of level l on span s depends: two 3-tap convolutions per
-// level, and the 2x2x2 average pooling between levels (voxel q of level l reads voxels
-// 2q and 2q + 1 of level l - 1).
-void encoderNeeds(int l, Span s, Span& acc)
+// Fold into `acc` the encoder outputs of level lt (the second convolution of that
+// level, in level-lt voxels) on which the encoder output of level l on span s depends:
+// two 3-tap convolutions per level, and the 2x2x2 average pooling between levels
+// (voxel q of level l reads voxels 2q and 2q + 1 of level l - 1).  An encoder output
+// shallower than lt does not depend on level lt.
+void encoderNeeds(int l, int lt, Span s, Span& acc)
 {
-    if (l == 0) {
+    if (l == lt) {
         acc = { std::min(acc.lo, s.lo), std::max(acc.hi, s.hi) };
         return;
     }
+    if (l < lt)
+        return;
     const Span x = widen(s, 2);
-    encoderNeeds(l - 1, { 2 * x.lo, 2 * x.hi + 1 }, acc);
+    encoderNeeds(l - 1, lt, { 2 * x.lo, 2 * x.hi + 1 }, acc);
 }
 
 // The same for the decoder output of level l (l < L - 1) on span s: its two
 // convolutions read the skip input (the encoder output of level l) and the nearest
 // upsampling of level l + 1 (voxel v reads voxel floor(v / 2)).
-void decoderNeeds(int L, int l, Span s, Span& acc)
+void decoderNeeds(int L, int l, int lt, Span s, Span& acc)
 {
     const Span in = widen(s, 2);
-    encoderNeeds(l, in, acc);
+    encoderNeeds(l, lt, in, acc);
     const Span up = { floorHalf(in.lo), floorHalf(in.hi) };
     if (l + 1 == L - 1)
-        encoderNeeds(L - 1, up, acc);
+        encoderNeeds(L - 1, lt, up, acc);
     else
-        decoderNeeds(L, l + 1, up, acc);
+        decoderNeeds(L, l + 1, lt, up, acc);
 }
 
-// Reach of an L-level network (L >= 2) along one axis: the output at voxel p depends
-// on level-0 encoder outputs within this many voxels of p, whatever p's alignment to
-// the pooling grids (7 (2^(L-1) - 1): 7, 21, 49, 105 for L = 2..5).
-int encoderReach(int L)
+// Along one axis: the level-lt voxels of the encoder outputs that the network's
+// outputs on level-0 voxels [p0, p1] depend on, widened by one voxel for the first
+// convolution of level lt (the second reads it with a one-voxel halo).
+Span encoderSpan(int L, int lt, int p0, int p1)
 {
-    int r = 0;
-    for (int p = 0; p < (8 << L); ++p) {
-        Span acc { p, p };
-        decoderNeeds(L, 0, { p, p }, acc);
-        r = std::max(r, std::max(p - acc.lo, acc.hi - p));
+    Span acc { p0 >> lt, p0 >> lt };
+    for (int p = p0; p <= p1; ++p)
+        decoderNeeds(L, 0, lt, { p, p }, acc);
+    return widen(acc, 1);
+}
+
+// For each level-lt brick b along one axis (nl bricks of bl voxels over diml voxels):
+// the range [out[2b], out[2b + 1]] of level-0 bricks (n0 of b0 voxels over dim0) whose
+// outputs need it; an empty range where none does.
+void encoderBrickRanges(int L, int lt, int dim0, int b0, int n0, int diml, int bl, int nl, int* out)
+{
+    for (int b = 0; b < nl; ++b) {
+        out[2 * b] = n0;
+        out[2 * b + 1] = -1;
     }
-    return r;
+    for (int c = 0; c < n0; ++c) {
+        const int p0 = c * b0, p1 = std::min(p0 + b0, dim0) - 1;
+        const Span sp = encoderSpan(L, lt, p0, p1);
+        const int lo = std::max(0, sp.lo), hi = std::min(diml - 1, sp.hi);
+        for (int b = lo / bl; lo <= hi && b <= hi / bl && b < nl; ++b) {
+            out[2 * b] = std::min(out[2 * b], c);
+            out[2 * b + 1] = std::max(out[2 * b + 1], c);
+        }
+    }
 }
 
 // Forward pass.  The encoder's pooling is fused into the second convolution of each
@@ -256,8 +278,8 @@ struct Sparse {
     const int* dec1bLen = nullptr;
     const int* dec1a = nullptr;
     const int* dec1aLen = nullptr;
-    const int* enc0 = nullptr; // both level-0 encoder convolutions (null: dense)
-    const int* enc0Len = nullptr;
+    const int* enc[3] = {}; // both encoder convolutions of levels 0-2 (null: dense)
+    const int* encLen[3] = {};
 };
 
 int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = nullptr,
@@ -279,26 +301,24 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
         beforeEp.list = sparse->before;
         beforeEp.listLen = sparse->beforeLen;
     }
-    nn::ConvOptions enc0Ep;
-    const bool sparseEnc0 = sparse && sparse->enc0 && d->L >= 2;
-    if (sparseEnc0) {
-        enc0Ep.list = sparse->enc0;
-        enc0Ep.listLen = sparse->enc0Len;
-    }
     const bool headFusable = wantHead && d->ch[0] == 16;
     bool headDone = false;
     for (int l = 0; l < d->L; ++l) {
         const bool last = d->L == 1; // encB(0) is the final convolution of a one-level net
-        const nn::ConvOptions* epA = last && sparse ? &beforeEp : (l == 0 && sparseEnc0 ? &enc0Ep : nullptr);
+        nn::ConvOptions encEp;
+        const bool sparseEnc = sparse && l < 3 && l < d->L - 1 && sparse->enc[l];
+        if (sparseEnc) {
+            encEp.list = sparse->enc[l];
+            encEp.listLen = sparse->encLen[l];
+        }
+        const nn::ConvOptions* epA = last && sparse ? &beforeEp : (sparseEnc ? &encEp : nullptr);
         if ((rc = conv(d, d->encA(l), encIn(d, l, input), l, d->ea[l].p, s, epA)) != DXMCG_OK)
             return rc;
         nn::ConvOptions ep;
         if (l < d->L - 1) {
             ep.pooled = d->x[l + 1].p;
-            if (l == 0 && sparseEnc0) {
-                ep.list = enc0Ep.list;
-                ep.listLen = enc0Ep.listLen;
-            }
+            ep.list = encEp.list;
+            ep.listLen = encEp.listLen;
         } else if (last && headFusable)
             ep = headEp;
         bool fused = false;
@@ -449,11 +469,13 @@ namespace nn {
         // further (grown by one level-1 brick).  One level further down the same sets
         // hold 94 % and 100 % of the level-2 bricks of the 512x512x400 torso, so the
         // level-2 decoder runs dense.
-        // Both level-0 encoder convolutions run on the tissue bricks grown by the
-        // network's reach plus one voxel (the second one's halo) along each axis: every
-        // value a tissue brick's output depends on is computed as in the dense pass, and
-        // what the others hold (stale values from earlier calls) reaches only outputs of
-        // bricks outside that set, which the readout does not use.
+        // The encoders of levels 0-2 run on the bricks of their grids that a tissue
+        // brick's outputs need: along each axis, the span of encoder outputs that the
+        // outputs of a level-0 brick depend on (every path through the network, at that
+        // brick's alignment to the pooling grids), plus the first convolution's halo.
+        // Every value a tissue brick's output depends on is computed as in the dense
+        // pass; what the other bricks hold (stale values from earlier calls) reaches
+        // only outputs of bricks outside that set, which the readout does not use.
         // The input pass marks the tissue bricks; every brick list comes from one launch.
         Sparse sp;
         const bool sparse = d->ch[0] == 16 && useTensorCores(d, nz, ny, nx, d->ch[0]);
@@ -480,7 +502,7 @@ namespace nn {
         if (sparse) {
             for (auto& l : d->list0)
                 NN_CUDA(l.reserve(nb));
-            NN_CUDA(d->listLens.reserve(5));
+            NN_CUDA(d->listLens.reserve(7));
             BrickListJobs lists;
             NN_CUDA(launchBrickGrow(d->mask0[0].p, count, d->mask0[1].p, s));
             lists.add(d->mask0[0].p, static_cast<int>(nb), d->list0[0].p, d->listLens.p);
@@ -490,18 +512,46 @@ namespace nn {
             sp.lastLen = d->listLens.p;
             sp.before = d->list0[1].p;
             sp.beforeLen = d->listLens.p + 1;
-            if (d->L >= 2) {
-                const int reach = encoderReach(d->L) + 1;
-                int radius[3];
-                for (int a = 0; a < 3; ++a)
-                    radius[a] = (reach + brick[a] - 1) / brick[a];
-                for (auto& m : d->maskEnc)
-                    NN_CUDA(m.reserve(nb));
-                NN_CUDA(d->listEnc.reserve(nb));
-                NN_CUDA(launchBrickDilate(d->mask0[0].p, count, radius, d->maskEnc[0].p, d->maskEnc[1].p, s));
-                lists.add(d->maskEnc[0].p, static_cast<int>(nb), d->listEnc.p, d->listLens.p + 4);
-                sp.enc0 = d->listEnc.p;
-                sp.enc0Len = d->listLens.p + 4;
+            // the encoders of levels 0 .. min(2, L - 2) that run on tcgen05: the bricks
+            // of their grids that some tissue brick's outputs need
+            const int dim0[3] = { nx, ny, nz };
+            int bl[3][3], cl[3][3], levels = 0;
+            size_t nRanges = 0, tmp1 = 1, tmp2 = 1;
+            for (int lt = 0; lt < 3 && lt <= d->L - 2; ++lt) {
+                if (!useTensorCores(d, nz >> lt, ny >> lt, nx >> lt, d->ch[lt]))
+                    break;
+                conv3TcBrickDims(nz >> lt, ny >> lt, nx >> lt, d->ch[lt], bl[lt], cl[lt]);
+                nRanges += 2 * static_cast<size_t>(cl[lt][0] + cl[lt][1] + cl[lt][2]);
+                tmp1 = std::max(tmp1, static_cast<size_t>(cl[lt][0]) * count[1] * count[2]);
+                tmp2 = std::max(tmp2, static_cast<size_t>(cl[lt][0]) * cl[lt][1] * count[2]);
+                levels = lt + 1;
+            }
+            if (levels > 0) {
+                d->encRangesHost.assign(nRanges, 0);
+                size_t off = 0;
+                for (int lt = 0; lt < levels; ++lt)
+                    for (int a = 0; a < 3; ++a) {
+                        encoderBrickRanges(d->L, lt, dim0[a], brick[a], count[a], dim0[a] >> lt, bl[lt][a],
+                            cl[lt][a], d->encRangesHost.data() + off);
+                        off += 2 * static_cast<size_t>(cl[lt][a]);
+                    }
+                NN_CUDA(d->encRanges.reserve(nRanges));
+                NN_CUDA(cudaMemcpyAsync(d->encRanges.p, d->encRangesHost.data(), nRanges * sizeof(int),
+                    cudaMemcpyHostToDevice, s));
+                NN_CUDA(d->maskTmp[0].reserve(tmp1));
+                NN_CUDA(d->maskTmp[1].reserve(tmp2));
+                off = 0;
+                for (int lt = 0; lt < levels; ++lt) {
+                    const size_t nbl = static_cast<size_t>(cl[lt][0]) * cl[lt][1] * cl[lt][2];
+                    NN_CUDA(d->maskEnc[lt].reserve(nbl));
+                    NN_CUDA(d->listEnc[lt].reserve(nbl));
+                    NN_CUDA(launchBrickMap(d->mask0[0].p, count, cl[lt], d->encRanges.p + off, d->maskEnc[lt].p,
+                        d->maskTmp[0].p, d->maskTmp[1].p, s));
+                    off += 2 * static_cast<size_t>(cl[lt][0] + cl[lt][1] + cl[lt][2]);
+                    lists.add(d->maskEnc[lt].p, static_cast<int>(nbl), d->listEnc[lt].p, d->listLens.p + 4 + lt);
+                    sp.enc[lt] = d->listEnc[lt].p;
+                    sp.encLen[lt] = d->listLens.p + 4 + lt;
+                }
             }
             const int D1 = nz >> 1, H1 = ny >> 1, W1 = nx >> 1;
             if (d->L >= 3 && useTensorCores(d, D1, H1, W1, d->ch[1])) {

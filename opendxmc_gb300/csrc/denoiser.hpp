@@ -67,15 +67,20 @@ void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3])
 // Brick sets of the world path (one byte per brick, bricks x fastest, all on the device;
 // the tissue set comes from launchPrepareInput's brick marks):
 //   grow:     the marked bricks and their 26 neighbours;
-//   dilate:   those and every brick within radius[a] bricks along each axis a (x, y,
-//             z), by three one-axis passes (tmp: scratch of the same size);
+//   map:      bricks of another brick grid (outCount per axis) that a marked brick
+//             needs: the union over marked bricks (cx, cy, cz) of the boxes
+//             X(cx) x Y(cy) x Z(cz), where `ranges` (device) holds for each output brick
+//             index b along x, then y, then z, the range [lo, hi] of input brick indices
+//             whose interval holds b; three one-axis passes (tmp1: outCount[0] x
+//             inCount[1] x inCount[2] bytes, tmp2: outCount[0] x outCount[1] x
+//             inCount[2]);
 //   coarsen:  bricks of the half-resolution level whose voxels cover a voxel of a
 //             marked brick of the level above (voxel v lies in coarse voxel v / 2);
 //   list:     the marked indices in increasing order, and how many (*listLen);
 //             launchBrickLists compacts up to kMaxBrickLists masks in one launch.
 cudaError_t launchBrickGrow(const uint8_t* active, const int count[3], uint8_t* grown, cudaStream_t s);
-cudaError_t launchBrickDilate(const uint8_t* active, const int count[3], const int radius[3], uint8_t* out,
-    uint8_t* tmp, cudaStream_t s);
+cudaError_t launchBrickMap(const uint8_t* in, const int inCount[3], const int outCount[3], const int* ranges,
+    uint8_t* out, uint8_t* tmp1, uint8_t* tmp2, cudaStream_t s);
 cudaError_t launchBrickCoarsen(const uint8_t* fine, const int fineBrick[3], const int fineCount[3],
     const int coarseBrick[3], const int coarseCount[3], uint8_t* coarse, cudaStream_t s);
 cudaError_t launchBrickList(const uint8_t* mask, int nb, int* list, int* listLen, cudaStream_t s);

@@ -253,8 +253,8 @@ def test_world_denoise_path(gpu, torch):
 def test_world_denoise_sparse_bricks_match_dense(gpu, torch):
     """The world path on tcgen05 computes the last convolution only on bricks holding a
     non-air voxel, the one before only on those and their neighbours, the level-1
-    decoder only where those read it, and both level-0 encoder convolutions only on the
-    tissue bricks grown by the network's reach (the body sits at one end of a long block
+    decoder only where those read it, and the encoder convolutions only on the bricks
+    that a tissue brick's outputs depend on (the body sits at one end of a long block
     of air, so bricks of every restricted layer are skipped).  Every voxel of a tissue
     brick equals the dense array path (prepare_input + forward); the voxels of the other
     bricks are 0."""
@@ -286,8 +286,9 @@ def test_world_denoise_sparse_bricks_match_dense(gpu, torch):
     tissue = (mat_w.reshape(shape) != 0).reshape(nz // 8, 8, ny // 16, 16, nx // 8, 8).any(axis=(1, 3, 5))
     in_tissue = np.repeat(np.repeat(np.repeat(tissue, 8, 0), 16, 1), 8, 2)
     assert 0.02 < tissue.mean() < 0.5  # the test skips most bricks
-    # the level-0 encoder's set: a three-level net reaches 21 voxels, its first
-    # convolution one more (3, 2, 3 bricks of 8, 16, 8 along x, y, z)
+    # the level-0 encoder's set lies within the tissue bricks grown by 3, 2, 3 bricks of
+    # 8, 16, 8 voxels along x, y, z (a three-level net reaches 21 voxels at most, its
+    # first convolution one more)
     enc = np.zeros_like(tissue)
     for dz in range(-3, 4):
         for dy in range(-2, 3):
@@ -375,7 +376,7 @@ def test_tensor_core_probe_is_exact(gpu, n):
 def test_world_denoise_sparse_matches_dense_at_full_size(gpu, torch):
     """The 512 x 512 x 400 spiral-CT torso (102,400 level-0 bricks, so the ordered
     brick lists are built over 25 passes of 4096 bricks; the four-level net's
-    level-0 encoder runs on the 72 % of the bricks within 7, 4, 7 bricks of tissue):
+    encoders run on 63 %, 67 % and 72 % of the level-0, -1 and -2 bricks):
     the sparse world path equals the dense array path on every voxel of a tissue
     brick."""
     from opendxmc_gb300 import denoise as DN

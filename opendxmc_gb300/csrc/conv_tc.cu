@@ -768,27 +768,6 @@ namespace {
         }
     }
 
-    // coarse[b] = 1 where coarse brick b (cb voxels of the half-resolution level, cc
-    // bricks per axis) covers a level-above voxel of an active fine brick (fb voxels,
-    // fc bricks per axis): fine voxel v lies in coarse voxel v / 2
-    __global__ void brickCoarsenKernel(const uint8_t* __restrict__ fine, int fbx, int fby, int fbz, int fcx, int fcy,
-        int fcz, int cbx, int cby, int cbz, int ccx, int ccy, int ccz, uint8_t* __restrict__ coarse)
-    {
-        const int nb = ccx * ccy * ccz;
-        for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
-            const int ix = b % ccx, iy = (b / ccx) % ccy, iz = b / (ccx * ccy);
-            // the coarse brick's footprint in fine voxels, then in fine bricks
-            const int x0 = (2 * ix * cbx) / fbx, x1 = min((2 * (ix + 1) * cbx - 1) / fbx, fcx - 1);
-            const int y0 = (2 * iy * cby) / fby, y1 = min((2 * (iy + 1) * cby - 1) / fby, fcy - 1);
-            const int z0 = (2 * iz * cbz) / fbz, z1 = min((2 * (iz + 1) * cbz - 1) / fbz, fcz - 1);
-            uint8_t g = 0;
-            for (int z = z0; z <= z1; ++z)
-                for (int y = y0; y <= y1; ++y)
-                    for (int x = x0; x <= x1; ++x)
-                        g |= fine[(static_cast<size_t>(z) * fcy + y) * fcx + x];
-            coarse[b] = g;
-        }
-    }
 
 } // namespace
 
@@ -879,16 +858,6 @@ namespace nn {
             inCount[1], inCount[2], 1, outCount[1], ry, tmp2);
         brickMapAxisKernel<<<grid(outCount[0] * outCount[1] * outCount[2]), 256, 0, s>>>(tmp2, outCount[0],
             outCount[1], inCount[2], 2, outCount[2], rz, out);
-        return cudaGetLastError();
-    }
-
-    cudaError_t launchBrickCoarsen(const uint8_t* fine, const int fineBrick[3], const int fineCount[3],
-        const int coarseBrick[3], const int coarseCount[3], uint8_t* coarse, cudaStream_t s)
-    {
-        const int nb = coarseCount[0] * coarseCount[1] * coarseCount[2];
-        brickCoarsenKernel<<<std::max(1, std::min((nb + 255) / 256, 4096)), 256, 0, s>>>(fine, fineBrick[0],
-            fineBrick[1], fineBrick[2], fineCount[0], fineCount[1], fineCount[2], coarseBrick[0], coarseBrick[1],
-            coarseBrick[2], coarseCount[0], coarseCount[1], coarseCount[2], coarse);
         return cudaGetLastError();
     }
 

@@ -3,6 +3,7 @@
 // tensor operation is a kernel of denoiser_kernels.cu.  No counterpart in the
 // reference.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -53,12 +54,12 @@ struct dxmcg_denoiser {
     // between calls (the input of a 512x512x400 world is 3.4 GB)
     DevBuf<bf16> worldInput;
     DevBuf<double> worldOut, meanSum;
-    // world path: brick masks and lists of the restricted layers (level 0: tissue,
-    // grown by one, grown by two; level 1: covered by the last, grown by one; the
-    // encoders of levels 0-2: the bricks the tissue bricks need, with two scratch
-    // masks and the brick ranges that map one grid onto the other)
-    DevBuf<uint8_t> mask0[3], mask1[2], maskEnc[3], maskTmp[2];
-    DevBuf<int> list0[2], list1[2], listEnc[3], listLens, encRanges;
+    // world path: brick masks and lists of the restricted layers (level 0: tissue and
+    // tissue grown by one; the decoders of levels 1-2 and the encoders of levels 0-2:
+    // the bricks that the tissue bricks need), two scratch masks and the brick ranges
+    // that map the tissue bricks onto those grids
+    DevBuf<uint8_t> mask0[2], mask1[2], mask2[2], maskEnc[3], maskTmp[2];
+    DevBuf<int> list0[2], list1[2], list2[2], listEnc[3], listLens, encRanges;
     std::vector<int> encRangesHost;
     DevBuf<unsigned long long> meanCount;
 
@@ -201,52 +202,70 @@ Span widen(Span s, int r) { return { s.lo - r, s.hi + r }; }
 
 int floorHalf(int a) { return a >= 0 ? a / 2 : -((1 - a) / 2); }
 
-// Fold into `acc` the encoder outputs of level lt (the second convolution of that
-// level, in level-lt voxels) on which the encoder output of level l on span s depends:
-// two 3-tap convolutions per level, and the 2x2x2 average pooling between levels
-// (voxel q of level l reads voxels 2q and 2q + 1 of level l - 1).  An encoder output
-// shallower than lt does not depend on level lt.
-void encoderNeeds(int l, int lt, Span s, Span& acc)
+// What a span describes (level-l voxels of one tensor, along one axis): the output
+// of the encoder of level l widened by one voxel (its two convolutions: the second
+// reads the first with a one-voxel halo), or the output of the second or the first
+// convolution of the decoder of level l.
+enum SpanKind { kEncoderPair, kDecoderSecond, kDecoderFirst };
+struct SpanTarget {
+    SpanKind kind;
+    int level;
+};
+
+void fold(Span& acc, Span s) { acc = { std::min(acc.lo, s.lo), std::max(acc.hi, s.hi) }; }
+
+// Fold into `acc` the voxels of the target on which the encoder output (second
+// convolution) of level l on span s depends: two 3-tap convolutions per level, and the
+// 2x2x2 average pooling between levels (voxel q of level l reads voxels 2q and 2q + 1
+// of level l - 1).  An encoder output depends on no decoder output, and on no encoder
+// deeper than itself.
+void encoderNeeds(int l, SpanTarget t, Span s, Span& acc)
 {
-    if (l == lt) {
-        acc = { std::min(acc.lo, s.lo), std::max(acc.hi, s.hi) };
+    if (t.kind != kEncoderPair || l < t.level)
+        return;
+    if (l == t.level) {
+        fold(acc, s);
         return;
     }
-    if (l < lt)
-        return;
     const Span x = widen(s, 2);
-    encoderNeeds(l - 1, lt, { 2 * x.lo, 2 * x.hi + 1 }, acc);
+    encoderNeeds(l - 1, t, { 2 * x.lo, 2 * x.hi + 1 }, acc);
 }
 
-// The same for the decoder output of level l (l < L - 1) on span s: its two
-// convolutions read the skip input (the encoder output of level l) and the nearest
-// upsampling of level l + 1 (voxel v reads voxel floor(v / 2)).
-void decoderNeeds(int L, int l, int lt, Span s, Span& acc)
+// The same for the decoder output of level l (l < L - 1) on span s: its second
+// convolution reads the first with a one-voxel halo, and the first reads the skip
+// input (the encoder output of level l) and the nearest upsampling of level l + 1
+// (voxel v reads voxel floor(v / 2)) with another.
+void decoderNeeds(int L, int l, SpanTarget t, Span s, Span& acc)
 {
+    if (t.kind == kDecoderSecond && l == t.level)
+        fold(acc, s);
+    if (t.kind == kDecoderFirst && l == t.level)
+        fold(acc, widen(s, 1));
     const Span in = widen(s, 2);
-    encoderNeeds(l, lt, in, acc);
+    encoderNeeds(l, t, in, acc);
     const Span up = { floorHalf(in.lo), floorHalf(in.hi) };
     if (l + 1 == L - 1)
-        encoderNeeds(L - 1, lt, up, acc);
+        encoderNeeds(L - 1, t, up, acc);
     else
-        decoderNeeds(L, l + 1, lt, up, acc);
+        decoderNeeds(L, l + 1, t, up, acc);
 }
 
-// Along one axis: the level-lt voxels of the encoder outputs that the network's
-// outputs on level-0 voxels [p0, p1] depend on, widened by one voxel for the first
-// convolution of level lt (the second reads it with a one-voxel halo).
-Span encoderSpan(int L, int lt, int p0, int p1)
+// Along one axis: the voxels of the target that the network's outputs on level-0
+// voxels [p0, p1] depend on (empty: lo > hi).
+Span networkSpan(int L, SpanTarget t, int p0, int p1)
 {
-    Span acc { p0 >> lt, p0 >> lt };
+    Span acc { INT_MAX, INT_MIN };
     for (int p = p0; p <= p1; ++p)
-        decoderNeeds(L, 0, lt, { p, p }, acc);
-    return widen(acc, 1);
+        decoderNeeds(L, 0, t, { p, p }, acc);
+    if (acc.lo > acc.hi)
+        return acc;
+    return t.kind == kEncoderPair ? widen(acc, 1) : acc;
 }
 
-// For each level-lt brick b along one axis (nl bricks of bl voxels over diml voxels):
-// the range [out[2b], out[2b + 1]] of level-0 bricks (n0 of b0 voxels over dim0) whose
-// outputs need it; an empty range where none does.
-void encoderBrickRanges(int L, int lt, int dim0, int b0, int n0, int diml, int bl, int nl, int* out)
+// For each brick b of the target's grid along one axis (nl bricks of bl voxels over
+// diml voxels): the range [out[2b], out[2b + 1]] of level-0 bricks (n0 of b0 voxels
+// over dim0) whose outputs need it; an empty range where none does.
+void brickRanges(int L, SpanTarget t, int dim0, int b0, int n0, int diml, int bl, int nl, int* out)
 {
     for (int b = 0; b < nl; ++b) {
         out[2 * b] = n0;
@@ -254,7 +273,7 @@ void encoderBrickRanges(int L, int lt, int dim0, int b0, int n0, int diml, int b
     }
     for (int c = 0; c < n0; ++c) {
         const int p0 = c * b0, p1 = std::min(p0 + b0, dim0) - 1;
-        const Span sp = encoderSpan(L, lt, p0, p1);
+        const Span sp = networkSpan(L, t, p0, p1);
         const int lo = std::max(0, sp.lo), hi = std::min(diml - 1, sp.hi);
         for (int b = lo / bl; lo <= hi && b <= hi / bl && b < nl; ++b) {
             out[2 * b] = std::min(out[2 * b], c);
@@ -278,6 +297,10 @@ struct Sparse {
     const int* dec1bLen = nullptr;
     const int* dec1a = nullptr;
     const int* dec1aLen = nullptr;
+    const int* dec2b = nullptr; // level-2 decoder (null: dense)
+    const int* dec2bLen = nullptr;
+    const int* dec2a = nullptr;
+    const int* dec2aLen = nullptr;
     const int* enc[3] = {}; // both encoder convolutions of levels 0-2 (null: dense)
     const int* encLen[3] = {};
 };
@@ -332,21 +355,31 @@ int forward(dxmcg_denoiser* d, const bf16* input, cudaStream_t s, float* pred = 
         if (last && ep.head)
             headDone = fused;
     }
-    nn::ConvOptions dec1aEp, dec1bEp;
+    nn::ConvOptions dec1aEp, dec1bEp, dec2aEp, dec2bEp;
     if (sparse && sparse->dec1a) {
         dec1aEp.list = sparse->dec1a;
         dec1aEp.listLen = sparse->dec1aLen;
         dec1bEp.list = sparse->dec1b;
         dec1bEp.listLen = sparse->dec1bLen;
     }
+    if (sparse && sparse->dec2a) {
+        dec2aEp.list = sparse->dec2a;
+        dec2aEp.listLen = sparse->dec2aLen;
+        dec2bEp.list = sparse->dec2b;
+        dec2bEp.listLen = sparse->dec2bLen;
+    }
     const bool sparse1 = sparse && sparse->dec1a;
+    const bool sparse2 = sparse && sparse->dec2a;
     for (int l = d->L - 2; l >= 0; --l) {
-        const nn::ConvOptions* epA = l == 0 && sparse ? &beforeEp : (l == 1 && sparse1 ? &dec1aEp : nullptr);
+        const nn::ConvOptions* epA = l == 0 && sparse
+            ? &beforeEp
+            : (l == 1 && sparse1 ? &dec1aEp : (l == 2 && sparse2 ? &dec2aEp : nullptr));
         if ((rc = conv(d, d->decA(l), decIn(d, l), l, d->da[l].p, s, epA)) != DXMCG_OK)
             return rc;
         const bool withHead = l == 0 && headFusable;
         bool fused = false;
-        const nn::ConvOptions* epB = withHead ? &headEp : (l == 1 && sparse1 ? &dec1bEp : nullptr);
+        const nn::ConvOptions* epB
+            = withHead ? &headEp : (l == 1 && sparse1 ? &dec1bEp : (l == 2 && sparse2 ? &dec2bEp : nullptr));
         if ((rc = conv(d, d->decB(l), plain(d->da[l].p, d->ch[l]), l, d->db[l].p, s, epB, &fused)) != DXMCG_OK)
             return rc;
         if (withHead)
@@ -463,19 +496,14 @@ namespace nn {
         // bricks holding a non-air voxel and the one before only those and their
         // neighbours (the last one's halo); the dose of the other voxels is 0.  Every
         // voxel of those bricks gets the same value as the dense pass.
-        // The level-1 decoder is restricted too: the one before the last reads the
-        // upsampled level-1 output in a one-voxel halo of its bricks (their set grown by
-        // one brick, coarsened to level 1), and that layer's input one level-1 voxel
-        // further (grown by one level-1 brick).  One level further down the same sets
-        // hold 94 % and 100 % of the level-2 bricks of the 512x512x400 torso, so the
-        // level-2 decoder runs dense.
-        // The encoders of levels 0-2 run on the bricks of their grids that a tissue
-        // brick's outputs need: along each axis, the span of encoder outputs that the
-        // outputs of a level-0 brick depend on (every path through the network, at that
-        // brick's alignment to the pooling grids), plus the first convolution's halo.
-        // Every value a tissue brick's output depends on is computed as in the dense
-        // pass; what the other bricks hold (stale values from earlier calls) reaches
-        // only outputs of bricks outside that set, which the readout does not use.
+        // The decoders of levels 1 and 2 and the encoders of levels 0-2 run on the bricks
+        // of their grids that a tissue brick's outputs need: along each axis, the span of
+        // that layer's outputs on which the outputs of a level-0 brick depend (every path
+        // through the network, at that brick's alignment to the pooling grids; for an
+        // encoder, plus its first convolution's halo).  Every value a tissue brick's
+        // output depends on is computed as in the dense pass; what the other bricks hold
+        // (stale values from earlier calls) reaches only outputs of bricks outside those
+        // sets, which the readout does not use.
         // The input pass marks the tissue bricks; every brick list comes from one launch.
         Sparse sp;
         const bool sparse = d->ch[0] == 16 && useTensorCores(d, nz, ny, nx, d->ch[0]);
@@ -502,7 +530,7 @@ namespace nn {
         if (sparse) {
             for (auto& l : d->list0)
                 NN_CUDA(l.reserve(nb));
-            NN_CUDA(d->listLens.reserve(7));
+            NN_CUDA(d->listLens.reserve(9));
             BrickListJobs lists;
             NN_CUDA(launchBrickGrow(d->mask0[0].p, count, d->mask0[1].p, s));
             lists.add(d->mask0[0].p, static_cast<int>(nb), d->list0[0].p, d->listLens.p);
@@ -512,28 +540,52 @@ namespace nn {
             sp.lastLen = d->listLens.p;
             sp.before = d->list0[1].p;
             sp.beforeLen = d->listLens.p + 1;
-            // the encoders of levels 0 .. min(2, L - 2) that run on tcgen05: the bricks
-            // of their grids that some tissue brick's outputs need
-            const int dim0[3] = { nx, ny, nz };
-            int bl[3][3], cl[3][3], levels = 0;
-            size_t nRanges = 0, tmp1 = 1, tmp2 = 1;
-            for (int lt = 0; lt < 3 && lt <= d->L - 2; ++lt) {
-                if (!useTensorCores(d, nz >> lt, ny >> lt, nx >> lt, d->ch[lt]))
-                    break;
-                conv3TcBrickDims(nz >> lt, ny >> lt, nx >> lt, d->ch[lt], bl[lt], cl[lt]);
-                nRanges += 2 * static_cast<size_t>(cl[lt][0] + cl[lt][1] + cl[lt][2]);
-                tmp1 = std::max(tmp1, static_cast<size_t>(cl[lt][0]) * count[1] * count[2]);
-                tmp2 = std::max(tmp2, static_cast<size_t>(cl[lt][0]) * cl[lt][1] * count[2]);
-                levels = lt + 1;
+            // The encoders of levels 0 .. min(2, L - 2) and the decoders of levels 1 and 2
+            // that run on tcgen05: the bricks of their grids that some tissue brick's
+            // outputs need, as the union over the tissue bricks of per-axis ranges.
+            struct SetSpec {
+                SpanTarget t;
+                DevBuf<uint8_t>* mask;
+                DevBuf<int>* list;
+                int lenIndex;
+                const int** spList;
+                const int** spLen;
+                int bl[3], cl[3];
+            };
+            std::vector<SetSpec> specs;
+            const auto tc = [&](int l) { return useTensorCores(d, nz >> l, ny >> l, nx >> l, d->ch[l]); };
+            for (int lt = 0; lt < 3 && lt <= d->L - 2 && tc(lt); ++lt)
+                specs.push_back({ { kEncoderPair, lt }, &d->maskEnc[lt], &d->listEnc[lt], 4 + lt, &sp.enc[lt],
+                    &sp.encLen[lt], {}, {} });
+            if (d->L >= 3 && tc(1)) {
+                specs.push_back({ { kDecoderSecond, 1 }, &d->mask1[0], &d->list1[0], 2, &sp.dec1b, &sp.dec1bLen, {},
+                    {} });
+                specs.push_back({ { kDecoderFirst, 1 }, &d->mask1[1], &d->list1[1], 3, &sp.dec1a, &sp.dec1aLen, {},
+                    {} });
+                if (d->L >= 4 && tc(2)) {
+                    specs.push_back({ { kDecoderSecond, 2 }, &d->mask2[0], &d->list2[0], 7, &sp.dec2b, &sp.dec2bLen,
+                        {}, {} });
+                    specs.push_back({ { kDecoderFirst, 2 }, &d->mask2[1], &d->list2[1], 8, &sp.dec2a, &sp.dec2aLen,
+                        {}, {} });
+                }
             }
-            if (levels > 0) {
+            const int dim0[3] = { nx, ny, nz };
+            size_t nRanges = 0, tmp1 = 1, tmp2 = 1;
+            for (auto& sc : specs) {
+                const int l = sc.t.level;
+                conv3TcBrickDims(nz >> l, ny >> l, nx >> l, d->ch[l], sc.bl, sc.cl);
+                nRanges += 2 * static_cast<size_t>(sc.cl[0] + sc.cl[1] + sc.cl[2]);
+                tmp1 = std::max(tmp1, static_cast<size_t>(sc.cl[0]) * count[1] * count[2]);
+                tmp2 = std::max(tmp2, static_cast<size_t>(sc.cl[0]) * sc.cl[1] * count[2]);
+            }
+            if (!specs.empty()) {
                 d->encRangesHost.assign(nRanges, 0);
                 size_t off = 0;
-                for (int lt = 0; lt < levels; ++lt)
+                for (auto& sc : specs)
                     for (int a = 0; a < 3; ++a) {
-                        encoderBrickRanges(d->L, lt, dim0[a], brick[a], count[a], dim0[a] >> lt, bl[lt][a],
-                            cl[lt][a], d->encRangesHost.data() + off);
-                        off += 2 * static_cast<size_t>(cl[lt][a]);
+                        brickRanges(d->L, sc.t, dim0[a], brick[a], count[a], dim0[a] >> sc.t.level, sc.bl[a],
+                            sc.cl[a], d->encRangesHost.data() + off);
+                        off += 2 * static_cast<size_t>(sc.cl[a]);
                     }
                 NN_CUDA(d->encRanges.reserve(nRanges));
                 NN_CUDA(cudaMemcpyAsync(d->encRanges.p, d->encRangesHost.data(), nRanges * sizeof(int),
@@ -541,36 +593,17 @@ namespace nn {
                 NN_CUDA(d->maskTmp[0].reserve(tmp1));
                 NN_CUDA(d->maskTmp[1].reserve(tmp2));
                 off = 0;
-                for (int lt = 0; lt < levels; ++lt) {
-                    const size_t nbl = static_cast<size_t>(cl[lt][0]) * cl[lt][1] * cl[lt][2];
-                    NN_CUDA(d->maskEnc[lt].reserve(nbl));
-                    NN_CUDA(d->listEnc[lt].reserve(nbl));
-                    NN_CUDA(launchBrickMap(d->mask0[0].p, count, cl[lt], d->encRanges.p + off, d->maskEnc[lt].p,
+                for (auto& sc : specs) {
+                    const size_t nbl = static_cast<size_t>(sc.cl[0]) * sc.cl[1] * sc.cl[2];
+                    NN_CUDA(sc.mask->reserve(nbl));
+                    NN_CUDA(sc.list->reserve(nbl));
+                    NN_CUDA(launchBrickMap(d->mask0[0].p, count, sc.cl, d->encRanges.p + off, sc.mask->p,
                         d->maskTmp[0].p, d->maskTmp[1].p, s));
-                    off += 2 * static_cast<size_t>(cl[lt][0] + cl[lt][1] + cl[lt][2]);
-                    lists.add(d->maskEnc[lt].p, static_cast<int>(nbl), d->listEnc[lt].p, d->listLens.p + 4 + lt);
-                    sp.enc[lt] = d->listEnc[lt].p;
-                    sp.encLen[lt] = d->listLens.p + 4 + lt;
+                    off += 2 * static_cast<size_t>(sc.cl[0] + sc.cl[1] + sc.cl[2]);
+                    lists.add(sc.mask->p, static_cast<int>(nbl), sc.list->p, d->listLens.p + sc.lenIndex);
+                    *sc.spList = sc.list->p;
+                    *sc.spLen = d->listLens.p + sc.lenIndex;
                 }
-            }
-            const int D1 = nz >> 1, H1 = ny >> 1, W1 = nx >> 1;
-            if (d->L >= 3 && useTensorCores(d, D1, H1, W1, d->ch[1])) {
-                int brick1[3], count1[3];
-                conv3TcBrickDims(D1, H1, W1, d->ch[1], brick1, count1);
-                const size_t nb1 = static_cast<size_t>(count1[0]) * count1[1] * count1[2];
-                for (auto& m : d->mask1)
-                    NN_CUDA(m.reserve(nb1));
-                for (auto& l : d->list1)
-                    NN_CUDA(l.reserve(nb1));
-                NN_CUDA(launchBrickGrow(d->mask0[1].p, count, d->mask0[2].p, s));
-                NN_CUDA(launchBrickCoarsen(d->mask0[2].p, brick, count, brick1, count1, d->mask1[0].p, s));
-                NN_CUDA(launchBrickGrow(d->mask1[0].p, count1, d->mask1[1].p, s));
-                lists.add(d->mask1[0].p, static_cast<int>(nb1), d->list1[0].p, d->listLens.p + 2);
-                lists.add(d->mask1[1].p, static_cast<int>(nb1), d->list1[1].p, d->listLens.p + 3);
-                sp.dec1b = d->list1[0].p;
-                sp.dec1bLen = d->listLens.p + 2;
-                sp.dec1a = d->list1[1].p;
-                sp.dec1aLen = d->listLens.p + 3;
             }
             NN_CUDA(launchBrickLists(lists, s));
         }

@@ -74,17 +74,13 @@ void conv3TcBrickDims(int D, int H, int W, int Cout, int brick[3], int count[3])
 //             whose interval holds b; three one-axis passes (tmp1: outCount[0] x
 //             inCount[1] x inCount[2] bytes, tmp2: outCount[0] x outCount[1] x
 //             inCount[2]);
-//   coarsen:  bricks of the half-resolution level whose voxels cover a voxel of a
-//             marked brick of the level above (voxel v lies in coarse voxel v / 2);
 //   list:     the marked indices in increasing order, and how many (*listLen);
 //             launchBrickLists compacts up to kMaxBrickLists masks in one launch.
 cudaError_t launchBrickGrow(const uint8_t* active, const int count[3], uint8_t* grown, cudaStream_t s);
 cudaError_t launchBrickMap(const uint8_t* in, const int inCount[3], const int outCount[3], const int* ranges,
     uint8_t* out, uint8_t* tmp1, uint8_t* tmp2, cudaStream_t s);
-cudaError_t launchBrickCoarsen(const uint8_t* fine, const int fineBrick[3], const int fineCount[3],
-    const int coarseBrick[3], const int coarseCount[3], uint8_t* coarse, cudaStream_t s);
 cudaError_t launchBrickList(const uint8_t* mask, int nb, int* list, int* listLen, cudaStream_t s);
-constexpr int kMaxBrickLists = 8;
+constexpr int kMaxBrickLists = 12;
 struct BrickListJobs {
     const uint8_t* mask[kMaxBrickLists] = {};
     int* list[kMaxBrickLists] = {};

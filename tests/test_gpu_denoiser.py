@@ -252,10 +252,10 @@ def test_world_denoise_path(gpu, torch):
 
 def test_world_denoise_sparse_bricks_match_dense(gpu, torch):
     """The world path on tcgen05 computes the last convolution only on bricks holding a
-    non-air voxel, the one before only on those and their neighbours, the level-1
-    decoder only where those read it, and the encoder convolutions only on the bricks
-    that a tissue brick's outputs depend on (the body sits at one end of a long block
-    of air, so bricks of every restricted layer are skipped).  Every voxel of a tissue
+    non-air voxel, the one before only on those and their neighbours, and the level-1
+    decoder and the encoders only on the bricks that a tissue brick's outputs depend on
+    (the body sits at one end of a long block of air, so bricks of every restricted
+    layer are skipped).  Every voxel of a tissue
     brick equals the dense array path (prepare_input + forward); the voxels of the other
     bricks are 0."""
     small = P.ellipsoid_phantom((32, 32, 24), (0.4, 0.4, 0.4), seed=8)
@@ -376,7 +376,8 @@ def test_tensor_core_probe_is_exact(gpu, n):
 def test_world_denoise_sparse_matches_dense_at_full_size(gpu, torch):
     """The 512 x 512 x 400 spiral-CT torso (102,400 level-0 bricks, so the ordered
     brick lists are built over 25 passes of 4096 bricks; the four-level net's
-    encoders run on 63 %, 67 % and 72 % of the level-0, -1 and -2 bricks):
+    encoders run on 63 %, 67 % and 72 % of the level-0, -1 and -2 bricks, its level-1
+    and level-2 decoders on 44 % and 53-56 %):
     the sparse world path equals the dense array path on every voxel of a tissue
     brick."""
     from opendxmc_gb300 import denoise as DN

@@ -453,7 +453,8 @@ DXMCG_API int dxmcg_denoiser_gather_patches(const void* const* inputs, const flo
  * denser than 0.2 g/cm3 (or `scale` when > 0), dose_out (host, N, mGy as
  * dxmcg_world_read_dose; may be NULL) and *scale_used (may be NULL).  On the tensor-core
  * path the last two convolutions skip output bricks (8 x 16 x 8 voxels) that hold no
- * non-air voxel (the one before: not within one brick of one); their voxels, all air,
+ * non-air voxel (the one before: not within one brick of one), and the other layers of
+ * levels 0-2 the bricks those do not depend on; the skipped bricks' voxels, all air,
  * get dose 0, and every other voxel the value of the full computation. */
 DXMCG_API int dxmcg_world_denoise(dxmcg_world* w, dxmcg_denoiser* d, double scale, double* dose_out,
     double* scale_used);
